@@ -1,0 +1,233 @@
+/*
+ * netlk - GB300 (sm_103a) phylogenetic-network likelihood, C ABI.
+ *
+ * Drop-in for the network log-likelihood hot path of NetRAX (the reference):
+ * Felsenstein pruning over every displayed tree of a rooted phylogenetic
+ * network, with subtrees shared across reticulation configurations, combined
+ * per partition under the AVERAGE (mixture) or BEST (maximum) model, plus the
+ * gradient with respect to every branch length and every reticulation
+ * probability from one adjoint sweep.
+ *
+ * Conventions
+ *  - Every entry point returns an int status (NETLK_OK == 0). No C++
+ *    exception crosses this boundary. netlk_last_error(ctx) gives a message.
+ *  - Plain pointers and sizes only. Host pointers unless a name says device.
+ *  - A context owns one CUDA stream and its device buffers; it is not
+ *    re-entrant (one host thread at a time per context).
+ *  - Node numbering follows the reference's Network: tips 0..n_tips-1, then
+ *    inner tree nodes, then reticulation nodes; edge ids are the reference's
+ *    pmatrix indices (src/io/NetworkIO.cpp:114-185).
+ */
+#ifndef NETLK_H
+#define NETLK_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------ status codes */
+#define NETLK_OK 0
+#define NETLK_ERR_INVALID_ARGUMENT 1 /* bad sizes, indices, NaN parameters   */
+#define NETLK_ERR_TOPOLOGY 2         /* not a rooted binary network, cycle   */
+#define NETLK_ERR_ENUMERATION 3      /* displayed-tree matching failed        */
+#define NETLK_ERR_CUDA 4             /* CUDA runtime error                    */
+#define NETLK_ERR_OUT_OF_MEMORY 5    /* device or host allocation failed      */
+#define NETLK_ERR_NUMERIC 6          /* -inf / NaN network log-likelihood     */
+#define NETLK_ERR_UNSUPPORTED 7      /* e.g. too many reticulations           */
+#define NETLK_ERR_NO_DEVICE 8        /* no CUDA device / wrong architecture   */
+#define NETLK_ERR_TIMEOUT 9          /* a bounded device wait ran out         */
+
+/* ------------------------------------------------------------ enumerations */
+#define NETLK_AVERAGE 0 /* LikelihoodVariant::AVERAGE_DISPLAYED_TREES */
+#define NETLK_BEST 1    /* LikelihoodVariant::BEST_DISPLAYED_TREE     */
+
+#define NETLK_FP64 0 /* plain FP64 CLVs, libpll scaling (2^-256 / 2^256)     */
+#define NETLK_FP32 1 /* FP32 CLVs, per-site power-of-two rescaling          */
+
+#define NETLK_MAX_RETICULATIONS 16
+
+/* ------------------------------------------------------------- descriptors */
+
+/* Rooted phylogenetic network.
+ * Replaces the reference's Network / AnnotatedNetwork topology
+ * (src/graph/Network.hpp:20-76, src/graph/AnnotatedNetwork.hpp:42-89). */
+typedef struct {
+  int32_t n_nodes;
+  int32_t n_tips;
+  int32_t n_edges;
+  int32_t n_reticulations;
+  int32_t root;                    /* node id of the root                    */
+  const int32_t *edge_parent;      /* [n_edges]                              */
+  const int32_t *edge_child;       /* [n_edges]                              */
+  const int32_t *node_child_edges; /* [2*n_nodes] outgoing edges of each node
+                                      in the reference's child order
+                                      (getChildren, src/helper/ChildrenHelper.cpp:6-21);
+                                      -1 where absent                        */
+  const int32_t *ret_node;         /* [n_reticulations] node of reticulation k */
+  const int32_t *ret_first_edge;   /* [n_reticulations] edge from first parent */
+  const int32_t *ret_second_edge;  /* [n_reticulations] edge from second parent */
+} netlk_topology;
+
+/* One alignment partition (pattern-compressed) with a GTR+Gamma model.
+ * Replaces the pll_partition_t + model parameters held by the reference's
+ * fake_treeinfo (src/RaxmlWrapper.cpp:671-766). */
+typedef struct {
+  int32_t states;                 /* 4 (DNA) or 20 (protein)                  */
+  int32_t rate_cats;              /* 1..8                                     */
+  int32_t n_patterns;
+  const uint32_t *tip_states;     /* [n_tips*n_patterns] state bitmask per tip
+                                     (row = tip); DNA A=1 C=2 G=4 T=8          */
+  const double *pattern_weights;  /* [n_patterns]                             */
+  const double *freqs;            /* [states]                                 */
+  const double *exchangeabilities;/* [states*(states-1)/2], row-major upper
+                                     triangle (AC AG AT CG CT GT for DNA)      */
+  double alpha;                   /* Gamma shape; used when rates == NULL     */
+  const double *rates;            /* optional [rate_cats] category rates      */
+  const double *rate_weights;     /* optional [rate_cats]; default 1/rate_cats */
+} netlk_partition;
+
+typedef struct {
+  int32_t variant;                   /* NETLK_AVERAGE / NETLK_BEST           */
+  int32_t precision;                 /* NETLK_FP64 / NETLK_FP32              */
+  double min_interesting_tree_logprob; /* NetraxOptions, default log(1e-6)   */
+  int32_t device;                    /* CUDA device ordinal                  */
+  int32_t use_cuda_graph;            /* 1: replay captured launch sequences  */
+  int32_t host_only;                 /* 1: build the DAG and schedules only,
+                                        touch no device (evaluation calls then
+                                        return NETLK_ERR_NO_DEVICE)          */
+} netlk_options;
+
+typedef struct {
+  int32_t n_variants;        /* inner displayed-tree variants (DAG nodes)    */
+  int32_t n_root_variants;   /* displayed trees at the network root          */
+  int32_t n_dtroot_slots;    /* distinct variants holding a tree's root CLV  */
+  int32_t n_levels;          /* dependency levels of the variant DAG         */
+  int32_t n_backward_ops;    /* variants visited by the adjoint sweep        */
+  int32_t n_adjoint_slots;   /* adjoint buffers after liveness reuse         */
+  int32_t max_variants_per_node;
+  int32_t n_degenerate;      /* child pairs whose combined set is empty (the
+                                reference stores a CLV for them; never used) */
+  int64_t n_patterns_total;  /* padded patterns over all partitions          */
+  int64_t site_clv_updates;  /* per forward pass: sum_variants patterns      */
+  int64_t tip_child_uses;    /* child operands that are tips                 */
+  int64_t fake_child_uses;   /* unary variants (fake all-ones right child)   */
+  int64_t device_bytes;      /* device memory held by the context            */
+} netlk_dag_stats;
+
+/* --------------------------------------------------------------- lifecycle */
+typedef struct netlk_ctx netlk_ctx;
+
+int netlk_options_default(netlk_options *opts);
+
+/* Builds the displayed-tree DAG (the reference's processNodeImproved schedule,
+ * src/likelihood/ImprovedLoglikelihood.cpp:194-408, on bitsets over the 2^r
+ * reticulation configurations), uploads tips and parameters.
+ * Replaces init_annotated_network (src/graph/AnnotatedNetwork.cpp:80-185) and
+ * createNetworkPllTreeinfo (src/RaxmlWrapper.cpp:671-766).
+ * branch_lengths: [n_edges] (clamped to [1e-6, 100] like the reference,
+ * src/RaxmlWrapper.cpp:754-763); ret_first_probs: [n_reticulations]. */
+int netlk_create(const netlk_topology *topo, const netlk_partition *parts,
+                 int32_t n_parts, const double *branch_lengths,
+                 const double *ret_first_probs, const netlk_options *opts,
+                 netlk_ctx **out);
+int netlk_destroy(netlk_ctx *ctx);
+
+/* Message of the last failing call on ctx (or of the last failed create when
+ * ctx is NULL). Valid until the next call on the same context. */
+const char *netlk_last_error(const netlk_ctx *ctx);
+const char *netlk_status_string(int status);
+
+int netlk_get_dag_stats(const netlk_ctx *ctx, netlk_dag_stats *out);
+
+/* Displayed-tree DAG export, for enumeration parity checks.
+ * node_of_variant [n_variants]; children [2*n_variants] (variant id >= 0,
+ * -1-tip for a tip, INT32_MIN for the fake all-ones child); edges
+ * [2*n_variants] (-1 for the fake child); covered [n_variants*words] bitset of
+ * the full reticulation configurations (bit t = tree index t of
+ * getTreeConfig, src/helper/ReticulationConfigHelper.cpp:188-203) the variant
+ * stands for; words = max(1, 2^r/64). Any output pointer may be NULL. */
+int netlk_dag_export(const netlk_ctx *ctx, int32_t *node_of_variant,
+                     int32_t *children, int32_t *edges, uint64_t *covered,
+                     int32_t words);
+
+/* Root-variant export: variant id [n_root_variants], the variant whose CLV
+ * gives its tree log-likelihood (findFirstNodeWithTwoActiveChildren +
+ * findMatchingDisplayedTree, src/likelihood/ImprovedLoglikelihood.cpp:428-432)
+ * [n_root_variants], and its log-probability [n_root_variants]. */
+int netlk_root_export(const netlk_ctx *ctx, int32_t *root_variant,
+                      int32_t *dtroot_variant, double *logprob);
+
+/* ----------------------------------------------------- parameter updates */
+/* Replace linked_branch_lengths (src/optimization/NetworkState.cpp:93-306). */
+int netlk_set_branch_lengths(netlk_ctx *ctx, const double *branch_lengths,
+                             int32_t n_edges);
+/* Replace setReticulationProb for all reticulations
+ * (src/optimization/ReticulationOptimization.cpp:25-38). */
+int netlk_set_reticulation_probs(netlk_ctx *ctx, const double *first_probs,
+                                 int32_t n_reticulations);
+/* Replace the substitution model of one partition (freqs, exchangeabilities,
+ * Gamma shape; rates NULL = mean discrete Gamma). */
+int netlk_set_model(netlk_ctx *ctx, int32_t partition, const double *freqs,
+                    const double *exchangeabilities, double alpha,
+                    const double *rates);
+
+/* -------------------------------------------------------------- evaluation */
+/* Network log-likelihood. Replaces computeLoglikelihood(ann_network, 0, 1)
+ * (src/likelihood/LikelihoodComputation.hpp:17-18 ->
+ * src/likelihood/ImprovedLoglikelihood.cpp:646-671). partition_logl
+ * [n_parts] mirrors fake_treeinfo->partition_loglh; tree_partition_logl
+ * [n_root_variants*n_parts] mirrors TreeLoglData::tree_partition_logl
+ * (NaN for trees below min_interesting_tree_logprob). Outputs may be NULL. */
+int netlk_loglikelihood(netlk_ctx *ctx, double *total, double *partition_logl,
+                        double *tree_partition_logl);
+
+/* Log-likelihood plus d logL / d branch length [n_edges] and
+ * d logL / d first-parent probability [n_reticulations] from one forward and
+ * one adjoint sweep. Replaces the per-edge sumtable / derivative recomputation
+ * of src/likelihood/LikelihoodDerivatives.cpp:190-344 and the Brent probes of
+ * src/optimization/ReticulationOptimization.cpp:25-118. */
+int netlk_loglikelihood_gradient(netlk_ctx *ctx, double *total,
+                                 double *partition_logl, double *d_brlen,
+                                 double *d_retprob);
+
+/* Derivatives of the reference's own formula for one edge
+ * (computeLoglikelihoodDerivatives, src/likelihood/LikelihoodDerivatives.cpp:30-188):
+ * mode 0 = true derivative of the network logL; mode 1 = the reference's
+ * restricted AVERAGE denominator (trees where the edge is taken) and BEST
+ * argmax of tree_logl * tree_prob. d2 receives the central difference of d1
+ * over +-1e-6 when not NULL. */
+int netlk_edge_derivatives(netlk_ctx *ctx, int32_t edge, int32_t mode,
+                           double *d1, double *d2);
+
+/* ------------------------------------------------- sharded (multi-rank) use */
+/* Per-(root variant, partition) log-likelihood partial sums over the patterns
+ * this context holds [n_root_variants*n_parts]; ranks that hold disjoint
+ * pattern slices all-reduce (SUM) these, which is what parallel_reduce_cb does
+ * at src/likelihood/ImprovedLoglikelihood.cpp:473-483. */
+int netlk_tree_partials(netlk_ctx *ctx, double *tree_partition_logl);
+/* Mixes global partials (AVERAGE / BEST, ImprovedLoglikelihood.cpp:521-644)
+ * and runs the adjoint sweep over the local patterns: d_brlen_partial
+ * [n_edges] must then be all-reduced (SUM); d_retprob [n_reticulations] and
+ * total are already global. */
+int netlk_mix_and_backward(netlk_ctx *ctx, const double *global_partials,
+                           double *total, double *partition_logl,
+                           double *d_brlen_partial, double *d_retprob);
+
+/* ------------------------------------------------------------------- debug */
+/* Copies the CLV (converted to double) and scale counters of one variant:
+ * clv [n_patterns*rate_cats*states] and scaler [n_patterns] of partition
+ * `partition`, after the last evaluation. */
+int netlk_get_clv(netlk_ctx *ctx, int32_t variant, int32_t partition,
+                  double *clv, int32_t *scaler);
+/* The context's CUDA stream (cudaStream_t) for external event timing. */
+int netlk_get_stream(netlk_ctx *ctx, void **stream);
+/* Kernels launched by this context since creation. */
+int netlk_launch_count(const netlk_ctx *ctx, int64_t *launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

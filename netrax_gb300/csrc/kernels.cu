@@ -1,0 +1,632 @@
+// netlk device kernels (sm_103a).
+//
+// Layout in HBM (N = padded patterns over all partitions, R rate categories):
+//   CLV of variant v:      clv[v][N][R][4]   (float or double, 16/32 B per (pattern, rate))
+//   scale counter:         scaler[v][N]      (int32, cumulative over the subtree)
+//   adjoint slot a:        adj[a][N][R][4]
+//   tips:                  tips[tip][N]      (uint8 4-bit state masks)
+//   P-matrices:            pmat[part][edge][R][4][4]
+// A warp owns 32/R consecutive patterns (lane = pattern*R + rate) and walks
+// the whole variant DAG for them: every (pattern, rate) value a lane reads in
+// the forward and adjoint sweeps was written by that same lane, so the sweeps
+// need no block- or grid-level synchronisation. Scaling decisions reduce over
+// the R lanes of a pattern with shuffles; per-site log-likelihood and edge
+// gradient sums reduce over the warp.
+//
+// Reference arithmetic restated (libpll is not vendored by NetRAX):
+//   pll_update_partials_single   (called at src/likelihood/ImprovedLoglikelihood.cpp:145,185)
+//   pll_compute_root_loglikelihood (src/likelihood/ImprovedLoglikelihood.cpp:450)
+//   pllmod_treeinfo_update_prob_matrices (src/likelihood/ImprovedLoglikelihood.cpp:661)
+//   AVERAGE / BEST mixing        (src/likelihood/ImprovedLoglikelihood.cpp:521-644)
+#include <cstdio>
+
+#include "kernels.cuh"
+
+namespace netlk {
+
+static int64_t g_launches = 0;
+int64_t launches_issued() { return g_launches; }
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+template <typename real>
+struct Vec;
+
+template <>
+struct Vec<float> {
+  static __device__ __forceinline__ void load(const float *p, float (&v)[4]) {
+    float4 t = *reinterpret_cast<const float4 *>(p);
+    v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+  }
+  static __device__ __forceinline__ void store(float *p, const float (&v)[4]) {
+    *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+  }
+  static __device__ __forceinline__ void ldg(const float *p, float (&v)[4]) {
+    float4 t = __ldg(reinterpret_cast<const float4 *>(p));
+    v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+  }
+};
+
+template <>
+struct Vec<double> {
+  static __device__ __forceinline__ void load(const double *p, double (&v)[4]) {
+    double2 a = reinterpret_cast<const double2 *>(p)[0];
+    double2 b = reinterpret_cast<const double2 *>(p)[1];
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+  }
+  static __device__ __forceinline__ void store(double *p, const double (&v)[4]) {
+    reinterpret_cast<double2 *>(p)[0] = make_double2(v[0], v[1]);
+    reinterpret_cast<double2 *>(p)[1] = make_double2(v[2], v[3]);
+  }
+  static __device__ __forceinline__ void ldg(const double *p, double (&v)[4]) {
+    double2 a = __ldg(reinterpret_cast<const double2 *>(p));
+    double2 b = __ldg(reinterpret_cast<const double2 *>(p) + 1);
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+  }
+};
+
+// Scaling rules. FP64 restates libpll's per-site rule: when every entry of a
+// site is below 2^-256 multiply the site by 2^256 and add one to its counter.
+// FP32 uses its own power-of-two unit: when the site maximum falls below
+// 2^-32, shift the site by 2^-e (max becomes [0.5, 1)) and add -e.
+template <typename real>
+struct Scale;
+
+template <>
+struct Scale<float> {
+  static constexpr double kLogUnit = -0.69314718055994530942;  // log(2^-1)
+  static __device__ __forceinline__ int rescale(float m, float (&v)[4]) {
+    if (m < 0x1p-32f && m > 0.0f) {
+      int e;
+      frexpf(m, &e);
+      const int k = -e;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) v[i] = ldexpf(v[i], k);
+      return k;
+    }
+    return 0;
+  }
+  // x * 2^k for the local shift k >= 0 of a site (applied to adjoint products)
+  static __device__ __forceinline__ float shift(float x, int k) { return ldexpf(x, k); }
+};
+
+template <>
+struct Scale<double> {
+  static constexpr double kLogUnit = -177.44567822334599921;  // log(2^-256)
+  static __device__ __forceinline__ int rescale(double m, double (&v)[4]) {
+    if (m < 0x1p-256) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) v[i] *= 0x1p256;
+      return 1;
+    }
+    return 0;
+  }
+  static __device__ __forceinline__ double shift(double x, int k) { return ldexp(x, 256 * k); }
+};
+
+template <typename real, int R>
+__device__ __forceinline__ void load_child(const SweepParams &p, int32_t ref, size_t g, int r,
+                                           real (&c)[4], int &s) {
+  if (ref >= 0) {
+    const real *clv = static_cast<const real *>(p.clv);
+    Vec<real>::load(clv + ((size_t)ref * p.n_patterns + g) * (R * 4) + r * 4, c);
+    s = p.scaler[(size_t)ref * p.n_patterns + g];
+  } else if (ref != INT32_MIN) {
+    const unsigned code = p.tips[(size_t)(-1 - ref) * p.n_patterns + g];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) c[i] = (real)((code >> i) & 1u);
+    s = 0;
+  } else {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) c[i] = (real)1;
+    s = 0;
+  }
+}
+
+template <typename real>
+__device__ __forceinline__ void matvec(const real *P, const real (&c)[4], real (&out)[4]) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    real row[4];
+    Vec<real>::ldg(P + 4 * i, row);
+    out[i] = row[0] * c[0] + row[1] * c[1] + row[2] * c[2] + row[3] * c[3];
+  }
+}
+
+template <typename real>
+__device__ __forceinline__ void matvec_t(const real *P, const real (&u)[4], real (&out)[4]) {
+#pragma unroll
+  for (int j = 0; j < 4; ++j) out[j] = 0;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    real row[4];
+    Vec<real>::ldg(P + 4 * i, row);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) out[j] += row[j] * u[i];
+  }
+}
+
+template <int R, typename T>
+__device__ __forceinline__ T rate_sum(T v) {
+#pragma unroll
+  for (int o = 1; o < R; o <<= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+
+template <int R, typename T>
+__device__ __forceinline__ T rate_max(T v) {
+#pragma unroll
+  for (int o = 1; o < R; o <<= 1) v = max(v, __shfl_xor_sync(kFull, v, o));
+  return v;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+
+// ------------------------------------------------------------------ forward
+template <typename real, int R>
+__global__ void __launch_bounds__(kThreads) forward_kernel(const SweepParams p) {
+  constexpr int PPW = 32 / R;
+  const int lane = threadIdx.x & 31;
+  const int r = lane % R;
+  const int pl = lane / R;
+  const int warps_total = gridDim.x * (kThreads / 32);
+  const int warp_id = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
+  const real *pmat = static_cast<const real *>(p.pmat);
+  real *clv = static_cast<real *>(p.clv);
+  const size_t N = (size_t)p.n_patterns;
+
+  for (int unit = warp_id; unit < p.n_units; unit += warps_total) {
+    const int part = p.unit_part[unit];
+    const size_t g = (size_t)unit * PPW + pl;
+    const real *pm = pmat + (size_t)part * p.n_edges * (R * 16) + r * 16;
+    const double wgt = p.weights[g];
+    real freq[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) freq[i] = (real)p.freqs[part * 4 + i];
+    const real rw = (real)p.rate_weights[part * R + r];
+
+    for (int o0 = 0; o0 < p.n_fwd_ops; o0 += kGroup) {
+      FwdOp op[kGroup];
+      real ca[kGroup][4], cb[kGroup][4];
+      int sa[kGroup], sb[kGroup];
+#pragma unroll
+      for (int j = 0; j < kGroup; ++j) {
+        op[j] = p.fwd_ops[o0 + j];
+        if (op[j].out < 0) continue;
+        load_child<real, R>(p, op[j].a, g, r, ca[j], sa[j]);
+        load_child<real, R>(p, op[j].b, g, r, cb[j], sb[j]);
+      }
+#pragma unroll
+      for (int j = 0; j < kGroup; ++j) {
+        if (op[j].out < 0) continue;
+        real v[4], pb[4];
+        matvec<real>(pm + (size_t)op[j].ea * (R * 16), ca[j], v);
+        if (op[j].b != INT32_MIN) {
+          matvec<real>(pm + (size_t)op[j].eb * (R * 16), cb[j], pb);
+#pragma unroll
+          for (int i = 0; i < 4; ++i) v[i] *= pb[i];
+        }
+        real m = max(max(v[0], v[1]), max(v[2], v[3]));
+        m = rate_max<R>(m);
+        const int s = sa[j] + sb[j] + Scale<real>::rescale(m, v);
+        Vec<real>::store(clv + ((size_t)op[j].out * N + g) * (R * 4) + r * 4, v);
+        if (r == 0) p.scaler[(size_t)op[j].out * N + g] = s;
+        if (op[j].slot >= 0) {
+          // pll_compute_root_loglikelihood for this site, summed over the warp.
+          real t = rw * (freq[0] * v[0] + freq[1] * v[1] + freq[2] * v[2] + freq[3] * v[3]);
+          t = rate_sum<R>(t);
+          double ll = 0.0;
+          if (r == 0 && wgt != 0.0) {
+            double lt = (sizeof(real) == 4) ? (double)logf((float)t) : log((double)t);
+            ll = wgt * (lt + (double)s * Scale<real>::kLogUnit);
+          }
+          ll = warp_sum(ll);
+          if (lane == 0) p.site_partial[(size_t)op[j].slot * p.n_units + unit] = ll;
+        }
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------ adjoint
+template <typename real, int R>
+__global__ void __launch_bounds__(kThreads) backward_kernel(const SweepParams p) {
+  extern __shared__ double sgrad[];
+  constexpr int PPW = 32 / R;
+  const int lane = threadIdx.x & 31;
+  const int r = lane % R;
+  const int pl = lane / R;
+  const int wib = threadIdx.x >> 5;
+  const int warps_total = gridDim.x * (kThreads / 32);
+  const int warp_id = blockIdx.x * (kThreads / 32) + wib;
+  const real *pmat = static_cast<const real *>(p.pmat);
+  const real *clv = static_cast<const real *>(p.clv);
+  real *adj = static_cast<real *>(p.adj);
+  const size_t N = (size_t)p.n_patterns;
+  double *my = sgrad + (size_t)wib * p.n_edges;
+  for (int e = lane; e < p.n_edges; e += 32) my[e] = 0.0;
+  __syncwarp();
+
+  for (int unit = warp_id; unit < p.n_units; unit += warps_total) {
+    const int part = p.unit_part[unit];
+    const size_t g = (size_t)unit * PPW + pl;
+    const real *pm = pmat + (size_t)part * p.n_edges * (R * 16) + r * 16;
+    const real wgt = (real)p.weights[g];
+    real freq[4], Q[16];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) freq[i] = (real)p.freqs[part * 4 + i];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) Q[i] = (real)p.Q[part * 16 + i];
+    const real rw = (real)p.rate_weights[part * R + r];
+    const real rate = (real)p.rates[part * R + r];
+
+    for (int o0 = 0; o0 < p.n_bwd_ops; o0 += kGroup) {
+      BwdOp op[kGroup];
+      real ax[kGroup][4], ca[kGroup][4], cb[kGroup][4], cx[kGroup][4];
+      int sx[kGroup], sa[kGroup], sb[kGroup];
+#pragma unroll
+      for (int j = 0; j < kGroup; ++j) {
+        op[j] = p.bwd_ops[o0 + j];
+        if (op[j].x < 0) continue;
+        if (op[j].adj_x >= 0) {
+          Vec<real>::load(adj + ((size_t)op[j].adj_x * N + g) * (R * 4) + r * 4, ax[j]);
+        } else {
+#pragma unroll
+          for (int i = 0; i < 4; ++i) ax[j][i] = 0;
+        }
+        if (op[j].seed >= 0)
+          Vec<real>::load(clv + ((size_t)op[j].x * N + g) * (R * 4) + r * 4, cx[j]);
+        sx[j] = p.scaler[(size_t)op[j].x * N + g];
+        load_child<real, R>(p, op[j].a, g, r, ca[j], sa[j]);
+        load_child<real, R>(p, op[j].b, g, r, cb[j], sb[j]);
+      }
+#pragma unroll
+      for (int j = 0; j < kGroup; ++j) {
+        if (op[j].x < 0) continue;
+        if (op[j].seed >= 0) {
+          // d(w_s log L_s)/d clv = w_s * rw_r * pi_i / L_s, times the tree weight.
+          real t = rw * (freq[0] * cx[j][0] + freq[1] * cx[j][1] + freq[2] * cx[j][2] + freq[3] * cx[j][3]);
+          t = rate_sum<R>(t);
+          const real sd = (real)p.seeds[(size_t)op[j].seed * p.n_parts + part] * wgt;
+          if (t > (real)0 && sd != (real)0) {
+            const real f = sd * rw / t;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) ax[j][i] += f * freq[i];
+          }
+        }
+        const bool fake = op[j].b == INT32_MIN;
+        const real *Pa = pm + (size_t)op[j].ea * (R * 16);
+        real pa[4], pb[4];
+        matvec<real>(Pa, ca[j], pa);
+        if (!fake) {
+          matvec<real>(pm + (size_t)op[j].eb * (R * 16), cb[j], pb);
+        } else {
+#pragma unroll
+          for (int i = 0; i < 4; ++i) pb[i] = 1;
+        }
+        // CLV_x = 2^k (Pa a) * (Pb b) with k the shift applied at x for this site
+        const int k = sx[j] - sa[j] - sb[j];
+        real ua[4], ub[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          ua[i] = ax[j][i] * pb[i];
+          ub[i] = ax[j][i] * pa[i];
+        }
+        if (k != 0) {
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            ua[i] = Scale<real>::shift(ua[i], k);
+            ub[i] = Scale<real>::shift(ub[i], k);
+          }
+        }
+        // d/dt of P(t r) c = r Q P(t r) c
+        real ga = 0, gb = 0;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const real qa = Q[4 * i] * pa[0] + Q[4 * i + 1] * pa[1] + Q[4 * i + 2] * pa[2] + Q[4 * i + 3] * pa[3];
+          ga += ua[i] * qa;
+          if (!fake) {
+            const real qb = Q[4 * i] * pb[0] + Q[4 * i + 1] * pb[1] + Q[4 * i + 2] * pb[2] + Q[4 * i + 3] * pb[3];
+            gb += ub[i] * qb;
+          }
+        }
+        ga = warp_sum(ga * rate);
+        if (lane == 0) my[op[j].ea] += (double)ga;
+        if (!fake) {
+          gb = warp_sum(gb * rate);
+          if (lane == 0) my[op[j].eb] += (double)gb;
+        }
+        const int mode_a = op[j].modes & 0xff, mode_b = (op[j].modes >> 8) & 0xff;
+        if (mode_a) {
+          real na[4];
+          matvec_t<real>(Pa, ua, na);
+          real *dst = adj + ((size_t)op[j].adj_a * N + g) * (R * 4) + r * 4;
+          if (mode_a == 2) {
+            real old[4];
+            Vec<real>::load(dst, old);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) na[i] += old[i];
+          }
+          Vec<real>::store(dst, na);
+        }
+        if (mode_b) {
+          real nb[4];
+          matvec_t<real>(pm + (size_t)op[j].eb * (R * 16), ub, nb);
+          real *dst = adj + ((size_t)op[j].adj_b * N + g) * (R * 4) + r * 4;
+          if (mode_b == 2) {
+            real old[4];
+            Vec<real>::load(dst, old);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) nb[i] += old[i];
+          }
+          Vec<real>::store(dst, nb);
+        }
+      }
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < p.n_edges; e += blockDim.x) {
+    double s = 0.0;
+    for (int w = 0; w < kThreads / 32; ++w) s += sgrad[(size_t)w * p.n_edges + e];
+    p.grad_partial[(size_t)blockIdx.x * p.n_edges + e] = s;
+  }
+}
+
+// ------------------------------------------------------------- P-matrices
+// P(t r) = U diag(exp(lambda r t)) U^-1 in FP64; a zero length gives the identity.
+__global__ void pmatrix_kernel(int n_parts, int n_edges, int R, const double *__restrict__ lambda,
+                               const double *__restrict__ U, const double *__restrict__ Uinv,
+                               const double *__restrict__ rates, const double *__restrict__ brlen,
+                               double *__restrict__ pmat64, float *__restrict__ pmat32) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int total = n_parts * n_edges * R * 16;
+  if (idx >= total) return;
+  const int ij = idx & 15;
+  const int i = ij >> 2, j = ij & 3;
+  const int rr = (idx >> 4) % R;
+  const int e = (idx >> 4) / R % n_edges;
+  const int part = (idx >> 4) / R / n_edges;
+  const double t = brlen[e] * rates[part * R + rr];
+  double v;
+  if (brlen[e] == 0.0) {
+    v = (i == j) ? 1.0 : 0.0;
+  } else {
+    v = 0.0;
+    for (int k = 0; k < 4; ++k)
+      v += U[part * 16 + i * 4 + k] * exp(lambda[part * 4 + k] * t) * Uinv[part * 16 + k * 4 + j];
+  }
+  pmat64[idx] = v;
+  if (pmat32) pmat32[idx] = (float)v;
+}
+
+// ------------------------------------------ per-(tree, partition) site sums
+// Deterministic compensated (Kahan) FP64 sum of the per-unit partials.
+__global__ void tree_reduce_kernel(const MixParams m) {
+  const int slot = blockIdx.x, part = blockIdx.y;
+  const int ub = m.parts[part].unit_begin, ue = m.parts[part].unit_end;
+  const double *src = m.site_partial + (size_t)slot * m.n_units;
+  double s = 0.0, c = 0.0;
+  for (int u = ub + threadIdx.x; u < ue; u += blockDim.x) {
+    const double y = src[u] - c;
+    const double t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __shared__ double red[256];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) m.tree_logl[(size_t)slot * m.n_parts + part] = red[0];
+}
+
+// --------------------------------------------------------------- mixture
+// AVERAGE: logL_p = log sum_T P(T) L_{T,p} (max-shifted); BEST: max_T.
+// Posterior tree weights become the adjoint seeds; the reticulation gradient
+// is sum_p sum_T w_{T,p} d log P(T) / d p_k.
+__global__ void mix_kernel(const MixParams m) {
+  const int32_t *slot_begin = m.slot_begin, *slot_roots = m.slot_roots;
+  __shared__ double sval[256];
+  __shared__ int sidx[256];
+  __shared__ double s_logl;
+  __shared__ int s_arg;
+  double *wts = m.weights;  // [n_roots]
+  const int tid = threadIdx.x;
+  double total = 0.0;
+  for (int r = tid; r < m.n_ret; r += blockDim.x) m.out[2 + m.n_parts + r] = 0.0;
+  __syncthreads();
+  for (int part = 0; part < m.n_parts; ++part) {
+    double best = -INFINITY;
+    int arg = 0x7fffffff;
+    for (int i = tid; i < m.n_roots; i += blockDim.x) {
+      if (m.root_logprob[i] < m.min_logprob) continue;
+      const double v = m.root_logprob[i] + m.tree_logl[(size_t)m.root_slot[i] * m.n_parts + part];
+      if (v > best || (v == best && i < arg)) {
+        best = v;
+        arg = i;
+      }
+    }
+    sval[tid] = best;
+    sidx[tid] = arg;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+      if (tid < o) {
+        const double a = sval[tid], b = sval[tid + o];
+        const int ia = sidx[tid], ib = sidx[tid + o];
+        if (b > a || (b == a && ib < ia)) {
+          sval[tid] = b;
+          sidx[tid] = ib;
+        }
+      }
+      __syncthreads();
+    }
+    const double mx = sval[0];
+    const int amax = sidx[0];
+    __syncthreads();
+    if (m.variant == 0) {  // AVERAGE
+      double acc = 0.0;
+      for (int i = tid; i < m.n_roots; i += blockDim.x) {
+        if (m.root_logprob[i] < m.min_logprob) continue;
+        acc += exp(m.root_logprob[i] + m.tree_logl[(size_t)m.root_slot[i] * m.n_parts + part] - mx);
+      }
+      sval[tid] = acc;
+      __syncthreads();
+      for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (tid < o) sval[tid] += sval[tid + o];
+        __syncthreads();
+      }
+      if (tid == 0) s_logl = mx + log(sval[0]);
+      __syncthreads();
+      const double lp = s_logl;
+      for (int i = tid; i < m.n_roots; i += blockDim.x) {
+        wts[i] = (m.root_logprob[i] < m.min_logprob)
+                     ? 0.0
+                     : exp(m.root_logprob[i] + m.tree_logl[(size_t)m.root_slot[i] * m.n_parts + part] - lp);
+      }
+    } else {  // BEST
+      if (tid == 0) {
+        s_logl = mx;
+        s_arg = amax;
+      }
+      __syncthreads();
+      for (int i = tid; i < m.n_roots; i += blockDim.x) wts[i] = (i == s_arg) ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    const double lp = s_logl;
+    total += lp;
+    if (tid == 0) m.out[2 + part] = lp;
+    for (int sl = tid; sl < m.n_slots; sl += blockDim.x) {
+      double s = 0.0;
+      for (int q = slot_begin[sl]; q < slot_begin[sl + 1]; ++q) s += wts[slot_roots[q]];
+      m.seeds[(size_t)sl * m.n_parts + part] = s;
+    }
+    for (int k = tid; k < m.n_ret; k += blockDim.x) {
+      double s = 0.0;
+      for (int i = 0; i < m.n_roots; ++i) s += wts[i] * m.root_dlogprob[(size_t)i * m.n_ret + k];
+      m.out[2 + m.n_parts + k] += s;
+    }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    m.out[0] = total;
+    m.out[1] = (isfinite(total) ? 0.0 : 1.0);
+  }
+}
+
+__global__ void grad_reduce_kernel(int n_blocks, int n_edges, const double *partial, double *grad) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n_edges) return;
+  double s = 0.0;
+  for (int b = 0; b < n_blocks; ++b) s += partial[(size_t)b * n_edges + e];
+  grad[e] = s;
+}
+
+template <typename real, int R>
+void fwd_launch(cudaStream_t s, int grid, const SweepParams &p) {
+  forward_kernel<real, R><<<grid, kThreads, 0, s>>>(p);
+}
+
+template <typename real, int R>
+void bwd_launch(cudaStream_t s, int grid, const SweepParams &p) {
+  const size_t smem = (size_t)(kThreads / 32) * p.n_edges * sizeof(double);
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(backward_kernel<real, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  backward_kernel<real, R><<<grid, kThreads, smem, s>>>(p);
+}
+
+template <typename real, int R>
+int occupancy(bool backward, int n_edges_hint) {
+  int nb = 0;
+  if (backward)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, backward_kernel<real, R>, kThreads,
+                                                  (size_t)(kThreads / 32) * n_edges_hint * sizeof(double));
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, forward_kernel<real, R>, kThreads, 0);
+  return nb;
+}
+
+}  // namespace
+
+#define NETLK_DISPATCH_R(R, FN, ...)             \
+  switch (R) {                                   \
+    case 1: FN<real, 1>(__VA_ARGS__); break;     \
+    case 2: FN<real, 2>(__VA_ARGS__); break;     \
+    case 4: FN<real, 4>(__VA_ARGS__); break;     \
+    case 8: FN<real, 8>(__VA_ARGS__); break;     \
+  }
+
+void launch_forward(cudaStream_t s, int precision, int R, int grid, const SweepParams &p) {
+  if (precision == 1) {
+    using real = float;
+    NETLK_DISPATCH_R(R, fwd_launch, s, grid, p);
+  } else {
+    using real = double;
+    NETLK_DISPATCH_R(R, fwd_launch, s, grid, p);
+  }
+  g_launches++;
+}
+
+void launch_backward(cudaStream_t s, int precision, int R, int grid, const SweepParams &p) {
+  if (precision == 1) {
+    using real = float;
+    NETLK_DISPATCH_R(R, bwd_launch, s, grid, p);
+  } else {
+    using real = double;
+    NETLK_DISPATCH_R(R, bwd_launch, s, grid, p);
+  }
+  g_launches++;
+}
+
+int max_resident_blocks(int precision, int R, bool backward, int n_edges_hint) {
+  int nb = 0;
+#define NETLK_OCC(real)                                       \
+  switch (R) {                                                \
+    case 1: nb = occupancy<real, 1>(backward, n_edges_hint); break; \
+    case 2: nb = occupancy<real, 2>(backward, n_edges_hint); break; \
+    case 4: nb = occupancy<real, 4>(backward, n_edges_hint); break; \
+    case 8: nb = occupancy<real, 8>(backward, n_edges_hint); break; \
+  }
+  if (precision == 1) {
+    NETLK_OCC(float)
+  } else {
+    NETLK_OCC(double)
+  }
+#undef NETLK_OCC
+  return nb < 1 ? 1 : nb;
+}
+
+void launch_pmatrix(cudaStream_t s, int n_parts, int n_edges, int R, const double *lambda, const double *U,
+                    const double *Uinv, const double *rates, const double *brlen, double *pmat64,
+                    float *pmat32) {
+  const int total = n_parts * n_edges * R * 16;
+  pmatrix_kernel<<<(total + 255) / 256, 256, 0, s>>>(n_parts, n_edges, R, lambda, U, Uinv, rates, brlen,
+                                                     pmat64, pmat32);
+  g_launches++;
+}
+
+void launch_tree_reduce(cudaStream_t s, const MixParams &m) {
+  dim3 grid(m.n_slots, m.n_parts);
+  tree_reduce_kernel<<<grid, 256, 0, s>>>(m);
+  g_launches++;
+}
+
+void launch_mix(cudaStream_t s, const MixParams &m) {
+  mix_kernel<<<1, 256, 0, s>>>(m);
+  g_launches++;
+}
+
+void launch_grad_reduce(cudaStream_t s, int n_blocks, int n_edges, const double *partial, double *grad) {
+  grad_reduce_kernel<<<(n_edges + 127) / 128, 128, 0, s>>>(n_blocks, n_edges, partial, grad);
+  g_launches++;
+}
+
+}  // namespace netlk

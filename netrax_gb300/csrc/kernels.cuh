@@ -1,0 +1,89 @@
+// Device-side data layout and kernel launchers of netlk (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace netlk {
+
+// Ops per unrolled group: the host pads every level of both schedules to a
+// multiple of this, with no-op entries (out / x == -1).
+constexpr int kGroup = 4;
+constexpr int kThreads = 256;
+
+// Forward op: CLV of variant `out` = (P[ea] . child a) (*) (P[eb] . child b).
+// Child refs: >= 0 variant, -1-tip for a tip, INT32_MIN for the fake all-ones
+// child (eb == -1). slot >= 0: the variant holds a displayed tree's root CLV;
+// its per-site log-likelihoods are summed into site_partial[slot].
+struct alignas(32) FwdOp {
+  int32_t out, a, b, ea, eb, slot, pad0, pad1;
+};
+
+// Adjoint op for variant x (reverse level order).
+// adj_x: adjoint slot holding contributions from x's parents, or -1 (none).
+// seed: dtroot slot whose tree weights seed x, or -1.
+// adj_a / adj_b: adjoint slot of the child, mode 0 none, 1 store, 2 accumulate.
+struct alignas(32) BwdOp {
+  int32_t x, a, b, ea, eb, adj_x, seed, modes;  // modes = mode_a | mode_b << 8
+  int32_t adj_a, adj_b, pad0, pad1, pad2, pad3, pad4, pad5;
+};
+
+struct DevPartition {
+  int32_t unit_begin, unit_end;  // units (warp pattern groups) of this partition
+};
+
+// Everything the sweeps read, in device memory.
+struct SweepParams {
+  int32_t n_units;      // pattern groups of 32/R patterns
+  int64_t n_patterns;   // padded total (N)
+  int32_t n_edges;
+  int32_t n_fwd_ops;
+  int32_t n_bwd_ops;
+  int32_t n_parts;
+  const FwdOp *fwd_ops;
+  const BwdOp *bwd_ops;
+  const int32_t *unit_part;     // [n_units]
+  const uint8_t *tips;          // [n_tips][N] 4-bit state masks
+  const double *weights;        // [N] pattern weights (0 for padding)
+  const void *pmat;             // [n_parts][n_edges][R][4][4] real
+  const double *freqs;          // [n_parts][4]
+  const double *rate_weights;   // [n_parts][R]
+  const double *rates;          // [n_parts][R]
+  const double *Q;              // [n_parts][16]
+  void *clv;                    // [V][N][R][4] real
+  int32_t *scaler;              // [V][N]
+  void *adj;                    // [A][N][R][4] real
+  double *site_partial;         // [n_slots][n_units]
+  const double *seeds;          // [n_slots][n_parts]
+  double *grad_partial;         // [gridDim][n_edges]
+};
+
+struct MixParams {
+  int32_t n_slots, n_parts, n_roots, n_ret, variant, n_units;
+  double min_logprob;
+  const DevPartition *parts;      // [n_parts]
+  const double *site_partial;     // [n_slots][n_units]
+  double *tree_logl;              // [n_slots][n_parts]
+  const int32_t *root_slot;       // [n_roots]
+  const double *root_logprob;     // [n_roots]
+  const double *root_dlogprob;    // [n_roots][n_ret]
+  double *seeds;                  // [n_slots][n_parts]
+  double *weights;                // [n_roots] scratch: tree posterior weights
+  const int32_t *slot_begin;      // [n_slots+1] CSR: roots whose tree root is a slot
+  const int32_t *slot_roots;      // [n_roots]
+  double *out;                    // [2 + n_parts + n_ret]: total, status, part logl, dret
+};
+
+void launch_pmatrix(cudaStream_t s, int n_parts, int n_edges, int R, const double *lambda,
+                    const double *U, const double *Uinv, const double *rates, const double *brlen,
+                    double *pmat64, float *pmat32);
+void launch_forward(cudaStream_t s, int precision, int R, int grid, const SweepParams &p);
+void launch_backward(cudaStream_t s, int precision, int R, int grid, const SweepParams &p);
+void launch_tree_reduce(cudaStream_t s, const MixParams &m);
+void launch_mix(cudaStream_t s, const MixParams &m);
+void launch_grad_reduce(cudaStream_t s, int n_blocks, int n_edges, const double *partial, double *grad);
+int max_resident_blocks(int precision, int R, bool backward, int n_edges);
+// Number of kernel launches issued by the launchers above (host counter).
+int64_t launches_issued();
+
+}  // namespace netlk

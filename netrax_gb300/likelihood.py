@@ -1,0 +1,260 @@
+"""Python host API over the netlk C ABI.
+
+Mirrors the reference's likelihood entry points:
+
+* ``NetworkLikelihood.loglikelihood()`` - ``computeLoglikelihood(ann_network,
+  incremental, update_pmatrices)`` (``src/likelihood/LikelihoodComputation.hpp:17-18``);
+  per-partition values mirror ``fake_treeinfo->partition_loglh`` and per-tree
+  values ``TreeLoglData::tree_partition_logl``.
+* ``loglikelihood_gradient()`` - one forward + one adjoint sweep giving
+  d logL / d branch length for every edge and d logL / d reticulation
+  probability, replacing the per-edge sumtable derivatives of
+  ``src/likelihood/LikelihoodDerivatives.cpp:190-344``.
+* ``set_branch_lengths`` / ``set_reticulation_probs`` / ``set_model`` - the
+  parameter updates the optimizers make (``src/optimization/NetworkState.cpp``,
+  ``ReticulationOptimization.cpp:25-38``).
+* ``NetworkLogL`` - a ``torch.autograd.Function`` over branch lengths and
+  reticulation probabilities.
+
+All evaluation runs in the CUDA library; there is no CPU fallback.
+"""
+import ctypes
+import math
+
+import numpy as np
+
+from . import _native as N
+from .network import NetworkDesc
+
+VARIANTS = {"AVERAGE": N.NETLK_AVERAGE, "BEST": N.NETLK_BEST}
+PRECISIONS = {"fp64": N.NETLK_FP64, "fp32": N.NETLK_FP32}
+
+
+def _ptr(a, ct):
+    return a.ctypes.data_as(ctypes.POINTER(ct)) if a is not None else None
+
+
+class NetworkLikelihood:
+    def __init__(self, network: NetworkDesc, partitions, variant="AVERAGE", precision="fp32",
+                 min_interesting_tree_logprob=math.log(1e-6), device=0, use_cuda_graph=True,
+                 host_only=False, rates=None):
+        L = N.lib()
+        self.network = network
+        self.n_parts = len(partitions)
+        self.n_edges = network.n_edges
+        self.n_ret = network.n_reticulations
+        keep = []
+
+        def arr(a, dt):
+            a = np.ascontiguousarray(a, dtype=dt)
+            keep.append(a)
+            return a
+
+        topo = N.Topology()
+        topo.n_nodes = network.n_nodes
+        topo.n_tips = network.n_tips
+        topo.n_edges = network.n_edges
+        topo.n_reticulations = network.n_reticulations
+        topo.root = network.root
+        topo.edge_parent = _ptr(arr(network.edge_parent, np.int32), ctypes.c_int32)
+        topo.edge_child = _ptr(arr(network.edge_child, np.int32), ctypes.c_int32)
+        topo.node_child_edges = _ptr(arr(network.node_child_edges, np.int32), ctypes.c_int32)
+        topo.ret_node = _ptr(arr(network.ret_node, np.int32), ctypes.c_int32)
+        topo.ret_first_edge = _ptr(arr(network.ret_first_edge, np.int32), ctypes.c_int32)
+        topo.ret_second_edge = _ptr(arr(network.ret_second_edge, np.int32), ctypes.c_int32)
+        parts = (N.Partition * self.n_parts)()
+        self.n_patterns = []
+        for i, pd in enumerate(partitions):
+            p = parts[i]
+            p.states = getattr(pd, "states", 4)
+            p.rate_cats = getattr(pd, "rate_cats", 4)
+            ts = arr(pd.tip_states, np.uint32)
+            p.n_patterns = ts.shape[1]
+            self.n_patterns.append(ts.shape[1])
+            p.tip_states = _ptr(ts, ctypes.c_uint32)
+            p.pattern_weights = _ptr(arr(pd.weights, np.float64), ctypes.c_double)
+            p.freqs = _ptr(arr(pd.freqs, np.float64), ctypes.c_double)
+            p.exchangeabilities = _ptr(arr(pd.exch, np.float64), ctypes.c_double)
+            p.alpha = float(pd.alpha)
+            r = None if rates is None else rates[i]
+            p.rates = _ptr(arr(r, np.float64), ctypes.c_double) if r is not None else None
+            p.rate_weights = None
+        opts = N.Options()
+        L.netlk_options_default(ctypes.byref(opts))
+        opts.variant = VARIANTS[variant]
+        opts.precision = PRECISIONS[precision]
+        opts.min_interesting_tree_logprob = float(min_interesting_tree_logprob)
+        opts.device = int(device)
+        opts.use_cuda_graph = int(bool(use_cuda_graph))
+        opts.host_only = int(bool(host_only))
+        bl = arr(network.branch_lengths, np.float64)
+        rp = arr(network.ret_first_probs, np.float64) if self.n_ret else None
+        h = ctypes.c_void_p()
+        st = L.netlk_create(ctypes.byref(topo), parts, self.n_parts, _ptr(bl, ctypes.c_double),
+                            _ptr(rp, ctypes.c_double), ctypes.byref(opts), ctypes.byref(h))
+        N.check(st, None)
+        self._h = h
+        self.variant, self.precision = variant, precision
+        self.branch_lengths = np.array(network.branch_lengths, np.float64)
+        self.ret_probs = np.array(network.ret_first_probs, np.float64)
+        s = N.DagStats()
+        N.check(L.netlk_get_dag_stats(self._h, ctypes.byref(s)), self._h)
+        self.stats = s.as_dict()
+        self.n_roots = self.stats["n_root_variants"]
+        self.n_variants = self.stats["n_variants"]
+
+    # ----------------------------------------------------------- lifecycle
+    def close(self):
+        if getattr(self, "_h", None):
+            N.lib().netlk_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---------------------------------------------------------- parameters
+    def set_branch_lengths(self, b):
+        b = np.ascontiguousarray(b, np.float64)
+        N.check(N.lib().netlk_set_branch_lengths(self._h, _ptr(b, ctypes.c_double), b.size), self._h)
+        self.branch_lengths = b.copy()
+
+    def set_reticulation_probs(self, p):
+        p = np.ascontiguousarray(p, np.float64)
+        N.check(N.lib().netlk_set_reticulation_probs(self._h, _ptr(p, ctypes.c_double), p.size), self._h)
+        self.ret_probs = p.copy()
+
+    def set_model(self, part, freqs, exch, alpha, rates=None):
+        f = np.ascontiguousarray(freqs, np.float64)
+        x = np.ascontiguousarray(exch, np.float64)
+        r = None if rates is None else np.ascontiguousarray(rates, np.float64)
+        N.check(N.lib().netlk_set_model(self._h, part, _ptr(f, ctypes.c_double), _ptr(x, ctypes.c_double),
+                                        float(alpha), _ptr(r, ctypes.c_double)), self._h)
+
+    # ---------------------------------------------------------- evaluation
+    def loglikelihood(self, details=False):
+        tot = ctypes.c_double()
+        pl = np.zeros(self.n_parts)
+        tl = np.zeros(self.n_roots * self.n_parts) if details else None
+        N.check(N.lib().netlk_loglikelihood(self._h, ctypes.byref(tot), _ptr(pl, ctypes.c_double),
+                                            _ptr(tl, ctypes.c_double)), self._h)
+        if details:
+            return tot.value, pl, tl.reshape(self.n_roots, self.n_parts)
+        return tot.value
+
+    def loglikelihood_gradient(self, details=False):
+        tot = ctypes.c_double()
+        pl = np.zeros(self.n_parts)
+        gb = np.zeros(self.n_edges)
+        gr = np.zeros(max(1, self.n_ret))
+        N.check(N.lib().netlk_loglikelihood_gradient(self._h, ctypes.byref(tot), _ptr(pl, ctypes.c_double),
+                                                     _ptr(gb, ctypes.c_double), _ptr(gr, ctypes.c_double)),
+                self._h)
+        if details:
+            return tot.value, gb, gr[:self.n_ret], pl
+        return tot.value, gb, gr[:self.n_ret]
+
+    def edge_derivatives(self, edge, second=True):
+        d1, d2 = ctypes.c_double(), ctypes.c_double()
+        N.check(N.lib().netlk_edge_derivatives(self._h, edge, 0, ctypes.byref(d1),
+                                               ctypes.byref(d2) if second else None), self._h)
+        return (d1.value, d2.value) if second else d1.value
+
+    def tree_partials(self):
+        out = np.zeros(self.n_roots * self.n_parts)
+        N.check(N.lib().netlk_tree_partials(self._h, _ptr(out, ctypes.c_double)), self._h)
+        return out.reshape(self.n_roots, self.n_parts)
+
+    def mix_and_backward(self, global_partials):
+        g = np.ascontiguousarray(global_partials, np.float64).ravel()
+        tot = ctypes.c_double()
+        pl = np.zeros(self.n_parts)
+        gb = np.zeros(self.n_edges)
+        gr = np.zeros(max(1, self.n_ret))
+        N.check(N.lib().netlk_mix_and_backward(self._h, _ptr(g, ctypes.c_double), ctypes.byref(tot),
+                                               _ptr(pl, ctypes.c_double), _ptr(gb, ctypes.c_double),
+                                               _ptr(gr, ctypes.c_double)), self._h)
+        return tot.value, gb, gr[:self.n_ret], pl
+
+    # ------------------------------------------------------- introspection
+    def dag_export(self):
+        V = self.n_variants
+        words = max(1, (1 << self.n_ret) // 64)
+        node = np.zeros(V, np.int32)
+        ch = np.zeros(2 * V, np.int32)
+        ed = np.zeros(2 * V, np.int32)
+        cov = np.zeros(V * words, np.uint64)
+        N.check(N.lib().netlk_dag_export(self._h, _ptr(node, ctypes.c_int32), _ptr(ch, ctypes.c_int32),
+                                         _ptr(ed, ctypes.c_int32), _ptr(cov, ctypes.c_uint64), words), self._h)
+        return node, ch.reshape(V, 2), ed.reshape(V, 2), cov.reshape(V, words)
+
+    def root_export(self):
+        R = self.n_roots
+        rv = np.zeros(R, np.int32)
+        dt = np.zeros(R, np.int32)
+        lp = np.zeros(R)
+        N.check(N.lib().netlk_root_export(self._h, _ptr(rv, ctypes.c_int32), _ptr(dt, ctypes.c_int32),
+                                          _ptr(lp, ctypes.c_double)), self._h)
+        return rv, dt, lp
+
+    def get_clv(self, variant, part):
+        n = self.n_patterns[part]
+        clv = np.zeros(n * 16)
+        sc = np.zeros(n, np.int32)
+        N.check(N.lib().netlk_get_clv(self._h, variant, part, _ptr(clv, ctypes.c_double),
+                                      _ptr(sc, ctypes.c_int32)), self._h)
+        return clv.reshape(n, 4, 4), sc
+
+    def stream(self):
+        s = ctypes.c_void_p()
+        N.check(N.lib().netlk_get_stream(self._h, ctypes.byref(s)), self._h)
+        return s.value
+
+    def launch_count(self):
+        n = ctypes.c_int64()
+        N.check(N.lib().netlk_launch_count(self._h, ctypes.byref(n)), self._h)
+        return n.value
+
+
+def compute_loglikelihood(lik: NetworkLikelihood, incremental=1, update_pmatrices=1):
+    """Same role and arguments as the reference's ``computeLoglikelihood``.
+
+    Every call recomputes the P-matrices and all displayed-tree CLVs on the GPU
+    (a full sweep costs less than the reference's validity bookkeeping), so
+    ``incremental`` and ``update_pmatrices`` only exist for call-site parity.
+    """
+    del incremental, update_pmatrices
+    return lik.loglikelihood()
+
+
+try:
+    import torch
+
+    class NetworkLogL(torch.autograd.Function):
+        """logL(branch_lengths, reticulation_probs) with the adjoint-sweep gradient."""
+
+        @staticmethod
+        def forward(ctx, branch_lengths, ret_probs, lik):
+            lik.set_branch_lengths(branch_lengths.detach().cpu().double().numpy())
+            if lik.n_ret:
+                lik.set_reticulation_probs(ret_probs.detach().cpu().double().numpy())
+            val, gb, gr = lik.loglikelihood_gradient()
+            ctx.save_for_backward(torch.from_numpy(gb), torch.from_numpy(np.array(gr, np.float64)))
+            ctx.devs = (branch_lengths.device, ret_probs.device)
+            return torch.tensor(val, dtype=torch.float64, device=branch_lengths.device)
+
+        @staticmethod
+        def backward(ctx, grad_out):
+            gb, gr = ctx.saved_tensors
+            g = grad_out.detach().cpu().double()
+            return (g * gb).to(ctx.devs[0]), (g * gr).to(ctx.devs[1]), None
+except ImportError:  # torch is optional for the C ABI itself
+    NetworkLogL = None

@@ -1,0 +1,75 @@
+"""Build and load the oracle's C arithmetic (``clv.c``) as a shared library.
+
+Test infrastructure only. Output goes to ``oracle/_build/`` (git-ignored).
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "liboracle.so")
+
+
+def build(force: bool = False) -> str:
+    src = os.path.join(HERE, "clv.c")
+    if (not force and os.path.exists(LIB)
+            and os.path.getmtime(LIB) >= os.path.getmtime(src)):
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    tmp = LIB + ".tmp%d" % os.getpid()
+    subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-fopenmp",
+                           "-std=c99", src, "-o", tmp, "-lm"])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = ctypes.CDLL(build())
+        dp = ctypes.POINTER(ctypes.c_double)
+        up = ctypes.POINTER(ctypes.c_uint32)
+        _lib.oracle_update_partial.argtypes = [
+            ctypes.c_int64, ctypes.c_int, ctypes.c_int, dp, up, dp, up, dp,
+            dp, up, dp]
+        _lib.oracle_update_partial.restype = None
+        _lib.oracle_root_logl.argtypes = [
+            ctypes.c_int64, ctypes.c_int, ctypes.c_int, dp, up, dp, dp, dp, dp]
+        _lib.oracle_root_logl.restype = ctypes.c_double
+        _lib.oracle_num_threads.restype = ctypes.c_int
+    return _lib
+
+
+def _dp(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _up(a):
+    if a is None:
+        return None
+    assert a.dtype == np.uint32 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+
+
+def update_partial(parent, parent_scaler, left, left_scaler, pl,
+                   right, right_scaler, pr):
+    n, R, S = parent.shape
+    lib().oracle_update_partial(n, R, S, _dp(parent), _up(parent_scaler),
+                                _dp(left), _up(left_scaler), _dp(pl),
+                                _dp(right), _up(right_scaler), _dp(pr))
+
+
+def root_logl(clv, scaler, freqs, rate_weights, weights, persite=None):
+    n, R, S = clv.shape
+    return lib().oracle_root_logl(n, R, S, _dp(clv), _up(scaler), _dp(freqs),
+                                  _dp(rate_weights), _dp(weights),
+                                  _dp(persite))

@@ -1,0 +1,157 @@
+"""C ABI surface and the displayed-tree DAG, on CPU (host_only contexts).
+
+* the library loads and exports every function ``include/netlk.h`` declares;
+* the Extended Newick reader numbers nodes / edges like the oracle (and so the
+  reference, src/io/NetworkIO.cpp:39-299);
+* the DAG compiled on bitsets equals the oracle's literal restatement of
+  processNodeImproved node by node: same variant count and order, same covered
+  configuration sets, same displayed-tree root variant per root tree, same
+  tree log-probabilities (the golden ``dag`` records);
+* invalid input is rejected with a status code, never a crash.
+"""
+import ctypes
+import math
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, GoldenPartition, golden_cases
+from netrax_gb300 import _native
+from netrax_gb300.likelihood import NetworkLikelihood
+from netrax_gb300.network import parse_extended_newick
+
+CASES = golden_cases()
+
+
+def test_header_symbols_exported():
+    header = open(os.path.join(ROOT, "include", "netlk.h")).read()
+    names = set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(netlk_\w+)\s*\(", header, re.M))
+    assert len(names) >= 19
+    L = _native.lib()
+    for n in sorted(names):
+        assert hasattr(L, n), n
+    assert set(names) == set(_native.EXPORTED)
+
+
+def _covered(cov_row, n_ret):
+    bits = set()
+    for w, word in enumerate(cov_row):
+        word = int(word)
+        for b in range(64):
+            if (word >> b) & 1 and w * 64 + b < (1 << n_ret):
+                bits.add(w * 64 + b)
+    return bits
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda c: c["name"])
+def test_dag_matches_oracle_enumeration(case):
+    from oracle import newick as onewick
+    net = parse_extended_newick(case["newick"])
+    onet = onewick.parse_newick(case["newick"])
+    assert net.root == onet.root and net.n_tips == onet.n_tips
+    assert list(net.edge_parent) == onet.edge_parent and list(net.edge_child) == onet.edge_child
+    assert np.allclose(net.branch_lengths, onet.edge_length, rtol=0, atol=0)
+    parts = [GoldenPartition(d) for d in case["partitions"]]
+    lik = NetworkLikelihood(net, parts, host_only=True)
+    node, ch, ed, cov = lik.dag_export()
+    got = [[int(node[i]), sorted(_covered(cov[i], net.n_reticulations))] for i in range(len(node))]
+    want = sorted(case["dag"], key=lambda x: x[0])
+    # variants of one node keep their order; nodes are listed in id order in the fixture
+    got_by_node = {}
+    for v, s in got:
+        got_by_node.setdefault(v, []).append(s)
+    want_by_node = {}
+    for v, s in want:
+        want_by_node.setdefault(v, []).append(s)
+    assert got_by_node == want_by_node
+    rv, dt, lp = lik.root_export()
+    for k, t in enumerate(case["AVERAGE"]["trees"]):
+        assert lp[k] == pytest.approx(t["logprob"], rel=1e-13, abs=1e-13)
+        dnode = int(node[dt[k]])
+        assert dnode == t["dtroot_node"]
+        same_node = [i for i in range(len(node)) if node[i] == dnode]
+        assert same_node.index(dt[k]) == t["dtroot_index"]
+    # children of each variant are variants of the node's children (or tips / fake)
+    for i in range(len(node)):
+        for j in range(2):
+            if ch[i, j] >= 0:
+                assert net.edge_child[ed[i, j]] == node[ch[i, j]]
+            elif ch[i, j] != -(2 ** 31):
+                assert net.edge_child[ed[i, j]] == -1 - ch[i, j]
+    assert lik.stats["site_clv_updates"] == lik.stats["n_variants"] * lik.stats["n_patterns_total"]
+
+
+def test_reference_numbering_of_small_network():
+    # ((A:2,((B:1,C:1)P:1)X#H1:0::0.3)Q:2,(D:2,X#H1:0::0.7)R:2); tips in string order
+    net = parse_extended_newick("((A:2,((B:1,C:1)P:1)X#H1:0::0.3)Q:2,(D:2,X#H1:0::0.7)R:2);")
+    assert net.n_tips == 4 and net.n_reticulations == 1
+    assert net.ret_first_probs[0] == pytest.approx(0.3)
+    assert net.n_edges == net.n_tips + (net.n_nodes - net.n_tips - 1) - 1 + 2
+    assert net.branch_lengths.min() == pytest.approx(1e-6)  # zero length clamped
+    assert net.root == net.n_nodes - 1 - net.n_reticulations
+
+
+@pytest.mark.parametrize("bad", [
+    "((A,B);",                       # unbalanced
+    "(A,B)",                         # no semicolon
+    "((A,(B)#H1:::0.3),(C,#H1:::0.9));",  # probabilities do not sum to one
+])
+def test_newick_rejects_bad_input(bad):
+    with pytest.raises(ValueError):
+        parse_extended_newick(bad)
+
+
+def _small():
+    net = parse_extended_newick("((A:0.2,(B:0.1)X#H1:0.1::0.3)Q:0.2,(C:0.2,X#H1:0.1::0.7)R:0.2);")
+    part = GoldenPartition({"tip_states": [[1, 2], [2, 4], [8, 1]], "weights": [1, 2],
+                            "freqs": [.25] * 4, "exch": [1] * 6, "alpha": 1.0})
+    return net, part
+
+
+def test_invalid_arguments_return_status():
+    net, part = _small()
+    bad = net.__class__(**{**net.__dict__})
+    bad.branch_lengths = net.branch_lengths.copy()
+    bad.branch_lengths[0] = float("nan")
+    with pytest.raises(_native.NetlkError) as e:
+        NetworkLikelihood(bad, [part], host_only=True)
+    assert e.value.status == 1
+    cyc = net.__class__(**{**net.__dict__})
+    cyc.edge_child = net.edge_child.copy()
+    cyc.edge_child[0] = net.root  # root gets a parent -> not a rooted network
+    with pytest.raises(_native.NetlkError) as e:
+        NetworkLikelihood(cyc, [part], host_only=True)
+    assert e.value.status == 2
+    p2 = GoldenPartition({"tip_states": [[1, 0], [2, 4], [8, 1]], "weights": [1, 2],
+                          "freqs": [.25] * 4, "exch": [1] * 6, "alpha": 1.0})
+    p2.states = 20
+    with pytest.raises(_native.NetlkError) as e:
+        NetworkLikelihood(net, [p2], host_only=True)
+    assert e.value.status == 7
+
+
+def test_host_only_context_refuses_evaluation():
+    net, part = _small()
+    lik = NetworkLikelihood(net, [part], host_only=True)
+    with pytest.raises(_native.NetlkError) as e:
+        lik.loglikelihood()
+    assert e.value.status == _native.NETLK_ERR_NO_DEVICE
+    lik.set_branch_lengths(net.branch_lengths * 2)
+    with pytest.raises(_native.NetlkError):
+        lik.set_branch_lengths(net.branch_lengths[:-1])
+    with pytest.raises(_native.NetlkError):
+        lik.set_reticulation_probs([1.5])
+    lik.close()
+
+
+def test_too_many_reticulations_unsupported():
+    from netrax_gb300 import synth
+    rng = np.random.default_rng(5)
+    net = parse_extended_newick(synth.random_network_newick(rng, 40, 17))
+    part = GoldenPartition({"tip_states": [[1]] * 40, "weights": [1], "freqs": [.25] * 4,
+                            "exch": [1] * 6, "alpha": 1.0})
+    with pytest.raises(_native.NetlkError) as e:
+        NetworkLikelihood(net, [part], host_only=True)
+    assert e.value.status == 7

@@ -1,0 +1,205 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle.
+
+Tolerances (the benchmark spec): plain FP64 GPU kernel within 1e-9 relative logL of the
+oracle; FP32 CLVs with power-of-two scaling within 1e-6 relative; FP64 scale
+counters bit-exact; displayed-tree enumeration bit-exact (checked on CPU in
+test_dag_abi.py and here through the per-tree values). Gradients against
+central finite differences of the FP64 oracle (h = 1e-5).
+"""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import GoldenPartition, golden_cases
+
+pytestmark = pytest.mark.gpu
+
+CASES = golden_cases()
+FP64_REL = 1e-9
+FP32_REL = 1e-6
+
+
+def _lik(case, variant, precision, **kw):
+    from netrax_gb300.likelihood import NetworkLikelihood
+    from netrax_gb300.network import parse_extended_newick
+    net = parse_extended_newick(case["newick"])
+    parts = [GoldenPartition(d) for d in case["partitions"]]
+    return NetworkLikelihood(net, parts, variant=variant, precision=precision, **kw)
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda c: c["name"])
+@pytest.mark.parametrize("variant", ["AVERAGE", "BEST"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_logl_matches_oracle(case, variant, precision):
+    g = case[variant]
+    tol = FP64_REL if precision == "fp64" else FP32_REL
+    with _lik(case, variant, precision) as lik:
+        total, part, trees = lik.loglikelihood(details=True)
+        assert total == pytest.approx(g["logl"], rel=tol)
+        assert np.allclose(part, g["partition_logl"], rtol=tol, atol=0)
+        for k, t in enumerate(g["trees"]):
+            if t["partition_logl"] is None:
+                assert np.all(np.isnan(trees[k]))
+                continue
+            assert np.allclose(trees[k], t["partition_logl"], rtol=tol, atol=0), k
+        again = lik.loglikelihood()
+        assert again == total  # repeated evaluation is bit-identical
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if "scaler_sums" in c["AVERAGE"]], ids=lambda c: c["name"])
+def test_fp64_scale_counters_bit_exact(case):
+    want = case["AVERAGE"]["scaler_sums"]
+    with _lik(case, "AVERAGE", "fp64") as lik:
+        lik.loglikelihood()
+        node, _, _, _ = lik.dag_export()
+        # variants are listed node by node in the fixture; map GPU variants in the same order
+        order = sorted(range(len(node)), key=lambda i: (node[i], i))
+        got = []
+        for i in order:
+            s = 0
+            for p in range(lik.n_parts):
+                _, sc = lik.get_clv(i, p)
+                s += int(sc.sum())
+            got.append(s)
+        assert got == want
+        if case["name"].endswith("deep"):
+            assert max(want) > 0  # the case really exercises the 2^256 rescaling
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if "fd_grad_brlen" in c["AVERAGE"]], ids=lambda c: c["name"])
+@pytest.mark.parametrize("variant", ["AVERAGE", "BEST"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_gradient_matches_finite_differences(case, variant, precision):
+    g = case[variant]
+    fd = np.array(g["fd_grad_brlen"])
+    fdr = np.array(g["fd_grad_retprob"])
+    rtol, atol = (1e-4, 2e-3) if precision == "fp64" else (2e-3, 2e-2)
+    with _lik(case, variant, precision) as lik:
+        total, gb, gr = lik.loglikelihood_gradient()
+        assert total == pytest.approx(g["logl"], rel=FP64_REL if precision == "fp64" else FP32_REL)
+        # edges sitting on the 1e-6 clamp only have a one-sided difference
+        free = lik.branch_lengths > 2e-5
+        assert np.allclose(gb[free], fd[free], rtol=rtol, atol=atol * max(1.0, np.abs(fd).max() * 1e-3))
+        if len(fdr):
+            assert np.allclose(gr, fdr, rtol=rtol, atol=atol)
+
+
+def test_gradient_logl_equals_logl_only():
+    case = [c for c in CASES if c["name"] == "synthetic_16taxa_4ret_3parts"][0]
+    for precision in ("fp64", "fp32"):
+        with _lik(case, "AVERAGE", precision) as lik:
+            a = lik.loglikelihood()
+            b, _, _ = lik.loglikelihood_gradient()
+            assert a == b
+
+
+def test_graph_and_direct_launch_agree():
+    case = [c for c in CASES if c["name"] == "synthetic_12taxa_3ret_2parts"][0]
+    with _lik(case, "AVERAGE", "fp32", use_cuda_graph=True) as a, \
+            _lik(case, "AVERAGE", "fp32", use_cuda_graph=False) as b:
+        ta, ga, ra = a.loglikelihood_gradient()
+        tb, gb, rb = b.loglikelihood_gradient()
+        assert ta == tb
+        assert np.array_equal(ga, gb) and np.array_equal(ra, rb)
+
+
+def test_parameter_updates_change_and_restore():
+    case = [c for c in CASES if c["name"] == "twoReticulations"][0]
+    with _lik(case, "AVERAGE", "fp64") as lik:
+        base = lik.loglikelihood()
+        bl = lik.branch_lengths.copy()
+        lik.set_branch_lengths(bl * 1.5)
+        changed = lik.loglikelihood()
+        assert changed != base  # BrlenOptTest.cpp:248: a brlen change moves logL
+        lik.set_branch_lengths(bl)
+        assert lik.loglikelihood() == base  # incremental == full (DOUBLE_EQ)
+        p = lik.ret_probs.copy()
+        lik.set_reticulation_probs(np.clip(p * 0.5, 1e-3, None))
+        assert lik.loglikelihood() != base
+        lik.set_reticulation_probs(p)
+        assert lik.loglikelihood() == base
+
+
+def test_sharded_partials_match_whole():
+    """Two contexts over disjoint pattern halves + SUM of partials == one context."""
+    case = [c for c in CASES if c["name"] == "synthetic_16taxa_4ret_3parts"][0]
+    from netrax_gb300.likelihood import NetworkLikelihood
+    from netrax_gb300.network import parse_extended_newick
+    net = parse_extended_newick(case["newick"])
+    full = [GoldenPartition(d) for d in case["partitions"]]
+    halves = [[], []]
+    for gp in full:
+        n = gp.tip_states.shape[1]
+        for h, sl in enumerate((slice(0, n // 2), slice(n // 2, n))):
+            q = GoldenPartition(case["partitions"][0])
+            q.tip_states = np.ascontiguousarray(gp.tip_states[:, sl])
+            q.weights = gp.weights[sl].copy()
+            q.freqs, q.exch, q.alpha = gp.freqs, gp.exch, gp.alpha
+            halves[h].append(q)
+    with NetworkLikelihood(net, full, precision="fp64") as whole, \
+            NetworkLikelihood(net, halves[0], precision="fp64") as h0, \
+            NetworkLikelihood(net, halves[1], precision="fp64") as h1:
+        tw, gw, rw = whole.loglikelihood_gradient()
+        glob = h0.tree_partials() + h1.tree_partials()
+        t0, g0, r0, _ = h0.mix_and_backward(glob)
+        t1, g1, r1, _ = h1.mix_and_backward(glob)
+        assert t0 == pytest.approx(tw, rel=1e-12) and t1 == t0
+        assert np.allclose(g0 + g1, gw, rtol=1e-9, atol=1e-9)
+        assert np.allclose(r0, rw, rtol=1e-9, atol=1e-9)
+
+
+def test_fp32_matches_fp64_on_larger_network():
+    """50 taxa / 4 reticulations / 10 uneven partitions (scaled down) - FP32 vs FP64 GPU."""
+    from netrax_gb300 import synth
+    from netrax_gb300.likelihood import NetworkLikelihood
+    w = synth.config(1, scale=0.05)
+    for variant in ("AVERAGE", "BEST"):
+        with NetworkLikelihood(w.network, w.partitions, variant=variant, precision="fp64") as a, \
+                NetworkLikelihood(w.network, w.partitions, variant=variant, precision="fp32") as b:
+            ta, ga, ra = a.loglikelihood_gradient()
+            tb, gb, rb = b.loglikelihood_gradient()
+            assert tb == pytest.approx(ta, rel=FP32_REL)
+            assert np.allclose(gb, ga, rtol=1e-3, atol=1e-2 * max(1.0, np.abs(ga).max() * 1e-3))
+            assert np.allclose(rb, ra, rtol=1e-3, atol=1e-2)
+
+
+def test_fp64_matches_oracle_on_synthetic_config():
+    """Config-0 shape (20 taxa / 1 reticulation / 1k sites) against the oracle, computed here."""
+    from netrax_gb300 import synth
+    from netrax_gb300.likelihood import NetworkLikelihood
+    from oracle import improved, newick
+    w = synth.config(0)
+    net = newick.parse_newick(w.newick)
+    parts = [improved.Partition(p.tip_states, p.weights, p.freqs, p.exch,
+                                _rates(p.alpha)) for p in w.partitions]
+    for variant in ("AVERAGE", "BEST"):
+        ref = improved.ImprovedOracle(net, parts, variant=variant).loglikelihood()
+        with NetworkLikelihood(w.network, w.partitions, variant=variant, precision="fp64") as lik:
+            assert lik.loglikelihood() == pytest.approx(ref, rel=FP64_REL)
+
+
+def _rates(alpha):
+    from oracle import pllmath
+    return pllmath.gamma_rates_mean(alpha, 4)
+
+
+def test_torch_autograd_function():
+    torch = pytest.importorskip("torch")
+    from netrax_gb300.likelihood import NetworkLogL
+    case = [c for c in CASES if c["name"] == "smallNetwork"][0]
+    with _lik(case, "AVERAGE", "fp64") as lik:
+        b = torch.tensor(lik.branch_lengths, dtype=torch.float64, requires_grad=True)
+        p = torch.tensor(lik.ret_probs, dtype=torch.float64, requires_grad=True)
+        y = NetworkLogL.apply(b, p, lik)
+        y.backward()
+        _, gb, gr = lik.loglikelihood_gradient()
+        assert np.allclose(b.grad.numpy(), gb) and np.allclose(p.grad.numpy(), gr)
+        assert float(y) == pytest.approx(case["AVERAGE"]["logl"], rel=FP64_REL)
+
+
+def test_launch_count_reported():
+    case = [c for c in CASES if c["name"] == "tinyNetwork"][0]
+    with _lik(case, "AVERAGE", "fp32") as lik:
+        lik.loglikelihood_gradient()
+        assert lik.launch_count() == 6  # P-matrices, forward, reduce, mix, adjoint, gradient reduce
