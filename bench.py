@@ -1,0 +1,387 @@
+#!/usr/bin/env python
+"""Benchmark of the network-likelihood hot path on GB300.
+
+Workload (one "step"): one log-likelihood + gradient evaluation - forward
+sweep over every displayed-tree variant, per-(tree, partition) site sums,
+AVERAGE mixture, adjoint sweep, gradient reduction - of the 100 taxa /
+8 reticulations / 100k DNA sites network (GTR+G4, seeded synthetic data, the
+configuration the differentiation target is quoted on), FP32 CLVs with
+per-site power-of-two scaling. Branch lengths change every step (a new
+optimizer iterate), so P-matrices are recomputed every step too.
+
+value: whole-job evals/s with inputs resident in HBM (device-resident branch
+lengths, CUDA events on the library's stream, max over ranks).
+e2e: the same through the C ABI with host buffers (host branch lengths in,
+logL + gradient out), wall clock.
+Multi-GPU: every rank evaluates its own replica (independent optimizer
+iterates) - weak scaling, no collective on the data path.
+
+``--impl reference`` times the CPU restatement of the reference's pruning
+(``oracle/``, OpenMP over sites, all host cores) on a bounded pattern sample.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "logL+grad evals/s & site-CLV updates/s, FP32 vs FP64 GPU at ≤1e-6 rel ΔlogL"
+UNIT = "logL+grad evals/s"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="netlk", choices=["netlk", "reference"])
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--variant", default="AVERAGE", choices=["AVERAGE", "BEST"])
+    ap.add_argument("--fp64-steps", type=int, default=20)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=16384, help="patterns in the CPU sample")
+    ap.add_argument("--scale", type=float, default=1.0, help="site-count scale (1.0 = full workload)")
+    return ap.parse_args()
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group(backend=backend)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(x, ws, device):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples during the timed region."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + self.QUERY, "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.device)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def load_traffic():
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def cpu_port_rate(w, n_sample, steps, warmup, variant):
+    """Oracle (CPU restatement, OpenMP) forward-pass time on a pattern sample;
+    returns (evals/s of the full workload extrapolated by patterns, info)."""
+    from oracle import build as obuild
+    from oracle import improved, newick, pllmath
+    net = newick.parse_newick(w.newick)
+    parts, total, used = [], 0, 0
+    remaining = n_sample
+    for p in w.partitions:
+        take = min(p.n_patterns, remaining) if remaining > 0 else 0
+        total += p.n_patterns
+        if take <= 0:
+            continue
+        remaining -= take
+        used += take
+        parts.append(improved.Partition(np.ascontiguousarray(p.tip_states[:, :take]),
+                                        np.ascontiguousarray(p.weights[:take]), p.freqs, p.exch,
+                                        pllmath.gamma_rates_mean(p.alpha, 4)))
+    orc = improved.ImprovedOracle(net, parts, variant=variant)
+    orc.loglikelihood()  # enumeration (host-side, untimed)
+    rng = np.random.default_rng(123)
+    base = list(orc.brlen)
+    for _ in range(warmup):
+        orc.recompute()
+    times = []
+    for _ in range(steps):
+        orc.brlen = [b * math.exp(0.02 * rng.standard_normal()) for b in base]
+        t = time.perf_counter()
+        orc.recompute()
+        times.append(time.perf_counter() - t)
+    t_step = statistics.median(times)
+    evals = 1.0 / (t_step * total / used)
+    info = {"value": evals, "unit": UNIT, "cores": int(obuild.lib().oracle_num_threads()), "kind": "port",
+            "sample": "forward (logL) pruning of all %d variants on %d of %d patterns, median of %d "
+                      "steps, extrapolated by patterns; the CPU arm computes no gradient, so this is an "
+                      "upper bound on its logL+grad rate"
+                      % (sum(len(x) for x in orc.pernode[net.n_tips:]), used, total, steps),
+            "site_clv_updates_per_s": orc.update_count / t_step}
+    return evals, info
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    from netrax_gb300 import synth
+    w = synth.config(2, scale=args.scale)
+    steps = max(1, min(args.steps, 5))
+    evals, info = cpu_port_rate(w, args.cpu_sample, steps, min(args.warmup, 1), args.variant)
+    line = {"impl": "reference", "metric": METRIC, "value": evals, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": steps, "warmup": min(args.warmup, 1), "ms_per_step": 1000.0 / evals,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": w.name, "patterns": w.n_patterns, "variant": args.variant},
+            "cpu_baseline": info,
+            "e2e": {"value": evals, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_netlk(args, ws, rank, local):
+    import torch
+    from netrax_gb300 import synth
+    from netrax_gb300.likelihood import NetworkLikelihood
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w = synth.config(2, scale=args.scale)
+    lik = NetworkLikelihood(w.network, w.partitions, variant=args.variant, precision=args.precision,
+                            device=local)
+    st = lik.stats
+    E = lik.n_edges
+    K, W = args.steps, max(3, args.warmup)
+    rng = np.random.default_rng(1000 + rank)
+    base = w.network.branch_lengths
+    host_bl = np.clip(base[None, :] * np.exp(0.05 * rng.standard_normal((K + W, E))), 1e-6, 100.0)
+    dev_bl = torch.from_numpy(host_bl).to(dev)
+    stream = torch.cuda.ExternalStream(lik.stream(), device=dev)
+
+    # ---------------------------------------------------- device-timed loop
+    for k in range(W):
+        lik.set_branch_lengths_device(dev_bl[k].data_ptr())
+        lik.enqueue(True)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    barrier(ws)
+    torch.cuda.synchronize()
+    l0 = lik.launch_count()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for k in range(K):
+        lik.set_branch_lengths_device(dev_bl[W + k].data_ptr())
+        lik.enqueue(True)
+    t1.record(stream)
+    t1.synchronize()
+    torch.cuda.synchronize()
+    barrier(ws)
+    clocks = sampler.stop()
+    launches = lik.launch_count() - l0
+    ms_local = t0.elapsed_time(t1) / K
+    ms = allreduce_max(ms_local, ws, dev)
+    value = ws * 1000.0 / ms
+
+    # ------------------------------------------- end to end through the C ABI
+    K2 = max(3, min(K, 100))
+    lik.set_branch_lengths(host_bl[0])
+    lik.loglikelihood_gradient()
+    barrier(ws)
+    t = time.perf_counter()
+    for k in range(K2):
+        lik.set_branch_lengths(host_bl[W + k % K])
+        lik.loglikelihood_gradient()
+    e2e_s = allreduce_max((time.perf_counter() - t) / K2, ws, dev)
+    h2d = E * 8
+    d2h = (2 + lik.n_parts + lik.n_ret) * 8 + E * 8
+
+    # --------------------------------------------- per-kernel event timings
+    lik.set_profiling(True)
+    for k in range(min(K, 20)):
+        lik.set_branch_lengths_device(dev_bl[W + k].data_ptr())
+        lik.enqueue(True)
+    kt = lik.kernel_times()
+    lik.set_profiling(False)
+    kavg = {k: (v[0] / v[1] if v[1] else 0.0) for k, v in kt.items()}
+
+    # ----------------------------------------------- accuracy vs FP64 plain
+    lik.set_branch_lengths(base)
+    l32, g32, r32 = lik.loglikelihood_gradient()
+    fp64 = None
+    if not args.no_fp64 and args.precision == "fp32":
+        lik64 = NetworkLikelihood(w.network, w.partitions, variant=args.variant, precision="fp64",
+                                  device=local)
+        l64, g64, r64 = lik64.loglikelihood_gradient()
+        s64 = torch.cuda.ExternalStream(lik64.stream(), device=dev)
+        for k in range(3):
+            lik64.set_branch_lengths_device(dev_bl[k].data_ptr())
+            lik64.enqueue(True)
+        torch.cuda.synchronize()
+        Kf = max(3, args.fp64_steps)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s64)
+        for k in range(Kf):
+            lik64.set_branch_lengths_device(dev_bl[W + k % K].data_ptr())
+            lik64.enqueue(True)
+        b.record(s64)
+        b.synchronize()
+        ms64 = a.elapsed_time(b) / Kf
+        lik64.set_profiling(True)
+        lik64.set_branch_lengths_device(dev_bl[W].data_ptr())
+        lik64.enqueue(True)
+        kt64 = lik64.kernel_times()
+        lik64.close()
+        gscale = max(1.0, float(np.abs(g64).max()))
+        fp64 = {"evals_per_s": 1000.0 / ms64, "ms_per_step": ms64,
+                "speedup_fp32_over_fp64": ms64 / ms_local,
+                "rel_dlogl": abs(l32 - l64) / abs(l64),
+                "max_rel_grad_err": float(np.abs(g32 - g64).max() / gscale),
+                "max_abs_retprob_grad_err": float(np.abs(r32 - r64).max()) if len(r64) else 0.0,
+                "kernel_ms": {k: (v[0] / v[1] if v[1] else 0.0) for k, v in kt64.items()}}
+
+    # ------------------------------------------------------------- roofline
+    peak, peak_kind = measured_peak()
+    fwd_b, bwd_b = st["forward_bytes"], st["backward_bytes"]
+    dom = "backward" if kavg["backward"] >= kavg["forward"] else "forward"
+    dom_bytes = bwd_b if dom == "backward" else fwd_b
+    achieved = dom_bytes / (kavg[dom] * 1e-3) / 1e9 if kavg[dom] > 0 else 0.0
+    traffic_tab = load_traffic()
+    traffic = None
+    tt = traffic_tab.get("%s_%s" % (dom, args.precision))
+    if tt:
+        traffic = tt["dram_bytes_per_site_update"] * st["site_clv_updates"]
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "kernel": dom + "_kernel",
+                "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind if peak_kind == "measured"
+                else "fallback 6.8 TB/s",
+                "algorithmic_bytes_per_launch": dom_bytes,
+                "algorithmic_bytes_per_site_update": dom_bytes / st["site_clv_updates"],
+                "forward": {"ms": kavg["forward"], "bytes": fwd_b,
+                            "GBps": fwd_b / (kavg["forward"] * 1e-3) / 1e9 if kavg["forward"] else 0.0},
+                "backward": {"ms": kavg["backward"], "bytes": bwd_b,
+                             "GBps": bwd_b / (kavg["backward"] * 1e-3) / 1e9 if kavg["backward"] else 0.0}}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        _, cpu = cpu_port_rate(w, args.cpu_sample, 3, 1, args.variant)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32" if args.precision == "fp32" else "f64", "data": "synthetic",
+            "config": {"workload": w.name, "taxa": 100, "reticulations": 8, "sites": w.n_sites,
+                       "patterns": w.n_patterns, "partitions": len(w.partitions), "model": "GTR+G4",
+                       "variant": args.variant, "precision": args.precision,
+                       "displayed_trees": lik.n_roots, "dag_variants": st["n_variants"],
+                       "site_clv_updates_per_eval": st["site_clv_updates"],
+                       "l2": "no flush: every eval streams %.1f GB of CLVs, far above the 129 MB L2"
+                             % ((fwd_b + bwd_b) / 1e9),
+                       "parallelism": "replica per GPU" if ws > 1 else "1 GPU", "seed": w.seed},
+            "site_clv_updates_per_s": value * st["site_clv_updates"],
+            "gpu_launches": int(launches),
+            "kernel_ms": kavg,
+            "autotune": lik.tuning(),
+            "e2e": {"value": ws / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": e2e_s * 1000.0},
+            "roofline": roofline,
+            "fp64_plain": fp64,
+            "clocks": clocks,
+            "cpu_baseline": cpu,
+            "logl": l32,
+        }
+        print(json.dumps(line), flush=True)
+    lik.close()
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_init()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_netlk(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

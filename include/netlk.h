@@ -98,6 +98,9 @@ typedef struct {
   int32_t host_only;                 /* 1: build the DAG and schedules only,
                                         touch no device (evaluation calls then
                                         return NETLK_ERR_NO_DEVICE)          */
+  int32_t autotune;                  /* 1: time the launch shapes of the two
+                                        sweeps on the first evaluation and keep
+                                        the fastest (default); 0: default shape */
 } netlk_options;
 
 typedef struct {
@@ -115,6 +118,10 @@ typedef struct {
   int64_t tip_child_uses;    /* child operands that are tips                 */
   int64_t fake_child_uses;   /* unary variants (fake all-ones right child)   */
   int64_t device_bytes;      /* device memory held by the context            */
+  int64_t forward_bytes;     /* algorithmic HBM bytes of one forward sweep:
+                                parent CLV + scaler writes, inner-child CLV +
+                                scaler reads, tip-code reads                  */
+  int64_t backward_bytes;    /* algorithmic HBM bytes of one adjoint sweep   */
 } netlk_dag_stats;
 
 /* --------------------------------------------------------------- lifecycle */
@@ -215,6 +222,34 @@ int netlk_tree_partials(netlk_ctx *ctx, double *tree_partition_logl);
 int netlk_mix_and_backward(netlk_ctx *ctx, const double *global_partials,
                            double *total, double *partition_logl,
                            double *d_brlen_partial, double *d_retprob);
+
+/* ------------------------------------------------ device-resident stepping */
+/* Enqueue an async copy of n_edges branch lengths from DEVICE memory into the
+ * context (no clamping; values must already lie in [1e-6, 100]). */
+int netlk_set_branch_lengths_device(netlk_ctx *ctx, const double *d_branch_lengths,
+                                    int32_t n_edges);
+/* Enqueue one evaluation on the context stream without waiting for it:
+ * with_gradient 0 = logL, 1 = logL + gradient. Results stay on the device
+ * (netlk_result_pointers); synchronise the stream before reading them. */
+int netlk_enqueue(netlk_ctx *ctx, int32_t with_gradient);
+/* Device pointers of the results: out [2 + n_parts + n_reticulations]
+ * (total, status flag, partition logL, d logL / d reticulation probability)
+ * and d_brlen [n_edges]. */
+int netlk_result_pointers(netlk_ctx *ctx, const double **d_out, const double **d_brlen);
+
+/* ----------------------------------------------------------- measurement */
+/* 1: launch without CUDA graphs and time every kernel with CUDA events on the
+ * context stream; 0: off (default). Switching resets the accumulators. */
+int netlk_set_profiling(netlk_ctx *ctx, int32_t enable);
+/* Per-kernel device time (ms, summed) and launch counts since profiling was
+ * enabled, for kernels 0 P-matrices, 1 forward sweep, 2 per-tree site sums,
+ * 3 mixture, 4 adjoint sweep, 5 gradient reduction. n >= 6. */
+int netlk_kernel_times(netlk_ctx *ctx, double *ms, int64_t *launches, int32_t n);
+
+/* Launch shapes the autotuner chose (index into its shape table) and the
+ * time (ms) it measured for each of the first n shapes (0 where untimed). */
+int netlk_tuning(const netlk_ctx *ctx, int32_t *fwd_shape, int32_t *bwd_shape, double *fwd_ms,
+                 double *bwd_ms, int32_t n);
 
 /* ------------------------------------------------------------------- debug */
 /* Copies the CLV (converted to double) and scale counters of one variant:

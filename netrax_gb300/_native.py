@@ -31,7 +31,8 @@ EXPORTED = [
     "netlk_set_branch_lengths", "netlk_set_reticulation_probs", "netlk_set_model",
     "netlk_loglikelihood", "netlk_loglikelihood_gradient", "netlk_edge_derivatives",
     "netlk_tree_partials", "netlk_mix_and_backward", "netlk_get_clv", "netlk_get_stream",
-    "netlk_launch_count",
+    "netlk_launch_count", "netlk_set_branch_lengths_device", "netlk_enqueue",
+    "netlk_result_pointers", "netlk_set_profiling", "netlk_kernel_times", "netlk_tuning",
 ]
 
 
@@ -56,7 +57,7 @@ class Options(ctypes.Structure):
     _fields_ = [("variant", ctypes.c_int32), ("precision", ctypes.c_int32),
                 ("min_interesting_tree_logprob", ctypes.c_double),
                 ("device", ctypes.c_int32), ("use_cuda_graph", ctypes.c_int32),
-                ("host_only", ctypes.c_int32)]
+                ("host_only", ctypes.c_int32), ("autotune", ctypes.c_int32)]
 
 
 class DagStats(ctypes.Structure):
@@ -66,7 +67,8 @@ class DagStats(ctypes.Structure):
                 ("max_variants_per_node", ctypes.c_int32), ("n_degenerate", ctypes.c_int32),
                 ("n_patterns_total", ctypes.c_int64), ("site_clv_updates", ctypes.c_int64),
                 ("tip_child_uses", ctypes.c_int64), ("fake_child_uses", ctypes.c_int64),
-                ("device_bytes", ctypes.c_int64)]
+                ("device_bytes", ctypes.c_int64), ("forward_bytes", ctypes.c_int64),
+                ("backward_bytes", ctypes.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -113,6 +115,12 @@ def lib():
     L.netlk_get_clv.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, c_double_p, c_int32_p]
     L.netlk_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
     L.netlk_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_int64)]
+    L.netlk_set_branch_lengths_device.argtypes = [vp, ctypes.c_void_p, ctypes.c_int32]
+    L.netlk_enqueue.argtypes = [vp, ctypes.c_int32]
+    L.netlk_result_pointers.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp)]
+    L.netlk_set_profiling.argtypes = [vp, ctypes.c_int32]
+    L.netlk_tuning.argtypes = [vp, c_int32_p, c_int32_p, c_double_p, c_double_p, ctypes.c_int32]
+    L.netlk_kernel_times.argtypes = [vp, c_double_p, ctypes.POINTER(ctypes.c_int64), ctypes.c_int32]
     for name in EXPORTED:
         f = getattr(L, name)
         if f.restype is ctypes.c_int or f.restype is None:

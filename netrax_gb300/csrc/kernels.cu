@@ -106,45 +106,68 @@ struct Scale<double> {
   static __device__ __forceinline__ double shift(double x, int k) { return ldexp(x, 256 * k); }
 };
 
+// Loads one child operand for the lane's kPPL patterns: a variant CLV (with
+// its scale counters), a tip (state mask expanded to 0/1) or the fake all-ones
+// child. g0: the lane's first pattern, r: its rate; `stride` patterns
+// separate the lane's patterns.
 template <typename real, int R>
-__device__ __forceinline__ void load_child(const SweepParams &p, int32_t ref, size_t g, int r,
-                                           real (&c)[4], int &s) {
+__device__ __forceinline__ void load_child(const SweepParams &p, int32_t ref, size_t g0, int r, int stride,
+                                           real (&c)[kPPL][4], int (&s)[kPPL]) {
   if (ref >= 0) {
-    const real *clv = static_cast<const real *>(p.clv);
-    Vec<real>::load(clv + ((size_t)ref * p.n_patterns + g) * (R * 4) + r * 4, c);
-    s = p.scaler[(size_t)ref * p.n_patterns + g];
-  } else if (ref != INT32_MIN) {
-    const unsigned code = p.tips[(size_t)(-1 - ref) * p.n_patterns + g];
+    const real *clv = static_cast<const real *>(p.clv) + ((size_t)ref * p.n_patterns + g0) * (R * 4) + r * 4;
+    const int32_t *sc = p.scaler + (size_t)ref * p.n_patterns + g0;
 #pragma unroll
-    for (int i = 0; i < 4; ++i) c[i] = (real)((code >> i) & 1u);
-    s = 0;
+    for (int k = 0; k < kPPL; ++k) {
+      Vec<real>::load(clv + (size_t)k * stride * (R * 4), c[k]);
+      s[k] = sc[(size_t)k * stride];
+    }
+  } else if (ref != INT32_MIN) {
+    const uint8_t *t = p.tips + (size_t)(-1 - ref) * p.n_patterns + g0;
+#pragma unroll
+    for (int k = 0; k < kPPL; ++k) {
+      const unsigned code = t[(size_t)k * stride];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) c[k][i] = (real)((code >> i) & 1u);
+      s[k] = 0;
+    }
   } else {
 #pragma unroll
-    for (int i = 0; i < 4; ++i) c[i] = (real)1;
-    s = 0;
+    for (int k = 0; k < kPPL; ++k) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) c[k][i] = (real)1;
+      s[k] = 0;
+    }
   }
 }
 
+// out[k] = P . c[k] for the lane's patterns (P: this lane's rate, row-major 4x4)
 template <typename real>
-__device__ __forceinline__ void matvec(const real *P, const real (&c)[4], real (&out)[4]) {
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    real row[4];
-    Vec<real>::ldg(P + 4 * i, row);
-    out[i] = row[0] * c[0] + row[1] * c[1] + row[2] * c[2] + row[3] * c[3];
-  }
-}
-
-template <typename real>
-__device__ __forceinline__ void matvec_t(const real *P, const real (&u)[4], real (&out)[4]) {
-#pragma unroll
-  for (int j = 0; j < 4; ++j) out[j] = 0;
+__device__ __forceinline__ void matvec2(const real *P, const real (&c)[kPPL][4], real (&out)[kPPL][4]) {
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     real row[4];
     Vec<real>::ldg(P + 4 * i, row);
 #pragma unroll
-    for (int j = 0; j < 4; ++j) out[j] += row[j] * u[i];
+    for (int k = 0; k < kPPL; ++k)
+      out[k][i] = row[0] * c[k][0] + row[1] * c[k][1] + row[2] * c[k][2] + row[3] * c[k][3];
+  }
+}
+
+// out[k] = P^T . u[k]
+template <typename real>
+__device__ __forceinline__ void matvec2_t(const real *P, const real (&u)[kPPL][4], real (&out)[kPPL][4]) {
+#pragma unroll
+  for (int k = 0; k < kPPL; ++k)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) out[k][j] = 0;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    real row[4];
+    Vec<real>::ldg(P + 4 * i, row);
+#pragma unroll
+    for (int k = 0; k < kPPL; ++k)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) out[k][j] += row[j] * u[k][i];
   }
 }
 
@@ -169,63 +192,99 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
+__device__ __forceinline__ FwdOp load_fwd_op(const FwdOp *ops, int i) {
+  const int4 *q = reinterpret_cast<const int4 *>(ops + i);
+  const int4 a = __ldg(q), b = __ldg(q + 1);
+  FwdOp o;
+  o.out = a.x; o.a = a.y; o.b = a.z; o.ea = a.w;
+  o.eb = b.x; o.slot = b.y; o.pad0 = b.z; o.pad1 = b.w;
+  return o;
+}
+
+__device__ __forceinline__ BwdOp load_bwd_op(const BwdOp *ops, int i) {
+  const int4 *q = reinterpret_cast<const int4 *>(ops + i);
+  const int4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
+  BwdOp o;
+  o.x = a.x; o.a = a.y; o.b = a.z; o.ea = a.w;
+  o.eb = b.x; o.seed = b.y; o.out_a = b.z; o.out_b = b.w;
+  o.msg_begin = c.x; o.msg_count = c.y; o.pad0 = o.pad1 = o.pad2 = o.pad3 = o.pad4 = o.pad5 = 0;
+  return o;
+}
+
 // ------------------------------------------------------------------ forward
-template <typename real, int R>
-__global__ void __launch_bounds__(kThreads) forward_kernel(const SweepParams p) {
-  constexpr int PPW = 32 / R;
+// CLV_out = (P[ea] . a) * (P[eb] . b), rescaled per site; site log-likelihoods
+// of displayed-tree root variants are summed over the warp's patterns.
+template <typename real, int R, int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) forward_kernel(const SweepParams p) {
+  constexpr int PPW = 32 / R;          // patterns per pass of the lane rows
+  constexpr int UNIT = PPW * kPPL;     // patterns per unit
   const int lane = threadIdx.x & 31;
   const int r = lane % R;
   const int pl = lane / R;
-  const int warps_total = gridDim.x * (kThreads / 32);
-  const int warp_id = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5);
+  const int warps_total = gridDim.x * (THREADS / 32);
+  const int warp_id = blockIdx.x * (THREADS / 32) + (threadIdx.x >> 5);
   const real *pmat = static_cast<const real *>(p.pmat);
   real *clv = static_cast<real *>(p.clv);
   const size_t N = (size_t)p.n_patterns;
 
   for (int unit = warp_id; unit < p.n_units; unit += warps_total) {
     const int part = p.unit_part[unit];
-    const size_t g = (size_t)unit * PPW + pl;
+    const size_t g0 = (size_t)unit * UNIT + pl;  // first pattern of the lane; second is g0 + PPW
     const real *pm = pmat + (size_t)part * p.n_edges * (R * 16) + r * 16;
-    const double wgt = p.weights[g];
+    double wgt[kPPL];
+#pragma unroll
+    for (int k = 0; k < kPPL; ++k) wgt[k] = p.weights[g0 + (size_t)k * PPW];
     real freq[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) freq[i] = (real)p.freqs[part * 4 + i];
     const real rw = (real)p.rate_weights[part * R + r];
 
-    for (int o0 = 0; o0 < p.n_fwd_ops; o0 += kGroup) {
-      FwdOp op[kGroup];
-      real ca[kGroup][4], cb[kGroup][4];
-      int sa[kGroup], sb[kGroup];
+    for (int o0 = 0; o0 < p.n_fwd_ops; o0 += kFwdGroup) {
+      FwdOp op[kFwdGroup];
+      real ca[kFwdGroup][kPPL][4], cb[kFwdGroup][kPPL][4];
+      int sa[kFwdGroup][kPPL], sb[kFwdGroup][kPPL];
 #pragma unroll
-      for (int j = 0; j < kGroup; ++j) {
-        op[j] = p.fwd_ops[o0 + j];
+      for (int j = 0; j < kFwdGroup; ++j) {
+        op[j] = load_fwd_op(p.fwd_ops, o0 + j);
         if (op[j].out < 0) continue;
-        load_child<real, R>(p, op[j].a, g, r, ca[j], sa[j]);
-        load_child<real, R>(p, op[j].b, g, r, cb[j], sb[j]);
+        load_child<real, R>(p, op[j].a, g0, r, PPW, ca[j], sa[j]);
+        load_child<real, R>(p, op[j].b, g0, r, PPW, cb[j], sb[j]);
       }
 #pragma unroll
-      for (int j = 0; j < kGroup; ++j) {
+      for (int j = 0; j < kFwdGroup; ++j) {
         if (op[j].out < 0) continue;
-        real v[4], pb[4];
-        matvec<real>(pm + (size_t)op[j].ea * (R * 16), ca[j], v);
+        real v[kPPL][4];
+        matvec2<real>(pm + (size_t)op[j].ea * (R * 16), ca[j], v);
         if (op[j].b != INT32_MIN) {
-          matvec<real>(pm + (size_t)op[j].eb * (R * 16), cb[j], pb);
+          real pb[kPPL][4];
+          matvec2<real>(pm + (size_t)op[j].eb * (R * 16), cb[j], pb);
 #pragma unroll
-          for (int i = 0; i < 4; ++i) v[i] *= pb[i];
+          for (int k = 0; k < kPPL; ++k)
+#pragma unroll
+            for (int i = 0; i < 4; ++i) v[k][i] *= pb[k][i];
         }
-        real m = max(max(v[0], v[1]), max(v[2], v[3]));
-        m = rate_max<R>(m);
-        const int s = sa[j] + sb[j] + Scale<real>::rescale(m, v);
-        Vec<real>::store(clv + ((size_t)op[j].out * N + g) * (R * 4) + r * 4, v);
-        if (r == 0) p.scaler[(size_t)op[j].out * N + g] = s;
+        real *dst = clv + ((size_t)op[j].out * N + g0) * (R * 4) + r * 4;
+        int32_t *sdst = p.scaler + (size_t)op[j].out * N + g0;
+        int s[kPPL];
+#pragma unroll
+        for (int k = 0; k < kPPL; ++k) {
+          real m = max(max(v[k][0], v[k][1]), max(v[k][2], v[k][3]));
+          m = rate_max<R>(m);
+          s[k] = sa[j][k] + sb[j][k] + Scale<real>::rescale(m, v[k]);
+          Vec<real>::store(dst + (size_t)k * PPW * (R * 4), v[k]);
+          if (r == 0) sdst[(size_t)k * PPW] = s[k];
+        }
         if (op[j].slot >= 0) {
-          // pll_compute_root_loglikelihood for this site, summed over the warp.
-          real t = rw * (freq[0] * v[0] + freq[1] * v[1] + freq[2] * v[2] + freq[3] * v[3]);
-          t = rate_sum<R>(t);
+          // pll_compute_root_loglikelihood for the lane's sites, summed over the warp
           double ll = 0.0;
-          if (r == 0 && wgt != 0.0) {
-            double lt = (sizeof(real) == 4) ? (double)logf((float)t) : log((double)t);
-            ll = wgt * (lt + (double)s * Scale<real>::kLogUnit);
+#pragma unroll
+          for (int k = 0; k < kPPL; ++k) {
+            real t = rw * (freq[0] * v[k][0] + freq[1] * v[k][1] + freq[2] * v[k][2] + freq[3] * v[k][3]);
+            t = rate_sum<R>(t);
+            if (r == 0 && wgt[k] != 0.0) {
+              const double lt = (sizeof(real) == 4) ? (double)logf((float)t) : log((double)t);
+              ll += wgt[k] * (lt + (double)s[k] * Scale<real>::kLogUnit);
+            }
           }
           ll = warp_sum(ll);
           if (lane == 0) p.site_partial[(size_t)op[j].slot * p.n_units + unit] = ll;
@@ -236,19 +295,25 @@ __global__ void __launch_bounds__(kThreads) forward_kernel(const SweepParams p) 
 }
 
 // ------------------------------------------------------------------ adjoint
-template <typename real, int R>
-__global__ void __launch_bounds__(kThreads) backward_kernel(const SweepParams p) {
+// Reverse sweep as message passing. For op x with CLV_x = 2^k (Pa a) * (Pb b):
+//   adj_x   = sum of incoming messages (+ seed: tree weight * w_s rw_r pi_i / L_s)
+//   u_a     = 2^k adj_x * (Pb b),  u_b = 2^k adj_x * (Pa a)
+//   dlogL/dt_ea += sum u_a . (r Q Pa a),  dlogL/dt_eb += sum u_b . (r Q Pb b)
+//   message to a = Pa^T u_a, message to b = Pb^T u_b
+template <typename real, int R, int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) backward_kernel(const SweepParams p) {
   extern __shared__ double sgrad[];
   constexpr int PPW = 32 / R;
+  constexpr int UNIT = PPW * kPPL;
   const int lane = threadIdx.x & 31;
   const int r = lane % R;
   const int pl = lane / R;
   const int wib = threadIdx.x >> 5;
-  const int warps_total = gridDim.x * (kThreads / 32);
-  const int warp_id = blockIdx.x * (kThreads / 32) + wib;
+  const int warps_total = gridDim.x * (THREADS / 32);
+  const int warp_id = blockIdx.x * (THREADS / 32) + wib;
   const real *pmat = static_cast<const real *>(p.pmat);
   const real *clv = static_cast<const real *>(p.clv);
-  real *adj = static_cast<real *>(p.adj);
+  real *msg = static_cast<real *>(p.msg);
   const size_t N = (size_t)p.n_patterns;
   double *my = sgrad + (size_t)wib * p.n_edges;
   for (int e = lane; e < p.n_edges; e += 32) my[e] = 0.0;
@@ -256,9 +321,12 @@ __global__ void __launch_bounds__(kThreads) backward_kernel(const SweepParams p)
 
   for (int unit = warp_id; unit < p.n_units; unit += warps_total) {
     const int part = p.unit_part[unit];
-    const size_t g = (size_t)unit * PPW + pl;
+    const size_t g0 = (size_t)unit * UNIT + pl;
+    const size_t lane_off = g0 * (R * 4) + r * 4;
     const real *pm = pmat + (size_t)part * p.n_edges * (R * 16) + r * 16;
-    const real wgt = (real)p.weights[g];
+    real wgt[kPPL];
+#pragma unroll
+    for (int k = 0; k < kPPL; ++k) wgt[k] = (real)p.weights[g0 + (size_t)k * PPW];
     real freq[4], Q[16];
 #pragma unroll
     for (int i = 0; i < 4; ++i) freq[i] = (real)p.freqs[part * 4 + i];
@@ -267,74 +335,95 @@ __global__ void __launch_bounds__(kThreads) backward_kernel(const SweepParams p)
     const real rw = (real)p.rate_weights[part * R + r];
     const real rate = (real)p.rates[part * R + r];
 
-    for (int o0 = 0; o0 < p.n_bwd_ops; o0 += kGroup) {
-      BwdOp op[kGroup];
-      real ax[kGroup][4], ca[kGroup][4], cb[kGroup][4], cx[kGroup][4];
-      int sx[kGroup], sa[kGroup], sb[kGroup];
+    for (int o0 = 0; o0 < p.n_bwd_ops; o0 += kBwdGroup) {
+      BwdOp op[kBwdGroup];
+      real ax[kBwdGroup][kPPL][4], ca[kBwdGroup][kPPL][4], cb[kBwdGroup][kPPL][4];
+      int sx[kBwdGroup][kPPL], sa[kBwdGroup][kPPL], sb[kBwdGroup][kPPL];
 #pragma unroll
-      for (int j = 0; j < kGroup; ++j) {
-        op[j] = p.bwd_ops[o0 + j];
+      for (int j = 0; j < kBwdGroup; ++j) {
+        op[j] = load_bwd_op(p.bwd_ops, o0 + j);
         if (op[j].x < 0) continue;
-        if (op[j].adj_x >= 0) {
-          Vec<real>::load(adj + ((size_t)op[j].adj_x * N + g) * (R * 4) + r * 4, ax[j]);
-        } else {
+        load_child<real, R>(p, op[j].a, g0, r, PPW, ca[j], sa[j]);
+        load_child<real, R>(p, op[j].b, g0, r, PPW, cb[j], sb[j]);
+        const int32_t *sxp = p.scaler + (size_t)op[j].x * N + g0;
 #pragma unroll
-          for (int i = 0; i < 4; ++i) ax[j][i] = 0;
+        for (int k = 0; k < kPPL; ++k) {
+          sx[j][k] = sxp[(size_t)k * PPW];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) ax[j][k][i] = 0;
         }
-        if (op[j].seed >= 0)
-          Vec<real>::load(clv + ((size_t)op[j].x * N + g) * (R * 4) + r * 4, cx[j]);
-        sx[j] = p.scaler[(size_t)op[j].x * N + g];
-        load_child<real, R>(p, op[j].a, g, r, ca[j], sa[j]);
-        load_child<real, R>(p, op[j].b, g, r, cb[j], sb[j]);
+        for (int m = 0; m < op[j].msg_count; ++m) {
+          const real *src = msg + (size_t)__ldg(p.msg_slots + op[j].msg_begin + m) * N * (R * 4) + lane_off;
+#pragma unroll
+          for (int k = 0; k < kPPL; ++k) {
+            real t[4];
+            Vec<real>::load(src + (size_t)k * PPW * (R * 4), t);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) ax[j][k][i] += t[i];
+          }
+        }
+        if (op[j].seed >= 0) {
+          // d(w_s log L_s)/d clv_x = w_s rw_r pi_i / L_s, times the tree weight
+          const real sd = (real)p.seeds[(size_t)op[j].seed * p.n_parts + part];
+          const real *cxp = clv + (size_t)op[j].x * N * (R * 4) + lane_off;
+#pragma unroll
+          for (int k = 0; k < kPPL; ++k) {
+            real cx[4];
+            Vec<real>::load(cxp + (size_t)k * PPW * (R * 4), cx);
+            real t = rw * (freq[0] * cx[0] + freq[1] * cx[1] + freq[2] * cx[2] + freq[3] * cx[3]);
+            t = rate_sum<R>(t);
+            const real s = sd * wgt[k];
+            if (t > (real)0 && s != (real)0) {
+              const real f = s * rw / t;
+#pragma unroll
+              for (int i = 0; i < 4; ++i) ax[j][k][i] += f * freq[i];
+            }
+          }
+        }
       }
 #pragma unroll
-      for (int j = 0; j < kGroup; ++j) {
+      for (int j = 0; j < kBwdGroup; ++j) {
         if (op[j].x < 0) continue;
-        if (op[j].seed >= 0) {
-          // d(w_s log L_s)/d clv = w_s * rw_r * pi_i / L_s, times the tree weight.
-          real t = rw * (freq[0] * cx[j][0] + freq[1] * cx[j][1] + freq[2] * cx[j][2] + freq[3] * cx[j][3]);
-          t = rate_sum<R>(t);
-          const real sd = (real)p.seeds[(size_t)op[j].seed * p.n_parts + part] * wgt;
-          if (t > (real)0 && sd != (real)0) {
-            const real f = sd * rw / t;
-#pragma unroll
-            for (int i = 0; i < 4; ++i) ax[j][i] += f * freq[i];
-          }
-        }
         const bool fake = op[j].b == INT32_MIN;
         const real *Pa = pm + (size_t)op[j].ea * (R * 16);
-        real pa[4], pb[4];
-        matvec<real>(Pa, ca[j], pa);
+        real pa[kPPL][4], pb[kPPL][4];
+        matvec2<real>(Pa, ca[j], pa);
         if (!fake) {
-          matvec<real>(pm + (size_t)op[j].eb * (R * 16), cb[j], pb);
+          matvec2<real>(pm + (size_t)op[j].eb * (R * 16), cb[j], pb);
         } else {
 #pragma unroll
-          for (int i = 0; i < 4; ++i) pb[i] = 1;
-        }
-        // CLV_x = 2^k (Pa a) * (Pb b) with k the shift applied at x for this site
-        const int k = sx[j] - sa[j] - sb[j];
-        real ua[4], ub[4];
+          for (int k = 0; k < kPPL; ++k)
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          ua[i] = ax[j][i] * pb[i];
-          ub[i] = ax[j][i] * pa[i];
+            for (int i = 0; i < 4; ++i) pb[k][i] = 1;
         }
-        if (k != 0) {
-#pragma unroll
-          for (int i = 0; i < 4; ++i) {
-            ua[i] = Scale<real>::shift(ua[i], k);
-            ub[i] = Scale<real>::shift(ub[i], k);
-          }
-        }
-        // d/dt of P(t r) c = r Q P(t r) c
+        real ua[kPPL][4], ub[kPPL][4];
         real ga = 0, gb = 0;
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const real qa = Q[4 * i] * pa[0] + Q[4 * i + 1] * pa[1] + Q[4 * i + 2] * pa[2] + Q[4 * i + 3] * pa[3];
-          ga += ua[i] * qa;
-          if (!fake) {
-            const real qb = Q[4 * i] * pb[0] + Q[4 * i + 1] * pb[1] + Q[4 * i + 2] * pb[2] + Q[4 * i + 3] * pb[3];
-            gb += ub[i] * qb;
+        for (int k = 0; k < kPPL; ++k) {
+          const int sh = sx[j][k] - sa[j][k] - sb[j][k];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            ua[k][i] = ax[j][k][i] * pb[k][i];
+            ub[k][i] = ax[j][k][i] * pa[k][i];
+          }
+          if (sh != 0) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+              ua[k][i] = Scale<real>::shift(ua[k][i], sh);
+              ub[k][i] = Scale<real>::shift(ub[k][i], sh);
+            }
+          }
+          // d/dt of P(t r) c = r Q P(t r) c
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const real qa = Q[4 * i] * pa[k][0] + Q[4 * i + 1] * pa[k][1] + Q[4 * i + 2] * pa[k][2] +
+                            Q[4 * i + 3] * pa[k][3];
+            ga += ua[k][i] * qa;
+            if (!fake) {
+              const real qb = Q[4 * i] * pb[k][0] + Q[4 * i + 1] * pb[k][1] + Q[4 * i + 2] * pb[k][2] +
+                              Q[4 * i + 3] * pb[k][3];
+              gb += ub[k][i] * qb;
+            }
           }
         }
         ga = warp_sum(ga * rate);
@@ -343,30 +432,19 @@ __global__ void __launch_bounds__(kThreads) backward_kernel(const SweepParams p)
           gb = warp_sum(gb * rate);
           if (lane == 0) my[op[j].eb] += (double)gb;
         }
-        const int mode_a = op[j].modes & 0xff, mode_b = (op[j].modes >> 8) & 0xff;
-        if (mode_a) {
-          real na[4];
-          matvec_t<real>(Pa, ua, na);
-          real *dst = adj + ((size_t)op[j].adj_a * N + g) * (R * 4) + r * 4;
-          if (mode_a == 2) {
-            real old[4];
-            Vec<real>::load(dst, old);
+        if (op[j].out_a >= 0) {
+          real na[kPPL][4];
+          matvec2_t<real>(Pa, ua, na);
+          real *dst = msg + (size_t)op[j].out_a * N * (R * 4) + lane_off;
 #pragma unroll
-            for (int i = 0; i < 4; ++i) na[i] += old[i];
-          }
-          Vec<real>::store(dst, na);
+          for (int k = 0; k < kPPL; ++k) Vec<real>::store(dst + (size_t)k * PPW * (R * 4), na[k]);
         }
-        if (mode_b) {
-          real nb[4];
-          matvec_t<real>(pm + (size_t)op[j].eb * (R * 16), ub, nb);
-          real *dst = adj + ((size_t)op[j].adj_b * N + g) * (R * 4) + r * 4;
-          if (mode_b == 2) {
-            real old[4];
-            Vec<real>::load(dst, old);
+        if (op[j].out_b >= 0) {
+          real nb[kPPL][4];
+          matvec2_t<real>(pm + (size_t)op[j].eb * (R * 16), ub, nb);
+          real *dst = msg + (size_t)op[j].out_b * N * (R * 4) + lane_off;
 #pragma unroll
-            for (int i = 0; i < 4; ++i) nb[i] += old[i];
-          }
-          Vec<real>::store(dst, nb);
+          for (int k = 0; k < kPPL; ++k) Vec<real>::store(dst + (size_t)k * PPW * (R * 4), nb[k]);
         }
       }
     }
@@ -374,7 +452,7 @@ __global__ void __launch_bounds__(kThreads) backward_kernel(const SweepParams p)
   __syncthreads();
   for (int e = threadIdx.x; e < p.n_edges; e += blockDim.x) {
     double s = 0.0;
-    for (int w = 0; w < kThreads / 32; ++w) s += sgrad[(size_t)w * p.n_edges + e];
+    for (int w = 0; w < THREADS / 32; ++w) s += sgrad[(size_t)w * p.n_edges + e];
     p.grad_partial[(size_t)blockIdx.x * p.n_edges + e] = s;
   }
 }
@@ -530,77 +608,99 @@ __global__ void grad_reduce_kernel(int n_blocks, int n_edges, const double *part
   grad[e] = s;
 }
 
-template <typename real, int R>
-void fwd_launch(cudaStream_t s, int grid, const SweepParams &p) {
-  forward_kernel<real, R><<<grid, kThreads, 0, s>>>(p);
-}
+// Launch shapes (threads per block, minimum resident blocks per SM) the
+// autotuner chooses from. Shape 0 is the default and exists for every
+// precision and rate count; the FP32 4-rate path (DNA GTR+G4) carries all.
+struct Shape {
+  int threads, minb;
+};
+constexpr Shape kShapes[] = {{128, 2}, {128, 3}, {128, 4}, {256, 1}, {64, 6}};
+constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
 
-template <typename real, int R>
-void bwd_launch(cudaStream_t s, int grid, const SweepParams &p) {
-  const size_t smem = (size_t)(kThreads / 32) * p.n_edges * sizeof(double);
+template <typename real, int R, int T, int M>
+size_t bwd_smem(int n_edges) {
+  const size_t smem = (size_t)(T / 32) * n_edges * sizeof(double);
   if (smem > 48 * 1024)
-    cudaFuncSetAttribute(backward_kernel<real, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  backward_kernel<real, R><<<grid, kThreads, smem, s>>>(p);
+    cudaFuncSetAttribute(backward_kernel<real, R, T, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  return smem;
 }
 
-template <typename real, int R>
-int occupancy(bool backward, int n_edges_hint) {
-  int nb = 0;
-  if (backward)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, backward_kernel<real, R>, kThreads,
-                                                  (size_t)(kThreads / 32) * n_edges_hint * sizeof(double));
-  else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, forward_kernel<real, R>, kThreads, 0);
-  return nb;
+template <typename real, int R, int T, int M>
+struct FwdRun {
+  static int run(cudaStream_t s, int grid, const SweepParams &p) {
+    forward_kernel<real, R, T, M><<<grid, T, 0, s>>>(p);
+    return 0;
+  }
+};
+template <typename real, int R, int T, int M>
+struct BwdRun {
+  static int run(cudaStream_t s, int grid, const SweepParams &p) {
+    backward_kernel<real, R, T, M><<<grid, T, bwd_smem<real, R, T, M>(p.n_edges), s>>>(p);
+    return 0;
+  }
+};
+template <typename real, int R, int T, int M>
+struct OccRun {
+  static int run(bool backward, int n_edges) {
+    int nb = 0;
+    if (backward)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, backward_kernel<real, R, T, M>, T,
+                                                    bwd_smem<real, R, T, M>(n_edges));
+    else
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, forward_kernel<real, R, T, M>, T, 0);
+    return nb;
+  }
+};
+template <typename real, int R, int T, int M>
+struct ThreadsRun {
+  static int run() { return T; }
+};
+
+// Calls F<real, R, threads, minb>::run for a runtime (precision, R, shape).
+template <template <typename, int, int, int> class F, class... A>
+int dispatch(int precision, int R, int shape, A &&...a) {
+  if (precision == 1 && R == 4) {
+    switch (shape) {
+      case 1: return F<float, 4, 128, 3>::run(a...);
+      case 2: return F<float, 4, 128, 4>::run(a...);
+      case 3: return F<float, 4, 256, 1>::run(a...);
+      case 4: return F<float, 4, 64, 6>::run(a...);
+      default: return F<float, 4, 128, 2>::run(a...);
+    }
+  }
+  if (precision == 1) {
+    switch (R) {
+      case 1: return F<float, 1, 128, 2>::run(a...);
+      case 2: return F<float, 2, 128, 2>::run(a...);
+      default: return F<float, 8, 128, 2>::run(a...);
+    }
+  }
+  switch (R) {
+    case 1: return F<double, 1, 128, 2>::run(a...);
+    case 2: return F<double, 2, 128, 2>::run(a...);
+    case 4: return F<double, 4, 128, 2>::run(a...);
+    default: return F<double, 8, 128, 2>::run(a...);
+  }
 }
 
 }  // namespace
 
-#define NETLK_DISPATCH_R(R, FN, ...)             \
-  switch (R) {                                   \
-    case 1: FN<real, 1>(__VA_ARGS__); break;     \
-    case 2: FN<real, 2>(__VA_ARGS__); break;     \
-    case 4: FN<real, 4>(__VA_ARGS__); break;     \
-    case 8: FN<real, 8>(__VA_ARGS__); break;     \
-  }
+int num_shapes(int precision, int R) { return (precision == 1 && R == 4) ? kNumShapes : 1; }
 
-void launch_forward(cudaStream_t s, int precision, int R, int grid, const SweepParams &p) {
-  if (precision == 1) {
-    using real = float;
-    NETLK_DISPATCH_R(R, fwd_launch, s, grid, p);
-  } else {
-    using real = double;
-    NETLK_DISPATCH_R(R, fwd_launch, s, grid, p);
-  }
+int shape_threads(int precision, int R, int shape) { return dispatch<ThreadsRun>(precision, R, shape); }
+
+void launch_forward(cudaStream_t s, int precision, int R, int shape, int grid, const SweepParams &p) {
+  dispatch<FwdRun>(precision, R, shape, s, grid, p);
   g_launches++;
 }
 
-void launch_backward(cudaStream_t s, int precision, int R, int grid, const SweepParams &p) {
-  if (precision == 1) {
-    using real = float;
-    NETLK_DISPATCH_R(R, bwd_launch, s, grid, p);
-  } else {
-    using real = double;
-    NETLK_DISPATCH_R(R, bwd_launch, s, grid, p);
-  }
+void launch_backward(cudaStream_t s, int precision, int R, int shape, int grid, const SweepParams &p) {
+  dispatch<BwdRun>(precision, R, shape, s, grid, p);
   g_launches++;
 }
 
-int max_resident_blocks(int precision, int R, bool backward, int n_edges_hint) {
-  int nb = 0;
-#define NETLK_OCC(real)                                       \
-  switch (R) {                                                \
-    case 1: nb = occupancy<real, 1>(backward, n_edges_hint); break; \
-    case 2: nb = occupancy<real, 2>(backward, n_edges_hint); break; \
-    case 4: nb = occupancy<real, 4>(backward, n_edges_hint); break; \
-    case 8: nb = occupancy<real, 8>(backward, n_edges_hint); break; \
-  }
-  if (precision == 1) {
-    NETLK_OCC(float)
-  } else {
-    NETLK_OCC(double)
-  }
-#undef NETLK_OCC
+int max_resident_blocks(int precision, int R, int shape, bool backward, int n_edges) {
+  const int nb = dispatch<OccRun>(precision, R, shape, backward, n_edges);
   return nb < 1 ? 1 : nb;
 }
 

@@ -6,9 +6,17 @@
 
 namespace netlk {
 
-// Ops per unrolled group: the host pads every level of both schedules to a
-// multiple of this, with no-op entries (out / x == -1).
-constexpr int kGroup = 4;
+// Ops per unrolled group of the forward / adjoint sweeps: the host pads every
+// level of each schedule to a multiple of its group size with no-op entries
+// (out / x == -1). All loads of a group are issued before any of its results
+// is computed, so the host never puts an op and its consumer in one group.
+constexpr int kFwdGroup = 4;
+constexpr int kBwdGroup = 2;
+// Patterns per lane: a lane handles rate r of patterns s and s + 32/R of its
+// unit, so one P-row load and one op decode serve two patterns.
+constexpr int kPPL = 2;
+// Partitions are padded to whole multiples of this many patterns.
+constexpr int kPatternAlign = 64;
 constexpr int kThreads = 256;
 
 // Forward op: CLV of variant `out` = (P[ea] . child a) (*) (P[eb] . child b).
@@ -19,13 +27,15 @@ struct alignas(32) FwdOp {
   int32_t out, a, b, ea, eb, slot, pad0, pad1;
 };
 
-// Adjoint op for variant x (reverse level order).
-// adj_x: adjoint slot holding contributions from x's parents, or -1 (none).
-// seed: dtroot slot whose tree weights seed x, or -1.
-// adj_a / adj_b: adjoint slot of the child, mode 0 none, 1 store, 2 accumulate.
-struct alignas(32) BwdOp {
-  int32_t x, a, b, ea, eb, adj_x, seed, modes;  // modes = mode_a | mode_b << 8
-  int32_t adj_a, adj_b, pad0, pad1, pad2, pad3, pad4, pad5;
+// Adjoint op for variant x (reverse level order), as message passing: the
+// adjoint of x is the sum of the messages its parents wrote for it
+// (msg_slots[msg_begin .. msg_begin + msg_count)); x then writes one message
+// per inner child (out_a / out_b: message slot, or -1) and adds its two edge
+// gradient terms. seed: displayed-tree root slot whose tree weight seeds x,
+// or -1. Message buffers are reused once their reader has run.
+struct alignas(64) BwdOp {
+  int32_t x, a, b, ea, eb, seed, out_a, out_b;
+  int32_t msg_begin, msg_count, pad0, pad1, pad2, pad3, pad4, pad5;
 };
 
 struct DevPartition {
@@ -34,7 +44,7 @@ struct DevPartition {
 
 // Everything the sweeps read, in device memory.
 struct SweepParams {
-  int32_t n_units;      // pattern groups of 32/R patterns
+  int32_t n_units;      // pattern groups of kPPL*32/R patterns (one per warp pass)
   int64_t n_patterns;   // padded total (N)
   int32_t n_edges;
   int32_t n_fwd_ops;
@@ -52,7 +62,8 @@ struct SweepParams {
   const double *Q;              // [n_parts][16]
   void *clv;                    // [V][N][R][4] real
   int32_t *scaler;              // [V][N]
-  void *adj;                    // [A][N][R][4] real
+  void *msg;                    // [M][N][R][4] real adjoint messages
+  const int32_t *msg_slots;     // message slots read by the adjoint ops
   double *site_partial;         // [n_slots][n_units]
   const double *seeds;          // [n_slots][n_parts]
   double *grad_partial;         // [gridDim][n_edges]
@@ -77,12 +88,16 @@ struct MixParams {
 void launch_pmatrix(cudaStream_t s, int n_parts, int n_edges, int R, const double *lambda,
                     const double *U, const double *Uinv, const double *rates, const double *brlen,
                     double *pmat64, float *pmat32);
-void launch_forward(cudaStream_t s, int precision, int R, int grid, const SweepParams &p);
-void launch_backward(cudaStream_t s, int precision, int R, int grid, const SweepParams &p);
+// Sweep launch shapes (threads per block, minimum blocks per SM): shape 0 is
+// the default; num_shapes() > 1 where the autotuner has alternatives.
+int num_shapes(int precision, int R);
+int shape_threads(int precision, int R, int shape);
+void launch_forward(cudaStream_t s, int precision, int R, int shape, int grid, const SweepParams &p);
+void launch_backward(cudaStream_t s, int precision, int R, int shape, int grid, const SweepParams &p);
 void launch_tree_reduce(cudaStream_t s, const MixParams &m);
 void launch_mix(cudaStream_t s, const MixParams &m);
 void launch_grad_reduce(cudaStream_t s, int n_blocks, int n_edges, const double *partial, double *grad);
-int max_resident_blocks(int precision, int R, bool backward, int n_edges);
+int max_resident_blocks(int precision, int R, int shape, bool backward, int n_edges);
 // Number of kernel launches issued by the launchers above (host counter).
 int64_t launches_issued();
 

@@ -94,14 +94,17 @@ struct netlk_ctx {
   std::vector<FwdOp> fwd;
   std::vector<BwdOp> bwd;
   int n_slots = 0, n_adj = 0, n_bwd_real = 0;
-  std::vector<int32_t> root_slot, slot_begin, slot_roots;
+  std::vector<int32_t> root_slot, slot_begin, slot_roots, msg_slots;
   int grid_fwd = 0, grid_bwd = 0;
+  int fwd_shape = 0, bwd_shape = 0, sms = 0;
+  bool tuned = false;
+  std::vector<double> tune_fwd_ms, tune_bwd_ms;
   int64_t site_updates = 0, tip_uses = 0, fake_uses = 0;
   // device
   int device = 0;
   cudaStream_t stream = nullptr;
   int64_t dev_bytes = 0;
-  DevBuf d_clv, d_scaler, d_adj, d_tips, d_weights, d_unit_part, d_fwd, d_bwd;
+  DevBuf d_clv, d_scaler, d_adj, d_msg_slots, d_tips, d_weights, d_unit_part, d_fwd, d_bwd;
   DevBuf d_pmat64, d_pmat32, d_lambda, d_U, d_Uinv, d_rates, d_rw, d_freqs, d_Q, d_brlen;
   DevBuf d_site_partial, d_tree_logl, d_root_slot, d_root_lp, d_root_dlp, d_seeds, d_wts;
   DevBuf d_slot_begin, d_slot_roots, d_parts, d_out, d_grad_partial, d_grad;
@@ -109,14 +112,50 @@ struct netlk_ctx {
   cudaGraphExec_t graph_logl = nullptr, graph_grad = nullptr, graph_partials = nullptr,
                   graph_mixbwd = nullptr;
   bool probs_dirty = true, model_dirty = true;
+  bool device_brlen = false;  // last branch lengths came from device memory
   int64_t launches = 0;
+  int64_t fwd_bytes = 0, bwd_bytes = 0;
+  // per-kernel event timing (profiling mode launches without graphs)
+  bool profiling = false;
+  std::vector<cudaEvent_t> prof_ev;
+  std::vector<int> prof_kernel;
+  int prof_n = 0;
+  double prof_ms[6] = {0, 0, 0, 0, 0, 0};
+  int64_t prof_cnt[6] = {0, 0, 0, 0, 0, 0};
+  void prof_mark(int kernel) {
+    if (!profiling) return;
+    if (prof_n >= (int)prof_ev.size()) {
+      cudaEvent_t e;
+      CUDA_OK(cudaEventCreate(&e));
+      prof_ev.push_back(e);
+      prof_kernel.push_back(-1);
+    }
+    prof_kernel[prof_n] = kernel;
+    CUDA_OK(cudaEventRecord(prof_ev[prof_n], stream));
+    prof_n++;
+  }
+  void prof_collect() {
+    if (!profiling || prof_n == 0) return;
+    CUDA_OK(cudaEventSynchronize(prof_ev[prof_n - 1]));
+    for (int i = 1; i < prof_n; ++i) {
+      float ms = 0.f;
+      CUDA_OK(cudaEventElapsedTime(&ms, prof_ev[i - 1], prof_ev[i]));
+      const int k = prof_kernel[i];
+      if (k >= 0 && k < 6) {
+        prof_ms[k] += ms;
+        prof_cnt[k]++;
+      }
+    }
+    prof_n = 0;
+  }
   std::string err;
 
   ~netlk_ctx() {
     if (device >= 0) cudaSetDevice(device);
+    for (auto e : prof_ev) cudaEventDestroy(e);
     for (auto g : {graph_logl, graph_grad, graph_partials, graph_mixbwd})
       if (g) cudaGraphExecDestroy(g);
-    for (DevBuf *b : {&d_clv, &d_scaler, &d_adj, &d_tips, &d_weights, &d_unit_part, &d_fwd, &d_bwd,
+    for (DevBuf *b : {&d_clv, &d_scaler, &d_adj, &d_msg_slots, &d_tips, &d_weights, &d_unit_part, &d_fwd, &d_bwd,
                       &d_pmat64, &d_pmat32, &d_lambda, &d_U, &d_Uinv, &d_rates, &d_rw, &d_freqs, &d_Q,
                       &d_brlen, &d_site_partial, &d_tree_logl, &d_root_slot, &d_root_lp, &d_root_dlp,
                       &d_seeds, &d_wts, &d_slot_begin, &d_slot_roots, &d_parts, &d_out, &d_grad_partial, &d_grad})
@@ -144,7 +183,8 @@ struct netlk_ctx {
     p.Q = d_Q.as<double>();
     p.clv = d_clv.p;
     p.scaler = d_scaler.as<int32_t>();
-    p.adj = d_adj.p;
+    p.msg = d_adj.p;
+    p.msg_slots = d_msg_slots.as<int32_t>();
     p.site_partial = d_site_partial.as<double>();
     p.seeds = d_seeds.as<double>();
     p.grad_partial = d_grad_partial.as<double>();
@@ -174,6 +214,17 @@ struct netlk_ctx {
     return m;
   }
 
+  // Persistent grid for a sweep: as many resident warps as fit, with the
+  // units spread evenly (every warp gets the same number of passes).
+  int grid_for(bool backward, int shape) const {
+    const int per_sm = max_resident_blocks(opts.precision, R, shape, backward, topo.n_edges);
+    const int wpb = shape_threads(opts.precision, R, shape) / 32;
+    const int64_t resident_warps = (int64_t)per_sm * sms * wpb;
+    const int64_t rounds = (n_units + resident_warps - 1) / resident_warps;
+    const int64_t warps = (n_units + rounds - 1) / rounds;
+    return (int)std::max<int64_t>(1, (warps + wpb - 1) / wpb);
+  }
+  void autotune();
   void build_schedules();
   void allocate_and_upload(const netlk_partition *in_parts);
   void upload_model();
@@ -216,9 +267,21 @@ void netlk_ctx::build_schedules() {
       tip_uses += is_tip_ref(var.ref[0]) + is_tip_ref(var.ref[1]);
       fake_uses += var.ref[1] == kFake;
     }
-    while (fwd.size() % kGroup) fwd.push_back(FwdOp{-1, 0, 0, 0, 0, -1, 0, 0});
+    while (fwd.size() % kFwdGroup) fwd.push_back(FwdOp{-1, 0, 0, 0, 0, -1, 0, 0});
   }
   site_updates = (int64_t)V * N;
+  const int64_t clv_b = (int64_t)R * S * (opts.precision == NETLK_FP32 ? 4 : 8);
+  auto child_bytes = [&](int32_t ref) -> int64_t {
+    if (ref >= 0) return clv_b + 4;
+    if (ref == kFake) return 0;
+    return 1;
+  };
+  fwd_bytes = 0;
+  for (const FwdOp &op : fwd) {
+    if (op.out < 0) continue;
+    fwd_bytes += N * (clv_b + 4 + child_bytes(op.a) + child_bytes(op.b));
+    if (op.slot >= 0) fwd_bytes += (int64_t)n_units * 8;
+  }
   // adjoint: variants reachable backwards from the displayed-tree roots
   std::vector<char> inb(V, 0);
   for (auto &rv : dag.roots) inb[rv.dtroot_variant] = 1;
@@ -228,10 +291,12 @@ void netlk_ctx::build_schedules() {
         for (int i = 0; i < 2; ++i)
           if (dag.vars[v].ref[i] >= 0) inb[dag.vars[v].ref[i]] = 1;
   bwd.clear();
+  msg_slots.clear();
   n_bwd_real = 0;
-  std::vector<int> adj_of(V, -1);
+  bwd_bytes = 0;
+  n_adj = 0;  // message buffers after liveness reuse
+  std::vector<std::vector<int32_t>> pending(V);  // message slots waiting for each variant
   std::vector<int> free_slots;
-  n_adj = 0;
   auto alloc_slot = [&]() {
     if (!free_slots.empty()) {
       int s = free_slots.back();
@@ -244,10 +309,10 @@ void netlk_ctx::build_schedules() {
     std::vector<int> ops;
     for (int v : by_level[L])
       if (inb[v]) ops.push_back(v);
-    for (size_t g0 = 0; g0 < ops.size(); g0 += kGroup) {
-      const size_t g1 = std::min(ops.size(), g0 + kGroup);
+    for (size_t g0 = 0; g0 < ops.size(); g0 += kBwdGroup) {
+      const size_t g1 = std::min(ops.size(), g0 + kBwdGroup);
       const size_t base = bwd.size();
-      // phase 1 of the kernel: every op of the group reads its own adjoint
+      // phase 1 of the kernel: every op of the group reads its messages
       for (size_t j = g0; j < g1; ++j) {
         const int x = ops[j];
         BwdOp op{};
@@ -256,36 +321,42 @@ void netlk_ctx::build_schedules() {
         op.b = dag.vars[x].ref[1];
         op.ea = dag.vars[x].edge[0];
         op.eb = dag.vars[x].edge[1];
-        op.adj_x = adj_of[x];
         op.seed = slot_of[x];
-        op.adj_a = op.adj_b = -1;
+        op.out_a = op.out_b = -1;
+        op.msg_begin = (int32_t)msg_slots.size();
+        op.msg_count = (int32_t)pending[x].size();
+        for (int32_t m : pending[x]) msg_slots.push_back(m);
         bwd.push_back(op);
         n_bwd_real++;
       }
-      for (size_t j = g0; j < g1; ++j)
-        if (adj_of[ops[j]] >= 0) free_slots.push_back(adj_of[ops[j]]);
-      // phase 2: children adjoints are stored (first writer) or accumulated
+      for (size_t j = g0; j < g1; ++j) {
+        for (int32_t m : pending[ops[j]]) free_slots.push_back(m);
+        pending[ops[j]].clear();
+      }
+      // phase 2: one fresh message buffer per inner child
       for (size_t j = g0; j < g1; ++j) {
         BwdOp &op = bwd[base + (j - g0)];
-        int modes[2] = {0, 0};
-        int32_t refs[2] = {op.a, op.b};
-        int32_t *dst[2] = {&op.adj_a, &op.adj_b};
-        for (int i = 0; i < 2; ++i) {
-          if (refs[i] < 0) continue;
-          if (adj_of[refs[i]] < 0) {
-            adj_of[refs[i]] = alloc_slot();
-            modes[i] = 1;
-          } else {
-            modes[i] = 2;
-          }
-          *dst[i] = adj_of[refs[i]];
+        if (op.a >= 0) {
+          op.out_a = alloc_slot();
+          pending[op.a].push_back(op.out_a);
         }
-        op.modes = modes[0] | (modes[1] << 8);
+        if (op.b >= 0) {
+          op.out_b = alloc_slot();
+          pending[op.b].push_back(op.out_b);
+        }
       }
-      while (bwd.size() % kGroup) {
+      for (size_t j = base; j < bwd.size(); ++j) {
+        const BwdOp &op = bwd[j];
+        int64_t b = 4 + child_bytes(op.a) + child_bytes(op.b) + (int64_t)op.msg_count * clv_b;
+        if (op.seed >= 0) b += clv_b;
+        if (op.out_a >= 0) b += clv_b;
+        if (op.out_b >= 0) b += clv_b;
+        bwd_bytes += N * b;
+      }
+      while (bwd.size() % kBwdGroup) {
         BwdOp nop{};
         nop.x = -1;
-        nop.adj_x = nop.seed = nop.adj_a = nop.adj_b = -1;
+        nop.seed = nop.out_a = nop.out_b = -1;
         bwd.push_back(nop);
       }
     }
@@ -295,12 +366,12 @@ void netlk_ctx::build_schedules() {
 // ------------------------------------------------------------ device setup
 void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
   const int V = (int)dag.vars.size();
-  ppw = 32 / R;
-  // patterns: every partition padded to whole 32-pattern blocks
+  ppw = (32 / R) * kPPL;  // patterns per unit (one warp pass)
+  // patterns: every partition padded to whole kPatternAlign-pattern blocks
   N = 0;
   n_units = 0;
   for (auto &pi : parts) {
-    pi.n_pad = (pi.n + 31) / 32 * 32;
+    pi.n_pad = (pi.n + kPatternAlign - 1) / kPatternAlign * kPatternAlign;
     pi.offset = N;
     pi.unit_begin = (int)(N / ppw);
     N += pi.n_pad;
@@ -333,6 +404,7 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
   d_clv.alloc(clv_per_var * V, dev_bytes);
   d_scaler.alloc((size_t)N * V * 4, dev_bytes);
   d_adj.alloc(clv_per_var * std::max(1, n_adj), dev_bytes);
+  d_msg_slots.alloc(std::max<size_t>(1, msg_slots.size()) * 4, dev_bytes);
   d_tips.alloc(tips.size(), dev_bytes);
   d_weights.alloc(N * 8, dev_bytes);
   d_unit_part.alloc(n_units * 4, dev_bytes);
@@ -362,18 +434,13 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
   d_out.alloc((2 + P + topo.n_ret) * 8, dev_bytes);
   d_grad.alloc(topo.n_edges * 8, dev_bytes);
 
-  int sms = 0;
   CUDA_OK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-  auto grid_for = [&](bool backward) {
-    const int per_sm = max_resident_blocks(opts.precision, R, backward, topo.n_edges);
-    const int64_t resident_warps = (int64_t)per_sm * sms * (kThreads / 32);
-    const int64_t rounds = (n_units + resident_warps - 1) / resident_warps;
-    const int64_t warps = (n_units + rounds - 1) / rounds;
-    return (int)std::max<int64_t>(1, (warps + kThreads / 32 - 1) / (kThreads / 32));
-  };
-  grid_fwd = grid_for(false);
-  grid_bwd = grid_for(true);
-  d_grad_partial.alloc((size_t)grid_bwd * topo.n_edges * 8, dev_bytes);
+  fwd_shape = bwd_shape = 0;
+  grid_fwd = grid_for(false, 0);
+  grid_bwd = grid_for(true, 0);
+  int max_bwd_grid = 0;
+  for (int sh = 0; sh < num_shapes(opts.precision, R); ++sh) max_bwd_grid = std::max(max_bwd_grid, grid_for(true, sh));
+  d_grad_partial.alloc((size_t)max_bwd_grid * topo.n_edges * 8, dev_bytes);
 
   std::vector<DevPartition> dparts(P);
   for (int p = 0; p < P; ++p) dparts[p] = DevPartition{parts[p].unit_begin, parts[p].unit_end};
@@ -383,6 +450,9 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
   CUDA_OK(cudaMemcpyAsync(d_fwd.p, fwd.data(), fwd.size() * sizeof(FwdOp), cudaMemcpyHostToDevice, stream));
   if (!bwd.empty())
     CUDA_OK(cudaMemcpyAsync(d_bwd.p, bwd.data(), bwd.size() * sizeof(BwdOp), cudaMemcpyHostToDevice, stream));
+  if (!msg_slots.empty())
+    CUDA_OK(cudaMemcpyAsync(d_msg_slots.p, msg_slots.data(), msg_slots.size() * 4, cudaMemcpyHostToDevice,
+                            stream));
   CUDA_OK(cudaMemcpyAsync(d_root_slot.p, root_slot.data(), root_slot.size() * 4, cudaMemcpyHostToDevice, stream));
   CUDA_OK(cudaMemcpyAsync(d_slot_begin.p, slot_begin.data(), slot_begin.size() * 4, cudaMemcpyHostToDevice, stream));
   CUDA_OK(cudaMemcpyAsync(d_slot_roots.p, slot_roots.data(), slot_roots.size() * 4, cudaMemcpyHostToDevice, stream));
@@ -437,24 +507,38 @@ void netlk_ctx::upload_probs() {
 }
 
 void netlk_ctx::enqueue(bool pm, bool fwd_on, bool reduce, bool mixk, bool bwd_on) {
-  if (pm)
+  prof_mark(-1);
+  if (pm) {
     launch_pmatrix(stream, P, topo.n_edges, R, d_lambda.as<double>(), d_U.as<double>(), d_Uinv.as<double>(),
                    d_rates.as<double>(), d_brlen.as<double>(), d_pmat64.as<double>(),
                    opts.precision == NETLK_FP32 ? d_pmat32.as<float>() : nullptr);
+    prof_mark(0);
+  }
   const SweepParams sp = sweep();
   const MixParams mp = mix();
-  if (fwd_on) launch_forward(stream, opts.precision, R, grid_fwd, sp);
-  if (reduce) launch_tree_reduce(stream, mp);
-  if (mixk) launch_mix(stream, mp);
+  if (fwd_on) {
+    launch_forward(stream, opts.precision, R, fwd_shape, grid_fwd, sp);
+    prof_mark(1);
+  }
+  if (reduce) {
+    launch_tree_reduce(stream, mp);
+    prof_mark(2);
+  }
+  if (mixk) {
+    launch_mix(stream, mp);
+    prof_mark(3);
+  }
   if (bwd_on && !bwd.empty()) {
-    launch_backward(stream, opts.precision, R, grid_bwd, sp);
+    launch_backward(stream, opts.precision, R, bwd_shape, grid_bwd, sp);
+    prof_mark(4);
     launch_grad_reduce(stream, grid_bwd, topo.n_edges, d_grad_partial.as<double>(), d_grad.as<double>());
+    prof_mark(5);
   }
 }
 
 void netlk_ctx::run(cudaGraphExec_t *cache, bool pm, bool fwd_on, bool reduce, bool mixk, bool bwd_on) {
   const int n = (int)pm + (int)fwd_on + (int)reduce + (int)mixk + (bwd_on && !bwd.empty() ? 2 : 0);
-  if (!opts.use_cuda_graph) {
+  if (!opts.use_cuda_graph || profiling) {
     enqueue(pm, fwd_on, reduce, mixk, bwd_on);
     launches += n;
     return;
@@ -472,13 +556,60 @@ void netlk_ctx::run(cudaGraphExec_t *cache, bool pm, bool fwd_on, bool reduce, b
   launches += n;
 }
 
+// Times every launch shape of the two sweeps once on this context's own
+// workload (after one full evaluation with the default shapes, so the
+// adjoint sweep sees real seeds) and keeps the fastest for the CUDA graphs.
+void netlk_ctx::autotune() {
+  tuned = true;
+  const int ns = num_shapes(opts.precision, R);
+  tune_fwd_ms.assign(ns, 0.0);
+  tune_bwd_ms.assign(ns, 0.0);
+  if (ns <= 1 || !opts.autotune) return;
+  std::memcpy(h_brlen.p, brlen.data(), brlen.size() * 8);
+  CUDA_OK(cudaMemcpyAsync(d_brlen.p, h_brlen.p, brlen.size() * 8, cudaMemcpyHostToDevice, stream));
+  enqueue(true, true, true, true, true);
+  cudaEvent_t e0, e1;
+  CUDA_OK(cudaEventCreate(&e0));
+  CUDA_OK(cudaEventCreate(&e1));
+  const SweepParams sp = sweep();
+  auto time_one = [&](bool backward, int sh) {
+    const int grid = grid_for(backward, sh);
+    float best = 1e30f;
+    for (int rep = 0; rep < 2; ++rep) {
+      CUDA_OK(cudaEventRecord(e0, stream));
+      if (backward)
+        launch_backward(stream, opts.precision, R, sh, grid, sp);
+      else
+        launch_forward(stream, opts.precision, R, sh, grid, sp);
+      CUDA_OK(cudaEventRecord(e1, stream));
+      CUDA_OK(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      CUDA_OK(cudaEventElapsedTime(&ms, e0, e1));
+      if (rep) best = std::min(best, ms);
+    }
+    return (double)best;
+  };
+  for (int sh = 0; sh < ns; ++sh) tune_fwd_ms[sh] = time_one(false, sh);
+  for (int sh = 0; sh < ns; ++sh) tune_bwd_ms[sh] = time_one(true, sh);
+  CUDA_OK(cudaGetLastError());
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  fwd_shape = (int)(std::min_element(tune_fwd_ms.begin(), tune_fwd_ms.end()) - tune_fwd_ms.begin());
+  bwd_shape = (int)(std::min_element(tune_bwd_ms.begin(), tune_bwd_ms.end()) - tune_bwd_ms.begin());
+  grid_fwd = grid_for(false, fwd_shape);
+  grid_bwd = grid_for(true, bwd_shape);
+}
+
 void netlk_ctx::prepare() {
   if (opts.host_only) throw Error(NETLK_ERR_NO_DEVICE, "context was created host_only");
   CUDA_OK(cudaSetDevice(device));
   if (model_dirty) upload_model();
   if (probs_dirty) upload_probs();
-  std::memcpy(h_brlen.p, brlen.data(), brlen.size() * 8);
-  CUDA_OK(cudaMemcpyAsync(d_brlen.p, h_brlen.p, brlen.size() * 8, cudaMemcpyHostToDevice, stream));
+  if (!tuned) autotune();
+  if (!device_brlen) {  // lengths set from device memory stay where they are
+    std::memcpy(h_brlen.p, brlen.data(), brlen.size() * 8);
+    CUDA_OK(cudaMemcpyAsync(d_brlen.p, h_brlen.p, brlen.size() * 8, cudaMemcpyHostToDevice, stream));
+  }
 }
 
 void netlk_ctx::finish(double *total, double *part_logl, double *d_brlen, double *d_ret) {
@@ -488,6 +619,7 @@ void netlk_ctx::finish(double *total, double *part_logl, double *d_brlen, double
     CUDA_OK(cudaMemcpyAsync(h_grad.p, d_grad.p, topo.n_edges * 8, cudaMemcpyDeviceToHost, stream));
   CUDA_OK(cudaStreamSynchronize(stream));
   CUDA_OK(cudaGetLastError());
+  prof_collect();
   const double *o = h_out.as<double>();
   if (o[1] != 0.0 || !std::isfinite(o[0]))
     throw Error(NETLK_ERR_NUMERIC, "Invalid network likelihood: negative infinity or NaN");
@@ -528,6 +660,7 @@ void set_brlen(netlk_ctx *c, const double *b) {
   check_finite(b, c->topo.n_edges, "branch length", 0.0, 1e300);
   c->brlen.assign(b, b + c->topo.n_edges);
   for (double &x : c->brlen) x = std::min(std::max(x, 1e-6), 100.0);  // brlen_min / brlen_max
+  c->device_brlen = false;
 }
 
 void set_probs(netlk_ctx *c, const double *p) {
@@ -549,6 +682,7 @@ int netlk_options_default(netlk_options *o) {
   o->device = 0;
   o->use_cuda_graph = 1;
   o->host_only = 0;
+  o->autotune = 1;
   return NETLK_OK;
 }
 
@@ -677,6 +811,8 @@ int netlk_get_dag_stats(const netlk_ctx *ctx, netlk_dag_stats *o) {
   o->tip_child_uses = ctx->tip_uses;
   o->fake_child_uses = ctx->fake_uses;
   o->device_bytes = ctx->dev_bytes;
+  o->forward_bytes = ctx->fwd_bytes;
+  o->backward_bytes = ctx->bwd_bytes;
   return NETLK_OK;
 }
 
@@ -848,6 +984,69 @@ int netlk_mix_and_backward(netlk_ctx *ctx, const double *global, double *total, 
   });
 }
 
+int netlk_set_branch_lengths_device(netlk_ctx *ctx, const double *d_b, int32_t n) {
+  if (!ctx) return NETLK_ERR_INVALID_ARGUMENT;
+  return guarded(ctx, [&] {
+    if (ctx->opts.host_only) throw Error(NETLK_ERR_NO_DEVICE, "context was created host_only");
+    if (!d_b || n != ctx->topo.n_edges) throw Error(NETLK_ERR_INVALID_ARGUMENT, "branch length count");
+    CUDA_OK(cudaSetDevice(ctx->device));
+    CUDA_OK(cudaMemcpyAsync(ctx->d_brlen.p, d_b, (size_t)n * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    ctx->device_brlen = true;
+  });
+}
+
+int netlk_enqueue(netlk_ctx *ctx, int32_t with_gradient) {
+  if (!ctx) return NETLK_ERR_INVALID_ARGUMENT;
+  return guarded(ctx, [&] {
+    if (ctx->opts.host_only) throw Error(NETLK_ERR_NO_DEVICE, "context was created host_only");
+    CUDA_OK(cudaSetDevice(ctx->device));
+    if (ctx->model_dirty) ctx->upload_model();
+    if (ctx->probs_dirty) ctx->upload_probs();
+    if (!ctx->tuned) ctx->autotune();
+    if (!ctx->device_brlen) {
+      std::memcpy(ctx->h_brlen.p, ctx->brlen.data(), ctx->brlen.size() * 8);
+      CUDA_OK(cudaMemcpyAsync(ctx->d_brlen.p, ctx->h_brlen.p, ctx->brlen.size() * 8, cudaMemcpyHostToDevice,
+                              ctx->stream));
+    }
+    if (with_gradient)
+      ctx->run(&ctx->graph_grad, true, true, true, true, true);
+    else
+      ctx->run(&ctx->graph_logl, true, true, true, true, false);
+    if (ctx->profiling) ctx->prof_collect();
+  });
+}
+
+int netlk_result_pointers(netlk_ctx *ctx, const double **d_out, const double **d_brlen) {
+  if (!ctx) return NETLK_ERR_INVALID_ARGUMENT;
+  if (d_out) *d_out = ctx->d_out.as<double>();
+  if (d_brlen) *d_brlen = ctx->d_grad.as<double>();
+  return NETLK_OK;
+}
+
+int netlk_set_profiling(netlk_ctx *ctx, int32_t enable) {
+  if (!ctx) return NETLK_ERR_INVALID_ARGUMENT;
+  return guarded(ctx, [&] {
+    ctx->profiling = enable != 0;
+    ctx->prof_n = 0;
+    for (int k = 0; k < 6; ++k) {
+      ctx->prof_ms[k] = 0.0;
+      ctx->prof_cnt[k] = 0;
+    }
+  });
+}
+
+int netlk_kernel_times(netlk_ctx *ctx, double *ms, int64_t *launches, int32_t n) {
+  if (!ctx || n < 6) return NETLK_ERR_INVALID_ARGUMENT;
+  return guarded(ctx, [&] {
+    if (ctx->stream) CUDA_OK(cudaStreamSynchronize(ctx->stream));
+    ctx->prof_collect();
+    for (int k = 0; k < 6; ++k) {
+      if (ms) ms[k] = ctx->prof_ms[k];
+      if (launches) launches[k] = ctx->prof_cnt[k];
+    }
+  });
+}
+
 int netlk_get_clv(netlk_ctx *ctx, int32_t variant, int32_t part, double *clv, int32_t *scaler) {
   if (!ctx) return NETLK_ERR_INVALID_ARGUMENT;
   return guarded(ctx, [&] {
@@ -873,6 +1072,18 @@ int netlk_get_clv(netlk_ctx *ctx, int32_t variant, int32_t part, double *clv, in
       CUDA_OK(cudaMemcpy(scaler, ctx->d_scaler.as<int32_t>() + (size_t)variant * ctx->N + pi.offset,
                          (size_t)pi.n * 4, cudaMemcpyDeviceToHost));
   });
+}
+
+int netlk_tuning(const netlk_ctx *ctx, int32_t *fwd_shape, int32_t *bwd_shape, double *fwd_ms, double *bwd_ms,
+                 int32_t n) {
+  if (!ctx) return NETLK_ERR_INVALID_ARGUMENT;
+  if (fwd_shape) *fwd_shape = ctx->fwd_shape;
+  if (bwd_shape) *bwd_shape = ctx->bwd_shape;
+  for (int i = 0; i < n; ++i) {
+    if (fwd_ms) fwd_ms[i] = i < (int)ctx->tune_fwd_ms.size() ? ctx->tune_fwd_ms[i] : 0.0;
+    if (bwd_ms) bwd_ms[i] = i < (int)ctx->tune_bwd_ms.size() ? ctx->tune_bwd_ms[i] : 0.0;
+  }
+  return NETLK_OK;
 }
 
 int netlk_get_stream(netlk_ctx *ctx, void **stream) {

@@ -37,7 +37,7 @@ def _ptr(a, ct):
 class NetworkLikelihood:
     def __init__(self, network: NetworkDesc, partitions, variant="AVERAGE", precision="fp32",
                  min_interesting_tree_logprob=math.log(1e-6), device=0, use_cuda_graph=True,
-                 host_only=False, rates=None):
+                 host_only=False, rates=None, autotune=True):
         L = N.lib()
         self.network = network
         self.n_parts = len(partitions)
@@ -87,6 +87,7 @@ class NetworkLikelihood:
         opts.device = int(device)
         opts.use_cuda_graph = int(bool(use_cuda_graph))
         opts.host_only = int(bool(host_only))
+        opts.autotune = int(bool(autotune))
         bl = arr(network.branch_lengths, np.float64)
         rp = arr(network.ret_first_probs, np.float64) if self.n_ret else None
         h = ctypes.c_void_p()
@@ -212,6 +213,40 @@ class NetworkLikelihood:
         N.check(N.lib().netlk_get_clv(self._h, variant, part, _ptr(clv, ctypes.c_double),
                                       _ptr(sc, ctypes.c_int32)), self._h)
         return clv.reshape(n, 4, 4), sc
+
+    # ------------------------------------------------ device-resident stepping
+    def set_branch_lengths_device(self, dev_ptr):
+        """Enqueue a copy of branch lengths from a device pointer (e.g. a CUDA tensor)."""
+        N.check(N.lib().netlk_set_branch_lengths_device(self._h, ctypes.c_void_p(dev_ptr), self.n_edges),
+                self._h)
+
+    def enqueue(self, with_gradient=True):
+        N.check(N.lib().netlk_enqueue(self._h, int(bool(with_gradient))), self._h)
+
+    def result_pointers(self):
+        o, g = ctypes.c_void_p(), ctypes.c_void_p()
+        N.check(N.lib().netlk_result_pointers(self._h, ctypes.byref(o), ctypes.byref(g)), self._h)
+        return o.value, g.value
+
+    def set_profiling(self, enable=True):
+        N.check(N.lib().netlk_set_profiling(self._h, int(bool(enable))), self._h)
+
+    KERNELS = ("pmatrix", "forward", "tree_reduce", "mix", "backward", "grad_reduce")
+
+    def kernel_times(self):
+        ms = np.zeros(6)
+        cnt = np.zeros(6, np.int64)
+        N.check(N.lib().netlk_kernel_times(self._h, _ptr(ms, ctypes.c_double),
+                                           cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), 6), self._h)
+        return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(self.KERNELS)}
+
+    def tuning(self, n=8):
+        fs, bs = ctypes.c_int32(), ctypes.c_int32()
+        fm, bm = np.zeros(n), np.zeros(n)
+        N.check(N.lib().netlk_tuning(self._h, ctypes.byref(fs), ctypes.byref(bs), _ptr(fm, ctypes.c_double),
+                                     _ptr(bm, ctypes.c_double), n), self._h)
+        return {"forward_shape": fs.value, "backward_shape": bs.value,
+                "forward_ms": [x for x in fm if x > 0], "backward_ms": [x for x in bm if x > 0]}
 
     def stream(self):
         s = ctypes.c_void_p()

@@ -408,6 +408,44 @@ class ImprovedOracle:
         for t in self.pernode[self.net.root]:
             self._tree_logl(t)
 
+    def recompute(self):
+        """Re-run the pruning of an enumerated DAG (after ``forward``) for new
+        branch lengths: the arithmetic of processPartitionsImproved without the
+        host-side enumeration. This is the timed CPU baseline."""
+        self.update_count = 0
+        pm = {}
+        for p, part in enumerate(self.parts):
+            for e in range(self.net.n_edges):
+                pm[(p, e)] = part.pmat(self.brlen[e])
+        for v in self.travbuffer:
+            for tree in self.pernode[v]:
+                if tree.is_tip or tree.children is None:
+                    continue
+                (lnode, li, le), rinfo = tree.children
+                ltree = self.pernode[lnode][li]
+                for p, part in enumerate(self.parts):
+                    lclv = part.tip_clv(lnode) if ltree.is_tip else ltree.clv[p]
+                    lsc = None if ltree.is_tip else ltree.scaler[p]
+                    if rinfo is None:
+                        cbuild.update_partial(tree.clv[p], tree.scaler[p], lclv, lsc, pm[(p, le)],
+                                              None, None, None)
+                    else:
+                        rnode, ri, re = rinfo
+                        rtree = self.pernode[rnode][ri]
+                        rclv = part.tip_clv(rnode) if rtree.is_tip else rtree.clv[p]
+                        rsc = None if rtree.is_tip else rtree.scaler[p]
+                        cbuild.update_partial(tree.clv[p], tree.scaler[p], lclv, lsc, pm[(p, le)],
+                                              rclv, rsc, pm[(p, re)])
+                    self.update_count += part.n
+        for t in self.pernode[self.net.root]:
+            if t.logprob < self.min_lp or t.dtroot is None:
+                continue
+            dn, di = t.dtroot
+            m = self.pernode[dn][di]
+            t.partition_logl = [cbuild.root_logl(m.clv[p], m.scaler[p], part.freqs, part.rate_weights,
+                                                 part.weights) for p, part in enumerate(self.parts)]
+        return self.evaluate()[0]
+
     def root_trees(self):
         return self.pernode[self.net.root]
 
