@@ -100,7 +100,9 @@ typedef struct {
                                         return NETLK_ERR_NO_DEVICE)          */
   int32_t autotune;                  /* 1: time the launch shapes of the two
                                         sweeps on the first evaluation and keep
-                                        the fastest (default); 0: default shape */
+                                        the fastest (default); 0: default shape.
+                                        The environment variable NETLK_SHAPES=
+                                        "f,b" fixes both shapes instead.      */
 } netlk_options;
 
 typedef struct {
@@ -122,6 +124,10 @@ typedef struct {
                                 parent CLV + scaler writes, inner-child CLV +
                                 scaler reads, tip-code reads                  */
   int64_t backward_bytes;    /* algorithmic HBM bytes of one adjoint sweep   */
+  int64_t launches_per_gradient_eval; /* kernels of one logL + gradient call:
+                                P-matrices, one forward launch per level,
+                                site sums, mixture, one adjoint launch per
+                                level, two gradient reduction stages          */
 } netlk_dag_stats;
 
 /* --------------------------------------------------------------- lifecycle */

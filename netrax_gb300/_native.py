@@ -68,7 +68,7 @@ class DagStats(ctypes.Structure):
                 ("n_patterns_total", ctypes.c_int64), ("site_clv_updates", ctypes.c_int64),
                 ("tip_child_uses", ctypes.c_int64), ("fake_child_uses", ctypes.c_int64),
                 ("device_bytes", ctypes.c_int64), ("forward_bytes", ctypes.c_int64),
-                ("backward_bytes", ctypes.c_int64)]
+                ("backward_bytes", ctypes.c_int64), ("launches_per_gradient_eval", ctypes.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -153,6 +153,36 @@ __device__ __forceinline__ void matvec2(const real *P, const real (&c)[kPPL][4],
   }
 }
 
+// Same products with P read from shared memory.
+template <typename real>
+__device__ __forceinline__ void matvec2_s(const real *P, const real (&c)[kPPL][4], real (&out)[kPPL][4]) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    real row[4];
+    Vec<real>::load(P + 4 * i, row);
+#pragma unroll
+    for (int k = 0; k < kPPL; ++k)
+      out[k][i] = row[0] * c[k][0] + row[1] * c[k][1] + row[2] * c[k][2] + row[3] * c[k][3];
+  }
+}
+
+template <typename real>
+__device__ __forceinline__ void matvec2_ts(const real *P, const real (&u)[kPPL][4], real (&out)[kPPL][4]) {
+#pragma unroll
+  for (int k = 0; k < kPPL; ++k)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) out[k][j] = 0;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    real row[4];
+    Vec<real>::load(P + 4 * i, row);
+#pragma unroll
+    for (int k = 0; k < kPPL; ++k)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) out[k][j] += row[j] * u[k][i];
+  }
+}
+
 // out[k] = P^T . u[k]
 template <typename real>
 __device__ __forceinline__ void matvec2_t(const real *P, const real (&u)[kPPL][4], real (&out)[kPPL][4]) {
@@ -192,6 +222,31 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
+// Stages the op's two P-matrices (all R rates) of one partition in the
+// warp's own shared-memory slice: sP[m][r][16], m = 0 for edge ea, 1 for edge
+// eb (zero for the fake child). 2*R*16 values = one 16-byte load per lane at
+// R = 4 in FP32; a __syncwarp (no block barrier) publishes them.
+template <typename real, int R>
+__device__ __forceinline__ void stage_pmats_warp(real *sP, const real *pm_part, int ea, int eb, int lane) {
+  constexpr int V = 16 / sizeof(real);  // values per 16-byte vector
+  constexpr int NV = 2 * R * 16 / V;
+  for (int i = lane; i < NV; i += 32) {
+    const int m = (i * V) / (R * 16), j = i * V - m * (R * 16);
+    const int e = m ? eb : ea;
+    if (e >= 0) {
+      if (sizeof(real) == 4) {
+        *reinterpret_cast<float4 *>(sP + i * V) = __ldg(reinterpret_cast<const float4 *>(pm_part + (size_t)e * (R * 16) + j));
+      } else {
+        *reinterpret_cast<double2 *>(sP + i * V) = __ldg(reinterpret_cast<const double2 *>(pm_part + (size_t)e * (R * 16) + j));
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < V; ++q) sP[i * V + q] = (real)0;
+    }
+  }
+  __syncwarp();
+}
+
 __device__ __forceinline__ FwdOp load_fwd_op(const FwdOp *ops, int i) {
   const int4 *q = reinterpret_cast<const int4 *>(ops + i);
   const int4 a = __ldg(q), b = __ldg(q + 1);
@@ -212,248 +267,223 @@ __device__ __forceinline__ BwdOp load_bwd_op(const BwdOp *ops, int i) {
 }
 
 // ------------------------------------------------------------------ forward
-// CLV_out = (P[ea] . a) * (P[eb] . b), rescaled per site; site log-likelihoods
-// of displayed-tree root variants are summed over the warp's patterns.
+// One launch per DAG level: blockIdx.y picks the op of the level, each warp
+// one unit of patterns. CLV_out = (P[ea] . a) * (P[eb] . b), rescaled per
+// site; site log-likelihoods of displayed-tree root variants are summed over
+// the warp's patterns into site_partial[slot][unit].
 template <typename real, int R, int THREADS, int MINB>
-__global__ void __launch_bounds__(THREADS, MINB) forward_kernel(const SweepParams p) {
+__global__ void __launch_bounds__(THREADS, MINB) forward_kernel(const SweepParams p, int op_begin) {
   constexpr int PPW = 32 / R;          // patterns per pass of the lane rows
   constexpr int UNIT = PPW * kPPL;     // patterns per unit
+  constexpr int WPB = THREADS / 32;
+  __shared__ __align__(16) real sPw[WPB][2 * R * 16];
   const int lane = threadIdx.x & 31;
   const int r = lane % R;
   const int pl = lane / R;
-  const int warps_total = gridDim.x * (THREADS / 32);
-  const int warp_id = blockIdx.x * (THREADS / 32) + (threadIdx.x >> 5);
-  const real *pmat = static_cast<const real *>(p.pmat);
-  real *clv = static_cast<real *>(p.clv);
+  const int unit = blockIdx.x * WPB + (threadIdx.x >> 5);
+  if (unit >= p.n_units) return;  // whole warp
+  real *sP = sPw[threadIdx.x >> 5];
+  const FwdOp op = load_fwd_op(p.fwd_ops, op_begin + blockIdx.y);
+  const int part = p.unit_part[unit];
   const size_t N = (size_t)p.n_patterns;
+  const size_t g0 = (size_t)unit * UNIT + pl;  // the lane's first pattern; the second is g0 + PPW
+  real ca[kPPL][4], cb[kPPL][4];
+  int sa[kPPL], sb[kPPL];
+  load_child<real, R>(p, op.a, g0, r, PPW, ca, sa);
+  load_child<real, R>(p, op.b, g0, r, PPW, cb, sb);
+  stage_pmats_warp<real, R>(sP, static_cast<const real *>(p.pmat) + (size_t)part * p.n_edges * (R * 16), op.ea,
+                            op.b == INT32_MIN ? -1 : op.eb, lane);
 
-  for (int unit = warp_id; unit < p.n_units; unit += warps_total) {
-    const int part = p.unit_part[unit];
-    const size_t g0 = (size_t)unit * UNIT + pl;  // first pattern of the lane; second is g0 + PPW
-    const real *pm = pmat + (size_t)part * p.n_edges * (R * 16) + r * 16;
-    double wgt[kPPL];
+  real v[kPPL][4];
+  matvec2_s<real>(sP + r * 16, ca, v);
+  if (op.b != INT32_MIN) {
+    real pb[kPPL][4];
+    matvec2_s<real>(sP + R * 16 + r * 16, cb, pb);
 #pragma unroll
-    for (int k = 0; k < kPPL; ++k) wgt[k] = p.weights[g0 + (size_t)k * PPW];
+    for (int k = 0; k < kPPL; ++k)
+#pragma unroll
+      for (int i = 0; i < 4; ++i) v[k][i] *= pb[k][i];
+  }
+  real *dst = static_cast<real *>(p.clv) + ((size_t)op.out * N + g0) * (R * 4) + r * 4;
+  int32_t *sdst = p.scaler + (size_t)op.out * N + g0;
+  int s[kPPL];
+#pragma unroll
+  for (int k = 0; k < kPPL; ++k) {
+    real m = max(max(v[k][0], v[k][1]), max(v[k][2], v[k][3]));
+    m = rate_max<R>(m);
+    s[k] = sa[k] + sb[k] + Scale<real>::rescale(m, v[k]);
+    Vec<real>::store(dst + (size_t)k * PPW * (R * 4), v[k]);
+    if (r == 0) sdst[(size_t)k * PPW] = s[k];
+  }
+  if (op.slot >= 0) {
+    // pll_compute_root_loglikelihood for the lane's sites, summed over the warp
+    const real rw = (real)p.rate_weights[part * R + r];
     real freq[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) freq[i] = (real)p.freqs[part * 4 + i];
-    const real rw = (real)p.rate_weights[part * R + r];
-
-    for (int o0 = 0; o0 < p.n_fwd_ops; o0 += kFwdGroup) {
-      FwdOp op[kFwdGroup];
-      real ca[kFwdGroup][kPPL][4], cb[kFwdGroup][kPPL][4];
-      int sa[kFwdGroup][kPPL], sb[kFwdGroup][kPPL];
+    double ll = 0.0;
 #pragma unroll
-      for (int j = 0; j < kFwdGroup; ++j) {
-        op[j] = load_fwd_op(p.fwd_ops, o0 + j);
-        if (op[j].out < 0) continue;
-        load_child<real, R>(p, op[j].a, g0, r, PPW, ca[j], sa[j]);
-        load_child<real, R>(p, op[j].b, g0, r, PPW, cb[j], sb[j]);
-      }
-#pragma unroll
-      for (int j = 0; j < kFwdGroup; ++j) {
-        if (op[j].out < 0) continue;
-        real v[kPPL][4];
-        matvec2<real>(pm + (size_t)op[j].ea * (R * 16), ca[j], v);
-        if (op[j].b != INT32_MIN) {
-          real pb[kPPL][4];
-          matvec2<real>(pm + (size_t)op[j].eb * (R * 16), cb[j], pb);
-#pragma unroll
-          for (int k = 0; k < kPPL; ++k)
-#pragma unroll
-            for (int i = 0; i < 4; ++i) v[k][i] *= pb[k][i];
-        }
-        real *dst = clv + ((size_t)op[j].out * N + g0) * (R * 4) + r * 4;
-        int32_t *sdst = p.scaler + (size_t)op[j].out * N + g0;
-        int s[kPPL];
-#pragma unroll
-        for (int k = 0; k < kPPL; ++k) {
-          real m = max(max(v[k][0], v[k][1]), max(v[k][2], v[k][3]));
-          m = rate_max<R>(m);
-          s[k] = sa[j][k] + sb[j][k] + Scale<real>::rescale(m, v[k]);
-          Vec<real>::store(dst + (size_t)k * PPW * (R * 4), v[k]);
-          if (r == 0) sdst[(size_t)k * PPW] = s[k];
-        }
-        if (op[j].slot >= 0) {
-          // pll_compute_root_loglikelihood for the lane's sites, summed over the warp
-          double ll = 0.0;
-#pragma unroll
-          for (int k = 0; k < kPPL; ++k) {
-            real t = rw * (freq[0] * v[k][0] + freq[1] * v[k][1] + freq[2] * v[k][2] + freq[3] * v[k][3]);
-            t = rate_sum<R>(t);
-            if (r == 0 && wgt[k] != 0.0) {
-              const double lt = (sizeof(real) == 4) ? (double)logf((float)t) : log((double)t);
-              ll += wgt[k] * (lt + (double)s[k] * Scale<real>::kLogUnit);
-            }
-          }
-          ll = warp_sum(ll);
-          if (lane == 0) p.site_partial[(size_t)op[j].slot * p.n_units + unit] = ll;
-        }
+    for (int k = 0; k < kPPL; ++k) {
+      real t = rw * (freq[0] * v[k][0] + freq[1] * v[k][1] + freq[2] * v[k][2] + freq[3] * v[k][3]);
+      t = rate_sum<R>(t);
+      const double w = p.weights[g0 + (size_t)k * PPW];
+      if (r == 0 && w != 0.0) {
+        const double lt = (sizeof(real) == 4) ? (double)logf((float)t) : log((double)t);
+        ll += w * (lt + (double)s[k] * Scale<real>::kLogUnit);
       }
     }
+    ll = warp_sum(ll);
+    if (lane == 0) p.site_partial[(size_t)op.slot * p.n_units + unit] = ll;
   }
 }
 
 // ------------------------------------------------------------------ adjoint
-// Reverse sweep as message passing. For op x with CLV_x = 2^k (Pa a) * (Pb b):
+// Reverse sweep as message passing, one launch per level (deepest first).
+// For op x with CLV_x = 2^k (Pa a) * (Pb b):
 //   adj_x   = sum of incoming messages (+ seed: tree weight * w_s rw_r pi_i / L_s)
 //   u_a     = 2^k adj_x * (Pb b),  u_b = 2^k adj_x * (Pa a)
 //   dlogL/dt_ea += sum u_a . (r Q Pa a),  dlogL/dt_eb += sum u_b . (r Q Pb b)
 //   message to a = Pa^T u_a, message to b = Pb^T u_b
+// The two edge terms are summed over the block and written to
+// grad_partial[op][blockIdx.x][2] for a deterministic reduction per edge.
 template <typename real, int R, int THREADS, int MINB>
-__global__ void __launch_bounds__(THREADS, MINB) backward_kernel(const SweepParams p) {
-  extern __shared__ double sgrad[];
+__global__ void __launch_bounds__(THREADS, MINB) backward_kernel(const SweepParams p, int op_begin) {
   constexpr int PPW = 32 / R;
   constexpr int UNIT = PPW * kPPL;
+  constexpr int WPB = THREADS / 32;
+  __shared__ __align__(16) real sPw[WPB][2 * R * 16];
+  __shared__ real sQw[WPB][16 + 4 + 2 * R];
   const int lane = threadIdx.x & 31;
   const int r = lane % R;
   const int pl = lane / R;
-  const int wib = threadIdx.x >> 5;
-  const int warps_total = gridDim.x * (THREADS / 32);
-  const int warp_id = blockIdx.x * (THREADS / 32) + wib;
-  const real *pmat = static_cast<const real *>(p.pmat);
+  const int unit = blockIdx.x * WPB + (threadIdx.x >> 5);
+  if (unit >= p.n_units) return;  // whole warp
+  real *sP = sPw[threadIdx.x >> 5];
+  real *sQ = sQw[threadIdx.x >> 5];
+  real *sF = sQ + 16, *sRW = sQ + 20, *sRate = sQ + 20 + R;
+  const int opi = op_begin + blockIdx.y;
+  const BwdOp op = load_bwd_op(p.bwd_ops, opi);
+  const bool fake = op.b == INT32_MIN;
+  const int part = p.unit_part[unit];
+  const size_t N = (size_t)p.n_patterns;
+  const size_t g0 = (size_t)unit * UNIT + pl;
+  const size_t lane_off = g0 * (R * 4) + r * 4;
   const real *clv = static_cast<const real *>(p.clv);
   real *msg = static_cast<real *>(p.msg);
-  const size_t N = (size_t)p.n_patterns;
-  double *my = sgrad + (size_t)wib * p.n_edges;
-  for (int e = lane; e < p.n_edges; e += 32) my[e] = 0.0;
-  __syncwarp();
 
-  for (int unit = warp_id; unit < p.n_units; unit += warps_total) {
-    const int part = p.unit_part[unit];
-    const size_t g0 = (size_t)unit * UNIT + pl;
-    const size_t lane_off = g0 * (R * 4) + r * 4;
-    const real *pm = pmat + (size_t)part * p.n_edges * (R * 16) + r * 16;
-    real wgt[kPPL];
+  real ca[kPPL][4], cb[kPPL][4], ax[kPPL][4], cx[kPPL][4];
+  int sa[kPPL], sb[kPPL], sx[kPPL];
 #pragma unroll
-    for (int k = 0; k < kPPL; ++k) wgt[k] = (real)p.weights[g0 + (size_t)k * PPW];
-    real freq[4], Q[16];
+  for (int k = 0; k < kPPL; ++k)
 #pragma unroll
-    for (int i = 0; i < 4; ++i) freq[i] = (real)p.freqs[part * 4 + i];
+    for (int i = 0; i < 4; ++i) ax[k][i] = 0;
+  {
+    load_child<real, R>(p, op.a, g0, r, PPW, ca, sa);
+    load_child<real, R>(p, op.b, g0, r, PPW, cb, sb);
+    const int32_t *sxp = p.scaler + (size_t)op.x * N + g0;
 #pragma unroll
-    for (int i = 0; i < 16; ++i) Q[i] = (real)p.Q[part * 16 + i];
-    const real rw = (real)p.rate_weights[part * R + r];
-    const real rate = (real)p.rates[part * R + r];
-
-    for (int o0 = 0; o0 < p.n_bwd_ops; o0 += kBwdGroup) {
-      BwdOp op[kBwdGroup];
-      real ax[kBwdGroup][kPPL][4], ca[kBwdGroup][kPPL][4], cb[kBwdGroup][kPPL][4];
-      int sx[kBwdGroup][kPPL], sa[kBwdGroup][kPPL], sb[kBwdGroup][kPPL];
+    for (int k = 0; k < kPPL; ++k) sx[k] = sxp[(size_t)k * PPW];
+    for (int m = 0; m < op.msg_count; ++m) {
+      const real *src = msg + (size_t)__ldg(p.msg_slots + op.msg_begin + m) * N * (R * 4) + lane_off;
 #pragma unroll
-      for (int j = 0; j < kBwdGroup; ++j) {
-        op[j] = load_bwd_op(p.bwd_ops, o0 + j);
-        if (op[j].x < 0) continue;
-        load_child<real, R>(p, op[j].a, g0, r, PPW, ca[j], sa[j]);
-        load_child<real, R>(p, op[j].b, g0, r, PPW, cb[j], sb[j]);
-        const int32_t *sxp = p.scaler + (size_t)op[j].x * N + g0;
+      for (int k = 0; k < kPPL; ++k) {
+        real t[4];
+        Vec<real>::load(src + (size_t)k * PPW * (R * 4), t);
 #pragma unroll
-        for (int k = 0; k < kPPL; ++k) {
-          sx[j][k] = sxp[(size_t)k * PPW];
-#pragma unroll
-          for (int i = 0; i < 4; ++i) ax[j][k][i] = 0;
-        }
-        for (int m = 0; m < op[j].msg_count; ++m) {
-          const real *src = msg + (size_t)__ldg(p.msg_slots + op[j].msg_begin + m) * N * (R * 4) + lane_off;
-#pragma unroll
-          for (int k = 0; k < kPPL; ++k) {
-            real t[4];
-            Vec<real>::load(src + (size_t)k * PPW * (R * 4), t);
-#pragma unroll
-            for (int i = 0; i < 4; ++i) ax[j][k][i] += t[i];
-          }
-        }
-        if (op[j].seed >= 0) {
-          // d(w_s log L_s)/d clv_x = w_s rw_r pi_i / L_s, times the tree weight
-          const real sd = (real)p.seeds[(size_t)op[j].seed * p.n_parts + part];
-          const real *cxp = clv + (size_t)op[j].x * N * (R * 4) + lane_off;
-#pragma unroll
-          for (int k = 0; k < kPPL; ++k) {
-            real cx[4];
-            Vec<real>::load(cxp + (size_t)k * PPW * (R * 4), cx);
-            real t = rw * (freq[0] * cx[0] + freq[1] * cx[1] + freq[2] * cx[2] + freq[3] * cx[3]);
-            t = rate_sum<R>(t);
-            const real s = sd * wgt[k];
-            if (t > (real)0 && s != (real)0) {
-              const real f = s * rw / t;
-#pragma unroll
-              for (int i = 0; i < 4; ++i) ax[j][k][i] += f * freq[i];
-            }
-          }
-        }
+        for (int i = 0; i < 4; ++i) ax[k][i] += t[i];
       }
+    }
+    if (op.seed >= 0) {
+      const real *cxp = clv + (size_t)op.x * N * (R * 4) + lane_off;
 #pragma unroll
-      for (int j = 0; j < kBwdGroup; ++j) {
-        if (op[j].x < 0) continue;
-        const bool fake = op[j].b == INT32_MIN;
-        const real *Pa = pm + (size_t)op[j].ea * (R * 16);
-        real pa[kPPL][4], pb[kPPL][4];
-        matvec2<real>(Pa, ca[j], pa);
-        if (!fake) {
-          matvec2<real>(pm + (size_t)op[j].eb * (R * 16), cb[j], pb);
-        } else {
+      for (int k = 0; k < kPPL; ++k) Vec<real>::load(cxp + (size_t)k * PPW * (R * 4), cx[k]);
+    }
+  }
+  if (lane < 16) sQ[lane] = (real)p.Q[part * 16 + lane];
+  if (lane < 4) sF[lane] = (real)p.freqs[part * 4 + lane];
+  if (lane < R) {
+    sRW[lane] = (real)p.rate_weights[part * R + lane];
+    sRate[lane] = (real)p.rates[part * R + lane];
+  }
+  stage_pmats_warp<real, R>(sP, static_cast<const real *>(p.pmat) + (size_t)part * p.n_edges * (R * 16), op.ea,
+                            fake ? -1 : op.eb, lane);  // its __syncwarp also publishes sQ
+
+  const real rw = sRW[r];
+  if (op.seed >= 0) {
+    // d(w_s log L_s)/d clv_x = w_s rw_r pi_i / L_s, times the tree weight
+    const real sd = (real)p.seeds[(size_t)op.seed * p.n_parts + part];
 #pragma unroll
-          for (int k = 0; k < kPPL; ++k)
+    for (int k = 0; k < kPPL; ++k) {
+      real t = rw * (sF[0] * cx[k][0] + sF[1] * cx[k][1] + sF[2] * cx[k][2] + sF[3] * cx[k][3]);
+      t = rate_sum<R>(t);
+      const real sw = sd * (real)p.weights[g0 + (size_t)k * PPW];
+      if (t > (real)0 && sw != (real)0) {
+        const real f = sw * rw / t;
 #pragma unroll
-            for (int i = 0; i < 4; ++i) pb[k][i] = 1;
-        }
-        real ua[kPPL][4], ub[kPPL][4];
-        real ga = 0, gb = 0;
-#pragma unroll
-        for (int k = 0; k < kPPL; ++k) {
-          const int sh = sx[j][k] - sa[j][k] - sb[j][k];
-#pragma unroll
-          for (int i = 0; i < 4; ++i) {
-            ua[k][i] = ax[j][k][i] * pb[k][i];
-            ub[k][i] = ax[j][k][i] * pa[k][i];
-          }
-          if (sh != 0) {
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-              ua[k][i] = Scale<real>::shift(ua[k][i], sh);
-              ub[k][i] = Scale<real>::shift(ub[k][i], sh);
-            }
-          }
-          // d/dt of P(t r) c = r Q P(t r) c
-#pragma unroll
-          for (int i = 0; i < 4; ++i) {
-            const real qa = Q[4 * i] * pa[k][0] + Q[4 * i + 1] * pa[k][1] + Q[4 * i + 2] * pa[k][2] +
-                            Q[4 * i + 3] * pa[k][3];
-            ga += ua[k][i] * qa;
-            if (!fake) {
-              const real qb = Q[4 * i] * pb[k][0] + Q[4 * i + 1] * pb[k][1] + Q[4 * i + 2] * pb[k][2] +
-                              Q[4 * i + 3] * pb[k][3];
-              gb += ub[k][i] * qb;
-            }
-          }
-        }
-        ga = warp_sum(ga * rate);
-        if (lane == 0) my[op[j].ea] += (double)ga;
-        if (!fake) {
-          gb = warp_sum(gb * rate);
-          if (lane == 0) my[op[j].eb] += (double)gb;
-        }
-        if (op[j].out_a >= 0) {
-          real na[kPPL][4];
-          matvec2_t<real>(Pa, ua, na);
-          real *dst = msg + (size_t)op[j].out_a * N * (R * 4) + lane_off;
-#pragma unroll
-          for (int k = 0; k < kPPL; ++k) Vec<real>::store(dst + (size_t)k * PPW * (R * 4), na[k]);
-        }
-        if (op[j].out_b >= 0) {
-          real nb[kPPL][4];
-          matvec2_t<real>(pm + (size_t)op[j].eb * (R * 16), ub, nb);
-          real *dst = msg + (size_t)op[j].out_b * N * (R * 4) + lane_off;
-#pragma unroll
-          for (int k = 0; k < kPPL; ++k) Vec<real>::store(dst + (size_t)k * PPW * (R * 4), nb[k]);
-        }
+        for (int i = 0; i < 4; ++i) ax[k][i] += f * sF[i];
       }
     }
   }
-  __syncthreads();
-  for (int e = threadIdx.x; e < p.n_edges; e += blockDim.x) {
-    double s = 0.0;
-    for (int w = 0; w < THREADS / 32; ++w) s += sgrad[(size_t)w * p.n_edges + e];
-    p.grad_partial[(size_t)blockIdx.x * p.n_edges + e] = s;
+  const real *Pa = sP + r * 16;
+  const real *Pb = sP + R * 16 + r * 16;
+  real pa[kPPL][4], pb[kPPL][4];
+  matvec2_s<real>(Pa, ca, pa);
+  if (!fake) {
+    matvec2_s<real>(Pb, cb, pb);
+  } else {
+#pragma unroll
+    for (int k = 0; k < kPPL; ++k)
+#pragma unroll
+      for (int i = 0; i < 4; ++i) pb[k][i] = 1;
+  }
+  real ua[kPPL][4], ub[kPPL][4];
+  real ga = 0, gb = 0;
+#pragma unroll
+  for (int k = 0; k < kPPL; ++k) {
+    const int sh = sx[k] - sa[k] - sb[k];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      ua[k][i] = ax[k][i] * pb[k][i];
+      ub[k][i] = ax[k][i] * pa[k][i];
+    }
+    if (sh != 0) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        ua[k][i] = Scale<real>::shift(ua[k][i], sh);
+        ub[k][i] = Scale<real>::shift(ub[k][i], sh);
+      }
+    }
+    // d/dt of P(t r) c = r Q P(t r) c
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const real qa = sQ[4 * i] * pa[k][0] + sQ[4 * i + 1] * pa[k][1] + sQ[4 * i + 2] * pa[k][2] + sQ[4 * i + 3] * pa[k][3];
+      ga += ua[k][i] * qa;
+      if (!fake) {
+        const real qb = sQ[4 * i] * pb[k][0] + sQ[4 * i + 1] * pb[k][1] + sQ[4 * i + 2] * pb[k][2] + sQ[4 * i + 3] * pb[k][3];
+        gb += ub[k][i] * qb;
+      }
+    }
+  }
+  if (op.out_a >= 0) {
+    real na[kPPL][4];
+    matvec2_ts<real>(Pa, ua, na);
+    real *d = msg + (size_t)op.out_a * N * (R * 4) + lane_off;
+#pragma unroll
+    for (int k = 0; k < kPPL; ++k) Vec<real>::store(d + (size_t)k * PPW * (R * 4), na[k]);
+  }
+  if (op.out_b >= 0) {
+    real nb[kPPL][4];
+    matvec2_ts<real>(Pb, ub, nb);
+    real *d = msg + (size_t)op.out_b * N * (R * 4) + lane_off;
+#pragma unroll
+    for (int k = 0; k < kPPL; ++k) Vec<real>::store(d + (size_t)k * PPW * (R * 4), nb[k]);
+  }
+  ga = warp_sum(ga * sRate[r]);
+  gb = warp_sum(gb * sRate[r]);
+  if (lane == 0) {
+    // per-warp edge terms, reduced in a fixed order by op_reduce_kernel
+    p.grad_partial[((size_t)opi * p.n_units + unit) * 2] = (double)ga;
+    p.grad_partial[((size_t)opi * p.n_units + unit) * 2 + 1] = (double)gb;
   }
 }
 
@@ -600,11 +630,43 @@ __global__ void mix_kernel(const MixParams m) {
   }
 }
 
-__global__ void grad_reduce_kernel(int n_blocks, int n_edges, const double *partial, double *grad) {
+// Gradient reduction in two fixed-order stages: per adjoint op, the block
+// partials of its launch (grid_partial[op][b][side]) -> op_sum[op][side];
+// then per edge e, the op sides that use it (CSR edge_entries[edge_begin[e] ..
+// edge_begin[e+1]) = op * 2 + side) -> d logL / d t_e.
+__global__ void op_reduce_kernel(int n_bx, const double *__restrict__ partial, double *__restrict__ op_sum) {
+  const int op = blockIdx.x;
+  __shared__ double ra[128], rb[128];
+  const double2 *src = reinterpret_cast<const double2 *>(partial) + (size_t)op * n_bx;
+  double a = 0.0, b = 0.0;
+  for (int i = threadIdx.x; i < n_bx; i += blockDim.x) {
+    const double2 v = src[i];
+    a += v.x;
+    b += v.y;
+  }
+  ra[threadIdx.x] = a;
+  rb[threadIdx.x] = b;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      ra[threadIdx.x] += ra[threadIdx.x + o];
+      rb[threadIdx.x] += rb[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    op_sum[2 * op] = ra[0];
+    op_sum[2 * op + 1] = rb[0];
+  }
+}
+
+__global__ void edge_reduce_kernel(int n_edges, const int32_t *__restrict__ edge_begin,
+                                   const int32_t *__restrict__ edge_entries, const double *__restrict__ op_sum,
+                                   double *__restrict__ grad) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n_edges) return;
   double s = 0.0;
-  for (int b = 0; b < n_blocks; ++b) s += partial[(size_t)b * n_edges + e];
+  for (int q = edge_begin[e]; q < edge_begin[e + 1]; ++q) s += op_sum[edge_entries[q]];
   grad[e] = s;
 }
 
@@ -614,41 +676,29 @@ __global__ void grad_reduce_kernel(int n_blocks, int n_edges, const double *part
 struct Shape {
   int threads, minb;
 };
-constexpr Shape kShapes[] = {{128, 2}, {128, 3}, {128, 4}, {256, 1}, {64, 6}};
+constexpr Shape kShapes[] = {{256, 4}, {128, 8}, {256, 3}, {128, 6}, {64, 12}};
 constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
 
 template <typename real, int R, int T, int M>
-size_t bwd_smem(int n_edges) {
-  const size_t smem = (size_t)(T / 32) * n_edges * sizeof(double);
-  if (smem > 48 * 1024)
-    cudaFuncSetAttribute(backward_kernel<real, R, T, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  return smem;
-}
-
-template <typename real, int R, int T, int M>
 struct FwdRun {
-  static int run(cudaStream_t s, int grid, const SweepParams &p) {
-    forward_kernel<real, R, T, M><<<grid, T, 0, s>>>(p);
+  static int run(cudaStream_t s, const SweepParams &p, const int32_t *level_begin, int n_levels) {
+    const int bx = (p.n_units + T / 32 - 1) / (T / 32);
+    for (int L = 0; L < n_levels; ++L) {
+      const int n = level_begin[L + 1] - level_begin[L];
+      if (n > 0) forward_kernel<real, R, T, M><<<dim3(bx, n), T, 0, s>>>(p, level_begin[L]);
+    }
     return 0;
   }
 };
 template <typename real, int R, int T, int M>
 struct BwdRun {
-  static int run(cudaStream_t s, int grid, const SweepParams &p) {
-    backward_kernel<real, R, T, M><<<grid, T, bwd_smem<real, R, T, M>(p.n_edges), s>>>(p);
+  static int run(cudaStream_t s, const SweepParams &p, const int32_t *level_begin, int n_levels) {
+    const int bx = (p.n_units + T / 32 - 1) / (T / 32);
+    for (int L = 0; L < n_levels; ++L) {
+      const int n = level_begin[L + 1] - level_begin[L];
+      if (n > 0) backward_kernel<real, R, T, M><<<dim3(bx, n), T, 0, s>>>(p, level_begin[L]);
+    }
     return 0;
-  }
-};
-template <typename real, int R, int T, int M>
-struct OccRun {
-  static int run(bool backward, int n_edges) {
-    int nb = 0;
-    if (backward)
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, backward_kernel<real, R, T, M>, T,
-                                                    bwd_smem<real, R, T, M>(n_edges));
-    else
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, forward_kernel<real, R, T, M>, T, 0);
-    return nb;
   }
 };
 template <typename real, int R, int T, int M>
@@ -661,25 +711,25 @@ template <template <typename, int, int, int> class F, class... A>
 int dispatch(int precision, int R, int shape, A &&...a) {
   if (precision == 1 && R == 4) {
     switch (shape) {
-      case 1: return F<float, 4, 128, 3>::run(a...);
-      case 2: return F<float, 4, 128, 4>::run(a...);
-      case 3: return F<float, 4, 256, 1>::run(a...);
-      case 4: return F<float, 4, 64, 6>::run(a...);
-      default: return F<float, 4, 128, 2>::run(a...);
+      case 1: return F<float, 4, 128, 8>::run(a...);
+      case 2: return F<float, 4, 256, 3>::run(a...);
+      case 3: return F<float, 4, 128, 6>::run(a...);
+      case 4: return F<float, 4, 64, 12>::run(a...);
+      default: return F<float, 4, 256, 4>::run(a...);
     }
   }
   if (precision == 1) {
     switch (R) {
-      case 1: return F<float, 1, 128, 2>::run(a...);
-      case 2: return F<float, 2, 128, 2>::run(a...);
-      default: return F<float, 8, 128, 2>::run(a...);
+      case 1: return F<float, 1, 256, 4>::run(a...);
+      case 2: return F<float, 2, 256, 4>::run(a...);
+      default: return F<float, 8, 256, 4>::run(a...);
     }
   }
   switch (R) {
-    case 1: return F<double, 1, 128, 2>::run(a...);
-    case 2: return F<double, 2, 128, 2>::run(a...);
-    case 4: return F<double, 4, 128, 2>::run(a...);
-    default: return F<double, 8, 128, 2>::run(a...);
+    case 1: return F<double, 1, 256, 2>::run(a...);
+    case 2: return F<double, 2, 256, 2>::run(a...);
+    case 4: return F<double, 4, 256, 2>::run(a...);
+    default: return F<double, 8, 256, 2>::run(a...);
   }
 }
 
@@ -689,19 +739,16 @@ int num_shapes(int precision, int R) { return (precision == 1 && R == 4) ? kNumS
 
 int shape_threads(int precision, int R, int shape) { return dispatch<ThreadsRun>(precision, R, shape); }
 
-void launch_forward(cudaStream_t s, int precision, int R, int shape, int grid, const SweepParams &p) {
-  dispatch<FwdRun>(precision, R, shape, s, grid, p);
-  g_launches++;
+void launch_forward(cudaStream_t s, int precision, int R, int shape, const SweepParams &p,
+                    const int32_t *level_begin, int n_levels) {
+  dispatch<FwdRun>(precision, R, shape, s, p, level_begin, n_levels);
+  for (int L = 0; L < n_levels; ++L) g_launches += level_begin[L + 1] > level_begin[L];
 }
 
-void launch_backward(cudaStream_t s, int precision, int R, int shape, int grid, const SweepParams &p) {
-  dispatch<BwdRun>(precision, R, shape, s, grid, p);
-  g_launches++;
-}
-
-int max_resident_blocks(int precision, int R, int shape, bool backward, int n_edges) {
-  const int nb = dispatch<OccRun>(precision, R, shape, backward, n_edges);
-  return nb < 1 ? 1 : nb;
+void launch_backward(cudaStream_t s, int precision, int R, int shape, const SweepParams &p,
+                     const int32_t *level_begin, int n_levels) {
+  dispatch<BwdRun>(precision, R, shape, s, p, level_begin, n_levels);
+  for (int L = 0; L < n_levels; ++L) g_launches += level_begin[L + 1] > level_begin[L];
 }
 
 void launch_pmatrix(cudaStream_t s, int n_parts, int n_edges, int R, const double *lambda, const double *U,
@@ -724,9 +771,11 @@ void launch_mix(cudaStream_t s, const MixParams &m) {
   g_launches++;
 }
 
-void launch_grad_reduce(cudaStream_t s, int n_blocks, int n_edges, const double *partial, double *grad) {
-  grad_reduce_kernel<<<(n_edges + 127) / 128, 128, 0, s>>>(n_blocks, n_edges, partial, grad);
-  g_launches++;
+void launch_grad_reduce(cudaStream_t s, int n_ops, int n_edges, int n_bx, const int32_t *edge_begin,
+                        const int32_t *edge_entries, const double *partial, double *op_sum, double *grad) {
+  op_reduce_kernel<<<n_ops, 128, 0, s>>>(n_bx, partial, op_sum);
+  edge_reduce_kernel<<<(n_edges + 127) / 128, 128, 0, s>>>(n_edges, edge_begin, edge_entries, op_sum, grad);
+  g_launches += 2;
 }
 
 }  // namespace netlk

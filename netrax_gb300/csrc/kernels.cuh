@@ -6,17 +6,12 @@
 
 namespace netlk {
 
-// Ops per unrolled group of the forward / adjoint sweeps: the host pads every
-// level of each schedule to a multiple of its group size with no-op entries
-// (out / x == -1). All loads of a group are issued before any of its results
-// is computed, so the host never puts an op and its consumer in one group.
-constexpr int kFwdGroup = 4;
-constexpr int kBwdGroup = 2;
 // Patterns per lane: a lane handles rate r of patterns s and s + 32/R of its
 // unit, so one P-row load and one op decode serve two patterns.
 constexpr int kPPL = 2;
-// Partitions are padded to whole multiples of this many patterns.
-constexpr int kPatternAlign = 64;
+// Blocks have at most 8 warps (one unit each); partitions are padded to a
+// whole number of 8-unit blocks so that a block never spans two partitions.
+constexpr int kMaxWarpsPerBlock = 8;
 constexpr int kThreads = 256;
 
 // Forward op: CLV of variant `out` = (P[ea] . child a) (*) (P[eb] . child b).
@@ -32,7 +27,8 @@ struct alignas(32) FwdOp {
 // (msg_slots[msg_begin .. msg_begin + msg_count)); x then writes one message
 // per inner child (out_a / out_b: message slot, or -1) and adds its two edge
 // gradient terms. seed: displayed-tree root slot whose tree weight seeds x,
-// or -1. Message buffers are reused once their reader has run.
+// or -1. A message buffer is reused only by levels launched after the level
+// that read it.
 struct alignas(64) BwdOp {
   int32_t x, a, b, ea, eb, seed, out_a, out_b;
   int32_t msg_begin, msg_count, pad0, pad1, pad2, pad3, pad4, pad5;
@@ -44,7 +40,7 @@ struct DevPartition {
 
 // Everything the sweeps read, in device memory.
 struct SweepParams {
-  int32_t n_units;      // pattern groups of kPPL*32/R patterns (one per warp pass)
+  int32_t n_units;      // pattern groups of kPPL*32/R patterns (one per warp and op)
   int64_t n_patterns;   // padded total (N)
   int32_t n_edges;
   int32_t n_fwd_ops;
@@ -66,7 +62,7 @@ struct SweepParams {
   const int32_t *msg_slots;     // message slots read by the adjoint ops
   double *site_partial;         // [n_slots][n_units]
   const double *seeds;          // [n_slots][n_parts]
-  double *grad_partial;         // [gridDim][n_edges]
+  double *grad_partial;         // [n_bwd_ops][n_units][2] per-warp edge terms (a, b)
 };
 
 struct MixParams {
@@ -92,12 +88,15 @@ void launch_pmatrix(cudaStream_t s, int n_parts, int n_edges, int R, const doubl
 // the default; num_shapes() > 1 where the autotuner has alternatives.
 int num_shapes(int precision, int R);
 int shape_threads(int precision, int R, int shape);
-void launch_forward(cudaStream_t s, int precision, int R, int shape, int grid, const SweepParams &p);
-void launch_backward(cudaStream_t s, int precision, int R, int shape, int grid, const SweepParams &p);
+// One launch per level: ops [level_begin[L], level_begin[L+1]) of the schedule.
+void launch_forward(cudaStream_t s, int precision, int R, int shape, const SweepParams &p,
+                    const int32_t *level_begin, int n_levels);
+void launch_backward(cudaStream_t s, int precision, int R, int shape, const SweepParams &p,
+                     const int32_t *level_begin, int n_levels);
 void launch_tree_reduce(cudaStream_t s, const MixParams &m);
 void launch_mix(cudaStream_t s, const MixParams &m);
-void launch_grad_reduce(cudaStream_t s, int n_blocks, int n_edges, const double *partial, double *grad);
-int max_resident_blocks(int precision, int R, int shape, bool backward, int n_edges);
+void launch_grad_reduce(cudaStream_t s, int n_ops, int n_edges, int n_bx, const int32_t *edge_begin,
+                        const int32_t *edge_entries, const double *partial, double *op_sum, double *grad);
 // Number of kernel launches issued by the launchers above (host counter).
 int64_t launches_issued();
 

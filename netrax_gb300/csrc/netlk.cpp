@@ -11,6 +11,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -95,7 +97,9 @@ struct netlk_ctx {
   std::vector<BwdOp> bwd;
   int n_slots = 0, n_adj = 0, n_bwd_real = 0;
   std::vector<int32_t> root_slot, slot_begin, slot_roots, msg_slots;
-  int grid_fwd = 0, grid_bwd = 0;
+  std::vector<int32_t> fwd_level_begin, bwd_level_begin;  // op ranges per launch
+  std::vector<int32_t> edge_begin, edge_entries;         // edge -> adjoint op sides
+  int fwd_launches = 0, bwd_launches = 0;
   int fwd_shape = 0, bwd_shape = 0, sms = 0;
   bool tuned = false;
   std::vector<double> tune_fwd_ms, tune_bwd_ms;
@@ -107,7 +111,7 @@ struct netlk_ctx {
   DevBuf d_clv, d_scaler, d_adj, d_msg_slots, d_tips, d_weights, d_unit_part, d_fwd, d_bwd;
   DevBuf d_pmat64, d_pmat32, d_lambda, d_U, d_Uinv, d_rates, d_rw, d_freqs, d_Q, d_brlen;
   DevBuf d_site_partial, d_tree_logl, d_root_slot, d_root_lp, d_root_dlp, d_seeds, d_wts;
-  DevBuf d_slot_begin, d_slot_roots, d_parts, d_out, d_grad_partial, d_grad;
+  DevBuf d_slot_begin, d_slot_roots, d_parts, d_out, d_grad_partial, d_grad, d_edge_begin, d_edge_entries, d_op_sum;
   PinnedBuf h_brlen, h_root_lp, h_root_dlp, h_out, h_grad, h_tree;
   cudaGraphExec_t graph_logl = nullptr, graph_grad = nullptr, graph_partials = nullptr,
                   graph_mixbwd = nullptr;
@@ -158,7 +162,8 @@ struct netlk_ctx {
     for (DevBuf *b : {&d_clv, &d_scaler, &d_adj, &d_msg_slots, &d_tips, &d_weights, &d_unit_part, &d_fwd, &d_bwd,
                       &d_pmat64, &d_pmat32, &d_lambda, &d_U, &d_Uinv, &d_rates, &d_rw, &d_freqs, &d_Q,
                       &d_brlen, &d_site_partial, &d_tree_logl, &d_root_slot, &d_root_lp, &d_root_dlp,
-                      &d_seeds, &d_wts, &d_slot_begin, &d_slot_roots, &d_parts, &d_out, &d_grad_partial, &d_grad})
+                      &d_seeds, &d_wts, &d_slot_begin, &d_slot_roots, &d_parts, &d_out, &d_grad_partial, &d_grad,
+                      &d_edge_begin, &d_edge_entries, &d_op_sum})
       b->free();
     if (stream) cudaStreamDestroy(stream);
   }
@@ -214,16 +219,6 @@ struct netlk_ctx {
     return m;
   }
 
-  // Persistent grid for a sweep: as many resident warps as fit, with the
-  // units spread evenly (every warp gets the same number of passes).
-  int grid_for(bool backward, int shape) const {
-    const int per_sm = max_resident_blocks(opts.precision, R, shape, backward, topo.n_edges);
-    const int wpb = shape_threads(opts.precision, R, shape) / 32;
-    const int64_t resident_warps = (int64_t)per_sm * sms * wpb;
-    const int64_t rounds = (n_units + resident_warps - 1) / resident_warps;
-    const int64_t warps = (n_units + rounds - 1) / rounds;
-    return (int)std::max<int64_t>(1, (warps + wpb - 1) / wpb);
-  }
   void autotune();
   void build_schedules();
   void allocate_and_upload(const netlk_partition *in_parts);
@@ -258,6 +253,7 @@ void netlk_ctx::build_schedules() {
   std::vector<std::vector<int>> by_level(dag.n_levels + 1);
   for (int v = 0; v < V; ++v) by_level[dag.vars[v].level].push_back(v);
   fwd.clear();
+  fwd_level_begin.assign(1, 0);
   tip_uses = fake_uses = 0;
   for (int L = 1; L <= dag.n_levels; ++L) {
     for (int v : by_level[L]) {
@@ -267,8 +263,10 @@ void netlk_ctx::build_schedules() {
       tip_uses += is_tip_ref(var.ref[0]) + is_tip_ref(var.ref[1]);
       fake_uses += var.ref[1] == kFake;
     }
-    while (fwd.size() % kFwdGroup) fwd.push_back(FwdOp{-1, 0, 0, 0, 0, -1, 0, 0});
+    fwd_level_begin.push_back((int32_t)fwd.size());
   }
+  fwd_launches = 0;
+  for (int L = 0; L < dag.n_levels; ++L) fwd_launches += fwd_level_begin[L + 1] > fwd_level_begin[L];
   site_updates = (int64_t)V * N;
   const int64_t clv_b = (int64_t)R * S * (opts.precision == NETLK_FP32 ? 4 : 8);
   auto child_bytes = [&](int32_t ref) -> int64_t {
@@ -278,7 +276,6 @@ void netlk_ctx::build_schedules() {
   };
   fwd_bytes = 0;
   for (const FwdOp &op : fwd) {
-    if (op.out < 0) continue;
     fwd_bytes += N * (clv_b + 4 + child_bytes(op.a) + child_bytes(op.b));
     if (op.slot >= 0) fwd_bytes += (int64_t)n_units * 8;
   }
@@ -292,73 +289,79 @@ void netlk_ctx::build_schedules() {
           if (dag.vars[v].ref[i] >= 0) inb[dag.vars[v].ref[i]] = 1;
   bwd.clear();
   msg_slots.clear();
+  bwd_level_begin.assign(1, 0);
   n_bwd_real = 0;
   bwd_bytes = 0;
   n_adj = 0;  // message buffers after liveness reuse
   std::vector<std::vector<int32_t>> pending(V);  // message slots waiting for each variant
   std::vector<int> free_slots;
-  auto alloc_slot = [&]() {
-    if (!free_slots.empty()) {
-      int s = free_slots.back();
-      free_slots.pop_back();
-      return s;
-    }
-    return n_adj++;
-  };
   for (int L = dag.n_levels; L >= 1; --L) {
-    std::vector<int> ops;
-    for (int v : by_level[L])
-      if (inb[v]) ops.push_back(v);
-    for (size_t g0 = 0; g0 < ops.size(); g0 += kBwdGroup) {
-      const size_t g1 = std::min(ops.size(), g0 + kBwdGroup);
-      const size_t base = bwd.size();
-      // phase 1 of the kernel: every op of the group reads its messages
-      for (size_t j = g0; j < g1; ++j) {
-        const int x = ops[j];
-        BwdOp op{};
-        op.x = x;
-        op.a = dag.vars[x].ref[0];
-        op.b = dag.vars[x].ref[1];
-        op.ea = dag.vars[x].edge[0];
-        op.eb = dag.vars[x].edge[1];
-        op.seed = slot_of[x];
-        op.out_a = op.out_b = -1;
-        op.msg_begin = (int32_t)msg_slots.size();
-        op.msg_count = (int32_t)pending[x].size();
-        for (int32_t m : pending[x]) msg_slots.push_back(m);
-        bwd.push_back(op);
-        n_bwd_real++;
+    const size_t base = bwd.size();
+    std::vector<int32_t> read_here;
+    for (int x : by_level[L]) {
+      if (!inb[x]) continue;
+      BwdOp op{};
+      op.x = x;
+      op.a = dag.vars[x].ref[0];
+      op.b = dag.vars[x].ref[1];
+      op.ea = dag.vars[x].edge[0];
+      op.eb = dag.vars[x].edge[1];
+      op.seed = slot_of[x];
+      op.out_a = op.out_b = -1;
+      op.msg_begin = (int32_t)msg_slots.size();
+      op.msg_count = (int32_t)pending[x].size();
+      for (int32_t m : pending[x]) {
+        msg_slots.push_back(m);
+        read_here.push_back(m);
       }
-      for (size_t j = g0; j < g1; ++j) {
-        for (int32_t m : pending[ops[j]]) free_slots.push_back(m);
-        pending[ops[j]].clear();
+      pending[x].clear();
+      bwd.push_back(op);
+      n_bwd_real++;
+    }
+    // outputs of this level take buffers freed by earlier levels only: the
+    // ops of one launch run concurrently
+    auto alloc_slot = [&]() {
+      if (!free_slots.empty()) {
+        int s = free_slots.back();
+        free_slots.pop_back();
+        return s;
       }
-      // phase 2: one fresh message buffer per inner child
-      for (size_t j = g0; j < g1; ++j) {
-        BwdOp &op = bwd[base + (j - g0)];
-        if (op.a >= 0) {
-          op.out_a = alloc_slot();
-          pending[op.a].push_back(op.out_a);
-        }
-        if (op.b >= 0) {
-          op.out_b = alloc_slot();
-          pending[op.b].push_back(op.out_b);
-        }
+      return n_adj++;
+    };
+    for (size_t j = base; j < bwd.size(); ++j) {
+      BwdOp &op = bwd[j];
+      if (op.a >= 0) {
+        op.out_a = alloc_slot();
+        pending[op.a].push_back(op.out_a);
       }
-      for (size_t j = base; j < bwd.size(); ++j) {
-        const BwdOp &op = bwd[j];
-        int64_t b = 4 + child_bytes(op.a) + child_bytes(op.b) + (int64_t)op.msg_count * clv_b;
-        if (op.seed >= 0) b += clv_b;
-        if (op.out_a >= 0) b += clv_b;
-        if (op.out_b >= 0) b += clv_b;
-        bwd_bytes += N * b;
+      if (op.b >= 0) {
+        op.out_b = alloc_slot();
+        pending[op.b].push_back(op.out_b);
       }
-      while (bwd.size() % kBwdGroup) {
-        BwdOp nop{};
-        nop.x = -1;
-        nop.seed = nop.out_a = nop.out_b = -1;
-        bwd.push_back(nop);
-      }
+      int64_t b = 4 + child_bytes(op.a) + child_bytes(op.b) + (int64_t)op.msg_count * clv_b;
+      if (op.seed >= 0) b += clv_b;
+      if (op.out_a >= 0) b += clv_b;
+      if (op.out_b >= 0) b += clv_b;
+      bwd_bytes += N * b;
+    }
+    for (int32_t m : read_here) free_slots.push_back(m);
+    bwd_level_begin.push_back((int32_t)bwd.size());
+  }
+  bwd_launches = 0;
+  for (int L = 0; L < dag.n_levels; ++L) bwd_launches += bwd_level_begin[L + 1] > bwd_level_begin[L];
+  // edge -> (adjoint op, side) entries for the gradient reduction
+  edge_begin.assign(topo.n_edges + 1, 0);
+  for (const BwdOp &op : bwd) {
+    edge_begin[op.ea + 1]++;
+    if (op.b != kFake) edge_begin[op.eb + 1]++;
+  }
+  for (int e = 0; e < topo.n_edges; ++e) edge_begin[e + 1] += edge_begin[e];
+  edge_entries.assign(edge_begin.back(), 0);
+  {
+    std::vector<int32_t> fill(edge_begin.begin(), edge_begin.end() - 1);
+    for (size_t j = 0; j < bwd.size(); ++j) {
+      edge_entries[fill[bwd[j].ea]++] = (int32_t)(2 * j);
+      if (bwd[j].b != kFake) edge_entries[fill[bwd[j].eb]++] = (int32_t)(2 * j + 1);
     }
   }
 }
@@ -367,11 +370,13 @@ void netlk_ctx::build_schedules() {
 void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
   const int V = (int)dag.vars.size();
   ppw = (32 / R) * kPPL;  // patterns per unit (one warp pass)
-  // patterns: every partition padded to whole kPatternAlign-pattern blocks
+  // patterns: every partition padded to whole blocks of the largest launch
+  // shape (8 warps x one unit each), so a block never spans two partitions
+  const int align = 8 * ppw;
   N = 0;
   n_units = 0;
   for (auto &pi : parts) {
-    pi.n_pad = (pi.n + kPatternAlign - 1) / kPatternAlign * kPatternAlign;
+    pi.n_pad = (pi.n + align - 1) / align * align;
     pi.offset = N;
     pi.unit_begin = (int)(N / ppw);
     N += pi.n_pad;
@@ -436,11 +441,14 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
 
   CUDA_OK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
   fwd_shape = bwd_shape = 0;
-  grid_fwd = grid_for(false, 0);
-  grid_bwd = grid_for(true, 0);
-  int max_bwd_grid = 0;
-  for (int sh = 0; sh < num_shapes(opts.precision, R); ++sh) max_bwd_grid = std::max(max_bwd_grid, grid_for(true, sh));
-  d_grad_partial.alloc((size_t)max_bwd_grid * topo.n_edges * 8, dev_bytes);
+  d_grad_partial.alloc(std::max<size_t>(1, bwd.size()) * n_units * 2 * 8, dev_bytes);
+  d_op_sum.alloc(std::max<size_t>(1, bwd.size()) * 2 * 8, dev_bytes);
+  d_edge_begin.alloc(edge_begin.size() * 4, dev_bytes);
+  d_edge_entries.alloc(std::max<size_t>(1, edge_entries.size()) * 4, dev_bytes);
+  CUDA_OK(cudaMemcpyAsync(d_edge_begin.p, edge_begin.data(), edge_begin.size() * 4, cudaMemcpyHostToDevice, stream));
+  if (!edge_entries.empty())
+    CUDA_OK(cudaMemcpyAsync(d_edge_entries.p, edge_entries.data(), edge_entries.size() * 4,
+                            cudaMemcpyHostToDevice, stream));
 
   std::vector<DevPartition> dparts(P);
   for (int p = 0; p < P; ++p) dparts[p] = DevPartition{parts[p].unit_begin, parts[p].unit_end};
@@ -517,7 +525,7 @@ void netlk_ctx::enqueue(bool pm, bool fwd_on, bool reduce, bool mixk, bool bwd_o
   const SweepParams sp = sweep();
   const MixParams mp = mix();
   if (fwd_on) {
-    launch_forward(stream, opts.precision, R, fwd_shape, grid_fwd, sp);
+    launch_forward(stream, opts.precision, R, fwd_shape, sp, fwd_level_begin.data(), dag.n_levels);
     prof_mark(1);
   }
   if (reduce) {
@@ -529,15 +537,18 @@ void netlk_ctx::enqueue(bool pm, bool fwd_on, bool reduce, bool mixk, bool bwd_o
     prof_mark(3);
   }
   if (bwd_on && !bwd.empty()) {
-    launch_backward(stream, opts.precision, R, bwd_shape, grid_bwd, sp);
+    launch_backward(stream, opts.precision, R, bwd_shape, sp, bwd_level_begin.data(), dag.n_levels);
     prof_mark(4);
-    launch_grad_reduce(stream, grid_bwd, topo.n_edges, d_grad_partial.as<double>(), d_grad.as<double>());
+    launch_grad_reduce(stream, (int)bwd.size(), topo.n_edges, n_units, d_edge_begin.as<int32_t>(),
+                       d_edge_entries.as<int32_t>(), d_grad_partial.as<double>(), d_op_sum.as<double>(),
+                       d_grad.as<double>());
     prof_mark(5);
   }
 }
 
 void netlk_ctx::run(cudaGraphExec_t *cache, bool pm, bool fwd_on, bool reduce, bool mixk, bool bwd_on) {
-  const int n = (int)pm + (int)fwd_on + (int)reduce + (int)mixk + (bwd_on && !bwd.empty() ? 2 : 0);
+  const int n = (int)pm + (fwd_on ? fwd_launches : 0) + (int)reduce + (int)mixk +
+                (bwd_on && !bwd.empty() ? bwd_launches + 2 : 0);
   if (!opts.use_cuda_graph || profiling) {
     enqueue(pm, fwd_on, reduce, mixk, bwd_on);
     launches += n;
@@ -564,6 +575,14 @@ void netlk_ctx::autotune() {
   const int ns = num_shapes(opts.precision, R);
   tune_fwd_ms.assign(ns, 0.0);
   tune_bwd_ms.assign(ns, 0.0);
+  if (const char *forced = std::getenv("NETLK_SHAPES")) {  // "fwd,bwd": fixed shapes, no timing
+    int f = 0, b = 0;
+    if (std::sscanf(forced, "%d,%d", &f, &b) == 2 && f >= 0 && f < ns && b >= 0 && b < ns) {
+      fwd_shape = f;
+      bwd_shape = b;
+      return;
+    }
+  }
   if (ns <= 1 || !opts.autotune) return;
   std::memcpy(h_brlen.p, brlen.data(), brlen.size() * 8);
   CUDA_OK(cudaMemcpyAsync(d_brlen.p, h_brlen.p, brlen.size() * 8, cudaMemcpyHostToDevice, stream));
@@ -573,14 +592,13 @@ void netlk_ctx::autotune() {
   CUDA_OK(cudaEventCreate(&e1));
   const SweepParams sp = sweep();
   auto time_one = [&](bool backward, int sh) {
-    const int grid = grid_for(backward, sh);
     float best = 1e30f;
     for (int rep = 0; rep < 2; ++rep) {
       CUDA_OK(cudaEventRecord(e0, stream));
       if (backward)
-        launch_backward(stream, opts.precision, R, sh, grid, sp);
+        launch_backward(stream, opts.precision, R, sh, sp, bwd_level_begin.data(), dag.n_levels);
       else
-        launch_forward(stream, opts.precision, R, sh, grid, sp);
+        launch_forward(stream, opts.precision, R, sh, sp, fwd_level_begin.data(), dag.n_levels);
       CUDA_OK(cudaEventRecord(e1, stream));
       CUDA_OK(cudaEventSynchronize(e1));
       float ms = 0.f;
@@ -596,8 +614,6 @@ void netlk_ctx::autotune() {
   cudaEventDestroy(e1);
   fwd_shape = (int)(std::min_element(tune_fwd_ms.begin(), tune_fwd_ms.end()) - tune_fwd_ms.begin());
   bwd_shape = (int)(std::min_element(tune_bwd_ms.begin(), tune_bwd_ms.end()) - tune_bwd_ms.begin());
-  grid_fwd = grid_for(false, fwd_shape);
-  grid_bwd = grid_for(true, bwd_shape);
 }
 
 void netlk_ctx::prepare() {
@@ -811,6 +827,7 @@ int netlk_get_dag_stats(const netlk_ctx *ctx, netlk_dag_stats *o) {
   o->tip_child_uses = ctx->tip_uses;
   o->fake_child_uses = ctx->fake_uses;
   o->device_bytes = ctx->dev_bytes;
+  o->launches_per_gradient_eval = 3 + ctx->fwd_launches + (ctx->bwd.empty() ? 0 : ctx->bwd_launches + 2);
   o->forward_bytes = ctx->fwd_bytes;
   o->backward_bytes = ctx->bwd_bytes;
   return NETLK_OK;
