@@ -147,13 +147,12 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def load_traffic():
-    path = os.path.join(ROOT, "profiles", "traffic.json")
-    try:
-        with open(path) as f:
-            return json.load(f)
-    except Exception:
-        return {}
+# DRAM bytes per site-CLV update of each sweep from one ncu capture
+# (profiles/sweep_dram_traffic_config2_scale0.3.md: dram__bytes_read.sum +
+# dram__bytes_write.sum of one evaluation's 16 level launches, same network at
+# 0.3 of its sites, scaled by updates; writes still dirty in L2 at a launch's
+# end are not counted).
+TRAFFIC_PER_UPDATE = {"forward_fp32": 101.2, "backward_fp32": 297.5}
 
 
 def cpu_port_rate(w, n_sample, steps, warmup, variant):
@@ -322,11 +321,10 @@ def run_netlk(args, ws, rank, local):
     dom = "backward" if kavg["backward"] >= kavg["forward"] else "forward"
     dom_bytes = bwd_b if dom == "backward" else fwd_b
     achieved = dom_bytes / (kavg[dom] * 1e-3) / 1e9 if kavg[dom] > 0 else 0.0
-    traffic_tab = load_traffic()
     traffic = None
-    tt = traffic_tab.get("%s_%s" % (dom, args.precision))
+    tt = TRAFFIC_PER_UPDATE.get("%s_%s" % (dom, args.precision))
     if tt:
-        traffic = tt["dram_bytes_per_site_update"] * st["site_clv_updates"]
+        traffic = tt * st["site_clv_updates"]
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "kernel": dom + "_kernel",
                 "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind if peak_kind == "measured"
