@@ -88,8 +88,8 @@ def lib():
     global _lib
     if _lib is not None:
         return _lib
-    path = _build.LIB
-    if not os.path.exists(path) or os.environ.get("NETLK_REBUILD"):
+    path = os.environ.get("NETLK_LIB") or _build.LIB  # NETLK_LIB: an alternative build
+    if not os.environ.get("NETLK_LIB") and (not os.path.exists(path) or os.environ.get("NETLK_REBUILD")):
         path = _build.build()
     L = ctypes.CDLL(path)
     vp = ctypes.c_void_p

@@ -110,21 +110,21 @@ struct Scale<double> {
 // its scale counters), a tip (state mask expanded to 0/1) or the fake all-ones
 // child. g0: the lane's first pattern, r: its rate; `stride` patterns
 // separate the lane's patterns.
-template <typename real, int R>
+template <typename real, int R, int PPL>
 __device__ __forceinline__ void load_child(const SweepParams &p, int32_t ref, size_t g0, int r, int stride,
-                                           real (&c)[kPPL][4], int (&s)[kPPL]) {
+                                           real (&c)[PPL][4], int (&s)[PPL]) {
   if (ref >= 0) {
     const real *clv = static_cast<const real *>(p.clv) + ((size_t)ref * p.n_patterns + g0) * (R * 4) + r * 4;
     const int32_t *sc = p.scaler + (size_t)ref * p.n_patterns + g0;
 #pragma unroll
-    for (int k = 0; k < kPPL; ++k) {
+    for (int k = 0; k < PPL; ++k) {
       Vec<real>::load(clv + (size_t)k * stride * (R * 4), c[k]);
       s[k] = sc[(size_t)k * stride];
     }
   } else if (ref != INT32_MIN) {
     const uint8_t *t = p.tips + (size_t)(-1 - ref) * p.n_patterns + g0;
 #pragma unroll
-    for (int k = 0; k < kPPL; ++k) {
+    for (int k = 0; k < PPL; ++k) {
       const unsigned code = t[(size_t)k * stride];
 #pragma unroll
       for (int i = 0; i < 4; ++i) c[k][i] = (real)((code >> i) & 1u);
@@ -132,7 +132,7 @@ __device__ __forceinline__ void load_child(const SweepParams &p, int32_t ref, si
     }
   } else {
 #pragma unroll
-    for (int k = 0; k < kPPL; ++k) {
+    for (int k = 0; k < PPL; ++k) {
 #pragma unroll
       for (int i = 0; i < 4; ++i) c[k][i] = (real)1;
       s[k] = 0;
@@ -141,35 +141,35 @@ __device__ __forceinline__ void load_child(const SweepParams &p, int32_t ref, si
 }
 
 // out[k] = P . c[k] for the lane's patterns (P: this lane's rate, row-major 4x4)
-template <typename real>
-__device__ __forceinline__ void matvec2(const real *P, const real (&c)[kPPL][4], real (&out)[kPPL][4]) {
+template <typename real, int PPL>
+__device__ __forceinline__ void matvec2(const real *P, const real (&c)[PPL][4], real (&out)[PPL][4]) {
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     real row[4];
     Vec<real>::ldg(P + 4 * i, row);
 #pragma unroll
-    for (int k = 0; k < kPPL; ++k)
+    for (int k = 0; k < PPL; ++k)
       out[k][i] = row[0] * c[k][0] + row[1] * c[k][1] + row[2] * c[k][2] + row[3] * c[k][3];
   }
 }
 
 // Same products with P read from shared memory.
-template <typename real>
-__device__ __forceinline__ void matvec2_s(const real *P, const real (&c)[kPPL][4], real (&out)[kPPL][4]) {
+template <typename real, int PPL>
+__device__ __forceinline__ void matvec2_s(const real *P, const real (&c)[PPL][4], real (&out)[PPL][4]) {
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     real row[4];
     Vec<real>::load(P + 4 * i, row);
 #pragma unroll
-    for (int k = 0; k < kPPL; ++k)
+    for (int k = 0; k < PPL; ++k)
       out[k][i] = row[0] * c[k][0] + row[1] * c[k][1] + row[2] * c[k][2] + row[3] * c[k][3];
   }
 }
 
-template <typename real>
-__device__ __forceinline__ void matvec2_ts(const real *P, const real (&u)[kPPL][4], real (&out)[kPPL][4]) {
+template <typename real, int PPL>
+__device__ __forceinline__ void matvec2_ts(const real *P, const real (&u)[PPL][4], real (&out)[PPL][4]) {
 #pragma unroll
-  for (int k = 0; k < kPPL; ++k)
+  for (int k = 0; k < PPL; ++k)
 #pragma unroll
     for (int j = 0; j < 4; ++j) out[k][j] = 0;
 #pragma unroll
@@ -177,17 +177,17 @@ __device__ __forceinline__ void matvec2_ts(const real *P, const real (&u)[kPPL][
     real row[4];
     Vec<real>::load(P + 4 * i, row);
 #pragma unroll
-    for (int k = 0; k < kPPL; ++k)
+    for (int k = 0; k < PPL; ++k)
 #pragma unroll
       for (int j = 0; j < 4; ++j) out[k][j] += row[j] * u[k][i];
   }
 }
 
 // out[k] = P^T . u[k]
-template <typename real>
-__device__ __forceinline__ void matvec2_t(const real *P, const real (&u)[kPPL][4], real (&out)[kPPL][4]) {
+template <typename real, int PPL>
+__device__ __forceinline__ void matvec2_t(const real *P, const real (&u)[PPL][4], real (&out)[PPL][4]) {
 #pragma unroll
-  for (int k = 0; k < kPPL; ++k)
+  for (int k = 0; k < PPL; ++k)
 #pragma unroll
     for (int j = 0; j < 4; ++j) out[k][j] = 0;
 #pragma unroll
@@ -195,7 +195,7 @@ __device__ __forceinline__ void matvec2_t(const real *P, const real (&u)[kPPL][4
     real row[4];
     Vec<real>::ldg(P + 4 * i, row);
 #pragma unroll
-    for (int k = 0; k < kPPL; ++k)
+    for (int k = 0; k < PPL; ++k)
 #pragma unroll
       for (int j = 0; j < 4; ++j) out[k][j] += row[j] * u[k][i];
   }
@@ -222,26 +222,36 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
+// P rows of one rate sit kPRow values apart in shared memory (16 used +
+// padding) so the four rate groups of a warp's LDS.128 hit distinct banks.
+template <typename real>
+struct PLayout {
+  static constexpr int kRow = (sizeof(real) == 4) ? 20 : 18;
+};
+
 // Stages the op's two P-matrices (all R rates) of one partition in the
-// warp's own shared-memory slice: sP[m][r][16], m = 0 for edge ea, 1 for edge
-// eb (zero for the fake child). 2*R*16 values = one 16-byte load per lane at
-// R = 4 in FP32; a __syncwarp (no block barrier) publishes them.
+// warp's own shared-memory slice: sP[(m*R + r)*kRow + 0..15], m = 0 for edge
+// ea, 1 for edge eb (zero for the fake child). 2*R*16 values = one 16-byte
+// load per lane at R = 4 in FP32; a __syncwarp (no block barrier) publishes them.
 template <typename real, int R>
 __device__ __forceinline__ void stage_pmats_warp(real *sP, const real *pm_part, int ea, int eb, int lane) {
   constexpr int V = 16 / sizeof(real);  // values per 16-byte vector
   constexpr int NV = 2 * R * 16 / V;
+  constexpr int ROW = PLayout<real>::kRow;
   for (int i = lane; i < NV; i += 32) {
     const int m = (i * V) / (R * 16), j = i * V - m * (R * 16);
+    const int rr = j / 16, c = j - rr * 16;
+    real *dst = sP + (m * R + rr) * ROW + c;
     const int e = m ? eb : ea;
     if (e >= 0) {
       if (sizeof(real) == 4) {
-        *reinterpret_cast<float4 *>(sP + i * V) = __ldg(reinterpret_cast<const float4 *>(pm_part + (size_t)e * (R * 16) + j));
+        *reinterpret_cast<float4 *>(dst) = __ldg(reinterpret_cast<const float4 *>(pm_part + (size_t)e * (R * 16) + j));
       } else {
-        *reinterpret_cast<double2 *>(sP + i * V) = __ldg(reinterpret_cast<const double2 *>(pm_part + (size_t)e * (R * 16) + j));
+        *reinterpret_cast<double2 *>(dst) = __ldg(reinterpret_cast<const double2 *>(pm_part + (size_t)e * (R * 16) + j));
       }
     } else {
 #pragma unroll
-      for (int q = 0; q < V; ++q) sP[i * V + q] = (real)0;
+      for (int q = 0; q < V; ++q) dst[q] = (real)0;
     }
   }
   __syncwarp();
@@ -271,44 +281,45 @@ __device__ __forceinline__ BwdOp load_bwd_op(const BwdOp *ops, int i) {
 // one unit of patterns. CLV_out = (P[ea] . a) * (P[eb] . b), rescaled per
 // site; site log-likelihoods of displayed-tree root variants are summed over
 // the warp's patterns into site_partial[slot][unit].
-template <typename real, int R, int THREADS, int MINB>
+template <typename real, int R, int THREADS, int MINB, int PPL>
 __global__ void __launch_bounds__(THREADS, MINB) forward_kernel(const SweepParams p, int op_begin) {
   constexpr int PPW = 32 / R;          // patterns per pass of the lane rows
-  constexpr int UNIT = PPW * kPPL;     // patterns per unit
+  constexpr int UNIT = PPW * PPL;      // patterns per forward unit
   constexpr int WPB = THREADS / 32;
-  __shared__ __align__(16) real sPw[WPB][2 * R * 16];
+  __shared__ __align__(16) real sPw[WPB][2 * R * PLayout<real>::kRow];
   const int lane = threadIdx.x & 31;
   const int r = lane % R;
   const int pl = lane / R;
   const int unit = blockIdx.x * WPB + (threadIdx.x >> 5);
-  if (unit >= p.n_units) return;  // whole warp
+  if (unit >= p.n_units_fwd) return;  // whole warp
   real *sP = sPw[threadIdx.x >> 5];
   const FwdOp op = load_fwd_op(p.fwd_ops, op_begin + blockIdx.y);
-  const int part = p.unit_part[unit];
+  const int part = p.unit_part[unit * (PPL / kPPLBase)];
   const size_t N = (size_t)p.n_patterns;
   const size_t g0 = (size_t)unit * UNIT + pl;  // the lane's first pattern; the second is g0 + PPW
-  real ca[kPPL][4], cb[kPPL][4];
-  int sa[kPPL], sb[kPPL];
-  load_child<real, R>(p, op.a, g0, r, PPW, ca, sa);
-  load_child<real, R>(p, op.b, g0, r, PPW, cb, sb);
+  real ca[PPL][4], cb[PPL][4];
+  int sa[PPL], sb[PPL];
+  load_child<real, R, PPL>(p, op.a, g0, r, PPW, ca, sa);
+  load_child<real, R, PPL>(p, op.b, g0, r, PPW, cb, sb);
   stage_pmats_warp<real, R>(sP, static_cast<const real *>(p.pmat) + (size_t)part * p.n_edges * (R * 16), op.ea,
                             op.b == INT32_MIN ? -1 : op.eb, lane);
 
-  real v[kPPL][4];
-  matvec2_s<real>(sP + r * 16, ca, v);
+  constexpr int ROW = PLayout<real>::kRow;
+  real v[PPL][4];
+  matvec2_s<real, PPL>(sP + r * ROW, ca, v);
   if (op.b != INT32_MIN) {
-    real pb[kPPL][4];
-    matvec2_s<real>(sP + R * 16 + r * 16, cb, pb);
+    real pb[PPL][4];
+    matvec2_s<real, PPL>(sP + (R + r) * ROW, cb, pb);
 #pragma unroll
-    for (int k = 0; k < kPPL; ++k)
+    for (int k = 0; k < PPL; ++k)
 #pragma unroll
       for (int i = 0; i < 4; ++i) v[k][i] *= pb[k][i];
   }
   real *dst = static_cast<real *>(p.clv) + ((size_t)op.out * N + g0) * (R * 4) + r * 4;
   int32_t *sdst = p.scaler + (size_t)op.out * N + g0;
-  int s[kPPL];
+  int s[PPL];
 #pragma unroll
-  for (int k = 0; k < kPPL; ++k) {
+  for (int k = 0; k < PPL; ++k) {
     real m = max(max(v[k][0], v[k][1]), max(v[k][2], v[k][3]));
     m = rate_max<R>(m);
     s[k] = sa[k] + sb[k] + Scale<real>::rescale(m, v[k]);
@@ -323,7 +334,7 @@ __global__ void __launch_bounds__(THREADS, MINB) forward_kernel(const SweepParam
     for (int i = 0; i < 4; ++i) freq[i] = (real)p.freqs[part * 4 + i];
     double ll = 0.0;
 #pragma unroll
-    for (int k = 0; k < kPPL; ++k) {
+    for (int k = 0; k < PPL; ++k) {
       real t = rw * (freq[0] * v[k][0] + freq[1] * v[k][1] + freq[2] * v[k][2] + freq[3] * v[k][3]);
       t = rate_sum<R>(t);
       const double w = p.weights[g0 + (size_t)k * PPW];
@@ -333,7 +344,7 @@ __global__ void __launch_bounds__(THREADS, MINB) forward_kernel(const SweepParam
       }
     }
     ll = warp_sum(ll);
-    if (lane == 0) p.site_partial[(size_t)op.slot * p.n_units + unit] = ll;
+    if (lane == 0) p.site_partial[(size_t)op.slot * p.n_units_fwd + unit] = ll;
   }
 }
 
@@ -346,12 +357,12 @@ __global__ void __launch_bounds__(THREADS, MINB) forward_kernel(const SweepParam
 //   message to a = Pa^T u_a, message to b = Pb^T u_b
 // The two edge terms are summed over the block and written to
 // grad_partial[op][blockIdx.x][2] for a deterministic reduction per edge.
-template <typename real, int R, int THREADS, int MINB>
+template <typename real, int R, int THREADS, int MINB, int PPL>
 __global__ void __launch_bounds__(THREADS, MINB) backward_kernel(const SweepParams p, int op_begin) {
   constexpr int PPW = 32 / R;
-  constexpr int UNIT = PPW * kPPL;
+  constexpr int UNIT = PPW * PPL;      // patterns per adjoint unit
   constexpr int WPB = THREADS / 32;
-  __shared__ __align__(16) real sPw[WPB][2 * R * 16];
+  __shared__ __align__(16) real sPw[WPB][2 * R * PLayout<real>::kRow];
   __shared__ real sQw[WPB][16 + 4 + 2 * R];
   const int lane = threadIdx.x & 31;
   const int r = lane % R;
@@ -371,22 +382,22 @@ __global__ void __launch_bounds__(THREADS, MINB) backward_kernel(const SweepPara
   const real *clv = static_cast<const real *>(p.clv);
   real *msg = static_cast<real *>(p.msg);
 
-  real ca[kPPL][4], cb[kPPL][4], ax[kPPL][4], cx[kPPL][4];
-  int sa[kPPL], sb[kPPL], sx[kPPL];
+  real ca[PPL][4], cb[PPL][4], ax[PPL][4], cx[PPL][4];
+  int sa[PPL], sb[PPL], sx[PPL];
 #pragma unroll
-  for (int k = 0; k < kPPL; ++k)
+  for (int k = 0; k < PPL; ++k)
 #pragma unroll
     for (int i = 0; i < 4; ++i) ax[k][i] = 0;
   {
-    load_child<real, R>(p, op.a, g0, r, PPW, ca, sa);
-    load_child<real, R>(p, op.b, g0, r, PPW, cb, sb);
+    load_child<real, R, PPL>(p, op.a, g0, r, PPW, ca, sa);
+    load_child<real, R, PPL>(p, op.b, g0, r, PPW, cb, sb);
     const int32_t *sxp = p.scaler + (size_t)op.x * N + g0;
 #pragma unroll
-    for (int k = 0; k < kPPL; ++k) sx[k] = sxp[(size_t)k * PPW];
+    for (int k = 0; k < PPL; ++k) sx[k] = sxp[(size_t)k * PPW];
     for (int m = 0; m < op.msg_count; ++m) {
       const real *src = msg + (size_t)__ldg(p.msg_slots + op.msg_begin + m) * N * (R * 4) + lane_off;
 #pragma unroll
-      for (int k = 0; k < kPPL; ++k) {
+      for (int k = 0; k < PPL; ++k) {
         real t[4];
         Vec<real>::load(src + (size_t)k * PPW * (R * 4), t);
 #pragma unroll
@@ -396,7 +407,7 @@ __global__ void __launch_bounds__(THREADS, MINB) backward_kernel(const SweepPara
     if (op.seed >= 0) {
       const real *cxp = clv + (size_t)op.x * N * (R * 4) + lane_off;
 #pragma unroll
-      for (int k = 0; k < kPPL; ++k) Vec<real>::load(cxp + (size_t)k * PPW * (R * 4), cx[k]);
+      for (int k = 0; k < PPL; ++k) Vec<real>::load(cxp + (size_t)k * PPW * (R * 4), cx[k]);
     }
   }
   if (lane < 16) sQ[lane] = (real)p.Q[part * 16 + lane];
@@ -413,7 +424,7 @@ __global__ void __launch_bounds__(THREADS, MINB) backward_kernel(const SweepPara
     // d(w_s log L_s)/d clv_x = w_s rw_r pi_i / L_s, times the tree weight
     const real sd = (real)p.seeds[(size_t)op.seed * p.n_parts + part];
 #pragma unroll
-    for (int k = 0; k < kPPL; ++k) {
+    for (int k = 0; k < PPL; ++k) {
       real t = rw * (sF[0] * cx[k][0] + sF[1] * cx[k][1] + sF[2] * cx[k][2] + sF[3] * cx[k][3]);
       t = rate_sum<R>(t);
       const real sw = sd * (real)p.weights[g0 + (size_t)k * PPW];
@@ -424,22 +435,22 @@ __global__ void __launch_bounds__(THREADS, MINB) backward_kernel(const SweepPara
       }
     }
   }
-  const real *Pa = sP + r * 16;
-  const real *Pb = sP + R * 16 + r * 16;
-  real pa[kPPL][4], pb[kPPL][4];
-  matvec2_s<real>(Pa, ca, pa);
+  const real *Pa = sP + r * PLayout<real>::kRow;
+  const real *Pb = sP + (R + r) * PLayout<real>::kRow;
+  real pa[PPL][4], pb[PPL][4];
+  matvec2_s<real, PPL>(Pa, ca, pa);
   if (!fake) {
-    matvec2_s<real>(Pb, cb, pb);
+    matvec2_s<real, PPL>(Pb, cb, pb);
   } else {
 #pragma unroll
-    for (int k = 0; k < kPPL; ++k)
+    for (int k = 0; k < PPL; ++k)
 #pragma unroll
       for (int i = 0; i < 4; ++i) pb[k][i] = 1;
   }
-  real ua[kPPL][4], ub[kPPL][4];
+  real ua[PPL][4], ub[PPL][4];
   real ga = 0, gb = 0;
 #pragma unroll
-  for (int k = 0; k < kPPL; ++k) {
+  for (int k = 0; k < PPL; ++k) {
     const int sh = sx[k] - sa[k] - sb[k];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
@@ -465,18 +476,18 @@ __global__ void __launch_bounds__(THREADS, MINB) backward_kernel(const SweepPara
     }
   }
   if (op.out_a >= 0) {
-    real na[kPPL][4];
-    matvec2_ts<real>(Pa, ua, na);
+    real na[PPL][4];
+    matvec2_ts<real, PPL>(Pa, ua, na);
     real *d = msg + (size_t)op.out_a * N * (R * 4) + lane_off;
 #pragma unroll
-    for (int k = 0; k < kPPL; ++k) Vec<real>::store(d + (size_t)k * PPW * (R * 4), na[k]);
+    for (int k = 0; k < PPL; ++k) Vec<real>::store(d + (size_t)k * PPW * (R * 4), na[k]);
   }
   if (op.out_b >= 0) {
-    real nb[kPPL][4];
-    matvec2_ts<real>(Pb, ub, nb);
+    real nb[PPL][4];
+    matvec2_ts<real, PPL>(Pb, ub, nb);
     real *d = msg + (size_t)op.out_b * N * (R * 4) + lane_off;
 #pragma unroll
-    for (int k = 0; k < kPPL; ++k) Vec<real>::store(d + (size_t)k * PPW * (R * 4), nb[k]);
+    for (int k = 0; k < PPL; ++k) Vec<real>::store(d + (size_t)k * PPW * (R * 4), nb[k]);
   }
   ga = warp_sum(ga * sRate[r]);
   gb = warp_sum(gb * sRate[r]);
@@ -682,10 +693,10 @@ constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
 template <typename real, int R, int T, int M>
 struct FwdRun {
   static int run(cudaStream_t s, const SweepParams &p, const int32_t *level_begin, int n_levels) {
-    const int bx = (p.n_units + T / 32 - 1) / (T / 32);
+    const int bx = (p.n_units_fwd + T / 32 - 1) / (T / 32);
     for (int L = 0; L < n_levels; ++L) {
       const int n = level_begin[L + 1] - level_begin[L];
-      if (n > 0) forward_kernel<real, R, T, M><<<dim3(bx, n), T, 0, s>>>(p, level_begin[L]);
+      if (n > 0) forward_kernel<real, R, T, M, kPPLForward><<<dim3(bx, n), T, 0, s>>>(p, level_begin[L]);
     }
     return 0;
   }
@@ -696,7 +707,7 @@ struct BwdRun {
     const int bx = (p.n_units + T / 32 - 1) / (T / 32);
     for (int L = 0; L < n_levels; ++L) {
       const int n = level_begin[L + 1] - level_begin[L];
-      if (n > 0) backward_kernel<real, R, T, M><<<dim3(bx, n), T, 0, s>>>(p, level_begin[L]);
+      if (n > 0) backward_kernel<real, R, T, M, kPPLBase><<<dim3(bx, n), T, 0, s>>>(p, level_begin[L]);
     }
     return 0;
   }

@@ -6,9 +6,14 @@
 
 namespace netlk {
 
-// Patterns per lane: a lane handles rate r of patterns s and s + 32/R of its
-// unit, so one P-row load and one op decode serve two patterns.
-constexpr int kPPL = 2;
+// Patterns per lane: a lane handles rate r of patterns s, s + 32/R, ... of
+// its unit, so one P-row load and one op decode serve several patterns. The
+// adjoint sweep (more live values per pattern) uses kPPLBase, the forward
+// sweep kPPLForward; units, the unit -> partition map and the adjoint's
+// per-unit gradient partials are counted in kPPLBase units.
+constexpr int kPPLBase = 2;
+constexpr int kPPLForward = 4;
+static_assert(kPPLForward % kPPLBase == 0, "forward units must be whole adjoint units");
 // Blocks have at most 8 warps (one unit each); partitions are padded to a
 // whole number of 8-unit blocks so that a block never spans two partitions.
 constexpr int kMaxWarpsPerBlock = 8;
@@ -35,12 +40,13 @@ struct alignas(64) BwdOp {
 };
 
 struct DevPartition {
-  int32_t unit_begin, unit_end;  // units (warp pattern groups) of this partition
+  int32_t unit_begin, unit_end;  // forward units of this partition
 };
 
 // Everything the sweeps read, in device memory.
 struct SweepParams {
-  int32_t n_units;      // pattern groups of kPPL*32/R patterns (one per warp and op)
+  int32_t n_units;      // adjoint units: kPPLBase*32/R patterns (one per warp and op)
+  int32_t n_units_fwd;  // forward units: kPPLForward*32/R patterns
   int64_t n_patterns;   // padded total (N)
   int32_t n_edges;
   int32_t n_fwd_ops;
@@ -60,16 +66,16 @@ struct SweepParams {
   int32_t *scaler;              // [V][N]
   void *msg;                    // [M][N][R][4] real adjoint messages
   const int32_t *msg_slots;     // message slots read by the adjoint ops
-  double *site_partial;         // [n_slots][n_units]
+  double *site_partial;         // [n_slots][n_units_fwd]
   const double *seeds;          // [n_slots][n_parts]
   double *grad_partial;         // [n_bwd_ops][n_units][2] per-warp edge terms (a, b)
 };
 
 struct MixParams {
-  int32_t n_slots, n_parts, n_roots, n_ret, variant, n_units;
+  int32_t n_slots, n_parts, n_roots, n_ret, variant, n_units;  // n_units: forward units
   double min_logprob;
   const DevPartition *parts;      // [n_parts]
-  const double *site_partial;     // [n_slots][n_units]
+  const double *site_partial;     // [n_slots][n_units] (forward units)
   double *tree_logl;              // [n_slots][n_parts]
   const int32_t *root_slot;       // [n_roots]
   const double *root_logprob;     // [n_roots]

@@ -91,7 +91,7 @@ struct netlk_ctx {
   std::vector<double> brlen, ret_probs;
   std::vector<PartInfo> parts;
   int64_t N = 0;
-  int n_units = 0, ppw = 8;
+  int n_units = 0, n_units_fwd = 0, ppw = 8;
   // schedules
   std::vector<FwdOp> fwd;
   std::vector<BwdOp> bwd;
@@ -171,6 +171,7 @@ struct netlk_ctx {
   SweepParams sweep() const {
     SweepParams p{};
     p.n_units = n_units;
+    p.n_units_fwd = n_units_fwd;
     p.n_patterns = N;
     p.n_edges = topo.n_edges;
     p.n_fwd_ops = (int)fwd.size();
@@ -203,7 +204,7 @@ struct netlk_ctx {
     m.n_roots = (int)dag.roots.size();
     m.n_ret = topo.n_ret;
     m.variant = opts.variant;
-    m.n_units = n_units;
+    m.n_units = n_units_fwd;
     m.min_logprob = opts.min_interesting_tree_logprob;
     m.parts = d_parts.as<DevPartition>();
     m.site_partial = d_site_partial.as<double>();
@@ -277,7 +278,7 @@ void netlk_ctx::build_schedules() {
   fwd_bytes = 0;
   for (const FwdOp &op : fwd) {
     fwd_bytes += N * (clv_b + 4 + child_bytes(op.a) + child_bytes(op.b));
-    if (op.slot >= 0) fwd_bytes += (int64_t)n_units * 8;
+    if (op.slot >= 0) fwd_bytes += (int64_t)n_units_fwd * 8;
   }
   // adjoint: variants reachable backwards from the displayed-tree roots
   std::vector<char> inb(V, 0);
@@ -369,20 +370,22 @@ void netlk_ctx::build_schedules() {
 // ------------------------------------------------------------ device setup
 void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
   const int V = (int)dag.vars.size();
-  ppw = (32 / R) * kPPL;  // patterns per unit (one warp pass)
+  ppw = (32 / R) * kPPLBase;                 // patterns per adjoint unit
+  const int ppw_f = (32 / R) * kPPLForward;  // patterns per forward unit
   // patterns: every partition padded to whole blocks of the largest launch
-  // shape (8 warps x one unit each), so a block never spans two partitions
-  const int align = 8 * ppw;
+  // shape (8 warps x one forward unit each), so a block never spans two partitions
+  const int align = 8 * ppw_f;
   N = 0;
   n_units = 0;
   for (auto &pi : parts) {
     pi.n_pad = (pi.n + align - 1) / align * align;
     pi.offset = N;
-    pi.unit_begin = (int)(N / ppw);
+    pi.unit_begin = (int)(N / ppw_f);
     N += pi.n_pad;
-    pi.unit_end = (int)(N / ppw);
+    pi.unit_end = (int)(N / ppw_f);
   }
   n_units = (int)(N / ppw);
+  n_units_fwd = (int)(N / ppw_f);
   build_schedules();
   if (opts.host_only) return;
   // host staging of tips / weights / unit map
@@ -402,7 +405,7 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
       if (!(w >= 0.0) || !std::isfinite(w)) throw Error(NETLK_ERR_INVALID_ARGUMENT, "pattern weight");
       weights[pi.offset + s] = w;
     }
-    for (int u = pi.unit_begin; u < pi.unit_end; ++u) unit_part[u] = p;
+    for (int u = (int)(pi.offset / ppw); u < (int)((pi.offset + pi.n_pad) / ppw); ++u) unit_part[u] = p;
   }
   const size_t real_sz = opts.precision == NETLK_FP32 ? 4 : 8;
   const size_t clv_per_var = (size_t)N * R * S * real_sz;
@@ -426,7 +429,7 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
   d_freqs.alloc(P * S * 8, dev_bytes);
   d_Q.alloc(P * S * S * 8, dev_bytes);
   d_brlen.alloc(topo.n_edges * 8, dev_bytes);
-  d_site_partial.alloc((size_t)n_slots * n_units * 8, dev_bytes);
+  d_site_partial.alloc((size_t)n_slots * n_units_fwd * 8, dev_bytes);
   d_tree_logl.alloc((size_t)n_slots * P * 8, dev_bytes);
   d_root_slot.alloc(root_slot.size() * 4, dev_bytes);
   d_root_lp.alloc(dag.roots.size() * 8, dev_bytes);
