@@ -148,8 +148,9 @@ int netlk_create(const netlk_topology *topo, const netlk_partition *parts,
                  netlk_ctx **out);
 int netlk_destroy(netlk_ctx *ctx);
 
-/* Message of the last failing call on ctx (or of the last failed create when
- * ctx is NULL). Valid until the next call on the same context. */
+/* Message of the last failing call on ctx (or, with ctx NULL, of the last
+ * failed netlk_create / context-free call on this thread). Valid until the
+ * next call on the same context. */
 const char *netlk_last_error(const netlk_ctx *ctx);
 const char *netlk_status_string(int status);
 
@@ -256,6 +257,36 @@ int netlk_kernel_times(netlk_ctx *ctx, double *ms, int64_t *launches, int32_t n)
  * time (ms) it measured for each of the first n shapes (0 where untimed). */
 int netlk_tuning(const netlk_ctx *ctx, int32_t *fwd_shape, int32_t *bwd_shape, double *fwd_ms,
                  double *bwd_ms, int32_t n);
+
+/* ---------------------------------------------------- allocation-free mixing */
+/* No counterpart in the reference: an extra entry point for callers that
+ * cannot allocate device memory - work recorded into a CUDA graph capture,
+ * programs whose device memory belongs to another allocator or a fixed
+ * budget, loops that must not synchronise on cudaMalloc / cudaFree.
+ *
+ * Mixes displayed-tree site log-likelihoods into the network log-likelihood
+ * exactly as netlk_loglikelihood mixes its own: per partition, AVERAGE =
+ * log sum_T exp(logprob_T + sum of the tree's site values) or BEST = max_T,
+ * skipping trees with logprob_T < min_interesting_tree_logprob; the total is
+ * the sum over partitions.
+ *   d_site_logl       device [n_trees * n_sites], row = displayed tree: weighted
+ *                     per-site (or per-site-block) log-likelihood contributions
+ *   d_part_site_begin device [n_parts + 1]: site range of each partition
+ *   d_tree_logprob    device [n_trees]: log P(tree)
+ *   d_out             device [1 + n_parts]: total, then per-partition logL
+ *   stream            cudaStream_t to launch on (NULL = default stream)
+ * Works in a fixed device array of NETLK_NOALLOC_MAX_TREE_PARTITIONS doubles
+ * (n_trees * n_parts above that is rejected with NETLK_ERR_INVALID_ARGUMENT;
+ * the message is in netlk_last_error(NULL)). Asynchronous: results are ready
+ * when the stream is. The first call on a device looks up that array's
+ * device address, so make it before any stream capture. All calls on a
+ * device share the array: calls whose work overlaps on the GPU race. */
+#define NETLK_NOALLOC_MAX_TREE_PARTITIONS 65536
+int netlk_mix_site_loglikelihoods_noalloc(const double *d_site_logl, int32_t n_trees, int64_t n_sites,
+                                          const int64_t *d_part_site_begin, int32_t n_parts,
+                                          const double *d_tree_logprob, int32_t variant,
+                                          double min_interesting_tree_logprob, double *d_out,
+                                          void *stream);
 
 /* ------------------------------------------------------------------- debug */
 /* Copies the CLV (converted to double) and scale counters of one variant:

@@ -33,6 +33,7 @@ EXPORTED = [
     "netlk_tree_partials", "netlk_mix_and_backward", "netlk_get_clv", "netlk_get_stream",
     "netlk_launch_count", "netlk_set_branch_lengths_device", "netlk_enqueue",
     "netlk_result_pointers", "netlk_set_profiling", "netlk_kernel_times", "netlk_tuning",
+    "netlk_mix_site_loglikelihoods_noalloc",
 ]
 
 
@@ -119,6 +120,8 @@ def lib():
     L.netlk_enqueue.argtypes = [vp, ctypes.c_int32]
     L.netlk_result_pointers.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp)]
     L.netlk_set_profiling.argtypes = [vp, ctypes.c_int32]
+    L.netlk_mix_site_loglikelihoods_noalloc.argtypes = [
+        vp, ctypes.c_int32, ctypes.c_int64, vp, ctypes.c_int32, vp, ctypes.c_int32, ctypes.c_double, vp, vp]
     L.netlk_tuning.argtypes = [vp, c_int32_p, c_int32_p, c_double_p, c_double_p, ctypes.c_int32]
     L.netlk_kernel_times.argtypes = [vp, c_double_p, ctypes.POINTER(ctypes.c_int64), ctypes.c_int32]
     for name in EXPORTED:

@@ -649,6 +649,11 @@ void netlk_ctx::finish(double *total, double *part_logl, double *d_brlen, double
 }
 
 // ------------------------------------------------------------------ C ABI
+namespace netlk {
+// Error text for context-free entry points (netlk_last_error(NULL)).
+void set_global_error(const std::string &msg) { g_create_error = msg; }
+}  // namespace netlk
+
 namespace {
 
 template <class F>
