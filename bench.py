@@ -52,6 +52,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=16384, help="patterns in the CPU sample")
     ap.add_argument("--scale", type=float, default=1.0, help="site-count scale (1.0 = full workload)")
+    ap.add_argument("--config", type=int, default=2, choices=[2, 3],
+                    help="2: 100 taxa / 8 reticulations / 100k DNA sites (the headline workload); "
+                         "3: 40 taxa / 3 reticulations / 50k protein sites")
     return ap.parse_args()
 
 
@@ -147,12 +150,12 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-# DRAM bytes per site-CLV update of each sweep from one ncu capture
+# DRAM bytes per site-CLV update of each sweep (DNA: 4 states) from one ncu capture
 # (profiles/sweep_dram_traffic_config2_scale0.3.md: dram__bytes_read.sum +
 # dram__bytes_write.sum of one evaluation's 16 level launches, same network at
 # 0.3 of its sites, scaled by updates; writes still dirty in L2 at a launch's
 # end are not counted).
-TRAFFIC_PER_UPDATE = {"forward_fp32": 101.2, "backward_fp32": 297.5}
+TRAFFIC_PER_UPDATE = {"forward_fp32_4": 101.2, "backward_fp32_4": 297.5}
 
 
 def cpu_port_rate(w, n_sample, steps, warmup, variant):
@@ -200,7 +203,7 @@ def run_reference(args, ws, rank):
     if rank != 0:
         return
     from netrax_gb300 import synth
-    w = synth.config(2, scale=args.scale)
+    w = synth.config(args.config, scale=args.scale)
     steps = max(1, min(args.steps, 5))
     evals, info = cpu_port_rate(w, args.cpu_sample, steps, min(args.warmup, 1), args.variant)
     line = {"impl": "reference", "metric": METRIC, "value": evals, "unit": UNIT, "n_gpus": args.gpus,
@@ -219,7 +222,7 @@ def run_netlk(args, ws, rank, local):
     from netrax_gb300.likelihood import NetworkLikelihood
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    w = synth.config(2, scale=args.scale)
+    w = synth.config(args.config, scale=args.scale)
     lik = NetworkLikelihood(w.network, w.partitions, variant=args.variant, precision=args.precision,
                             device=local)
     st = lik.stats
@@ -322,7 +325,7 @@ def run_netlk(args, ws, rank, local):
     dom_bytes = bwd_b if dom == "backward" else fwd_b
     achieved = dom_bytes / (kavg[dom] * 1e-3) / 1e9 if kavg[dom] > 0 else 0.0
     traffic = None
-    tt = TRAFFIC_PER_UPDATE.get("%s_%s" % (dom, args.precision))
+    tt = TRAFFIC_PER_UPDATE.get("%s_%s_%d" % (dom, args.precision, lik.states))
     if tt:
         traffic = tt * st["site_clv_updates"]
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -345,8 +348,9 @@ def run_netlk(args, ws, rank, local):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": W,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32" if args.precision == "fp32" else "f64", "data": "synthetic",
-            "config": {"workload": w.name, "taxa": 100, "reticulations": 8, "sites": w.n_sites,
-                       "patterns": w.n_patterns, "partitions": len(w.partitions), "model": "GTR+G4",
+            "config": {"workload": w.name, "taxa": w.network.n_tips, "reticulations": w.network.n_reticulations,
+                       "sites": w.n_sites, "patterns": w.n_patterns, "partitions": len(w.partitions),
+                       "model": "GTR+G4" if lik.states == 4 else "20-state GTR (LG-like)+G4",
                        "variant": args.variant, "precision": args.precision,
                        "displayed_trees": lik.n_roots, "dag_variants": st["n_variants"],
                        "site_clv_updates_per_eval": st["site_clv_updates"],

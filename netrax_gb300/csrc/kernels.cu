@@ -21,90 +21,15 @@
 #include <cstdio>
 
 #include "kernels.cuh"
+#include "kernels_common.cuh"
 
 namespace netlk {
 
 static int64_t g_launches = 0;
 int64_t launches_issued() { return g_launches; }
+void add_launches(int64_t n) { g_launches += n; }
 
 namespace {
-
-constexpr unsigned kFull = 0xffffffffu;
-
-template <typename real>
-struct Vec;
-
-template <>
-struct Vec<float> {
-  static __device__ __forceinline__ void load(const float *p, float (&v)[4]) {
-    float4 t = *reinterpret_cast<const float4 *>(p);
-    v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
-  }
-  static __device__ __forceinline__ void store(float *p, const float (&v)[4]) {
-    *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
-  }
-  static __device__ __forceinline__ void ldg(const float *p, float (&v)[4]) {
-    float4 t = __ldg(reinterpret_cast<const float4 *>(p));
-    v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
-  }
-};
-
-template <>
-struct Vec<double> {
-  static __device__ __forceinline__ void load(const double *p, double (&v)[4]) {
-    double2 a = reinterpret_cast<const double2 *>(p)[0];
-    double2 b = reinterpret_cast<const double2 *>(p)[1];
-    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
-  }
-  static __device__ __forceinline__ void store(double *p, const double (&v)[4]) {
-    reinterpret_cast<double2 *>(p)[0] = make_double2(v[0], v[1]);
-    reinterpret_cast<double2 *>(p)[1] = make_double2(v[2], v[3]);
-  }
-  static __device__ __forceinline__ void ldg(const double *p, double (&v)[4]) {
-    double2 a = __ldg(reinterpret_cast<const double2 *>(p));
-    double2 b = __ldg(reinterpret_cast<const double2 *>(p) + 1);
-    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
-  }
-};
-
-// Scaling rules. FP64 restates libpll's per-site rule: when every entry of a
-// site is below 2^-256 multiply the site by 2^256 and add one to its counter.
-// FP32 uses its own power-of-two unit: when the site maximum falls below
-// 2^-32, shift the site by 2^-e (max becomes [0.5, 1)) and add -e.
-template <typename real>
-struct Scale;
-
-template <>
-struct Scale<float> {
-  static constexpr double kLogUnit = -0.69314718055994530942;  // log(2^-1)
-  static __device__ __forceinline__ int rescale(float m, float (&v)[4]) {
-    if (m < 0x1p-32f && m > 0.0f) {
-      int e;
-      frexpf(m, &e);
-      const int k = -e;
-#pragma unroll
-      for (int i = 0; i < 4; ++i) v[i] = ldexpf(v[i], k);
-      return k;
-    }
-    return 0;
-  }
-  // x * 2^k for the local shift k >= 0 of a site (applied to adjoint products)
-  static __device__ __forceinline__ float shift(float x, int k) { return ldexpf(x, k); }
-};
-
-template <>
-struct Scale<double> {
-  static constexpr double kLogUnit = -177.44567822334599921;  // log(2^-256)
-  static __device__ __forceinline__ int rescale(double m, double (&v)[4]) {
-    if (m < 0x1p-256) {
-#pragma unroll
-      for (int i = 0; i < 4; ++i) v[i] *= 0x1p256;
-      return 1;
-    }
-    return 0;
-  }
-  static __device__ __forceinline__ double shift(double x, int k) { return ldexp(x, 256 * k); }
-};
 
 // Loads one child operand for the lane's kPPL patterns: a variant CLV (with
 // its scale counters), a tip (state mask expanded to 0/1) or the fake all-ones
@@ -201,26 +126,8 @@ __device__ __forceinline__ void matvec2_t(const real *P, const real (&u)[PPL][4]
   }
 }
 
-template <int R, typename T>
-__device__ __forceinline__ T rate_sum(T v) {
-#pragma unroll
-  for (int o = 1; o < R; o <<= 1) v += __shfl_xor_sync(kFull, v, o);
-  return v;
-}
 
-template <int R, typename T>
-__device__ __forceinline__ T rate_max(T v) {
-#pragma unroll
-  for (int o = 1; o < R; o <<= 1) v = max(v, __shfl_xor_sync(kFull, v, o));
-  return v;
-}
 
-template <typename T>
-__device__ __forceinline__ T warp_sum(T v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
-  return v;
-}
 
 // P rows of one rate sit kPRow values apart in shared memory (16 used +
 // padding) so the four rate groups of a warp's LDS.128 hit distinct banks.
@@ -257,24 +164,7 @@ __device__ __forceinline__ void stage_pmats_warp(real *sP, const real *pm_part, 
   __syncwarp();
 }
 
-__device__ __forceinline__ FwdOp load_fwd_op(const FwdOp *ops, int i) {
-  const int4 *q = reinterpret_cast<const int4 *>(ops + i);
-  const int4 a = __ldg(q), b = __ldg(q + 1);
-  FwdOp o;
-  o.out = a.x; o.a = a.y; o.b = a.z; o.ea = a.w;
-  o.eb = b.x; o.slot = b.y; o.pad0 = b.z; o.pad1 = b.w;
-  return o;
-}
 
-__device__ __forceinline__ BwdOp load_bwd_op(const BwdOp *ops, int i) {
-  const int4 *q = reinterpret_cast<const int4 *>(ops + i);
-  const int4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
-  BwdOp o;
-  o.x = a.x; o.a = a.y; o.b = a.z; o.ea = a.w;
-  o.eb = b.x; o.seed = b.y; o.out_a = b.z; o.out_b = b.w;
-  o.msg_begin = c.x; o.msg_count = c.y; o.pad0 = o.pad1 = o.pad2 = o.pad3 = o.pad4 = o.pad5 = 0;
-  return o;
-}
 
 // ------------------------------------------------------------------ forward
 // One launch per DAG level: blockIdx.y picks the op of the level, each warp
@@ -499,27 +389,30 @@ __global__ void __launch_bounds__(THREADS, MINB) backward_kernel(const SweepPara
 }
 
 // ------------------------------------------------------------- P-matrices
-// P(t r) = U diag(exp(lambda r t)) U^-1 in FP64; a zero length gives the identity.
-__global__ void pmatrix_kernel(int n_parts, int n_edges, int R, const double *__restrict__ lambda,
+// P(t r) = U diag(exp(lambda r t)) U^-1 in FP64; a zero length gives the
+// identity. One thread per entry of pmat[part][edge][rate][S][S].
+__global__ void pmatrix_kernel(int n_parts, int n_edges, int R, int S, const double *__restrict__ lambda,
                                const double *__restrict__ U, const double *__restrict__ Uinv,
                                const double *__restrict__ rates, const double *__restrict__ brlen,
                                double *__restrict__ pmat64, float *__restrict__ pmat32) {
-  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-  const int total = n_parts * n_edges * R * 16;
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int SS = S * S;
+  const int64_t total = (int64_t)n_parts * n_edges * R * SS;
   if (idx >= total) return;
-  const int ij = idx & 15;
-  const int i = ij >> 2, j = ij & 3;
-  const int rr = (idx >> 4) % R;
-  const int e = (idx >> 4) / R % n_edges;
-  const int part = (idx >> 4) / R / n_edges;
+  const int ij = (int)(idx % SS);
+  const int i = ij / S, j = ij - i * S;
+  const int64_t q = idx / SS;  // (part, edge, rate)
+  const int rr = (int)(q % R);
+  const int e = (int)(q / R % n_edges);
+  const int part = (int)(q / R / n_edges);
   const double t = brlen[e] * rates[part * R + rr];
   double v;
   if (brlen[e] == 0.0) {
     v = (i == j) ? 1.0 : 0.0;
   } else {
     v = 0.0;
-    for (int k = 0; k < 4; ++k)
-      v += U[part * 16 + i * 4 + k] * exp(lambda[part * 4 + k] * t) * Uinv[part * 16 + k * 4 + j];
+    for (int k = 0; k < S; ++k)
+      v += U[(size_t)part * SS + i * S + k] * exp(lambda[part * S + k] * t) * Uinv[(size_t)part * SS + k * S + j];
   }
   pmat64[idx] = v;
   if (pmat32) pmat32[idx] = (float)v;
@@ -762,12 +655,12 @@ void launch_backward(cudaStream_t s, int precision, int R, int shape, const Swee
   for (int L = 0; L < n_levels; ++L) g_launches += level_begin[L + 1] > level_begin[L];
 }
 
-void launch_pmatrix(cudaStream_t s, int n_parts, int n_edges, int R, const double *lambda, const double *U,
+void launch_pmatrix(cudaStream_t s, int n_parts, int n_edges, int R, int S, const double *lambda, const double *U,
                     const double *Uinv, const double *rates, const double *brlen, double *pmat64,
                     float *pmat32) {
-  const int total = n_parts * n_edges * R * 16;
-  pmatrix_kernel<<<(total + 255) / 256, 256, 0, s>>>(n_parts, n_edges, R, lambda, U, Uinv, rates, brlen,
-                                                     pmat64, pmat32);
+  const int64_t total = (int64_t)n_parts * n_edges * R * S * S;
+  pmatrix_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(n_parts, n_edges, R, S, lambda, U, Uinv, rates,
+                                                                 brlen, pmat64, pmat32);
   g_launches++;
 }
 

@@ -55,14 +55,15 @@ struct SweepParams {
   const FwdOp *fwd_ops;
   const BwdOp *bwd_ops;
   const int32_t *unit_part;     // [n_units]
-  const uint8_t *tips;          // [n_tips][N] 4-bit state masks
+  const uint8_t *tips;          // [n_tips][N] 4-bit state masks (4-state partitions)
+  const uint32_t *tips32;       // [n_tips][N] 20-bit state masks (20-state partitions)
   const double *weights;        // [N] pattern weights (0 for padding)
-  const void *pmat;             // [n_parts][n_edges][R][4][4] real
-  const double *freqs;          // [n_parts][4]
+  const void *pmat;             // [n_parts][n_edges][R][S][S] real
+  const double *freqs;          // [n_parts][S]
   const double *rate_weights;   // [n_parts][R]
   const double *rates;          // [n_parts][R]
-  const double *Q;              // [n_parts][16]
-  void *clv;                    // [V][N][R][4] real
+  const double *Q;              // [n_parts][S*S]
+  void *clv;                    // [V][N][R][S] real
   int32_t *scaler;              // [V][N]
   void *msg;                    // [M][N][R][4] real adjoint messages
   const int32_t *msg_slots;     // message slots read by the adjoint ops
@@ -87,7 +88,7 @@ struct MixParams {
   double *out;                    // [2 + n_parts + n_ret]: total, status, part logl, dret
 };
 
-void launch_pmatrix(cudaStream_t s, int n_parts, int n_edges, int R, const double *lambda,
+void launch_pmatrix(cudaStream_t s, int n_parts, int n_edges, int R, int S, const double *lambda,
                     const double *U, const double *Uinv, const double *rates, const double *brlen,
                     double *pmat64, float *pmat32);
 // Sweep launch shapes (threads per block, minimum blocks per SM): shape 0 is
@@ -103,7 +104,11 @@ void launch_tree_reduce(cudaStream_t s, const MixParams &m);
 void launch_mix(cudaStream_t s, const MixParams &m);
 void launch_grad_reduce(cudaStream_t s, int n_ops, int n_edges, int n_bx, const int32_t *edge_begin,
                         const int32_t *edge_entries, const double *partial, double *op_sum, double *grad);
+// 20-state forward (backward = false) or adjoint sweep, one launch per level.
+void launch_sweep20(cudaStream_t s, int precision, int R, bool backward, const SweepParams &p,
+                    const int32_t *level_begin, int n_levels);
 // Number of kernel launches issued by the launchers above (host counter).
 int64_t launches_issued();
+void add_launches(int64_t n);
 
 }  // namespace netlk

@@ -180,7 +180,8 @@ struct netlk_ctx {
     p.fwd_ops = d_fwd.as<FwdOp>();
     p.bwd_ops = d_bwd.as<BwdOp>();
     p.unit_part = d_unit_part.as<int32_t>();
-    p.tips = d_tips.as<uint8_t>();
+    p.tips = S == 4 ? d_tips.as<uint8_t>() : nullptr;
+    p.tips32 = S == 20 ? d_tips.as<uint32_t>() : nullptr;
     p.weights = d_weights.as<double>();
     p.pmat = opts.precision == NETLK_FP32 ? d_pmat32.p : d_pmat64.p;
     p.freqs = d_freqs.as<double>();
@@ -273,7 +274,7 @@ void netlk_ctx::build_schedules() {
   auto child_bytes = [&](int32_t ref) -> int64_t {
     if (ref >= 0) return clv_b + 4;
     if (ref == kFake) return 0;
-    return 1;
+    return S == 4 ? 1 : 4;  // tip state mask
   };
   fwd_bytes = 0;
   for (const FwdOp &op : fwd) {
@@ -389,16 +390,21 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
   build_schedules();
   if (opts.host_only) return;
   // host staging of tips / weights / unit map
-  std::vector<uint8_t> tips((size_t)topo.n_tips * N, 0x0f);
+  const uint32_t all_states = S == 4 ? 0xfu : 0xfffffu;
+  std::vector<uint8_t> tips(S == 4 ? (size_t)topo.n_tips * N : 0, 0x0f);
+  std::vector<uint32_t> tips32(S == 20 ? (size_t)topo.n_tips * N : 0, all_states);
   std::vector<double> weights(N, 0.0);
   std::vector<int32_t> unit_part(n_units);
   for (int p = 0; p < P; ++p) {
     const PartInfo &pi = parts[p];
     for (int t = 0; t < topo.n_tips; ++t)
       for (int s = 0; s < pi.n; ++s) {
-        uint32_t code = in[p].tip_states[(size_t)t * pi.n + s] & 0xfu;
+        uint32_t code = in[p].tip_states[(size_t)t * pi.n + s] & all_states;
         if (!code) throw Error(NETLK_ERR_INVALID_ARGUMENT, "tip state mask 0");
-        tips[(size_t)t * N + pi.offset + s] = (uint8_t)code;
+        if (S == 4)
+          tips[(size_t)t * N + pi.offset + s] = (uint8_t)code;
+        else
+          tips32[(size_t)t * N + pi.offset + s] = code;
       }
     for (int s = 0; s < pi.n; ++s) {
       double w = in[p].pattern_weights ? in[p].pattern_weights[s] : 1.0;
@@ -413,7 +419,7 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
   d_scaler.alloc((size_t)N * V * 4, dev_bytes);
   d_adj.alloc(clv_per_var * std::max(1, n_adj), dev_bytes);
   d_msg_slots.alloc(std::max<size_t>(1, msg_slots.size()) * 4, dev_bytes);
-  d_tips.alloc(tips.size(), dev_bytes);
+  d_tips.alloc(S == 4 ? tips.size() : tips32.size() * 4, dev_bytes);
   d_weights.alloc(N * 8, dev_bytes);
   d_unit_part.alloc(n_units * 4, dev_bytes);
   d_fwd.alloc(fwd.size() * sizeof(FwdOp), dev_bytes);
@@ -455,7 +461,10 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
 
   std::vector<DevPartition> dparts(P);
   for (int p = 0; p < P; ++p) dparts[p] = DevPartition{parts[p].unit_begin, parts[p].unit_end};
-  CUDA_OK(cudaMemcpyAsync(d_tips.p, tips.data(), tips.size(), cudaMemcpyHostToDevice, stream));
+  if (S == 4)
+    CUDA_OK(cudaMemcpyAsync(d_tips.p, tips.data(), tips.size(), cudaMemcpyHostToDevice, stream));
+  else
+    CUDA_OK(cudaMemcpyAsync(d_tips.p, tips32.data(), tips32.size() * 4, cudaMemcpyHostToDevice, stream));
   CUDA_OK(cudaMemcpyAsync(d_weights.p, weights.data(), N * 8, cudaMemcpyHostToDevice, stream));
   CUDA_OK(cudaMemcpyAsync(d_unit_part.p, unit_part.data(), n_units * 4, cudaMemcpyHostToDevice, stream));
   CUDA_OK(cudaMemcpyAsync(d_fwd.p, fwd.data(), fwd.size() * sizeof(FwdOp), cudaMemcpyHostToDevice, stream));
@@ -520,7 +529,7 @@ void netlk_ctx::upload_probs() {
 void netlk_ctx::enqueue(bool pm, bool fwd_on, bool reduce, bool mixk, bool bwd_on) {
   prof_mark(-1);
   if (pm) {
-    launch_pmatrix(stream, P, topo.n_edges, R, d_lambda.as<double>(), d_U.as<double>(), d_Uinv.as<double>(),
+    launch_pmatrix(stream, P, topo.n_edges, R, S, d_lambda.as<double>(), d_U.as<double>(), d_Uinv.as<double>(),
                    d_rates.as<double>(), d_brlen.as<double>(), d_pmat64.as<double>(),
                    opts.precision == NETLK_FP32 ? d_pmat32.as<float>() : nullptr);
     prof_mark(0);
@@ -528,7 +537,10 @@ void netlk_ctx::enqueue(bool pm, bool fwd_on, bool reduce, bool mixk, bool bwd_o
   const SweepParams sp = sweep();
   const MixParams mp = mix();
   if (fwd_on) {
-    launch_forward(stream, opts.precision, R, fwd_shape, sp, fwd_level_begin.data(), dag.n_levels);
+    if (S == 20)
+      launch_sweep20(stream, opts.precision, R, false, sp, fwd_level_begin.data(), dag.n_levels);
+    else
+      launch_forward(stream, opts.precision, R, fwd_shape, sp, fwd_level_begin.data(), dag.n_levels);
     prof_mark(1);
   }
   if (reduce) {
@@ -540,7 +552,10 @@ void netlk_ctx::enqueue(bool pm, bool fwd_on, bool reduce, bool mixk, bool bwd_o
     prof_mark(3);
   }
   if (bwd_on && !bwd.empty()) {
-    launch_backward(stream, opts.precision, R, bwd_shape, sp, bwd_level_begin.data(), dag.n_levels);
+    if (S == 20)
+      launch_sweep20(stream, opts.precision, R, true, sp, bwd_level_begin.data(), dag.n_levels);
+    else
+      launch_backward(stream, opts.precision, R, bwd_shape, sp, bwd_level_begin.data(), dag.n_levels);
     prof_mark(4);
     launch_grad_reduce(stream, (int)bwd.size(), topo.n_edges, n_units, d_edge_begin.as<int32_t>(),
                        d_edge_entries.as<int32_t>(), d_grad_partial.as<double>(), d_op_sum.as<double>(),
@@ -575,7 +590,7 @@ void netlk_ctx::run(cudaGraphExec_t *cache, bool pm, bool fwd_on, bool reduce, b
 // adjoint sweep sees real seeds) and keeps the fastest for the CUDA graphs.
 void netlk_ctx::autotune() {
   tuned = true;
-  const int ns = num_shapes(opts.precision, R);
+  const int ns = S == 4 ? num_shapes(opts.precision, R) : 1;
   tune_fwd_ms.assign(ns, 0.0);
   tune_bwd_ms.assign(ns, 0.0);
   if (const char *forced = std::getenv("NETLK_SHAPES")) {  // "fwd,bwd": fixed shapes, no timing
@@ -746,9 +761,10 @@ int netlk_create(const netlk_topology *topo, const netlk_partition *in_parts, in
     c->P = n_parts;
     c->S = in_parts[0].states;
     c->R = in_parts[0].rate_cats;
-    if (c->S != 4) throw Error(NETLK_ERR_UNSUPPORTED, "this build evaluates 4-state (DNA) partitions");
-    if (c->R != 1 && c->R != 2 && c->R != 4 && c->R != 8)
-      throw Error(NETLK_ERR_UNSUPPORTED, "rate_cats must be 1, 2, 4 or 8");
+    if (c->S != 4 && c->S != 20)
+      throw Error(NETLK_ERR_UNSUPPORTED, "states must be 4 (DNA) or 20 (protein)");
+    if (c->R != 1 && c->R != 2 && c->R != 4 && (c->R != 8 || c->S != 4))
+      throw Error(NETLK_ERR_UNSUPPORTED, "rate_cats must be 1, 2, 4 or 8 (at most 4 with 20 states)");
     c->parts.resize(n_parts);
     for (int p = 0; p < n_parts; ++p) {
       const netlk_partition &ip = in_parts[p];

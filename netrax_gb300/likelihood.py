@@ -64,6 +64,8 @@ class NetworkLikelihood:
         topo.ret_second_edge = _ptr(arr(network.ret_second_edge, np.int32), ctypes.c_int32)
         parts = (N.Partition * self.n_parts)()
         self.n_patterns = []
+        self.states = getattr(partitions[0], "states", 4)
+        self.rate_cats = getattr(partitions[0], "rate_cats", 4)
         for i, pd in enumerate(partitions):
             p = parts[i]
             p.states = getattr(pd, "states", 4)
@@ -208,11 +210,11 @@ class NetworkLikelihood:
 
     def get_clv(self, variant, part):
         n = self.n_patterns[part]
-        clv = np.zeros(n * 16)
+        clv = np.zeros(n * self.rate_cats * self.states)
         sc = np.zeros(n, np.int32)
         N.check(N.lib().netlk_get_clv(self._h, variant, part, _ptr(clv, ctypes.c_double),
                                       _ptr(sc, ctypes.c_int32)), self._h)
-        return clv.reshape(n, 4, 4), sc
+        return clv.reshape(n, self.rate_cats, self.states), sc
 
     # ------------------------------------------------ device-resident stepping
     def set_branch_lengths_device(self, dev_ptr):

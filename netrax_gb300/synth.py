@@ -145,6 +145,12 @@ def random_network_newick(rng, n_taxa, n_ret, mean_brlen=0.1):
 
 def simulate_dna(rng, net: NetworkDesc, n_sites, freqs, exch, alpha, rate_cats=4):
     """Simulate DNA columns on displayed trees; returns codes [n_tips][n_sites]."""
+    return simulate(rng, net, n_sites, freqs, exch, alpha, rate_cats)
+
+
+def simulate(rng, net: NetworkDesc, n_sites, freqs, exch, alpha, rate_cats=4):
+    """Simulate columns of any state count on displayed trees; returns state
+    bitmasks (1 << state) [n_tips][n_sites]."""
     from . import model
     lam, U, Uinv = model.eigen(freqs, exch)
     rates = model.gamma_mean_rates(alpha, rate_cats)
@@ -154,7 +160,8 @@ def simulate_dna(rng, net: NetworkDesc, n_sites, freqs, exch, alpha, rate_cats=4
     cat = rng.integers(0, rate_cats, size=n_sites)
     state = np.full((n_nodes, n_sites), -1, np.int64)
     cumf = np.cumsum(freqs)
-    state[net.root] = np.minimum(np.searchsorted(cumf, rng.uniform(size=n_sites) * cumf[-1]), 3)
+    S = len(freqs)
+    state[net.root] = np.minimum(np.searchsorted(cumf, rng.uniform(size=n_sites) * cumf[-1]), S - 1)
     ret_index = {int(v): k for k, v in enumerate(net.ret_node)}
     # parents before children
     order = [net.root]
@@ -191,13 +198,30 @@ def simulate_dna(rng, net: NetworkDesc, n_sites, freqs, exch, alpha, rate_cats=4
         rows = np.clip(rows, 0.0, None)
         cum = np.cumsum(rows, axis=1)
         u = rng.uniform(size=n_sites) * cum[:, -1]
-        state[c] = np.minimum((u[:, None] > cum).sum(axis=1), 3)
+        state[c] = np.minimum((u[:, None] > cum).sum(axis=1), S - 1)
     return (1 << state[:net.n_tips]).astype(np.uint32)
 
 
 def compress(codes):
     cols, counts = np.unique(codes.T, axis=0, return_counts=True)
     return np.ascontiguousarray(cols.T.astype(np.uint32)), counts.astype(np.float64)
+
+
+def make_protein_workload(name, n_taxa, n_ret, partition_sites, seed, alpha=0.8):
+    """LG-like 20-state model: 190 exchangeabilities ~ Gamma(1, 1), frequencies
+    ~ Dirichlet(1^20), Gamma shape alpha, 4 mean-rate categories."""
+    rng = np.random.default_rng(seed)
+    text = random_network_newick(rng, n_taxa, n_ret)
+    net = parse_extended_newick(text)
+    parts = []
+    for ns in partition_sites:
+        freqs = np.maximum(rng.dirichlet(np.ones(20)), 1e-3)
+        freqs /= freqs.sum()
+        exch = np.maximum(rng.gamma(1.0, 1.0, size=190), 1e-3)
+        codes = simulate(rng, net, ns, freqs, exch, alpha)
+        pat, w = compress(codes)
+        parts.append(PartitionData(pat, w, freqs, exch, alpha, ns, states=20))
+    return Workload(name, text, net, parts, seed)
 
 
 def make_workload(name, n_taxa, n_ret, partition_sites, seed, alpha=0.8):
@@ -222,7 +246,7 @@ CONFIG1_SITES = [500, 1000, 2000, 3000, 5000, 7000, 10000, 12000, 15000, 20000]
 
 
 def config(idx, scale=1.0):
-    """BASELINE configurations 0-2 (DNA). ``scale`` shrinks the site counts."""
+    """Configurations 0-2 (DNA) and 3 (protein). ``scale`` shrinks the site counts."""
     s = lambda n: max(32, int(round(n * scale)))
     if idx == 0:
         return make_workload("20 taxa / 1 reticulation / 1k DNA sites", 20, 1, [s(1000)], CONFIG_SEEDS[0])
@@ -232,4 +256,7 @@ def config(idx, scale=1.0):
     if idx == 2:
         return make_workload("100 taxa / 8 reticulations / 100k DNA sites", 100, 8, [s(100000)],
                              CONFIG_SEEDS[2])
-    raise ValueError("config %d is not a DNA configuration" % idx)
+    if idx == 3:
+        return make_protein_workload("40 taxa / 3 reticulations / 50k protein sites", 40, 3, [s(50000)],
+                                     CONFIG_SEEDS[3])
+    raise ValueError("config %d is not built" % idx)

@@ -29,14 +29,15 @@ class GoldenPartition:
         self.freqs = np.array(d["freqs"], dtype=np.float64)
         self.exch = np.array(d["exch"], dtype=np.float64)
         self.alpha = float(d["alpha"])
-        self.states = 4
+        self.states = int(d.get("states", 4))
         self.rate_cats = 4
 
 
 def golden_cases():
     ref = load_golden("reference_cases.json")["cases"]
     syn = load_golden("synthetic_cases.json")["cases"]
-    return ref + syn
+    pro = load_golden("protein_cases.json")["cases"]
+    return ref + syn + pro
 
 
 @pytest.fixture(scope="session")

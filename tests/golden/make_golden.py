@@ -11,6 +11,8 @@ Cases:
   GTR+G4 model with AVERAGE and BEST: network logL, per-partition logL,
   per-displayed-tree logL, the naive 2^r evaluation, the displayed-tree DAG
   (covered configuration sets per node), central-difference gradients.
+* ``protein_cases.json`` - 20-state (LG-like) cases on small seeded networks,
+  with gaps and an ambiguity code.
 * ``synthetic_cases.json`` - seeded synthetic networks (several partitions,
   and one deep 200-taxon case whose FP64 CLVs trigger the 2^256 scaling)
   with the same outputs plus per-variant scale-counter checksums.
@@ -182,6 +184,39 @@ def synthetic_cases():
     return out
 
 
+def protein_cases():
+    """20-state cases: an LG-like model on small seeded networks."""
+    from netrax_gb300 import synth
+    from netrax_gb300.network import parse_extended_newick
+    specs = [("protein_8taxa_2ret", 8, 2, [150], 21), ("protein_10taxa_3ret_2parts", 10, 3, [120, 90], 22)]
+    out = []
+    for name, nt, nr, sites, seed in specs:
+        rng = np.random.default_rng(seed)
+        text = synth.random_network_newick(rng, nt, nr)
+        pnet = parse_extended_newick(text)
+        parts = []
+        for ns in sites:
+            freqs = np.maximum(rng.dirichlet(np.ones(20)), 1e-3)
+            freqs /= freqs.sum()
+            exch = np.maximum(rng.gamma(1.0, 1.0, size=190), 1e-3)
+            codes = synth.simulate(rng, pnet, ns, freqs, exch, 0.8)
+            if name.endswith("2parts"):
+                codes[0, :5] = (1 << 20) - 1  # gaps: every state
+                codes[1, 3] = (1 << 2) | (1 << 7)  # an ambiguity
+            pat, w = synth.compress(codes)
+            parts.append({"freqs": freqs.tolist(), "exch": exch.tolist(), "alpha": 0.8,
+                          "tip_states": pat.tolist(), "weights": w.tolist(), "states": 20})
+        net = newick.parse_newick(text)
+        case = {"name": name, "newick": text, "partitions": parts, "states": 20}
+        for variant in ("AVERAGE", "BEST"):
+            res, orc = score(net, parts, variant, with_grad=True, with_naive=nr <= 3, scalers=True)
+            case[variant] = res
+        case["dag"] = covered_lists(orc)
+        out.append(case)
+        print(name, case["AVERAGE"]["logl"], case["BEST"]["logl"], flush=True)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
@@ -190,6 +225,8 @@ def main():
         json.dump({"model": MODEL, "cases": reference_cases(a.reference)}, f)
     with open(os.path.join(HERE, "synthetic_cases.json"), "w") as f:
         json.dump({"cases": synthetic_cases()}, f)
+    with open(os.path.join(HERE, "protein_cases.json"), "w") as f:
+        json.dump({"cases": protein_cases()}, f)
 
 
 if __name__ == "__main__":

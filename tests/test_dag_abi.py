@@ -126,9 +126,18 @@ def test_invalid_arguments_return_status():
     assert e.value.status == 2
     p2 = GoldenPartition({"tip_states": [[1, 0], [2, 4], [8, 1]], "weights": [1, 2],
                           "freqs": [.25] * 4, "exch": [1] * 6, "alpha": 1.0})
-    p2.states = 20
+    p2.states = 61  # codon models are not on this path
     with pytest.raises(_native.NetlkError) as e:
         NetworkLikelihood(net, [p2], host_only=True)
+    assert e.value.status == 7
+    p3 = GoldenPartition({"tip_states": [[1, 0], [2, 4], [8, 1]], "weights": [1, 2],
+                          "freqs": [.25] * 4, "exch": [1] * 6, "alpha": 1.0})
+    p3.rate_cats = 8
+    p3.states = 20
+    p3.freqs = np.full(20, 0.05)
+    p3.exch = np.ones(190)
+    with pytest.raises(_native.NetlkError) as e:
+        NetworkLikelihood(net, [p3], host_only=True)
     assert e.value.status == 7
 
 
