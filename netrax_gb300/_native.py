@@ -58,7 +58,8 @@ class Options(ctypes.Structure):
     _fields_ = [("variant", ctypes.c_int32), ("precision", ctypes.c_int32),
                 ("min_interesting_tree_logprob", ctypes.c_double),
                 ("device", ctypes.c_int32), ("use_cuda_graph", ctypes.c_int32),
-                ("host_only", ctypes.c_int32), ("autotune", ctypes.c_int32)]
+                ("host_only", ctypes.c_int32), ("autotune", ctypes.c_int32),
+                ("tensor_cores", ctypes.c_int32)]
 
 
 class DagStats(ctypes.Structure):

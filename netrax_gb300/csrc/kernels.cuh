@@ -70,6 +70,7 @@ struct SweepParams {
   double *site_partial;         // [n_slots][n_units_fwd]
   const double *seeds;          // [n_slots][n_parts]
   double *grad_partial;         // [n_bwd_ops][n_units][2] per-warp edge terms (a, b)
+  int32_t *fault;               // set to 1 by a sweep whose bounded wait gave up
 };
 
 struct MixParams {
@@ -107,6 +108,10 @@ void launch_grad_reduce(cudaStream_t s, int n_ops, int n_edges, int n_bx, const 
 // 20-state forward (backward = false) or adjoint sweep, one launch per level.
 void launch_sweep20(cudaStream_t s, int precision, int R, bool backward, const SweepParams &p,
                     const int32_t *level_begin, int n_levels);
+// Tensor-core (tcgen05) forward sweep for 20-state FP32 contexts with 4 rate
+// categories; one launch per level.
+bool sweep20_tc_supported(int precision, int R);
+void launch_forward20_tc(cudaStream_t s, const SweepParams &p, const int32_t *level_begin, int n_levels, int n_sms);
 // Number of kernel launches issued by the launchers above (host counter).
 int64_t launches_issued();
 void add_launches(int64_t n);

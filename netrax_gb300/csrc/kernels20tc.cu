@@ -1,0 +1,367 @@
+// Tensor-core forward sweep for 20-state partitions with 4 rate categories,
+// FP32 CLVs (tcgen05, kind::tf32, accumulators in TMEM).
+//
+// Per op and tile of 128 patterns (the MMA's M), child c's contribution for
+// rate r is the GEMM D[128 x 20] = A[128 x 20] . P_r^T with A the child's CLV
+// rows. The CLV tile [128 patterns][4 rates x 20 states] is already K-major:
+// rate r's operand is columns 20r..20r+19 of it. K runs in steps of 8, so
+// rate r reads columns 20r..20r+23 and B's columns 20..23 are zero (the four
+// extra A columns are the next rate's first states, or a zero pad chunk).
+//
+// FP32 accuracy from TF32 inputs (3xTF32): every operand x = hi + lo with hi
+// = x rounded to TF32 and lo = x - hi rounded to TF32. One N=64 MMA computes
+// A_hi . [B_hi | B_lo] into columns [0, 64) and one N=32 MMA adds A_lo . B_hi
+// into columns [0, 32); the epilogue adds column i and 32 + i. Tip children
+// are exact 0/1 rows and need no lo part.
+//
+// A CTA (one per SM) walks a contiguous range of (op, tile) items; 256
+// threads split the child tiles into shared memory, one thread issues the
+// MMAs while all threads fetch the next item's tiles, and 8 warps
+// read TMEM (warp w: patterns 32(w%4)..+31, rates 2(w/4) and 2(w/4)+1),
+// multiply the children, rescale and store. TMEM: 512 columns, child c rate r
+// at column 256c + 64r, so the kernel runs one CTA per SM (its shared memory
+// allows no more).
+#include "kernels.cuh"
+#include "kernels_common.cuh"
+#include "tc.cuh"
+
+namespace netlk {
+namespace {
+
+constexpr int kTM = 128;                       // patterns per tile
+constexpr int kTThreads = 256;
+constexpr int kAChunk = kTM * 16 + 16;         // one 4-column slab of a tile (+16 B: bank spread)
+constexpr int kAChunks = 21;                   // 80 columns + one zero slab
+constexpr int kABytes = kAChunks * kAChunk;    // 43344
+constexpr int kBChunk = 64 * 16;               // 64 B rows (hi 0-31, lo 32-63) x 4 columns
+constexpr int kBBytes = 6 * kBChunk;           // K = 24
+constexpr int kSmemA = 4 * kABytes;            // [child][hi, lo]
+constexpr int kOutRow = 336;                   // staged output row: 320 B + 16 B bank spread
+static_assert(kTM * kOutRow <= kABytes, "output staging fits one A tile");
+constexpr int kSmemB = 8 * kBBytes;            // [child][rate]
+constexpr int kSmemMisc = 16 + 4 * kTM * 4;    // mbarrier, TMEM address, two exchange arrays
+constexpr int kSmemBytes = kSmemA + kSmemB + kSmemMisc;
+static_assert(kSmemBytes <= 232448, "shared memory of one CTA");
+
+constexpr uint32_t kIdN64 = tc::idesc_tf32(128, 64);
+constexpr uint32_t kIdN32 = tc::idesc_tf32(128, 32);
+
+// Child kinds: absent (the fake all-ones child), tip (0/1 rows), inner (CLV).
+enum { kAbsent = 0, kTip = 1, kInner = 2 };
+
+__device__ __forceinline__ int child_kind(int32_t ref) {
+  return ref >= 0 ? kInner : (ref == INT32_MIN ? kAbsent : kTip);
+}
+
+// TF32 split with round-to-nearest parts: x = hi + lo, |lo| <= 2^-12 |x|, and
+// lo itself rounded to TF32 (so the tensor core reads both exactly).
+__device__ __forceinline__ void split4(const float4 &x, float4 &hi, float4 &lo) {
+  hi = make_float4(tc::tf32_rna(x.x), tc::tf32_rna(x.y), tc::tf32_rna(x.z), tc::tf32_rna(x.w));
+  lo = make_float4(tc::tf32_rna(x.x - hi.x), tc::tf32_rna(x.y - hi.y), tc::tf32_rna(x.z - hi.z), tc::tf32_rna(x.w - hi.w));
+}
+
+// Stages P_r (20x20, row = output state) of both children as B tiles: row
+// n < 20 holds hi(P[n][k]), row 32 + n holds lo(P[n][k]). Rows 20-31, 52-63
+// and columns 20-23 stay zero from the kernel's start.
+__device__ __forceinline__ void stage_b(const SweepParams &p, unsigned char *sB, int part, int ea, int eb) {
+  const float4 *pm = reinterpret_cast<const float4 *>(static_cast<const float *>(p.pmat) +
+                                                      (size_t)part * p.n_edges * 1600);
+  float4 v[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int f = threadIdx.x + u * kTThreads, c = f / 400, e = c ? eb : ea;
+    if (f < 800 && e >= 0) v[u] = __ldg(pm + (size_t)e * 400 + (f - c * 400));
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int f = threadIdx.x + u * kTThreads, c = f / 400, e = c ? eb : ea;
+    if (f >= 800 || e < 0) continue;
+    const int rem = f - c * 400, r = rem / 100, e2 = rem - r * 100, i = e2 / 5, j4 = e2 - i * 5;
+    unsigned char *base = sB + (c * 4 + r) * kBBytes + j4 * kBChunk + (i & 7) * 16;
+    float4 hi, lo;
+    split4(v[u], hi, lo);
+    *reinterpret_cast<float4 *>(base + (i >> 3) * 128) = hi;
+    *reinterpret_cast<float4 *>(base + (4 + (i >> 3)) * 128) = lo;
+  }
+}
+
+// Issues the global loads of child `ref` of tile g0 into registers: CLV
+// float4s for an inner child, the tip's state masks (in .x) for a tip.
+__device__ __forceinline__ void fetch(const SweepParams &p, int kind, int32_t ref, size_t g0, float4 (&x)[10]) {
+  const size_t N = (size_t)p.n_patterns;
+  if (kind == kInner) {
+    const float4 *src = reinterpret_cast<const float4 *>(static_cast<const float *>(p.clv) + ((size_t)ref * N + g0) * 80);
+#pragma unroll
+    for (int i = 0; i < 10; ++i) x[i] = __ldg(src + threadIdx.x + i * kTThreads);
+  } else if (kind == kTip) {
+    const uint32_t *code = p.tips32 + (size_t)(-1 - ref) * N + g0;
+#pragma unroll
+    for (int i = 0; i < 10; ++i) x[i].x = __uint_as_float(__ldg(code + (threadIdx.x + i * kTThreads) / 20));
+  }
+}
+
+// Writes fetched registers into the A tiles: split hi/lo for an inner child,
+// 0/1 expansion of the mask (columns 4kc.. = rate kc/5, states 4(kc%5)..) for a tip.
+__device__ __forceinline__ void put(int kind, const float4 (&x)[10], unsigned char *sAh, unsigned char *sAl) {
+  if (kind == kInner) {
+#pragma unroll
+    for (int i = 0; i < 10; ++i) {
+      const int f = threadIdx.x + i * kTThreads, m = f / 20, kc = f - m * 20, off = kc * kAChunk + m * 16;
+      float4 hi, lo;
+      split4(x[i], hi, lo);
+      *reinterpret_cast<float4 *>(sAh + off) = hi;
+      *reinterpret_cast<float4 *>(sAl + off) = lo;
+    }
+  } else if (kind == kTip) {
+#pragma unroll
+    for (int i = 0; i < 10; ++i) {
+      const int f = threadIdx.x + i * kTThreads, m = f / 20, kc = f - m * 20;
+      const uint32_t b = __float_as_uint(x[i].x) >> (4 * (kc % 5));
+      *reinterpret_cast<float4 *>(sAh + kc * kAChunk + m * 16) =
+          make_float4((float)(b & 1u), (float)((b >> 1) & 1u), (float)((b >> 2) & 1u), (float)((b >> 3) & 1u));
+    }
+  }
+}
+
+// Reads the 20 states of one (child, rate) accumulator for this lane's
+// pattern: columns i (hi . B_hi + lo . B_hi) plus 32 + i (hi . B_lo).
+__device__ __forceinline__ void read_d(uint32_t t, float (&v)[20]) {
+  uint32_t a[16], b[4], c[16], d[4];
+  tc::ld16(t, a);
+  tc::ld4(t + 16, b);
+  tc::ld16(t + 32, c);
+  tc::ld4(t + 48, d);
+  tc::ld_wait();
+  tc::ld_fence(a);
+  tc::ld_fence(b);
+  tc::ld_fence(c);
+  tc::ld_fence(d);
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(a[i]) + __uint_as_float(c[i]);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) v[16 + i] = __uint_as_float(b[i]) + __uint_as_float(d[i]);
+}
+
+// Persistent over the level: CTA b takes work items [b W / G, (b+1) W / G)
+// of the W = ops x tiles items (item = op * n_tiles + tile), so consecutive
+// items share the op and its staged B tiles. The next item's child tiles are
+// fetched into registers while the current item's MMAs and epilogue run.
+__global__ void __launch_bounds__(kTThreads, 1)
+    forward20_tc_kernel(const SweepParams p, int op_begin, int n_ops, int n_tiles) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  unsigned char *sA = smem;
+  unsigned char *sB = smem + kSmemA;
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(sB + kSmemB);
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(sB + kSmemB + 8);
+  float *s_max = reinterpret_cast<float *>(sB + kSmemB + 16);  // [2][128]
+  float *s_t = s_max + 2 * kTM;                                 // [2][128]
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const size_t N = (size_t)p.n_patterns;
+  const long long W = (long long)n_ops * n_tiles;
+  const int item_begin = (int)(W * blockIdx.x / gridDim.x), item_end = (int)(W * (blockIdx.x + 1) / gridDim.x);
+
+  if (warp == 0) tc::tmem_alloc(tc::smem_u32(tmem_slot), 512);
+  if (threadIdx.x == 0) tc::mbar_init(tc::smem_u32(mbar), 1);
+  // zero slab 20 of every A tile (rate 3's last K step reads it) and all of B
+  for (int i = threadIdx.x; i < 4 * kTM; i += kTThreads)
+    *reinterpret_cast<float4 *>(sA + (i / kTM) * kABytes + 20 * kAChunk + (i % kTM) * 16) = make_float4(0, 0, 0, 0);
+  for (int i = threadIdx.x; i < kSmemB / 16; i += kTThreads)
+    reinterpret_cast<float4 *>(sB)[i] = make_float4(0, 0, 0, 0);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tmem_slot;
+
+  const int q = warp & 3, h = warp >> 2;
+  const int m = 32 * q + lane;
+  const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
+  int staged_op = -1, staged_part = -1;
+  uint32_t phase = 0;
+  bool failed = false;
+
+  int oi = item_begin / n_tiles;
+  FwdOp op = load_fwd_op(p.fwd_ops, op_begin + oi);
+  int ka = child_kind(op.a), kb = child_kind(op.b);
+  float4 xa[10], xb[10];
+  if (item_begin < item_end) {
+    const size_t g0 = (size_t)(item_begin - oi * n_tiles) * kTM;
+    fetch(p, ka, op.a, g0, xa);
+    fetch(p, kb, op.b, g0, xb);
+  }
+  for (int item = item_begin; item < item_end; ++item) {
+    const int tile = item - oi * n_tiles;
+    const size_t g0 = (size_t)tile * kTM;
+    // partitions are padded to whole 256-pattern blocks: a tile has one partition
+    const int part = p.unit_part[g0 / 16];
+    if (oi != staged_op || part != staged_part) {
+      stage_b(p, sB, part, op.ea, kb == kAbsent ? -1 : op.eb);
+      staged_op = oi;
+      staged_part = part;
+    }
+    put(ka, xa, sA, sA + kABytes);
+    put(kb, xb, sA + 2 * kABytes, sA + 3 * kABytes);
+    tc::fence_proxy_async();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      tc::fence_after_sync();
+#pragma unroll 1
+      for (int c = 0; c < 2; ++c) {
+        const int kind = c ? kb : ka;
+        if (kind == kAbsent) continue;
+        // descriptors of the tiles' first slabs; a K step adds its byte offset / 16
+        const uint64_t dah = tc::smem_desc(tc::smem_u32(sA + (2 * c) * kABytes), kAChunk, 128);
+        const uint64_t dal = dah + (kABytes >> 4);
+        const uint64_t db = tc::smem_desc(tc::smem_u32(sB + (c * 4) * kBBytes), kBChunk, 128);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const uint32_t d = tmem + 256 * c + 64 * r;
+#pragma unroll
+          for (int s = 0; s < 3; ++s) {
+            const uint32_t ko = ((5 * r + 2 * s) * kAChunk) >> 4;
+            const uint64_t bd = db + ((r * kBBytes + 2 * s * kBChunk) >> 4);
+            tc::mma_tf32(d, dah + ko, bd, kIdN64, s > 0);
+            if (kind == kInner) tc::mma_tf32(d, dal + ko, bd, kIdN32, 1);
+          }
+        }
+      }
+      tc::commit(tc::smem_u32(mbar));
+    }
+    // the current item's op, for the epilogue; then prefetch the next item
+    const FwdOp cur = op;
+    const int cka = ka, ckb = kb;
+    const size_t g = g0 + m;
+    const int sab = (cka == kInner ? p.scaler[(size_t)cur.a * N + g] : 0) +
+                    (ckb == kInner ? p.scaler[(size_t)cur.b * N + g] : 0);
+    const double wg = p.weights[g];
+    if (item + 1 < item_end) {
+      const int noi = (item + 1) / n_tiles;
+      if (noi != oi) {
+        oi = noi;
+        op = load_fwd_op(p.fwd_ops, op_begin + oi);
+        ka = child_kind(op.a);
+        kb = child_kind(op.b);
+      }
+      const size_t gn = (size_t)(item + 1 - oi * n_tiles) * kTM;
+      fetch(p, ka, op.a, gn, xa);
+      fetch(p, kb, op.b, gn, xb);
+    }
+    const bool ok = tc::mbar_wait(tc::smem_u32(mbar), phase);
+    phase ^= 1;
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+      break;
+    }
+    tc::fence_after_sync();
+
+    // ------------------------------------------------------------ epilogue
+    float v[2][20];
+    float mx = 0.f;
+#pragma unroll
+    for (int rr = 0; rr < 2; ++rr) {
+      const int r = 2 * h + rr;
+      read_d(lane_base + 64 * r, v[rr]);
+      if (ckb != kAbsent) {
+        float w[20];
+        read_d(lane_base + 256 + 64 * r, w);
+#pragma unroll
+        for (int i = 0; i < 20; ++i) v[rr][i] *= w[i];
+      }
+#pragma unroll
+      for (int i = 0; i < 20; ++i) mx = fmaxf(mx, v[rr][i]);
+    }
+    s_max[h * kTM + m] = mx;
+    __syncthreads();
+    mx = fmaxf(s_max[m], s_max[kTM + m]);
+    int sc = sab;
+    if (mx < 0x1p-32f && mx > 0.0f) {
+      int e;
+      frexpf(mx, &e);
+#pragma unroll
+      for (int rr = 0; rr < 2; ++rr)
+#pragma unroll
+        for (int i = 0; i < 20; ++i) v[rr][i] = ldexpf(v[rr][i], -e);
+      sc -= e;
+    }
+    // output tile through shared memory (child a's hi tile is free now): rows
+    // of kOutRow bytes, so the 8 lanes of a 16-byte store phase hit distinct banks
+    {
+      unsigned char *row = sA + m * kOutRow + 160 * h;
+#pragma unroll
+      for (int j = 0; j < 10; ++j) {
+        const int rr = j / 5, i = 4 * (j % 5);
+        *reinterpret_cast<float4 *>(row + 16 * j) = make_float4(v[rr][i], v[rr][i + 1], v[rr][i + 2], v[rr][i + 3]);
+      }
+    }
+    if (h == 0) p.scaler[(size_t)cur.out * N + g] = sc;
+    if (cur.slot >= 0) {
+      float t = 0.f;
+#pragma unroll
+      for (int rr = 0; rr < 2; ++rr) {
+        float u = 0.f;
+#pragma unroll
+        for (int i = 0; i < 20; ++i) u += (float)p.freqs[part * 20 + i] * v[rr][i];
+        t += (float)p.rate_weights[part * 4 + 2 * h + rr] * u;
+      }
+      s_t[h * kTM + m] = t;
+      __syncthreads();
+      if (h == 0) {
+        t = s_t[m] + s_t[kTM + m];
+        double ll = 0.0;
+        if (wg != 0.0) ll = wg * ((double)logf(t) + (double)sc * Scale<float>::kLogUnit);
+        ll = warp_sum(ll);
+        if (lane == 0) p.site_partial[(size_t)cur.slot * p.n_units_fwd + g0 / 32 + q] = ll;
+      }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    {  // coalesced copy of the staged tile: 128 rows x 320 contiguous bytes in the CLV
+      float4 *dst = reinterpret_cast<float4 *>(static_cast<float *>(p.clv) + ((size_t)cur.out * N + g0) * 80);
+#pragma unroll
+      for (int i = 0; i < 10; ++i) {
+        const int f = threadIdx.x + i * kTThreads, r = f / 20;
+        dst[f] = *reinterpret_cast<const float4 *>(sA + r * kOutRow + (f - r * 20) * 16);
+      }
+    }
+    __syncthreads();
+    // the staging rows overlap the tile's zero slab: clear it again
+    if (threadIdx.x < (kTM * kOutRow - 20 * kAChunk) / 16)
+      *reinterpret_cast<float4 *>(sA + 20 * kAChunk + 16 * threadIdx.x) = make_float4(0, 0, 0, 0);
+  }
+  if (failed) {
+    if (threadIdx.x == 0) atomicExch(p.fault, 1);
+    // the MMAs may still run: give them one more bounded wait before TMEM is released
+    tc::mbar_wait(tc::smem_u32(mbar), phase ^ 1);
+    __syncthreads();
+  }
+  tc::fence_after_sync();
+  if (warp == 0) tc::tmem_free(tmem, 512);
+}
+
+}  // namespace
+
+bool sweep20_tc_supported(int precision, int R) { return precision == 1 && R == 4; }
+
+void launch_forward20_tc(cudaStream_t s, const SweepParams &p, const int32_t *level_begin, int n_levels,
+                         int n_sms) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  static bool attr_set[64] = {};
+  if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+    cudaFuncSetAttribute(forward20_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+    attr_set[dev] = true;
+  }
+  const int n_tiles = (int)(p.n_patterns / kTM);
+  int launched = 0;
+  for (int L = 0; L < n_levels; ++L) {
+    const int n = level_begin[L + 1] - level_begin[L];
+    if (n <= 0) continue;
+    const long long items = (long long)n * n_tiles;
+    const int grid = (int)(items < n_sms ? items : n_sms);  // one CTA per SM
+    forward20_tc_kernel<<<grid, kTThreads, kSmemBytes, s>>>(p, level_begin[L], n, n_tiles);
+    ++launched;
+  }
+  add_launches(launched);
+}
+
+}  // namespace netlk

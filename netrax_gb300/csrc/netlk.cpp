@@ -102,6 +102,7 @@ struct netlk_ctx {
   int fwd_launches = 0, bwd_launches = 0;
   int fwd_shape = 0, bwd_shape = 0, sms = 0;
   bool tuned = false;
+  bool use_tc = false;  // 20-state FP32 forward on the tensor cores
   std::vector<double> tune_fwd_ms, tune_bwd_ms;
   int64_t site_updates = 0, tip_uses = 0, fake_uses = 0;
   // device
@@ -195,6 +196,7 @@ struct netlk_ctx {
     p.site_partial = d_site_partial.as<double>();
     p.seeds = d_seeds.as<double>();
     p.grad_partial = d_grad_partial.as<double>();
+    p.fault = reinterpret_cast<int32_t *>(d_out.as<double>() + 2 + P + topo.n_ret);
     return p;
   }
 
@@ -445,7 +447,7 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
   d_slot_begin.alloc(slot_begin.size() * 4, dev_bytes);
   d_slot_roots.alloc(slot_roots.size() * 4, dev_bytes);
   d_parts.alloc(P * sizeof(DevPartition), dev_bytes);
-  d_out.alloc((2 + P + topo.n_ret) * 8, dev_bytes);
+  d_out.alloc((3 + P + topo.n_ret) * 8, dev_bytes);  // + the sweeps' fault word
   d_grad.alloc(topo.n_edges * 8, dev_bytes);
 
   CUDA_OK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
@@ -482,7 +484,7 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
   h_brlen.alloc(topo.n_edges * 8);
   h_root_lp.alloc(dag.roots.size() * 8);
   h_root_dlp.alloc(dag.roots.size() * std::max(1, topo.n_ret) * 8);
-  h_out.alloc((2 + P + topo.n_ret) * 8);
+  h_out.alloc((3 + P + topo.n_ret) * 8);
   h_grad.alloc(topo.n_edges * 8);
   h_tree.alloc((size_t)n_slots * P * 8);
 }
@@ -537,7 +539,10 @@ void netlk_ctx::enqueue(bool pm, bool fwd_on, bool reduce, bool mixk, bool bwd_o
   const SweepParams sp = sweep();
   const MixParams mp = mix();
   if (fwd_on) {
-    if (S == 20)
+    if (use_tc) {
+      CUDA_OK(cudaMemsetAsync(sp.fault, 0, 8, stream));
+      launch_forward20_tc(stream, sp, fwd_level_begin.data(), dag.n_levels, sms);
+    } else if (S == 20)
       launch_sweep20(stream, opts.precision, R, false, sp, fwd_level_begin.data(), dag.n_levels);
     else
       launch_forward(stream, opts.precision, R, fwd_shape, sp, fwd_level_begin.data(), dag.n_levels);
@@ -647,7 +652,7 @@ void netlk_ctx::prepare() {
 }
 
 void netlk_ctx::finish(double *total, double *part_logl, double *d_brlen, double *d_ret) {
-  const int nout = 2 + P + topo.n_ret;
+  const int nout = 3 + P + topo.n_ret;
   CUDA_OK(cudaMemcpyAsync(h_out.p, d_out.p, nout * 8, cudaMemcpyDeviceToHost, stream));
   if (d_brlen)
     CUDA_OK(cudaMemcpyAsync(h_grad.p, d_grad.p, topo.n_edges * 8, cudaMemcpyDeviceToHost, stream));
@@ -655,6 +660,8 @@ void netlk_ctx::finish(double *total, double *part_logl, double *d_brlen, double
   CUDA_OK(cudaGetLastError());
   prof_collect();
   const double *o = h_out.as<double>();
+  if (use_tc && *reinterpret_cast<const int32_t *>(o + nout - 1) != 0)
+    throw Error(NETLK_ERR_CUDA, "tensor-core sweep: an MMA completion wait timed out");
   if (o[1] != 0.0 || !std::isfinite(o[0]))
     throw Error(NETLK_ERR_NUMERIC, "Invalid network likelihood: negative infinity or NaN");
   if (total) *total = o[0];
@@ -722,6 +729,7 @@ int netlk_options_default(netlk_options *o) {
   o->use_cuda_graph = 1;
   o->host_only = 0;
   o->autotune = 1;
+  o->tensor_cores = 1;
   return NETLK_OK;
 }
 
@@ -765,6 +773,7 @@ int netlk_create(const netlk_topology *topo, const netlk_partition *in_parts, in
       throw Error(NETLK_ERR_UNSUPPORTED, "states must be 4 (DNA) or 20 (protein)");
     if (c->R != 1 && c->R != 2 && c->R != 4 && (c->R != 8 || c->S != 4))
       throw Error(NETLK_ERR_UNSUPPORTED, "rate_cats must be 1, 2, 4 or 8 (at most 4 with 20 states)");
+    c->use_tc = c->opts.tensor_cores && c->S == 20 && sweep20_tc_supported(c->opts.precision, c->R);
     c->parts.resize(n_parts);
     for (int p = 0; p < n_parts; ++p) {
       const netlk_partition &ip = in_parts[p];

@@ -201,6 +201,30 @@ def test_protein_fp32_matches_fp64_and_oracle():
             assert np.allclose(rb, ra, rtol=1e-3, atol=1e-2)
 
 
+def test_protein_tensor_cores_match_cuda_cores():
+    """The tcgen05 forward (3xTF32, FP32 accumulation) against the CUDA-core
+    FP32 forward and the FP64 run, on a 40-taxon / 3-reticulation protein
+    workload with 2 partitions (tiles must not mix partitions)."""
+    from netrax_gb300 import synth
+    from netrax_gb300.likelihood import NetworkLikelihood
+    w = synth.make_protein_workload("protein 2 partitions", 40, 3, [700, 1300], 77)
+    for variant in ("AVERAGE", "BEST"):
+        with NetworkLikelihood(w.network, w.partitions, variant=variant, precision="fp64") as a, \
+                NetworkLikelihood(w.network, w.partitions, variant=variant, precision="fp32",
+                                  tensor_cores=False) as b, \
+                NetworkLikelihood(w.network, w.partitions, variant=variant, precision="fp32") as c:
+            ta, pa = a.loglikelihood(details=True)[:2]
+            tb, pb = b.loglikelihood(details=True)[:2]
+            tc, pc = c.loglikelihood(details=True)[:2]
+            assert tb == pytest.approx(ta, rel=FP32_REL)
+            assert tc == pytest.approx(ta, rel=FP32_REL)
+            assert np.allclose(pc, pa, rtol=FP32_REL, atol=0)
+            _, ga, ra = a.loglikelihood_gradient()
+            _, gc, rc = c.loglikelihood_gradient()
+            assert np.allclose(gc, ga, rtol=1e-3, atol=1e-2 * max(1.0, np.abs(ga).max() * 1e-3))
+            assert np.allclose(rc, ra, rtol=1e-3, atol=1e-2)
+
+
 def test_protein_sharded_partials_match_whole():
     from netrax_gb300 import synth
     from netrax_gb300.likelihood import NetworkLikelihood
