@@ -294,6 +294,27 @@ int netlk_mix_site_loglikelihoods_noalloc(const double *d_site_logl, int32_t n_t
                                           double min_interesting_tree_logprob, double *d_out,
                                           void *stream);
 
+/* ------------------------------------------------------- batched candidates */
+/* The candidate networks of one search move, scored together. Replaces the
+ * sequential perform / computeLoglikelihood / undo loop over candidates in
+ * filterCandidates (src/search/Filtering.cpp:239-249). A batch holds n
+ * contexts (any topologies and partitions, one device) and captures one
+ * logL + gradient evaluation of each - branch-length upload, the whole
+ * launch sequence, result download - into ONE CUDA graph in which the
+ * contexts' branches run concurrently; every call is one graph launch and
+ * one synchronisation. The contexts stay owned by the caller, must outlive
+ * the batch, and must not be evaluated concurrently with it. Each context
+ * uses the branch lengths of its last netlk_set_branch_lengths
+ * (netlk_set_branch_lengths_device lengths are rejected). Errors return a
+ * status; netlk_last_error(NULL) names the failing candidate. */
+typedef struct netlk_batch netlk_batch;
+int netlk_batch_create(netlk_ctx *const *ctxs, int32_t n, netlk_batch **out);
+/* totals [n]; d_brlen[i] [n_edges of context i] and d_retprob[i]
+ * [n_reticulations of context i] may be NULL (either array or entry). */
+int netlk_batch_loglikelihood_gradient(netlk_batch *batch, double *totals, double *const *d_brlen,
+                                       double *const *d_retprob);
+int netlk_batch_destroy(netlk_batch *batch);
+
 /* ------------------------------------------------------------------- debug */
 /* Copies the CLV (converted to double) and scale counters of one variant:
  * clv [n_patterns*rate_cats*states] and scaler [n_patterns] of partition

@@ -18,7 +18,9 @@ c_double_p = ctypes.POINTER(ctypes.c_double)
 NETLK_OK = 0
 NETLK_AVERAGE, NETLK_BEST = 0, 1
 NETLK_FP64, NETLK_FP32 = 0, 1
+NETLK_ERR_INVALID_ARGUMENT = 1
 NETLK_ERR_NO_DEVICE = 8
+NETLK_ERR_TIMEOUT = 9
 
 STATUS_NAMES = {
     1: "INVALID_ARGUMENT", 2: "TOPOLOGY", 3: "ENUMERATION", 4: "CUDA",
@@ -33,7 +35,8 @@ EXPORTED = [
     "netlk_tree_partials", "netlk_mix_and_backward", "netlk_get_clv", "netlk_get_stream",
     "netlk_launch_count", "netlk_set_branch_lengths_device", "netlk_enqueue",
     "netlk_result_pointers", "netlk_set_profiling", "netlk_kernel_times", "netlk_tuning",
-    "netlk_mix_site_loglikelihoods_noalloc",
+    "netlk_mix_site_loglikelihoods_noalloc", "netlk_batch_create",
+    "netlk_batch_loglikelihood_gradient", "netlk_batch_destroy",
 ]
 
 
@@ -125,6 +128,10 @@ def lib():
         vp, ctypes.c_int32, ctypes.c_int64, vp, ctypes.c_int32, vp, ctypes.c_int32, ctypes.c_double, vp, vp]
     L.netlk_tuning.argtypes = [vp, c_int32_p, c_int32_p, c_double_p, c_double_p, ctypes.c_int32]
     L.netlk_kernel_times.argtypes = [vp, c_double_p, ctypes.POINTER(ctypes.c_int64), ctypes.c_int32]
+    L.netlk_batch_create.argtypes = [ctypes.POINTER(vp), ctypes.c_int32, ctypes.POINTER(vp)]
+    L.netlk_batch_loglikelihood_gradient.argtypes = [vp, c_double_p, ctypes.POINTER(c_double_p),
+                                                     ctypes.POINTER(c_double_p)]
+    L.netlk_batch_destroy.argtypes = [vp]
     for name in EXPORTED:
         f = getattr(L, name)
         if f.restype is ctypes.c_int or f.restype is None:

@@ -230,8 +230,11 @@ struct netlk_ctx {
   void upload_probs();
   void enqueue(bool pm, bool fwd_on, bool reduce, bool mixk, bool bwd_on);
   void run(cudaGraphExec_t *cache, bool pm, bool fwd_on, bool reduce, bool mixk, bool bwd_on);
-  void prepare();
+  void prepare_state();  // model / probabilities uploads and launch-shape tuning
+  void prepare();        // prepare_state + branch-length upload
   void finish(double *total, double *part_logl, double *d_brlen, double *d_ret);
+  // results from the pinned host copies of the last evaluation
+  void read_results(double *total, double *part_logl, double *d_brlen, double *d_ret);
 };
 
 // ------------------------------------------------------------------ schedules
@@ -639,12 +642,16 @@ void netlk_ctx::autotune() {
   bwd_shape = (int)(std::min_element(tune_bwd_ms.begin(), tune_bwd_ms.end()) - tune_bwd_ms.begin());
 }
 
-void netlk_ctx::prepare() {
+void netlk_ctx::prepare_state() {
   if (opts.host_only) throw Error(NETLK_ERR_NO_DEVICE, "context was created host_only");
   CUDA_OK(cudaSetDevice(device));
   if (model_dirty) upload_model();
   if (probs_dirty) upload_probs();
   if (!tuned) autotune();
+}
+
+void netlk_ctx::prepare() {
+  prepare_state();
   if (!device_brlen) {  // lengths set from device memory stay where they are
     std::memcpy(h_brlen.p, brlen.data(), brlen.size() * 8);
     CUDA_OK(cudaMemcpyAsync(d_brlen.p, h_brlen.p, brlen.size() * 8, cudaMemcpyHostToDevice, stream));
@@ -659,9 +666,14 @@ void netlk_ctx::finish(double *total, double *part_logl, double *d_brlen, double
   CUDA_OK(cudaStreamSynchronize(stream));
   CUDA_OK(cudaGetLastError());
   prof_collect();
+  read_results(total, part_logl, d_brlen, d_ret);
+}
+
+void netlk_ctx::read_results(double *total, double *part_logl, double *d_brlen, double *d_ret) {
+  const int nout = 3 + P + topo.n_ret;
   const double *o = h_out.as<double>();
   if (use_tc && *reinterpret_cast<const int32_t *>(o + nout - 1) != 0)
-    throw Error(NETLK_ERR_CUDA, "tensor-core sweep: an MMA completion wait timed out");
+    throw Error(NETLK_ERR_TIMEOUT, "tensor-core sweep: an MMA completion wait timed out");
   if (o[1] != 0.0 || !std::isfinite(o[0]))
     throw Error(NETLK_ERR_NUMERIC, "Invalid network likelihood: negative infinity or NaN");
   if (total) *total = o[0];
@@ -1149,3 +1161,121 @@ int netlk_launch_count(const netlk_ctx *ctx, int64_t *launches) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------- batched candidates
+struct netlk_batch {
+  std::vector<netlk_ctx *> ctxs;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> join;
+  cudaGraphExec_t exec = nullptr;
+
+  ~netlk_batch() {
+    cudaSetDevice(device);
+    if (exec) cudaGraphExecDestroy(exec);
+    for (cudaEvent_t e : join) cudaEventDestroy(e);
+    if (fork) cudaEventDestroy(fork);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  // One graph: fork from the batch stream into every context's stream, per
+  // context the branch-length upload, the logL + gradient launch sequence and
+  // the result downloads, then join back.
+  void capture() {
+    CUDA_OK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    CUDA_OK(cudaEventRecord(fork, stream));
+    for (size_t i = 0; i < ctxs.size(); ++i) {
+      netlk_ctx *c = ctxs[i];
+      const bool prof = c->profiling;
+      c->profiling = false;
+      CUDA_OK(cudaStreamWaitEvent(c->stream, fork, 0));
+      CUDA_OK(cudaMemcpyAsync(c->d_brlen.p, c->h_brlen.p, c->brlen.size() * 8, cudaMemcpyHostToDevice,
+                              c->stream));
+      c->enqueue(true, true, true, true, true);
+      CUDA_OK(cudaMemcpyAsync(c->h_out.p, c->d_out.p, (3 + c->P + c->topo.n_ret) * 8, cudaMemcpyDeviceToHost,
+                              c->stream));
+      CUDA_OK(cudaMemcpyAsync(c->h_grad.p, c->d_grad.p, c->topo.n_edges * 8, cudaMemcpyDeviceToHost, c->stream));
+      CUDA_OK(cudaEventRecord(join[i], c->stream));
+      CUDA_OK(cudaStreamWaitEvent(stream, join[i], 0));
+      c->profiling = prof;
+    }
+    cudaGraph_t graph;
+    CUDA_OK(cudaStreamEndCapture(stream, &graph));
+    cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    CUDA_OK(e);
+  }
+};
+
+
+int netlk_batch_create(netlk_ctx *const *ctxs, int32_t n, netlk_batch **out) {
+  if (!ctxs || n <= 0 || !out) {
+    netlk::set_global_error("batch: contexts and output pointer required, n > 0");
+    return NETLK_ERR_INVALID_ARGUMENT;
+  }
+  *out = nullptr;
+  return guarded(nullptr, [&] {
+    auto b = std::make_unique<netlk_batch>();
+    for (int i = 0; i < n; ++i) {
+      if (!ctxs[i]) throw Error(NETLK_ERR_INVALID_ARGUMENT, "batch: context " + std::to_string(i) + " is NULL");
+      if (ctxs[i]->opts.host_only)
+        throw Error(NETLK_ERR_NO_DEVICE, "batch: context " + std::to_string(i) + " was created host_only");
+      if (i && ctxs[i]->device != ctxs[0]->device)
+        throw Error(NETLK_ERR_INVALID_ARGUMENT, "batch: all contexts must be on one device");
+      for (int j = 0; j < i; ++j)
+        if (ctxs[j] == ctxs[i]) throw Error(NETLK_ERR_INVALID_ARGUMENT, "batch: a context appears twice");
+    }
+    b->ctxs.assign(ctxs, ctxs + n);
+    b->device = ctxs[0]->device;
+    CUDA_OK(cudaSetDevice(b->device));
+    CUDA_OK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    CUDA_OK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+    b->join.resize(n);
+    for (auto &e : b->join) CUDA_OK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    *out = b.release();
+  });
+}
+
+int netlk_batch_loglikelihood_gradient(netlk_batch *b, double *totals, double *const *d_brlen,
+                                       double *const *d_retprob) {
+  if (!b) {
+    netlk::set_global_error("batch: NULL batch");
+    return NETLK_ERR_INVALID_ARGUMENT;
+  }
+  return guarded(nullptr, [&] {
+    for (size_t i = 0; i < b->ctxs.size(); ++i) {
+      netlk_ctx *c = b->ctxs[i];
+      if (c->device_brlen)
+        throw Error(NETLK_ERR_INVALID_ARGUMENT,
+                    "batch: context " + std::to_string(i) + " has device-resident branch lengths");
+      c->prepare_state();  // uploads and tuning happen outside the graph
+      CUDA_OK(cudaStreamSynchronize(c->stream));
+      std::memcpy(c->h_brlen.p, c->brlen.data(), c->brlen.size() * 8);
+    }
+    CUDA_OK(cudaSetDevice(b->device));
+    if (!b->exec) b->capture();
+    CUDA_OK(cudaGraphLaunch(b->exec, b->stream));
+    CUDA_OK(cudaStreamSynchronize(b->stream));
+    CUDA_OK(cudaGetLastError());
+    for (size_t i = 0; i < b->ctxs.size(); ++i) {
+      netlk_ctx *c = b->ctxs[i];
+      c->launches += 1 + c->fwd_launches + 2 + (c->bwd.empty() ? 0 : c->bwd_launches + 2);
+      std::vector<double> g(c->topo.n_edges, 0.0);
+      double tot = 0.0;
+      try {
+        c->read_results(&tot, nullptr, g.data(), d_retprob ? d_retprob[i] : nullptr);
+      } catch (const Error &e) {
+        throw Error(e.status, "batch: candidate " + std::to_string(i) + ": " + e.what());
+      }
+      if (c->bwd.empty()) std::fill(g.begin(), g.end(), 0.0);
+      if (totals) totals[i] = tot;
+      if (d_brlen && d_brlen[i]) std::memcpy(d_brlen[i], g.data(), g.size() * 8);
+    }
+  });
+}
+
+int netlk_batch_destroy(netlk_batch *b) {
+  delete b;
+  return NETLK_OK;
+}

@@ -296,3 +296,47 @@ try:
             return (g * gb).to(ctx.devs[0]), (g * gr).to(ctx.devs[1]), None
 except ImportError:  # torch is optional for the C ABI itself
     NetworkLogL = None
+
+
+class NetworkBatch:
+    """Candidate networks of one search move scored together: one CUDA graph
+    holding a logL + gradient evaluation of every context, launched once per
+    call (``netlk_batch_*``). The contexts stay owned by the caller and must
+    outlive the batch."""
+
+    def __init__(self, liks):
+        self.liks = list(liks)
+        L = N.lib()
+        arr = (ctypes.c_void_p * len(self.liks))(*[lk._h for lk in self.liks])
+        h = ctypes.c_void_p()
+        N.check(L.netlk_batch_create(arr, len(self.liks), ctypes.byref(h)))
+        self._h = h
+
+    def loglikelihood_gradient(self):
+        """Returns (totals [n], list of d logL / d branch length, list of
+        d logL / d reticulation probability)."""
+        n = len(self.liks)
+        tot = np.zeros(n)
+        gb = [np.zeros(lk.n_edges) for lk in self.liks]
+        gr = [np.zeros(max(1, lk.n_ret)) for lk in self.liks]
+        pb = (ctypes.POINTER(ctypes.c_double) * n)(*[_ptr(g, ctypes.c_double) for g in gb])
+        pr = (ctypes.POINTER(ctypes.c_double) * n)(*[_ptr(g, ctypes.c_double) for g in gr])
+        N.check(N.lib().netlk_batch_loglikelihood_gradient(self._h, _ptr(tot, ctypes.c_double), pb, pr))
+        return tot, gb, [g[:lk.n_ret] for g, lk in zip(gr, self.liks)]
+
+    def close(self):
+        if getattr(self, "_h", None):
+            N.lib().netlk_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

@@ -180,31 +180,37 @@ def simulate(rng, net: NetworkDesc, n_sites, freqs, exch, alpha, rate_cats=4):
             if indeg[c] == 0:
                 order.append(c)
                 queue.append(c)
+    S_ = len(freqs)
+
+    def pmats(blen):
+        # [rate_cats, S, S]: U diag(exp(lam t r_c)) Uinv, clipped at 0
+        P = np.einsum("ik,ck,kj->cij", U, np.exp(lam[None, :] * (blen * rates)[:, None]), Uinv)
+        return np.clip(P, 0.0, None)
+
     for c in order[1:]:
         if c in ret_index:
             k = ret_index[c]
             e1, e2 = net.ret_first_edge[k], net.ret_second_edge[k]
             take2 = cfg[:, k]
             pstate = np.where(take2, state[net.edge_parent[e2]], state[net.edge_parent[e1]])
-            blen = np.where(take2, net.branch_lengths[e2], net.branch_lengths[e1])
+            rows = np.where(take2[:, None], pmats(net.branch_lengths[e2])[cat, pstate],
+                            pmats(net.branch_lengths[e1])[cat, pstate])
         else:
             e = int(np.nonzero(net.edge_child == c)[0][0])
-            pstate = state[net.edge_parent[e]]
-            blen = np.full(n_sites, net.branch_lengths[e])
-        t = blen * rates[cat]
-        # P rows for every site: U diag(exp(lam t)) Uinv, row = parent state
-        Ex = np.exp(lam[None, :] * t[:, None])                    # [n, S]
-        rows = np.einsum("nk,kj->nj", U[pstate] * Ex, Uinv)        # [n, S]
-        rows = np.clip(rows, 0.0, None)
+            rows = pmats(net.branch_lengths[e])[cat, state[net.edge_parent[e]]]   # [n, S]
         cum = np.cumsum(rows, axis=1)
         u = rng.uniform(size=n_sites) * cum[:, -1]
-        state[c] = np.minimum((u[:, None] > cum).sum(axis=1), S - 1)
+        state[c] = np.minimum((u[:, None] > cum).sum(axis=1), S_ - 1)
     return (1 << state[:net.n_tips]).astype(np.uint32)
 
 
 def compress(codes):
-    cols, counts = np.unique(codes.T, axis=0, return_counts=True)
-    return np.ascontiguousarray(cols.T.astype(np.uint32)), counts.astype(np.float64)
+    """Pattern compression: distinct columns (in byte order of the column) and
+    their multiplicities."""
+    c = np.ascontiguousarray(codes.T.astype(np.uint32))
+    v = c.view(np.dtype((np.void, c.shape[1] * 4))).ravel()
+    _, first, counts = np.unique(v, return_index=True, return_counts=True)
+    return np.ascontiguousarray(c[first].T), counts.astype(np.float64)
 
 
 def make_protein_workload(name, n_taxa, n_ret, partition_sites, seed, alpha=0.8):
@@ -245,8 +251,41 @@ CONFIG_SEEDS = {0: 1000, 1: 1001, 2: 1002, 3: 1003, 4: 1004}
 CONFIG1_SITES = [500, 1000, 2000, 3000, 5000, 7000, 10000, 12000, 15000, 20000]
 
 
+def candidate_specs(n=64, scale=1.0, seed=None):
+    """Shapes of the candidate networks of one search move, drawn
+    independently: taxa ~ U{30..120}, reticulations ~ U{0..6}, 1-8 partitions
+    of U{1k..30k} DNA sites each (``scale`` shrinks the site counts)."""
+    rng = np.random.default_rng(CONFIG_SEEDS[4] if seed is None else seed)
+    out = []
+    for i in range(n):
+        nt = int(rng.integers(30, 121))
+        nr = int(rng.integers(0, 7))
+        npart = int(rng.integers(1, 9))
+        sites = [max(32, int(round(int(rng.integers(1000, 30001)) * scale))) for _ in range(npart)]
+        out.append(("candidate %d: %d taxa / %d reticulations / %d partitions" % (i, nt, nr, npart),
+                    nt, nr, sites, int(rng.integers(0, 2 ** 31))))
+    return out
+
+
+def _make_candidate(spec):
+    return make_workload(*spec)
+
+
+def candidate_batch(n=64, scale=1.0, seed=None, workers=1):
+    """Workloads of ``candidate_specs``; ``workers`` > 1 simulates them in a
+    spawned process pool (start it before any GPU work in the caller)."""
+    specs = candidate_specs(n, scale, seed)
+    if workers <= 1:
+        return [make_workload(*sp) for sp in specs]
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    with cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+        return list(ex.map(_make_candidate, specs))
+
+
 def config(idx, scale=1.0):
-    """Configurations 0-2 (DNA) and 3 (protein). ``scale`` shrinks the site counts."""
+    """Configurations 0-2 (DNA), 3 (protein) and 4 (a batch of 64 candidate
+    networks, returned as a list of workloads). ``scale`` shrinks the site counts."""
     s = lambda n: max(32, int(round(n * scale)))
     if idx == 0:
         return make_workload("20 taxa / 1 reticulation / 1k DNA sites", 20, 1, [s(1000)], CONFIG_SEEDS[0])
@@ -259,4 +298,6 @@ def config(idx, scale=1.0):
     if idx == 3:
         return make_protein_workload("40 taxa / 3 reticulations / 50k protein sites", 40, 3, [s(50000)],
                                      CONFIG_SEEDS[3])
+    if idx == 4:
+        return candidate_batch(64, scale)
     raise ValueError("config %d is not built" % idx)

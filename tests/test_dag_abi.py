@@ -164,3 +164,18 @@ def test_too_many_reticulations_unsupported():
     with pytest.raises(_native.NetlkError) as e:
         NetworkLikelihood(net, [part], host_only=True)
     assert e.value.status == 7
+
+
+def test_batch_rejects_bad_arguments():
+    import ctypes
+    net, part = _small()
+    L = _native.lib()
+    h = ctypes.c_void_p()
+    assert L.netlk_batch_create(None, 0, ctypes.byref(h)) == _native.NETLK_ERR_INVALID_ARGUMENT
+    lik = NetworkLikelihood(net, [part], host_only=True)
+    arr = (ctypes.c_void_p * 1)(lik._h)
+    assert L.netlk_batch_create(arr, 1, ctypes.byref(h)) == _native.NETLK_ERR_NO_DEVICE
+    assert b"host_only" in L.netlk_last_error(None)
+    assert not h.value
+    assert L.netlk_batch_loglikelihood_gradient(None, None, None, None) == _native.NETLK_ERR_INVALID_ARGUMENT
+    lik.close()

@@ -276,3 +276,30 @@ def test_launch_count_reported():
         # adjoint launch per level, two gradient reduction stages
         assert lik.launch_count() - before == lik.stats["launches_per_gradient_eval"]
         assert lik.stats["launches_per_gradient_eval"] <= 5 + 2 * lik.stats["n_levels"]
+
+
+def test_batch_matches_individual_contexts():
+    """One CUDA graph over several candidate networks (DNA of different sizes,
+    plus a protein context on the tensor-core path) == each context alone;
+    a second call picks up new branch lengths."""
+    from netrax_gb300 import synth
+    from netrax_gb300.likelihood import NetworkBatch, NetworkLikelihood
+    ws = synth.candidate_batch(5, scale=0.03)
+    ws.append(synth.make_protein_workload("protein candidate", 30, 2, [600], 5))
+    liks = [NetworkLikelihood(w.network, w.partitions, precision="fp32") for w in ws]
+    try:
+        with NetworkBatch(liks) as batch:
+            rng = np.random.default_rng(3)
+            for rep in range(2):
+                if rep:
+                    for lk, w in zip(liks, ws):
+                        lk.set_branch_lengths(w.network.branch_lengths * np.exp(0.1 * rng.standard_normal(lk.n_edges)))
+                tot, gb, gr = batch.loglikelihood_gradient()
+                for i, lk in enumerate(liks):
+                    t1, g1, r1 = lk.loglikelihood_gradient()
+                    assert tot[i] == t1
+                    assert np.array_equal(gb[i], g1)
+                    assert np.array_equal(gr[i], r1)
+    finally:
+        for lk in liks:
+            lk.close()
