@@ -213,12 +213,19 @@ int netlk_loglikelihood_gradient(netlk_ctx *ctx, double *total,
                                  double *partition_logl, double *d_brlen,
                                  double *d_retprob);
 
-/* Derivatives of the reference's own formula for one edge
- * (computeLoglikelihoodDerivatives, src/likelihood/LikelihoodDerivatives.cpp:30-188):
- * mode 0 = true derivative of the network logL; mode 1 = the reference's
- * restricted AVERAGE denominator (trees where the edge is taken) and BEST
- * argmax of tree_logl * tree_prob. d2 receives the central difference of d1
- * over +-1e-6 when not NULL. */
+/* First and second derivative of the log-likelihood w.r.t. one branch
+ * length, for the Newton-Raphson callback (network_derivative_func_multi,
+ * src/optimization/BranchLengthOptimization.cpp:171-200) that calls
+ * computeLoglikelihoodDerivatives (src/likelihood/LikelihoodDerivatives.cpp:190-232).
+ * mode 0: the true derivative of the network logL (adjoint sweep).
+ * mode 1: the reference's own formula, per partition: AVERAGE mixes only the
+ *   displayed trees on which the edge is active (isActiveBranch: a
+ *   reticulation edge counts where the tree's configurations may take it) in
+ *   numerator and denominator; BEST differentiates the active tree with the
+ *   largest tree_logl * tree_prob. Trees are grouped by displayed tree at the
+ *   network root (the reference groups by the virtually rerooted tree pairs
+ *   at the edge).
+ * d2 receives the central difference of d1 over +-1e-6 when not NULL. */
 int netlk_edge_derivatives(netlk_ctx *ctx, int32_t edge, int32_t mode,
                            double *d1, double *d2);
 

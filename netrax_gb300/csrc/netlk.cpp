@@ -982,31 +982,105 @@ int netlk_loglikelihood_gradient(netlk_ctx *ctx, double *total, double *part_log
   });
 }
 
+namespace {
+
+// Roots (displayed trees) on which an edge counts as active for the
+// reference's derivative: isActiveBranch (src/helper/EdgeHelper.cpp:84-95)
+// - the tree's configuration set is compatible with taking this edge's
+// parent; always true for an edge that does not enter a reticulation.
+std::vector<char> active_roots(const netlk_ctx *c, int edge) {
+  const Topology &T = c->topo;
+  const int child = T.edge_child[edge], k = T.node_ret[child];
+  std::vector<char> act(c->dag.roots.size(), 1);
+  if (k < 0) return act;
+  const int want = edge == T.ret_second_edge[k] ? 1 : 0;
+  const size_t n_cfg = (size_t)1 << T.n_ret;
+  for (size_t i = 0; i < c->dag.roots.size(); ++i) {
+    const Bits &set = c->dag.vars[c->dag.roots[i].variant].set;
+    bool any = false;
+    for (size_t t = 0; t < n_cfg && !any; ++t)
+      if (set.test(t) && (int)((t >> k) & 1) == want) any = true;
+    act[i] = any;
+  }
+  return act;
+}
+
+// d logL / d t_edge as the reference's computeLoglikelihoodDerivatives
+// computes it (src/likelihood/LikelihoodDerivatives.cpp:30-183), per
+// partition: AVERAGE mixes only the trees on which the edge is active
+// (numerator and denominator), BEST takes the derivative of the active tree
+// with the largest tree_logl * tree_prob.
+double reference_edge_d1(netlk_ctx *c, int edge) {
+  const std::vector<char> act = active_roots(c, edge);
+  const size_t nr = c->dag.roots.size();
+  std::vector<double> g(c->topo.n_edges, 0.0);
+  double tot = 0.0;
+  c->prepare();
+  if (c->opts.variant == NETLK_AVERAGE) {
+    double *lp = c->h_root_lp.as<double>();
+    for (size_t i = 0; i < nr; ++i)
+      if (!act[i]) lp[i] = -INFINITY;
+    CUDA_OK(cudaMemcpyAsync(c->d_root_lp.p, lp, nr * 8, cudaMemcpyHostToDevice, c->stream));
+    c->probs_dirty = true;  // the next evaluation uploads the real log-probabilities again
+    c->run(&c->graph_grad, true, true, true, true, true);
+    c->finish(&tot, nullptr, g.data(), nullptr);
+    return g[edge];
+  }
+  c->run(&c->graph_partials, true, true, true, false, false);
+  CUDA_OK(cudaMemcpyAsync(c->h_tree.p, c->d_tree_logl.p, (size_t)c->n_slots * c->P * 8, cudaMemcpyDeviceToHost,
+                          c->stream));
+  CUDA_OK(cudaStreamSynchronize(c->stream));
+  double *t = c->h_tree.as<double>();
+  std::vector<double> keep((size_t)c->n_slots * c->P, -INFINITY);
+  for (int p = 0; p < c->P; ++p) {
+    int best = -1;
+    double score = -INFINITY;
+    for (size_t i = 0; i < nr; ++i) {
+      const double lpi = c->dag.roots[i].logprob;
+      if (!act[i] || lpi < c->opts.min_interesting_tree_logprob) continue;
+      const double v = t[(size_t)c->root_slot[i] * c->P + p] * std::exp(lpi);
+      if (v > score || best < 0) {
+        score = v;
+        best = (int)i;
+      }
+    }
+    if (best < 0) throw Error(NETLK_ERR_NUMERIC, "no displayed tree contains the edge");
+    const size_t sl = (size_t)c->root_slot[best] * c->P + p;
+    keep[sl] = t[sl];
+  }
+  std::memcpy(t, keep.data(), keep.size() * 8);
+  CUDA_OK(cudaMemcpyAsync(c->d_tree_logl.p, t, keep.size() * 8, cudaMemcpyHostToDevice, c->stream));
+  c->run(&c->graph_mixbwd, false, false, false, true, true);
+  c->finish(&tot, nullptr, g.data(), nullptr);
+  return g[edge];
+}
+
+}  // namespace
+
 int netlk_edge_derivatives(netlk_ctx *ctx, int32_t edge, int32_t mode, double *d1, double *d2) {
   if (!ctx) return NETLK_ERR_INVALID_ARGUMENT;
   return guarded(ctx, [&] {
     if (edge < 0 || edge >= ctx->topo.n_edges) throw Error(NETLK_ERR_INVALID_ARGUMENT, "edge");
-    if (mode != 0) throw Error(NETLK_ERR_UNSUPPORTED, "only mode 0 (true derivative) is built");
-    std::vector<double> g(ctx->topo.n_edges);
-    double tot;
-    ctx->prepare();
-    ctx->run(&ctx->graph_grad, true, true, true, true, true);
-    ctx->finish(&tot, nullptr, g.data(), nullptr);
-    if (d1) *d1 = g[edge];
-    if (d2) {
-      const double h = 1e-6, b0 = ctx->brlen[edge];
-      double gp, gm;
-      ctx->brlen[edge] = b0 + h;
+    if (mode != 0 && mode != 1) throw Error(NETLK_ERR_INVALID_ARGUMENT, "mode must be 0 or 1");
+    // first derivative at the context's current lengths
+    auto first = [&]() -> double {
+      if (mode == 1) return reference_edge_d1(ctx, edge);
+      std::vector<double> g(ctx->topo.n_edges);
+      double tot;
       ctx->prepare();
       ctx->run(&ctx->graph_grad, true, true, true, true, true);
       ctx->finish(&tot, nullptr, g.data(), nullptr);
-      gp = g[edge];
+      return ctx->bwd.empty() ? 0.0 : g[edge];
+    };
+    const double g0 = first();
+    if (d1) *d1 = g0;
+    if (d2) {  // central difference of the first derivative
+      const double h = 1e-6, b0 = ctx->brlen[edge];
+      ctx->brlen[edge] = b0 + h;
+      const double gp = first();
       ctx->brlen[edge] = std::max(b0 - h, 1e-6);
       const double hm = b0 - ctx->brlen[edge];
-      ctx->prepare();
-      ctx->run(&ctx->graph_grad, true, true, true, true, true);
-      ctx->finish(&tot, nullptr, g.data(), nullptr);
-      gm = g[edge];
+      const double gm = first();
       ctx->brlen[edge] = b0;
       *d2 = (gp - gm) / (h + hm);
     }

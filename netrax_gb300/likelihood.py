@@ -166,9 +166,11 @@ class NetworkLikelihood:
             return tot.value, gb, gr[:self.n_ret], pl
         return tot.value, gb, gr[:self.n_ret]
 
-    def edge_derivatives(self, edge, second=True):
+    def edge_derivatives(self, edge, second=True, mode=0):
+        """d logL / d t_edge (and the second derivative): mode 0 the true
+        derivative, mode 1 the reference's own formula with its restrictions."""
         d1, d2 = ctypes.c_double(), ctypes.c_double()
-        N.check(N.lib().netlk_edge_derivatives(self._h, edge, 0, ctypes.byref(d1),
+        N.check(N.lib().netlk_edge_derivatives(self._h, edge, int(mode), ctypes.byref(d1),
                                                ctypes.byref(d2) if second else None), self._h)
         return (d1.value, d2.value) if second else d1.value
 

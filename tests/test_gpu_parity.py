@@ -303,3 +303,52 @@ def test_batch_matches_individual_contexts():
     finally:
         for lk in liks:
             lk.close()
+
+
+@pytest.mark.parametrize("variant", ["AVERAGE", "BEST"])
+def test_reference_derivative_mode(variant):
+    """netlk_edge_derivatives mode 1 (the reference's per-partition formula:
+    AVERAGE over trees where the edge is active, BEST = derivative of the
+    active tree with the largest tree_logl * tree_prob) against central
+    differences of that formula evaluated from the per-tree sums."""
+    case = [c for c in CASES if c["name"] == "synthetic_16taxa_4ret_3parts"][0]
+    with _lik(case, variant, "fp64") as lik:
+        net = lik.network
+        rv, _, lp = lik.root_export()
+        _, _, _, cov = lik.dag_export()
+        base = net.branch_lengths.copy()
+        min_lp = math.log(1e-6)
+        edges = [int(net.ret_first_edge[0]), int(net.ret_second_edge[0]), int(net.ret_second_edge[-1])]
+        tree_edge = [e for e in range(lik.n_edges) if net.edge_child[e] not in set(net.ret_node)][0]
+        for e in edges + [tree_edge]:
+            child = int(net.edge_child[e])
+            act = np.ones(len(rv), bool)
+            if child in set(int(x) for x in net.ret_node):
+                k = [int(x) for x in net.ret_node].index(child)
+                want = 1 if e == int(net.ret_second_edge[k]) else 0
+                for i, v in enumerate(rv):
+                    words = cov[v]
+                    cfgs = [t for t in range(1 << lik.n_ret) if (int(words[t >> 6]) >> (t & 63)) & 1]
+                    act[i] = any(((t >> k) & 1) == want for t in cfgs)
+            use = act & (lp >= min_lp)
+            t0 = lik.tree_partials()
+            choice = [int(np.argmax(np.where(use, t0[:, p] * np.exp(lp), -np.inf))) for p in range(lik.n_parts)]
+
+            def f(delta):
+                b = base.copy()
+                b[e] += delta
+                lik.set_branch_lengths(b)
+                t = lik.tree_partials()
+                if variant == "AVERAGE":
+                    return sum(np.logaddexp.reduce(lp[use] + t[use, p]) for p in range(lik.n_parts))
+                return sum(t[choice[p], p] for p in range(lik.n_parts))
+
+            h = 1e-5
+            want_d1 = (f(h) - f(-h)) / (2 * h)
+            lik.set_branch_lengths(base)
+            got = lik.edge_derivatives(e, second=False, mode=1)
+            assert got == pytest.approx(want_d1, rel=1e-5, abs=1e-4)
+            if e == tree_edge and variant == "AVERAGE":
+                assert got == pytest.approx(lik.edge_derivatives(e, second=False, mode=0), rel=1e-12, abs=1e-9)
+        # the context is left evaluating the real mixture
+        assert lik.loglikelihood() == pytest.approx(case[variant]["logl"], rel=FP64_REL)
