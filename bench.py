@@ -52,8 +52,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=16384, help="patterns in the CPU sample")
     ap.add_argument("--scale", type=float, default=1.0, help="site-count scale (1.0 = full workload)")
-    ap.add_argument("--config", type=int, default=2, choices=[2, 3, 4],
-                    help="2: 100 taxa / 8 reticulations / 100k DNA sites (the headline workload); "
+    ap.add_argument("--config", type=int, default=2, choices=[1, 2, 3, 4],
+                    help="1: 50 taxa / 4 reticulations / 10 uneven DNA partitions (75.5k sites); "
+                         "2: 100 taxa / 8 reticulations / 100k DNA sites (the headline workload); "
                          "3: 40 taxa / 3 reticulations / 50k protein sites; "
                          "4: a batch of 64 candidate networks scored in one CUDA graph")
     return ap.parse_args()

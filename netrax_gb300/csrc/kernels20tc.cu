@@ -184,16 +184,18 @@ __global__ void __launch_bounds__(kTThreads, 1)
   FwdOp op = load_fwd_op(p.fwd_ops, op_begin + oi);
   int ka = child_kind(op.a), kb = child_kind(op.b);
   float4 xa[10], xb[10];
+  // partitions are padded to whole 256-pattern blocks: a tile has one partition
+  int part_next = 0;
   if (item_begin < item_end) {
     const size_t g0 = (size_t)(item_begin - oi * n_tiles) * kTM;
     fetch(p, ka, op.a, g0, xa);
     fetch(p, kb, op.b, g0, xb);
+    part_next = p.unit_part[g0 / 16];
   }
   for (int item = item_begin; item < item_end; ++item) {
     const int tile = item - oi * n_tiles;
     const size_t g0 = (size_t)tile * kTM;
-    // partitions are padded to whole 256-pattern blocks: a tile has one partition
-    const int part = p.unit_part[g0 / 16];
+    const int part = part_next;
     if (oi != staged_op || part != staged_part) {
       stage_b(p, sB, part, op.ea, kb == kAbsent ? -1 : op.eb);
       staged_op = oi;
@@ -245,6 +247,7 @@ __global__ void __launch_bounds__(kTThreads, 1)
       const size_t gn = (size_t)(item + 1 - oi * n_tiles) * kTM;
       fetch(p, ka, op.a, gn, xa);
       fetch(p, kb, op.b, gn, xb);
+      part_next = p.unit_part[gn / 16];
     }
     const bool ok = tc::mbar_wait(tc::smem_u32(mbar), phase);
     phase ^= 1;
