@@ -105,10 +105,11 @@ typedef struct {
                                         "f,b" fixes both shapes instead.      */
   int32_t tensor_cores;              /* 1 (default): 20-state FP32 contexts
                                         with 4 rate categories run the P x CLV
-                                        products of the forward sweep on the
-                                        tensor cores (3xTF32 split, FP32
-                                        accumulation); 0: CUDA cores only.
-                                        No effect on other contexts.         */
+                                        products of the forward and adjoint
+                                        sweeps on the tensor cores (3xTF32
+                                        split, FP32 accumulation); 0: CUDA
+                                        cores only. No effect on other
+                                        contexts.                            */
 } netlk_options;
 
 typedef struct {

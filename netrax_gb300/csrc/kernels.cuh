@@ -108,10 +108,11 @@ void launch_grad_reduce(cudaStream_t s, int n_ops, int n_edges, int n_bx, const 
 // 20-state forward (backward = false) or adjoint sweep, one launch per level.
 void launch_sweep20(cudaStream_t s, int precision, int R, bool backward, const SweepParams &p,
                     const int32_t *level_begin, int n_levels);
-// Tensor-core (tcgen05) forward sweep for 20-state FP32 contexts with 4 rate
-// categories; one launch per level.
+// Tensor-core (tcgen05) forward and adjoint sweeps for 20-state FP32
+// contexts with 4 rate categories; one launch per level.
 bool sweep20_tc_supported(int precision, int R);
 void launch_forward20_tc(cudaStream_t s, const SweepParams &p, const int32_t *level_begin, int n_levels, int n_sms);
+void launch_backward20_tc(cudaStream_t s, const SweepParams &p, const int32_t *level_begin, int n_levels, int n_sms);
 // Number of kernel launches issued by the launchers above (host counter).
 int64_t launches_issued();
 void add_launches(int64_t n);

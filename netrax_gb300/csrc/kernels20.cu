@@ -67,14 +67,39 @@ __device__ __forceinline__ void store20(real *dst, const real (&v)[S20]) {
   }
 }
 
-// out = P . c with P row-major 20x20 in shared memory
+// 16-byte shared-memory vectors of a 20-wide row: 5 float4 / 10 double2.
+template <typename real>
+struct Row16;
+template <>
+struct Row16<float> {
+  using V = float4;
+  static constexpr int kPer = 4;
+  __device__ static void get(const V &v, float (&o)[4]) { o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w; }
+};
+template <>
+struct Row16<double> {
+  using V = double2;
+  static constexpr int kPer = 2;
+  __device__ static void get(const V &v, double (&o)[2]) { o[0] = v.x; o[1] = v.y; }
+};
+
+// out = P . c with P row-major 20x20 in shared memory (16-byte aligned rows),
+// read as 16-byte vectors; the sum over j runs in index order.
 template <typename real>
 __device__ __forceinline__ void mv20(const real *P, const real (&c)[S20], real (&out)[S20]) {
+  using RV = Row16<real>;
+  constexpr int K = RV::kPer;
+  const typename RV::V *P4 = reinterpret_cast<const typename RV::V *>(P);
 #pragma unroll
   for (int i = 0; i < S20; ++i) {
     real acc = 0;
 #pragma unroll
-    for (int j = 0; j < S20; ++j) acc += P[i * S20 + j] * c[j];
+    for (int q = 0; q < S20 / K; ++q) {
+      real e[K];
+      RV::get(P4[i * (S20 / K) + q], e);
+#pragma unroll
+      for (int t = 0; t < K; ++t) acc += e[t] * c[q * K + t];
+    }
     out[i] = acc;
   }
 }
@@ -82,12 +107,20 @@ __device__ __forceinline__ void mv20(const real *P, const real (&c)[S20], real (
 // out = P^T . u
 template <typename real>
 __device__ __forceinline__ void mv20_t(const real *P, const real (&u)[S20], real (&out)[S20]) {
+  using RV = Row16<real>;
+  constexpr int K = RV::kPer;
+  const typename RV::V *P4 = reinterpret_cast<const typename RV::V *>(P);
 #pragma unroll
   for (int j = 0; j < S20; ++j) out[j] = 0;
 #pragma unroll
   for (int i = 0; i < S20; ++i) {
 #pragma unroll
-    for (int j = 0; j < S20; ++j) out[j] += P[i * S20 + j] * u[i];
+    for (int q = 0; q < S20 / K; ++q) {
+      real e[K];
+      RV::get(P4[i * (S20 / K) + q], e);
+#pragma unroll
+      for (int t = 0; t < K; ++t) out[q * K + t] += e[t] * u[i];
+    }
   }
 }
 
@@ -201,12 +234,11 @@ __device__ __noinline__ real side20(const real (&ax)[S20], const real (&other)[S
     for (int i = 0; i < S20; ++i) u[i] = Scale<real>::shift(u[i], sh);
   }
   real g = 0;
+  {
+    real q[S20];
+    mv20<real>(sQ, own, q);
 #pragma unroll
-  for (int i = 0; i < S20; ++i) {
-    real q = 0;
-#pragma unroll
-    for (int j = 0; j < S20; ++j) q += sQ[i * S20 + j] * own[j];
-    g += u[i] * q;
+    for (int i = 0; i < S20; ++i) g += u[i] * q[i];
   }
   if (out >= 0) {
     real n[S20];
@@ -221,7 +253,8 @@ template <typename real, int R>
 __global__ void __launch_bounds__(kWarps20 * 32) backward20_kernel(const SweepParams p, int op_begin) {
   constexpr int PPW = 32 / R, UNIT = PPW * kPPLBase, ST = P20<real>::kStride;
   __shared__ __align__(16) real sP[2 * R * ST];
-  __shared__ real sQ[400], sF[S20];
+  __shared__ __align__(16) real sQ[400];
+  __shared__ real sF[S20];
   const int opi = op_begin + blockIdx.y;
   const BwdOp op = load_bwd_op(p.bwd_ops, opi);
   const bool fake = op.b == INT32_MIN;

@@ -341,6 +341,372 @@ __global__ void __launch_bounds__(kTThreads, 1)
   if (warp == 0) tc::tmem_free(tmem, 512);
 }
 
+// ------------------------------------------------------------------ adjoint
+// Per op and tile of 128 patterns, for each half of the rates (2 rates):
+//   round 1: D = c . [P_r | Q] for both children (c = child CLV rows; Q is
+//            the rate matrix, the same for every edge and rate), giving
+//            p = P_r c and Q c in TMEM;
+//   epilogue 1: u_a = 2^sh adj_x (*) p_b, u_b = 2^sh adj_x (*) p_a (adj_x =
+//            the sum of x's incoming messages + the displayed-tree seed);
+//   round 2: D = u . P_r (the messages P_r^T u);
+//   epilogue 2: edge terms rate_r (P_r^T u) . (Q c) = rate_r u . (Q P_r c)
+//            (P_r = exp(Q t r) commutes with Q), and the messages go to the
+//            children's slots.
+// TMEM: child c, local rate l at column 256c + 128l: [0,64) p (or the message
+// in round 2), [64,128) Q c. A tiles hold one rate half (40 columns + a zero
+// slab); B tiles hold P_r (rows = output state), Q, and P_r^T for all rates.
+constexpr int kHChunks = 11;
+constexpr int kHBytes = kHChunks * kAChunk;            // 22704
+constexpr int kBwdA = 4 * kHBytes;                     // [child][hi, lo]
+constexpr int kBwdB1 = 8 * kBBytes;                    // [child][rate] P_r
+constexpr int kBwdB2 = 8 * kBBytes;                    // [child][rate] P_r^T
+constexpr int kStageRow = 176;                         // staged message row: 160 B + 16 B bank spread
+constexpr int kBwdMisc = 16 + 4 * 2 * kTM * 4;         // mbarrier, TMEM address, 4 exchange arrays [2][128]
+constexpr int kBwdSmem = kBwdA + kBwdB1 + kBBytes + kBwdB2 + kBwdMisc;
+static_assert(2 * kTM * kStageRow <= kBwdA, "message staging fits the A tiles");
+static_assert(kBwdSmem <= 232448, "shared memory of one CTA");
+
+// B tiles of the adjoint: P_r (as the forward) and P_r^T (row n = j, column
+// k = i holds P_r[i][j]) of both children, and Q when `with_q`.
+__device__ __forceinline__ void stage_b_adj(const SweepParams &p, unsigned char *sB1, unsigned char *sBQ,
+                                            unsigned char *sB2, int part, int ea, int eb, bool with_q) {
+  const float4 *pm = reinterpret_cast<const float4 *>(static_cast<const float *>(p.pmat) +
+                                                      (size_t)part * p.n_edges * 1600);
+  float4 v[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int f = threadIdx.x + u * kTThreads, c = f / 400, e = c ? eb : ea;
+    if (f < 800 && e >= 0) v[u] = __ldg(pm + (size_t)e * 400 + (f - c * 400));
+  }
+  if (with_q && threadIdx.x < 100) {  // Q[i][4 j4 .. 4 j4 + 3], FP64 -> FP32
+    const int i = threadIdx.x / 5, j4 = threadIdx.x - i * 5;
+    const double *q = p.Q + (size_t)part * 400 + i * 20 + 4 * j4;
+    const float4 x = make_float4((float)q[0], (float)q[1], (float)q[2], (float)q[3]);
+    float4 hi, lo;
+    split4(x, hi, lo);
+    unsigned char *base = sBQ + j4 * kBChunk + (i & 7) * 16;
+    *reinterpret_cast<float4 *>(base + (i >> 3) * 128) = hi;
+    *reinterpret_cast<float4 *>(base + (4 + (i >> 3)) * 128) = lo;
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int f = threadIdx.x + u * kTThreads, c = f / 400, e = c ? eb : ea;
+    if (f >= 800 || e < 0) continue;
+    const int rem = f - c * 400, r = rem / 100, e2 = rem - r * 100, i = e2 / 5, j4 = e2 - i * 5;
+    float4 hi, lo;
+    split4(v[u], hi, lo);
+    unsigned char *base = sB1 + (c * 4 + r) * kBBytes + j4 * kBChunk + (i & 7) * 16;
+    *reinterpret_cast<float4 *>(base + (i >> 3) * 128) = hi;
+    *reinterpret_cast<float4 *>(base + (4 + (i >> 3)) * 128) = lo;
+    // transposed: rows n = 4 j4 + t, column k = i
+    unsigned char *tb = sB2 + (c * 4 + r) * kBBytes + (i >> 2) * kBChunk + (i & 3) * 4;
+    const float h4[4] = {hi.x, hi.y, hi.z, hi.w}, l4[4] = {lo.x, lo.y, lo.z, lo.w};
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int n = 4 * j4 + t;
+      *reinterpret_cast<float *>(tb + (n >> 3) * 128 + (n & 7) * 16) = h4[t];
+      *reinterpret_cast<float *>(tb + ((32 + n) >> 3) * 128 + (n & 7) * 16) = l4[t];
+    }
+  }
+}
+
+// Child rows of one rate half (columns 40h .. 40h+39) into an A tile pair.
+__device__ __forceinline__ void put_half(const SweepParams &p, int kind, int32_t ref, size_t g0, int h,
+                                         unsigned char *sAh, unsigned char *sAl) {
+  const size_t N = (size_t)p.n_patterns;
+  if (kind == kInner) {
+    const float *src = static_cast<const float *>(p.clv) + ((size_t)ref * N + g0) * 80 + 40 * h;
+    float4 x[5];
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+      const int f = threadIdx.x + i * kTThreads, m = f / 10, kc = f - m * 10;
+      x[i] = __ldg(reinterpret_cast<const float4 *>(src + (size_t)m * 80) + kc);
+    }
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+      const int f = threadIdx.x + i * kTThreads, m = f / 10, kc = f - m * 10, off = kc * kAChunk + m * 16;
+      float4 hi, lo;
+      split4(x[i], hi, lo);
+      *reinterpret_cast<float4 *>(sAh + off) = hi;
+      *reinterpret_cast<float4 *>(sAl + off) = lo;
+    }
+  } else if (kind == kTip) {
+    const uint32_t *code = p.tips32 + (size_t)(-1 - ref) * N + g0;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+      const int f = threadIdx.x + i * kTThreads, m = f / 10, kc = f - m * 10;
+      const uint32_t b = __ldg(code + m) >> (4 * (kc % 5));  // local columns 4kc.. = states 4(kc%5)..
+      *reinterpret_cast<float4 *>(sAh + kc * kAChunk + m * 16) =
+          make_float4((float)(b & 1u), (float)((b >> 1) & 1u), (float)((b >> 2) & 1u), (float)((b >> 3) & 1u));
+    }
+  }
+}
+
+// 20 values of one thread's row into an A tile pair: local columns
+// 20l .. 20l + 19 (slabs 5l .. 5l + 4), split hi / lo.
+__device__ __forceinline__ void put_row(const float (&v)[20], int m, int l, unsigned char *sAh, unsigned char *sAl) {
+#pragma unroll
+  for (int q = 0; q < 5; ++q) {
+    const int off = (5 * l + q) * kAChunk + m * 16;
+    float4 hi, lo;
+    split4(make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]), hi, lo);
+    *reinterpret_cast<float4 *>(sAh + off) = hi;
+    *reinterpret_cast<float4 *>(sAl + off) = lo;
+  }
+}
+
+__global__ void __launch_bounds__(kTThreads, 1)
+    backward20_tc_kernel(const SweepParams p, int op_begin, int n_ops, int n_tiles) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  unsigned char *sA = smem;
+  unsigned char *sB1 = smem + kBwdA;
+  unsigned char *sBQ = sB1 + kBwdB1;
+  unsigned char *sB2 = sBQ + kBBytes;
+  unsigned char *misc = sB2 + kBwdB2;
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(misc);
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(misc + 8);
+  float *s_t = reinterpret_cast<float *>(misc + 16);  // [2][128] seed denominators
+  float *s_ga = s_t + 2 * kTM;                         // [2][128] edge terms, side a
+  float *s_gb = s_ga + 2 * kTM;                        // [2][128] edge terms, side b
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const size_t N = (size_t)p.n_patterns;
+  const long long W = (long long)n_ops * n_tiles;
+  const int item_begin = (int)(W * blockIdx.x / gridDim.x), item_end = (int)(W * (blockIdx.x + 1) / gridDim.x);
+
+  if (warp == 0) tc::tmem_alloc(tc::smem_u32(tmem_slot), 512);
+  if (threadIdx.x == 0) tc::mbar_init(tc::smem_u32(mbar), 1);
+  for (int i = threadIdx.x; i < 4 * kTM; i += kTThreads)
+    *reinterpret_cast<float4 *>(sA + (i / kTM) * kHBytes + 10 * kAChunk + (i % kTM) * 16) = make_float4(0, 0, 0, 0);
+  for (int i = threadIdx.x; i < (kBwdB1 + kBBytes + kBwdB2) / 16; i += kTThreads)
+    reinterpret_cast<float4 *>(sB1)[i] = make_float4(0, 0, 0, 0);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tmem_slot;
+
+  const int q = warp & 3, hh = warp >> 2;  // pattern quarter, local rate
+  const int m = 32 * q + lane;
+  const uint32_t lane_base = tmem + ((uint32_t)(32 * q) << 16);
+  const float *clv = static_cast<const float *>(p.clv);
+  float *msg = static_cast<float *>(p.msg);
+  int staged_op = -1, staged_part = -1;
+  uint32_t phase = 0;
+  bool failed = false;
+
+  for (int item = item_begin; item < item_end && !failed; ++item) {
+    const int oi = item / n_tiles, tile = item - oi * n_tiles, opi = op_begin + oi;
+    const size_t g0 = (size_t)tile * kTM, g = g0 + m;
+    const BwdOp op = load_bwd_op(p.bwd_ops, opi);
+    const int ka = child_kind(op.a), kb = child_kind(op.b);
+    const int part = p.unit_part[g0 / 16];  // partitions are padded to whole 256-pattern blocks
+    if (oi != staged_op || part != staged_part) {
+      stage_b_adj(p, sB1, sBQ, sB2, part, op.ea, kb == kAbsent ? -1 : op.eb, part != staged_part);
+      staged_op = oi;
+      staged_part = part;
+    }
+    const int sh = p.scaler[(size_t)op.x * N + g] - (ka == kInner ? p.scaler[(size_t)op.a * N + g] : 0) -
+                   (kb == kInner ? p.scaler[(size_t)op.b * N + g] : 0);
+    // displayed-tree seed: w_s rw_r pi_i / L_s with L_s summed over all rates
+    float tseed = 0.f, sw = 0.f;
+    if (op.seed >= 0) {
+      const float *cx = clv + ((size_t)op.x * N + g) * 80 + 40 * hh;
+      float part_t = 0.f;
+#pragma unroll
+      for (int l = 0; l < 2; ++l) {
+        float u = 0.f;
+#pragma unroll
+        for (int i = 0; i < 20; ++i) u += (float)p.freqs[part * 20 + i] * cx[20 * l + i];
+        part_t += (float)p.rate_weights[part * 4 + 2 * hh + l] * u;
+      }
+      s_t[hh * kTM + m] = part_t;
+      __syncthreads();
+      tseed = s_t[m] + s_t[kTM + m];
+      sw = (float)p.seeds[(size_t)op.seed * p.n_parts + part] * (float)p.weights[g];
+    }
+    float ga = 0.f, gb = 0.f;
+    for (int h = 0; h < 2; ++h) {
+      const int r = 2 * h + hh;  // this thread's rate in this half
+      // ---------------------------------------------------- round 1: p and Q c
+      put_half(p, ka, op.a, g0, h, sA, sA + kHBytes);
+      put_half(p, kb, op.b, g0, h, sA + 2 * kHBytes, sA + 3 * kHBytes);
+      tc::fence_proxy_async();
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        tc::fence_after_sync();
+#pragma unroll 1
+        for (int c = 0; c < 2; ++c) {
+          const int kind = c ? kb : ka;
+          if (kind == kAbsent) continue;
+          const uint64_t dah = tc::smem_desc(tc::smem_u32(sA + (2 * c) * kHBytes), kAChunk, 128);
+          const uint64_t dal = dah + (kHBytes >> 4);
+          const uint64_t dq = tc::smem_desc(tc::smem_u32(sBQ), kBChunk, 128);
+#pragma unroll
+          for (int l = 0; l < 2; ++l) {
+            const uint64_t db = tc::smem_desc(tc::smem_u32(sB1 + (c * 4 + 2 * h + l) * kBBytes), kBChunk, 128);
+            const uint32_t d = tmem + 256 * c + 128 * l;
+#pragma unroll
+            for (int st = 0; st < 3; ++st) {
+              const uint32_t ko = ((5 * l + 2 * st) * kAChunk) >> 4, bo = (2 * st * kBChunk) >> 4;
+              tc::mma_tf32(d, dah + ko, db + bo, kIdN64, st > 0);
+              tc::mma_tf32(d + 64, dah + ko, dq + bo, kIdN64, st > 0);
+              if (kind == kInner) {
+                tc::mma_tf32(d, dal + ko, db + bo, kIdN32, 1);
+                tc::mma_tf32(d + 64, dal + ko, dq + bo, kIdN32, 1);
+              }
+            }
+          }
+        }
+        tc::commit(tc::smem_u32(mbar));
+      }
+      // adjoint of x for (pattern g, rate r): incoming messages + seed
+      float ax[20];
+#pragma unroll
+      for (int i = 0; i < 20; ++i) ax[i] = 0.f;
+      for (int mi = 0; mi < op.msg_count; ++mi) {
+        const float4 *src = reinterpret_cast<const float4 *>(
+            msg + ((size_t)__ldg(p.msg_slots + op.msg_begin + mi) * N + g) * 80 + 20 * r);
+#pragma unroll
+        for (int j = 0; j < 5; ++j) {
+          const float4 v = src[j];
+          ax[4 * j] += v.x;
+          ax[4 * j + 1] += v.y;
+          ax[4 * j + 2] += v.z;
+          ax[4 * j + 3] += v.w;
+        }
+      }
+      if (op.seed >= 0 && tseed > 0.f && sw != 0.f) {
+        const float f = sw * (float)p.rate_weights[part * 4 + r] / tseed;
+#pragma unroll
+        for (int i = 0; i < 20; ++i) ax[i] += f * (float)p.freqs[part * 20 + i];
+      }
+      bool ok = tc::mbar_wait(tc::smem_u32(mbar), phase);
+      phase ^= 1;
+      if (__syncthreads_or(!ok)) {
+        failed = true;
+        break;
+      }
+      tc::fence_after_sync();
+      // ----------------------------------------------------------- epilogue 1
+      {
+        float pa[20], pb[20];
+        read_d(lane_base + 128 * hh, pa);
+        if (kb != kAbsent) {
+          read_d(lane_base + 256 + 128 * hh, pb);
+        } else {
+#pragma unroll
+          for (int i = 0; i < 20; ++i) pb[i] = 1.f;
+        }
+        float u[20];
+#pragma unroll
+        for (int i = 0; i < 20; ++i) u[i] = Scale<float>::shift(ax[i] * pb[i], sh);
+        put_row(u, m, hh, sA, sA + kHBytes);
+        if (kb != kAbsent) {
+#pragma unroll
+          for (int i = 0; i < 20; ++i) u[i] = Scale<float>::shift(ax[i] * pa[i], sh);
+          put_row(u, m, hh, sA + 2 * kHBytes, sA + 3 * kHBytes);
+        }
+      }
+      tc::fence_proxy_async();
+      tc::fence_before_sync();
+      __syncthreads();
+      // ------------------------------------------------- round 2: P_r^T u
+      if (threadIdx.x == 0) {
+        tc::fence_after_sync();
+#pragma unroll 1
+        for (int c = 0; c < 2; ++c) {
+          if ((c ? kb : ka) == kAbsent) continue;
+          const uint64_t dah = tc::smem_desc(tc::smem_u32(sA + (2 * c) * kHBytes), kAChunk, 128);
+          const uint64_t dal = dah + (kHBytes >> 4);
+#pragma unroll
+          for (int l = 0; l < 2; ++l) {
+            const uint64_t db = tc::smem_desc(tc::smem_u32(sB2 + (c * 4 + 2 * h + l) * kBBytes), kBChunk, 128);
+            const uint32_t d = tmem + 256 * c + 128 * l;
+#pragma unroll
+            for (int st = 0; st < 3; ++st) {
+              const uint32_t ko = ((5 * l + 2 * st) * kAChunk) >> 4, bo = (2 * st * kBChunk) >> 4;
+              tc::mma_tf32(d, dah + ko, db + bo, kIdN64, st > 0);
+              tc::mma_tf32(d, dal + ko, db + bo, kIdN32, 1);
+            }
+          }
+        }
+        tc::commit(tc::smem_u32(mbar));
+      }
+      ok = tc::mbar_wait(tc::smem_u32(mbar), phase);
+      phase ^= 1;
+      if (__syncthreads_or(!ok)) {
+        failed = true;
+        break;
+      }
+      tc::fence_after_sync();
+      // ----------------------------------------------------------- epilogue 2
+      const float rate = (float)p.rates[part * 4 + r];
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        if ((c ? kb : ka) == kAbsent) continue;
+        float mv[20], qc[20];
+        read_d(lane_base + 256 * c + 128 * hh, mv);
+        read_d(lane_base + 256 * c + 128 * hh + 64, qc);
+        float dot = 0.f;
+#pragma unroll
+        for (int i = 0; i < 20; ++i) dot += mv[i] * qc[i];
+        if (c) gb += rate * dot; else ga += rate * dot;
+        // message row (this rate's 20 states) staged for a coalesced copy
+        float4 *row = reinterpret_cast<float4 *>(sA + (c * kTM + m) * kStageRow + 80 * hh);
+#pragma unroll
+        for (int j = 0; j < 5; ++j) row[j] = make_float4(mv[4 * j], mv[4 * j + 1], mv[4 * j + 2], mv[4 * j + 3]);
+      }
+      tc::fence_before_sync();
+      __syncthreads();
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const int out = c ? op.out_b : op.out_a;
+        if (out < 0 || (c ? kb : ka) == kAbsent) continue;
+        float4 *dst = reinterpret_cast<float4 *>(msg + ((size_t)out * N + g0) * 80 + 40 * h);
+#pragma unroll
+        for (int i = 0; i < 5; ++i) {
+          const int f = threadIdx.x + i * kTThreads, rr = f / 10, c4 = f - rr * 10;
+          dst[(size_t)rr * 20 + c4] = *reinterpret_cast<const float4 *>(sA + (c * kTM + rr) * kStageRow + 16 * c4);
+        }
+      }
+      __syncthreads();
+      // the staging rows overlap the zero slabs of the child-a tiles: clear them again
+      if (threadIdx.x < 2 * kTM) {
+        const int t = threadIdx.x >> 7, rr = threadIdx.x & (kTM - 1);
+        *reinterpret_cast<float4 *>(sA + t * kHBytes + 10 * kAChunk + rr * 16) = make_float4(0, 0, 0, 0);
+      }
+    }
+    if (failed) break;
+    // edge terms per 16-pattern unit, summed in a fixed order
+    s_ga[hh * kTM + m] = ga;
+    s_gb[hh * kTM + m] = gb;
+    __syncthreads();
+    if (hh == 0) {
+      double va = (double)s_ga[m] + (double)s_ga[kTM + m];
+      double vb = (double)s_gb[m] + (double)s_gb[kTM + m];
+#pragma unroll
+      for (int o = 8; o > 0; o >>= 1) {
+        va += __shfl_xor_sync(0xffffffffu, va, o);
+        vb += __shfl_xor_sync(0xffffffffu, vb, o);
+      }
+      if ((lane & 15) == 0) {
+        const size_t unit = g0 / 16 + (size_t)(m >> 4);
+        p.grad_partial[((size_t)opi * p.n_units + unit) * 2] = va;
+        p.grad_partial[((size_t)opi * p.n_units + unit) * 2 + 1] = vb;
+      }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+  }
+  if (failed) {
+    if (threadIdx.x == 0) atomicExch(p.fault, 1);
+    tc::mbar_wait(tc::smem_u32(mbar), phase ^ 1);
+    __syncthreads();
+  }
+  tc::fence_after_sync();
+  if (warp == 0) tc::tmem_free(tmem, 512);
+}
+
 }  // namespace
 
 bool sweep20_tc_supported(int precision, int R) { return precision == 1 && R == 4; }
@@ -362,6 +728,32 @@ void launch_forward20_tc(cudaStream_t s, const SweepParams &p, const int32_t *le
     const long long items = (long long)n * n_tiles;
     const int grid = (int)(items < n_sms ? items : n_sms);  // one CTA per SM
     forward20_tc_kernel<<<grid, kTThreads, kSmemBytes, s>>>(p, level_begin[L], n, n_tiles);
+    ++launched;
+  }
+  add_launches(launched);
+}
+
+}  // namespace netlk
+
+namespace netlk {
+
+void launch_backward20_tc(cudaStream_t s, const SweepParams &p, const int32_t *level_begin, int n_levels,
+                          int n_sms) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  static bool attr_set[64] = {};
+  if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+    cudaFuncSetAttribute(backward20_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kBwdSmem);
+    attr_set[dev] = true;
+  }
+  const int n_tiles = (int)(p.n_patterns / kTM);
+  int launched = 0;
+  for (int L = 0; L < n_levels; ++L) {
+    const int n = level_begin[L + 1] - level_begin[L];
+    if (n <= 0) continue;
+    const long long items = (long long)n * n_tiles;
+    const int grid = (int)(items < n_sms ? items : n_sms);
+    backward20_tc_kernel<<<grid, kTThreads, kBwdSmem, s>>>(p, level_begin[L], n, n_tiles);
     ++launched;
   }
   add_launches(launched);

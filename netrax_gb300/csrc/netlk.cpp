@@ -541,11 +541,11 @@ void netlk_ctx::enqueue(bool pm, bool fwd_on, bool reduce, bool mixk, bool bwd_o
   }
   const SweepParams sp = sweep();
   const MixParams mp = mix();
+  if (use_tc && (fwd_on || bwd_on)) CUDA_OK(cudaMemsetAsync(sp.fault, 0, 8, stream));
   if (fwd_on) {
-    if (use_tc) {
-      CUDA_OK(cudaMemsetAsync(sp.fault, 0, 8, stream));
+    if (use_tc)
       launch_forward20_tc(stream, sp, fwd_level_begin.data(), dag.n_levels, sms);
-    } else if (S == 20)
+    else if (S == 20)
       launch_sweep20(stream, opts.precision, R, false, sp, fwd_level_begin.data(), dag.n_levels);
     else
       launch_forward(stream, opts.precision, R, fwd_shape, sp, fwd_level_begin.data(), dag.n_levels);
@@ -560,7 +560,9 @@ void netlk_ctx::enqueue(bool pm, bool fwd_on, bool reduce, bool mixk, bool bwd_o
     prof_mark(3);
   }
   if (bwd_on && !bwd.empty()) {
-    if (S == 20)
+    if (use_tc)
+      launch_backward20_tc(stream, sp, bwd_level_begin.data(), dag.n_levels, sms);
+    else if (S == 20)
       launch_sweep20(stream, opts.precision, R, true, sp, bwd_level_begin.data(), dag.n_levels);
     else
       launch_backward(stream, opts.precision, R, bwd_shape, sp, bwd_level_begin.data(), dag.n_levels);
