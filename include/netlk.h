@@ -110,6 +110,19 @@ typedef struct {
                                         split, FP32 accumulation); 0: CUDA
                                         cores only. No effect on other
                                         contexts.                            */
+  int32_t checkpoint_segments;       /* CLV checkpointing for DAGs whose CLVs
+                                        do not fit in device memory:
+                                        0 (default) = automatic - all CLVs are
+                                        stored while they fit in 70 % of the
+                                        free device memory, otherwise the
+                                        levels are cut into ceil(sqrt(levels))
+                                        segments (more if needed); 1 = store
+                                        every CLV; k >= 2 = k segments. With
+                                        k segments only the CLVs read across a
+                                        segment boundary are kept, the adjoint
+                                        recomputes the other CLVs of each
+                                        segment before its levels (one extra
+                                        forward over them).                   */
 } netlk_options;
 
 typedef struct {
@@ -134,7 +147,11 @@ typedef struct {
   int64_t launches_per_gradient_eval; /* kernels of one logL + gradient call:
                                 P-matrices, one forward launch per level,
                                 site sums, mixture, one adjoint launch per
-                                level, two gradient reduction stages          */
+                                level, the recompute launches of checkpointed
+                                segments, two gradient reduction stages       */
+  int32_t checkpoint_segments; /* segments in use (1 = every CLV stored)     */
+  int32_t clv_slots;           /* CLV buffers held (= n_variants when 1)     */
+  int64_t recompute_site_updates; /* extra forward updates per gradient eval */
 } netlk_dag_stats;
 
 /* --------------------------------------------------------------- lifecycle */

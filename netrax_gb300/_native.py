@@ -62,7 +62,7 @@ class Options(ctypes.Structure):
                 ("min_interesting_tree_logprob", ctypes.c_double),
                 ("device", ctypes.c_int32), ("use_cuda_graph", ctypes.c_int32),
                 ("host_only", ctypes.c_int32), ("autotune", ctypes.c_int32),
-                ("tensor_cores", ctypes.c_int32)]
+                ("tensor_cores", ctypes.c_int32), ("checkpoint_segments", ctypes.c_int32)]
 
 
 class DagStats(ctypes.Structure):
@@ -73,7 +73,9 @@ class DagStats(ctypes.Structure):
                 ("n_patterns_total", ctypes.c_int64), ("site_clv_updates", ctypes.c_int64),
                 ("tip_child_uses", ctypes.c_int64), ("fake_child_uses", ctypes.c_int64),
                 ("device_bytes", ctypes.c_int64), ("forward_bytes", ctypes.c_int64),
-                ("backward_bytes", ctypes.c_int64), ("launches_per_gradient_eval", ctypes.c_int64)]
+                ("backward_bytes", ctypes.c_int64), ("launches_per_gradient_eval", ctypes.c_int64),
+                ("checkpoint_segments", ctypes.c_int32), ("clv_slots", ctypes.c_int32),
+                ("recompute_site_updates", ctypes.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -100,6 +100,17 @@ struct netlk_ctx {
   std::vector<int32_t> fwd_level_begin, bwd_level_begin;  // op ranges per launch
   std::vector<int32_t> edge_begin, edge_entries;         // edge -> adjoint op sides
   int fwd_launches = 0, bwd_launches = 0;
+  // CLV checkpointing: levels cut into segments; a variant read by an op of a
+  // later segment keeps a permanent CLV slot, the others share one segment's
+  // worth of slots and are recomputed before their segment's adjoint levels
+  int n_segments = 1, n_clv_slots = 0;
+  std::vector<int32_t> var_slot;           // CLV / scale-counter slot per variant
+  std::vector<char> var_ckpt;              // permanent slot
+  std::vector<int> seg_lo, seg_hi;         // level range (1-based) per segment
+  std::vector<FwdOp> rfwd;                 // recompute ops (no site sums)
+  std::vector<int32_t> rfwd_level_begin;   // per level, like fwd_level_begin
+  int rfwd_launches = 0;
+  int64_t recompute_updates = 0;
   int fwd_shape = 0, bwd_shape = 0, sms = 0;
   bool tuned = false;
   bool use_tc = false;  // 20-state FP32 forward on the tensor cores
@@ -109,7 +120,7 @@ struct netlk_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   int64_t dev_bytes = 0;
-  DevBuf d_clv, d_scaler, d_adj, d_msg_slots, d_tips, d_weights, d_unit_part, d_fwd, d_bwd;
+  DevBuf d_clv, d_scaler, d_adj, d_msg_slots, d_tips, d_weights, d_unit_part, d_fwd, d_bwd, d_rfwd;
   DevBuf d_pmat64, d_pmat32, d_lambda, d_U, d_Uinv, d_rates, d_rw, d_freqs, d_Q, d_brlen;
   DevBuf d_site_partial, d_tree_logl, d_root_slot, d_root_lp, d_root_dlp, d_seeds, d_wts;
   DevBuf d_slot_begin, d_slot_roots, d_parts, d_out, d_grad_partial, d_grad, d_edge_begin, d_edge_entries, d_op_sum;
@@ -160,7 +171,7 @@ struct netlk_ctx {
     for (auto e : prof_ev) cudaEventDestroy(e);
     for (auto g : {graph_logl, graph_grad, graph_partials, graph_mixbwd})
       if (g) cudaGraphExecDestroy(g);
-    for (DevBuf *b : {&d_clv, &d_scaler, &d_adj, &d_msg_slots, &d_tips, &d_weights, &d_unit_part, &d_fwd, &d_bwd,
+    for (DevBuf *b : {&d_clv, &d_scaler, &d_adj, &d_msg_slots, &d_tips, &d_weights, &d_unit_part, &d_fwd, &d_bwd, &d_rfwd,
                       &d_pmat64, &d_pmat32, &d_lambda, &d_U, &d_Uinv, &d_rates, &d_rw, &d_freqs, &d_Q,
                       &d_brlen, &d_site_partial, &d_tree_logl, &d_root_slot, &d_root_lp, &d_root_dlp,
                       &d_seeds, &d_wts, &d_slot_begin, &d_slot_roots, &d_parts, &d_out, &d_grad_partial, &d_grad,
@@ -224,7 +235,8 @@ struct netlk_ctx {
   }
 
   void autotune();
-  void build_schedules();
+  void build_schedules(int segments);
+  int choose_segments(size_t free_bytes) const;
   void allocate_and_upload(const netlk_partition *in_parts);
   void upload_model();
   void upload_probs();
@@ -238,8 +250,59 @@ struct netlk_ctx {
 };
 
 // ------------------------------------------------------------------ schedules
-void netlk_ctx::build_schedules() {
+// Segments: contiguous level ranges with about V / k variants each.
+void netlk_ctx::build_schedules(int segments) {
   const int V = (int)dag.vars.size();
+  n_segments = std::max(1, std::min(segments, std::max(1, dag.n_levels)));
+  std::vector<int> seg_of_level(dag.n_levels + 2, 0);
+  seg_lo.assign(n_segments, 1);
+  seg_hi.assign(n_segments, dag.n_levels);
+  {
+    std::vector<int64_t> cnt(dag.n_levels + 2, 0);
+    for (const Variant &v : dag.vars) cnt[v.level]++;
+    int s = 0;
+    int64_t acc = 0;
+    for (int L = 1; L <= dag.n_levels; ++L) {
+      // open the next segment once this one holds its share (levels left >= segments left)
+      if (s + 1 < n_segments && acc >= (int64_t)(s + 1) * V / n_segments && dag.n_levels - L + 1 >= n_segments - s - 1) {
+        seg_hi[s] = L - 1;
+        ++s;
+        seg_lo[s] = L;
+      }
+      seg_of_level[L] = s;
+      acc += cnt[L];
+    }
+    n_segments = s + 1;
+    seg_lo.resize(n_segments);
+    seg_hi.resize(n_segments);
+    seg_hi[n_segments - 1] = dag.n_levels;
+  }
+  // permanent slots: variants read by an op of a later segment
+  var_ckpt.assign(V, 0);
+  var_slot.assign(V, 0);
+  if (n_segments == 1) {
+    for (int v = 0; v < V; ++v) var_slot[v] = v;
+    n_clv_slots = V;
+  } else {
+    for (int v = 0; v < V; ++v)
+      for (int i = 0; i < 2; ++i) {
+        const int32_t c = dag.vars[v].ref[i];
+        if (c >= 0 && seg_of_level[dag.vars[v].level] > seg_of_level[dag.vars[c].level]) var_ckpt[c] = 1;
+      }
+    int n_ckpt = 0;
+    for (int v = 0; v < V; ++v)
+      if (var_ckpt[v]) var_slot[v] = n_ckpt++;
+    std::vector<int> used(n_segments, 0);
+    int region = 0;
+    for (int v = 0; v < V; ++v)
+      if (!var_ckpt[v]) {
+        const int sg = seg_of_level[dag.vars[v].level];
+        var_slot[v] = n_ckpt + used[sg]++;
+        region = std::max(region, used[sg]);
+      }
+    n_clv_slots = n_ckpt + region;
+  }
+  auto map_ref = [&](int32_t r) { return r >= 0 ? var_slot[r] : r; };
   // displayed-tree root slots
   std::vector<int> slot_of(V, -1);
   n_slots = 0;
@@ -265,7 +328,7 @@ void netlk_ctx::build_schedules() {
   for (int L = 1; L <= dag.n_levels; ++L) {
     for (int v : by_level[L]) {
       const Variant &var = dag.vars[v];
-      FwdOp op{v, var.ref[0], var.ref[1], var.edge[0], var.edge[1], slot_of[v], 0, 0};
+      FwdOp op{var_slot[v], map_ref(var.ref[0]), map_ref(var.ref[1]), var.edge[0], var.edge[1], slot_of[v], 0, 0};
       fwd.push_back(op);
       tip_uses += is_tip_ref(var.ref[0]) + is_tip_ref(var.ref[1]);
       fake_uses += var.ref[1] == kFake;
@@ -274,6 +337,23 @@ void netlk_ctx::build_schedules() {
   }
   fwd_launches = 0;
   for (int L = 0; L < dag.n_levels; ++L) fwd_launches += fwd_level_begin[L + 1] > fwd_level_begin[L];
+  // recompute ops: the non-permanent variants of every segment but the last
+  // (whose CLVs are still in place when the adjoint starts)
+  rfwd.clear();
+  rfwd_level_begin.assign(1, 0);
+  rfwd_launches = 0;
+  recompute_updates = 0;
+  for (int L = 1; L <= dag.n_levels; ++L) {
+    if (n_segments > 1 && seg_of_level[L] < n_segments - 1)
+      for (int v : by_level[L]) {
+        if (var_ckpt[v]) continue;
+        const Variant &var = dag.vars[v];
+        rfwd.push_back(FwdOp{var_slot[v], map_ref(var.ref[0]), map_ref(var.ref[1]), var.edge[0], var.edge[1], -1, 0, 0});
+      }
+    rfwd_level_begin.push_back((int32_t)rfwd.size());
+    rfwd_launches += rfwd_level_begin[L] > rfwd_level_begin[L - 1];
+  }
+  recompute_updates = (int64_t)rfwd.size() * N;
   site_updates = (int64_t)V * N;
   const int64_t clv_b = (int64_t)R * S * (opts.precision == NETLK_FP32 ? 4 : 8);
   auto child_bytes = [&](int32_t ref) -> int64_t {
@@ -308,8 +388,8 @@ void netlk_ctx::build_schedules() {
     for (int x : by_level[L]) {
       if (!inb[x]) continue;
       BwdOp op{};
-      op.x = x;
-      op.a = dag.vars[x].ref[0];
+      op.x = var_slot[x];
+      op.a = dag.vars[x].ref[0];  // variant ids until the message slots are placed
       op.b = dag.vars[x].ref[1];
       op.ea = dag.vars[x].edge[0];
       op.eb = dag.vars[x].edge[1];
@@ -354,6 +434,10 @@ void netlk_ctx::build_schedules() {
     for (int32_t m : read_here) free_slots.push_back(m);
     bwd_level_begin.push_back((int32_t)bwd.size());
   }
+  for (BwdOp &op : bwd) {  // variant ids -> CLV slots
+    op.a = map_ref(op.a);
+    op.b = map_ref(op.b);
+  }
   bwd_launches = 0;
   for (int L = 0; L < dag.n_levels; ++L) bwd_launches += bwd_level_begin[L + 1] > bwd_level_begin[L];
   // edge -> (adjoint op, side) entries for the gradient reduction
@@ -392,7 +476,13 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
   }
   n_units = (int)(N / ppw);
   n_units_fwd = (int)(N / ppw_f);
-  build_schedules();
+  int segments = opts.checkpoint_segments;
+  if (segments <= 0) {
+    size_t free_b = 0, total_b = 0;
+    if (!opts.host_only && cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) free_b = 0;
+    segments = opts.host_only ? 1 : choose_segments(free_b);
+  }
+  build_schedules(segments);
   if (opts.host_only) return;
   // host staging of tips / weights / unit map
   const uint32_t all_states = S == 4 ? 0xfu : 0xfffffu;
@@ -420,8 +510,9 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
   }
   const size_t real_sz = opts.precision == NETLK_FP32 ? 4 : 8;
   const size_t clv_per_var = (size_t)N * R * S * real_sz;
-  d_clv.alloc(clv_per_var * V, dev_bytes);
-  d_scaler.alloc((size_t)N * V * 4, dev_bytes);
+  (void)V;
+  d_clv.alloc(clv_per_var * n_clv_slots, dev_bytes);
+  d_scaler.alloc((size_t)N * n_clv_slots * 4, dev_bytes);
   d_adj.alloc(clv_per_var * std::max(1, n_adj), dev_bytes);
   d_msg_slots.alloc(std::max<size_t>(1, msg_slots.size()) * 4, dev_bytes);
   d_tips.alloc(S == 4 ? tips.size() : tips32.size() * 4, dev_bytes);
@@ -429,6 +520,7 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
   d_unit_part.alloc(n_units * 4, dev_bytes);
   d_fwd.alloc(fwd.size() * sizeof(FwdOp), dev_bytes);
   d_bwd.alloc(bwd.size() * sizeof(BwdOp), dev_bytes);
+  d_rfwd.alloc(std::max<size_t>(1, rfwd.size()) * sizeof(FwdOp), dev_bytes);
   const size_t nm = (size_t)P * topo.n_edges * R * S * S;
   d_pmat64.alloc(nm * 8, dev_bytes);
   if (opts.precision == NETLK_FP32) d_pmat32.alloc(nm * 4, dev_bytes);
@@ -473,6 +565,8 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
   CUDA_OK(cudaMemcpyAsync(d_weights.p, weights.data(), N * 8, cudaMemcpyHostToDevice, stream));
   CUDA_OK(cudaMemcpyAsync(d_unit_part.p, unit_part.data(), n_units * 4, cudaMemcpyHostToDevice, stream));
   CUDA_OK(cudaMemcpyAsync(d_fwd.p, fwd.data(), fwd.size() * sizeof(FwdOp), cudaMemcpyHostToDevice, stream));
+  if (!rfwd.empty())
+    CUDA_OK(cudaMemcpyAsync(d_rfwd.p, rfwd.data(), rfwd.size() * sizeof(FwdOp), cudaMemcpyHostToDevice, stream));
   if (!bwd.empty())
     CUDA_OK(cudaMemcpyAsync(d_bwd.p, bwd.data(), bwd.size() * sizeof(BwdOp), cudaMemcpyHostToDevice, stream));
   if (!msg_slots.empty())
@@ -531,6 +625,30 @@ void netlk_ctx::upload_probs() {
   probs_dirty = false;
 }
 
+// Automatic checkpointing: every CLV is stored while all of them take at most
+// 70 % of the free device memory; otherwise ceil(sqrt(levels)) segments, or
+// more until the permanent + one segment's CLVs fit.
+int netlk_ctx::choose_segments(size_t free_bytes) const {
+  const size_t per = (size_t)N * R * S * (opts.precision == NETLK_FP32 ? 4 : 8) + (size_t)N * 4;
+  const double budget = 0.7 * (double)free_bytes;
+  if ((double)per * dag.vars.size() <= budget || dag.n_levels <= 1) return 1;
+  const int n_levels = dag.n_levels;
+  int k = (int)std::ceil(std::sqrt((double)n_levels));
+  for (; k <= n_levels; ++k) {
+    netlk_ctx probe;  // slot count of a k-segment split, host side only
+    probe.dag = dag;
+    probe.N = N;
+    probe.R = R;
+    probe.S = S;
+    probe.opts = opts;
+    probe.topo = topo;
+    probe.device = -1;
+    probe.build_schedules(k);
+    if ((double)per * probe.n_clv_slots <= budget) return k;
+  }
+  return n_levels;
+}
+
 void netlk_ctx::enqueue(bool pm, bool fwd_on, bool reduce, bool mixk, bool bwd_on) {
   prof_mark(-1);
   if (pm) {
@@ -560,12 +678,29 @@ void netlk_ctx::enqueue(bool pm, bool fwd_on, bool reduce, bool mixk, bool bwd_o
     prof_mark(3);
   }
   if (bwd_on && !bwd.empty()) {
-    if (use_tc)
-      launch_backward20_tc(stream, sp, bwd_level_begin.data(), dag.n_levels, sms);
-    else if (S == 20)
-      launch_sweep20(stream, opts.precision, R, true, sp, bwd_level_begin.data(), dag.n_levels);
-    else
-      launch_backward(stream, opts.precision, R, bwd_shape, sp, bwd_level_begin.data(), dag.n_levels);
+    // segments from the top: recompute the segment's non-permanent CLVs
+    // (every segment but the last), then its adjoint levels
+    SweepParams rp = sp;
+    rp.fwd_ops = d_rfwd.as<FwdOp>();
+    for (int sg = n_segments - 1; sg >= 0; --sg) {
+      const int lo = seg_lo[sg], nl = seg_hi[sg] - seg_lo[sg] + 1;
+      if (sg < n_segments - 1) {
+        const int32_t *rb = rfwd_level_begin.data() + (lo - 1);
+        if (use_tc)
+          launch_forward20_tc(stream, rp, rb, nl, sms);
+        else if (S == 20)
+          launch_sweep20(stream, opts.precision, R, false, rp, rb, nl);
+        else
+          launch_forward(stream, opts.precision, R, fwd_shape, rp, rb, nl);
+      }
+      const int32_t *bb = bwd_level_begin.data() + (dag.n_levels - seg_hi[sg]);
+      if (use_tc)
+        launch_backward20_tc(stream, sp, bb, nl, sms);
+      else if (S == 20)
+        launch_sweep20(stream, opts.precision, R, true, sp, bb, nl);
+      else
+        launch_backward(stream, opts.precision, R, bwd_shape, sp, bb, nl);
+    }
     prof_mark(4);
     launch_grad_reduce(stream, (int)bwd.size(), topo.n_edges, n_units, d_edge_begin.as<int32_t>(),
                        d_edge_entries.as<int32_t>(), d_grad_partial.as<double>(), d_op_sum.as<double>(),
@@ -576,7 +711,7 @@ void netlk_ctx::enqueue(bool pm, bool fwd_on, bool reduce, bool mixk, bool bwd_o
 
 void netlk_ctx::run(cudaGraphExec_t *cache, bool pm, bool fwd_on, bool reduce, bool mixk, bool bwd_on) {
   const int n = (int)pm + (fwd_on ? fwd_launches : 0) + (int)reduce + (int)mixk +
-                (bwd_on && !bwd.empty() ? bwd_launches + 2 : 0);
+                (bwd_on && !bwd.empty() ? bwd_launches + rfwd_launches + 2 : 0);
   if (!opts.use_cuda_graph || profiling) {
     enqueue(pm, fwd_on, reduce, mixk, bwd_on);
     launches += n;
@@ -744,6 +879,7 @@ int netlk_options_default(netlk_options *o) {
   o->host_only = 0;
   o->autotune = 1;
   o->tensor_cores = 1;
+  o->checkpoint_segments = 0;
   return NETLK_OK;
 }
 
@@ -874,9 +1010,13 @@ int netlk_get_dag_stats(const netlk_ctx *ctx, netlk_dag_stats *o) {
   o->tip_child_uses = ctx->tip_uses;
   o->fake_child_uses = ctx->fake_uses;
   o->device_bytes = ctx->dev_bytes;
-  o->launches_per_gradient_eval = 3 + ctx->fwd_launches + (ctx->bwd.empty() ? 0 : ctx->bwd_launches + 2);
+  o->launches_per_gradient_eval =
+      3 + ctx->fwd_launches + (ctx->bwd.empty() ? 0 : ctx->bwd_launches + ctx->rfwd_launches + 2);
   o->forward_bytes = ctx->fwd_bytes;
   o->backward_bytes = ctx->bwd_bytes;
+  o->checkpoint_segments = ctx->n_segments;
+  o->clv_slots = ctx->n_clv_slots;
+  o->recompute_site_updates = ctx->recompute_updates;
   return NETLK_OK;
 }
 
@@ -1191,8 +1331,11 @@ int netlk_get_clv(netlk_ctx *ctx, int32_t variant, int32_t part, double *clv, in
     if (variant < 0 || variant >= (int)ctx->dag.vars.size() || part < 0 || part >= ctx->P)
       throw Error(NETLK_ERR_INVALID_ARGUMENT, "variant / partition");
     if (ctx->opts.host_only) throw Error(NETLK_ERR_NO_DEVICE, "context was created host_only");
+    if (!ctx->var_ckpt.empty() && ctx->n_segments > 1 && !ctx->var_ckpt[variant])
+      throw Error(NETLK_ERR_UNSUPPORTED, "with checkpointing only the CLVs kept across segments are resident");
     CUDA_OK(cudaSetDevice(ctx->device));
     const PartInfo &pi = ctx->parts[part];
+    variant = ctx->var_slot[variant];
     const size_t per = (size_t)ctx->R * ctx->S;
     const size_t n = (size_t)pi.n * per;
     if (clv) {
@@ -1336,7 +1479,7 @@ int netlk_batch_loglikelihood_gradient(netlk_batch *b, double *totals, double *c
     CUDA_OK(cudaGetLastError());
     for (size_t i = 0; i < b->ctxs.size(); ++i) {
       netlk_ctx *c = b->ctxs[i];
-      c->launches += 1 + c->fwd_launches + 2 + (c->bwd.empty() ? 0 : c->bwd_launches + 2);
+      c->launches += 1 + c->fwd_launches + 2 + (c->bwd.empty() ? 0 : c->bwd_launches + c->rfwd_launches + 2);
       std::vector<double> g(c->topo.n_edges, 0.0);
       double tot = 0.0;
       try {

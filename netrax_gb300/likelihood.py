@@ -37,7 +37,7 @@ def _ptr(a, ct):
 class NetworkLikelihood:
     def __init__(self, network: NetworkDesc, partitions, variant="AVERAGE", precision="fp32",
                  min_interesting_tree_logprob=math.log(1e-6), device=0, use_cuda_graph=True,
-                 host_only=False, rates=None, autotune=True, tensor_cores=True):
+                 host_only=False, rates=None, autotune=True, tensor_cores=True, checkpoint_segments=0):
         L = N.lib()
         self.network = network
         self.n_parts = len(partitions)
@@ -91,6 +91,7 @@ class NetworkLikelihood:
         opts.host_only = int(bool(host_only))
         opts.autotune = int(bool(autotune))
         opts.tensor_cores = int(bool(tensor_cores))
+        opts.checkpoint_segments = int(checkpoint_segments)
         bl = arr(network.branch_lengths, np.float64)
         rp = arr(network.ret_first_probs, np.float64) if self.n_ret else None
         h = ctypes.c_void_p()

@@ -179,3 +179,24 @@ def test_batch_rejects_bad_arguments():
     assert not h.value
     assert L.netlk_batch_loglikelihood_gradient(None, None, None, None) == _native.NETLK_ERR_INVALID_ARGUMENT
     lik.close()
+
+
+def test_checkpoint_segments_reduce_clv_slots():
+    """Cutting the levels into segments keeps only the CLVs read across a
+    segment boundary; every other variant is recomputed once per gradient."""
+    from netrax_gb300 import synth
+    w = synth.config(2, scale=0.002)
+    full = NetworkLikelihood(w.network, w.partitions, host_only=True, checkpoint_segments=1).stats
+    assert full["checkpoint_segments"] == 1 and full["clv_slots"] == full["n_variants"]
+    assert full["recompute_site_updates"] == 0
+    prev = None
+    for k in (2, 4):
+        st = NetworkLikelihood(w.network, w.partitions, host_only=True, checkpoint_segments=k).stats
+        assert st["checkpoint_segments"] == k
+        assert st["clv_slots"] < full["clv_slots"]
+        assert 0 < st["recompute_site_updates"] < full["site_clv_updates"]
+        assert st["launches_per_gradient_eval"] > full["launches_per_gradient_eval"]
+        prev = st
+    # automatic mode on a host-only context stores everything
+    auto = NetworkLikelihood(w.network, w.partitions, host_only=True).stats
+    assert auto["checkpoint_segments"] == 1

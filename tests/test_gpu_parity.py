@@ -357,3 +357,32 @@ def test_reference_derivative_mode(variant):
                 assert got == pytest.approx(lik.edge_derivatives(e, second=False, mode=0), rel=1e-12, abs=1e-9)
         # the context is left evaluating the real mixture
         assert lik.loglikelihood() == pytest.approx(case[variant]["logl"], rel=FP64_REL)
+
+
+@pytest.mark.parametrize("kind", ["dna_fp32", "dna_fp64", "protein_tc"])
+def test_checkpointed_gradients_are_identical(kind):
+    """O(sqrt n) CLV checkpointing: 2-4 segments give the same logL and
+    gradient, bit for bit, as storing every CLV (the recomputed CLVs are the
+    same numbers), with fewer CLV buffers."""
+    from netrax_gb300 import synth
+    from netrax_gb300.likelihood import NetworkLikelihood
+    if kind == "protein_tc":
+        w = synth.make_protein_workload("protein", 30, 3, [500], 9)
+        prec = "fp32"
+    else:
+        w = synth.config(2, scale=0.01)
+        prec = "fp32" if kind == "dna_fp32" else "fp64"
+    for variant in ("AVERAGE", "BEST"):
+        with NetworkLikelihood(w.network, w.partitions, variant=variant, precision=prec, checkpoint_segments=1) as a:
+            ta, ga, ra = a.loglikelihood_gradient()
+            la = a.loglikelihood()
+            slots = a.stats["clv_slots"]
+            for k in (2, 3, 4):
+                with NetworkLikelihood(w.network, w.partitions, variant=variant, precision=prec,
+                                       checkpoint_segments=k) as b:
+                    assert b.stats["clv_slots"] < slots
+                    tb, gb, rb = b.loglikelihood_gradient()
+                    assert tb == ta and np.array_equal(gb, ga) and np.array_equal(rb, ra)
+                    assert b.loglikelihood() == la
+                    tb2, gb2, _ = b.loglikelihood_gradient()  # again, after a logL-only call
+                    assert tb2 == ta and np.array_equal(gb2, ga)
