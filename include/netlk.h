@@ -123,6 +123,14 @@ typedef struct {
                                         recomputes the other CLVs of each
                                         segment before its levels (one extra
                                         forward over them).                   */
+  int32_t incremental;               /* 1 (default): netlk_loglikelihood and
+                                        netlk_edge_loglikelihood recompute
+                                        only the CLVs that depend on branch
+                                        lengths changed since the last full
+                                        forward sweep (the reference's
+                                        clv_valid flags, InvalidationHelper.cpp
+                                        :52-237); 0: every call recomputes
+                                        every CLV. Results are identical.     */
 } netlk_options;
 
 typedef struct {
@@ -230,6 +238,18 @@ int netlk_loglikelihood(netlk_ctx *ctx, double *total, double *partition_logl,
 int netlk_loglikelihood_gradient(netlk_ctx *ctx, double *total,
                                  double *partition_logl, double *d_brlen,
                                  double *d_retprob);
+
+/* Log-likelihood with branch `edge` set to `length` (clamped like every
+ * length; the other lengths, the model and the probabilities unchanged);
+ * the context keeps the new length. Replaces computeLoglikelihoodBrlenOpt
+ * (src/likelihood/VirtualRerooting.cpp:348-585), the per-edge evaluation of
+ * the branch-length optimizer's Newton-Raphson accept / revert and Brent
+ * probes: with incremental evaluation on, only the variants above the edge
+ * are recomputed. */
+int netlk_edge_loglikelihood(netlk_ctx *ctx, int32_t edge, double length, double *total);
+/* Site-CLV updates the last evaluation computed in its forward sweep
+ * (fewer than n_variants * patterns after an incremental evaluation). */
+int netlk_last_site_updates(const netlk_ctx *ctx, int64_t *site_updates);
 
 /* First and second derivative of the log-likelihood w.r.t. one branch
  * length, for the Newton-Raphson callback (network_derivative_func_multi,

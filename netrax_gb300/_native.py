@@ -36,7 +36,8 @@ EXPORTED = [
     "netlk_launch_count", "netlk_set_branch_lengths_device", "netlk_enqueue",
     "netlk_result_pointers", "netlk_set_profiling", "netlk_kernel_times", "netlk_tuning",
     "netlk_mix_site_loglikelihoods_noalloc", "netlk_batch_create",
-    "netlk_batch_loglikelihood_gradient", "netlk_batch_destroy",
+    "netlk_batch_loglikelihood_gradient", "netlk_batch_destroy", "netlk_edge_loglikelihood",
+    "netlk_last_site_updates",
 ]
 
 
@@ -62,7 +63,8 @@ class Options(ctypes.Structure):
                 ("min_interesting_tree_logprob", ctypes.c_double),
                 ("device", ctypes.c_int32), ("use_cuda_graph", ctypes.c_int32),
                 ("host_only", ctypes.c_int32), ("autotune", ctypes.c_int32),
-                ("tensor_cores", ctypes.c_int32), ("checkpoint_segments", ctypes.c_int32)]
+                ("tensor_cores", ctypes.c_int32), ("checkpoint_segments", ctypes.c_int32),
+                ("incremental", ctypes.c_int32)]
 
 
 class DagStats(ctypes.Structure):
@@ -134,6 +136,8 @@ def lib():
     L.netlk_batch_loglikelihood_gradient.argtypes = [vp, c_double_p, ctypes.POINTER(c_double_p),
                                                      ctypes.POINTER(c_double_p)]
     L.netlk_batch_destroy.argtypes = [vp]
+    L.netlk_edge_loglikelihood.argtypes = [vp, ctypes.c_int32, ctypes.c_double, c_double_p]
+    L.netlk_last_site_updates.argtypes = [vp, ctypes.POINTER(ctypes.c_int64)]
     for name in EXPORTED:
         f = getattr(L, name)
         if f.restype is ctypes.c_int or f.restype is None:

@@ -111,6 +111,12 @@ struct netlk_ctx {
   std::vector<int32_t> rfwd_level_begin;   // per level, like fwd_level_begin
   int rfwd_launches = 0;
   int64_t recompute_updates = 0;
+  // incremental evaluation: the lengths the stored CLVs were computed with
+  bool clv_valid = false;
+  std::vector<double> clv_brlen;
+  std::vector<FwdOp> ifwd;                 // ops of the variants to recompute
+  std::vector<int32_t> ifwd_level_begin;
+  int64_t last_updates = 0;
   int fwd_shape = 0, bwd_shape = 0, sms = 0;
   bool tuned = false;
   bool use_tc = false;  // 20-state FP32 forward on the tensor cores
@@ -120,11 +126,11 @@ struct netlk_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   int64_t dev_bytes = 0;
-  DevBuf d_clv, d_scaler, d_adj, d_msg_slots, d_tips, d_weights, d_unit_part, d_fwd, d_bwd, d_rfwd;
+  DevBuf d_clv, d_scaler, d_adj, d_msg_slots, d_tips, d_weights, d_unit_part, d_fwd, d_bwd, d_rfwd, d_ifwd;
   DevBuf d_pmat64, d_pmat32, d_lambda, d_U, d_Uinv, d_rates, d_rw, d_freqs, d_Q, d_brlen;
   DevBuf d_site_partial, d_tree_logl, d_root_slot, d_root_lp, d_root_dlp, d_seeds, d_wts;
   DevBuf d_slot_begin, d_slot_roots, d_parts, d_out, d_grad_partial, d_grad, d_edge_begin, d_edge_entries, d_op_sum;
-  PinnedBuf h_brlen, h_root_lp, h_root_dlp, h_out, h_grad, h_tree;
+  PinnedBuf h_brlen, h_root_lp, h_root_dlp, h_out, h_grad, h_tree, h_ifwd;
   cudaGraphExec_t graph_logl = nullptr, graph_grad = nullptr, graph_partials = nullptr,
                   graph_mixbwd = nullptr;
   bool probs_dirty = true, model_dirty = true;
@@ -171,7 +177,7 @@ struct netlk_ctx {
     for (auto e : prof_ev) cudaEventDestroy(e);
     for (auto g : {graph_logl, graph_grad, graph_partials, graph_mixbwd})
       if (g) cudaGraphExecDestroy(g);
-    for (DevBuf *b : {&d_clv, &d_scaler, &d_adj, &d_msg_slots, &d_tips, &d_weights, &d_unit_part, &d_fwd, &d_bwd, &d_rfwd,
+    for (DevBuf *b : {&d_clv, &d_scaler, &d_adj, &d_msg_slots, &d_tips, &d_weights, &d_unit_part, &d_fwd, &d_bwd, &d_rfwd, &d_ifwd,
                       &d_pmat64, &d_pmat32, &d_lambda, &d_U, &d_Uinv, &d_rates, &d_rw, &d_freqs, &d_Q,
                       &d_brlen, &d_site_partial, &d_tree_logl, &d_root_slot, &d_root_lp, &d_root_dlp,
                       &d_seeds, &d_wts, &d_slot_begin, &d_slot_roots, &d_parts, &d_out, &d_grad_partial, &d_grad,
@@ -242,6 +248,9 @@ struct netlk_ctx {
   void upload_probs();
   void enqueue(bool pm, bool fwd_on, bool reduce, bool mixk, bool bwd_on);
   void run(cudaGraphExec_t *cache, bool pm, bool fwd_on, bool reduce, bool mixk, bool bwd_on);
+  // logL recomputing only the CLVs above changed branch lengths; false when a
+  // full evaluation is needed instead
+  bool run_incremental();
   void prepare_state();  // model / probabilities uploads and launch-shape tuning
   void prepare();        // prepare_state + branch-length upload
   void finish(double *total, double *part_logl, double *d_brlen, double *d_ret);
@@ -521,6 +530,7 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
   d_fwd.alloc(fwd.size() * sizeof(FwdOp), dev_bytes);
   d_bwd.alloc(bwd.size() * sizeof(BwdOp), dev_bytes);
   d_rfwd.alloc(std::max<size_t>(1, rfwd.size()) * sizeof(FwdOp), dev_bytes);
+  d_ifwd.alloc(fwd.size() * sizeof(FwdOp), dev_bytes);
   const size_t nm = (size_t)P * topo.n_edges * R * S * S;
   d_pmat64.alloc(nm * 8, dev_bytes);
   if (opts.precision == NETLK_FP32) d_pmat32.alloc(nm * 4, dev_bytes);
@@ -584,6 +594,7 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
   h_out.alloc((3 + P + topo.n_ret) * 8);
   h_grad.alloc(topo.n_edges * 8);
   h_tree.alloc((size_t)n_slots * P * 8);
+  h_ifwd.alloc(fwd.size() * sizeof(FwdOp));
 }
 
 void netlk_ctx::upload_model() {
@@ -609,6 +620,7 @@ void netlk_ctx::upload_model() {
   CUDA_OK(cudaMemcpyAsync(d_Q.p, Q.data(), Q.size() * 8, cudaMemcpyHostToDevice, stream));
   CUDA_OK(cudaStreamSynchronize(stream));
   model_dirty = false;
+  clv_valid = false;
 }
 
 void netlk_ctx::upload_probs() {
@@ -712,6 +724,11 @@ void netlk_ctx::enqueue(bool pm, bool fwd_on, bool reduce, bool mixk, bool bwd_o
 void netlk_ctx::run(cudaGraphExec_t *cache, bool pm, bool fwd_on, bool reduce, bool mixk, bool bwd_on) {
   const int n = (int)pm + (fwd_on ? fwd_launches : 0) + (int)reduce + (int)mixk +
                 (bwd_on && !bwd.empty() ? bwd_launches + rfwd_launches + 2 : 0);
+  if (fwd_on && pm) {  // every CLV recomputed from the current lengths
+    clv_valid = !device_brlen;
+    clv_brlen = brlen;
+    last_updates = site_updates;
+  }
   if (!opts.use_cuda_graph || profiling) {
     enqueue(pm, fwd_on, reduce, mixk, bwd_on);
     launches += n;
@@ -728,6 +745,55 @@ void netlk_ctx::run(cudaGraphExec_t *cache, bool pm, bool fwd_on, bool reduce, b
   }
   CUDA_OK(cudaGraphLaunch(*cache, stream));
   launches += n;
+}
+
+bool netlk_ctx::run_incremental() {
+  if (!opts.incremental || !clv_valid || n_segments != 1 || device_brlen || profiling) return false;
+  const int E = topo.n_edges;
+  std::vector<char> dirty_edge(E, 0);
+  for (int e = 0; e < E; ++e) dirty_edge[e] = brlen[e] != clv_brlen[e];
+  // with one segment the CLV slots are the variant ids; fwd is in level order
+  std::vector<char> dirty(dag.vars.size(), 0);
+  ifwd.clear();
+  ifwd_level_begin.assign(1, 0);
+  int n_launch = 0;
+  for (int L = 0; L < dag.n_levels; ++L) {
+    for (int i = fwd_level_begin[L]; i < fwd_level_begin[L + 1]; ++i) {
+      const FwdOp &op = fwd[i];
+      const bool d = dirty_edge[op.ea] || (op.eb >= 0 && dirty_edge[op.eb]) || (op.a >= 0 && dirty[op.a]) ||
+                     (op.b >= 0 && dirty[op.b]);
+      if (d) {
+        dirty[op.out] = 1;
+        ifwd.push_back(op);
+      }
+    }
+    ifwd_level_begin.push_back((int32_t)ifwd.size());
+    n_launch += ifwd_level_begin[L + 1] > ifwd_level_begin[L];
+  }
+  const SweepParams sp = sweep();
+  const MixParams mp = mix();
+  if (use_tc) CUDA_OK(cudaMemsetAsync(sp.fault, 0, 8, stream));
+  launch_pmatrix(stream, P, topo.n_edges, R, S, d_lambda.as<double>(), d_U.as<double>(), d_Uinv.as<double>(),
+                 d_rates.as<double>(), d_brlen.as<double>(), d_pmat64.as<double>(),
+                 opts.precision == NETLK_FP32 ? d_pmat32.as<float>() : nullptr);
+  if (!ifwd.empty()) {
+    std::memcpy(h_ifwd.p, ifwd.data(), ifwd.size() * sizeof(FwdOp));
+    CUDA_OK(cudaMemcpyAsync(d_ifwd.p, h_ifwd.p, ifwd.size() * sizeof(FwdOp), cudaMemcpyHostToDevice, stream));
+    SweepParams ip = sp;
+    ip.fwd_ops = d_ifwd.as<FwdOp>();
+    if (use_tc)
+      launch_forward20_tc(stream, ip, ifwd_level_begin.data(), dag.n_levels, sms);
+    else if (S == 20)
+      launch_sweep20(stream, opts.precision, R, false, ip, ifwd_level_begin.data(), dag.n_levels);
+    else
+      launch_forward(stream, opts.precision, R, fwd_shape, ip, ifwd_level_begin.data(), dag.n_levels);
+  }
+  launch_tree_reduce(stream, mp);
+  launch_mix(stream, mp);
+  launches += 3 + n_launch;
+  clv_brlen = brlen;
+  last_updates = (int64_t)ifwd.size() * N;
+  return true;
 }
 
 // Times every launch shape of the two sweeps once on this context's own
@@ -880,6 +946,7 @@ int netlk_options_default(netlk_options *o) {
   o->autotune = 1;
   o->tensor_cores = 1;
   o->checkpoint_segments = 0;
+  o->incremental = 1;
   return NETLK_OK;
 }
 
@@ -1092,7 +1159,7 @@ int netlk_loglikelihood(netlk_ctx *ctx, double *total, double *part_logl, double
   if (!ctx) return NETLK_ERR_INVALID_ARGUMENT;
   return guarded(ctx, [&] {
     ctx->prepare();
-    ctx->run(&ctx->graph_logl, true, true, true, true, false);
+    if (!ctx->run_incremental()) ctx->run(&ctx->graph_logl, true, true, true, true, false);
     if (tree_partition_logl)
       CUDA_OK(cudaMemcpyAsync(ctx->h_tree.p, ctx->d_tree_logl.p, (size_t)ctx->n_slots * ctx->P * 8,
                               cudaMemcpyDeviceToHost, ctx->stream));
@@ -1227,6 +1294,26 @@ int netlk_edge_derivatives(netlk_ctx *ctx, int32_t edge, int32_t mode, double *d
       *d2 = (gp - gm) / (h + hm);
     }
   });
+}
+
+int netlk_edge_loglikelihood(netlk_ctx *ctx, int32_t edge, double length, double *total) {
+  if (!ctx) return NETLK_ERR_INVALID_ARGUMENT;
+  return guarded(ctx, [&] {
+    if (edge < 0 || edge >= ctx->topo.n_edges) throw Error(NETLK_ERR_INVALID_ARGUMENT, "edge");
+    if (!std::isfinite(length) || length < 0.0) throw Error(NETLK_ERR_INVALID_ARGUMENT, "branch length");
+    if (ctx->device_brlen)
+      throw Error(NETLK_ERR_INVALID_ARGUMENT, "branch lengths are device-resident: set them on the host first");
+    ctx->brlen[edge] = std::min(std::max(length, 1e-6), 100.0);
+    ctx->prepare();
+    if (!ctx->run_incremental()) ctx->run(&ctx->graph_logl, true, true, true, true, false);
+    ctx->finish(total, nullptr, nullptr, nullptr);
+  });
+}
+
+int netlk_last_site_updates(const netlk_ctx *ctx, int64_t *site_updates) {
+  if (!ctx || !site_updates) return NETLK_ERR_INVALID_ARGUMENT;
+  *site_updates = ctx->last_updates;
+  return NETLK_OK;
 }
 
 int netlk_tree_partials(netlk_ctx *ctx, double *out) {
@@ -1488,6 +1575,9 @@ int netlk_batch_loglikelihood_gradient(netlk_batch *b, double *totals, double *c
         throw Error(e.status, "batch: candidate " + std::to_string(i) + ": " + e.what());
       }
       if (c->bwd.empty()) std::fill(g.begin(), g.end(), 0.0);
+      c->clv_valid = true;  // every CLV now matches the context's host lengths
+      c->clv_brlen = c->brlen;
+      c->last_updates = c->site_updates;
       if (totals) totals[i] = tot;
       if (d_brlen && d_brlen[i]) std::memcpy(d_brlen[i], g.data(), g.size() * 8);
     }

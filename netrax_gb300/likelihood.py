@@ -37,7 +37,8 @@ def _ptr(a, ct):
 class NetworkLikelihood:
     def __init__(self, network: NetworkDesc, partitions, variant="AVERAGE", precision="fp32",
                  min_interesting_tree_logprob=math.log(1e-6), device=0, use_cuda_graph=True,
-                 host_only=False, rates=None, autotune=True, tensor_cores=True, checkpoint_segments=0):
+                 host_only=False, rates=None, autotune=True, tensor_cores=True, checkpoint_segments=0,
+                 incremental=True):
         L = N.lib()
         self.network = network
         self.n_parts = len(partitions)
@@ -92,6 +93,7 @@ class NetworkLikelihood:
         opts.autotune = int(bool(autotune))
         opts.tensor_cores = int(bool(tensor_cores))
         opts.checkpoint_segments = int(checkpoint_segments)
+        opts.incremental = int(bool(incremental))
         bl = arr(network.branch_lengths, np.float64)
         rp = arr(network.ret_first_probs, np.float64) if self.n_ret else None
         h = ctypes.c_void_p()
@@ -166,6 +168,17 @@ class NetworkLikelihood:
         if details:
             return tot.value, gb, gr[:self.n_ret], pl
         return tot.value, gb, gr[:self.n_ret]
+
+    def edge_loglikelihood(self, edge, length):
+        """Network logL with branch ``edge`` set to ``length`` (kept)."""
+        tot = ctypes.c_double()
+        N.check(N.lib().netlk_edge_loglikelihood(self._h, int(edge), float(length), ctypes.byref(tot)), self._h)
+        return tot.value
+
+    def last_site_updates(self):
+        n = ctypes.c_int64()
+        N.check(N.lib().netlk_last_site_updates(self._h, ctypes.byref(n)), self._h)
+        return n.value
 
     def edge_derivatives(self, edge, second=True, mode=0):
         """d logL / d t_edge (and the second derivative): mode 0 the true

@@ -386,3 +386,62 @@ def test_checkpointed_gradients_are_identical(kind):
                     assert b.loglikelihood() == la
                     tb2, gb2, _ = b.loglikelihood_gradient()  # again, after a logL-only call
                     assert tb2 == ta and np.array_equal(gb2, ga)
+
+
+@pytest.mark.parametrize("kind", ["dna_fp32", "dna_fp64", "protein_tc"])
+def test_incremental_matches_full(kind):
+    """Incremental evaluation (only the variants above changed branch
+    lengths) gives exactly the full evaluation's logL along a sequence of
+    single-edge, multi-edge, no-op, probability and model changes, and
+    recomputes fewer CLVs when one edge changes; netlk_edge_loglikelihood ==
+    setting the length and evaluating."""
+    from netrax_gb300 import synth
+    from netrax_gb300.likelihood import NetworkLikelihood
+    if kind == "protein_tc":
+        w = synth.make_protein_workload("protein", 24, 2, [400], 4)
+        prec = "fp32"
+    else:
+        w = synth.config(0)
+        prec = "fp32" if kind == "dna_fp32" else "fp64"
+    rng = np.random.default_rng(5)
+    E = w.network.n_edges
+    with NetworkLikelihood(w.network, w.partitions, precision=prec) as inc, \
+            NetworkLikelihood(w.network, w.partitions, precision=prec, incremental=False) as full:
+        b = w.network.branch_lengths.copy()
+        assert inc.loglikelihood() == full.loglikelihood()
+        total_updates = inc.stats["site_clv_updates"]
+        fewer = 0
+        for step in range(12):
+            kind_step = step % 6
+            if kind_step in (0, 1, 2):       # one edge
+                e = int(rng.integers(E))
+                b[e] *= float(np.exp(0.3 * rng.standard_normal()))
+            elif kind_step == 3:             # several edges
+                for e in rng.choice(E, 3, replace=False):
+                    b[e] *= float(np.exp(0.3 * rng.standard_normal()))
+            elif kind_step == 4 and w.network.n_reticulations:  # probabilities only
+                p = np.clip(rng.uniform(0.2, 0.8, w.network.n_reticulations), 0.01, 0.99)
+                inc.set_reticulation_probs(p)
+                full.set_reticulation_probs(p)
+            inc.set_branch_lengths(b)
+            full.set_branch_lengths(b)
+            li, lf = inc.loglikelihood(), full.loglikelihood()
+            assert li == lf
+            if kind_step in (0, 1, 2):
+                fewer += inc.last_site_updates() < total_updates
+            if kind_step == 5:                # no change at all: nothing recomputed
+                assert inc.last_site_updates() == 0
+        assert fewer >= 1
+        # the edge evaluation entry point
+        e = int(rng.integers(E))
+        le = inc.edge_loglikelihood(e, 0.05)
+        b[e] = 0.05
+        full.set_branch_lengths(b)
+        assert le == full.loglikelihood()
+        # a gradient evaluation in between leaves the incremental state consistent
+        tg = inc.loglikelihood_gradient()[0]
+        assert tg == full.loglikelihood_gradient()[0]
+        b[(e + 1) % E] *= 1.5
+        inc.set_branch_lengths(b)
+        full.set_branch_lengths(b)
+        assert inc.loglikelihood() == full.loglikelihood()
