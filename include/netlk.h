@@ -360,6 +360,23 @@ int netlk_batch_loglikelihood_gradient(netlk_batch *batch, double *totals, doubl
                                        double *const *d_retprob);
 int netlk_batch_destroy(netlk_batch *batch);
 
+/* ----------------------------------------------------- alignment front end */
+/* The steps between an alignment file and netlk_partition, done in the
+ * reference by raxml-ng / libpll before NetRAX builds its partitions
+ * (pattern compression: opts.use_pattern_compression, src/RaxmlWrapper.cpp:329-330).
+ * netlk_encode_states: characters -> state masks. states 4: bit i = A C G T
+ * (U = T; IUPAC codes R Y S W K M B D H V = their unions; N ? - . O X = all);
+ * states 20: bit i = A R N D C Q E G H I L K M F P S T W Y V (B = N|D,
+ * Z = Q|E, J = I|L; X ? - . * = all). Case-insensitive. An unknown character
+ * returns NETLK_ERR_INVALID_ARGUMENT with its index in bad_index. */
+int netlk_encode_states(const char *chars, int64_t n, int32_t states, uint32_t *out_masks, int64_t *bad_index);
+/* Distinct alignment columns and their multiplicities. tip_states
+ * [n_tips][n_sites] (row = tip); out_patterns receives [n_tips][*n_patterns]
+ * (capacity n_tips * n_sites), out_weights [*n_patterns] (capacity n_sites);
+ * columns keep the order of their first occurrence. */
+int netlk_compress_patterns(const uint32_t *tip_states, int32_t n_tips, int64_t n_sites, uint32_t *out_patterns,
+                            double *out_weights, int64_t *n_patterns);
+
 /* ------------------------------------------------------------------- debug */
 /* Copies the CLV (converted to double) and scale counters of one variant:
  * clv [n_patterns*rate_cats*states] and scaler [n_patterns] of partition

@@ -37,7 +37,7 @@ EXPORTED = [
     "netlk_result_pointers", "netlk_set_profiling", "netlk_kernel_times", "netlk_tuning",
     "netlk_mix_site_loglikelihoods_noalloc", "netlk_batch_create",
     "netlk_batch_loglikelihood_gradient", "netlk_batch_destroy", "netlk_edge_loglikelihood",
-    "netlk_last_site_updates",
+    "netlk_last_site_updates", "netlk_encode_states", "netlk_compress_patterns",
 ]
 
 
@@ -138,6 +138,10 @@ def lib():
     L.netlk_batch_destroy.argtypes = [vp]
     L.netlk_edge_loglikelihood.argtypes = [vp, ctypes.c_int32, ctypes.c_double, c_double_p]
     L.netlk_last_site_updates.argtypes = [vp, ctypes.POINTER(ctypes.c_int64)]
+    L.netlk_encode_states.argtypes = [ctypes.c_char_p, ctypes.c_int64, ctypes.c_int32, c_uint32_p,
+                                      ctypes.POINTER(ctypes.c_int64)]
+    L.netlk_compress_patterns.argtypes = [c_uint32_p, ctypes.c_int32, ctypes.c_int64, c_uint32_p, c_double_p,
+                                          ctypes.POINTER(ctypes.c_int64)]
     for name in EXPORTED:
         f = getattr(L, name)
         if f.restype is ctypes.c_int or f.restype is None:
