@@ -1,0 +1,112 @@
+"""Edge cases of the network likelihood against the oracle: the smallest
+tree, one-pattern and all-gap partitions, zero-weight patterns, clamped
+lengths and probabilities, many small partitions, ten reticulations."""
+import math
+
+import numpy as np
+import pytest
+
+from netrax_gb300 import synth
+from netrax_gb300.network import parse_extended_newick
+
+pytestmark = pytest.mark.gpu
+
+FP64_REL = 1e-9
+FP32_REL = 1e-6
+
+
+def _parts(rng, n_tips, sizes, gaps=False):
+    out = []
+    for n in sizes:
+        codes = (1 << rng.integers(0, 4, size=(n_tips, n))).astype(np.uint32)
+        if gaps:
+            codes[:] = 15
+        freqs = rng.dirichlet(np.ones(4))
+        exch = rng.dirichlet(np.ones(6)) * 6
+        out.append(synth.PartitionData(codes, np.ones(n), freqs, exch, 0.7, n))
+    return out
+
+
+def _oracle(text, parts, variant):
+    from oracle import improved, newick, pllmath
+    net = newick.parse_newick(text)
+    ps = [improved.Partition(p.tip_states, p.weights, p.freqs, p.exch, pllmath.gamma_rates_mean(p.alpha, 4))
+          for p in parts]
+    return improved.ImprovedOracle(net, ps, variant=variant).loglikelihood()
+
+
+def _check(text, parts, variant="AVERAGE"):
+    from netrax_gb300.likelihood import NetworkLikelihood
+    net = parse_extended_newick(text)
+    want = _oracle(text, parts, variant)
+    sites = sum(p.n_sites for p in parts)
+    # FP32 rounds each site likelihood at ~1e-7 relative: where logL is near
+    # zero (all-gap columns) that is an absolute error of ~1e-7 per site
+    for prec, tol, atol in (("fp64", FP64_REL, 1e-12), ("fp32", FP32_REL, 2e-7 * sites)):
+        with NetworkLikelihood(net, parts, variant=variant, precision=prec) as lik:
+            got = lik.loglikelihood()
+            assert got == pytest.approx(want, rel=tol, abs=atol)
+    return want
+
+
+def test_three_taxon_tree():
+    rng = np.random.default_rng(0)
+    _check("((A:0.1,B:0.2):0.05,C:0.3);", _parts(rng, 3, [5]))
+
+
+@pytest.mark.parametrize("variant", ["AVERAGE", "BEST"])
+def test_one_pattern_and_many_small_partitions(variant):
+    rng = np.random.default_rng(1)
+    text = synth.random_network_newick(rng, 9, 2)
+    sizes = [1, 2, 3, 5, 8, 13, 21, 34, 40, 1, 7, 16]
+    _check(text, _parts(rng, 9, sizes), variant)
+
+
+def test_all_gap_partition_has_zero_loglikelihood():
+    rng = np.random.default_rng(2)
+    text = synth.random_network_newick(rng, 7, 1)
+    want = _check(text, _parts(rng, 7, [11], gaps=True))
+    assert abs(want) < 1e-12
+
+
+def test_zero_weight_patterns_are_ignored():
+    from netrax_gb300.likelihood import NetworkLikelihood
+    rng = np.random.default_rng(3)
+    text = synth.random_network_newick(rng, 8, 2)
+    net = parse_extended_newick(text)
+    p = _parts(rng, 8, [30])[0]
+    w = p.weights.copy()
+    w[::3] = 0.0
+    zero = synth.PartitionData(p.tip_states, w, p.freqs, p.exch, p.alpha, p.n_sites)
+    keep = w > 0
+    dropped = synth.PartitionData(np.ascontiguousarray(p.tip_states[:, keep]), w[keep], p.freqs, p.exch,
+                                  p.alpha, int(keep.sum()))
+    with NetworkLikelihood(net, [zero], precision="fp64") as a, \
+            NetworkLikelihood(net, [dropped], precision="fp64") as b:
+        assert a.loglikelihood() == pytest.approx(b.loglikelihood(), rel=1e-14)
+
+
+def test_lengths_and_probabilities_are_clamped_like_the_reference():
+    """Branch lengths clamp to [1e-6, 100] and reticulation probabilities to
+    [1e-6, 1 - 1e-6] (RaxmlWrapper.cpp brlen_min/max, NetraxOptions brprob bounds)."""
+    from netrax_gb300.likelihood import NetworkLikelihood
+    rng = np.random.default_rng(4)
+    text = synth.random_network_newick(rng, 10, 2)
+    net = parse_extended_newick(text)
+    parts = _parts(rng, 10, [25])
+    with NetworkLikelihood(net, parts, precision="fp64") as lik:
+        b = net.branch_lengths.copy()
+        b[0], b[1] = 0.0, 1000.0
+        lik.set_branch_lengths(b)
+        lik.set_reticulation_probs(np.array([0.0, 1.0]))
+        l0 = lik.loglikelihood()
+        b[0], b[1] = 1e-6, 100.0
+        lik.set_branch_lengths(b)
+        lik.set_reticulation_probs(np.array([1e-6, 1.0 - 1e-6]))
+        assert lik.loglikelihood() == l0
+
+
+def test_ten_reticulations():
+    rng = np.random.default_rng(5)
+    text = synth.random_network_newick(rng, 14, 10)
+    _check(text, _parts(rng, 14, [20]))
