@@ -445,21 +445,19 @@ __global__ void tree_reduce_kernel(const MixParams m) {
 // AVERAGE: logL_p = log sum_T P(T) L_{T,p} (max-shifted); BEST: max_T.
 // Posterior tree weights become the adjoint seeds; the reticulation gradient
 // is sum_p sum_T w_{T,p} d log P(T) / d p_k.
+// Mixture, one warp per partition (partitions p = warp, warp + 8, ...):
+// per partition the best root (ties to the lower index), AVERAGE = max-shifted
+// log-sum-exp over the roots with log P(T) >= min_logprob, BEST = the max;
+// posterior weights w[p][root], the adjoint seeds per slot, and the partition's
+// d logL / d p_k partials; then thread 0 adds the partitions in index order.
+// All sums use fixed shuffle trees, so results do not depend on scheduling.
 __global__ void mix_kernel(const MixParams m) {
-  const int32_t *slot_begin = m.slot_begin, *slot_roots = m.slot_roots;
-  __shared__ double sval[256];
-  __shared__ int sidx[256];
-  __shared__ double s_logl;
-  __shared__ int s_arg;
-  double *wts = m.weights;  // [n_roots]
-  const int tid = threadIdx.x;
-  double total = 0.0;
-  for (int r = tid; r < m.n_ret; r += blockDim.x) m.out[2 + m.n_parts + r] = 0.0;
-  __syncthreads();
-  for (int part = 0; part < m.n_parts; ++part) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, n_warps = blockDim.x >> 5;
+  for (int part = warp; part < m.n_parts; part += n_warps) {
+    double *wts = m.weights + (size_t)part * m.n_roots;
     double best = -INFINITY;
     int arg = 0x7fffffff;
-    for (int i = tid; i < m.n_roots; i += blockDim.x) {
+    for (int i = lane; i < m.n_roots; i += 32) {
       if (m.root_logprob[i] < m.min_logprob) continue;
       const double v = m.root_logprob[i] + m.tree_logl[(size_t)m.root_slot[i] * m.n_parts + part];
       if (v > best || (v == best && i < arg)) {
@@ -467,68 +465,66 @@ __global__ void mix_kernel(const MixParams m) {
         arg = i;
       }
     }
-    sval[tid] = best;
-    sidx[tid] = arg;
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-      if (tid < o) {
-        const double a = sval[tid], b = sval[tid + o];
-        const int ia = sidx[tid], ib = sidx[tid + o];
-        if (b > a || (b == a && ib < ia)) {
-          sval[tid] = b;
-          sidx[tid] = ib;
-        }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double b = __shfl_xor_sync(0xffffffffu, best, o);
+      const int ib = __shfl_xor_sync(0xffffffffu, arg, o);
+      if (b > best || (b == best && ib < arg)) {
+        best = b;
+        arg = ib;
       }
-      __syncthreads();
     }
-    const double mx = sval[0];
-    const int amax = sidx[0];
-    __syncthreads();
+    double lp;
     if (m.variant == 0) {  // AVERAGE
       double acc = 0.0;
-      for (int i = tid; i < m.n_roots; i += blockDim.x) {
+      for (int i = lane; i < m.n_roots; i += 32) {
         if (m.root_logprob[i] < m.min_logprob) continue;
-        acc += exp(m.root_logprob[i] + m.tree_logl[(size_t)m.root_slot[i] * m.n_parts + part] - mx);
+        acc += exp(m.root_logprob[i] + m.tree_logl[(size_t)m.root_slot[i] * m.n_parts + part] - best);
       }
-      sval[tid] = acc;
-      __syncthreads();
-      for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if (tid < o) sval[tid] += sval[tid + o];
-        __syncthreads();
-      }
-      if (tid == 0) s_logl = mx + log(sval[0]);
-      __syncthreads();
-      const double lp = s_logl;
-      for (int i = tid; i < m.n_roots; i += blockDim.x) {
+      acc = warp_sum(acc);
+      lp = best + log(acc);
+      for (int i = lane; i < m.n_roots; i += 32)
         wts[i] = (m.root_logprob[i] < m.min_logprob)
                      ? 0.0
                      : exp(m.root_logprob[i] + m.tree_logl[(size_t)m.root_slot[i] * m.n_parts + part] - lp);
-      }
     } else {  // BEST
-      if (tid == 0) {
-        s_logl = mx;
-        s_arg = amax;
+      lp = best;
+      for (int i = lane; i < m.n_roots; i += 32) wts[i] = (i == arg) ? 1.0 : 0.0;
+    }
+    __syncwarp();
+    if (lane == 0) m.out[2 + part] = lp;
+    for (int sl = lane; sl < m.n_slots; sl += 32) {
+      double sum = 0.0;
+      for (int q = m.slot_begin[sl]; q < m.slot_begin[sl + 1]; ++q) sum += wts[m.slot_roots[q]];
+      m.seeds[(size_t)sl * m.n_parts + part] = sum;
+    }
+    // d logL_p / d p_k = sum_T w_T d log P(T) / d p_k, 8 reticulations per pass
+    for (int k0 = 0; k0 < m.n_ret; k0 += 8) {
+      double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      for (int i = lane; i < m.n_roots; i += 32) {
+        const double w = wts[i];
+        if (w == 0.0) continue;
+        const double *d = m.root_dlogprob + (size_t)i * m.n_ret;
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+          if (k0 + j < m.n_ret) acc[j] += w * d[k0 + j];
       }
-      __syncthreads();
-      for (int i = tid; i < m.n_roots; i += blockDim.x) wts[i] = (i == s_arg) ? 1.0 : 0.0;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const double v = warp_sum(acc[j]);
+        if (lane == 0 && k0 + j < m.n_ret) m.dret_part[(size_t)part * m.n_ret + k0 + j] = v;
+      }
     }
-    __syncthreads();
-    const double lp = s_logl;
-    total += lp;
-    if (tid == 0) m.out[2 + part] = lp;
-    for (int sl = tid; sl < m.n_slots; sl += blockDim.x) {
-      double s = 0.0;
-      for (int q = slot_begin[sl]; q < slot_begin[sl + 1]; ++q) s += wts[slot_roots[q]];
-      m.seeds[(size_t)sl * m.n_parts + part] = s;
-    }
-    for (int k = tid; k < m.n_ret; k += blockDim.x) {
-      double s = 0.0;
-      for (int i = 0; i < m.n_roots; ++i) s += wts[i] * m.root_dlogprob[(size_t)i * m.n_ret + k];
-      m.out[2 + m.n_parts + k] += s;
-    }
-    __syncthreads();
   }
-  if (tid == 0) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double total = 0.0;
+    for (int p = 0; p < m.n_parts; ++p) total += m.out[2 + p];
+    for (int k = 0; k < m.n_ret; ++k) {
+      double sum = 0.0;
+      for (int p = 0; p < m.n_parts; ++p) sum += m.dret_part[(size_t)p * m.n_ret + k];
+      m.out[2 + m.n_parts + k] = sum;
+    }
     m.out[0] = total;
     m.out[1] = (isfinite(total) ? 0.0 : 1.0);
   }

@@ -83,7 +83,8 @@ struct MixParams {
   const double *root_logprob;     // [n_roots]
   const double *root_dlogprob;    // [n_roots][n_ret]
   double *seeds;                  // [n_slots][n_parts]
-  double *weights;                // [n_roots] scratch: tree posterior weights
+  double *weights;                // [n_parts][n_roots] scratch: tree posterior weights
+  double *dret_part;              // [n_parts][n_ret] scratch: per-partition d logL / d p_k
   const int32_t *slot_begin;      // [n_slots+1] CSR: roots whose tree root is a slot
   const int32_t *slot_roots;      // [n_roots]
   double *out;                    // [2 + n_parts + n_ret]: total, status, part logl, dret

@@ -128,7 +128,7 @@ struct netlk_ctx {
   int64_t dev_bytes = 0;
   DevBuf d_clv, d_scaler, d_adj, d_msg_slots, d_tips, d_weights, d_unit_part, d_fwd, d_bwd, d_rfwd, d_ifwd;
   DevBuf d_pmat64, d_pmat32, d_lambda, d_U, d_Uinv, d_rates, d_rw, d_freqs, d_Q, d_brlen;
-  DevBuf d_site_partial, d_tree_logl, d_root_slot, d_root_lp, d_root_dlp, d_seeds, d_wts;
+  DevBuf d_site_partial, d_tree_logl, d_root_slot, d_root_lp, d_root_dlp, d_seeds, d_wts, d_dret;
   DevBuf d_slot_begin, d_slot_roots, d_parts, d_out, d_grad_partial, d_grad, d_edge_begin, d_edge_entries, d_op_sum;
   PinnedBuf h_brlen, h_root_lp, h_root_dlp, h_out, h_grad, h_tree, h_ifwd;
   cudaGraphExec_t graph_logl = nullptr, graph_grad = nullptr, graph_partials = nullptr,
@@ -180,7 +180,7 @@ struct netlk_ctx {
     for (DevBuf *b : {&d_clv, &d_scaler, &d_adj, &d_msg_slots, &d_tips, &d_weights, &d_unit_part, &d_fwd, &d_bwd, &d_rfwd, &d_ifwd,
                       &d_pmat64, &d_pmat32, &d_lambda, &d_U, &d_Uinv, &d_rates, &d_rw, &d_freqs, &d_Q,
                       &d_brlen, &d_site_partial, &d_tree_logl, &d_root_slot, &d_root_lp, &d_root_dlp,
-                      &d_seeds, &d_wts, &d_slot_begin, &d_slot_roots, &d_parts, &d_out, &d_grad_partial, &d_grad,
+                      &d_seeds, &d_wts, &d_dret, &d_slot_begin, &d_slot_roots, &d_parts, &d_out, &d_grad_partial, &d_grad,
                       &d_edge_begin, &d_edge_entries, &d_op_sum})
       b->free();
     if (stream) cudaStreamDestroy(stream);
@@ -234,6 +234,7 @@ struct netlk_ctx {
     m.root_dlogprob = d_root_dlp.as<double>();
     m.seeds = d_seeds.as<double>();
     m.weights = d_wts.as<double>();
+    m.dret_part = d_dret.as<double>();
     m.slot_begin = d_slot_begin.as<int32_t>();
     m.slot_roots = d_slot_roots.as<int32_t>();
     m.out = d_out.as<double>();
@@ -548,7 +549,8 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
   d_root_lp.alloc(dag.roots.size() * 8, dev_bytes);
   d_root_dlp.alloc(dag.roots.size() * std::max(1, topo.n_ret) * 8, dev_bytes);
   d_seeds.alloc((size_t)n_slots * P * 8, dev_bytes);
-  d_wts.alloc(dag.roots.size() * 8, dev_bytes);
+  d_wts.alloc((size_t)P * dag.roots.size() * 8, dev_bytes);
+  d_dret.alloc((size_t)P * std::max(1, topo.n_ret) * 8, dev_bytes);
   d_slot_begin.alloc(slot_begin.size() * 4, dev_bytes);
   d_slot_roots.alloc(slot_roots.size() * 4, dev_bytes);
   d_parts.alloc(P * sizeof(DevPartition), dev_bytes);
