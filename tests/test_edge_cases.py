@@ -110,3 +110,26 @@ def test_ten_reticulations():
     rng = np.random.default_rng(5)
     text = synth.random_network_newick(rng, 14, 10)
     _check(text, _parts(rng, 14, [20]))
+
+
+@pytest.mark.parametrize("states,rate_cats", [(4, 1), (4, 2), (4, 8), (20, 1), (20, 2)])
+def test_rate_category_counts(states, rate_cats):
+    """Rate-category counts other than 4 (DNA 1/2/8, protein 1/2; the
+    CUDA-core sweeps) against the oracle, with a finite gradient."""
+    from netrax_gb300.likelihood import NetworkLikelihood
+    from oracle import improved, newick, pllmath
+    rng = np.random.default_rng(10 + states + rate_cats)
+    text = synth.random_network_newick(rng, 10, 2)
+    n = 60
+    codes = (1 << rng.integers(0, states, size=(10, n))).astype(np.uint32)
+    freqs = rng.dirichlet(np.ones(states))
+    exch = rng.gamma(1.0, 1.0, size=states * (states - 1) // 2) + 1e-3
+    part = synth.PartitionData(codes, np.ones(n), freqs, exch, 0.6, n, rate_cats=rate_cats, states=states)
+    opart = improved.Partition(codes, np.ones(n), freqs, exch, pllmath.gamma_rates_mean(0.6, rate_cats))
+    want = improved.ImprovedOracle(newick.parse_newick(text), [opart], variant="AVERAGE").loglikelihood()
+    net = parse_extended_newick(text)
+    for prec, tol in (("fp64", FP64_REL), ("fp32", FP32_REL)):
+        with NetworkLikelihood(net, [part], precision=prec) as lik:
+            got, gb, gr = lik.loglikelihood_gradient()
+            assert got == pytest.approx(want, rel=tol)
+            assert np.all(np.isfinite(gb)) and np.all(np.isfinite(gr))
