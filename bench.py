@@ -352,7 +352,7 @@ def run_netlk(args, ws, rank, local):
             "dtype": "f32" if args.precision == "fp32" else "f64", "data": "synthetic",
             "config": {"workload": w.name, "taxa": w.network.n_tips, "reticulations": w.network.n_reticulations,
                        "sites": w.n_sites, "patterns": w.n_patterns, "partitions": len(w.partitions),
-                       "model": "GTR+G4" if lik.states == 4 else "20-state GTR (LG-like)+G4",
+                       "substitution_model": "GTR+G4" if lik.states == 4 else "20-state GTR (LG-like)+G4",
                        "variant": args.variant, "precision": args.precision,
                        "displayed_trees": lik.n_roots, "dag_variants": st["n_variants"],
                        "site_clv_updates_per_eval": st["site_clv_updates"],
