@@ -257,15 +257,17 @@ __global__ void __launch_bounds__(THREADS, MINB) backward_kernel(const SweepPara
   const int lane = threadIdx.x & 31;
   const int r = lane % R;
   const int pl = lane / R;
+  // a warp covers UPU base units (kPPLBase patterns per lane each)
+  constexpr int UPU = PPL / kPPLBase;
   const int unit = blockIdx.x * WPB + (threadIdx.x >> 5);
-  if (unit >= p.n_units) return;  // whole warp
+  if (unit >= p.n_units / UPU) return;  // whole warp
   real *sP = sPw[threadIdx.x >> 5];
   real *sQ = sQw[threadIdx.x >> 5];
   real *sF = sQ + 16, *sRW = sQ + 20, *sRate = sQ + 20 + R;
   const int opi = op_begin + blockIdx.y;
   const BwdOp op = load_bwd_op(p.bwd_ops, opi);
   const bool fake = op.b == INT32_MIN;
-  const int part = p.unit_part[unit];
+  const int part = p.unit_part[unit * UPU];
   const size_t N = (size_t)p.n_patterns;
   const size_t g0 = (size_t)unit * UNIT + pl;
   const size_t lane_off = g0 * (R * 4) + r * 4;
@@ -382,9 +384,13 @@ __global__ void __launch_bounds__(THREADS, MINB) backward_kernel(const SweepPara
   ga = warp_sum(ga * sRate[r]);
   gb = warp_sum(gb * sRate[r]);
   if (lane == 0) {
-    // per-warp edge terms, reduced in a fixed order by op_reduce_kernel
-    p.grad_partial[((size_t)opi * p.n_units + unit) * 2] = (double)ga;
-    p.grad_partial[((size_t)opi * p.n_units + unit) * 2 + 1] = (double)gb;
+    // per-warp edge terms in the warp's first base unit (zeros in the
+    // others), reduced in a fixed order by op_reduce_kernel
+    double *gp = p.grad_partial + ((size_t)opi * p.n_units + (size_t)unit * UPU) * 2;
+    gp[0] = (double)ga;
+    gp[1] = (double)gb;
+#pragma unroll
+    for (int k = 2; k < 2 * UPU; ++k) gp[k] = 0.0;
   }
 }
 
@@ -573,13 +579,18 @@ __global__ void edge_reduce_kernel(int n_edges, const int32_t *__restrict__ edge
 // Launch shapes (threads per block, minimum resident blocks per SM) the
 // autotuner chooses from. Shape 0 is the default and exists for every
 // precision and rate count; the FP32 4-rate path (DNA GTR+G4) carries all.
+// Shapes 5-7 and 10-11 give the adjoint four patterns per lane (two base
+// units per warp) and shapes 8-9 eight, which amortises an op's decode and P staging
+// over more patterns at the cost of registers (occupancy).
 struct Shape {
-  int threads, minb;
+  int threads, minb, adjoint_ppl;
 };
-constexpr Shape kShapes[] = {{256, 4}, {128, 8}, {256, 3}, {128, 6}, {64, 12}};
+constexpr Shape kShapes[] = {{256, 4, 2}, {128, 8, 2}, {256, 3, 2}, {128, 6, 2}, {64, 12, 2},
+                             {256, 2, 4}, {128, 4, 4}, {64, 8, 4},  {128, 2, 8}, {64, 4, 8},
+                             {32, 16, 4}, {64, 6, 4}};
 constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
 
-template <typename real, int R, int T, int M>
+template <typename real, int R, int T, int M, int BPPL>
 struct FwdRun {
   static int run(cudaStream_t s, const SweepParams &p, const int32_t *level_begin, int n_levels) {
     const int bx = (p.n_units_fwd + T / 32 - 1) / (T / 32);
@@ -590,46 +601,54 @@ struct FwdRun {
     return 0;
   }
 };
-template <typename real, int R, int T, int M>
+template <typename real, int R, int T, int M, int BPPL>
 struct BwdRun {
   static int run(cudaStream_t s, const SweepParams &p, const int32_t *level_begin, int n_levels) {
-    const int bx = (p.n_units + T / 32 - 1) / (T / 32);
+    const int warps = p.n_units / (BPPL / kPPLBase);
+    const int bx = (warps + T / 32 - 1) / (T / 32);
     for (int L = 0; L < n_levels; ++L) {
       const int n = level_begin[L + 1] - level_begin[L];
-      if (n > 0) backward_kernel<real, R, T, M, kPPLBase><<<dim3(bx, n), T, 0, s>>>(p, level_begin[L]);
+      if (n > 0) backward_kernel<real, R, T, M, BPPL><<<dim3(bx, n), T, 0, s>>>(p, level_begin[L]);
     }
     return 0;
   }
 };
-template <typename real, int R, int T, int M>
+template <typename real, int R, int T, int M, int BPPL>
 struct ThreadsRun {
   static int run() { return T; }
 };
 
 // Calls F<real, R, threads, minb>::run for a runtime (precision, R, shape).
-template <template <typename, int, int, int> class F, class... A>
+template <template <typename, int, int, int, int> class F, class... A>
 int dispatch(int precision, int R, int shape, A &&...a) {
   if (precision == 1 && R == 4) {
     switch (shape) {
-      case 1: return F<float, 4, 128, 8>::run(a...);
-      case 2: return F<float, 4, 256, 3>::run(a...);
-      case 3: return F<float, 4, 128, 6>::run(a...);
-      case 4: return F<float, 4, 64, 12>::run(a...);
-      default: return F<float, 4, 256, 4>::run(a...);
+      case 1: return F<float, 4, 128, 8, 2>::run(a...);
+      case 2: return F<float, 4, 256, 3, 2>::run(a...);
+      case 3: return F<float, 4, 128, 6, 2>::run(a...);
+      case 4: return F<float, 4, 64, 12, 2>::run(a...);
+      case 5: return F<float, 4, 256, 2, 4>::run(a...);
+      case 6: return F<float, 4, 128, 4, 4>::run(a...);
+      case 7: return F<float, 4, 64, 8, 4>::run(a...);
+      case 8: return F<float, 4, 128, 2, 8>::run(a...);
+      case 9: return F<float, 4, 64, 4, 8>::run(a...);
+      case 10: return F<float, 4, 32, 16, 4>::run(a...);
+      case 11: return F<float, 4, 64, 6, 4>::run(a...);
+      default: return F<float, 4, 256, 4, 2>::run(a...);
     }
   }
   if (precision == 1) {
     switch (R) {
-      case 1: return F<float, 1, 256, 4>::run(a...);
-      case 2: return F<float, 2, 256, 4>::run(a...);
-      default: return F<float, 8, 256, 4>::run(a...);
+      case 1: return F<float, 1, 256, 4, 2>::run(a...);
+      case 2: return F<float, 2, 256, 4, 2>::run(a...);
+      default: return F<float, 8, 256, 4, 2>::run(a...);
     }
   }
   switch (R) {
-    case 1: return F<double, 1, 256, 2>::run(a...);
-    case 2: return F<double, 2, 256, 2>::run(a...);
-    case 4: return F<double, 4, 256, 2>::run(a...);
-    default: return F<double, 8, 256, 2>::run(a...);
+    case 1: return F<double, 1, 256, 2, 2>::run(a...);
+    case 2: return F<double, 2, 256, 2, 2>::run(a...);
+    case 4: return F<double, 4, 256, 2, 2>::run(a...);
+    default: return F<double, 8, 256, 2, 2>::run(a...);
   }
 }
 

@@ -445,3 +445,24 @@ def test_incremental_matches_full(kind):
         inc.set_branch_lengths(b)
         full.set_branch_lengths(b)
         assert inc.loglikelihood() == full.loglikelihood()
+
+
+def test_adjoint_launch_shapes_agree(monkeypatch):
+    """Every launch shape of the DNA FP32 sweeps (the adjoint with two or four
+    patterns per lane) gives the same logL and, up to FP32 summation order,
+    the same gradient."""
+    from netrax_gb300 import synth
+    from netrax_gb300.likelihood import NetworkLikelihood
+    w = synth.config(1, scale=0.02)
+    res = {}
+    for shapes in ("0,0", "0,5", "0,6", "5,2", "6,4", "7,7", "8,8", "9,9", "10,10", "11,11"):
+        monkeypatch.setenv("NETLK_SHAPES", shapes)
+        with NetworkLikelihood(w.network, w.partitions, precision="fp32") as lik:
+            res[shapes] = lik.loglikelihood_gradient()  # the first evaluation fixes the shapes
+            tun = lik.tuning()
+            assert (tun["forward_shape"], tun["backward_shape"]) == tuple(int(x) for x in shapes.split(","))
+    t0, g0, r0 = res["0,0"]
+    for k, (t, g, r) in res.items():
+        assert t == t0
+        assert np.allclose(g, g0, rtol=1e-5, atol=1e-6 * max(1.0, np.abs(g0).max()))
+        assert np.allclose(r, r0, rtol=1e-5, atol=1e-6)
