@@ -180,8 +180,10 @@ __global__ void __launch_bounds__(THREADS, MINB) forward_kernel(const SweepParam
   const int lane = threadIdx.x & 31;
   const int r = lane % R;
   const int pl = lane / R;
+  // a warp covers UFW forward units (kPPLForward patterns per lane each)
+  constexpr int UFW = PPL / kPPLForward;
   const int unit = blockIdx.x * WPB + (threadIdx.x >> 5);
-  if (unit >= p.n_units_fwd) return;  // whole warp
+  if (unit >= p.n_units_fwd / UFW) return;  // whole warp
   real *sP = sPw[threadIdx.x >> 5];
   const FwdOp op = load_fwd_op(p.fwd_ops, op_begin + blockIdx.y);
   const int part = p.unit_part[unit * (PPL / kPPLBase)];
@@ -234,7 +236,12 @@ __global__ void __launch_bounds__(THREADS, MINB) forward_kernel(const SweepParam
       }
     }
     ll = warp_sum(ll);
-    if (lane == 0) p.site_partial[(size_t)op.slot * p.n_units_fwd + unit] = ll;
+    if (lane == 0) {  // the warp's first forward unit carries its sum, the others zero
+      double *sp = p.site_partial + (size_t)op.slot * p.n_units_fwd + (size_t)unit * UFW;
+      sp[0] = ll;
+#pragma unroll
+      for (int k = 1; k < UFW; ++k) sp[k] = 0.0;
+    }
   }
 }
 
@@ -580,28 +587,30 @@ __global__ void edge_reduce_kernel(int n_edges, const int32_t *__restrict__ edge
 // autotuner chooses from. Shape 0 is the default and exists for every
 // precision and rate count; the FP32 4-rate path (DNA GTR+G4) carries all.
 // Shapes 5-7 and 10-11 give the adjoint four patterns per lane (two base
-// units per warp) and shapes 8-9 eight, which amortises an op's decode and P staging
+// units per warp) and shapes 8-9 eight (the forward sweep keeps four: eight
+// measured slower on the DNA workloads), which amortises an op's decode and P staging
 // over more patterns at the cost of registers (occupancy).
 struct Shape {
-  int threads, minb, adjoint_ppl;
+  int threads, minb, forward_ppl, adjoint_ppl;
 };
-constexpr Shape kShapes[] = {{256, 4, 2}, {128, 8, 2}, {256, 3, 2}, {128, 6, 2}, {64, 12, 2},
-                             {256, 2, 4}, {128, 4, 4}, {64, 8, 4},  {128, 2, 8}, {64, 4, 8},
-                             {32, 16, 4}, {64, 6, 4}};
+constexpr Shape kShapes[] = {{256, 4, 4, 2}, {128, 8, 4, 2}, {256, 3, 4, 2}, {128, 6, 4, 2}, {64, 12, 4, 2},
+                             {256, 2, 4, 4}, {128, 4, 4, 4}, {64, 8, 4, 4},  {128, 2, 4, 8}, {64, 4, 4, 8},
+                             {32, 16, 4, 4}, {64, 6, 4, 4}};
 constexpr int kNumShapes = sizeof(kShapes) / sizeof(kShapes[0]);
 
-template <typename real, int R, int T, int M, int BPPL>
+template <typename real, int R, int T, int M, int FPPL, int BPPL>
 struct FwdRun {
   static int run(cudaStream_t s, const SweepParams &p, const int32_t *level_begin, int n_levels) {
-    const int bx = (p.n_units_fwd + T / 32 - 1) / (T / 32);
+    const int warps = p.n_units_fwd / (FPPL / kPPLForward);
+    const int bx = (warps + T / 32 - 1) / (T / 32);
     for (int L = 0; L < n_levels; ++L) {
       const int n = level_begin[L + 1] - level_begin[L];
-      if (n > 0) forward_kernel<real, R, T, M, kPPLForward><<<dim3(bx, n), T, 0, s>>>(p, level_begin[L]);
+      if (n > 0) forward_kernel<real, R, T, M, FPPL><<<dim3(bx, n), T, 0, s>>>(p, level_begin[L]);
     }
     return 0;
   }
 };
-template <typename real, int R, int T, int M, int BPPL>
+template <typename real, int R, int T, int M, int FPPL, int BPPL>
 struct BwdRun {
   static int run(cudaStream_t s, const SweepParams &p, const int32_t *level_begin, int n_levels) {
     const int warps = p.n_units / (BPPL / kPPLBase);
@@ -613,42 +622,42 @@ struct BwdRun {
     return 0;
   }
 };
-template <typename real, int R, int T, int M, int BPPL>
+template <typename real, int R, int T, int M, int FPPL, int BPPL>
 struct ThreadsRun {
   static int run() { return T; }
 };
 
 // Calls F<real, R, threads, minb>::run for a runtime (precision, R, shape).
-template <template <typename, int, int, int, int> class F, class... A>
+template <template <typename, int, int, int, int, int> class F, class... A>
 int dispatch(int precision, int R, int shape, A &&...a) {
   if (precision == 1 && R == 4) {
     switch (shape) {
-      case 1: return F<float, 4, 128, 8, 2>::run(a...);
-      case 2: return F<float, 4, 256, 3, 2>::run(a...);
-      case 3: return F<float, 4, 128, 6, 2>::run(a...);
-      case 4: return F<float, 4, 64, 12, 2>::run(a...);
-      case 5: return F<float, 4, 256, 2, 4>::run(a...);
-      case 6: return F<float, 4, 128, 4, 4>::run(a...);
-      case 7: return F<float, 4, 64, 8, 4>::run(a...);
-      case 8: return F<float, 4, 128, 2, 8>::run(a...);
-      case 9: return F<float, 4, 64, 4, 8>::run(a...);
-      case 10: return F<float, 4, 32, 16, 4>::run(a...);
-      case 11: return F<float, 4, 64, 6, 4>::run(a...);
-      default: return F<float, 4, 256, 4, 2>::run(a...);
+      case 1: return F<float, 4, 128, 8, 4, 2>::run(a...);
+      case 2: return F<float, 4, 256, 3, 4, 2>::run(a...);
+      case 3: return F<float, 4, 128, 6, 4, 2>::run(a...);
+      case 4: return F<float, 4, 64, 12, 4, 2>::run(a...);
+      case 5: return F<float, 4, 256, 2, 4, 4>::run(a...);
+      case 6: return F<float, 4, 128, 4, 4, 4>::run(a...);
+      case 7: return F<float, 4, 64, 8, 4, 4>::run(a...);
+      case 8: return F<float, 4, 128, 2, 4, 8>::run(a...);
+      case 9: return F<float, 4, 64, 4, 4, 8>::run(a...);
+      case 10: return F<float, 4, 32, 16, 4, 4>::run(a...);
+      case 11: return F<float, 4, 64, 6, 4, 4>::run(a...);
+      default: return F<float, 4, 256, 4, 4, 2>::run(a...);
     }
   }
   if (precision == 1) {
     switch (R) {
-      case 1: return F<float, 1, 256, 4, 2>::run(a...);
-      case 2: return F<float, 2, 256, 4, 2>::run(a...);
-      default: return F<float, 8, 256, 4, 2>::run(a...);
+      case 1: return F<float, 1, 256, 4, 4, 2>::run(a...);
+      case 2: return F<float, 2, 256, 4, 4, 2>::run(a...);
+      default: return F<float, 8, 256, 4, 4, 2>::run(a...);
     }
   }
   switch (R) {
-    case 1: return F<double, 1, 256, 2, 2>::run(a...);
-    case 2: return F<double, 2, 256, 2, 2>::run(a...);
-    case 4: return F<double, 4, 256, 2, 2>::run(a...);
-    default: return F<double, 8, 256, 2, 2>::run(a...);
+    case 1: return F<double, 1, 256, 2, 4, 2>::run(a...);
+    case 2: return F<double, 2, 256, 2, 4, 2>::run(a...);
+    case 4: return F<double, 4, 256, 2, 4, 2>::run(a...);
+    default: return F<double, 8, 256, 2, 4, 2>::run(a...);
   }
 }
 
