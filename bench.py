@@ -157,7 +157,7 @@ class ClockSampler:
 # dram__bytes_write.sum of one evaluation's 16 level launches, same network at
 # 0.3 of its sites, scaled by updates; writes still dirty in L2 at a launch's
 # end are not counted).
-TRAFFIC_PER_UPDATE = {"forward_fp32_4": 101.2, "backward_fp32_4": 297.5}
+TRAFFIC_PER_UPDATE = {"forward_fp32_4": 102.5, "backward_fp32_4": 295.9}
 
 
 def cpu_port_rate(w, n_sample, steps, warmup, variant):
