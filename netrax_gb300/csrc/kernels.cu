@@ -347,7 +347,12 @@ __global__ void __launch_bounds__(THREADS, MINB) backward_kernel(const SweepPara
       for (int i = 0; i < 4; ++i) pb[k][i] = 1;
   }
   real ua[PPL][4], ub[PPL][4];
-  real ga = 0, gb = 0;
+  // edge terms per base unit (patterns k < kPPLBase of the lane in unit 0,
+  // the next kPPLBase in unit 1, ...): every launch shape sums them in the
+  // same order, so the gradient does not depend on the shape
+  real ga[UPU], gb[UPU];
+#pragma unroll
+  for (int u = 0; u < UPU; ++u) ga[u] = gb[u] = 0;
 #pragma unroll
   for (int k = 0; k < PPL; ++k) {
     const int sh = sx[k] - sa[k] - sb[k];
@@ -367,10 +372,10 @@ __global__ void __launch_bounds__(THREADS, MINB) backward_kernel(const SweepPara
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const real qa = sQ[4 * i] * pa[k][0] + sQ[4 * i + 1] * pa[k][1] + sQ[4 * i + 2] * pa[k][2] + sQ[4 * i + 3] * pa[k][3];
-      ga += ua[k][i] * qa;
+      ga[k / kPPLBase] += ua[k][i] * qa;
       if (!fake) {
         const real qb = sQ[4 * i] * pb[k][0] + sQ[4 * i + 1] * pb[k][1] + sQ[4 * i + 2] * pb[k][2] + sQ[4 * i + 3] * pb[k][3];
-        gb += ub[k][i] * qb;
+        gb[k / kPPLBase] += ub[k][i] * qb;
       }
     }
   }
@@ -388,16 +393,16 @@ __global__ void __launch_bounds__(THREADS, MINB) backward_kernel(const SweepPara
 #pragma unroll
     for (int k = 0; k < PPL; ++k) Vec<real>::store(d + (size_t)k * PPW * (R * 4), nb[k]);
   }
-  ga = warp_sum(ga * sRate[r]);
-  gb = warp_sum(gb * sRate[r]);
-  if (lane == 0) {
-    // per-warp edge terms in the warp's first base unit (zeros in the
-    // others), reduced in a fixed order by op_reduce_kernel
-    double *gp = p.grad_partial + ((size_t)opi * p.n_units + (size_t)unit * UPU) * 2;
-    gp[0] = (double)ga;
-    gp[1] = (double)gb;
+  double *gp = p.grad_partial + ((size_t)opi * p.n_units + (size_t)unit * UPU) * 2;
 #pragma unroll
-    for (int k = 2; k < 2 * UPU; ++k) gp[k] = 0.0;
+  for (int u = 0; u < UPU; ++u) {
+    // per-unit edge terms, reduced in a fixed order by op_reduce_kernel
+    const real sa_ = warp_sum(ga[u] * sRate[r]);
+    const real sb_ = warp_sum(gb[u] * sRate[r]);
+    if (lane == 0) {
+      gp[2 * u] = (double)sa_;
+      gp[2 * u + 1] = (double)sb_;
+    }
   }
 }
 
@@ -589,7 +594,8 @@ __global__ void edge_reduce_kernel(int n_edges, const int32_t *__restrict__ edge
 // Shapes 5-7 and 10-11 give the adjoint four patterns per lane (two base
 // units per warp) and shapes 8-9 eight (the forward sweep keeps four: eight
 // measured slower on the DNA workloads), which amortises an op's decode and P staging
-// over more patterns at the cost of registers (occupancy).
+// over more patterns at the cost of registers (occupancy); their edge terms
+// are still summed per 16-pattern unit, so every shape gives the same bits.
 struct Shape {
   int threads, minb, forward_ppl, adjoint_ppl;
 };
