@@ -393,15 +393,24 @@ __global__ void __launch_bounds__(THREADS, MINB) backward_kernel(const SweepPara
 #pragma unroll
     for (int k = 0; k < PPL; ++k) Vec<real>::store(d + (size_t)k * PPW * (R * 4), nb[k]);
   }
-  double *gp = p.grad_partial + ((size_t)opi * p.n_units + (size_t)unit * UPU) * 2;
-#pragma unroll
-  for (int u = 0; u < UPU; ++u) {
-    // per-unit edge terms, reduced in a fixed order by op_reduce_kernel
-    const real sa_ = warp_sum(ga[u] * sRate[r]);
-    const real sb_ = warp_sum(gb[u] * sRate[r]);
+  // per-unit edge terms, reduced in a fixed order by op_reduce_kernel
+  if constexpr (UPU == 1) {
+    const real sa_ = warp_sum(ga[0] * sRate[r]);
+    const real sb_ = warp_sum(gb[0] * sRate[r]);
     if (lane == 0) {
-      gp[2 * u] = (double)sa_;
-      gp[2 * u + 1] = (double)sb_;
+      p.grad_partial[((size_t)opi * p.n_units + unit) * 2] = (double)sa_;
+      p.grad_partial[((size_t)opi * p.n_units + unit) * 2 + 1] = (double)sb_;
+    }
+  } else {
+    double *gp = p.grad_partial + ((size_t)opi * p.n_units + (size_t)unit * UPU) * 2;
+#pragma unroll
+    for (int u = 0; u < UPU; ++u) {
+      const real sa_ = warp_sum(ga[u] * sRate[r]);
+      const real sb_ = warp_sum(gb[u] * sRate[r]);
+      if (lane == 0) {
+        gp[2 * u] = (double)sa_;
+        gp[2 * u + 1] = (double)sb_;
+      }
     }
   }
 }
