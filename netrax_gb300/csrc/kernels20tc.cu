@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(kTThreads, 1)
   const int item_begin = (int)(W * blockIdx.x / gridDim.x), item_end = (int)(W * (blockIdx.x + 1) / gridDim.x);
 
   if (warp == 0) tc::tmem_alloc(tc::smem_u32(tmem_slot), 512);
-  if (threadIdx.x == 0) tc::mbar_init(tc::smem_u32(mbar), 1);
+  if (threadIdx.x == 0) tc::mbar_init(tc::smem_u32(mbar), 2);
   // zero slab 20 of every A tile (rate 3's last K step reads it) and all of B
   for (int i = threadIdx.x; i < 4 * kTM; i += kTThreads)
     *reinterpret_cast<float4 *>(sA + (i / kTM) * kABytes + 20 * kAChunk + (i % kTM) * 16) = make_float4(0, 0, 0, 0);
@@ -205,12 +205,14 @@ __global__ void __launch_bounds__(kTThreads, 1)
     put(kb, xb, sA + 2 * kABytes, sA + 3 * kABytes);
     tc::fence_proxy_async();
     __syncthreads();
-    if (threadIdx.x == 0) {
+    // child c's MMAs are issued by thread 32c (one per warp of warps 0-1):
+    // their accumulators are disjoint, and each issuer commits its own
+    // MMAs to the mbarrier (two arrivals per item)
+    if ((threadIdx.x & 31) == 0 && threadIdx.x < 64) {
+      const int c = threadIdx.x >> 5;
+      const int kind = c ? kb : ka;
       tc::fence_after_sync();
-#pragma unroll 1
-      for (int c = 0; c < 2; ++c) {
-        const int kind = c ? kb : ka;
-        if (kind == kAbsent) continue;
+      if (kind != kAbsent) {
         // descriptors of the tiles' first slabs; a K step adds its byte offset / 16
         const uint64_t dah = tc::smem_desc(tc::smem_u32(sA + (2 * c) * kABytes), kAChunk, 128);
         const uint64_t dal = dah + (kABytes >> 4);
@@ -227,7 +229,7 @@ __global__ void __launch_bounds__(kTThreads, 1)
           }
         }
       }
-      tc::commit(tc::smem_u32(mbar));
+      tc::commit(tc::smem_u32(mbar));  // arrives at once when this thread issued nothing
     }
     // the current item's op, for the epilogue; then prefetch the next item
     const FwdOp cur = op;
