@@ -65,20 +65,8 @@ __device__ __forceinline__ void load_child(const SweepParams &p, int32_t ref, si
   }
 }
 
-// out[k] = P . c[k] for the lane's patterns (P: this lane's rate, row-major 4x4)
-template <typename real, int PPL>
-__device__ __forceinline__ void matvec2(const real *P, const real (&c)[PPL][4], real (&out)[PPL][4]) {
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    real row[4];
-    Vec<real>::ldg(P + 4 * i, row);
-#pragma unroll
-    for (int k = 0; k < PPL; ++k)
-      out[k][i] = row[0] * c[k][0] + row[1] * c[k][1] + row[2] * c[k][2] + row[3] * c[k][3];
-  }
-}
-
-// Same products with P read from shared memory.
+// out[k] = P . c[k] for the lane's patterns, P (this lane's rate, row-major
+// 4x4) read from shared memory.
 template <typename real, int PPL>
 __device__ __forceinline__ void matvec2_s(const real *P, const real (&c)[PPL][4], real (&out)[PPL][4]) {
 #pragma unroll
@@ -91,6 +79,7 @@ __device__ __forceinline__ void matvec2_s(const real *P, const real (&c)[PPL][4]
   }
 }
 
+// out[k] = P^T . u[k], P from shared memory.
 template <typename real, int PPL>
 __device__ __forceinline__ void matvec2_ts(const real *P, const real (&u)[PPL][4], real (&out)[PPL][4]) {
 #pragma unroll
@@ -107,27 +96,6 @@ __device__ __forceinline__ void matvec2_ts(const real *P, const real (&u)[PPL][4
       for (int j = 0; j < 4; ++j) out[k][j] += row[j] * u[k][i];
   }
 }
-
-// out[k] = P^T . u[k]
-template <typename real, int PPL>
-__device__ __forceinline__ void matvec2_t(const real *P, const real (&u)[PPL][4], real (&out)[PPL][4]) {
-#pragma unroll
-  for (int k = 0; k < PPL; ++k)
-#pragma unroll
-    for (int j = 0; j < 4; ++j) out[k][j] = 0;
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    real row[4];
-    Vec<real>::ldg(P + 4 * i, row);
-#pragma unroll
-    for (int k = 0; k < PPL; ++k)
-#pragma unroll
-      for (int j = 0; j < 4; ++j) out[k][j] += row[j] * u[k][i];
-  }
-}
-
-
-
 
 // P rows of one rate sit kPRow values apart in shared memory (16 used +
 // padding) so the four rate groups of a warp's LDS.128 hit distinct banks.
