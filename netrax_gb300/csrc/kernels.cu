@@ -188,25 +188,21 @@ __global__ void __launch_bounds__(THREADS, MINB) forward_kernel(const SweepParam
   }
   if (op.slot >= 0) {
     // pll_compute_root_loglikelihood for the lane's sites, summed over the warp
-    const real rw = (real)p.rate_weights[part * R + r];
+    const real rw = model_val<real>(p.rate_weights, p.rate_weights32, part * R + r);
     real freq[4];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) freq[i] = (real)p.freqs[part * 4 + i];
-    double ll = 0.0;
+    for (int i = 0; i < 4; ++i) freq[i] = model_val<real>(p.freqs, p.freqs32, part * 4 + i);
+    SiteSum<real> ll;
 #pragma unroll
     for (int k = 0; k < PPL; ++k) {
       real t = rw * (freq[0] * v[k][0] + freq[1] * v[k][1] + freq[2] * v[k][2] + freq[3] * v[k][3]);
       t = rate_sum<R>(t);
-      const double w = p.weights[g0 + (size_t)k * PPW];
-      if (r == 0 && w != 0.0) {
-        const double lt = (sizeof(real) == 4) ? (double)logf((float)t) : log((double)t);
-        ll += w * (lt + (double)s[k] * Scale<real>::kLogUnit);
-      }
+      if (r == 0) ll.add(p, g0 + (size_t)k * PPW, t, s[k]);
     }
-    ll = warp_sum(ll);
-    if (lane == 0) {  // the warp's first forward unit carries its sum, the others zero
-      double *sp = p.site_partial + (size_t)op.slot * p.n_units_fwd + (size_t)unit * UFW;
-      sp[0] = ll;
+    // the warp's first forward unit carries its sum, the others zero
+    double *sp = p.site_partial + (size_t)op.slot * p.n_units_fwd + (size_t)unit * UFW;
+    ll.store(sp, lane);
+    if (lane == 0) {
 #pragma unroll
       for (int k = 1; k < UFW; ++k) sp[k] = 0.0;
     }
@@ -277,11 +273,11 @@ __global__ void __launch_bounds__(THREADS, MINB) backward_kernel(const SweepPara
       for (int k = 0; k < PPL; ++k) Vec<real>::load(cxp + (size_t)k * PPW * (R * 4), cx[k]);
     }
   }
-  if (lane < 16) sQ[lane] = (real)p.Q[part * 16 + lane];
-  if (lane < 4) sF[lane] = (real)p.freqs[part * 4 + lane];
+  if (lane < 16) sQ[lane] = model_val<real>(p.Q, p.Q32, part * 16 + lane);
+  if (lane < 4) sF[lane] = model_val<real>(p.freqs, p.freqs32, part * 4 + lane);
   if (lane < R) {
-    sRW[lane] = (real)p.rate_weights[part * R + lane];
-    sRate[lane] = (real)p.rates[part * R + lane];
+    sRW[lane] = model_val<real>(p.rate_weights, p.rate_weights32, part * R + lane);
+    sRate[lane] = model_val<real>(p.rates, p.rates32, part * R + lane);
   }
   stage_pmats_warp<real, R>(sP, static_cast<const real *>(p.pmat) + (size_t)part * p.n_edges * (R * 16), op.ea,
                             fake ? -1 : op.eb, lane);  // its __syncwarp also publishes sQ
@@ -289,12 +285,12 @@ __global__ void __launch_bounds__(THREADS, MINB) backward_kernel(const SweepPara
   const real rw = sRW[r];
   if (op.seed >= 0) {
     // d(w_s log L_s)/d clv_x = w_s rw_r pi_i / L_s, times the tree weight
-    const real sd = (real)p.seeds[(size_t)op.seed * p.n_parts + part];
+    const real sd = model_val<real>(p.seeds, p.seeds32, (size_t)op.seed * p.n_parts + part);
 #pragma unroll
     for (int k = 0; k < PPL; ++k) {
       real t = rw * (sF[0] * cx[k][0] + sF[1] * cx[k][1] + sF[2] * cx[k][2] + sF[3] * cx[k][3]);
       t = rate_sum<R>(t);
-      const real sw = sd * (real)p.weights[g0 + (size_t)k * PPW];
+      const real sw = sd * pattern_weight<real>(p, g0 + (size_t)k * PPW);
       if (t > (real)0 && sw != (real)0) {
         const real f = sw * rw / t;
 #pragma unroll
@@ -365,20 +361,14 @@ __global__ void __launch_bounds__(THREADS, MINB) backward_kernel(const SweepPara
   if constexpr (UPU == 1) {
     const real sa_ = warp_sum(ga[0] * sRate[r]);
     const real sb_ = warp_sum(gb[0] * sRate[r]);
-    if (lane == 0) {
-      p.grad_partial[((size_t)opi * p.n_units + unit) * 2] = (double)sa_;
-      p.grad_partial[((size_t)opi * p.n_units + unit) * 2 + 1] = (double)sb_;
-    }
+    if (lane == 0) store_edge_terms<real>(p.grad_partial + ((size_t)opi * p.n_units + unit) * 2, sa_, sb_);
   } else {
     double *gp = p.grad_partial + ((size_t)opi * p.n_units + (size_t)unit * UPU) * 2;
 #pragma unroll
     for (int u = 0; u < UPU; ++u) {
       const real sa_ = warp_sum(ga[u] * sRate[r]);
       const real sb_ = warp_sum(gb[u] * sRate[r]);
-      if (lane == 0) {
-        gp[2 * u] = (double)sa_;
-        gp[2 * u + 1] = (double)sb_;
-      }
+      if (lane == 0) store_edge_terms<real>(gp + 2 * u, sa_, sb_);
     }
   }
 }
@@ -419,9 +409,10 @@ __global__ void tree_reduce_kernel(const MixParams m) {
   const int slot = blockIdx.x, part = blockIdx.y;
   const int ub = m.parts[part].unit_begin, ue = m.parts[part].unit_end;
   const double *src = m.site_partial + (size_t)slot * m.n_units;
+  const float2 *src32 = reinterpret_cast<const float2 *>(src);
   double s = 0.0, c = 0.0;
   for (int u = ub + threadIdx.x; u < ue; u += blockDim.x) {
-    const double y = src[u] - c;
+    const double y = (m.ff ? ff_to_double(src32[u]) : src[u]) - c;
     const double t = s + y;
     c = (t - s) - y;
     s = t;
@@ -492,6 +483,7 @@ __global__ void mix_kernel(const MixParams m) {
       double sum = 0.0;
       for (int q = m.slot_begin[sl]; q < m.slot_begin[sl + 1]; ++q) sum += wts[m.slot_roots[q]];
       m.seeds[(size_t)sl * m.n_parts + part] = sum;
+      if (m.seeds32) m.seeds32[(size_t)sl * m.n_parts + part] = (float)sum;
     }
     // d logL_p / d p_k = sum_T w_T d log P(T) / d p_k, 8 reticulations per pass
     for (int k0 = 0; k0 < m.n_ret; k0 += 8) {
@@ -529,15 +521,24 @@ __global__ void mix_kernel(const MixParams m) {
 // partials of its launch (grid_partial[op][b][side]) -> op_sum[op][side];
 // then per edge e, the op sides that use it (CSR edge_entries[edge_begin[e] ..
 // edge_begin[e+1]) = op * 2 + side) -> d logL / d t_e.
-__global__ void op_reduce_kernel(int n_bx, const double *__restrict__ partial, double *__restrict__ op_sum) {
+// ff: each partial is a pair of float pairs (FP32 sweeps), else two doubles.
+__global__ void op_reduce_kernel(int n_bx, const double *__restrict__ partial, double *__restrict__ op_sum,
+                                 int ff) {
   const int op = blockIdx.x;
   __shared__ double ra[128], rb[128];
   const double2 *src = reinterpret_cast<const double2 *>(partial) + (size_t)op * n_bx;
+  const float4 *src32 = reinterpret_cast<const float4 *>(src);
   double a = 0.0, b = 0.0;
   for (int i = threadIdx.x; i < n_bx; i += blockDim.x) {
-    const double2 v = src[i];
-    a += v.x;
-    b += v.y;
+    if (ff) {
+      const float4 v = src32[i];
+      a += ff_to_double(make_float2(v.x, v.y));
+      b += ff_to_double(make_float2(v.z, v.w));
+    } else {
+      const double2 v = src[i];
+      a += v.x;
+      b += v.y;
+    }
   }
   ra[threadIdx.x] = a;
   rb[threadIdx.x] = b;
@@ -683,8 +684,9 @@ void launch_mix(cudaStream_t s, const MixParams &m) {
 }
 
 void launch_grad_reduce(cudaStream_t s, int n_ops, int n_edges, int n_bx, const int32_t *edge_begin,
-                        const int32_t *edge_entries, const double *partial, double *op_sum, double *grad) {
-  op_reduce_kernel<<<n_ops, 128, 0, s>>>(n_bx, partial, op_sum);
+                        const int32_t *edge_entries, const double *partial, double *op_sum, double *grad,
+                        bool ff) {
+  op_reduce_kernel<<<n_ops, 128, 0, s>>>(n_bx, partial, op_sum, ff ? 1 : 0);
   edge_reduce_kernel<<<(n_edges + 127) / 128, 128, 0, s>>>(n_edges, edge_begin, edge_entries, op_sum, grad);
   g_launches += 2;
 }

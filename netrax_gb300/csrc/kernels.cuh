@@ -63,10 +63,21 @@ struct SweepParams {
   const double *rate_weights;   // [n_parts][R]
   const double *rates;          // [n_parts][R]
   const double *Q;              // [n_parts][S*S]
+  // FP32 sweeps read float copies instead (GB300's FP64 pipe is a small
+  // fraction of its FP32 one, so the FP32 kernels issue no FP64 instruction):
+  const float2 *weights32;      // [N] (hi, lo): hi + lo == the double weight to ~2^-48
+  const float *freqs32;         // [n_parts][S]
+  const float *rate_weights32;  // [n_parts][R]
+  const float *rates32;         // [n_parts][R]
+  const float *Q32;             // [n_parts][S*S]
+  const float *seeds32;         // [n_slots][n_parts]
   void *clv;                    // [V][N][R][S] real
   int32_t *scaler;              // [V][N]
   void *msg;                    // [M][N][R][4] real adjoint messages
   const int32_t *msg_slots;     // message slots read by the adjoint ops
+  // site_partial and grad_partial hold doubles in FP64 contexts and, in FP32
+  // contexts, float pairs (hi, lo) in the same 8 bytes whose exact sum is the
+  // value (see ff_to_double)
   double *site_partial;         // [n_slots][n_units_fwd]
   const double *seeds;          // [n_slots][n_parts]
   double *grad_partial;         // [n_bwd_ops][n_units][2] per-warp edge terms (a, b)
@@ -75,6 +86,7 @@ struct SweepParams {
 
 struct MixParams {
   int32_t n_slots, n_parts, n_roots, n_ret, variant, n_units;  // n_units: forward units
+  int32_t ff;                     // 1: site_partial holds float pairs (FP32 sweeps)
   double min_logprob;
   const DevPartition *parts;      // [n_parts]
   const double *site_partial;     // [n_slots][n_units] (forward units)
@@ -83,6 +95,7 @@ struct MixParams {
   const double *root_logprob;     // [n_roots]
   const double *root_dlogprob;    // [n_roots][n_ret]
   double *seeds;                  // [n_slots][n_parts]
+  float *seeds32;                 // [n_slots][n_parts] float copy for the FP32 sweeps (or null)
   double *weights;                // [n_parts][n_roots] scratch: tree posterior weights
   double *dret_part;              // [n_parts][n_ret] scratch: per-partition d logL / d p_k
   const int32_t *slot_begin;      // [n_slots+1] CSR: roots whose tree root is a slot
@@ -104,8 +117,10 @@ void launch_backward(cudaStream_t s, int precision, int R, int shape, const Swee
                      const int32_t *level_begin, int n_levels);
 void launch_tree_reduce(cudaStream_t s, const MixParams &m);
 void launch_mix(cudaStream_t s, const MixParams &m);
+// ff: the partials are float pairs (FP32 sweeps) rather than doubles.
 void launch_grad_reduce(cudaStream_t s, int n_ops, int n_edges, int n_bx, const int32_t *edge_begin,
-                        const int32_t *edge_entries, const double *partial, double *op_sum, double *grad);
+                        const int32_t *edge_entries, const double *partial, double *op_sum, double *grad,
+                        bool ff);
 // 20-state forward (backward = false) or adjoint sweep, one launch per level.
 void launch_sweep20(cudaStream_t s, int precision, int R, bool backward, const SweepParams &p,
                     const int32_t *level_begin, int n_levels);

@@ -178,8 +178,8 @@ __global__ void __launch_bounds__(kWarps20 * 32) forward20_kernel(const SweepPar
   if (unit >= p.n_units_fwd) return;  // whole warp, after the only barrier
   const size_t N = (size_t)p.n_patterns;
   const real *Pa = sP + r * ST, *Pb = sP + (R + r) * ST;
-  const real rw = (real)p.rate_weights[part * R + r];
-  double ll = 0.0;
+  const real rw = model_val<real>(p.rate_weights, p.rate_weights32, part * R + r);
+  SiteSum<real> ll;
   for (int pass = 0; pass < kPPLForward; ++pass) {
     const size_t g = (size_t)unit * UNIT + pass * PPW + pl;
     real ca[S20], v[S20];
@@ -205,19 +205,12 @@ __global__ void __launch_bounds__(kWarps20 * 32) forward20_kernel(const SweepPar
     if (op.slot >= 0) {
       real t = 0;
 #pragma unroll
-      for (int i = 0; i < S20; ++i) t += (real)p.freqs[part * S20 + i] * v[i];
+      for (int i = 0; i < S20; ++i) t += model_val<real>(p.freqs, p.freqs32, part * S20 + i) * v[i];
       t = rate_sum<R>(rw * t);
-      const double w = p.weights[g];
-      if (r == 0 && w != 0.0) {
-        const double lt = (sizeof(real) == 4) ? (double)logf((float)t) : log((double)t);
-        ll += w * (lt + (double)s * Scale<real>::kLogUnit);
-      }
+      if (r == 0) ll.add(p, g, t, s);
     }
   }
-  if (op.slot >= 0) {
-    ll = warp_sum(ll);
-    if (lane == 0) p.site_partial[(size_t)op.slot * p.n_units_fwd + unit] = ll;
-  }
+  if (op.slot >= 0) ll.store(p.site_partial + (size_t)op.slot * p.n_units_fwd + unit, lane);
 }
 
 // One side of an adjoint op: u = 2^sh adj_x * other (the sibling's projected
@@ -261,16 +254,16 @@ __global__ void __launch_bounds__(kWarps20 * 32) backward20_kernel(const SweepPa
   const int unit0 = blockIdx.x * kWarps20;
   const int part = p.unit_part[unit0];
   stage_p20<real, R>(p, sP, part, op.ea, fake ? -1 : op.eb);
-  for (int i = threadIdx.x; i < 400; i += blockDim.x) sQ[i] = (real)p.Q[part * 400 + i];
-  if (threadIdx.x < S20) sF[threadIdx.x] = (real)p.freqs[part * S20 + threadIdx.x];
+  for (int i = threadIdx.x; i < 400; i += blockDim.x) sQ[i] = model_val<real>(p.Q, p.Q32, part * 400 + i);
+  if (threadIdx.x < S20) sF[threadIdx.x] = model_val<real>(p.freqs, p.freqs32, part * S20 + threadIdx.x);
   __syncthreads();
   const int lane = threadIdx.x & 31, r = lane % R, pl = lane / R;
   const int unit = unit0 + (threadIdx.x >> 5);
   if (unit >= p.n_units) return;  // whole warp, after the only barrier
   const size_t N = (size_t)p.n_patterns;
   const real *Pa = sP + r * ST, *Pb = sP + (R + r) * ST;
-  const real rw = (real)p.rate_weights[part * R + r];
-  const real rate = (real)p.rates[part * R + r];
+  const real rw = model_val<real>(p.rate_weights, p.rate_weights32, part * R + r);
+  const real rate = model_val<real>(p.rates, p.rates32, part * R + r);
   real *msg = static_cast<real *>(p.msg);
   real ga = 0, gb = 0;
   for (int pass = 0; pass < kPPLBase; ++pass) {
@@ -291,7 +284,8 @@ __global__ void __launch_bounds__(kWarps20 * 32) backward20_kernel(const SweepPa
 #pragma unroll
       for (int i = 0; i < S20; ++i) t += sF[i] * cx[i];
       t = rate_sum<R>(rw * t);
-      const real sw = (real)p.seeds[(size_t)op.seed * p.n_parts + part] * (real)p.weights[g];
+      const real sw = model_val<real>(p.seeds, p.seeds32, (size_t)op.seed * p.n_parts + part) *
+                      pattern_weight<real>(p, g);
       if (t > (real)0 && sw != (real)0) {
         const real f = sw * rw / t;
 #pragma unroll
@@ -320,10 +314,7 @@ __global__ void __launch_bounds__(kWarps20 * 32) backward20_kernel(const SweepPa
   }
   ga = warp_sum(ga * rate);
   gb = warp_sum(gb * rate);
-  if (lane == 0) {
-    p.grad_partial[((size_t)opi * p.n_units + unit) * 2] = (double)ga;
-    p.grad_partial[((size_t)opi * p.n_units + unit) * 2 + 1] = (double)gb;
-  }
+  if (lane == 0) store_edge_terms<real>(p.grad_partial + ((size_t)opi * p.n_units + unit) * 2, ga, gb);
 }
 
 template <typename real, int R>

@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(kTThreads, 1)
     const size_t g = g0 + m;
     const int sab = (cka == kInner ? p.scaler[(size_t)cur.a * N + g] : 0) +
                     (ckb == kInner ? p.scaler[(size_t)cur.b * N + g] : 0);
-    const double wg = p.weights[g];
+    const float2 wg = p.weights32[g];
     if (item + 1 < item_end) {
       const int noi = (item + 1) / n_tiles;
       if (noi != oi) {
@@ -305,17 +305,15 @@ __global__ void __launch_bounds__(kTThreads, 1)
       for (int rr = 0; rr < 2; ++rr) {
         float u = 0.f;
 #pragma unroll
-        for (int i = 0; i < 20; ++i) u += (float)p.freqs[part * 20 + i] * v[rr][i];
-        t += (float)p.rate_weights[part * 4 + 2 * h + rr] * u;
+        for (int i = 0; i < 20; ++i) u += p.freqs32[part * 20 + i] * v[rr][i];
+        t += p.rate_weights32[part * 4 + 2 * h + rr] * u;
       }
       s_t[h * kTM + m] = t;
       __syncthreads();
       if (h == 0) {
-        t = s_t[m] + s_t[kTM + m];
-        double ll = 0.0;
-        if (wg != 0.0) ll = wg * ((double)logf(t) + (double)sc * Scale<float>::kLogUnit);
-        ll = warp_sum(ll);
-        if (lane == 0) p.site_partial[(size_t)cur.slot * p.n_units_fwd + g0 / 32 + q] = ll;
+        SiteSum<float> ll;
+        ll.add_w(wg, s_t[m] + s_t[kTM + m], sc);
+        ll.store(p.site_partial + (size_t)cur.slot * p.n_units_fwd + g0 / 32 + q, lane);
       }
     }
     tc::fence_before_sync();
@@ -380,10 +378,9 @@ __device__ __forceinline__ void stage_b_adj(const SweepParams &p, unsigned char 
     const int f = threadIdx.x + u * kTThreads, c = f / 400, e = c ? eb : ea;
     if (f < 800 && e >= 0) v[u] = __ldg(pm + (size_t)e * 400 + (f - c * 400));
   }
-  if (with_q && threadIdx.x < 100) {  // Q[i][4 j4 .. 4 j4 + 3], FP64 -> FP32
+  if (with_q && threadIdx.x < 100) {  // Q[i][4 j4 .. 4 j4 + 3]
     const int i = threadIdx.x / 5, j4 = threadIdx.x - i * 5;
-    const double *q = p.Q + (size_t)part * 400 + i * 20 + 4 * j4;
-    const float4 x = make_float4((float)q[0], (float)q[1], (float)q[2], (float)q[3]);
+    const float4 x = __ldg(reinterpret_cast<const float4 *>(p.Q32 + (size_t)part * 400 + i * 20 + 4 * j4));
     float4 hi, lo;
     split4(x, hi, lo);
     unsigned char *base = sBQ + j4 * kBChunk + (i & 7) * 16;
@@ -518,13 +515,13 @@ __global__ void __launch_bounds__(kTThreads, 1)
       for (int l = 0; l < 2; ++l) {
         float u = 0.f;
 #pragma unroll
-        for (int i = 0; i < 20; ++i) u += (float)p.freqs[part * 20 + i] * cx[20 * l + i];
-        part_t += (float)p.rate_weights[part * 4 + 2 * hh + l] * u;
+        for (int i = 0; i < 20; ++i) u += p.freqs32[part * 20 + i] * cx[20 * l + i];
+        part_t += p.rate_weights32[part * 4 + 2 * hh + l] * u;
       }
       s_t[hh * kTM + m] = part_t;
       __syncthreads();
       tseed = s_t[m] + s_t[kTM + m];
-      sw = (float)p.seeds[(size_t)op.seed * p.n_parts + part] * (float)p.weights[g];
+      sw = p.seeds32[(size_t)op.seed * p.n_parts + part] * p.weights32[g].x;
     }
     float ga = 0.f, gb = 0.f;
     for (int h = 0; h < 2; ++h) {
@@ -578,9 +575,9 @@ __global__ void __launch_bounds__(kTThreads, 1)
         }
       }
       if (op.seed >= 0 && tseed > 0.f && sw != 0.f) {
-        const float f = sw * (float)p.rate_weights[part * 4 + r] / tseed;
+        const float f = sw * p.rate_weights32[part * 4 + r] / tseed;
 #pragma unroll
-        for (int i = 0; i < 20; ++i) ax[i] += f * (float)p.freqs[part * 20 + i];
+        for (int i = 0; i < 20; ++i) ax[i] += f * p.freqs32[part * 20 + i];
       }
       bool ok = tc::mbar_wait(tc::smem_u32(mbar), phase);
       phase ^= 1;
@@ -642,7 +639,7 @@ __global__ void __launch_bounds__(kTThreads, 1)
       }
       tc::fence_after_sync();
       // ----------------------------------------------------------- epilogue 2
-      const float rate = (float)p.rates[part * 4 + r];
+      const float rate = p.rates32[part * 4 + r];
 #pragma unroll
       for (int c = 0; c < 2; ++c) {
         if ((c ? kb : ka) == kAbsent) continue;
@@ -684,17 +681,18 @@ __global__ void __launch_bounds__(kTThreads, 1)
     s_gb[hh * kTM + m] = gb;
     __syncthreads();
     if (hh == 0) {
-      double va = (double)s_ga[m] + (double)s_ga[kTM + m];
-      double vb = (double)s_gb[m] + (double)s_gb[kTM + m];
+      // float-float sums over the unit's 16 lanes (no FP64 instruction)
+      FF va = two_sum(s_ga[m], s_ga[kTM + m]);
+      FF vb = two_sum(s_gb[m], s_gb[kTM + m]);
 #pragma unroll
       for (int o = 8; o > 0; o >>= 1) {
-        va += __shfl_xor_sync(0xffffffffu, va, o);
-        vb += __shfl_xor_sync(0xffffffffu, vb, o);
+        va = ff_add(va, FF{__shfl_xor_sync(0xffffffffu, va.hi, o), __shfl_xor_sync(0xffffffffu, va.lo, o)});
+        vb = ff_add(vb, FF{__shfl_xor_sync(0xffffffffu, vb.hi, o), __shfl_xor_sync(0xffffffffu, vb.lo, o)});
       }
       if ((lane & 15) == 0) {
         const size_t unit = g0 / 16 + (size_t)(m >> 4);
-        p.grad_partial[((size_t)opi * p.n_units + unit) * 2] = va;
-        p.grad_partial[((size_t)opi * p.n_units + unit) * 2 + 1] = vb;
+        *reinterpret_cast<float4 *>(p.grad_partial + ((size_t)opi * p.n_units + unit) * 2) =
+            make_float4(va.hi, va.lo, vb.hi, vb.lo);
       }
     }
     tc::fence_before_sync();

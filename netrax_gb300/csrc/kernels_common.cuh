@@ -126,5 +126,126 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
+// ------------------------------------------------- float-float arithmetic
+// A value is the unevaluated sum hi + lo of two floats (about 48 significant
+// bits). Error-free transforms: TwoSum (Knuth, TAOCP vol. 2, 4.2.2) and the
+// FMA product error (a*b - fl(a*b) is exact in one fma). The FP32 sweeps use
+// it for their per-site log-likelihood sums, so they issue no FP64
+// instruction: GB300 runs FP64 at a small fraction of its FP32 rate.
+struct FF {
+  float hi, lo;
+};
+
+__device__ __forceinline__ FF two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return FF{s, (a - (s - bb)) + (b - bb)};
+}
+
+// requires |a| >= |b| (or a == 0)
+__device__ __forceinline__ FF quick_two_sum(float a, float b) {
+  const float s = a + b;
+  return FF{s, b - (s - a)};
+}
+
+__device__ __forceinline__ FF ff_add(FF x, FF y) {
+  const FF s = two_sum(x.hi, y.hi);
+  return quick_two_sum(s.hi, s.lo + (x.lo + y.lo));
+}
+
+__device__ __forceinline__ FF ff_mul(FF x, FF y) {
+  const float p = x.hi * y.hi;
+  const float e = __fmaf_rn(x.hi, y.hi, -p);
+  return quick_two_sum(p, e + (x.hi * y.lo + x.lo * y.hi));
+}
+
+__device__ __forceinline__ FF warp_sum_ff(FF v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const FF t{__shfl_xor_sync(kFull, v.hi, o), __shfl_xor_sync(kFull, v.lo, o)};
+    v = ff_add(v, t);
+  }
+  return v;
+}
+
+// The double a float pair stands for (hi + lo rounded once).
+__host__ __device__ __forceinline__ double ff_to_double(float2 v) { return (double)v.x + (double)v.y; }
+
+// Sum over a warp's sites of w_s (log t_s + k_s log unit): the root
+// log-likelihood of pll_compute_root_loglikelihood for the sites a warp
+// covers. add() is called by the lane that owns a site; store() by the whole
+// warp, lane 0 writing the 8-byte result: a double in FP64 sweeps, a float
+// pair in FP32 ones. A zero-weight site (padding) adds nothing; a site whose
+// likelihood is 0 makes the sum -inf, as in double arithmetic.
+template <typename real>
+struct SiteSum;
+
+template <>
+struct SiteSum<double> {
+  double ll = 0.0;
+  __device__ __forceinline__ void add(const SweepParams &p, size_t g, double t, int k) {
+    const double w = p.weights[g];
+    if (w != 0.0) ll += w * (log(t) + (double)k * Scale<double>::kLogUnit);
+  }
+  __device__ __forceinline__ void store(double *dst, int lane) {
+    ll = warp_sum(ll);
+    if (lane == 0) *dst = ll;
+  }
+};
+
+template <>
+struct SiteSum<float> {
+  static constexpr float kUnitHi = (float)Scale<float>::kLogUnit;
+  static constexpr float kUnitLo = (float)(Scale<float>::kLogUnit - (double)kUnitHi);
+  FF ll{0.f, 0.f};
+  float bad = 0.f;  // sum of the non-finite terms (-inf or NaN), kept apart
+  __device__ __forceinline__ void add(const SweepParams &p, size_t g, float t, int k) { add_w(p.weights32[g], t, k); }
+  __device__ __forceinline__ void add_w(float2 w, float t, int k) {
+    if (w.x == 0.f) return;
+    const float lt = logf(t);
+    if (!isfinite(lt)) {
+      bad += w.x * lt;
+      return;
+    }
+    const float kf = (float)k;  // exact: |k| < 2^24
+    const float ph = kf * kUnitHi;
+    const FF ku = quick_two_sum(ph, __fmaf_rn(kf, kUnitHi, -ph) + kf * kUnitLo);
+    const FF y = ff_add(ku, FF{lt, 0.f});
+    ll = ff_add(ll, ff_mul(FF{w.x, w.y}, y));
+  }
+  __device__ __forceinline__ void store(double *dst, int lane) {
+    ll = warp_sum_ff(ll);
+    bad = warp_sum(bad);
+    if (lane == 0) *reinterpret_cast<float2 *>(dst) = bad != 0.f ? make_float2(bad, 0.f) : make_float2(ll.hi, ll.lo);
+  }
+};
+
+// A model value as the sweep's arithmetic type: the float copy in FP32
+// sweeps, the double itself in FP64 ones.
+template <typename real>
+__device__ __forceinline__ real model_val(const double *d, const float *f, size_t i) {
+  if constexpr (sizeof(real) == 4) return f[i];
+  else return d[i];
+}
+
+// A pattern's weight as the sweep's arithmetic type.
+template <typename real>
+__device__ __forceinline__ real pattern_weight(const SweepParams &p, size_t g) {
+  if constexpr (sizeof(real) == 4) return p.weights32[g].x;
+  else return p.weights[g];
+}
+
+// Writes one (a, b) pair of edge terms: two doubles, or two float pairs
+// (value, 0) in FP32 sweeps.
+template <typename real>
+__device__ __forceinline__ void store_edge_terms(double *dst, real a, real b) {
+  if constexpr (sizeof(real) == 4) {
+    *reinterpret_cast<float4 *>(dst) = make_float4(a, 0.f, b, 0.f);
+  } else {
+    dst[0] = a;
+    dst[1] = b;
+  }
+}
+
 }  // namespace
 }  // namespace netlk

@@ -128,6 +128,9 @@ struct netlk_ctx {
   int64_t dev_bytes = 0;
   DevBuf d_clv, d_scaler, d_adj, d_msg_slots, d_tips, d_weights, d_unit_part, d_fwd, d_bwd, d_rfwd, d_ifwd;
   DevBuf d_pmat64, d_pmat32, d_lambda, d_U, d_Uinv, d_rates, d_rw, d_freqs, d_Q, d_brlen;
+  // FP32 contexts: float copies the sweeps read (weights as hi/lo pairs)
+  DevBuf d_weights32, d_model32, d_seeds32;
+  size_t m32_freqs = 0, m32_rw = 0, m32_rates = 0;  // offsets (floats) in d_model32; Q at 0
   DevBuf d_site_partial, d_tree_logl, d_root_slot, d_root_lp, d_root_dlp, d_seeds, d_wts, d_dret;
   DevBuf d_slot_begin, d_slot_roots, d_parts, d_out, d_grad_partial, d_grad, d_edge_begin, d_edge_entries, d_op_sum;
   PinnedBuf h_brlen, h_root_lp, h_root_dlp, h_out, h_grad, h_tree, h_ifwd;
@@ -181,7 +184,7 @@ struct netlk_ctx {
                       &d_pmat64, &d_pmat32, &d_lambda, &d_U, &d_Uinv, &d_rates, &d_rw, &d_freqs, &d_Q,
                       &d_brlen, &d_site_partial, &d_tree_logl, &d_root_slot, &d_root_lp, &d_root_dlp,
                       &d_seeds, &d_wts, &d_dret, &d_slot_begin, &d_slot_roots, &d_parts, &d_out, &d_grad_partial, &d_grad,
-                      &d_edge_begin, &d_edge_entries, &d_op_sum})
+                      &d_edge_begin, &d_edge_entries, &d_op_sum, &d_weights32, &d_model32, &d_seeds32})
       b->free();
     if (stream) cudaStreamDestroy(stream);
   }
@@ -206,6 +209,15 @@ struct netlk_ctx {
     p.rate_weights = d_rw.as<double>();
     p.rates = d_rates.as<double>();
     p.Q = d_Q.as<double>();
+    if (opts.precision == NETLK_FP32) {
+      const float *m32 = d_model32.as<float>();
+      p.weights32 = d_weights32.as<float2>();
+      p.Q32 = m32;
+      p.freqs32 = m32 + m32_freqs;
+      p.rate_weights32 = m32 + m32_rw;
+      p.rates32 = m32 + m32_rates;
+      p.seeds32 = d_seeds32.as<float>();
+    }
     p.clv = d_clv.p;
     p.scaler = d_scaler.as<int32_t>();
     p.msg = d_adj.p;
@@ -233,6 +245,8 @@ struct netlk_ctx {
     m.root_logprob = d_root_lp.as<double>();
     m.root_dlogprob = d_root_dlp.as<double>();
     m.seeds = d_seeds.as<double>();
+    m.ff = opts.precision == NETLK_FP32 ? 1 : 0;
+    m.seeds32 = opts.precision == NETLK_FP32 ? d_seeds32.as<float>() : nullptr;
     m.weights = d_wts.as<double>();
     m.dret_part = d_dret.as<double>();
     m.slot_begin = d_slot_begin.as<int32_t>();
@@ -549,6 +563,15 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
   d_root_lp.alloc(dag.roots.size() * 8, dev_bytes);
   d_root_dlp.alloc(dag.roots.size() * std::max(1, topo.n_ret) * 8, dev_bytes);
   d_seeds.alloc((size_t)n_slots * P * 8, dev_bytes);
+  if (opts.precision == NETLK_FP32) {
+    auto up4 = [](size_t n) { return (n + 3) & ~(size_t)3; };  // 16-byte aligned sub-arrays
+    m32_freqs = up4((size_t)P * S * S);
+    m32_rw = m32_freqs + up4((size_t)P * S);
+    m32_rates = m32_rw + up4((size_t)P * R);
+    d_model32.alloc((m32_rates + up4((size_t)P * R)) * 4, dev_bytes);
+    d_weights32.alloc(N * 8, dev_bytes);
+    d_seeds32.alloc((size_t)n_slots * P * 4, dev_bytes);
+  }
   d_wts.alloc((size_t)P * dag.roots.size() * 8, dev_bytes);
   d_dret.alloc((size_t)P * std::max(1, topo.n_ret) * 8, dev_bytes);
   d_slot_begin.alloc(slot_begin.size() * 4, dev_bytes);
@@ -575,6 +598,16 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
   else
     CUDA_OK(cudaMemcpyAsync(d_tips.p, tips32.data(), tips32.size() * 4, cudaMemcpyHostToDevice, stream));
   CUDA_OK(cudaMemcpyAsync(d_weights.p, weights.data(), N * 8, cudaMemcpyHostToDevice, stream));
+  std::vector<float> w32;
+  if (opts.precision == NETLK_FP32) {
+    w32.resize(2 * (size_t)N);
+    for (int64_t g = 0; g < N; ++g) {
+      const float hi = (float)weights[g];
+      w32[2 * g] = hi;
+      w32[2 * g + 1] = (float)(weights[g] - (double)hi);
+    }
+    CUDA_OK(cudaMemcpyAsync(d_weights32.p, w32.data(), N * 8, cudaMemcpyHostToDevice, stream));
+  }
   CUDA_OK(cudaMemcpyAsync(d_unit_part.p, unit_part.data(), n_units * 4, cudaMemcpyHostToDevice, stream));
   CUDA_OK(cudaMemcpyAsync(d_fwd.p, fwd.data(), fwd.size() * sizeof(FwdOp), cudaMemcpyHostToDevice, stream));
   if (!rfwd.empty())
@@ -620,6 +653,15 @@ void netlk_ctx::upload_model() {
   CUDA_OK(cudaMemcpyAsync(d_rw.p, rw.data(), rw.size() * 8, cudaMemcpyHostToDevice, stream));
   CUDA_OK(cudaMemcpyAsync(d_freqs.p, fr.data(), fr.size() * 8, cudaMemcpyHostToDevice, stream));
   CUDA_OK(cudaMemcpyAsync(d_Q.p, Q.data(), Q.size() * 8, cudaMemcpyHostToDevice, stream));
+  std::vector<float> m32;
+  if (opts.precision == NETLK_FP32) {
+    m32.assign(d_model32.bytes / 4, 0.f);
+    for (size_t i = 0; i < Q.size(); ++i) m32[i] = (float)Q[i];
+    for (size_t i = 0; i < fr.size(); ++i) m32[m32_freqs + i] = (float)fr[i];
+    for (size_t i = 0; i < rw.size(); ++i) m32[m32_rw + i] = (float)rw[i];
+    for (size_t i = 0; i < rates.size(); ++i) m32[m32_rates + i] = (float)rates[i];
+    CUDA_OK(cudaMemcpyAsync(d_model32.p, m32.data(), m32.size() * 4, cudaMemcpyHostToDevice, stream));
+  }
   CUDA_OK(cudaStreamSynchronize(stream));
   model_dirty = false;
   clv_valid = false;
@@ -718,7 +760,7 @@ void netlk_ctx::enqueue(bool pm, bool fwd_on, bool reduce, bool mixk, bool bwd_o
     prof_mark(4);
     launch_grad_reduce(stream, (int)bwd.size(), topo.n_edges, n_units, d_edge_begin.as<int32_t>(),
                        d_edge_entries.as<int32_t>(), d_grad_partial.as<double>(), d_op_sum.as<double>(),
-                       d_grad.as<double>());
+                       d_grad.as<double>(), opts.precision == NETLK_FP32);
     prof_mark(5);
   }
 }
