@@ -18,6 +18,7 @@
 //   pll_compute_root_loglikelihood (src/likelihood/ImprovedLoglikelihood.cpp:450)
 //   pllmod_treeinfo_update_prob_matrices (src/likelihood/ImprovedLoglikelihood.cpp:661)
 //   AVERAGE / BEST mixing        (src/likelihood/ImprovedLoglikelihood.cpp:521-644)
+#include <algorithm>
 #include <cstdio>
 
 #include "kernels.cuh"
@@ -135,25 +136,18 @@ __device__ __forceinline__ void stage_pmats_warp(real *sP, const real *pm_part, 
 
 
 // ------------------------------------------------------------------ forward
-// One launch per DAG level: blockIdx.y picks the op of the level, each warp
-// one unit of patterns. CLV_out = (P[ea] . a) * (P[eb] . b), rescaled per
-// site; site log-likelihoods of displayed-tree root variants are summed over
-// the warp's patterns into site_partial[slot][unit].
-template <typename real, int R, int THREADS, int MINB, int PPL>
-__global__ void __launch_bounds__(THREADS, MINB) forward_kernel(const SweepParams p, int op_begin) {
+// One op for one warp's unit of patterns: CLV_out = (P[ea] . a) * (P[eb] . b),
+// rescaled per site; site log-likelihoods of displayed-tree root variants are
+// summed over the warp's patterns into site_partial[slot][unit]. sP: the
+// warp's shared-memory P staging slice.
+template <typename real, int R, int PPL>
+__device__ __forceinline__ void forward_op(const SweepParams &p, const FwdOp &op, int unit, real *sP, int lane) {
   constexpr int PPW = 32 / R;          // patterns per pass of the lane rows
   constexpr int UNIT = PPW * PPL;      // patterns per forward unit
-  constexpr int WPB = THREADS / 32;
-  __shared__ __align__(16) real sPw[WPB][2 * R * PLayout<real>::kRow];
-  const int lane = threadIdx.x & 31;
   const int r = lane % R;
   const int pl = lane / R;
   // a warp covers UFW forward units (kPPLForward patterns per lane each)
   constexpr int UFW = PPL / kPPLForward;
-  const int unit = blockIdx.x * WPB + (threadIdx.x >> 5);
-  if (unit >= p.n_units_fwd / UFW) return;  // whole warp
-  real *sP = sPw[threadIdx.x >> 5];
-  const FwdOp op = load_fwd_op(p.fwd_ops, op_begin + blockIdx.y);
   const int part = p.unit_part[unit * (PPL / kPPLBase)];
   const size_t N = (size_t)p.n_patterns;
   const size_t g0 = (size_t)unit * UNIT + pl;  // the lane's first pattern; the second is g0 + PPW
@@ -209,6 +203,36 @@ __global__ void __launch_bounds__(THREADS, MINB) forward_kernel(const SweepParam
   }
 }
 
+// One launch per DAG level: blockIdx.y picks the op of the level, each warp
+// one unit of patterns.
+template <typename real, int R, int THREADS, int MINB, int PPL>
+__global__ void __launch_bounds__(THREADS, MINB) forward_kernel(const SweepParams p, int op_begin) {
+  constexpr int WPB = THREADS / 32;
+  __shared__ __align__(16) real sPw[WPB][2 * R * PLayout<real>::kRow];
+  const int unit = blockIdx.x * WPB + (threadIdx.x >> 5);
+  if (unit >= p.n_units_fwd / (PPL / kPPLForward)) return;  // whole warp
+  forward_op<real, R, PPL>(p, load_fwd_op(p.fwd_ops, op_begin + blockIdx.y), unit, sPw[threadIdx.x >> 5],
+                           threadIdx.x & 31);
+}
+
+// The whole sweep in one launch: each warp walks every op of walk_fwd_ops
+// (a topological order chosen for cache locality) for its own unit. A lane
+// only reads values it wrote itself, so no warp waits for another; a child
+// CLV is read back soon after it was written, mostly from L2.
+template <typename real, int R, int THREADS, int MINB, int PPL>
+__global__ void __launch_bounds__(THREADS, MINB) forward_walk_kernel(const SweepParams p, int unit_begin, int unit_end) {
+  constexpr int WPB = THREADS / 32;
+  __shared__ __align__(16) real sPw[WPB][2 * R * PLayout<real>::kRow];
+  const int unit = unit_begin + blockIdx.x * WPB + (threadIdx.x >> 5);
+  if (unit >= unit_end) return;  // whole warp
+  real *sP = sPw[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  for (int i = 0; i < p.n_walk_fwd; ++i) {
+    __syncwarp();  // every lane is done with the previous op's P
+    forward_op<real, R, PPL>(p, load_fwd_op(p.walk_fwd_ops, i), unit, sP, lane);
+  }
+}
+
 // ------------------------------------------------------------------ adjoint
 // Reverse sweep as message passing, one launch per level (deepest first).
 // For op x with CLV_x = 2^k (Pa a) * (Pb b):
@@ -218,25 +242,20 @@ __global__ void __launch_bounds__(THREADS, MINB) forward_kernel(const SweepParam
 //   message to a = Pa^T u_a, message to b = Pb^T u_b
 // The two edge terms are summed over the block and written to
 // grad_partial[op][blockIdx.x][2] for a deterministic reduction per edge.
-template <typename real, int R, int THREADS, int MINB, int PPL>
-__global__ void __launch_bounds__(THREADS, MINB) backward_kernel(const SweepParams p, int op_begin) {
+// One adjoint op for one warp's unit. opi: the op's index in the level
+// schedule (its grad_partial row); msg_slots: the schedule's message slot list.
+// sP, sQ: the warp's shared-memory staging slices.
+template <typename real, int R, int PPL>
+__device__ __forceinline__ void backward_op(const SweepParams &p, const BwdOp &op, int opi,
+                                            const int32_t *__restrict__ msg_slots, int unit, real *sP, real *sQ,
+                                            int lane) {
   constexpr int PPW = 32 / R;
   constexpr int UNIT = PPW * PPL;      // patterns per adjoint unit
-  constexpr int WPB = THREADS / 32;
-  __shared__ __align__(16) real sPw[WPB][2 * R * PLayout<real>::kRow];
-  __shared__ real sQw[WPB][16 + 4 + 2 * R];
-  const int lane = threadIdx.x & 31;
   const int r = lane % R;
   const int pl = lane / R;
   // a warp covers UPU base units (kPPLBase patterns per lane each)
   constexpr int UPU = PPL / kPPLBase;
-  const int unit = blockIdx.x * WPB + (threadIdx.x >> 5);
-  if (unit >= p.n_units / UPU) return;  // whole warp
-  real *sP = sPw[threadIdx.x >> 5];
-  real *sQ = sQw[threadIdx.x >> 5];
   real *sF = sQ + 16, *sRW = sQ + 20, *sRate = sQ + 20 + R;
-  const int opi = op_begin + blockIdx.y;
-  const BwdOp op = load_bwd_op(p.bwd_ops, opi);
   const bool fake = op.b == INT32_MIN;
   const int part = p.unit_part[unit * UPU];
   const size_t N = (size_t)p.n_patterns;
@@ -258,7 +277,7 @@ __global__ void __launch_bounds__(THREADS, MINB) backward_kernel(const SweepPara
 #pragma unroll
     for (int k = 0; k < PPL; ++k) sx[k] = sxp[(size_t)k * PPW];
     for (int m = 0; m < op.msg_count; ++m) {
-      const real *src = msg + (size_t)__ldg(p.msg_slots + op.msg_begin + m) * N * (R * 4) + lane_off;
+      const real *src = msg + (size_t)__ldg(msg_slots + op.msg_begin + m) * N * (R * 4) + lane_off;
 #pragma unroll
       for (int k = 0; k < PPL; ++k) {
         real t[4];
@@ -370,6 +389,39 @@ __global__ void __launch_bounds__(THREADS, MINB) backward_kernel(const SweepPara
       const real sb_ = warp_sum(gb[u] * sRate[r]);
       if (lane == 0) store_edge_terms<real>(gp + 2 * u, sa_, sb_);
     }
+  }
+}
+
+// One launch per level (deepest first): blockIdx.y picks the op.
+template <typename real, int R, int THREADS, int MINB, int PPL>
+__global__ void __launch_bounds__(THREADS, MINB) backward_kernel(const SweepParams p, int op_begin) {
+  constexpr int WPB = THREADS / 32;
+  __shared__ __align__(16) real sPw[WPB][2 * R * PLayout<real>::kRow];
+  __shared__ real sQw[WPB][16 + 4 + 2 * R];
+  const int unit = blockIdx.x * WPB + (threadIdx.x >> 5);
+  if (unit >= p.n_units / (PPL / kPPLBase)) return;  // whole warp
+  const int opi = op_begin + blockIdx.y;
+  backward_op<real, R, PPL>(p, load_bwd_op(p.bwd_ops, opi), opi, p.msg_slots, unit, sPw[threadIdx.x >> 5],
+                            sQw[threadIdx.x >> 5], threadIdx.x & 31);
+}
+
+// The whole adjoint sweep in one launch: each warp walks walk_bwd_ops (the
+// reverse of the forward walk, with its own message slots) for its unit. An
+// op's level-schedule index (its grad_partial row) travels in pad0.
+template <typename real, int R, int THREADS, int MINB, int PPL>
+__global__ void __launch_bounds__(THREADS, MINB) backward_walk_kernel(const SweepParams p, int unit_begin,
+                                                                       int unit_end) {
+  constexpr int WPB = THREADS / 32;
+  __shared__ __align__(16) real sPw[WPB][2 * R * PLayout<real>::kRow];
+  __shared__ real sQw[WPB][16 + 4 + 2 * R];
+  const int unit = unit_begin + blockIdx.x * WPB + (threadIdx.x >> 5);
+  if (unit >= unit_end) return;  // whole warp
+  const int lane = threadIdx.x & 31;
+  for (int i = 0; i < p.n_walk_bwd; ++i) {
+    __syncwarp();  // every lane is done with the previous op's staged values
+    const BwdOp op = load_bwd_op(p.walk_bwd_ops, i);
+    backward_op<real, R, PPL>(p, op, op.pad0, p.walk_msg_slots, unit, sPw[threadIdx.x >> 5], sQw[threadIdx.x >> 5],
+                              lane);
   }
 }
 
@@ -606,6 +658,45 @@ struct BwdRun {
     return 0;
   }
 };
+// Walk sweeps run every op in one launch per warp, so a warp that starts in a
+// later wave than the others would run a whole sweep alone: the units are cut
+// into chunks of at most one wave (every warp resident) of nearly equal size,
+// one launch each.
+template <class K>
+int walk_chunks(K kernel, int threads, int warps) {
+  int dev = 0, sms = 1, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0);
+  const int wave = std::max(1, per_sm * sms * (threads / 32));
+  return std::max(1, (warps + wave - 1) / wave);
+}
+template <class K>
+int launch_walk_chunks(K kernel, int threads, int warps, cudaStream_t s, const SweepParams &p, bool count_only) {
+  const int wpb = threads / 32;
+  const int n_chunks = walk_chunks(kernel, threads, warps);
+  if (count_only) return n_chunks;
+  const int per = (warps + n_chunks - 1) / n_chunks;
+  for (int c = 0; c < n_chunks; ++c) {
+    const int b = c * per, e = std::min(warps, b + per);
+    kernel<<<(e - b + wpb - 1) / wpb, threads, 0, s>>>(p, b, e);
+  }
+  return n_chunks;
+}
+template <typename real, int R, int T, int M, int FPPL, int BPPL>
+struct FwdWalkRun {
+  static int run(cudaStream_t s, const SweepParams &p, bool count_only) {
+    return launch_walk_chunks(forward_walk_kernel<real, R, T, M, FPPL>, T, p.n_units_fwd / (FPPL / kPPLForward), s, p,
+                              count_only);
+  }
+};
+template <typename real, int R, int T, int M, int FPPL, int BPPL>
+struct BwdWalkRun {
+  static int run(cudaStream_t s, const SweepParams &p, bool count_only) {
+    return launch_walk_chunks(backward_walk_kernel<real, R, T, M, BPPL>, T, p.n_units / (BPPL / kPPLBase), s, p,
+                              count_only);
+  }
+};
 template <typename real, int R, int T, int M, int FPPL, int BPPL>
 struct ThreadsRun {
   static int run() { return T; }
@@ -645,20 +736,59 @@ int dispatch(int precision, int R, int shape, A &&...a) {
   }
 }
 
+// Walk shapes (one warp per block, so a chunk spreads evenly over the SMs):
+// {threads, minimum blocks per SM, forward and adjoint patterns per lane}.
+constexpr Shape kWalkShapes[] = {{32, 32, 4, 2}, {32, 24, 4, 2}, {32, 16, 4, 4}};
+constexpr int kNumWalkShapes = sizeof(kWalkShapes) / sizeof(kWalkShapes[0]);
+
+template <template <typename, int, int, int, int, int> class F, class... A>
+int dispatch_walk(int w, A &&...a) {
+  switch (w) {
+    case 1: return F<float, 4, 32, 24, 4, 2>::run(a...);
+    case 2: return F<float, 4, 32, 16, 4, 4>::run(a...);
+    default: return F<float, 4, 32, 32, 4, 2>::run(a...);
+  }
+}
+
 }  // namespace
 
-int num_shapes(int precision, int R) { return (precision == 1 && R == 4) ? kNumShapes : 1; }
+int num_level_shapes(int precision, int R) { return (precision == 1 && R == 4) ? kNumShapes : 1; }
+int num_shapes(int precision, int R) { return (precision == 1 && R == 4) ? kNumShapes + kNumWalkShapes : 1; }
 
-int shape_threads(int precision, int R, int shape) { return dispatch<ThreadsRun>(precision, R, shape); }
+int sweep_launches(int precision, int R, int shape, const SweepParams &p, bool backward, const int32_t *level_begin,
+                   int n_levels) {
+  const int nl = num_level_shapes(precision, R);
+  if (shape >= nl)
+    return backward ? dispatch_walk<BwdWalkRun>(shape - nl, cudaStream_t(nullptr), p, true)
+                    : dispatch_walk<FwdWalkRun>(shape - nl, cudaStream_t(nullptr), p, true);
+  int n = 0;
+  for (int L = 0; L < n_levels; ++L) n += level_begin[L + 1] > level_begin[L];
+  return n;
+}
+
+int shape_threads(int precision, int R, int shape) {
+  const int nl = num_level_shapes(precision, R);
+  return shape >= nl ? kWalkShapes[shape - nl].threads : dispatch<ThreadsRun>(precision, R, shape);
+}
 
 void launch_forward(cudaStream_t s, int precision, int R, int shape, const SweepParams &p,
                     const int32_t *level_begin, int n_levels) {
+  const int nl = num_level_shapes(precision, R);
+  if (shape >= nl) {
+    g_launches += dispatch_walk<FwdWalkRun>(shape - nl, s, p, false);
+    return;
+  }
   dispatch<FwdRun>(precision, R, shape, s, p, level_begin, n_levels);
   for (int L = 0; L < n_levels; ++L) g_launches += level_begin[L + 1] > level_begin[L];
 }
 
 void launch_backward(cudaStream_t s, int precision, int R, int shape, const SweepParams &p,
                      const int32_t *level_begin, int n_levels) {
+  const int nl = num_level_shapes(precision, R);
+  if (shape >= nl) {
+    g_launches += dispatch_walk<BwdWalkRun>(shape - nl, s, p, false);
+    return;
+  }
   dispatch<BwdRun>(precision, R, shape, s, p, level_begin, n_levels);
   for (int L = 0; L < n_levels; ++L) g_launches += level_begin[L + 1] > level_begin[L];
 }

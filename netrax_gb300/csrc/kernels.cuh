@@ -82,6 +82,13 @@ struct SweepParams {
   const double *seeds;          // [n_slots][n_parts]
   double *grad_partial;         // [n_bwd_ops][n_units][2] per-warp edge terms (a, b)
   int32_t *fault;               // set to 1 by a sweep whose bounded wait gave up
+  // single-launch (walk) sweeps: every op in one cache-friendly topological
+  // order; the adjoint ops carry their level-schedule index in pad0
+  const FwdOp *walk_fwd_ops;
+  int32_t n_walk_fwd;
+  const BwdOp *walk_bwd_ops;
+  int32_t n_walk_bwd;
+  const int32_t *walk_msg_slots;
 };
 
 struct MixParams {
@@ -107,8 +114,14 @@ void launch_pmatrix(cudaStream_t s, int n_parts, int n_edges, int R, int S, cons
                     const double *U, const double *Uinv, const double *rates, const double *brlen,
                     double *pmat64, float *pmat32);
 // Sweep launch shapes (threads per block, minimum blocks per SM): shape 0 is
-// the default; num_shapes() > 1 where the autotuner has alternatives.
+// the default; num_shapes() > 1 where the autotuner has alternatives. Shapes
+// from num_level_shapes() on are walk shapes: the whole sweep in one launch
+// over the walk schedule (level_begin / n_levels are then unused).
 int num_shapes(int precision, int R);
+int num_level_shapes(int precision, int R);
+// Kernel launches one sweep issues with this shape.
+int sweep_launches(int precision, int R, int shape, const SweepParams &p, bool backward, const int32_t *level_begin,
+                   int n_levels);
 int shape_threads(int precision, int R, int shape);
 // One launch per level: ops [level_begin[L], level_begin[L+1]) of the schedule.
 void launch_forward(cudaStream_t s, int precision, int R, int shape, const SweepParams &p,

@@ -101,7 +101,7 @@ __device__ __forceinline__ BwdOp load_bwd_op(const BwdOp *ops, int i) {
   BwdOp o;
   o.x = a.x; o.a = a.y; o.b = a.z; o.ea = a.w;
   o.eb = b.x; o.seed = b.y; o.out_a = b.z; o.out_b = b.w;
-  o.msg_begin = c.x; o.msg_count = c.y; o.pad0 = o.pad1 = o.pad2 = o.pad3 = o.pad4 = o.pad5 = 0;
+  o.msg_begin = c.x; o.msg_count = c.y; o.pad0 = c.z; o.pad1 = c.w; o.pad2 = o.pad3 = o.pad4 = o.pad5 = 0;
   return o;
 }
 

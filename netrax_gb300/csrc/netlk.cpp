@@ -116,6 +116,15 @@ struct netlk_ctx {
   std::vector<double> clv_brlen;
   std::vector<FwdOp> ifwd;                 // ops of the variants to recompute
   std::vector<int32_t> ifwd_level_begin;
+  // walk schedules (one segment only): the whole sweep as one op list per
+  // warp, in a depth-first order; wbwd carries its level-schedule index in pad0
+  std::vector<FwdOp> wfwd;
+  std::vector<BwdOp> wbwd;
+  std::vector<int32_t> wmsg_slots;
+  int n_wadj = 0;
+  bool walk_ok = false;
+  // best level-schedule shapes (the walk shapes only run the full sweeps)
+  int fwd_lshape = 0, bwd_lshape = 0;
   int64_t last_updates = 0;
   int fwd_shape = 0, bwd_shape = 0, sms = 0;
   bool tuned = false;
@@ -127,6 +136,7 @@ struct netlk_ctx {
   cudaStream_t stream = nullptr;
   int64_t dev_bytes = 0;
   DevBuf d_clv, d_scaler, d_adj, d_msg_slots, d_tips, d_weights, d_unit_part, d_fwd, d_bwd, d_rfwd, d_ifwd;
+  DevBuf d_wfwd, d_wbwd, d_wmsg_slots;
   DevBuf d_pmat64, d_pmat32, d_lambda, d_U, d_Uinv, d_rates, d_rw, d_freqs, d_Q, d_brlen;
   // FP32 contexts: float copies the sweeps read (weights as hi/lo pairs)
   DevBuf d_weights32, d_model32, d_seeds32;
@@ -184,7 +194,8 @@ struct netlk_ctx {
                       &d_pmat64, &d_pmat32, &d_lambda, &d_U, &d_Uinv, &d_rates, &d_rw, &d_freqs, &d_Q,
                       &d_brlen, &d_site_partial, &d_tree_logl, &d_root_slot, &d_root_lp, &d_root_dlp,
                       &d_seeds, &d_wts, &d_dret, &d_slot_begin, &d_slot_roots, &d_parts, &d_out, &d_grad_partial, &d_grad,
-                      &d_edge_begin, &d_edge_entries, &d_op_sum, &d_weights32, &d_model32, &d_seeds32})
+                      &d_edge_begin, &d_edge_entries, &d_op_sum, &d_weights32, &d_model32, &d_seeds32,
+                      &d_wfwd, &d_wbwd, &d_wmsg_slots})
       b->free();
     if (stream) cudaStreamDestroy(stream);
   }
@@ -226,6 +237,13 @@ struct netlk_ctx {
     p.seeds = d_seeds.as<double>();
     p.grad_partial = d_grad_partial.as<double>();
     p.fault = reinterpret_cast<int32_t *>(d_out.as<double>() + 2 + P + topo.n_ret);
+    if (walk_ok) {
+      p.walk_fwd_ops = d_wfwd.as<FwdOp>();
+      p.n_walk_fwd = (int32_t)wfwd.size();
+      p.walk_bwd_ops = d_wbwd.as<BwdOp>();
+      p.n_walk_bwd = (int32_t)wbwd.size();
+      p.walk_msg_slots = d_wmsg_slots.as<int32_t>();
+    }
     return p;
   }
 
@@ -256,7 +274,10 @@ struct netlk_ctx {
   }
 
   void autotune();
+  void count_launches();
   void build_schedules(int segments);
+  void build_walk(const std::vector<char> &inb, const std::vector<int> &slot_of,
+                  const std::vector<std::vector<int>> &by_level, const std::vector<int> &bwd_var);
   int choose_segments(size_t free_bytes) const;
   void allocate_and_upload(const netlk_partition *in_parts);
   void upload_model();
@@ -404,8 +425,12 @@ void netlk_ctx::build_schedules(int segments) {
   n_bwd_real = 0;
   bwd_bytes = 0;
   n_adj = 0;  // message buffers after liveness reuse
-  std::vector<std::vector<int32_t>> pending(V);  // message slots waiting for each variant
+  // messages waiting for each variant: (sending variant, slot); an op sums
+  // its messages in sender order, in every schedule, so the walk and the
+  // level sweeps add them in the same order
+  std::vector<std::vector<std::pair<int32_t, int32_t>>> pending(V);
   std::vector<int> free_slots;
+  std::vector<int> bwd_var;  // variant id of each adjoint op
   for (int L = dag.n_levels; L >= 1; --L) {
     const size_t base = bwd.size();
     std::vector<int32_t> read_here;
@@ -421,12 +446,14 @@ void netlk_ctx::build_schedules(int segments) {
       op.out_a = op.out_b = -1;
       op.msg_begin = (int32_t)msg_slots.size();
       op.msg_count = (int32_t)pending[x].size();
-      for (int32_t m : pending[x]) {
-        msg_slots.push_back(m);
-        read_here.push_back(m);
+      std::sort(pending[x].begin(), pending[x].end());
+      for (const auto &m : pending[x]) {
+        msg_slots.push_back(m.second);
+        read_here.push_back(m.second);
       }
       pending[x].clear();
       bwd.push_back(op);
+      bwd_var.push_back(x);
       n_bwd_real++;
     }
     // outputs of this level take buffers freed by earlier levels only: the
@@ -443,11 +470,11 @@ void netlk_ctx::build_schedules(int segments) {
       BwdOp &op = bwd[j];
       if (op.a >= 0) {
         op.out_a = alloc_slot();
-        pending[op.a].push_back(op.out_a);
+        pending[op.a].push_back({bwd_var[j], op.out_a});
       }
       if (op.b >= 0) {
         op.out_b = alloc_slot();
-        pending[op.b].push_back(op.out_b);
+        pending[op.b].push_back({bwd_var[j], op.out_b});
       }
       int64_t b = 4 + child_bytes(op.a) + child_bytes(op.b) + (int64_t)op.msg_count * clv_b;
       if (op.seed >= 0) b += clv_b;
@@ -458,6 +485,7 @@ void netlk_ctx::build_schedules(int segments) {
     for (int32_t m : read_here) free_slots.push_back(m);
     bwd_level_begin.push_back((int32_t)bwd.size());
   }
+  build_walk(inb, slot_of, by_level, bwd_var);
   for (BwdOp &op : bwd) {  // variant ids -> CLV slots
     op.a = map_ref(op.a);
     op.b = map_ref(op.b);
@@ -479,6 +507,94 @@ void netlk_ctx::build_schedules(int segments) {
       if (bwd[j].b != kFake) edge_entries[fill[bwd[j].eb]++] = (int32_t)(2 * j + 1);
     }
   }
+}
+
+// Walk schedules: with one segment (CLV slot = variant id) every op can run
+// in any topological order, one warp carrying its patterns through all of
+// them. The forward order is a depth-first post-order from the top levels
+// down, the child with the larger subtree first, so a child CLV is read soon
+// after it was written (while it is still in L2); the adjoint runs the
+// reverse order. Message slots are reused as soon as their reader has run.
+// Called while the level schedule's adjoint ops still hold variant ids.
+void netlk_ctx::build_walk(const std::vector<char> &inb, const std::vector<int> &slot_of,
+                           const std::vector<std::vector<int>> &by_level, const std::vector<int> &bwd_var) {
+  wfwd.clear();
+  wbwd.clear();
+  wmsg_slots.clear();
+  n_wadj = 0;
+  walk_ok = false;
+  if (n_segments != 1 || S != 4) return;
+  const int V = (int)dag.vars.size();
+  std::vector<double> size(V, 1.0);  // ordering heuristic: shared descendants counted per path
+  for (int L = 1; L <= dag.n_levels; ++L)
+    for (int v : by_level[L])
+      for (int i = 0; i < 2; ++i)
+        if (dag.vars[v].ref[i] >= 0) size[v] += size[dag.vars[v].ref[i]];
+  std::vector<int> order;
+  order.reserve(V);
+  std::vector<char> seen(V, 0);
+  std::vector<std::pair<int, int>> st;  // (variant, children visited)
+  for (int L = dag.n_levels; L >= 1; --L)
+    for (int v0 : by_level[L]) {
+      if (seen[v0]) continue;
+      seen[v0] = 1;
+      st.assign(1, {v0, 0});
+      while (!st.empty()) {
+        const int v = st.back().first, k = st.back().second;
+        int c[2] = {dag.vars[v].ref[0], dag.vars[v].ref[1]};
+        if (c[1] >= 0 && (c[0] < 0 || size[c[1]] > size[c[0]])) std::swap(c[0], c[1]);
+        if (k < 2) {
+          st.back().second++;
+          if (c[k] >= 0 && !seen[c[k]]) {
+            seen[c[k]] = 1;
+            st.push_back({c[k], 0});
+          }
+        } else {
+          order.push_back(v);
+          st.pop_back();
+        }
+      }
+    }
+  for (int v : order) {
+    const Variant &var = dag.vars[v];
+    wfwd.push_back(FwdOp{v, var.ref[0], var.ref[1], var.edge[0], var.edge[1], slot_of[v], 0, 0});
+  }
+  std::vector<int> level_index(V, -1);
+  for (size_t j = 0; j < bwd.size(); ++j) level_index[bwd_var[j]] = (int)j;
+  std::vector<std::vector<std::pair<int32_t, int32_t>>> pending(V);
+  std::vector<int> free_slots;
+  for (auto it = order.rbegin(); it != order.rend(); ++it) {
+    const int x = *it;
+    if (!inb[x]) continue;
+    BwdOp op = bwd[level_index[x]];  // a, b still variant ids (= CLV slots here)
+    op.pad0 = level_index[x];
+    op.msg_begin = (int32_t)wmsg_slots.size();
+    op.msg_count = (int32_t)pending[x].size();
+    std::sort(pending[x].begin(), pending[x].end());
+    for (const auto &m : pending[x]) wmsg_slots.push_back(m.second);
+    auto alloc_slot = [&]() {
+      if (!free_slots.empty()) {
+        const int sl = free_slots.back();
+        free_slots.pop_back();
+        return sl;
+      }
+      return n_wadj++;
+    };
+    op.out_a = op.out_b = -1;
+    if (op.a >= 0) {
+      op.out_a = alloc_slot();
+      pending[op.a].push_back({x, op.out_a});
+    }
+    if (op.b >= 0) {
+      op.out_b = alloc_slot();
+      pending[op.b].push_back({x, op.out_b});
+    }
+    for (const auto &m : pending[x]) free_slots.push_back(m.second);
+    pending[x].clear();
+    wbwd.push_back(op);
+  }
+  // the walk shares the message buffers sized for the level schedule
+  walk_ok = n_wadj <= std::max(1, n_adj) && (int)wbwd.size() == n_bwd_real;
 }
 
 // ------------------------------------------------------------ device setup
@@ -545,6 +661,11 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
   d_fwd.alloc(fwd.size() * sizeof(FwdOp), dev_bytes);
   d_bwd.alloc(bwd.size() * sizeof(BwdOp), dev_bytes);
   d_rfwd.alloc(std::max<size_t>(1, rfwd.size()) * sizeof(FwdOp), dev_bytes);
+  if (walk_ok) {
+    d_wfwd.alloc(wfwd.size() * sizeof(FwdOp), dev_bytes);
+    d_wbwd.alloc(std::max<size_t>(1, wbwd.size()) * sizeof(BwdOp), dev_bytes);
+    d_wmsg_slots.alloc(std::max<size_t>(1, wmsg_slots.size()) * 4, dev_bytes);
+  }
   d_ifwd.alloc(fwd.size() * sizeof(FwdOp), dev_bytes);
   const size_t nm = (size_t)P * topo.n_edges * R * S * S;
   d_pmat64.alloc(nm * 8, dev_bytes);
@@ -612,6 +733,14 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
   CUDA_OK(cudaMemcpyAsync(d_fwd.p, fwd.data(), fwd.size() * sizeof(FwdOp), cudaMemcpyHostToDevice, stream));
   if (!rfwd.empty())
     CUDA_OK(cudaMemcpyAsync(d_rfwd.p, rfwd.data(), rfwd.size() * sizeof(FwdOp), cudaMemcpyHostToDevice, stream));
+  if (walk_ok) {
+    CUDA_OK(cudaMemcpyAsync(d_wfwd.p, wfwd.data(), wfwd.size() * sizeof(FwdOp), cudaMemcpyHostToDevice, stream));
+    if (!wbwd.empty())
+      CUDA_OK(cudaMemcpyAsync(d_wbwd.p, wbwd.data(), wbwd.size() * sizeof(BwdOp), cudaMemcpyHostToDevice, stream));
+    if (!wmsg_slots.empty())
+      CUDA_OK(cudaMemcpyAsync(d_wmsg_slots.p, wmsg_slots.data(), wmsg_slots.size() * 4, cudaMemcpyHostToDevice,
+                              stream));
+  }
   if (!bwd.empty())
     CUDA_OK(cudaMemcpyAsync(d_bwd.p, bwd.data(), bwd.size() * sizeof(BwdOp), cudaMemcpyHostToDevice, stream));
   if (!msg_slots.empty())
@@ -747,7 +876,7 @@ void netlk_ctx::enqueue(bool pm, bool fwd_on, bool reduce, bool mixk, bool bwd_o
         else if (S == 20)
           launch_sweep20(stream, opts.precision, R, false, rp, rb, nl);
         else
-          launch_forward(stream, opts.precision, R, fwd_shape, rp, rb, nl);
+          launch_forward(stream, opts.precision, R, fwd_lshape, rp, rb, nl);
       }
       const int32_t *bb = bwd_level_begin.data() + (dag.n_levels - seg_hi[sg]);
       if (use_tc)
@@ -830,7 +959,7 @@ bool netlk_ctx::run_incremental() {
     else if (S == 20)
       launch_sweep20(stream, opts.precision, R, false, ip, ifwd_level_begin.data(), dag.n_levels);
     else
-      launch_forward(stream, opts.precision, R, fwd_shape, ip, ifwd_level_begin.data(), dag.n_levels);
+      launch_forward(stream, opts.precision, R, fwd_lshape, ip, ifwd_level_begin.data(), dag.n_levels);
   }
   launch_tree_reduce(stream, mp);
   launch_mix(stream, mp);
@@ -843,9 +972,20 @@ bool netlk_ctx::run_incremental() {
 // Times every launch shape of the two sweeps once on this context's own
 // workload (after one full evaluation with the default shapes, so the
 // adjoint sweep sees real seeds) and keeps the fastest for the CUDA graphs.
+// Launch counts of the chosen shapes (a walk shape issues one launch per chunk).
+void netlk_ctx::count_launches() {
+  if (S != 4) return;
+  const SweepParams sp = sweep();
+  fwd_launches = sweep_launches(opts.precision, R, fwd_shape, sp, false, fwd_level_begin.data(), dag.n_levels);
+  if (!bwd.empty())
+    bwd_launches = sweep_launches(opts.precision, R, bwd_shape, sp, true, bwd_level_begin.data(), dag.n_levels);
+}
+
 void netlk_ctx::autotune() {
   tuned = true;
-  const int ns = S == 4 ? num_shapes(opts.precision, R) : 1;
+  // walk shapes only where the walk schedule exists (one segment, DNA)
+  const int nls = S == 4 ? num_level_shapes(opts.precision, R) : 1;
+  const int ns = S == 4 && walk_ok ? num_shapes(opts.precision, R) : nls;
   tune_fwd_ms.assign(ns, 0.0);
   tune_bwd_ms.assign(ns, 0.0);
   if (const char *forced = std::getenv("NETLK_SHAPES")) {  // "fwd,bwd": fixed shapes, no timing
@@ -853,6 +993,9 @@ void netlk_ctx::autotune() {
     if (std::sscanf(forced, "%d,%d", &f, &b) == 2 && f >= 0 && f < ns && b >= 0 && b < ns) {
       fwd_shape = f;
       bwd_shape = b;
+      fwd_lshape = f < nls ? f : 0;
+      bwd_lshape = b < nls ? b : 0;
+      count_launches();
       return;
     }
   }
@@ -887,6 +1030,9 @@ void netlk_ctx::autotune() {
   cudaEventDestroy(e1);
   fwd_shape = (int)(std::min_element(tune_fwd_ms.begin(), tune_fwd_ms.end()) - tune_fwd_ms.begin());
   bwd_shape = (int)(std::min_element(tune_bwd_ms.begin(), tune_bwd_ms.end()) - tune_bwd_ms.begin());
+  fwd_lshape = (int)(std::min_element(tune_fwd_ms.begin(), tune_fwd_ms.begin() + nls) - tune_fwd_ms.begin());
+  bwd_lshape = (int)(std::min_element(tune_bwd_ms.begin(), tune_bwd_ms.begin() + nls) - tune_bwd_ms.begin());
+  count_launches();
 }
 
 void netlk_ctx::prepare_state() {

@@ -104,11 +104,17 @@ class NetworkLikelihood:
         self.variant, self.precision = variant, precision
         self.branch_lengths = np.array(network.branch_lengths, np.float64)
         self.ret_probs = np.array(network.ret_first_probs, np.float64)
+        st0 = self.stats
+        self.n_roots = st0["n_root_variants"]
+        self.n_variants = st0["n_variants"]
+
+    @property
+    def stats(self):
+        """netlk_dag_stats as a dict, queried now (the launch count per
+        evaluation follows the launch shapes the first evaluation chose)."""
         s = N.DagStats()
-        N.check(L.netlk_get_dag_stats(self._h, ctypes.byref(s)), self._h)
-        self.stats = s.as_dict()
-        self.n_roots = self.stats["n_root_variants"]
-        self.n_variants = self.stats["n_variants"]
+        N.check(N.lib().netlk_get_dag_stats(self._h, ctypes.byref(s)), self._h)
+        return s.as_dict()
 
     # ----------------------------------------------------------- lifecycle
     def close(self):

@@ -454,7 +454,9 @@ def test_adjoint_launch_shapes_agree(monkeypatch):
     from netrax_gb300.likelihood import NetworkLikelihood
     w = synth.config(1, scale=0.02)
     res = {}
-    for shapes in ("0,0", "0,5", "0,6", "5,2", "6,4", "7,7", "8,8", "9,9", "10,10", "11,11"):
+    # 12-14: walk shapes (the whole sweep in one launch per chunk of units)
+    for shapes in ("0,0", "0,5", "0,6", "5,2", "6,4", "7,7", "8,8", "9,9", "10,10", "11,11", "12,12", "13,13",
+                   "14,14", "1,12", "12,10"):
         monkeypatch.setenv("NETLK_SHAPES", shapes)
         with NetworkLikelihood(w.network, w.partitions, precision="fp32") as lik:
             res[shapes] = lik.loglikelihood_gradient()  # the first evaluation fixes the shapes
@@ -463,5 +465,39 @@ def test_adjoint_launch_shapes_agree(monkeypatch):
     t0, g0, r0 = res["0,0"]
     for k, (t, g, r) in res.items():
         # edge terms are summed per 16-pattern unit in every shape: same bits
+        assert t == t0
+        assert np.array_equal(g, g0) and np.array_equal(r, r0)
+
+
+def test_walk_sweeps_in_several_chunks(monkeypatch):
+    """A walk sweep over more warps than one wave holds runs in equal chunks
+    of units; it gives the level sweeps' logL and gradient bit for bit."""
+    from netrax_gb300.likelihood import NetworkLikelihood
+    from netrax_gb300.network import parse_extended_newick
+    text = "((A:0.2,((B:0.1,C:0.15)P:0.1)X#H1:0.1::0.3)Q:0.2,(D:0.2,X#H1:0.12::0.7)R:0.2);"
+    rng = np.random.default_rng(11)
+    n = 200_000  # > one wave of the 16-blocks-per-SM walk shape on 152 SMs
+
+    class Part:
+        tip_states = (1 << rng.integers(0, 4, size=(4, n))).astype(np.uint32)
+        weights = rng.integers(1, 4, size=n).astype(np.float64)
+        freqs = np.array([0.2, 0.3, 0.3, 0.2])
+        exch = np.array([1.0, 2.5, 0.8, 1.2, 3.0, 1.0])
+        alpha = 0.8
+        states = 4
+        rate_cats = 4
+
+    res = {}
+    for shapes in ("0,0", "14,14", "12,12"):
+        monkeypatch.setenv("NETLK_SHAPES", shapes)
+        with NetworkLikelihood(parse_extended_newick(text), [Part], precision="fp32", device=0) as lik:
+            res[shapes] = lik.loglikelihood_gradient()
+            l0 = lik.launch_count()
+            lik.loglikelihood_gradient()
+            if shapes == "14,14":  # P-matrices, 2 x chunks, site sums, mixture, gradient reduction (2)
+                n = lik.launch_count() - l0
+                assert (n - 5) % 2 == 0 and (n - 5) // 2 >= 2
+    t0, g0, r0 = res["0,0"]
+    for t, g, r in res.values():
         assert t == t0
         assert np.array_equal(g, g0) and np.array_equal(r, r0)
