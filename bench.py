@@ -154,10 +154,12 @@ class ClockSampler:
 
 # DRAM bytes per site-CLV update of each sweep (DNA: 4 states) from one ncu capture
 # (profiles/sweep_dram_traffic_config2_scale0.3.md: dram__bytes_read.sum +
-# dram__bytes_write.sum of one evaluation's 16 level launches, same network at
-# 0.3 of its sites, scaled by updates; writes still dirty in L2 at a launch's
-# end are not counted).
-TRAFFIC_PER_UPDATE = {"forward_fp32_4": 102.5, "backward_fp32_4": 295.9}
+# dram__bytes_write.sum of the 100-taxon / 8-reticulation network at 0.3 of its
+# sites, scaled by updates; writes still dirty in L2 at a launch's end are not
+# counted). Keyed by sweep, schedule (level: one launch per DAG level; walk:
+# one warp walks the whole DAG), precision and states.
+TRAFFIC_PER_UPDATE = {"forward_level_fp32_4": 102.3, "backward_level_fp32_4": 295.9,
+                      "backward_walk_fp32_4": 220.3}
 
 
 def cpu_port_rate(w, n_sample, steps, warmup, variant):
@@ -326,12 +328,18 @@ def run_netlk(args, ws, rank, local):
     dom = "backward" if kavg["backward"] >= kavg["forward"] else "forward"
     dom_bytes = bwd_b if dom == "backward" else fwd_b
     achieved = dom_bytes / (kavg[dom] * 1e-3) / 1e9 if kavg[dom] > 0 else 0.0
+    tuning = lik.tuning()
+    sched = "walk" if tuning.get(dom + "_walk") else "level"
     traffic = None
-    tt = TRAFFIC_PER_UPDATE.get("%s_%s_%d" % (dom, args.precision, lik.states))
+    tt = TRAFFIC_PER_UPDATE.get("%s_%s_%s_%d" % (dom, sched, args.precision, lik.states))
     if tt:
         traffic = tt * st["site_clv_updates"]
+    if lik.states == 20:  # FP32 with 4 rates runs the tensor-core (tcgen05) sweeps
+        kname = dom + ("20_tc_kernel" if args.precision == "fp32" and lik.rate_cats == 4 else "20_kernel")
+    else:
+        kname = dom + ("_walk" if sched == "walk" else "") + "_kernel"
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic, "kernel": dom + "_kernel",
+                "frac": achieved / peak, "traffic": traffic, "kernel": kname,
                 "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind if peak_kind == "measured"
                 else "fallback 6.8 TB/s",
                 "algorithmic_bytes_per_launch": dom_bytes,
@@ -362,7 +370,7 @@ def run_netlk(args, ws, rank, local):
             "site_clv_updates_per_s": value * st["site_clv_updates"],
             "gpu_launches": int(launches),
             "kernel_ms": kavg,
-            "autotune": lik.tuning(),
+            "autotune": tuning,
             "e2e": {"value": ws / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": e2e_s * 1000.0},
             "roofline": roofline,

@@ -308,6 +308,12 @@ int netlk_kernel_times(netlk_ctx *ctx, double *ms, int64_t *launches, int32_t n)
  * time (ms) it measured for each of the first n shapes (0 where untimed). */
 int netlk_tuning(const netlk_ctx *ctx, int32_t *fwd_shape, int32_t *bwd_shape, double *fwd_ms,
                  double *bwd_ms, int32_t n);
+/* Index of the first walk shape in the autotuner's table: shapes from it on
+ * run a sweep as one op walk per warp (whole DAG per launch) instead of one
+ * launch per DAG level. Equals the table size where the context has no walk
+ * shapes (20 states, FP64, several checkpoint segments). No counterpart in the
+ * reference (measurement). */
+int netlk_walk_shape_begin(const netlk_ctx *ctx, int32_t *first_walk_shape);
 
 /* ---------------------------------------------------- allocation-free mixing */
 /* No counterpart in the reference: an extra entry point for callers that

@@ -34,7 +34,7 @@ EXPORTED = [
     "netlk_loglikelihood", "netlk_loglikelihood_gradient", "netlk_edge_derivatives",
     "netlk_tree_partials", "netlk_mix_and_backward", "netlk_get_clv", "netlk_get_stream",
     "netlk_launch_count", "netlk_set_branch_lengths_device", "netlk_enqueue",
-    "netlk_result_pointers", "netlk_set_profiling", "netlk_kernel_times", "netlk_tuning",
+    "netlk_result_pointers", "netlk_set_profiling", "netlk_kernel_times", "netlk_tuning", "netlk_walk_shape_begin",
     "netlk_mix_site_loglikelihoods_noalloc", "netlk_batch_create",
     "netlk_batch_loglikelihood_gradient", "netlk_batch_destroy", "netlk_edge_loglikelihood",
     "netlk_last_site_updates", "netlk_encode_states", "netlk_compress_patterns",
@@ -131,6 +131,7 @@ def lib():
     L.netlk_mix_site_loglikelihoods_noalloc.argtypes = [
         vp, ctypes.c_int32, ctypes.c_int64, vp, ctypes.c_int32, vp, ctypes.c_int32, ctypes.c_double, vp, vp]
     L.netlk_tuning.argtypes = [vp, c_int32_p, c_int32_p, c_double_p, c_double_p, ctypes.c_int32]
+    L.netlk_walk_shape_begin.argtypes = [vp, c_int32_p]
     L.netlk_kernel_times.argtypes = [vp, c_double_p, ctypes.POINTER(ctypes.c_int64), ctypes.c_int32]
     L.netlk_batch_create.argtypes = [ctypes.POINTER(vp), ctypes.c_int32, ctypes.POINTER(vp)]
     L.netlk_batch_loglikelihood_gradient.argtypes = [vp, c_double_p, ctypes.POINTER(c_double_p),

@@ -1644,6 +1644,13 @@ int netlk_tuning(const netlk_ctx *ctx, int32_t *fwd_shape, int32_t *bwd_shape, d
   return NETLK_OK;
 }
 
+int netlk_walk_shape_begin(const netlk_ctx *ctx, int32_t *first_walk_shape) {
+  if (!ctx || !first_walk_shape) return NETLK_ERR_INVALID_ARGUMENT;
+  const int nls = ctx->S == 4 ? num_level_shapes(ctx->opts.precision, ctx->R) : 1;
+  *first_walk_shape = ctx->S == 4 && ctx->walk_ok ? nls : (int32_t)ctx->tune_fwd_ms.size();
+  return NETLK_OK;
+}
+
 int netlk_get_stream(netlk_ctx *ctx, void **stream) {
   if (!ctx || !stream) return NETLK_ERR_INVALID_ARGUMENT;
   *stream = (void *)ctx->stream;

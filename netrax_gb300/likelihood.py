@@ -270,7 +270,10 @@ class NetworkLikelihood:
         fm, bm = np.zeros(n), np.zeros(n)
         N.check(N.lib().netlk_tuning(self._h, ctypes.byref(fs), ctypes.byref(bs), _ptr(fm, ctypes.c_double),
                                      _ptr(bm, ctypes.c_double), n), self._h)
+        ws = ctypes.c_int32()
+        N.check(N.lib().netlk_walk_shape_begin(self._h, ctypes.byref(ws)), self._h)
         return {"forward_shape": fs.value, "backward_shape": bs.value,
+                "forward_walk": fs.value >= ws.value, "backward_walk": bs.value >= ws.value,
                 "forward_ms": [x for x in fm if x > 0], "backward_ms": [x for x in bm if x > 0]}
 
     def stream(self):
