@@ -66,44 +66,127 @@ __device__ __forceinline__ void load_child(const SweepParams &p, int32_t ref, si
   }
 }
 
-// out[k] = P . c[k] for the lane's patterns, P (this lane's rate, row-major
-// 4x4) read from shared memory.
-template <typename real, int PPL>
-__device__ __forceinline__ void matvec2_s(const real *P, const real (&c)[PPL][4], real (&out)[PPL][4]) {
+// Asks L2 for the lane's part of child `ref`'s CLV and scale counters (a
+// variant only: tips are small and stay cached), ahead of their use by a
+// later op of a walk.
+template <typename real, int R, int PPL>
+__device__ __forceinline__ void prefetch_child(const SweepParams &p, int32_t ref, size_t g0, int r, int stride) {
+  if (ref < 0) return;
+  const real *clv = static_cast<const real *>(p.clv) + ((size_t)ref * p.n_patterns + g0) * (R * 4) + r * 4;
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    real row[4];
-    Vec<real>::load(P + 4 * i, row);
-#pragma unroll
-    for (int k = 0; k < PPL; ++k)
-      out[k][i] = row[0] * c[k][0] + row[1] * c[k][1] + row[2] * c[k][2] + row[3] * c[k][3];
+  for (int k = 0; k < PPL; ++k) asm volatile("prefetch.global.L2 [%0];" ::"l"(clv + (size_t)k * stride * (R * 4)));
+  if (r == 0) {
+    const int32_t *sc = p.scaler + (size_t)ref * p.n_patterns + g0;
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(sc));
   }
 }
 
-// out[k] = P^T . u[k], P from shared memory.
-template <typename real, int PPL>
-__device__ __forceinline__ void matvec2_ts(const real *P, const real (&u)[PPL][4], real (&out)[PPL][4]) {
+// FP32 mat-vecs on pairs of output states with paired FP32 instructions
+// (FMUL2 / FFMA2; the input entry is broadcast to both halves of the pair),
+// half the instructions of the scalar form and the same operation order:
+// out_i = fma(M_i3, c_3, fma(M_i2, c_2, fma(M_i1, c_1, M_i0 c_0))).
+// out[k] = M . c[k] with MT = M transposed (row j of MT = column j of M).
+template <int PPL>
+__device__ __forceinline__ void mv_pairs_cols(const float *MT, const float (&c)[PPL][4], float (&out)[PPL][4]) {
+  float2 m01[4], m23[4];
 #pragma unroll
-  for (int k = 0; k < PPL; ++k)
+  for (int j = 0; j < 4; ++j) {
+    const float4 q = *reinterpret_cast<const float4 *>(MT + 4 * j);
+    m01[j] = make_float2(q.x, q.y);
+    m23[j] = make_float2(q.z, q.w);
+  }
 #pragma unroll
-    for (int j = 0; j < 4; ++j) out[k][j] = 0;
+  for (int k = 0; k < PPL; ++k) {
+    float2 a = __fmul2_rn(m01[0], make_float2(c[k][0], c[k][0]));
+    float2 b = __fmul2_rn(m23[0], make_float2(c[k][0], c[k][0]));
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    real row[4];
-    Vec<real>::load(P + 4 * i, row);
-#pragma unroll
-    for (int k = 0; k < PPL; ++k)
-#pragma unroll
-      for (int j = 0; j < 4; ++j) out[k][j] += row[j] * u[k][i];
+    for (int j = 1; j < 4; ++j) {
+      a = __ffma2_rn(m01[j], make_float2(c[k][j], c[k][j]), a);
+      b = __ffma2_rn(m23[j], make_float2(c[k][j], c[k][j]), b);
+    }
+    out[k][0] = a.x;
+    out[k][1] = a.y;
+    out[k][2] = b.x;
+    out[k][3] = b.y;
   }
 }
 
-// P rows of one rate sit kPRow values apart in shared memory (16 used +
-// padding) so the four rate groups of a warp's LDS.128 hit distinct banks.
+// out[k] = M^T . u[k] with M row-major.
+template <int PPL>
+__device__ __forceinline__ void mv_pairs_rows_t(const float *M, const float (&u)[PPL][4], float (&out)[PPL][4]) {
+  float2 m01[4], m23[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float4 q = *reinterpret_cast<const float4 *>(M + 4 * i);
+    m01[i] = make_float2(q.x, q.y);
+    m23[i] = make_float2(q.z, q.w);
+  }
+#pragma unroll
+  for (int k = 0; k < PPL; ++k) {
+    float2 a = __fmul2_rn(m01[0], make_float2(u[k][0], u[k][0]));
+    float2 b = __fmul2_rn(m23[0], make_float2(u[k][0], u[k][0]));
+#pragma unroll
+    for (int i = 1; i < 4; ++i) {
+      a = __ffma2_rn(m01[i], make_float2(u[k][i], u[k][i]), a);
+      b = __ffma2_rn(m23[i], make_float2(u[k][i], u[k][i]), b);
+    }
+    out[k][0] = a.x;
+    out[k][1] = a.y;
+    out[k][2] = b.x;
+    out[k][3] = b.y;
+  }
+}
+
+// Staged P-matrix slices in shared memory. One slice per (child, rate),
+// kRow values apart so the four rate groups of a warp's 16-byte loads hit
+// distinct banks: FP64 holds P row-major (16 values + 2 padding); FP32 holds
+// P row-major in [0, 16) and P transposed in [16, 32) (+ 4 padding), the two
+// layouts the paired mat-vecs read.
 template <typename real>
 struct PLayout {
-  static constexpr int kRow = (sizeof(real) == 4) ? 20 : 18;
+  static constexpr int kRow = (sizeof(real) == 4) ? 36 : 18;
+  static constexpr int kT = (sizeof(real) == 4) ? 16 : 0;  // transposed copy (FP32)
 };
+
+// out[k] = P . c[k] for the lane's patterns; P: the lane's (child, rate)
+// slice in shared memory.
+template <typename real, int PPL>
+__device__ __forceinline__ void matvec2_s(const real *P, const real (&c)[PPL][4], real (&out)[PPL][4]) {
+  if constexpr (sizeof(real) == 4) {
+    mv_pairs_cols<PPL>(P + PLayout<float>::kT, c, out);
+  } else {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      real row[4];
+      Vec<real>::load(P + 4 * i, row);
+#pragma unroll
+      for (int k = 0; k < PPL; ++k)
+        out[k][i] = row[0] * c[k][0] + row[1] * c[k][1] + row[2] * c[k][2] + row[3] * c[k][3];
+    }
+  }
+}
+
+// out[k] = P^T . u[k], P: the lane's slice in shared memory.
+template <typename real, int PPL>
+__device__ __forceinline__ void matvec2_ts(const real *P, const real (&u)[PPL][4], real (&out)[PPL][4]) {
+  if constexpr (sizeof(real) == 4) {
+    mv_pairs_rows_t<PPL>(P, u, out);
+  } else {
+#pragma unroll
+    for (int k = 0; k < PPL; ++k)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) out[k][j] = 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      real row[4];
+      Vec<real>::load(P + 4 * i, row);
+#pragma unroll
+      for (int k = 0; k < PPL; ++k)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) out[k][j] += row[j] * u[k][i];
+    }
+  }
+}
 
 // Stages the op's two P-matrices (all R rates) of one partition in the
 // warp's own shared-memory slice: sP[(m*R + r)*kRow + 0..15], m = 0 for edge
@@ -119,12 +202,18 @@ __device__ __forceinline__ void stage_pmats_warp(real *sP, const real *pm_part, 
     const int rr = j / 16, c = j - rr * 16;
     real *dst = sP + (m * R + rr) * ROW + c;
     const int e = m ? eb : ea;
-    if (e >= 0) {
-      if (sizeof(real) == 4) {
-        *reinterpret_cast<float4 *>(dst) = __ldg(reinterpret_cast<const float4 *>(pm_part + (size_t)e * (R * 16) + j));
-      } else {
-        *reinterpret_cast<double2 *>(dst) = __ldg(reinterpret_cast<const double2 *>(pm_part + (size_t)e * (R * 16) + j));
-      }
+    if constexpr (sizeof(real) == 4) {
+      // one row of P: row-major, and as a column of the transposed copy
+      const float4 v = e >= 0 ? __ldg(reinterpret_cast<const float4 *>(pm_part + (size_t)e * (R * 16) + j))
+                              : make_float4(0.f, 0.f, 0.f, 0.f);
+      *reinterpret_cast<float4 *>(dst) = v;
+      real *t = sP + (m * R + rr) * ROW + PLayout<real>::kT + c / 4;
+      t[0] = v.x;
+      t[4] = v.y;
+      t[8] = v.z;
+      t[12] = v.w;
+    } else if (e >= 0) {
+      *reinterpret_cast<double2 *>(dst) = __ldg(reinterpret_cast<const double2 *>(pm_part + (size_t)e * (R * 16) + j));
     } else {
 #pragma unroll
       for (int q = 0; q < V; ++q) dst[q] = (real)0;
@@ -136,12 +225,23 @@ __device__ __forceinline__ void stage_pmats_warp(real *sP, const real *pm_part, 
 
 
 // ------------------------------------------------------------------ forward
+// The CLV (and scale counters) a walk's previous op left in registers, for a
+// next op that has it as a child.
+template <typename real, int PPL>
+struct FwdCarry {
+  real v[PPL][4];
+  int s[PPL];
+  int32_t var = INT32_MAX;  // variant held, INT32_MAX: none
+};
+
 // One op for one warp's unit of patterns: CLV_out = (P[ea] . a) * (P[eb] . b),
 // rescaled per site; site log-likelihoods of displayed-tree root variants are
 // summed over the warp's patterns into site_partial[slot][unit]. sP: the
-// warp's shared-memory P staging slice.
-template <typename real, int R, int PPL>
-__device__ __forceinline__ void forward_op(const SweepParams &p, const FwdOp &op, int unit, real *sP, int lane) {
+// warp's shared-memory P staging slice. With CARRY, a child held in `carry`
+// is taken from there instead of memory, and the result is left in it.
+template <typename real, int R, int PPL, bool CARRY = false>
+__device__ __forceinline__ void forward_op(const SweepParams &p, const FwdOp &op, int unit, real *sP, int lane,
+                                           FwdCarry<real, PPL> *carry = nullptr) {
   constexpr int PPW = 32 / R;          // patterns per pass of the lane rows
   constexpr int UNIT = PPW * PPL;      // patterns per forward unit
   const int r = lane % R;
@@ -153,8 +253,25 @@ __device__ __forceinline__ void forward_op(const SweepParams &p, const FwdOp &op
   const size_t g0 = (size_t)unit * UNIT + pl;  // the lane's first pattern; the second is g0 + PPW
   real ca[PPL][4], cb[PPL][4];
   int sa[PPL], sb[PPL];
-  load_child<real, R, PPL>(p, op.a, g0, r, PPW, ca, sa);
-  load_child<real, R, PPL>(p, op.b, g0, r, PPW, cb, sb);
+  if constexpr (CARRY) {
+    auto take = [&](int32_t ref, real(&c)[PPL][4], int(&sc)[PPL]) {
+      if (ref == carry->var) {
+#pragma unroll
+        for (int k = 0; k < PPL; ++k) {
+#pragma unroll
+          for (int i = 0; i < 4; ++i) c[k][i] = carry->v[k][i];
+          sc[k] = carry->s[k];
+        }
+      } else {
+        load_child<real, R, PPL>(p, ref, g0, r, PPW, c, sc);
+      }
+    };
+    take(op.a, ca, sa);
+    take(op.b, cb, sb);
+  } else {
+    load_child<real, R, PPL>(p, op.a, g0, r, PPW, ca, sa);
+    load_child<real, R, PPL>(p, op.b, g0, r, PPW, cb, sb);
+  }
   stage_pmats_warp<real, R>(sP, static_cast<const real *>(p.pmat) + (size_t)part * p.n_edges * (R * 16), op.ea,
                             op.b == INT32_MIN ? -1 : op.eb, lane);
 
@@ -179,6 +296,15 @@ __device__ __forceinline__ void forward_op(const SweepParams &p, const FwdOp &op
     s[k] = sa[k] + sb[k] + Scale<real>::rescale(m, v[k]);
     Vec<real>::store(dst + (size_t)k * PPW * (R * 4), v[k]);
     if (r == 0) sdst[(size_t)k * PPW] = s[k];
+  }
+  if constexpr (CARRY) {
+#pragma unroll
+    for (int k = 0; k < PPL; ++k) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) carry->v[k][i] = v[k][i];
+      carry->s[k] = s[k];
+    }
+    carry->var = op.out;
   }
   if (op.slot >= 0) {
     // pll_compute_root_loglikelihood for the lane's sites, summed over the warp
@@ -227,13 +353,60 @@ __global__ void __launch_bounds__(THREADS, MINB) forward_walk_kernel(const Sweep
   if (unit >= unit_end) return;  // whole warp
   real *sP = sPw[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
-  for (int i = 0; i < p.n_walk_fwd; ++i) {
+  constexpr int PPW = 32 / R;
+  const size_t g0 = (size_t)unit * PPW * PPL + lane / R;
+  const int n = p.n_walk_fwd;
+  FwdCarry<real, PPL> carry;  // a parent right after its child reads it from here
+  for (int i = 0; i < n; ++i) {
+    int4 h = make_int4(-1, -1, -1, -1);
+    if (i + 1 < n) h = __ldg(reinterpret_cast<const int4 *>(p.walk_fwd_ops + i + 1));  // out, a, b, ea
     __syncwarp();  // every lane is done with the previous op's P
-    forward_op<real, R, PPL>(p, load_fwd_op(p.walk_fwd_ops, i), unit, sP, lane);
+    forward_op<real, R, PPL, true>(p, load_fwd_op(p.walk_fwd_ops, i), unit, sP, lane, &carry);
+    // the next op's children: a variant written long before (not the op
+    // just computed) comes from DRAM
+    prefetch_child<real, R, PPL>(p, h.y, g0, lane % R, PPW);
+    prefetch_child<real, R, PPL>(p, h.z, g0, lane % R, PPW);
   }
 }
 
 // ------------------------------------------------------------------ adjoint
+// The partition's rate matrix, frequencies, rate weights and rates into a
+// warp's shared-memory slice sQ: [0,16) Q (transposed in FP32), [16,20) pi,
+// then R rate weights and R rates. Published by the next __syncwarp.
+template <typename real, int R>
+__device__ __forceinline__ void stage_model(const SweepParams &p, int part, real *sQ, int lane) {
+  // FP32 keeps Q transposed (sQ[4j + i] = Q[i][j]) for the paired mat-vec
+  if (lane < 16)
+    sQ[lane] = model_val<real>(p.Q, p.Q32, part * 16 + (sizeof(real) == 4 ? (lane % 4) * 4 + lane / 4 : lane));
+  if (lane < 4) sQ[16 + lane] = model_val<real>(p.freqs, p.freqs32, part * 4 + lane);
+  if (lane < R) {
+    sQ[20 + lane] = model_val<real>(p.rate_weights, p.rate_weights32, part * R + lane);
+    sQ[20 + R + lane] = model_val<real>(p.rates, p.rates32, part * R + lane);
+  }
+}
+
+// Values per warp in the model slice: Q, pi, R rate weights, R rates,
+// rounded up to whole 16-byte vectors (the paired mat-vec reads Q's rows as
+// float4 in every warp's slice).
+template <int R>
+struct ModelSlice {
+  static constexpr int kSize = (16 + 4 + 2 * R + 3) / 4 * 4;
+};
+
+// q[k] = Q . x[k] with sQ as stage_model leaves it.
+template <typename real, int PPL>
+__device__ __forceinline__ void matvec_q(const real *sQ, const real (&x)[PPL][4], real (&q)[PPL][4]) {
+  if constexpr (sizeof(real) == 4) {
+    mv_pairs_cols<PPL>(sQ, x, q);
+  } else {
+#pragma unroll
+    for (int k = 0; k < PPL; ++k)
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+        q[k][i] = sQ[4 * i] * x[k][0] + sQ[4 * i + 1] * x[k][1] + sQ[4 * i + 2] * x[k][2] + sQ[4 * i + 3] * x[k][3];
+  }
+}
+
 // Reverse sweep as message passing, one launch per level (deepest first).
 // For op x with CLV_x = 2^k (Pa a) * (Pb b):
 //   adj_x   = sum of incoming messages (+ seed: tree weight * w_s rw_r pi_i / L_s)
@@ -245,12 +418,25 @@ __global__ void __launch_bounds__(THREADS, MINB) forward_walk_kernel(const Sweep
 // One adjoint op for one warp's unit. opi: the op's index in the level
 // schedule (its grad_partial row); msg_slots: the schedule's message slot list.
 // sP, sQ: the warp's shared-memory staging slices.
-template <typename real, int R, int PPL>
+// Patterns per register group in the adjoint op: 4 where the launch shape
+// leaves 128 or more registers per thread, else one base unit.
+template <int THREADS, int MINB, int PPL>
+struct AdjGroup {
+  static constexpr int G = (65536 / (THREADS * MINB) >= 128 && PPL >= 4) ? 4 : kPPLBase;
+};
+
+// WALK: the walk schedule's op: model values already staged in sQ, and a
+// message marked for the next op (out = -2) passed in `carry` (pad4 = 1:
+// the op's adjoint starts from it).
+template <typename real, int R, int PPL, int G, bool WALK = false>
 __device__ __forceinline__ void backward_op(const SweepParams &p, const BwdOp &op, int opi,
                                             const int32_t *__restrict__ msg_slots, int unit, real *sP, real *sQ,
-                                            int lane) {
+                                            int lane, real (&carry)[PPL][4]) {
   constexpr int PPW = 32 / R;
   constexpr int UNIT = PPW * PPL;      // patterns per adjoint unit
+  // the lane's patterns are processed in groups of G (whole base units): the
+  // op's decode and staging serve them all, registers hold one group
+  static_assert(PPL % G == 0 && G % kPPLBase == 0, "whole groups of whole units");
   const int r = lane % R;
   const int pl = lane / R;
   // a warp covers UPU base units (kPPLBase patterns per lane each)
@@ -264,22 +450,37 @@ __device__ __forceinline__ void backward_op(const SweepParams &p, const BwdOp &o
   const real *clv = static_cast<const real *>(p.clv);
   real *msg = static_cast<real *>(p.msg);
 
-  real ca[PPL][4], cb[PPL][4], ax[PPL][4], cx[PPL][4];
-  int sa[PPL], sb[PPL], sx[PPL];
+  real ca[G][4], cb[G][4], ax[G][4], cx[G][4];
+  int sa[G], sb[G], sx[G];
+  // the group's children, counters, incoming messages (+ the message kept in
+  // registers by the previous op) and, at a displayed-tree root, its own CLV
+  auto load_group = [&](int grp) {
+    const size_t gg = g0 + (size_t)grp * G * PPW;
+    const size_t off = lane_off + (size_t)grp * G * PPW * (R * 4);
 #pragma unroll
-  for (int k = 0; k < PPL; ++k)
+    for (int k = 0; k < G; ++k)
 #pragma unroll
-    for (int i = 0; i < 4; ++i) ax[k][i] = 0;
-  {
-    load_child<real, R, PPL>(p, op.a, g0, r, PPW, ca, sa);
-    load_child<real, R, PPL>(p, op.b, g0, r, PPW, cb, sb);
-    const int32_t *sxp = p.scaler + (size_t)op.x * N + g0;
+      for (int i = 0; i < 4; ++i) ax[k][i] = 0;
+    if constexpr (WALK) {
+      if (op.pad4) {
 #pragma unroll
-    for (int k = 0; k < PPL; ++k) sx[k] = sxp[(size_t)k * PPW];
+        for (int k = 0; k < G; ++k)
+#pragma unroll
+          for (int i = 0; i < 4; ++i) ax[k][i] += carry[grp * G + k][i];
+      }
+    }
+    load_child<real, R, G>(p, op.a, gg, r, PPW, ca, sa);
+    load_child<real, R, G>(p, op.b, gg, r, PPW, cb, sb);
+    const int32_t *sxp = p.scaler + (size_t)op.x * N + gg;
+#pragma unroll
+    for (int k = 0; k < G; ++k) sx[k] = sxp[(size_t)k * PPW];
     for (int m = 0; m < op.msg_count; ++m) {
-      const real *src = msg + (size_t)__ldg(msg_slots + op.msg_begin + m) * N * (R * 4) + lane_off;
+      int slot;
+      if constexpr (WALK) slot = m == 0 ? op.msg0 : m == 1 ? op.msg1 : m == 2 ? op.msg2 : __ldg(msg_slots + op.msg_begin + m);
+      else slot = __ldg(msg_slots + op.msg_begin + m);
+      const real *src = msg + (size_t)slot * N * (R * 4) + off;
 #pragma unroll
-      for (int k = 0; k < PPL; ++k) {
+      for (int k = 0; k < G; ++k) {
         real t[4];
         Vec<real>::load(src + (size_t)k * PPW * (R * 4), t);
 #pragma unroll
@@ -287,49 +488,20 @@ __device__ __forceinline__ void backward_op(const SweepParams &p, const BwdOp &o
       }
     }
     if (op.seed >= 0) {
-      const real *cxp = clv + (size_t)op.x * N * (R * 4) + lane_off;
+      const real *cxp = clv + (size_t)op.x * N * (R * 4) + off;
 #pragma unroll
-      for (int k = 0; k < PPL; ++k) Vec<real>::load(cxp + (size_t)k * PPW * (R * 4), cx[k]);
+      for (int k = 0; k < G; ++k) Vec<real>::load(cxp + (size_t)k * PPW * (R * 4), cx[k]);
     }
-  }
-  if (lane < 16) sQ[lane] = model_val<real>(p.Q, p.Q32, part * 16 + lane);
-  if (lane < 4) sF[lane] = model_val<real>(p.freqs, p.freqs32, part * 4 + lane);
-  if (lane < R) {
-    sRW[lane] = model_val<real>(p.rate_weights, p.rate_weights32, part * R + lane);
-    sRate[lane] = model_val<real>(p.rates, p.rates32, part * R + lane);
-  }
+  };
+  load_group(0);
+  if (!WALK) stage_model<real, R>(p, part, sQ, lane);
   stage_pmats_warp<real, R>(sP, static_cast<const real *>(p.pmat) + (size_t)part * p.n_edges * (R * 16), op.ea,
                             fake ? -1 : op.eb, lane);  // its __syncwarp also publishes sQ
 
   const real rw = sRW[r];
-  if (op.seed >= 0) {
-    // d(w_s log L_s)/d clv_x = w_s rw_r pi_i / L_s, times the tree weight
-    const real sd = model_val<real>(p.seeds, p.seeds32, (size_t)op.seed * p.n_parts + part);
-#pragma unroll
-    for (int k = 0; k < PPL; ++k) {
-      real t = rw * (sF[0] * cx[k][0] + sF[1] * cx[k][1] + sF[2] * cx[k][2] + sF[3] * cx[k][3]);
-      t = rate_sum<R>(t);
-      const real sw = sd * pattern_weight<real>(p, g0 + (size_t)k * PPW);
-      if (t > (real)0 && sw != (real)0) {
-        const real f = sw * rw / t;
-#pragma unroll
-        for (int i = 0; i < 4; ++i) ax[k][i] += f * sF[i];
-      }
-    }
-  }
+  const real sd = op.seed >= 0 ? model_val<real>(p.seeds, p.seeds32, (size_t)op.seed * p.n_parts + part) : (real)0;
   const real *Pa = sP + r * PLayout<real>::kRow;
   const real *Pb = sP + (R + r) * PLayout<real>::kRow;
-  real pa[PPL][4], pb[PPL][4];
-  matvec2_s<real, PPL>(Pa, ca, pa);
-  if (!fake) {
-    matvec2_s<real, PPL>(Pb, cb, pb);
-  } else {
-#pragma unroll
-    for (int k = 0; k < PPL; ++k)
-#pragma unroll
-      for (int i = 0; i < 4; ++i) pb[k][i] = 1;
-  }
-  real ua[PPL][4], ub[PPL][4];
   // edge terms per base unit (patterns k < kPPLBase of the lane in unit 0,
   // the next kPPLBase in unit 1, ...): every launch shape sums them in the
   // same order, so the gradient does not depend on the shape
@@ -337,44 +509,100 @@ __device__ __forceinline__ void backward_op(const SweepParams &p, const BwdOp &o
 #pragma unroll
   for (int u = 0; u < UPU; ++u) ga[u] = gb[u] = 0;
 #pragma unroll
-  for (int k = 0; k < PPL; ++k) {
-    const int sh = sx[k] - sa[k] - sb[k];
+  for (int grp = 0; grp < PPL / G; ++grp) {
+    if (grp > 0) load_group(grp);
+    const size_t gg = g0 + (size_t)grp * G * PPW;
+    const size_t off = lane_off + (size_t)grp * G * PPW * (R * 4);
+    if (op.seed >= 0) {
+      // d(w_s log L_s)/d clv_x = w_s rw_r pi_i / L_s, times the tree weight
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      ua[k][i] = ax[k][i] * pb[k][i];
-      ub[k][i] = ax[k][i] * pa[k][i];
+      for (int k = 0; k < G; ++k) {
+        real t = rw * (sF[0] * cx[k][0] + sF[1] * cx[k][1] + sF[2] * cx[k][2] + sF[3] * cx[k][3]);
+        t = rate_sum<R>(t);
+        const real sw = sd * pattern_weight<real>(p, gg + (size_t)k * PPW);
+        if (t > (real)0 && sw != (real)0) {
+          const real f = sw * rw / t;
+#pragma unroll
+          for (int i = 0; i < 4; ++i) ax[k][i] += f * sF[i];
+        }
+      }
     }
-    if (sh != 0) {
+    real pa[G][4], pb[G][4];
+    matvec2_s<real, G>(Pa, ca, pa);
+    if (!fake) {
+      matvec2_s<real, G>(Pb, cb, pb);
+    } else {
+#pragma unroll
+      for (int k = 0; k < G; ++k)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) pb[k][i] = 1;
+    }
+    real ua[G][4], ub[G][4];
+#pragma unroll
+    for (int k = 0; k < G; ++k) {
+      const int sh = sx[k] - sa[k] - sb[k];
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
-        ua[k][i] = Scale<real>::shift(ua[k][i], sh);
-        ub[k][i] = Scale<real>::shift(ub[k][i], sh);
+        ua[k][i] = ax[k][i] * pb[k][i];
+        ub[k][i] = ax[k][i] * pa[k][i];
+      }
+      if (sh != 0) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          ua[k][i] = Scale<real>::shift(ua[k][i], sh);
+          ub[k][i] = Scale<real>::shift(ub[k][i], sh);
+        }
       }
     }
     // d/dt of P(t r) c = r Q P(t r) c
+    {
+      real qa[G][4];
+      matvec_q<real, G>(sQ, pa, qa);
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const real qa = sQ[4 * i] * pa[k][0] + sQ[4 * i + 1] * pa[k][1] + sQ[4 * i + 2] * pa[k][2] + sQ[4 * i + 3] * pa[k][3];
-      ga[k / kPPLBase] += ua[k][i] * qa;
+      for (int k = 0; k < G; ++k)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) ga[(grp * G + k) / kPPLBase] += ua[k][i] * qa[k][i];
       if (!fake) {
-        const real qb = sQ[4 * i] * pb[k][0] + sQ[4 * i + 1] * pb[k][1] + sQ[4 * i + 2] * pb[k][2] + sQ[4 * i + 3] * pb[k][3];
-        gb[k / kPPLBase] += ub[k][i] * qb;
+        real qb[G][4];
+        matvec_q<real, G>(sQ, pb, qb);
+#pragma unroll
+        for (int k = 0; k < G; ++k)
+#pragma unroll
+          for (int i = 0; i < 4; ++i) gb[(grp * G + k) / kPPLBase] += ub[k][i] * qb[k][i];
       }
     }
-  }
-  if (op.out_a >= 0) {
-    real na[PPL][4];
-    matvec2_ts<real, PPL>(Pa, ua, na);
-    real *d = msg + (size_t)op.out_a * N * (R * 4) + lane_off;
+    if (op.out_a >= 0) {
+      real na[G][4];
+      matvec2_ts<real, G>(Pa, ua, na);
+      real *d = msg + (size_t)op.out_a * N * (R * 4) + off;
 #pragma unroll
-    for (int k = 0; k < PPL; ++k) Vec<real>::store(d + (size_t)k * PPW * (R * 4), na[k]);
-  }
-  if (op.out_b >= 0) {
-    real nb[PPL][4];
-    matvec2_ts<real, PPL>(Pb, ub, nb);
-    real *d = msg + (size_t)op.out_b * N * (R * 4) + lane_off;
+      for (int k = 0; k < G; ++k) Vec<real>::store(d + (size_t)k * PPW * (R * 4), na[k]);
+    } else if constexpr (WALK) {
+      if (op.out_a == -2) {
+        real na[G][4];
+        matvec2_ts<real, G>(Pa, ua, na);
 #pragma unroll
-    for (int k = 0; k < PPL; ++k) Vec<real>::store(d + (size_t)k * PPW * (R * 4), nb[k]);
+        for (int k = 0; k < G; ++k)
+#pragma unroll
+          for (int i = 0; i < 4; ++i) carry[grp * G + k][i] = na[k][i];
+      }
+    }
+    if (op.out_b >= 0) {
+      real nb[G][4];
+      matvec2_ts<real, G>(Pb, ub, nb);
+      real *d = msg + (size_t)op.out_b * N * (R * 4) + off;
+#pragma unroll
+      for (int k = 0; k < G; ++k) Vec<real>::store(d + (size_t)k * PPW * (R * 4), nb[k]);
+    } else if constexpr (WALK) {
+      if (op.out_b == -2) {
+        real nb[G][4];
+        matvec2_ts<real, G>(Pb, ub, nb);
+#pragma unroll
+        for (int k = 0; k < G; ++k)
+#pragma unroll
+          for (int i = 0; i < 4; ++i) carry[grp * G + k][i] = nb[k][i];
+      }
+    }
   }
   // per-unit edge terms, reduced in a fixed order by op_reduce_kernel
   if constexpr (UPU == 1) {
@@ -397,12 +625,14 @@ template <typename real, int R, int THREADS, int MINB, int PPL>
 __global__ void __launch_bounds__(THREADS, MINB) backward_kernel(const SweepParams p, int op_begin) {
   constexpr int WPB = THREADS / 32;
   __shared__ __align__(16) real sPw[WPB][2 * R * PLayout<real>::kRow];
-  __shared__ real sQw[WPB][16 + 4 + 2 * R];
+  __shared__ __align__(16) real sQw[WPB][ModelSlice<R>::kSize];
   const int unit = blockIdx.x * WPB + (threadIdx.x >> 5);
   if (unit >= p.n_units / (PPL / kPPLBase)) return;  // whole warp
   const int opi = op_begin + blockIdx.y;
-  backward_op<real, R, PPL>(p, load_bwd_op(p.bwd_ops, opi), opi, p.msg_slots, unit, sPw[threadIdx.x >> 5],
-                            sQw[threadIdx.x >> 5], threadIdx.x & 31);
+  real unused[PPL][4];  // the level schedule passes no message in registers
+  backward_op<real, R, PPL, AdjGroup<THREADS, MINB, PPL>::G>(p, load_bwd_op(p.bwd_ops, opi), opi, p.msg_slots, unit,
+                                                             sPw[threadIdx.x >> 5], sQw[threadIdx.x >> 5],
+                                                             threadIdx.x & 31, unused);
 }
 
 // The whole adjoint sweep in one launch: each warp walks walk_bwd_ops (the
@@ -413,15 +643,33 @@ __global__ void __launch_bounds__(THREADS, MINB) backward_walk_kernel(const Swee
                                                                        int unit_end) {
   constexpr int WPB = THREADS / 32;
   __shared__ __align__(16) real sPw[WPB][2 * R * PLayout<real>::kRow];
-  __shared__ real sQw[WPB][16 + 4 + 2 * R];
+  __shared__ __align__(16) real sQw[WPB][ModelSlice<R>::kSize];
   const int unit = unit_begin + blockIdx.x * WPB + (threadIdx.x >> 5);
   if (unit >= unit_end) return;  // whole warp
   const int lane = threadIdx.x & 31;
-  for (int i = 0; i < p.n_walk_bwd; ++i) {
+  real *sQ = sQw[threadIdx.x >> 5];
+  // a warp's patterns belong to one partition for the whole walk
+  stage_model<real, R>(p, p.unit_part[unit * (PPL / kPPLBase)], sQ, lane);
+  constexpr int PPW = 32 / R;
+  const size_t g0 = (size_t)unit * PPW * PPL + lane / R;
+  const int n = p.n_walk_bwd;
+  real carry[PPL][4];  // a message passed to the next op in registers
+  // the children of op i+2 are asked for in L2 after op i, a whole op
+  // before they are read
+  if (n > 0) {
+    const int4 h = __ldg(reinterpret_cast<const int4 *>(p.walk_bwd_ops));  // x, a, b, ea
+    prefetch_child<real, R, PPL>(p, h.y, g0, lane % R, PPW);
+    prefetch_child<real, R, PPL>(p, h.z, g0, lane % R, PPW);
+  }
+  for (int i = 0; i < n; ++i) {
+    int4 h = make_int4(-1, -1, -1, -1);
+    if (i + 1 < n) h = __ldg(reinterpret_cast<const int4 *>(p.walk_bwd_ops + i + 1));
     __syncwarp();  // every lane is done with the previous op's staged values
-    const BwdOp op = load_bwd_op(p.walk_bwd_ops, i);
-    backward_op<real, R, PPL>(p, op, op.pad0, p.walk_msg_slots, unit, sPw[threadIdx.x >> 5], sQw[threadIdx.x >> 5],
-                              lane);
+    const BwdOp op = load_bwd_op<true>(p.walk_bwd_ops, i);
+    backward_op<real, R, PPL, AdjGroup<THREADS, MINB, PPL>::G, true>(p, op, op.pad0, p.walk_msg_slots, unit,
+                                                                     sPw[threadIdx.x >> 5], sQ, lane, carry);
+    prefetch_child<real, R, PPL>(p, h.y, g0, lane % R, PPW);
+    prefetch_child<real, R, PPL>(p, h.z, g0, lane % R, PPW);
   }
 }
 
@@ -738,7 +986,7 @@ int dispatch(int precision, int R, int shape, A &&...a) {
 
 // Walk shapes (one warp per block, so a chunk spreads evenly over the SMs):
 // {threads, minimum blocks per SM, forward and adjoint patterns per lane}.
-constexpr Shape kWalkShapes[] = {{32, 32, 4, 2}, {32, 24, 4, 2}, {32, 16, 4, 4}};
+constexpr Shape kWalkShapes[] = {{32, 32, 4, 2}, {32, 24, 4, 2}, {32, 16, 4, 4}, {32, 19, 4, 4}, {32, 20, 4, 4}};
 constexpr int kNumWalkShapes = sizeof(kWalkShapes) / sizeof(kWalkShapes[0]);
 
 template <template <typename, int, int, int, int, int> class F, class... A>
@@ -746,6 +994,8 @@ int dispatch_walk(int w, A &&...a) {
   switch (w) {
     case 1: return F<float, 4, 32, 24, 4, 2>::run(a...);
     case 2: return F<float, 4, 32, 16, 4, 4>::run(a...);
+    case 3: return F<float, 4, 32, 19, 4, 4>::run(a...);
+    case 4: return F<float, 4, 32, 20, 4, 4>::run(a...);
     default: return F<float, 4, 32, 32, 4, 2>::run(a...);
   }
 }

@@ -33,10 +33,13 @@ struct alignas(32) FwdOp {
 // per inner child (out_a / out_b: message slot, or -1) and adds its two edge
 // gradient terms. seed: displayed-tree root slot whose tree weight seeds x,
 // or -1. A message buffer is reused only by levels launched after the level
-// that read it.
+// that read it. msg0..msg2 repeat the first three message slots, so a sweep
+// reads them with the op instead of through the slot list. In the walk
+// schedule out_a / out_b = -2 keeps that message in registers for the next
+// op, whose pad4 = 1 (its only message).
 struct alignas(64) BwdOp {
   int32_t x, a, b, ea, eb, seed, out_a, out_b;
-  int32_t msg_begin, msg_count, pad0, pad1, pad2, pad3, pad4, pad5;
+  int32_t msg_begin, msg_count, pad0, msg0, msg1, msg2, pad4, pad5;
 };
 
 struct DevPartition {

@@ -95,13 +95,18 @@ __device__ __forceinline__ FwdOp load_fwd_op(const FwdOp *ops, int i) {
   return o;
 }
 
+// FULL: also the inline message slots msg1, msg2 and pad4 (the walk
+// schedule's fields); otherwise they read as -1 / 0.
+template <bool FULL = false>
 __device__ __forceinline__ BwdOp load_bwd_op(const BwdOp *ops, int i) {
   const int4 *q = reinterpret_cast<const int4 *>(ops + i);
   const int4 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2);
+  const int4 d = FULL ? __ldg(q + 3) : make_int4(-1, -1, 0, 0);
   BwdOp o;
   o.x = a.x; o.a = a.y; o.b = a.z; o.ea = a.w;
   o.eb = b.x; o.seed = b.y; o.out_a = b.z; o.out_b = b.w;
-  o.msg_begin = c.x; o.msg_count = c.y; o.pad0 = c.z; o.pad1 = c.w; o.pad2 = o.pad3 = o.pad4 = o.pad5 = 0;
+  o.msg_begin = c.x; o.msg_count = c.y; o.pad0 = c.z; o.msg0 = c.w; o.msg1 = d.x; o.msg2 = d.y;
+  o.pad4 = d.z; o.pad5 = d.w;
   return o;
 }
 

@@ -28,6 +28,13 @@ namespace {
 
 thread_local std::string g_create_error;
 
+// Copies an adjoint op's first three message slots (already appended to
+// `slots` from op.msg_begin on) into the op itself.
+void set_inline_msgs(BwdOp &op, const std::vector<int32_t> &slots) {
+  int32_t *inl[3] = {&op.msg0, &op.msg1, &op.msg2};
+  for (int m = 0; m < 3; ++m) *inl[m] = m < op.msg_count ? slots[op.msg_begin + m] : -1;
+}
+
 #define CUDA_OK(expr)                                                                     \
   do {                                                                                    \
     cudaError_t _e = (expr);                                                              \
@@ -451,6 +458,7 @@ void netlk_ctx::build_schedules(int segments) {
         msg_slots.push_back(m.second);
         read_here.push_back(m.second);
       }
+      set_inline_msgs(op, msg_slots);
       pending[x].clear();
       bwd.push_back(op);
       bwd_var.push_back(x);
@@ -563,15 +571,27 @@ void netlk_ctx::build_walk(const std::vector<char> &inb, const std::vector<int> 
   for (size_t j = 0; j < bwd.size(); ++j) level_index[bwd_var[j]] = (int)j;
   std::vector<std::vector<std::pair<int32_t, int32_t>>> pending(V);
   std::vector<int> free_slots;
-  for (auto it = order.rbegin(); it != order.rend(); ++it) {
-    const int x = *it;
-    if (!inb[x]) continue;
+  // adjoint walk order, and how many adjoint ops send a message to each variant
+  std::vector<int> radj;
+  for (auto it = order.rbegin(); it != order.rend(); ++it)
+    if (inb[*it]) radj.push_back(*it);
+  std::vector<int> n_senders(V, 0);
+  for (int x : radj)
+    for (int i = 0; i < 2; ++i)
+      if (dag.vars[x].ref[i] >= 0) n_senders[dag.vars[x].ref[i]]++;
+  int carried_to = -1;  // variant whose only message the previous op kept in registers
+  for (size_t j = 0; j < radj.size(); ++j) {
+    const int x = radj[j];
+    const int y = j + 1 < radj.size() ? radj[j + 1] : -1;
     BwdOp op = bwd[level_index[x]];  // a, b still variant ids (= CLV slots here)
     op.pad0 = level_index[x];
+    op.pad4 = x == carried_to;  // the adjoint starts from the message in registers
+    carried_to = -1;
     op.msg_begin = (int32_t)wmsg_slots.size();
     op.msg_count = (int32_t)pending[x].size();
     std::sort(pending[x].begin(), pending[x].end());
     for (const auto &m : pending[x]) wmsg_slots.push_back(m.second);
+    set_inline_msgs(op, wmsg_slots);
     auto alloc_slot = [&]() {
       if (!free_slots.empty()) {
         const int sl = free_slots.back();
@@ -581,11 +601,20 @@ void netlk_ctx::build_walk(const std::vector<char> &inb, const std::vector<int> 
       return n_wadj++;
     };
     op.out_a = op.out_b = -1;
-    if (op.a >= 0) {
+    // a child that is the next op and hears from no other op gets its
+    // message in registers (out = -2)
+    auto keep = [&](int32_t c) { return c >= 0 && c == y && n_senders[c] == 1 && op.a != op.b; };
+    if (keep(op.a)) {
+      op.out_a = -2;
+      carried_to = op.a;
+    } else if (op.a >= 0) {
       op.out_a = alloc_slot();
       pending[op.a].push_back({x, op.out_a});
     }
-    if (op.b >= 0) {
+    if (keep(op.b)) {
+      op.out_b = -2;
+      carried_to = op.b;
+    } else if (op.b >= 0) {
       op.out_b = alloc_slot();
       pending[op.b].push_back({x, op.out_b});
     }

@@ -265,7 +265,7 @@ class NetworkLikelihood:
                                            cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), 6), self._h)
         return {k: (float(ms[i]), int(cnt[i])) for i, k in enumerate(self.KERNELS)}
 
-    def tuning(self, n=16):
+    def tuning(self, n=32):
         fs, bs = ctypes.c_int32(), ctypes.c_int32()
         fm, bm = np.zeros(n), np.zeros(n)
         N.check(N.lib().netlk_tuning(self._h, ctypes.byref(fs), ctypes.byref(bs), _ptr(fm, ctypes.c_double),
