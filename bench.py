@@ -159,7 +159,7 @@ class ClockSampler:
 # counted). Keyed by sweep, schedule (level: one launch per DAG level; walk:
 # one warp walks the whole DAG), precision and states.
 TRAFFIC_PER_UPDATE = {"forward_level_fp32_4": 102.3, "backward_level_fp32_4": 295.9,
-                      "backward_walk_fp32_4": 220.3}
+                      "forward_walk_fp32_4": 85.8, "backward_walk_fp32_4": 221.7}
 
 
 def cpu_port_rate(w, n_sample, steps, warmup, variant):
