@@ -454,6 +454,38 @@ __device__ __forceinline__ void put_row(const float (&v)[20], int m, int l, unsi
   }
 }
 
+// Asks L2 for the DRAM data of adjoint item (op, tile g0): its children's
+// CLV rows (or tip state masks), its own CLV at a displayed-tree root, the
+// scale counters and the incoming messages. All CTAs of a level move through
+// their items in step, so without this each item's loads arrive as one burst
+// the whole GPU waits for; issued an item ahead they stream in while the
+// current item's MMAs and epilogues run.
+__device__ __forceinline__ void prefetch_item20(const SweepParams &p, const BwdOp &op, size_t g0) {
+  const size_t N = (size_t)p.n_patterns;
+  const int t = threadIdx.x;
+  auto pf = [](const void *a) { asm volatile("prefetch.global.L2 [%0];" ::"l"(a)); };
+  auto rows = [&](const float *base) {  // 128 rows x 320 B = 320 lines of 128 B
+    const char *b = reinterpret_cast<const char *>(base + g0 * 80);
+    pf(b + 128 * t);
+    if (t < 320 - kTThreads) pf(b + 128 * (t + kTThreads));
+  };
+  const float *clv = static_cast<const float *>(p.clv);
+  const int32_t refs[2] = {op.a, op.b};
+  for (int c = 0; c < 2; ++c) {
+    const int32_t ref = refs[c];
+    if (ref >= 0) {
+      rows(clv + (size_t)ref * N * 80);
+      if (t < 4) pf(p.scaler + (size_t)ref * N + g0 + 32 * t);
+    } else if (ref != INT32_MIN && t < 4) {
+      pf(p.tips32 + (size_t)(-1 - ref) * N + g0 + 32 * t);
+    }
+  }
+  if (t >= 4 && t < 8) pf(p.scaler + (size_t)op.x * N + g0 + 32 * (t - 4));
+  if (op.seed >= 0) rows(clv + (size_t)op.x * N * 80);
+  const float *msg = static_cast<const float *>(p.msg);
+  for (int mi = 0; mi < op.msg_count; ++mi) rows(msg + (size_t)__ldg(p.msg_slots + op.msg_begin + mi) * N * 80);
+}
+
 __global__ void __launch_bounds__(kTThreads, 1)
     backward20_tc_kernel(const SweepParams p, int op_begin, int n_ops, int n_tiles) {
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -474,7 +506,7 @@ __global__ void __launch_bounds__(kTThreads, 1)
   const int item_begin = (int)(W * blockIdx.x / gridDim.x), item_end = (int)(W * (blockIdx.x + 1) / gridDim.x);
 
   if (warp == 0) tc::tmem_alloc(tc::smem_u32(tmem_slot), 512);
-  if (threadIdx.x == 0) tc::mbar_init(tc::smem_u32(mbar), 1);
+  if (threadIdx.x == 0) tc::mbar_init(tc::smem_u32(mbar), 2);  // one commit per child's issuing thread
   for (int i = threadIdx.x; i < 4 * kTM; i += kTThreads)
     *reinterpret_cast<float4 *>(sA + (i / kTM) * kHBytes + 10 * kAChunk + (i % kTM) * 16) = make_float4(0, 0, 0, 0);
   for (int i = threadIdx.x; i < (kBwdB1 + kBBytes + kBwdB2) / 16; i += kTThreads)
@@ -498,6 +530,11 @@ __global__ void __launch_bounds__(kTThreads, 1)
     const size_t g0 = (size_t)tile * kTM, g = g0 + m;
     const BwdOp op = load_bwd_op(p.bwd_ops, opi);
     const int ka = child_kind(op.a), kb = child_kind(op.b);
+    if (item + 1 < item_end) {
+      const int noi = (item + 1) / n_tiles;
+      prefetch_item20(p, noi == oi ? op : load_bwd_op(p.bwd_ops, op_begin + noi),
+                      (size_t)(item + 1 - noi * n_tiles) * kTM);
+    }
     const int part = p.unit_part[g0 / 16];  // partitions are padded to whole 256-pattern blocks
     if (oi != staged_op || part != staged_part) {
       stage_b_adj(p, sB1, sBQ, sB2, part, op.ea, kb == kAbsent ? -1 : op.eb, part != staged_part);
@@ -509,7 +546,17 @@ __global__ void __launch_bounds__(kTThreads, 1)
     // displayed-tree seed: w_s rw_r pi_i / L_s with L_s summed over all rates
     float tseed = 0.f, sw = 0.f;
     if (op.seed >= 0) {
-      const float *cx = clv + ((size_t)op.x * N + g) * 80 + 40 * hh;
+      // the thread's 2 rates x 20 states: 160 contiguous bytes as 10 vector loads
+      const float4 *cx4 = reinterpret_cast<const float4 *>(clv + ((size_t)op.x * N + g) * 80 + 40 * hh);
+      float cx[40];
+#pragma unroll
+      for (int j = 0; j < 10; ++j) {
+        const float4 v = cx4[j];
+        cx[4 * j] = v.x;
+        cx[4 * j + 1] = v.y;
+        cx[4 * j + 2] = v.z;
+        cx[4 * j + 3] = v.w;
+      }
       float part_t = 0.f;
 #pragma unroll
       for (int l = 0; l < 2; ++l) {
@@ -531,12 +578,14 @@ __global__ void __launch_bounds__(kTThreads, 1)
       put_half(p, kb, op.b, g0, h, sA + 2 * kHBytes, sA + 3 * kHBytes);
       tc::fence_proxy_async();
       __syncthreads();
-      if (threadIdx.x == 0) {
+      // child c's MMAs are issued by thread 32c: the two children's
+      // accumulators are disjoint, and each issuer commits its own MMAs to
+      // the mbarrier (two arrivals per round)
+      if ((threadIdx.x & 31) == 0 && threadIdx.x < 64) {
         tc::fence_after_sync();
-#pragma unroll 1
-        for (int c = 0; c < 2; ++c) {
-          const int kind = c ? kb : ka;
-          if (kind == kAbsent) continue;
+        const int c = threadIdx.x >> 5;
+        const int kind = c ? kb : ka;
+        if (kind != kAbsent) {
           const uint64_t dah = tc::smem_desc(tc::smem_u32(sA + (2 * c) * kHBytes), kAChunk, 128);
           const uint64_t dal = dah + (kHBytes >> 4);
           const uint64_t dq = tc::smem_desc(tc::smem_u32(sBQ), kBChunk, 128);
@@ -556,7 +605,7 @@ __global__ void __launch_bounds__(kTThreads, 1)
             }
           }
         }
-        tc::commit(tc::smem_u32(mbar));
+        tc::commit(tc::smem_u32(mbar));  // arrives at once when this thread issued nothing
       }
       // adjoint of x for (pattern g, rate r): incoming messages + seed
       float ax[20];
@@ -610,11 +659,10 @@ __global__ void __launch_bounds__(kTThreads, 1)
       tc::fence_before_sync();
       __syncthreads();
       // ------------------------------------------------- round 2: P_r^T u
-      if (threadIdx.x == 0) {
+      if ((threadIdx.x & 31) == 0 && threadIdx.x < 64) {
         tc::fence_after_sync();
-#pragma unroll 1
-        for (int c = 0; c < 2; ++c) {
-          if ((c ? kb : ka) == kAbsent) continue;
+        const int c = threadIdx.x >> 5;
+        if ((c ? kb : ka) != kAbsent) {
           const uint64_t dah = tc::smem_desc(tc::smem_u32(sA + (2 * c) * kHBytes), kAChunk, 128);
           const uint64_t dal = dah + (kHBytes >> 4);
 #pragma unroll
@@ -629,7 +677,7 @@ __global__ void __launch_bounds__(kTThreads, 1)
             }
           }
         }
-        tc::commit(tc::smem_u32(mbar));
+        tc::commit(tc::smem_u32(mbar));  // arrives at once when this thread issued nothing
       }
       ok = tc::mbar_wait(tc::smem_u32(mbar), phase);
       phase ^= 1;

@@ -454,9 +454,10 @@ def test_adjoint_launch_shapes_agree(monkeypatch):
     from netrax_gb300.likelihood import NetworkLikelihood
     w = synth.config(1, scale=0.02)
     res = {}
-    # 12-14: walk shapes (the whole sweep in one launch per chunk of units)
+    # 12-16: walk shapes (the whole sweep in one launch per chunk of units;
+    # CLVs and single messages handed between consecutive ops in registers)
     for shapes in ("0,0", "0,5", "0,6", "5,2", "6,4", "7,7", "8,8", "9,9", "10,10", "11,11", "12,12", "13,13",
-                   "14,14", "1,12", "12,10"):
+                   "14,14", "15,15", "16,16", "13,16", "1,12", "12,10"):
         monkeypatch.setenv("NETLK_SHAPES", shapes)
         with NetworkLikelihood(w.network, w.partitions, precision="fp32") as lik:
             res[shapes] = lik.loglikelihood_gradient()  # the first evaluation fixes the shapes
