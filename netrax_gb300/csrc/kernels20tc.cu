@@ -409,18 +409,31 @@ __device__ __forceinline__ void stage_b_adj(const SweepParams &p, unsigned char 
   }
 }
 
-// Child rows of one rate half (columns 40h .. 40h+39) into an A tile pair.
-__device__ __forceinline__ void put_half(const SweepParams &p, int kind, int32_t ref, size_t g0, int h,
-                                         unsigned char *sAh, unsigned char *sAl) {
+// Child rows of one rate half (columns 40h .. 40h+39) into registers: CLV
+// float4s of an inner child, the state masks (in .x) of a tip. Both
+// children are fetched before either is stored, so their loads overlap.
+__device__ __forceinline__ void fetch_half(const SweepParams &p, int kind, int32_t ref, size_t g0, int h,
+                                           float4 (&x)[5]) {
   const size_t N = (size_t)p.n_patterns;
   if (kind == kInner) {
     const float *src = static_cast<const float *>(p.clv) + ((size_t)ref * N + g0) * 80 + 40 * h;
-    float4 x[5];
 #pragma unroll
     for (int i = 0; i < 5; ++i) {
       const int f = threadIdx.x + i * kTThreads, m = f / 10, kc = f - m * 10;
       x[i] = __ldg(reinterpret_cast<const float4 *>(src + (size_t)m * 80) + kc);
     }
+  } else if (kind == kTip) {
+    const uint32_t *code = p.tips32 + (size_t)(-1 - ref) * N + g0;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) x[i].x = __uint_as_float(__ldg(code + (threadIdx.x + i * kTThreads) / 10));
+  }
+}
+
+// The fetched half rows into an A tile pair: split hi / lo for an inner
+// child, 0/1 expansion of the mask (local columns 4kc.. = states 4(kc%5)..)
+// for a tip.
+__device__ __forceinline__ void put_half(int kind, const float4 (&x)[5], unsigned char *sAh, unsigned char *sAl) {
+  if (kind == kInner) {
 #pragma unroll
     for (int i = 0; i < 5; ++i) {
       const int f = threadIdx.x + i * kTThreads, m = f / 10, kc = f - m * 10, off = kc * kAChunk + m * 16;
@@ -430,11 +443,10 @@ __device__ __forceinline__ void put_half(const SweepParams &p, int kind, int32_t
       *reinterpret_cast<float4 *>(sAl + off) = lo;
     }
   } else if (kind == kTip) {
-    const uint32_t *code = p.tips32 + (size_t)(-1 - ref) * N + g0;
 #pragma unroll
     for (int i = 0; i < 5; ++i) {
       const int f = threadIdx.x + i * kTThreads, m = f / 10, kc = f - m * 10;
-      const uint32_t b = __ldg(code + m) >> (4 * (kc % 5));  // local columns 4kc.. = states 4(kc%5)..
+      const uint32_t b = __float_as_uint(x[i].x) >> (4 * (kc % 5));
       *reinterpret_cast<float4 *>(sAh + kc * kAChunk + m * 16) =
           make_float4((float)(b & 1u), (float)((b >> 1) & 1u), (float)((b >> 2) & 1u), (float)((b >> 3) & 1u));
     }
@@ -574,8 +586,13 @@ __global__ void __launch_bounds__(kTThreads, 1)
     for (int h = 0; h < 2; ++h) {
       const int r = 2 * h + hh;  // this thread's rate in this half
       // ---------------------------------------------------- round 1: p and Q c
-      put_half(p, ka, op.a, g0, h, sA, sA + kHBytes);
-      put_half(p, kb, op.b, g0, h, sA + 2 * kHBytes, sA + 3 * kHBytes);
+      {
+        float4 xa[5], xb[5];
+        fetch_half(p, ka, op.a, g0, h, xa);
+        fetch_half(p, kb, op.b, g0, h, xb);
+        put_half(ka, xa, sA, sA + kHBytes);
+        put_half(kb, xb, sA + 2 * kHBytes, sA + 3 * kHBytes);
+      }
       tc::fence_proxy_async();
       __syncthreads();
       // child c's MMAs are issued by thread 32c: the two children's
