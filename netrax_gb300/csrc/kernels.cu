@@ -362,8 +362,8 @@ __global__ void __launch_bounds__(THREADS, MINB) forward_walk_kernel(const Sweep
     if (i + 1 < n) h = __ldg(reinterpret_cast<const int4 *>(p.walk_fwd_ops + i + 1));  // out, a, b, ea
     __syncwarp();  // every lane is done with the previous op's P
     forward_op<real, R, PPL, true>(p, load_fwd_op(p.walk_fwd_ops, i), unit, sP, lane, &carry);
-    // the next op's children: a variant written long before (not the op
-    // just computed) comes from DRAM
+    // the next op's children are asked for in L2 as this op ends (a child
+    // written long before, not the one just computed, may be in DRAM)
     prefetch_child<real, R, PPL>(p, h.y, g0, lane % R, PPW);
     prefetch_child<real, R, PPL>(p, h.z, g0, lane % R, PPW);
   }
@@ -654,8 +654,8 @@ __global__ void __launch_bounds__(THREADS, MINB) backward_walk_kernel(const Swee
   const size_t g0 = (size_t)unit * PPW * PPL + lane / R;
   const int n = p.n_walk_bwd;
   real carry[PPL][4];  // a message passed to the next op in registers
-  // the children of op i+2 are asked for in L2 after op i, a whole op
-  // before they are read
+  // the next op's children are asked for in L2 as each op ends (the first
+  // op's before the loop)
   if (n > 0) {
     const int4 h = __ldg(reinterpret_cast<const int4 *>(p.walk_bwd_ops));  // x, a, b, ea
     prefetch_child<real, R, PPL>(p, h.y, g0, lane % R, PPW);
