@@ -206,6 +206,22 @@ int netlk_dag_export(const netlk_ctx *ctx, int32_t *node_of_variant,
 int netlk_root_export(const netlk_ctx *ctx, int32_t *root_variant,
                       int32_t *dtroot_variant, double *logprob);
 
+/* Walk schedule export, for checks of the host schedule. No counterpart in
+ * the reference (introspection of this library's single-launch sweeps).
+ * Counts: n_fwd forward ops, n_bwd adjoint ops, n_slot_reads message-slot
+ * reads; all 0 when the context has no walk schedule (20 states, or more
+ * than one checkpoint segment; FP64 contexts have one but run the level
+ * sweeps). Arrays (NULL: counts only):
+ *   fwd_variant [n_fwd]   variant computed by each forward op, in walk order
+ *   bwd_ops [6 * n_bwd]   per adjoint op in walk order: variant x, message
+ *                         slot written for child a and for child b (-1 none,
+ *                         -2 kept in registers for the next op), 1 if its
+ *                         only message comes from the previous op's
+ *                         registers, first index into slot_reads, count
+ *   slot_reads [n_slot_reads]  message slots the adjoint ops read */
+int netlk_walk_export(const netlk_ctx *ctx, int32_t *n_fwd, int32_t *n_bwd, int32_t *n_slot_reads,
+                      int32_t *fwd_variant, int32_t *bwd_ops, int32_t *slot_reads);
+
 /* ----------------------------------------------------- parameter updates */
 /* Replace linked_branch_lengths (src/optimization/NetworkState.cpp:93-306). */
 int netlk_set_branch_lengths(netlk_ctx *ctx, const double *branch_lengths,

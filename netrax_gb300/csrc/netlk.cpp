@@ -1327,6 +1327,27 @@ int netlk_dag_export(const netlk_ctx *ctx, int32_t *node_of_variant, int32_t *ch
   return NETLK_OK;
 }
 
+int netlk_walk_export(const netlk_ctx *ctx, int32_t *n_fwd, int32_t *n_bwd, int32_t *n_slot_reads,
+                      int32_t *fwd_variant, int32_t *bwd_ops, int32_t *slot_reads) {
+  if (!ctx) return NETLK_ERR_INVALID_ARGUMENT;
+  const bool w = ctx->walk_ok;
+  if (n_fwd) *n_fwd = w ? (int32_t)ctx->wfwd.size() : 0;
+  if (n_bwd) *n_bwd = w ? (int32_t)ctx->wbwd.size() : 0;
+  if (n_slot_reads) *n_slot_reads = w ? (int32_t)ctx->wmsg_slots.size() : 0;
+  if (!w) return NETLK_OK;
+  if (fwd_variant)
+    for (size_t i = 0; i < ctx->wfwd.size(); ++i) fwd_variant[i] = ctx->wfwd[i].out;
+  if (bwd_ops)
+    for (size_t i = 0; i < ctx->wbwd.size(); ++i) {
+      const BwdOp &o = ctx->wbwd[i];
+      const int32_t row[6] = {o.x, o.out_a, o.out_b, o.pad4, o.msg_begin, o.msg_count};
+      for (int k = 0; k < 6; ++k) bwd_ops[6 * i + k] = row[k];
+    }
+  if (slot_reads)
+    for (size_t i = 0; i < ctx->wmsg_slots.size(); ++i) slot_reads[i] = ctx->wmsg_slots[i];
+  return NETLK_OK;
+}
+
 int netlk_root_export(const netlk_ctx *ctx, int32_t *root_variant, int32_t *dtroot_variant, double *logprob) {
   if (!ctx) return NETLK_ERR_INVALID_ARGUMENT;
   netlk_ctx *c = const_cast<netlk_ctx *>(ctx);

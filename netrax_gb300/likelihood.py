@@ -231,6 +231,22 @@ class NetworkLikelihood:
                                           _ptr(lp, ctypes.c_double)), self._h)
         return rv, dt, lp
 
+    def walk_export(self):
+        """The walk schedule of the single-launch sweeps: (forward variants in
+        walk order, adjoint ops [n, 6] = (variant, slot out a, slot out b,
+        message from registers, first slot read, slot reads), slot reads);
+        empty arrays when the context has no walk schedule."""
+        nf, nb, ns = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        N.check(N.lib().netlk_walk_export(self._h, ctypes.byref(nf), ctypes.byref(nb), ctypes.byref(ns),
+                                          None, None, None), self._h)
+        fwd = np.zeros(max(1, nf.value), np.int32)
+        bwd = np.zeros(max(1, 6 * nb.value), np.int32)
+        slots = np.zeros(max(1, ns.value), np.int32)
+        N.check(N.lib().netlk_walk_export(self._h, ctypes.byref(nf), ctypes.byref(nb), ctypes.byref(ns),
+                                          _ptr(fwd, ctypes.c_int32), _ptr(bwd, ctypes.c_int32),
+                                          _ptr(slots, ctypes.c_int32)), self._h)
+        return fwd[:nf.value], bwd[:6 * nb.value].reshape(nb.value, 6), slots[:ns.value]
+
     def get_clv(self, variant, part):
         n = self.n_patterns[part]
         clv = np.zeros(n * self.rate_cats * self.states)

@@ -200,3 +200,94 @@ def test_checkpoint_segments_reduce_clv_slots():
     # automatic mode on a host-only context stores everything
     auto = NetworkLikelihood(w.network, w.partitions, host_only=True).stats
     assert auto["checkpoint_segments"] == 1
+
+
+def _check_walk(lik):
+    """Invariants of the single-launch (walk) schedules, from the exported
+    schedule and the DAG: the forward walk is a topological order of every
+    variant; the adjoint walk visits the variants reachable from the
+    displayed-tree roots, each before its children; every message is written
+    to a slot no unread message holds, and read exactly once, by its child; a
+    message kept in registers goes to the very next op, whose only message
+    it is."""
+    node, ch, ed, cov = lik.dag_export()
+    rv, dt, lp = lik.root_export()[:3]
+    fwd, bwd, slots = lik.walk_export()
+    V = len(node)
+    assert sorted(fwd.tolist()) == list(range(V))
+    pos = {int(v): i for i, v in enumerate(fwd)}
+    for v in range(V):
+        for c in ch[v]:
+            if c >= 0:
+                assert pos[int(c)] < pos[v], "child computed after its parent"
+    # variants the adjoint reaches: displayed-tree roots and their descendants
+    reach, stack = set(), [int(x) for x in dt]
+    while stack:
+        v = stack.pop()
+        if v in reach:
+            continue
+        reach.add(v)
+        stack.extend(int(c) for c in ch[v] if c >= 0)
+    xs = [int(r[0]) for r in bwd]
+    assert sorted(xs) == sorted(reach)
+    bpos = {x: i for i, x in enumerate(xs)}
+    senders = {v: 0 for v in range(V)}
+    for x in xs:
+        for c in ch[x]:
+            if c >= 0:
+                assert bpos[x] < bpos[int(c)], "adjoint of a child before its parent"
+                senders[int(c)] += 1
+    held = {}        # slot -> (sender, receiver) of the unread message it holds
+    received = {x: 0 for x in xs}
+    carried_to = None
+    for i, (x, out_a, out_b, from_regs, begin, count) in enumerate(bwd.tolist()):
+        if from_regs:
+            assert carried_to == x and count == 0 and senders[x] == 1
+            received[x] += 1
+        else:
+            assert carried_to is None
+        carried_to = None
+        for s in slots[begin:begin + count].tolist():
+            assert s in held and held[s][1] == x, "message read by the wrong op"
+            del held[s]
+            received[x] += 1
+        for c, out in zip(ch[x].tolist(), (out_a, out_b)):
+            if c < 0:
+                assert out == -1
+            elif out == -2:
+                assert i + 1 < len(xs) and xs[i + 1] == c and senders[c] == 1
+                carried_to = c
+            else:
+                assert out >= 0 and out not in held, "slot overwritten before it was read"
+                held[out] = (x, c)
+    assert not held, "messages never read"
+    assert all(received[x] == senders[x] for x in xs)
+
+
+@pytest.mark.parametrize("case", CASES, ids=lambda c: c["name"])
+def test_walk_schedule_invariants(case):
+    net = parse_extended_newick(case["newick"])
+    parts = [GoldenPartition(d) for d in case["partitions"]]
+    lik = NetworkLikelihood(net, parts, host_only=True)
+    if parts[0].states == 4:
+        _check_walk(lik)
+    else:  # 20-state contexts run level sweeps only
+        fwd, bwd, slots = lik.walk_export()
+        assert len(fwd) == len(bwd) == len(slots) == 0
+    lik.close()
+
+
+@pytest.mark.parametrize("cfg", [1, 2])
+def test_walk_schedule_invariants_synthetic(cfg):
+    """The 50-taxon / 4-reticulation and 100-taxon / 8-reticulation networks
+    (947 variants); with checkpoint segments there is no walk schedule."""
+    from netrax_gb300 import synth
+    w = synth.config(cfg, scale=0.002)
+    lik = NetworkLikelihood(w.network, w.partitions, host_only=True)
+    _check_walk(lik)
+    fwd, bwd, slots = lik.walk_export()
+    assert (bwd[:, 1] == -2).sum() + (bwd[:, 2] == -2).sum() == bwd[:, 3].sum() > 0
+    lik.close()
+    seg = NetworkLikelihood(w.network, w.partitions, host_only=True, checkpoint_segments=2)
+    assert all(len(a) == 0 for a in seg.walk_export())
+    seg.close()
