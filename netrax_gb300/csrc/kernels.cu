@@ -829,12 +829,19 @@ __global__ void op_reduce_kernel(int n_bx, const double *__restrict__ partial, d
   const double2 *src = reinterpret_cast<const double2 *>(partial) + (size_t)op * n_bx;
   const float4 *src32 = reinterpret_cast<const float4 *>(src);
   double a = 0.0, b = 0.0;
-  for (int i = threadIdx.x; i < n_bx; i += blockDim.x) {
-    if (ff) {
+  if (ff) {
+    // float-float sums (about 48 bits; no FP64 instruction per element: GB300
+    // runs FP64 at a small fraction of its FP32 rate), one double per thread
+    FF fa{0.f, 0.f}, fb{0.f, 0.f};
+    for (int i = threadIdx.x; i < n_bx; i += blockDim.x) {
       const float4 v = src32[i];
-      a += ff_to_double(make_float2(v.x, v.y));
-      b += ff_to_double(make_float2(v.z, v.w));
-    } else {
+      fa = ff_add(fa, FF{v.x, v.y});
+      fb = ff_add(fb, FF{v.z, v.w});
+    }
+    a = ff_to_double(make_float2(fa.hi, fa.lo));
+    b = ff_to_double(make_float2(fb.hi, fb.lo));
+  } else {
+    for (int i = threadIdx.x; i < n_bx; i += blockDim.x) {
       const double2 v = src[i];
       a += v.x;
       b += v.y;
