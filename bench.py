@@ -52,6 +52,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=16384, help="patterns in the CPU sample")
     ap.add_argument("--scale", type=float, default=1.0, help="site-count scale (1.0 = full workload)")
+    ap.add_argument("--op", default="eval", choices=["eval", "edge"],
+                    help="eval: logL + gradient evaluations (the headline); edge: the branch-length "
+                         "optimizer's per-edge calls (incremental edge logL, edge derivatives)")
     ap.add_argument("--config", type=int, default=2, choices=[1, 2, 3, 4],
                     help="1: 50 taxa / 4 reticulations / 10 uneven DNA partitions (75.5k sites); "
                          "2: 100 taxa / 8 reticulations / 100k DNA sites (the headline workload); "
@@ -464,11 +467,81 @@ def run_batch(args, ws, rank, local):
         lk.close()
 
 
+def run_edge(args, ws, rank, local):
+    """The branch-length optimizer's per-edge calls on one context, host
+    synchronous like its Newton-Raphson loop (BranchLengthOptimization.cpp:
+    171-200, VirtualRerooting.cpp:348-585): a full logL after every length
+    changed, netlk_edge_loglikelihood (only the variants above the edge are
+    recomputed) and netlk_edge_derivatives (d1 from the adjoint sweep, d2 by a
+    central difference of d1)."""
+    import torch
+    from netrax_gb300 import synth
+    from netrax_gb300.likelihood import NetworkLikelihood
+    torch.cuda.set_device(local)
+    w = synth.config(args.config, scale=args.scale)
+    lik = NetworkLikelihood(w.network, w.partitions, variant=args.variant, precision=args.precision,
+                            device=local)
+    E = lik.n_edges
+    base = np.array(w.network.branch_lengths, np.float64)
+    rng = np.random.default_rng(2000 + rank)
+    lik.loglikelihood_gradient()  # launch-shape autotuning and a full sweep
+    K, W = args.steps, max(3, args.warmup)
+
+    def full_once(k):
+        lik.set_branch_lengths(np.clip(base * np.exp(0.05 * rng.standard_normal(E)), 1e-6, 100.0))
+        return lik.loglikelihood()
+
+    for k in range(W):
+        full_once(k)
+    t = time.perf_counter()
+    nf = max(3, K // 10)
+    for k in range(nf):
+        full_once(k)
+    full_s = (time.perf_counter() - t) / nf
+    full_updates = lik.last_site_updates()
+
+    edges = [(k * 37) % E for k in range(K + W)]
+    for k in range(W):
+        lik.edge_loglikelihood(edges[k], base[edges[k]] * 1.01)
+    t = time.perf_counter()
+    upd = 0
+    for k in range(K):
+        e = edges[W + k]
+        lik.edge_loglikelihood(e, base[e] * (1.0 + 0.02 * ((k % 5) - 2)))
+        upd += lik.last_site_updates()
+    edge_s = (time.perf_counter() - t) / K
+
+    nd = max(3, K // 10)
+    lik.edge_derivatives(edges[0])
+    t = time.perf_counter()
+    for k in range(nd):
+        lik.edge_derivatives(edges[k])
+    der_s = (time.perf_counter() - t) / nd
+    lik.close()
+    if rank == 0:
+        line = {
+            "metric": "edge logL evals/s (incremental) & edge derivative evals/s",
+            "value": 1.0 / edge_s, "unit": "edge logL evals/s", "n_gpus": ws, "steps": K, "warmup": W,
+            "ms_per_step": edge_s * 1000.0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32" if args.precision == "fp32" else "f64", "data": "synthetic",
+            "config": {"workload": w.name, "taxa": w.network.n_tips, "reticulations": w.network.n_reticulations,
+                       "sites": w.n_sites, "patterns": w.n_patterns, "edges": E, "variant": args.variant,
+                       "precision": args.precision, "timing": "host wall clock around synchronous calls"},
+            "edge_logl_ms": edge_s * 1000.0,
+            "mean_site_updates_per_edge_eval": upd / K,
+            "full_logl_ms": full_s * 1000.0, "full_site_updates": full_updates,
+            "edge_derivatives_ms": der_s * 1000.0, "edge_derivatives_per_s": 1.0 / der_s,
+        }
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     ws, rank, local = dist_init()
     if args.impl == "reference":
         run_reference(args, ws, rank)
+    elif args.op == "edge":
+        run_edge(args, ws, rank, local)
     elif args.config == 4:
         run_batch(args, ws, rank, local)
     else:

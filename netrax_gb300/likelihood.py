@@ -306,9 +306,11 @@ class NetworkLikelihood:
 def compute_loglikelihood(lik: NetworkLikelihood, incremental=1, update_pmatrices=1):
     """Same role and arguments as the reference's ``computeLoglikelihood``.
 
-    Every call recomputes the P-matrices and all displayed-tree CLVs on the GPU
-    (a full sweep costs less than the reference's validity bookkeeping), so
-    ``incremental`` and ``update_pmatrices`` only exist for call-site parity.
+    The context keeps the branch lengths its stored CLVs were computed with;
+    with its ``incremental`` option on (the default) a call recomputes only
+    the variants above the changed edges, otherwise every CLV. The P-matrices
+    are recomputed on the GPU at every call, so the two arguments only exist
+    for call-site parity.
     """
     del incremental, update_pmatrices
     return lik.loglikelihood()
