@@ -628,9 +628,11 @@ __global__ void __launch_bounds__(THREADS, MINB) backward_kernel(const SweepPara
   __shared__ __align__(16) real sQw[WPB][ModelSlice<R>::kSize];
   const int unit = blockIdx.x * WPB + (threadIdx.x >> 5);
   if (unit >= p.n_units / (PPL / kPPLBase)) return;  // whole warp
-  const int opi = op_begin + blockIdx.y;
+  const BwdOp op = load_bwd_op(p.bwd_ops, op_begin + blockIdx.y);
   real unused[PPL][4];  // the level schedule passes no message in registers
-  backward_op<real, R, PPL, AdjGroup<THREADS, MINB, PPL>::G>(p, load_bwd_op(p.bwd_ops, opi), opi, p.msg_slots, unit,
+  // op.pad0: the op's grad_partial row (its index in the full schedule, also
+  // when a subset of the ops is launched)
+  backward_op<real, R, PPL, AdjGroup<THREADS, MINB, PPL>::G>(p, op, op.pad0, p.msg_slots, unit,
                                                              sPw[threadIdx.x >> 5], sQw[threadIdx.x >> 5],
                                                              threadIdx.x & 31, unused);
 }

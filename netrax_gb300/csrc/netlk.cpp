@@ -144,13 +144,19 @@ struct netlk_ctx {
   int64_t dev_bytes = 0;
   DevBuf d_clv, d_scaler, d_adj, d_msg_slots, d_tips, d_weights, d_unit_part, d_fwd, d_bwd, d_rfwd, d_ifwd;
   DevBuf d_wfwd, d_wbwd, d_wmsg_slots;
+  // one edge's derivative: the adjoint ops its terms depend on (the ops that
+  // use the edge and every op above them), run through the level kernel
+  std::vector<std::vector<int32_t>> bwd_parents;  // adjoint op -> ops that send it a message
+  std::vector<BwdOp> ibwd;
+  std::vector<int32_t> ibwd_level_begin;
+  DevBuf d_ibwd;
   DevBuf d_pmat64, d_pmat32, d_lambda, d_U, d_Uinv, d_rates, d_rw, d_freqs, d_Q, d_brlen;
   // FP32 contexts: float copies the sweeps read (weights as hi/lo pairs)
   DevBuf d_weights32, d_model32, d_seeds32;
   size_t m32_freqs = 0, m32_rw = 0, m32_rates = 0;  // offsets (floats) in d_model32; Q at 0
   DevBuf d_site_partial, d_tree_logl, d_root_slot, d_root_lp, d_root_dlp, d_seeds, d_wts, d_dret;
   DevBuf d_slot_begin, d_slot_roots, d_parts, d_out, d_grad_partial, d_grad, d_edge_begin, d_edge_entries, d_op_sum;
-  PinnedBuf h_brlen, h_root_lp, h_root_dlp, h_out, h_grad, h_tree, h_ifwd;
+  PinnedBuf h_brlen, h_root_lp, h_root_dlp, h_out, h_grad, h_tree, h_ifwd, h_ibwd;
   cudaGraphExec_t graph_logl = nullptr, graph_grad = nullptr, graph_partials = nullptr,
                   graph_mixbwd = nullptr;
   bool probs_dirty = true, model_dirty = true;
@@ -294,6 +300,10 @@ struct netlk_ctx {
   // logL recomputing only the CLVs above changed branch lengths; false when a
   // full evaluation is needed instead
   bool run_incremental();
+  // d logL / d t_e from an incremental forward and the adjoint ops edge e's
+  // terms depend on, bit-identical to the full gradient's entry; false where
+  // the full evaluation is needed instead
+  bool edge_d1_partial(int e, double *d1);
   void prepare_state();  // model / probabilities uploads and launch-shape tuning
   void prepare();        // prepare_state + branch-length upload
   void finish(double *total, double *part_logl, double *d_brlen, double *d_ret);
@@ -494,10 +504,13 @@ void netlk_ctx::build_schedules(int segments) {
     bwd_level_begin.push_back((int32_t)bwd.size());
   }
   build_walk(inb, slot_of, by_level, bwd_var);
-  for (BwdOp &op : bwd) {  // variant ids -> CLV slots
+  for (size_t j = 0; j < bwd.size(); ++j) {  // variant ids -> CLV slots
+    BwdOp &op = bwd[j];
     op.a = map_ref(op.a);
     op.b = map_ref(op.b);
+    op.pad0 = (int32_t)j;  // the op's grad_partial row, wherever it is launched from
   }
+  bwd_parents.clear();
   bwd_launches = 0;
   for (int L = 0; L < dag.n_levels; ++L) bwd_launches += bwd_level_begin[L + 1] > bwd_level_begin[L];
   // edge -> (adjoint op, side) entries for the gradient reduction
@@ -696,6 +709,7 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
     d_wmsg_slots.alloc(std::max<size_t>(1, wmsg_slots.size()) * 4, dev_bytes);
   }
   d_ifwd.alloc(fwd.size() * sizeof(FwdOp), dev_bytes);
+  d_ibwd.alloc(std::max<size_t>(1, bwd.size()) * sizeof(BwdOp), dev_bytes);
   const size_t nm = (size_t)P * topo.n_edges * R * S * S;
   d_pmat64.alloc(nm * 8, dev_bytes);
   if (opts.precision == NETLK_FP32) d_pmat32.alloc(nm * 4, dev_bytes);
@@ -788,6 +802,7 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
   h_grad.alloc(topo.n_edges * 8);
   h_tree.alloc((size_t)n_slots * P * 8);
   h_ifwd.alloc(fwd.size() * sizeof(FwdOp));
+  h_ibwd.alloc(std::max<size_t>(1, bwd.size()) * sizeof(BwdOp));
 }
 
 void netlk_ctx::upload_model() {
@@ -995,6 +1010,57 @@ bool netlk_ctx::run_incremental() {
   launches += 3 + n_launch;
   clv_brlen = brlen;
   last_updates = (int64_t)ifwd.size() * N;
+  return true;
+}
+
+bool netlk_ctx::edge_d1_partial(int e, double *d1) {
+  if (S != 4 || bwd.empty() || n_segments != 1 || !opts.incremental || device_brlen || profiling) return false;
+  prepare();
+  if (!run_incremental()) return false;
+  const int nb = (int)bwd.size();
+  if (bwd_parents.empty()) {  // with one segment CLV slots are variant ids
+    std::vector<int32_t> op_of(dag.vars.size(), -1);
+    for (int j = 0; j < nb; ++j) op_of[bwd[j].x] = j;
+    bwd_parents.assign(nb, {});
+    for (int j = 0; j < nb; ++j)
+      for (int32_t c : {bwd[j].a, bwd[j].b})
+        if (c >= 0 && op_of[c] >= 0) bwd_parents[op_of[c]].push_back(j);
+  }
+  // the ops using edge e, closed upward: every message such an op reads comes
+  // from an op that runs in this call (parents precede children in bwd)
+  std::vector<char> need(nb, 0);
+  for (int j = 0; j < nb; ++j) need[j] = bwd[j].ea == e || (bwd[j].b != kFake && bwd[j].eb == e);
+  for (int j = nb - 1; j >= 0; --j)
+    if (need[j])
+      for (int32_t q : bwd_parents[j]) need[q] = 1;
+  ibwd.clear();
+  ibwd_level_begin.assign(1, 0);
+  int n_launch = 0;
+  for (int L = 0; L < dag.n_levels; ++L) {
+    for (int j = bwd_level_begin[L]; j < bwd_level_begin[L + 1]; ++j)
+      if (need[j]) ibwd.push_back(bwd[j]);  // pad0 keeps its grad_partial row
+    ibwd_level_begin.push_back((int32_t)ibwd.size());
+    n_launch += ibwd_level_begin[L + 1] > ibwd_level_begin[L];
+  }
+  std::memcpy(h_ibwd.p, ibwd.data(), ibwd.size() * sizeof(BwdOp));
+  CUDA_OK(cudaMemcpyAsync(d_ibwd.p, h_ibwd.p, ibwd.size() * sizeof(BwdOp), cudaMemcpyHostToDevice, stream));
+  SweepParams bp = sweep();
+  bp.bwd_ops = d_ibwd.as<BwdOp>();
+  launch_backward(stream, opts.precision, R, bwd_lshape, bp, ibwd_level_begin.data(), dag.n_levels);
+  // rows of the ops not run hold older values: only edge e's sum is read
+  launch_grad_reduce(stream, nb, topo.n_edges, n_units, d_edge_begin.as<int32_t>(), d_edge_entries.as<int32_t>(),
+                     d_grad_partial.as<double>(), d_op_sum.as<double>(), d_grad.as<double>(),
+                     opts.precision == NETLK_FP32);
+  launches += n_launch + 2;
+  const int nout = 3 + P + topo.n_ret;
+  CUDA_OK(cudaMemcpyAsync(h_out.p, d_out.p, nout * 8, cudaMemcpyDeviceToHost, stream));
+  CUDA_OK(cudaMemcpyAsync(h_grad.p, d_grad.as<double>() + e, 8, cudaMemcpyDeviceToHost, stream));
+  CUDA_OK(cudaStreamSynchronize(stream));
+  CUDA_OK(cudaGetLastError());
+  const double *o = h_out.as<double>();
+  if (o[1] != 0.0 || !std::isfinite(o[0]))
+    throw Error(NETLK_ERR_NUMERIC, "Invalid network likelihood: negative infinity or NaN");
+  *d1 = h_grad.as<double>()[0];
   return true;
 }
 
@@ -1514,6 +1580,8 @@ int netlk_edge_derivatives(netlk_ctx *ctx, int32_t edge, int32_t mode, double *d
     // first derivative at the context's current lengths
     auto first = [&]() -> double {
       if (mode == 1) return reference_edge_d1(ctx, edge);
+      double d;
+      if (ctx->edge_d1_partial(edge, &d)) return d;
       std::vector<double> g(ctx->topo.n_edges);
       double tot;
       ctx->prepare();

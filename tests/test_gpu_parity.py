@@ -502,3 +502,37 @@ def test_walk_sweeps_in_several_chunks(monkeypatch):
     for t, g, r in res.values():
         assert t == t0
         assert np.array_equal(g, g0) and np.array_equal(r, r0)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_edge_derivatives_from_partial_adjoint(precision):
+    """netlk_edge_derivatives mode 0 runs an incremental forward and only the
+    adjoint ops the edge's terms depend on; its d1 is the full gradient's
+    entry bit for bit, and d2 the central difference of two full gradients."""
+    from netrax_gb300 import synth
+    from netrax_gb300.likelihood import NetworkLikelihood
+    w = synth.config(1, scale=0.02)
+    net = w.network
+    with NetworkLikelihood(net, w.partitions, precision=precision) as lik:
+        logl0, g0, _ = lik.loglikelihood_gradient()
+        base = np.array(net.branch_lengths, np.float64)
+        ret_edges = [int(x) for x in net.ret_first_edge] + [int(x) for x in net.ret_second_edge]
+        tip_edges = [e for e in range(lik.n_edges) if int(net.edge_child[e]) < net.n_tips][:2]
+        inner = [e for e in range(lik.n_edges) if e not in ret_edges and e not in tip_edges][:3]
+        for e in ret_edges[:2] + tip_edges + inner:
+            d1 = lik.edge_derivatives(e, second=False)
+            assert d1 == g0[e]
+            d1b, d2 = lik.edge_derivatives(e, second=True)
+            assert d1b == g0[e]
+            h = 1e-6
+            hm = base[e] - max(base[e] - h, 1e-6)
+            b = base.copy()
+            b[e] = base[e] + h
+            lik.set_branch_lengths(b)
+            gp = lik.loglikelihood_gradient()[1][e]
+            b[e] = base[e] - hm
+            lik.set_branch_lengths(b)
+            gm = lik.loglikelihood_gradient()[1][e]
+            lik.set_branch_lengths(base)
+            assert d2 == (gp - gm) / (h + hm)
+            assert lik.loglikelihood() == logl0
