@@ -24,6 +24,11 @@ What it restates (file:line cites the NetRAX sources, path within the project):
   not vendor (the ``libs/raxml-ng`` submodule is empty): GTR eigensystem,
   P = U diag(exp(lambda r t)) U^-1, Yang (1994) mean discrete-Gamma rates,
   Felsenstein pruning with per-site 2^256 scaling, root log-likelihood.
+* ``derivatives.py`` - the per-edge branch-length derivatives of
+  ``src/likelihood/LikelihoodDerivatives.cpp:13-344`` (per-tree sumtable
+  derivatives at the edge, AVERAGE / BEST combination, the ``isActiveBranch``
+  restriction of ``src/helper/EdgeHelper.cpp:84-95``) and the exact gradient of
+  the network log-likelihood, analytic in both cases.
 * ``naive.py``    - the naive per-displayed-tree evaluator of
   ``src/likelihood/NaiveLoglikelihood.cpp:35-115`` (branch lengths merged across
   unary nodes as in ``src/helper/NetworkFunctions.cpp:132-226``), an

@@ -1,0 +1,92 @@
+"""GPU: gradients and edge derivatives against the oracle's analytic derivatives.
+
+``tests/golden/derivative_cases.json`` holds, per golden case, the derivatives
+that ``oracle/derivatives.py`` computes the reference's way (per-tree sumtable
+derivatives at the edge, combined by ``LikelihoodDerivatives.cpp``'s
+formulas; pinned on CPU against finite differences in
+``test_oracle_derivatives.py``). Through the C ABI:
+
+* the adjoint gradient (``netlk_loglikelihood_gradient``): FP64 within 1e-8
+  relative (plus 1e-9 of the largest entry), FP32 within 1e-4 relative (plus
+  1e-4 of the largest entry), for every branch length and reticulation
+  probability;
+* ``netlk_edge_derivatives`` mode 0 (true derivative) and mode 1 (the
+  reference's formula), FP64: d1 within 1e-8 relative on every edge; d2 - a
+  central difference of d1 over +-1e-6 - within 1e-4 relative where the
+  length is at least 1e-3 (nearer the 1e-6 clamp the difference is one-sided).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, GoldenPartition, golden_cases
+
+pytestmark = pytest.mark.gpu
+
+CASES = {c["name"]: c for c in golden_cases()}
+with open(os.path.join(GOLDEN, "derivative_cases.json")) as _f:
+    DERIVS = {c["name"]: c for c in json.load(_f)["cases"]}
+NAMES = sorted(DERIVS)
+
+
+def _lik(name, variant, precision):
+    from netrax_gb300.likelihood import NetworkLikelihood
+    from netrax_gb300.network import parse_extended_newick
+    case = CASES[name]
+    net = parse_extended_newick(case["newick"])
+    parts = [GoldenPartition(d) for d in case["partitions"]]
+    return NetworkLikelihood(net, parts, variant=variant, precision=precision)
+
+
+def _close(got, want, rel, abs_frac):
+    got, want = np.asarray(got, float), np.asarray(want, float)
+    scale = max(1.0, float(np.abs(want).max())) if want.size else 1.0
+    err = np.abs(got - want)
+    ok = err <= rel * np.abs(want) + abs_frac * scale
+    return bool(ok.all()), float((err / np.maximum(np.abs(want), scale * 1e-3)).max()) if want.size else 0.0
+
+
+@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("variant", ["AVERAGE", "BEST"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_gradient_matches_analytic_oracle(name, variant, precision):
+    want = DERIVS[name][variant]
+    rel, absf = (1e-8, 1e-9) if precision == "fp64" else (1e-4, 1e-4)
+    with _lik(name, variant, precision) as lik:
+        _, gb, gr = lik.loglikelihood_gradient()
+    ok, worst = _close(gb, want["grad_brlen"], rel, absf)
+    print("%s %s %s brlen worst relative error %.2e" % (name, variant, precision, worst))
+    assert ok, worst
+    if len(want["grad_retprob"]):
+        ok, worst = _close(gr, want["grad_retprob"], rel, absf)
+        print("%s %s %s retprob worst relative error %.2e" % (name, variant, precision, worst))
+        assert ok, worst
+
+
+@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("variant", ["AVERAGE", "BEST"])
+@pytest.mark.parametrize("mode", [0, 1])
+def test_edge_derivatives_match_analytic_oracle(name, variant, mode):
+    want = DERIVS[name][variant]
+    key = "true" if mode == 0 else "reference"
+    w1 = np.array(want["d1_" + key])
+    w2 = np.array(want["d2_" + key])
+    with _lik(name, variant, "fp64") as lik:
+        lengths = lik.branch_lengths.copy()
+        got1, got2 = [], []
+        for e in range(lik.n_edges):
+            d1, d2 = lik.edge_derivatives(e, second=True, mode=mode)
+            got1.append(d1)
+            got2.append(d2)
+        # the context is left evaluating the network at its own lengths
+        assert lik.loglikelihood() == pytest.approx(CASES[name][variant]["logl"], rel=1e-9)
+    ok, worst = _close(got1, w1, 1e-8, 1e-9)
+    print("%s %s mode %d d1 worst relative error %.2e" % (name, variant, mode, worst))
+    assert ok, worst
+    far = lengths >= 1e-3
+    if far.any():
+        ok, worst = _close(np.array(got2)[far], w2[far], 1e-4, 1e-6)
+        print("%s %s mode %d d2 worst relative error %.2e" % (name, variant, mode, worst))
+        assert ok, worst
