@@ -508,7 +508,8 @@ def test_walk_sweeps_in_several_chunks(monkeypatch):
 def test_edge_derivatives_from_partial_adjoint(precision):
     """netlk_edge_derivatives mode 0 runs an incremental forward and only the
     adjoint ops the edge's terms depend on; its d1 is the full gradient's
-    entry bit for bit, and d2 the central difference of two full gradients."""
+    entry bit for bit, and d2 the central difference of two full gradients
+    (step 1e-6 in FP64, max(t/200, min(1e-4, (t - 1e-6)/3)) in FP32)."""
     from netrax_gb300 import synth
     from netrax_gb300.likelihood import NetworkLikelihood
     w = synth.config(1, scale=0.02)
@@ -524,15 +525,17 @@ def test_edge_derivatives_from_partial_adjoint(precision):
             assert d1 == g0[e]
             d1b, d2 = lik.edge_derivatives(e, second=True)
             assert d1b == g0[e]
-            h = 1e-6
-            hm = base[e] - max(base[e] - h, 1e-6)
+            t = base[e]
+            h = max(t / 200.0, min(1e-4, (t - 1e-6) / 3.0)) if precision == "fp32" else 1e-6
             b = base.copy()
-            b[e] = base[e] + h
+            b[e] = min(t + h, 100.0)
+            hp = b[e] - t
             lik.set_branch_lengths(b)
             gp = lik.loglikelihood_gradient()[1][e]
-            b[e] = base[e] - hm
+            b[e] = max(t - h, 1e-6)
+            hm = t - b[e]
             lik.set_branch_lengths(b)
             gm = lik.loglikelihood_gradient()[1][e]
             lik.set_branch_lengths(base)
-            assert d2 == (gp - gm) / (h + hm)
+            assert d2 == (gp - gm) / (hp + hm)
             assert lik.loglikelihood() == logl0
