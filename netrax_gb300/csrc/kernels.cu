@@ -604,6 +604,25 @@ __device__ __forceinline__ void backward_op(const SweepParams &p, const BwdOp &o
       }
     }
   }
+  // Every message slot is read by exactly one op, and the slot's next message
+  // rewrites the warp's whole range of it, so once all lanes have read them
+  // the incoming messages are dead: drop the warp's lines from L2 without
+  // writing them back to DRAM. The range is UNIT * R * 4 reals at a multiple
+  // of itself inside a slot of N * R * 4 reals (N is a multiple of 256
+  // patterns / R), all multiples of 128 bytes.
+  if (op.msg_count > 0) {
+    constexpr int kBytes = UNIT * R * 4 * (int)sizeof(real);
+    static_assert(kBytes % 128 == 0, "whole L2 lines per warp range");
+    __syncwarp();
+    for (int m = 0; m < op.msg_count; ++m) {
+      int slot;
+      if constexpr (WALK) slot = m == 0 ? op.msg0 : m == 1 ? op.msg1 : m == 2 ? op.msg2 : __ldg(msg_slots + op.msg_begin + m);
+      else slot = __ldg(msg_slots + op.msg_begin + m);
+      const char *base = reinterpret_cast<const char *>(msg + (size_t)slot * N * (R * 4)) + (size_t)unit * kBytes;
+      for (int l = lane; l < kBytes / 128; l += 32)
+        asm volatile("discard.global.L2 [%0], 128;" ::"l"(base + (size_t)l * 128) : "memory");
+    }
+  }
   // per-unit edge terms, reduced in a fixed order by op_reduce_kernel
   if constexpr (UPU == 1) {
     const real sa_ = warp_sum(ga[0] * sRate[r]);
