@@ -160,9 +160,11 @@ class ClockSampler:
 # dram__bytes_write.sum of the 100-taxon / 8-reticulation network at 0.3 of its
 # sites, scaled by updates; writes still dirty in L2 at a launch's end are not
 # counted). Keyed by sweep, schedule (level: one launch per DAG level; walk:
-# one warp walks the whole DAG), precision and states.
+# one warp walks the whole DAG), precision and states. The level figures were
+# captured before the adjoint dropped read messages from L2, so they are an
+# upper bound for the current level adjoint.
 TRAFFIC_PER_UPDATE = {"forward_level_fp32_4": 102.3, "backward_level_fp32_4": 295.9,
-                      "forward_walk_fp32_4": 85.8, "backward_walk_fp32_4": 221.7}
+                      "forward_walk_fp32_4": 85.8, "backward_walk_fp32_4": 213.3}
 
 
 def cpu_port_rate(w, n_sample, steps, warmup, variant):
