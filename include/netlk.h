@@ -336,9 +336,9 @@ int netlk_walk_shape_begin(const netlk_ctx *ctx, int32_t *first_walk_shape);
 
 /* ---------------------------------------------------- allocation-free mixing */
 /* No counterpart in the reference: an extra entry point for callers that
- * cannot allocate device memory - work recorded into a CUDA graph capture,
- * programs whose device memory belongs to another allocator or a fixed
- * budget, loops that must not synchronise on cudaMalloc / cudaFree.
+ * cannot allocate device memory: programs whose device memory belongs to
+ * another allocator or a fixed budget, and latency-bound loops that must not
+ * pay for cudaMalloc / cudaFree, which synchronise the device.
  *
  * Mixes displayed-tree site log-likelihoods into the network log-likelihood
  * exactly as netlk_loglikelihood mixes its own: per partition, AVERAGE =

@@ -1,11 +1,9 @@
 // Allocation-free mixing of displayed-tree site log-likelihoods.
 //
 // Who needs this: callers that must not allocate device memory themselves or
-// have it allocated on their behalf - code running while a CUDA graph is
-// being captured (an allocation there breaks the capture), programs whose
-// device memory is fully handed to another allocator or a fixed budget, and
-// latency-critical loops where cudaMalloc/cudaFree would synchronise the
-// device. They still pass every input and output buffer; the only working
+// have it allocated on their behalf - programs whose device memory is fully
+// handed to another allocator or a fixed budget, and latency-critical loops
+// where cudaMalloc/cudaFree would synchronise the device. They still pass every input and output buffer; the only working
 // memory this entry point needs - the per-(tree, partition) sums between its
 // two kernels - lives in the fixed array below, which is part of the loaded
 // library image on every GPU that loads it and stays there until exit.

@@ -1,9 +1,8 @@
 """The allocation-free mixing entry point against the context path.
 
 ``netlk_mix_site_loglikelihoods_noalloc`` serves callers that cannot allocate
-device memory (work recorded into a CUDA graph capture, memory owned by
-another allocator or a fixed budget, loops that must not synchronise on
-cudaMalloc). It works in a fixed device array inside the library, so this test
+device memory (memory owned by another allocator or a fixed budget, loops
+that must not pay for the device synchronisation of cudaMalloc). It works in a fixed device array inside the library, so this test
 only hands it input and output buffers. The per-site log-likelihoods of every
 displayed tree come from the oracle; the answer must equal what
 ``netlk_loglikelihood`` (the existing entry point, FP64 context) returns for
