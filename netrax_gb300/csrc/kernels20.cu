@@ -314,7 +314,9 @@ __global__ void __launch_bounds__(kWarps20 * 32) backward20_kernel(const SweepPa
   }
   ga = warp_sum(ga * rate);
   gb = warp_sum(gb * rate);
-  if (lane == 0) store_edge_terms<real>(p.grad_partial + ((size_t)opi * p.n_units + unit) * 2, ga, gb);
+  // row op.pad0: the op's index in the full schedule, also when a subset of
+  // the ops is launched (edge derivatives)
+  if (lane == 0) store_edge_terms<real>(p.grad_partial + ((size_t)op.pad0 * p.n_units + unit) * 2, ga, gb);
 }
 
 template <typename real, int R>

@@ -756,7 +756,9 @@ __global__ void __launch_bounds__(kTThreads, 1)
       }
       if ((lane & 15) == 0) {
         const size_t unit = g0 / 16 + (size_t)(m >> 4);
-        *reinterpret_cast<float4 *>(p.grad_partial + ((size_t)opi * p.n_units + unit) * 2) =
+        // row op.pad0: the op's index in the full schedule, also when a
+        // subset of the ops is launched (edge derivatives)
+        *reinterpret_cast<float4 *>(p.grad_partial + ((size_t)op.pad0 * p.n_units + unit) * 2) =
             make_float4(va.hi, va.lo, vb.hi, vb.lo);
       }
     }

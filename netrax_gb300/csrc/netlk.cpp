@@ -1014,7 +1014,7 @@ bool netlk_ctx::run_incremental() {
 }
 
 bool netlk_ctx::edge_d1_partial(int e, double *d1) {
-  if (S != 4 || bwd.empty() || n_segments != 1 || !opts.incremental || device_brlen || profiling) return false;
+  if (bwd.empty() || n_segments != 1 || !opts.incremental || device_brlen || profiling) return false;
   prepare();
   if (!run_incremental()) return false;
   const int nb = (int)bwd.size();
@@ -1046,7 +1046,12 @@ bool netlk_ctx::edge_d1_partial(int e, double *d1) {
   CUDA_OK(cudaMemcpyAsync(d_ibwd.p, h_ibwd.p, ibwd.size() * sizeof(BwdOp), cudaMemcpyHostToDevice, stream));
   SweepParams bp = sweep();
   bp.bwd_ops = d_ibwd.as<BwdOp>();
-  launch_backward(stream, opts.precision, R, bwd_lshape, bp, ibwd_level_begin.data(), dag.n_levels);
+  if (use_tc)
+    launch_backward20_tc(stream, bp, ibwd_level_begin.data(), dag.n_levels, sms);
+  else if (S == 20)
+    launch_sweep20(stream, opts.precision, R, true, bp, ibwd_level_begin.data(), dag.n_levels);
+  else
+    launch_backward(stream, opts.precision, R, bwd_lshape, bp, ibwd_level_begin.data(), dag.n_levels);
   // rows of the ops not run hold older values: only edge e's sum is read
   launch_grad_reduce(stream, nb, topo.n_edges, n_units, d_edge_begin.as<int32_t>(), d_edge_entries.as<int32_t>(),
                      d_grad_partial.as<double>(), d_op_sum.as<double>(), d_grad.as<double>(),
@@ -1058,6 +1063,8 @@ bool netlk_ctx::edge_d1_partial(int e, double *d1) {
   CUDA_OK(cudaStreamSynchronize(stream));
   CUDA_OK(cudaGetLastError());
   const double *o = h_out.as<double>();
+  if (use_tc && *reinterpret_cast<const int32_t *>(o + nout - 1) != 0)
+    throw Error(NETLK_ERR_TIMEOUT, "tensor-core sweep: an MMA completion wait timed out");
   if (o[1] != 0.0 || !std::isfinite(o[0]))
     throw Error(NETLK_ERR_NUMERIC, "Invalid network likelihood: negative infinity or NaN");
   *d1 = h_grad.as<double>()[0];

@@ -504,15 +504,17 @@ def test_walk_sweeps_in_several_chunks(monkeypatch):
         assert np.array_equal(g, g0) and np.array_equal(r, r0)
 
 
+@pytest.mark.parametrize("config", [1, 3], ids=["dna", "protein"])
 @pytest.mark.parametrize("precision", ["fp32", "fp64"])
-def test_edge_derivatives_from_partial_adjoint(precision):
+def test_edge_derivatives_from_partial_adjoint(precision, config):
     """netlk_edge_derivatives mode 0 runs an incremental forward and only the
     adjoint ops the edge's terms depend on; its d1 is the full gradient's
     entry bit for bit, and d2 the central difference of two full gradients
-    (step 1e-6 in FP64, max(t/200, min(1e-4, (t - 1e-6)/3)) in FP32)."""
+    (step 1e-6 in FP64, max(t/200, min(1e-4, (t - 1e-6)/3)) in FP32). DNA
+    (50 taxa, 10 partitions) and protein (40 taxa; FP32 on the tensor cores)."""
     from netrax_gb300 import synth
     from netrax_gb300.likelihood import NetworkLikelihood
-    w = synth.config(1, scale=0.02)
+    w = synth.config(config, scale=0.02)
     net = w.network
     with NetworkLikelihood(net, w.partitions, precision=precision) as lik:
         logl0, g0, _ = lik.loglikelihood_gradient()
