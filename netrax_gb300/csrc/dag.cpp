@@ -192,7 +192,8 @@ struct Compiler {
     Bits both = take(v, lc) & take(v, rc);
     const std::vector<int32_t> lv = D.node_vars[lc], rv = D.node_vars[rc];
     for (int32_t l : lv) {
-      const Bits &ls = set_of(l);
+      // a copy: add() below may grow D.vars and move the set a reference points to
+      const Bits ls = set_of(l);
       if (!ls.intersects(both)) continue;
       for (int32_t r : rv) {
         const Bits &rs = set_of(r);

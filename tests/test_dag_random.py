@@ -1,0 +1,150 @@
+"""CPU: the compiled displayed-tree DAG against the oracle on random networks.
+
+The reference's sample networks and the synthetic workloads place every
+reticulation between two tree edges. Here arcs may start or end on any edge,
+reticulation edges included, which produces reticulations directly below
+reticulations, arcs leaving reticulated subtrees and nodes that die in some
+configurations. For 60 seeded networks (4-14 taxa, 1-5 reticulations) the
+host-only context's DAG must equal the oracle's literal restatement of
+processNodeImproved node by node (variant order and covered configuration
+sets), with the same displayed-tree root variant and log-probability per root
+tree - or both must reject the network.
+"""
+import numpy as np
+import pytest
+
+from conftest import GoldenPartition
+from netrax_gb300.likelihood import NetworkLikelihood
+from netrax_gb300.network import parse_extended_newick
+
+
+def nasty_network(rng, n_taxa, n_ret, mean_brlen=0.1):
+    """Extended Newick of a random tree with n_ret arcs between any two edges."""
+    children, parents, length, prob = {}, {}, {}, {}
+    nid = n_taxa
+    lineages = list(range(n_taxa))
+    while len(lineages) > 1:
+        i, j = rng.choice(len(lineages), size=2, replace=False)
+        a, b = lineages[i], lineages[j]
+        v, nid = nid, nid + 1
+        children[v] = [a, b]
+        for c in (a, b):
+            length[(v, c)] = rng.exponential(mean_brlen)
+            parents[c] = [v]
+        lineages = [x for k, x in enumerate(lineages) if k not in (i, j)] + [v]
+    root = lineages[0]
+    is_ret = set()
+
+    def descendants(v):
+        out, st = set(), [v]
+        while st:
+            x = st.pop()
+            if x not in out:
+                out.add(x)
+                st.extend(children.get(x, []))
+        return out
+
+    added = 0
+    for _ in range(10000):
+        if added == n_ret:
+            break
+        edges = sorted(length)
+        (u, v), (x, y) = [edges[k] for k in rng.choice(len(edges), 2, replace=False)]
+        if u in descendants(y):
+            continue  # the arc would close a cycle
+        s, t = nid, nid + 1
+        nid += 2
+        for (p, c), new in (((u, v), s), ((x, y), t)):
+            L = length.pop((p, c))
+            f = rng.uniform()
+            children[p] = [new if k == c else k for k in children[p]]
+            children[new] = [c]
+            parents[c] = [new if k == p else k for k in parents[c]]
+            parents[new] = [p]
+            length[(p, new)] = f * L
+            length[(new, c)] = (1 - f) * L
+            if (p, c) in prob:  # a split reticulation edge keeps its probability
+                prob[(new, c)] = prob.pop((p, c))
+        children[s].append(t)
+        parents[t].append(s)
+        length[(s, t)] = rng.exponential(mean_brlen)
+        is_ret.add(t)
+        p1 = rng.uniform(0.2, 0.8)
+        prob[(x, t)] = p1
+        prob[(s, t)] = 1.0 - p1
+        added += 1
+    assert added == n_ret
+    ret_name = {t: "H%d" % (k + 1) for k, t in enumerate(sorted(is_ret))}
+    seen = set()
+
+    def emit(v, parent):
+        if v in is_ret:
+            tail = "#%s:%.17g::%.17g" % (ret_name[v], length[(parent, v)], prob[(parent, v)])
+            if v in seen:
+                return tail
+            seen.add(v)
+            return "(" + ",".join(emit(c, v) for c in children[v]) + ")" + tail
+        brl = "" if parent is None else ":%.17g" % length[(parent, v)]
+        if v < n_taxa:
+            return "T%d" % v + brl
+        return "(" + ",".join(emit(c, v) for c in children[v]) + ")" + brl
+
+    return emit(root, None) + ";"
+
+
+def _partition(rng, n_tips, n=6):
+    return GoldenPartition({"tip_states": rng.integers(1, 16, size=(n_tips, n)).tolist(),
+                            "weights": [1.0] * n, "freqs": [0.25, 0.25, 0.25, 0.25],
+                            "exch": [1.0] * 6, "alpha": 1.0})
+
+
+def _covered(cov_row, n_ret):
+    bits = set()
+    for w, word in enumerate(cov_row):
+        word = int(word)
+        for b in range(64):
+            if (word >> b) & 1 and w * 64 + b < (1 << n_ret):
+                bits.add(w * 64 + b)
+    return bits
+
+
+@pytest.mark.parametrize("seed", range(60))
+def test_random_network_dag_matches_oracle(seed):
+    from oracle import improved, newick as onewick, pllmath
+    rng = np.random.default_rng(5000 + seed)
+    n_taxa = int(rng.integers(4, 15))
+    n_ret = int(rng.integers(1, 6))
+    text = nasty_network(rng, n_taxa, n_ret)
+    part = _partition(rng, n_taxa)
+    onet = onewick.parse_newick(text)
+    opart = improved.Partition(part.tip_states, part.weights, part.freqs, part.exch,
+                               pllmath.gamma_rates_mean(part.alpha, 4))
+    orc = improved.ImprovedOracle(onet, [opart])
+    try:
+        orc.loglikelihood()
+        oracle_error = None
+    except RuntimeError as e:
+        oracle_error = str(e)
+    net = parse_extended_newick(text)
+    try:
+        lik = NetworkLikelihood(net, [part], host_only=True)
+    except Exception as e:  # the product must reject exactly what the oracle rejects
+        assert oracle_error is not None, (text, e)
+        return
+    assert oracle_error is None, (text, oracle_error)
+    node, _, _, cov = lik.dag_export()
+    got = {}
+    for i in range(len(node)):
+        got.setdefault(int(node[i]), []).append(_covered(cov[i], net.n_reticulations))
+    want = {v: [set(s) for s in sets] for v, sets in orc.dag_summary().items() if sets}
+    assert got == want, text
+    rv, dt, lp = lik.root_export()
+    trees = orc.root_trees()
+    assert len(trees) == len(rv)
+    for k, t in enumerate(trees):
+        assert lp[k] == pytest.approx(t.logprob, rel=1e-13, abs=1e-13)
+        if t.dtroot is None:
+            continue
+        dnode = int(node[dt[k]])
+        assert dnode == t.dtroot[0]
+        assert [i for i in range(len(node)) if node[i] == dnode].index(dt[k]) == t.dtroot[1]
