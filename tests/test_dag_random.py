@@ -8,7 +8,9 @@ configurations. For 60 seeded networks (4-14 taxa, 1-5 reticulations) the
 host-only context's DAG must equal the oracle's literal restatement of
 processNodeImproved node by node (variant order and covered configuration
 sets), with the same displayed-tree root variant and log-probability per root
-tree - or both must reject the network.
+tree - or both must reject the network - and its single-launch walk schedules
+must keep their invariants (topological order, message slots written before
+they are read and read once, register hand-offs to the next op only).
 """
 import numpy as np
 import pytest
@@ -16,6 +18,7 @@ import pytest
 from conftest import GoldenPartition
 from netrax_gb300.likelihood import NetworkLikelihood
 from netrax_gb300.network import parse_extended_newick
+from test_dag_abi import _check_walk
 
 
 def nasty_network(rng, n_taxa, n_ret, mean_brlen=0.1):
@@ -148,3 +151,5 @@ def test_random_network_dag_matches_oracle(seed):
         dnode = int(node[dt[k]])
         assert dnode == t.dtroot[0]
         assert [i for i in range(len(node)) if node[i] == dnode].index(dt[k]) == t.dtroot[1]
+    _check_walk(lik)
+    lik.close()
