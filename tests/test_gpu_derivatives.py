@@ -114,3 +114,43 @@ def test_fp32_edge_derivatives_match_analytic_oracle(name, variant, mode):
         err = np.abs(got[free, 1] - w2[free]) / np.maximum(1.0, np.abs(w2[free]))
         print("%s %s fp32 mode %d d2 worst error %.2e" % (name, variant, mode, err.max()))
         assert err.max() <= 4e-3, err.max()
+
+
+@pytest.mark.parametrize("seed", range(12))
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_random_networks_match_oracle(seed, precision):
+    """Random networks with arcs on any edge (reticulations below
+    reticulations, nodes that die in some configurations; the generator of
+    test_dag_random.py), 40 simulated-free random patterns: logL against the
+    DAG oracle (FP64 1e-9, FP32 1e-6) and the adjoint gradient against the
+    analytic derivative oracle (FP64 1e-8, FP32 1e-4 plus 1e-4 of the largest
+    entry), AVERAGE and BEST."""
+    from netrax_gb300.likelihood import NetworkLikelihood
+    from netrax_gb300.network import parse_extended_newick
+    from oracle import derivatives, improved, newick as onewick, pllmath
+    from test_dag_random import nasty_network
+    rng = np.random.default_rng(7000 + seed)
+    n_taxa = int(rng.integers(4, 16))
+    n_ret = int(rng.integers(1, 6))
+    text = nasty_network(rng, n_taxa, n_ret)
+    freqs = rng.dirichlet(np.ones(4))
+    part = GoldenPartition({"tip_states": rng.integers(1, 16, size=(n_taxa, 40)).tolist(),
+                            "weights": rng.integers(1, 4, size=40).astype(float).tolist(),
+                            "freqs": (freqs / freqs.sum()).tolist(),
+                            "exch": (rng.dirichlet(np.ones(6)) * 6).tolist(), "alpha": 0.7})
+    onet = onewick.parse_newick(text)
+    net = parse_extended_newick(text)
+    rel, absf = (1e-8, 1e-9) if precision == "fp64" else (1e-4, 1e-4)
+    for variant in ("AVERAGE", "BEST"):
+        opart = improved.Partition(part.tip_states, part.weights, part.freqs, part.exch,
+                                   pllmath.gamma_rates_mean(part.alpha, 4))
+        orc = improved.ImprovedOracle(onet, [opart], variant=variant)
+        want_logl = orc.loglikelihood()
+        g, gr = derivatives.EdgeDerivativeOracle(orc).gradient()
+        with NetworkLikelihood(net, [part], variant=variant, precision=precision) as lik:
+            total, gb, gbr = lik.loglikelihood_gradient()
+        assert total == pytest.approx(want_logl, rel=1e-9 if precision == "fp64" else 1e-6), text
+        ok, worst = _close(gb, g, rel, absf)
+        assert ok, (variant, worst, text)
+        ok, worst = _close(gbr, gr, rel, absf)
+        assert ok, (variant, worst, text)
