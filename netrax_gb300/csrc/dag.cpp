@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <cmath>
 #include <deque>
+#include <unordered_map>
 
 #include "../../include/netlk.h"
 #include "internal.hpp"
@@ -108,6 +109,18 @@ struct Compiler {
   Bits ALL, EMPTY;
   std::vector<Bits> first_mask, second_mask;
 
+  // Per node, owner[c] = index (in node_vars) of the variant whose set holds
+  // configuration c, or -1. The variant sets of a node are pairwise disjoint
+  // (every configuration displays at most one tree below a node), which turns
+  // the pairwise set intersections of the two-child step and of the root
+  // matching into one pass over the configurations; a node whose sets do
+  // overlap (owner_state 2) keeps the pairwise path. 0: not built yet.
+  std::vector<std::vector<int32_t>> owner;
+  std::vector<signed char> owner_state;
+  // the node being processed: hash of each variant set -> variant, for the
+  // equal-set check of add()
+  std::unordered_multimap<uint64_t, int32_t> node_sets;
+
   Compiler(const Topology &t, Dag &d) : T(t), D(d) {
     D.r = T.n_ret;
     n_trees = (size_t)1 << D.r;
@@ -142,13 +155,31 @@ struct Compiler {
   const Bits &set_of(int32_t ref) const { return is_tip_ref(ref) ? ALL : D.vars[ref].set; }
   int level_of(int32_t ref) const { return (ref >= 0) ? D.vars[ref].level : 0; }
 
+  const std::vector<int32_t> *owners(int node) {
+    if (owner_state[node] == 0) {
+      std::vector<int32_t> &o = owner[node];
+      o.assign(n_trees, -1);
+      owner_state[node] = 1;
+      const std::vector<int32_t> &vars = D.node_vars[node];
+      for (int32_t i = 0; i < (int32_t)vars.size(); ++i)
+        set_of(vars[i]).for_each([&](size_t c) {
+          if (o[c] >= 0) owner_state[node] = 2;
+          o[c] = i;
+        });
+    }
+    return owner_state[node] == 1 ? &owner[node] : nullptr;
+  }
+
   void add(int node, const Bits &set, int32_t r0, int e0, int32_t r1, int e1) {
     if (!set.any()) {
       D.n_degenerate++;
       return;
     }
-    for (int32_t v : D.node_vars[node])
-      if (D.vars[v].set == set) return;  // tree_already_present_and_fine
+    // tree_already_present_and_fine: an equal set at this node is kept once
+    const uint64_t h = set.hash();
+    for (auto it = node_sets.equal_range(h); it.first != it.second; ++it.first)
+      if (D.vars[it.first->second].set == set) return;
+    node_sets.emplace(h, (int32_t)D.vars.size());
     Variant var;
     var.node = node;
     var.ref[0] = r0;
@@ -191,14 +222,45 @@ struct Compiler {
     int rc = T.child(v, 1), re = T.cedge(v, 1);
     Bits both = take(v, lc) & take(v, rc);
     const std::vector<int32_t> lv = D.node_vars[lc], rv = D.node_vars[rc];
-    for (int32_t l : lv) {
-      // a copy: add() below may grow D.vars and move the set a reference points to
-      const Bits ls = set_of(l);
-      if (!ls.intersects(both)) continue;
-      for (int32_t r : rv) {
-        const Bits &rs = set_of(r);
-        if (!rs.intersects(both)) continue;
-        if (ls.intersects(rs)) add(v, ls & rs & both, l, le, r, re);
+    const std::vector<int32_t> *ol = owners(lc), *orr = owners(rc);
+    if (ol && orr) {
+      // the pairs (l, r) whose sets share a configuration, with l and r both
+      // meeting `both`, in the order of the nested loop below; each gets the
+      // configurations of `both` it holds (none: a degenerate pair, counted
+      // by add() like the nested loop's)
+      std::vector<char> lb(lv.size(), 0), rb(rv.size(), 0);
+      both.for_each([&](size_t c) {
+        if ((*ol)[c] >= 0) lb[(*ol)[c]] = 1;
+        if ((*orr)[c] >= 0) rb[(*orr)[c]] = 1;
+      });
+      std::unordered_map<int64_t, size_t> at;
+      std::vector<std::pair<int64_t, std::vector<uint32_t>>> pairs;
+      for (size_t c = 0; c < n_trees; ++c) {
+        const int32_t li = (*ol)[c], ri = (*orr)[c];
+        if (li < 0 || ri < 0 || !lb[li] || !rb[ri]) continue;
+        const int64_t key = (int64_t)li * (int64_t)rv.size() + ri;
+        auto ins = at.emplace(key, pairs.size());
+        if (ins.second) pairs.emplace_back(key, std::vector<uint32_t>());
+        if (both.test(c)) pairs[ins.first->second].second.push_back((uint32_t)c);
+      }
+      std::sort(pairs.begin(), pairs.end(),
+                [](const auto &a, const auto &b) { return a.first < b.first; });
+      for (const auto &pr : pairs) {
+        Bits s = EMPTY;
+        for (uint32_t c : pr.second) s.set(c);
+        const int64_t li = pr.first / (int64_t)rv.size(), ri = pr.first % (int64_t)rv.size();
+        add(v, s, lv[li], le, rv[ri], re);
+      }
+    } else {
+      for (int32_t l : lv) {
+        // a copy: add() below may grow D.vars and move the set a reference points to
+        const Bits ls = set_of(l);
+        if (!ls.intersects(both)) continue;
+        for (int32_t r : rv) {
+          const Bits &rs = set_of(r);
+          if (!rs.intersects(both)) continue;
+          if (ls.intersects(rs)) add(v, ls & rs & both, l, le, r, re);
+        }
       }
     }
     Bits rdead = dead_settings(v, rc);
@@ -245,9 +307,12 @@ struct Compiler {
   void run() {
     D.vars.clear();
     D.node_vars.assign(T.n_nodes, {});
+    owner.assign(T.n_nodes, {});
+    owner_state.assign(T.n_nodes, 0);
     for (int t = 0; t < T.n_tips; ++t) D.node_vars[t].push_back(tip_ref(t));
     for (int v : T.post_order) {
       if (v < T.n_tips) continue;
+      node_sets.clear();
       if (T.n_children(v) == 1)
         single(v);
       else
@@ -265,10 +330,21 @@ struct Compiler {
       size_t t0 = (size_t)D.vars[v].set.first();
       int dt = displayed_tree_root(t0);
       int found = -1, n_found = 0;
-      for (int32_t cand : D.node_vars[dt]) {
-        if (set_of(cand).intersects(D.vars[v].set)) {
-          found = cand;
-          n_found++;
+      if (const std::vector<int32_t> *od = owners(dt)) {
+        // the variants of dt meeting the root variant's set
+        std::vector<int32_t> hit;
+        D.vars[v].set.for_each([&](size_t c) {
+          const int32_t i = (*od)[c];
+          if (i >= 0 && std::find(hit.begin(), hit.end(), i) == hit.end()) hit.push_back(i);
+        });
+        n_found = (int)hit.size();
+        if (n_found) found = D.node_vars[dt][*std::max_element(hit.begin(), hit.end())];
+      } else {
+        for (int32_t cand : D.node_vars[dt]) {
+          if (set_of(cand).intersects(D.vars[v].set)) {
+            found = cand;
+            n_found++;
+          }
         }
       }
       if (n_found != 1 || found < 0)
@@ -303,16 +379,14 @@ void root_probabilities(const Topology &topo, Dag &dag, const std::vector<double
   for (auto &rv : dag.roots) {
     const Bits &set = dag.vars[rv.variant].set;
     double m = -INFINITY;
-    for (size_t t = 0; t < n; ++t)
-      if (set.test(t)) m = std::max(m, lp[t]);
+    set.for_each([&](size_t t) { m = std::max(m, lp[t]); });
     double acc = 0.0;
     std::vector<double> dacc(r, 0.0);
-    for (size_t t = 0; t < n; ++t) {
-      if (!set.test(t)) continue;
+    set.for_each([&](size_t t) {
       double w = std::exp(lp[t] - m);
       acc += w;
       for (int k = 0; k < r; ++k) dacc[k] += w * (((t >> k) & 1) ? -1.0 / (1.0 - p[k]) : 1.0 / p[k]);
-    }
+    });
     rv.logprob = m + std::log(acc);
     rv.dlogprob.assign(r, 0.0);
     for (int k = 0; k < r; ++k) rv.dlogprob[k] = dacc[k] / acc;

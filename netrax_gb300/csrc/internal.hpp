@@ -56,6 +56,17 @@ struct Bits {
       if (w[i]) return (int64_t)(i * 64 + __builtin_ctzll(w[i]));
     return -1;
   }
+  // f(t) for every member t, in increasing order
+  template <class F>
+  void for_each(F &&f) const {
+    for (size_t i = 0; i < w.size(); ++i)
+      for (uint64_t x = w[i]; x; x &= x - 1) f(i * 64 + (size_t)__builtin_ctzll(x));
+  }
+  uint64_t hash() const {
+    uint64_t h = 1469598103934665603ull;
+    for (uint64_t x : w) h = (h ^ x) * 1099511628211ull;
+    return h;
+  }
 };
 
 constexpr int32_t kFake = INT32_MIN;  // fake all-ones child (Operation.cpp:19-33)
