@@ -280,7 +280,7 @@ int netlk_last_site_updates(const netlk_ctx *ctx, int64_t *site_updates);
  *   network root (the reference groups by the virtually rerooted tree pairs
  *   at the edge).
  * d2 receives, when not NULL, the central difference of d1 over +-h (kept
- * inside [1e-6, 100]): h = 1e-6 for FP64 contexts; for FP32 contexts
+ * inside [1e-6, 100]): h = min(1e-6, t/200) for FP64 contexts; for FP32 contexts
  * h = max(t/200, min(1e-4, (t - 1e-6)/3)), which keeps the FP32 rounding noise
  * of d1 from dominating (the reference computes d2 from its sumtables). */
 int netlk_edge_derivatives(netlk_ctx *ctx, int32_t edge, int32_t mode,

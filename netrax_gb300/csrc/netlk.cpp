@@ -1600,15 +1600,19 @@ int netlk_edge_derivatives(netlk_ctx *ctx, int32_t edge, int32_t mode, double *d
     if (d1) *d1 = g0;
     if (d2) {  // central difference of the first derivative
       // FP64: a step of 1e-6 (second derivatives within ~1e-8 of the analytic
-      // value). FP32: the first derivative carries rounding noise of ~1e-5
-      // relative, which a 1e-6 step amplifies to errors of tens of percent, so
-      // the step grows with the length: t/200, but at least 1e-4 where that
-      // keeps t - h above a third of t (worst error ~5e-4 of the analytic value
-      // on the golden cases, measured against t/100, t/50, 1e-4 and 1e-6).
+      // value), t/200 below t = 2e-4: near the 1e-6 length clamp a site that
+      // needs a change on the branch has L ~ t, so d2 ~ -1/t^2 and only a step
+      // well below t resolves it (30 % median error at the clamp with 1e-6,
+      // 0.2 % with t/200). FP32: the first derivative carries rounding noise of
+      // ~1e-5 relative, which a 1e-6 step amplifies to errors of tens of
+      // percent, so the step grows with the length: t/200, but at least 1e-4
+      // where that keeps t - h above a third of t (worst error ~2e-3 of the
+      // analytic value on the golden cases, measured against t/100, t/50, 1e-4
+      // and 1e-6).
       const double b0 = ctx->brlen[edge];
       const double h = ctx->opts.precision == NETLK_FP32
                            ? std::max(b0 / 200.0, std::min(1e-4, (b0 - 1e-6) / 3.0))
-                           : 1e-6;
+                           : std::min(1e-6, b0 / 200.0);
       ctx->brlen[edge] = std::min(b0 + h, 100.0);
       const double hp = ctx->brlen[edge] - b0;
       const double gp = first();

@@ -510,7 +510,7 @@ def test_edge_derivatives_from_partial_adjoint(precision, config):
     """netlk_edge_derivatives mode 0 runs an incremental forward and only the
     adjoint ops the edge's terms depend on; its d1 is the full gradient's
     entry bit for bit, and d2 the central difference of two full gradients
-    (step 1e-6 in FP64, max(t/200, min(1e-4, (t - 1e-6)/3)) in FP32). DNA
+    (step min(1e-6, t/200) in FP64, max(t/200, min(1e-4, (t - 1e-6)/3)) in FP32). DNA
     (50 taxa, 10 partitions) and protein (40 taxa; FP32 on the tensor cores)."""
     from netrax_gb300 import synth
     from netrax_gb300.likelihood import NetworkLikelihood
@@ -528,7 +528,7 @@ def test_edge_derivatives_from_partial_adjoint(precision, config):
             d1b, d2 = lik.edge_derivatives(e, second=True)
             assert d1b == g0[e]
             t = base[e]
-            h = max(t / 200.0, min(1e-4, (t - 1e-6) / 3.0)) if precision == "fp32" else 1e-6
+            h = max(t / 200.0, min(1e-4, (t - 1e-6) / 3.0)) if precision == "fp32" else min(1e-6, t / 200.0)
             b = base.copy()
             b[e] = min(t + h, 100.0)
             hp = b[e] - t
