@@ -167,7 +167,7 @@ def synthetic_cases():
             freqs /= freqs.sum()
             exch = rng.dirichlet(np.ones(6)) * 6
             codes = synth.simulate_dna(rng, pnet, ns, freqs, exch, 0.8)
-            pat, w = synth.compress(codes)
+            pat, w = pllmath.compress_patterns(codes)  # columns in lexicographic order of their codes
             parts.append({"freqs": freqs.tolist(), "exch": exch.tolist(), "alpha": 0.8,
                           "tip_states": pat.tolist(), "weights": w.tolist()})
         net = newick.parse_newick(text)
@@ -203,7 +203,7 @@ def protein_cases():
             if name.endswith("2parts"):
                 codes[0, :5] = (1 << 20) - 1  # gaps: every state
                 codes[1, 3] = (1 << 2) | (1 << 7)  # an ambiguity
-            pat, w = synth.compress(codes)
+            pat, w = pllmath.compress_patterns(codes)  # columns in lexicographic order of their codes
             parts.append({"freqs": freqs.tolist(), "exch": exch.tolist(), "alpha": 0.8,
                           "tip_states": pat.tolist(), "weights": w.tolist(), "states": 20})
         net = newick.parse_newick(text)
