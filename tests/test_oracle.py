@@ -99,3 +99,18 @@ def test_mixture_against_mpmath_high_precision():
             acc += mpmath.exp(mpmath.mpf(t.logprob) + mpmath.mpf(t.partition_logl[0]))
         ref = float(mpmath.log(acc))
     assert total == pytest.approx(ref, rel=1e-15, abs=1e-12)
+
+
+def test_protein_fixture_regenerates_byte_for_byte():
+    """tests/golden/make_golden.py reproduces the committed 20-state fixture
+    exactly (simulation, pattern compression, oracle scores, central-difference
+    gradients): the fixture is the output of the committed script."""
+    import json
+    import os
+    import sys
+    from conftest import GOLDEN
+    sys.path.insert(0, GOLDEN)
+    import make_golden
+    fresh = json.loads(json.dumps(make_golden.protein_cases()))
+    with open(os.path.join(GOLDEN, "protein_cases.json")) as f:
+        assert fresh == json.load(f)["cases"]
