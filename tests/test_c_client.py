@@ -30,7 +30,7 @@ def test_c_client_builds_and_matches_python(tmp_path):
     exe = str(tmp_path / "abi_client")
     subprocess.check_call([gcc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic",
                            os.path.join(ROOT, "tests", "abi_client.c"), "-I", os.path.join(ROOT, "include"),
-                           "-L", libdir, "-lnetlk", "-Wl,-rpath," + libdir, "-lm", "-o", exe])
+                           lib._name, "-Wl,-rpath," + libdir, "-lm", "-o", exe])
     out = subprocess.run([exe], capture_output=True, text=True, timeout=60)
     assert out.returncode == 0, out.stderr
     got = dict(line.split("=", 1) for line in out.stdout.strip().splitlines())
