@@ -1712,9 +1712,11 @@ int netlk_enqueue(netlk_ctx *ctx, int32_t with_gradient) {
 
 int netlk_result_pointers(netlk_ctx *ctx, const double **d_out, const double **d_brlen) {
   if (!ctx) return NETLK_ERR_INVALID_ARGUMENT;
-  if (d_out) *d_out = ctx->d_out.as<double>();
-  if (d_brlen) *d_brlen = ctx->d_grad.as<double>();
-  return NETLK_OK;
+  return guarded(ctx, [&] {
+    if (ctx->opts.host_only) throw Error(NETLK_ERR_NO_DEVICE, "context was created host_only");
+    if (d_out) *d_out = ctx->d_out.as<double>();
+    if (d_brlen) *d_brlen = ctx->d_grad.as<double>();
+  });
 }
 
 int netlk_set_profiling(netlk_ctx *ctx, int32_t enable) {

@@ -147,6 +147,11 @@ def test_host_only_context_refuses_evaluation():
     with pytest.raises(_native.NetlkError) as e:
         lik.loglikelihood()
     assert e.value.status == _native.NETLK_ERR_NO_DEVICE
+    for call in (lik.loglikelihood_gradient, lambda: lik.enqueue(True), lik.result_pointers,
+                 lambda: lik.edge_derivatives(0), lambda: lik.edge_loglikelihood(0, 0.1)):
+        with pytest.raises(_native.NetlkError) as e:
+            call()
+        assert e.value.status == _native.NETLK_ERR_NO_DEVICE
     lik.set_branch_lengths(net.branch_lengths * 2)
     with pytest.raises(_native.NetlkError):
         lik.set_branch_lengths(net.branch_lengths[:-1])
