@@ -219,6 +219,19 @@ int netlk_root_export(const netlk_ctx *ctx, int32_t *root_variant,
  *                         only message comes from the previous op's
  *                         registers, first index into slot_reads, count
  *   slot_reads [n_slot_reads]  message slots the adjoint ops read */
+/* CLV checkpointing plan, no counterpart in the reference (introspection of
+ * this library's O(sqrt n) memory plan). n_segments: level segments (1 = every
+ * CLV stored); n_clv_slots: CLV buffers held. Arrays (NULL: counts only):
+ *   var_slot [n_variants]    CLV buffer of each variant (dag_export order)
+ *   permanent [n_variants]   1 if the variant is read by an op of a later
+ *                            segment and keeps its buffer for the whole
+ *                            evaluation; the others share their segment's
+ *                            buffers and are recomputed before the segment's
+ *                            adjoint (all but the last segment)
+ *   seg_levels [2 * n_segments]  first and last DAG level of each segment
+ *                            (levels count from 1 = variants above tips only) */
+int netlk_checkpoint_export(const netlk_ctx *ctx, int32_t *n_segments, int32_t *n_clv_slots, int32_t *var_slot,
+                            int32_t *permanent, int32_t *seg_levels);
 int netlk_walk_export(const netlk_ctx *ctx, int32_t *n_fwd, int32_t *n_bwd, int32_t *n_slot_reads,
                       int32_t *fwd_variant, int32_t *bwd_ops, int32_t *slot_reads);
 

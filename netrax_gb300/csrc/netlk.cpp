@@ -1421,6 +1421,23 @@ int netlk_walk_export(const netlk_ctx *ctx, int32_t *n_fwd, int32_t *n_bwd, int3
   return NETLK_OK;
 }
 
+int netlk_checkpoint_export(const netlk_ctx *ctx, int32_t *n_segments, int32_t *n_clv_slots, int32_t *var_slot,
+                            int32_t *permanent, int32_t *seg_levels) {
+  if (!ctx) return NETLK_ERR_INVALID_ARGUMENT;
+  if (n_segments) *n_segments = ctx->n_segments;
+  if (n_clv_slots) *n_clv_slots = ctx->n_clv_slots;
+  for (size_t v = 0; v < ctx->var_slot.size(); ++v) {
+    if (var_slot) var_slot[v] = ctx->var_slot[v];
+    if (permanent) permanent[v] = ctx->n_segments > 1 ? ctx->var_ckpt[v] : 1;
+  }
+  if (seg_levels)
+    for (int s = 0; s < ctx->n_segments; ++s) {
+      seg_levels[2 * s] = ctx->seg_lo[s];
+      seg_levels[2 * s + 1] = ctx->seg_hi[s];
+    }
+  return NETLK_OK;
+}
+
 int netlk_root_export(const netlk_ctx *ctx, int32_t *root_variant, int32_t *dtroot_variant, double *logprob) {
   if (!ctx) return NETLK_ERR_INVALID_ARGUMENT;
   netlk_ctx *c = const_cast<netlk_ctx *>(ctx);

@@ -231,6 +231,20 @@ class NetworkLikelihood:
                                           _ptr(lp, ctypes.c_double)), self._h)
         return rv, dt, lp
 
+    def checkpoint_export(self):
+        """(n_segments, n_clv_slots, var_slot [V], permanent [V], seg_levels [n_segments][2])."""
+        ns, nc = ctypes.c_int32(), ctypes.c_int32()
+        N.check(N.lib().netlk_checkpoint_export(self._h, ctypes.byref(ns), ctypes.byref(nc), None, None, None),
+                self._h)
+        V = self.n_variants
+        slot = np.zeros(V, np.int32)
+        perm = np.zeros(V, np.int32)
+        seg = np.zeros(2 * ns.value, np.int32)
+        N.check(N.lib().netlk_checkpoint_export(self._h, ctypes.byref(ns), ctypes.byref(nc),
+                                                _ptr(slot, ctypes.c_int32), _ptr(perm, ctypes.c_int32),
+                                                _ptr(seg, ctypes.c_int32)), self._h)
+        return ns.value, nc.value, slot, perm, seg.reshape(-1, 2)
+
     def walk_export(self):
         """The walk schedule of the single-launch sweeps: (forward variants in
         walk order, adjoint ops [n, 6] = (variant, slot out a, slot out b,

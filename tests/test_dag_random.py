@@ -173,3 +173,81 @@ def test_fourteen_reticulations_compile_quickly():
     rv, dt, lp = lik.root_export()
     assert np.isclose(np.logaddexp.reduce(lp), 0.0, atol=1e-9)  # the root variants cover every configuration once
     lik.close()
+
+
+def _replay_checkpoint_plan(lik):
+    """Replays one logL + gradient evaluation of a checkpointed context on
+    symbolic buffers: the forward sweep level by level, then per segment from
+    the top the recompute of its non-permanent variants and its adjoint levels
+    (deepest first). Every CLV read - a child of a forward or recompute op, an
+    adjoint op's own CLV / scale counters and its children - must find the
+    expected variant in its buffer; a level's ops run in one launch, so they
+    read before any of them writes and never write the same buffer."""
+    node, ch, _, _ = lik.dag_export()
+    _, dt, _ = lik.root_export()
+    ns, n_slots, slot, perm, seg = lik.checkpoint_export()
+    V = len(node)
+    level = np.zeros(V, np.int64)
+    for v in range(V):  # variants are stored children first
+        kids = [int(c) for c in ch[v] if c >= 0]
+        assert all(c < v for c in kids)
+        level[v] = 1 + max([level[c] for c in kids], default=0)
+    n_levels = int(level.max())
+    assert seg[0, 0] == 1 and seg[-1, 1] == n_levels
+    assert all(seg[i + 1, 0] == seg[i, 1] + 1 for i in range(ns - 1))
+    by_level = [[v for v in range(V) if level[v] == L] for L in range(n_levels + 1)]
+    adjoint = np.zeros(V, bool)
+    for v in set(int(x) for x in dt):
+        adjoint[v] = True
+    for v in range(V - 1, -1, -1):
+        if adjoint[v]:
+            for c in ch[v]:
+                if c >= 0:
+                    adjoint[int(c)] = True
+    assert slot.min() >= 0 and slot.max() < n_slots
+    held = {}
+
+    def run_level(ops):
+        for v in ops:  # reads first
+            for c in ch[v]:
+                if c >= 0:
+                    assert held.get(int(slot[c])) == int(c), ("child", v, int(c))
+        written = [int(slot[v]) for v in ops]
+        assert len(set(written)) == len(written), "two ops of a level write one buffer"
+        for v in ops:
+            held[int(slot[v])] = v
+
+    for L in range(1, n_levels + 1):
+        run_level(by_level[L])
+    for s in range(ns - 1, -1, -1):
+        lo, hi = int(seg[s, 0]), int(seg[s, 1])
+        if s < ns - 1:
+            for L in range(lo, hi + 1):
+                run_level([v for v in by_level[L] if not perm[v]])
+        for L in range(hi, lo - 1, -1):
+            for v in by_level[L]:
+                if not adjoint[v]:
+                    continue
+                assert held.get(int(slot[v])) == v, ("own CLV", v)
+                for c in ch[v]:
+                    if c >= 0:
+                        assert held.get(int(slot[c])) == int(c), ("adjoint child", v, int(c))
+
+
+@pytest.mark.parametrize("seed", range(30))
+def test_random_network_checkpoint_plan_is_sound(seed):
+    """O(sqrt n) CLV checkpointing on random networks with 2, 3 and 5
+    segments: no buffer is overwritten before its last read (replayed on
+    symbolic buffers), and the plan never holds more buffers than variants
+    (small networks save none: every variant is read across a segment)."""
+    rng = np.random.default_rng(8000 + seed)
+    n_taxa = int(rng.integers(8, 30))
+    n_ret = int(rng.integers(1, 7))
+    net = parse_extended_newick(nasty_network(rng, n_taxa, n_ret))
+    part = _partition(rng, n_taxa, n=4)
+    for k in (2, 3, 5):
+        lik = NetworkLikelihood(net, [part], host_only=True, checkpoint_segments=k)
+        ns, n_slots, _, _, _ = lik.checkpoint_export()
+        assert n_slots <= lik.n_variants
+        _replay_checkpoint_plan(lik)
+        lik.close()
