@@ -232,6 +232,19 @@ int netlk_root_export(const netlk_ctx *ctx, int32_t *root_variant,
  *                            (levels count from 1 = variants above tips only) */
 int netlk_checkpoint_export(const netlk_ctx *ctx, int32_t *n_segments, int32_t *n_clv_slots, int32_t *var_slot,
                             int32_t *permanent, int32_t *seg_levels);
+/* Level schedule of the adjoint sweep (one launch per DAG level, deepest
+ * first), no counterpart in the reference (introspection of its message
+ * buffers). Counts: n_ops adjoint ops, n_slot_reads message-buffer reads,
+ * n_levels levels. Arrays (NULL: counts only):
+ *   ops [7 * n_ops]      per op in launch order: CLV buffer of its variant,
+ *                        of child a and of child b (-1-tip for a tip,
+ *                        INT32_MIN for the fake child), message buffer
+ *                        written for a and for b (-1 none), first index into
+ *                        slot_reads, count
+ *   slot_reads [n_slot_reads]  message buffers the ops read
+ *   level_begin [n_levels + 1] first op of each launch */
+int netlk_adjoint_export(const netlk_ctx *ctx, int32_t *n_ops, int32_t *n_slot_reads, int32_t *n_levels,
+                         int32_t *ops, int32_t *slot_reads, int32_t *level_begin);
 int netlk_walk_export(const netlk_ctx *ctx, int32_t *n_fwd, int32_t *n_bwd, int32_t *n_slot_reads,
                       int32_t *fwd_variant, int32_t *bwd_ops, int32_t *slot_reads);
 

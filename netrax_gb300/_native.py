@@ -30,7 +30,7 @@ STATUS_NAMES = {
 EXPORTED = [
     "netlk_options_default", "netlk_create", "netlk_destroy", "netlk_last_error",
     "netlk_status_string", "netlk_get_dag_stats", "netlk_dag_export", "netlk_root_export", "netlk_walk_export",
-    "netlk_checkpoint_export",
+    "netlk_checkpoint_export", "netlk_adjoint_export",
     "netlk_set_branch_lengths", "netlk_set_reticulation_probs", "netlk_set_model",
     "netlk_loglikelihood", "netlk_loglikelihood_gradient", "netlk_edge_derivatives",
     "netlk_tree_partials", "netlk_mix_and_backward", "netlk_get_clv", "netlk_get_stream",
@@ -116,6 +116,7 @@ def lib():
     L.netlk_root_export.argtypes = [vp, c_int32_p, c_int32_p, c_double_p]
     L.netlk_walk_export.argtypes = [vp, c_int32_p, c_int32_p, c_int32_p, c_int32_p, c_int32_p, c_int32_p]
     L.netlk_checkpoint_export.argtypes = [vp, c_int32_p, c_int32_p, c_int32_p, c_int32_p, c_int32_p]
+    L.netlk_adjoint_export.argtypes = [vp, c_int32_p, c_int32_p, c_int32_p, c_int32_p, c_int32_p, c_int32_p]
     L.netlk_set_branch_lengths.argtypes = [vp, c_double_p, ctypes.c_int32]
     L.netlk_set_reticulation_probs.argtypes = [vp, c_double_p, ctypes.c_int32]
     L.netlk_set_model.argtypes = [vp, ctypes.c_int32, c_double_p, c_double_p, ctypes.c_double, c_double_p]

@@ -1438,6 +1438,25 @@ int netlk_checkpoint_export(const netlk_ctx *ctx, int32_t *n_segments, int32_t *
   return NETLK_OK;
 }
 
+int netlk_adjoint_export(const netlk_ctx *ctx, int32_t *n_ops, int32_t *n_slot_reads, int32_t *n_levels,
+                         int32_t *ops, int32_t *slot_reads, int32_t *level_begin) {
+  if (!ctx) return NETLK_ERR_INVALID_ARGUMENT;
+  if (n_ops) *n_ops = (int32_t)ctx->bwd.size();
+  if (n_slot_reads) *n_slot_reads = (int32_t)ctx->msg_slots.size();
+  if (n_levels) *n_levels = (int32_t)ctx->bwd_level_begin.size() - 1;
+  if (ops)
+    for (size_t i = 0; i < ctx->bwd.size(); ++i) {
+      const BwdOp &o = ctx->bwd[i];
+      const int32_t row[7] = {o.x, o.a, o.b, o.out_a, o.out_b, o.msg_begin, o.msg_count};
+      for (int k = 0; k < 7; ++k) ops[7 * i + k] = row[k];
+    }
+  if (slot_reads)
+    for (size_t i = 0; i < ctx->msg_slots.size(); ++i) slot_reads[i] = ctx->msg_slots[i];
+  if (level_begin)
+    for (size_t i = 0; i < ctx->bwd_level_begin.size(); ++i) level_begin[i] = ctx->bwd_level_begin[i];
+  return NETLK_OK;
+}
+
 int netlk_root_export(const netlk_ctx *ctx, int32_t *root_variant, int32_t *dtroot_variant, double *logprob) {
   if (!ctx) return NETLK_ERR_INVALID_ARGUMENT;
   netlk_ctx *c = const_cast<netlk_ctx *>(ctx);

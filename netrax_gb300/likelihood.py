@@ -231,6 +231,19 @@ class NetworkLikelihood:
                                           _ptr(lp, ctypes.c_double)), self._h)
         return rv, dt, lp
 
+    def adjoint_export(self):
+        """Level adjoint schedule: (ops [n][7], slot_reads [m], level_begin [levels + 1])."""
+        n, m, nl = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        N.check(N.lib().netlk_adjoint_export(self._h, ctypes.byref(n), ctypes.byref(m), ctypes.byref(nl),
+                                             None, None, None), self._h)
+        ops = np.zeros(7 * max(1, n.value), np.int32)
+        reads = np.zeros(max(1, m.value), np.int32)
+        lb = np.zeros(nl.value + 1, np.int32)
+        N.check(N.lib().netlk_adjoint_export(self._h, ctypes.byref(n), ctypes.byref(m), ctypes.byref(nl),
+                                             _ptr(ops, ctypes.c_int32), _ptr(reads, ctypes.c_int32),
+                                             _ptr(lb, ctypes.c_int32)), self._h)
+        return ops[:7 * n.value].reshape(-1, 7), reads[:m.value], lb
+
     def checkpoint_export(self):
         """(n_segments, n_clv_slots, var_slot [V], permanent [V], seg_levels [n_segments][2])."""
         ns, nc = ctypes.c_int32(), ctypes.c_int32()

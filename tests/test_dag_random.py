@@ -251,3 +251,48 @@ def test_random_network_checkpoint_plan_is_sound(seed):
         assert n_slots <= lik.n_variants
         _replay_checkpoint_plan(lik)
         lik.close()
+
+
+def _replay_adjoint_messages(lik):
+    """Replays the level adjoint's message buffers (one launch per level): each
+    op reads only messages addressed to its own variant, each message is read
+    exactly once and before its buffer is written again, no buffer is both
+    read and written, or written twice, within one launch, and no message is
+    left unread. (The sweeps drop a buffer's lines from L2 as soon as it has
+    been read, which relies on exactly this.)"""
+    ops, reads, lb = lik.adjoint_export()
+    held = {}
+    for L in range(len(lb) - 1):
+        lo, hi = int(lb[L]), int(lb[L + 1])
+        read_here = []
+        for x, _, _, _, _, mb, mc in ops[lo:hi]:
+            for r in reads[mb:mb + mc]:
+                assert held.get(int(r)) == int(x), ("message to another variant", int(r))
+                read_here.append(int(r))
+        assert len(set(read_here)) == len(read_here), "a buffer read twice"
+        for r in read_here:
+            del held[r]
+        written = []
+        for _, a, b, oa, ob, _, _ in ops[lo:hi]:
+            for child, out in ((a, oa), (b, ob)):
+                if out >= 0:
+                    assert child >= 0, "message to a tip or the fake child"
+                    assert int(out) not in held, "a buffer written before its message was read"
+                    written.append((int(out), int(child)))
+        slots = [s for s, _ in written]
+        assert len(set(slots)) == len(slots), "two messages in one buffer in one launch"
+        assert not set(slots) & set(read_here), "a buffer read and written in one launch"
+        for s, child in written:
+            held[s] = child
+    assert not held, "messages left unread"
+
+
+@pytest.mark.parametrize("seed", range(30))
+def test_random_network_adjoint_messages_are_read_once(seed):
+    rng = np.random.default_rng(9100 + seed)
+    n_taxa = int(rng.integers(4, 30))
+    n_ret = int(rng.integers(0, 7))
+    net = parse_extended_newick(nasty_network(rng, n_taxa, n_ret))
+    lik = NetworkLikelihood(net, [_partition(rng, n_taxa, n=4)], host_only=True)
+    _replay_adjoint_messages(lik)
+    lik.close()
