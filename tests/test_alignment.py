@@ -89,3 +89,49 @@ def test_fasta_logl_matches_golden():
                                   alpha=part["alpha"])
     with NetworkLikelihood(net, [pd], precision="fp64") as lik:
         assert lik.loglikelihood() == pytest.approx(case["AVERAGE"]["logl"], rel=1e-9)
+
+
+def test_front_end_fuzz():
+    """netlk_encode_states on arbitrary bytes (DNA): either every character is
+    a known code (case-insensitive) and the masks are the table's, or the call
+    returns NETLK_ERR_INVALID_ARGUMENT with the index of the first unknown one;
+    netlk_compress_patterns equals a first-occurrence unique of the columns."""
+    import ctypes
+    from netrax_gb300 import _native as N
+    dna = {"A": 1, "C": 2, "G": 4, "T": 8, "U": 8, "R": 5, "Y": 10, "S": 6, "W": 9, "K": 12, "M": 3, "B": 14,
+           "D": 13, "H": 11, "V": 7, "N": 15, "?": 15, "-": 15, ".": 15, "O": 15, "X": 15}
+    L = N.lib()
+    rng = np.random.default_rng(11)
+    alphabet = list(b"ACGTUNRYSWKMBDHV-?.xacgtnZ!")
+    for it in range(2000):
+        n = int(rng.integers(0, 30))
+        if it % 2:
+            raw = bytes(rng.integers(0, 256, size=n).astype(np.uint8))
+        else:
+            raw = bytes(rng.choice(alphabet, size=n).astype(np.uint8))
+        out = np.zeros(max(1, n), np.uint32)
+        bad = ctypes.c_int64(-7)
+        st = L.netlk_encode_states(raw, n, 4, out.ctypes.data_as(N.c_uint32_p), ctypes.byref(bad))
+        want_bad = next((i for i, c in enumerate(raw) if c >= 128 or chr(c).upper() not in dna), -1)
+        if want_bad >= 0:
+            assert st == N.NETLK_ERR_INVALID_ARGUMENT and bad.value == want_bad
+        else:
+            assert st == 0 and [int(x) for x in out[:n]] == [dna[chr(c).upper()] for c in raw]
+    for _ in range(300):
+        nt, ns = int(rng.integers(1, 6)), int(rng.integers(0, 50))
+        codes = rng.integers(1, 4, size=(nt, ns)).astype(np.uint32)
+        pat = np.zeros(nt * max(1, ns), np.uint32)
+        w = np.zeros(max(1, ns))
+        k = ctypes.c_int64(-1)
+        assert L.netlk_compress_patterns(codes.ctypes.data_as(N.c_uint32_p), nt, ns, pat.ctypes.data_as(N.c_uint32_p),
+                                         w.ctypes.data_as(N.c_double_p), ctypes.byref(k)) == 0
+        order, count = [], {}
+        for j in range(ns):
+            c = tuple(codes[:, j])
+            if c not in count:
+                order.append(c)
+                count[c] = 0
+            count[c] += 1
+        got = pat[:nt * k.value].reshape(nt, k.value)
+        assert [tuple(got[:, j]) for j in range(k.value)] == order
+        assert list(w[:k.value]) == [float(count[c]) for c in order]
