@@ -608,8 +608,8 @@ __device__ __forceinline__ void backward_op(const SweepParams &p, const BwdOp &o
   // rewrites the warp's whole range of it, so once all lanes have read them
   // the incoming messages are dead: drop the warp's lines from L2 without
   // writing them back to DRAM. The range is UNIT * R * 4 reals at a multiple
-  // of itself inside a slot of N * R * 4 reals (N is a multiple of 256
-  // patterns / R), all multiples of 128 bytes.
+  // of itself inside a slot of N * R * 4 reals (N is a multiple of 1024 / R
+  // patterns), all multiples of 128 bytes.
   if (op.msg_count > 0) {
     constexpr int kBytes = UNIT * R * 4 * (int)sizeof(real);
     static_assert(kBytes % 128 == 0, "whole L2 lines per warp range");
