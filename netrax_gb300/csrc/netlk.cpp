@@ -1649,6 +1649,12 @@ int netlk_edge_derivatives(netlk_ctx *ctx, int32_t edge, int32_t mode, double *d
       const double h = ctx->opts.precision == NETLK_FP32
                            ? std::max(b0 / 200.0, std::min(1e-4, (b0 - 1e-6) / 3.0))
                            : std::min(1e-6, b0 / 200.0);
+      // the edge gets its length back however this block is left
+      struct Restore {
+        double &len;
+        double value;
+        ~Restore() { len = value; }
+      } restore{ctx->brlen[edge], b0};
       ctx->brlen[edge] = std::min(b0 + h, 100.0);
       const double hp = ctx->brlen[edge] - b0;
       const double gp = first();
