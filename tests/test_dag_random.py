@@ -296,3 +296,17 @@ def test_random_network_adjoint_messages_are_read_once(seed):
     lik = NetworkLikelihood(net, [_partition(rng, n_taxa, n=4)], host_only=True)
     _replay_adjoint_messages(lik)
     lik.close()
+
+
+def test_checkpoint_export_without_segments():
+    """With one segment every variant keeps its own CLV buffer (buffer id =
+    variant id) for the whole evaluation, and the plan replays trivially."""
+    from netrax_gb300 import synth
+    w = synth.config(2, scale=0.01)
+    lik = NetworkLikelihood(w.network, w.partitions, host_only=True, checkpoint_segments=1)
+    ns, n_slots, slot, perm, seg = lik.checkpoint_export()
+    assert ns == 1 and n_slots == lik.n_variants
+    assert np.array_equal(slot, np.arange(lik.n_variants)) and perm.all()
+    assert seg.tolist() == [[1, lik.stats["n_levels"]]]
+    _replay_checkpoint_plan(lik)
+    lik.close()
