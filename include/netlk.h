@@ -206,19 +206,6 @@ int netlk_dag_export(const netlk_ctx *ctx, int32_t *node_of_variant,
 int netlk_root_export(const netlk_ctx *ctx, int32_t *root_variant,
                       int32_t *dtroot_variant, double *logprob);
 
-/* Walk schedule export, for checks of the host schedule. No counterpart in
- * the reference (introspection of this library's single-launch sweeps).
- * Counts: n_fwd forward ops, n_bwd adjoint ops, n_slot_reads message-slot
- * reads; all 0 when the context has no walk schedule (20 states, or more
- * than one checkpoint segment; FP64 contexts have one but run the level
- * sweeps). Arrays (NULL: counts only):
- *   fwd_variant [n_fwd]   variant computed by each forward op, in walk order
- *   bwd_ops [6 * n_bwd]   per adjoint op in walk order: variant x, message
- *                         slot written for child a and for child b (-1 none,
- *                         -2 kept in registers for the next op), 1 if its
- *                         only message comes from the previous op's
- *                         registers, first index into slot_reads, count
- *   slot_reads [n_slot_reads]  message slots the adjoint ops read */
 /* CLV checkpointing plan, no counterpart in the reference (introspection of
  * this library's O(sqrt n) memory plan). n_segments: level segments (1 = every
  * CLV stored); n_clv_slots: CLV buffers held. Arrays (NULL: counts only):
@@ -245,6 +232,19 @@ int netlk_checkpoint_export(const netlk_ctx *ctx, int32_t *n_segments, int32_t *
  *   level_begin [n_levels + 1] first op of each launch */
 int netlk_adjoint_export(const netlk_ctx *ctx, int32_t *n_ops, int32_t *n_slot_reads, int32_t *n_levels,
                          int32_t *ops, int32_t *slot_reads, int32_t *level_begin);
+/* Walk schedule export, for checks of the host schedule. No counterpart in
+ * the reference (introspection of this library's single-launch sweeps).
+ * Counts: n_fwd forward ops, n_bwd adjoint ops, n_slot_reads message-slot
+ * reads; all 0 when the context has no walk schedule (20 states, or more
+ * than one checkpoint segment; FP64 contexts have one but run the level
+ * sweeps). Arrays (NULL: counts only):
+ *   fwd_variant [n_fwd]   variant computed by each forward op, in walk order
+ *   bwd_ops [6 * n_bwd]   per adjoint op in walk order: variant x, message
+ *                         slot written for child a and for child b (-1 none,
+ *                         -2 kept in registers for the next op), 1 if its
+ *                         only message comes from the previous op's
+ *                         registers, first index into slot_reads, count
+ *   slot_reads [n_slot_reads]  message slots the adjoint ops read */
 int netlk_walk_export(const netlk_ctx *ctx, int32_t *n_fwd, int32_t *n_bwd, int32_t *n_slot_reads,
                       int32_t *fwd_variant, int32_t *bwd_ops, int32_t *slot_reads);
 
@@ -373,7 +373,10 @@ int netlk_walk_shape_begin(const netlk_ctx *ctx, int32_t *first_walk_shape);
  * the sum over partitions.
  *   d_site_logl       device [n_trees * n_sites], row = displayed tree: weighted
  *                     per-site (or per-site-block) log-likelihood contributions
- *   d_part_site_begin device [n_parts + 1]: site range of each partition
+ *   d_part_site_begin device [n_parts + 1]: site range of each partition,
+ *                     0 <= begin[0] <= ... <= begin[n_parts] <= n_sites (a range
+ *                     outside [0, n_sites] is clipped to it, so a bad range
+ *                     gives a wrong sum but reads nothing out of bounds)
  *   d_tree_logprob    device [n_trees]: log P(tree)
  *   d_out             device [1 + n_parts]: total, then per-partition logL
  *   stream            cudaStream_t to launch on (NULL = default stream)
@@ -381,8 +384,10 @@ int netlk_walk_shape_begin(const netlk_ctx *ctx, int32_t *first_walk_shape);
  * (n_trees * n_parts above that is rejected with NETLK_ERR_INVALID_ARGUMENT;
  * the message is in netlk_last_error(NULL)). Asynchronous: results are ready
  * when the stream is. The first call on a device looks up that array's
- * device address, so make it before any stream capture. All calls on a
- * device share the array: calls whose work overlaps on the GPU race. */
+ * device address (and looks it up again after the device's context was
+ * recreated, e.g. by cudaDeviceReset), so make it before any stream capture.
+ * All calls on a device share the array: calls whose work overlaps on the
+ * GPU race. */
 #define NETLK_NOALLOC_MAX_TREE_PARTITIONS 65536
 int netlk_mix_site_loglikelihoods_noalloc(const double *d_site_logl, int32_t n_trees, int64_t n_sites,
                                           const int64_t *d_part_site_begin, int32_t n_parts,
@@ -438,6 +443,11 @@ int netlk_get_clv(netlk_ctx *ctx, int32_t variant, int32_t partition,
 int netlk_get_stream(netlk_ctx *ctx, void **stream);
 /* Kernels launched by this context since creation. */
 int netlk_launch_count(const netlk_ctx *ctx, int64_t *launches);
+/* Host-side failure injection for tests, no counterpart in the reference:
+ * the next evaluation call on ctx fails with `status` (a NETLK_ERR_* code)
+ * after its kernels have run, where a timed-out device wait or a CUDA error
+ * would be reported. Nothing is done on the device. 0 clears it. */
+int netlk_inject_failure(netlk_ctx *ctx, int32_t status);
 
 #ifdef __cplusplus
 }

@@ -38,7 +38,7 @@ EXPORTED = [
     "netlk_result_pointers", "netlk_set_profiling", "netlk_kernel_times", "netlk_tuning", "netlk_walk_shape_begin",
     "netlk_mix_site_loglikelihoods_noalloc", "netlk_batch_create",
     "netlk_batch_loglikelihood_gradient", "netlk_batch_destroy", "netlk_edge_loglikelihood",
-    "netlk_last_site_updates", "netlk_encode_states", "netlk_compress_patterns",
+    "netlk_last_site_updates", "netlk_encode_states", "netlk_compress_patterns", "netlk_inject_failure",
 ]
 
 
@@ -128,6 +128,7 @@ def lib():
     L.netlk_get_clv.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, c_double_p, c_int32_p]
     L.netlk_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
     L.netlk_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_int64)]
+    L.netlk_inject_failure.argtypes = [vp, ctypes.c_int32]
     L.netlk_set_branch_lengths_device.argtypes = [vp, ctypes.c_void_p, ctypes.c_int32]
     L.netlk_enqueue.argtypes = [vp, ctypes.c_int32]
     L.netlk_result_pointers.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp)]

@@ -133,6 +133,7 @@ struct netlk_ctx {
   // best level-schedule shapes (the walk shapes only run the full sweeps)
   int fwd_lshape = 0, bwd_lshape = 0;
   int64_t last_updates = 0;
+  int32_t inject_status = 0;  // netlk_inject_failure: fail the next result check
   int fwd_shape = 0, bwd_shape = 0, sms = 0;
   bool tuned = false;
   bool use_tc = false;  // 20-state FP32 forward on the tensor cores
@@ -307,6 +308,14 @@ struct netlk_ctx {
   void prepare_state();  // model / probabilities uploads and launch-shape tuning
   void prepare();        // prepare_state + branch-length upload
   void finish(double *total, double *part_logl, double *d_brlen, double *d_ret);
+  // a failure planted by netlk_inject_failure, thrown once
+  void check_injected() {
+    if (inject_status) {
+      const int st = inject_status;
+      inject_status = 0;
+      throw Error(st, "injected failure (netlk_inject_failure)");
+    }
+  }
   // results from the pinned host copies of the last evaluation
   void read_results(double *total, double *part_logl, double *d_brlen, double *d_ret);
 };
@@ -1063,6 +1072,7 @@ bool netlk_ctx::edge_d1_partial(int e, double *d1) {
   CUDA_OK(cudaStreamSynchronize(stream));
   CUDA_OK(cudaGetLastError());
   const double *o = h_out.as<double>();
+  check_injected();
   if (use_tc && *reinterpret_cast<const int32_t *>(o + nout - 1) != 0)
     throw Error(NETLK_ERR_TIMEOUT, "tensor-core sweep: an MMA completion wait timed out");
   if (o[1] != 0.0 || !std::isfinite(o[0]))
@@ -1167,6 +1177,7 @@ void netlk_ctx::finish(double *total, double *part_logl, double *d_brlen, double
 void netlk_ctx::read_results(double *total, double *part_logl, double *d_brlen, double *d_ret) {
   const int nout = 3 + P + topo.n_ret;
   const double *o = h_out.as<double>();
+  check_injected();
   if (use_tc && *reinterpret_cast<const int32_t *>(o + nout - 1) != 0)
     throw Error(NETLK_ERR_TIMEOUT, "tensor-core sweep: an MMA completion wait timed out");
   if (o[1] != 0.0 || !std::isfinite(o[0]))
@@ -1185,6 +1196,10 @@ void set_global_error(const std::string &msg) { g_create_error = msg; }
 
 namespace {
 
+// Every failed call forgets the stored CLVs: an error thrown after a launch
+// (a timed-out MMA wait, a CUDA error, a -inf logL) may leave them partial,
+// so the next evaluation runs a full forward sweep instead of an
+// incremental one over buffers it cannot trust.
 template <class F>
 int guarded(netlk_ctx *ctx, F &&f) {
   try {
@@ -1192,13 +1207,28 @@ int guarded(netlk_ctx *ctx, F &&f) {
     if (ctx) ctx->err.clear();
     return NETLK_OK;
   } catch (const Error &e) {
-    if (ctx) ctx->err = e.what(); else g_create_error = e.what();
+    if (ctx) {
+      ctx->err = e.what();
+      ctx->clv_valid = false;
+    } else {
+      g_create_error = e.what();
+    }
     return e.status;
   } catch (const std::bad_alloc &) {
-    if (ctx) ctx->err = "host allocation failed"; else g_create_error = "host allocation failed";
+    if (ctx) {
+      ctx->err = "host allocation failed";
+      ctx->clv_valid = false;
+    } else {
+      g_create_error = "host allocation failed";
+    }
     return NETLK_ERR_OUT_OF_MEMORY;
   } catch (const std::exception &e) {
-    if (ctx) ctx->err = e.what(); else g_create_error = e.what();
+    if (ctx) {
+      ctx->err = e.what();
+      ctx->clv_valid = false;
+    } else {
+      g_create_error = e.what();
+    }
     return NETLK_ERR_INVALID_ARGUMENT;
   }
 }
@@ -1834,6 +1864,12 @@ int netlk_walk_shape_begin(const netlk_ctx *ctx, int32_t *first_walk_shape) {
   return NETLK_OK;
 }
 
+int netlk_inject_failure(netlk_ctx *ctx, int32_t status) {
+  if (!ctx || status < 0 || status > NETLK_ERR_TIMEOUT) return NETLK_ERR_INVALID_ARGUMENT;
+  ctx->inject_status = status;
+  return NETLK_OK;
+}
+
 int netlk_get_stream(netlk_ctx *ctx, void **stream) {
   if (!ctx || !stream) return NETLK_ERR_INVALID_ARGUMENT;
   *stream = (void *)ctx->stream;
@@ -1937,6 +1973,7 @@ int netlk_batch_loglikelihood_gradient(netlk_batch *b, double *totals, double *c
                     "batch: context " + std::to_string(i) + " has device-resident branch lengths");
       c->prepare_state();  // uploads and tuning happen outside the graph
       CUDA_OK(cudaStreamSynchronize(c->stream));
+      c->clv_valid = false;  // the graph rewrites its CLVs; valid again once its results check out
       std::memcpy(c->h_brlen.p, c->brlen.data(), c->brlen.size() * 8);
     }
     CUDA_OK(cudaSetDevice(b->device));

@@ -12,6 +12,7 @@
 // (kernels.cu) without a context: the caller supplies per-site (or per-block)
 // log-likelihood contributions of each displayed tree instead of the
 // library's own forward sweep.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -35,17 +36,51 @@ namespace {
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 double *g_scratch_ptr[kMaxDevices] = {nullptr};
+unsigned long long g_scratch_ctx[kMaxDevices] = {0};
 
-// Device address of the array on the current device, looked up once per
-// device. In host code the symbol name is only a stand-in and must never be
-// handed to a kernel.
+typedef CUresult(CUDAAPI *CtxGetCurrentFn)(CUcontext *);
+typedef CUresult(CUDAAPI *CtxGetIdFn)(CUcontext, unsigned long long *);
+
+// Process-unique id of the current CUDA context (0 if it cannot be read).
+// The driver functions are fetched through the runtime, so the library does
+// not link libcuda itself.
+unsigned long long current_context_id() {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    looked_up = true;
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<CtxGetIdFn>(f);
+  }
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current && get_id && get_current(&ctx) == CUDA_SUCCESS && ctx && get_id(ctx, &id) == CUDA_SUCCESS)
+    return id;
+  return 0;
+}
+
+// Device address of the array on the current device, looked up at the first
+// call on a device, and again whenever the device's context has changed
+// since (after cudaDeviceReset the library image is loaded anew and the old
+// address is gone). In host code the symbol name is only a stand-in and must
+// never be handed to a kernel.
 cudaError_t scratch_address(int device, double **out) {
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_ptr[device]) {
+  const unsigned long long ctx = current_context_id();
+  if (!g_scratch_ptr[device] || ctx == 0 || ctx != g_scratch_ctx[device]) {
     void *p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_tree_partition_sum);
     if (e != cudaSuccess) return e;
     g_scratch_ptr[device] = static_cast<double *>(p);
+    g_scratch_ctx[device] = ctx;
   }
   *out = g_scratch_ptr[device];
   return cudaSuccess;
@@ -57,7 +92,10 @@ __global__ void noalloc_reduce_kernel(const double *__restrict__ site_logl, int6
                                       const int64_t *__restrict__ part_begin, int n_parts,
                                       double *__restrict__ sum) {
   const int tree = blockIdx.x, part = blockIdx.y;
-  const int64_t b = part_begin[part], e = part_begin[part + 1];
+  // a range outside [0, n_sites] is clipped to it: a bad caller range gives
+  // a wrong sum, never an out-of-bounds read
+  const int64_t b = min(max(part_begin[part], (int64_t)0), n_sites);
+  const int64_t e = min(max(part_begin[part + 1], b), n_sites);
   const double *src = site_logl + (size_t)tree * n_sites;
   double s = 0.0, c = 0.0;
   for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) {

@@ -219,7 +219,8 @@ def protein_cases():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", required=True,
+                    help="path of the NetRAX source tree (read-only input)")
     a = ap.parse_args()
     with open(os.path.join(HERE, "reference_cases.json"), "w") as f:
         json.dump({"model": MODEL, "cases": reference_cases(a.reference)}, f)

@@ -77,7 +77,8 @@ def extract(reference):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", required=True,
+                    help="path of the NetRAX source tree (read-only input)")
     a = ap.parse_args()
     cases = []
     for k, (name, text) in enumerate(extract(a.reference)):

@@ -133,3 +133,36 @@ def test_rate_category_counts(states, rate_cats):
             got, gb, gr = lik.loglikelihood_gradient()
             assert got == pytest.approx(want, rel=tol)
             assert np.all(np.isfinite(gb)) and np.all(np.isfinite(gr))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_failed_evaluation_forgets_the_stored_clvs(precision):
+    """An evaluation that fails after its kernels ran (a timed-out device
+    wait, a CUDA error) may leave the stored CLVs partial, so it must not
+    leave them marked valid: the next edge evaluation has to run the full
+    forward sweep instead of an incremental one over them. The failure is
+    injected on the host (netlk_inject_failure); nothing faults on the GPU."""
+    from netrax_gb300 import _native as N
+    from netrax_gb300.likelihood import NetworkLikelihood
+    rng = np.random.default_rng(6)
+    text = synth.random_network_newick(rng, 10, 2)
+    net = parse_extended_newick(text)
+    parts = _parts(rng, 10, [40])
+    with NetworkLikelihood(net, parts, precision=precision) as lik, \
+            NetworkLikelihood(net, parts, precision=precision) as fresh:
+        lik.loglikelihood()
+        full = lik.last_site_updates()
+        lik.edge_loglikelihood(0, net.branch_lengths[0] * 1.5)
+        assert lik.last_site_updates() < full  # incremental while nothing failed
+        N.check(N.lib().netlk_inject_failure(lik._h, N.NETLK_ERR_TIMEOUT))
+        with pytest.raises(N.NetlkError) as ei:
+            lik.edge_loglikelihood(1, net.branch_lengths[1] * 1.5)
+        assert ei.value.status == N.NETLK_ERR_TIMEOUT
+        got = lik.edge_loglikelihood(2, net.branch_lengths[2] * 1.5)
+        assert lik.last_site_updates() == full
+        b = net.branch_lengths.copy()
+        b[0] *= 1.5
+        b[1] *= 1.5
+        b[2] *= 1.5
+        fresh.set_branch_lengths(b)
+        assert got == fresh.loglikelihood()
