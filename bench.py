@@ -16,8 +16,10 @@ logL + gradient out), wall clock.
 Multi-GPU: every rank evaluates its own replica (independent optimizer
 iterates) - weak scaling, no collective on the data path.
 
-``--impl reference`` times the CPU restatement of the reference's pruning
-(``oracle/``, OpenMP over sites, all host cores) on a bounded pattern sample.
+``--impl reference`` times the oracle's FP64 CPU restatement of the path
+(``oracle/``: the reference's schedule and pruning arithmetic plus an adjoint
+sweep for the gradient, all host cores) on the full workload, logL + gradient
+per step, with the same --steps / --warmup.
 """
 import argparse
 import json
@@ -50,7 +52,6 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=20)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-sample", type=int, default=16384, help="patterns in the CPU sample")
     ap.add_argument("--scale", type=float, default=1.0, help="site-count scale (1.0 = full workload)")
     ap.add_argument("--op", default="eval", choices=["eval", "edge"],
                     help="eval: logL + gradient evaluations (the headline); edge: the branch-length "
@@ -167,44 +168,43 @@ TRAFFIC_PER_UPDATE = {"forward_level_fp32_4": 102.3, "backward_level_fp32_4": 29
                       "forward_walk_fp32_4": 85.8, "backward_walk_fp32_4": 213.3}
 
 
-def cpu_port_rate(w, n_sample, steps, warmup, variant):
-    """Oracle (CPU restatement, OpenMP) forward-pass time on a pattern sample;
-    returns (evals/s of the full workload extrapolated by patterns, info)."""
-    from oracle import build as obuild
-    from oracle import improved, newick, pllmath
+def cpu_rate(w, steps, warmup, variant, seed=123):
+    """The oracle's FP64 CPU sweeps on the FULL workload, one thread per host
+    core: per step, new branch lengths, the forward pruning of every
+    displayed-tree variant (the reference's schedule and libpll arithmetic,
+    threads as the reference's MPI ranks over pattern slices), the mixture, and
+    an adjoint sweep for d logL / d every branch length and reticulation
+    probability. Returns (evals/s, info)."""
+    from oracle import improved, newick, pllmath, sweep
     net = newick.parse_newick(w.newick)
-    parts, total, used = [], 0, 0
-    remaining = n_sample
-    for p in w.partitions:
-        take = min(p.n_patterns, remaining) if remaining > 0 else 0
-        total += p.n_patterns
-        if take <= 0:
-            continue
-        remaining -= take
-        used += take
-        parts.append(improved.Partition(np.ascontiguousarray(p.tip_states[:, :take]),
-                                        np.ascontiguousarray(p.weights[:take]), p.freqs, p.exch,
-                                        pllmath.gamma_rates_mean(p.alpha, 4)))
+    parts = [improved.Partition(p.tip_states, p.weights, p.freqs, p.exch, pllmath.gamma_rates_mean(p.alpha, 4))
+             for p in w.partitions]
     orc = improved.ImprovedOracle(net, parts, variant=variant)
-    orc.loglikelihood()  # enumeration (host-side, untimed)
-    rng = np.random.default_rng(123)
-    base = list(orc.brlen)
-    for _ in range(warmup):
-        orc.recompute()
+    orc.loglikelihood()  # the reference's displayed-tree enumeration (host-side, untimed)
+    so = sweep.SweepOracle(orc)
+    rng = np.random.default_rng(seed)
+    base = np.array(orc.brlen, np.float64)
+
+    def lengths():
+        return np.clip(base * np.exp(0.05 * rng.standard_normal(base.size)), 1e-6, 100.0)
+
+    for _ in range(warmup):  # the first step also faults in the CLV and adjoint buffers
+        so.evaluate(lengths())
     times = []
     for _ in range(steps):
-        orc.brlen = [b * math.exp(0.02 * rng.standard_normal()) for b in base]
+        b = lengths()
         t = time.perf_counter()
-        orc.recompute()
+        so.evaluate(b)
         times.append(time.perf_counter() - t)
-    t_step = statistics.median(times)
-    evals = 1.0 / (t_step * total / used)
-    info = {"value": evals, "unit": UNIT, "cores": int(obuild.lib().oracle_num_threads()), "kind": "port",
-            "sample": "forward (logL) pruning of all %d variants on %d of %d patterns, median of %d "
-                      "steps, extrapolated by patterns; the CPU arm computes no gradient, so this is an "
-                      "upper bound on its logL+grad rate"
-                      % (sum(len(x) for x in orc.pernode[net.n_tips:]), used, total, steps),
-            "site_clv_updates_per_s": orc.update_count / t_step}
+    evals = steps / sum(times)
+    patterns = sum(p.n for p in parts)
+    info = {"value": evals, "unit": UNIT, "cores": sweep.threads(), "kind": "port",
+            "sample": "full workload: all %d patterns, logL + gradient per step (forward pruning of all %d "
+                      "variants with per-site scaling, mixture, adjoint sweep), FP64, %d timed steps after "
+                      "%d warm-up, new branch lengths every step" % (patterns, so.n_var, steps, warmup),
+            "ms_per_step": 1000.0 / evals,
+            "site_clv_updates_per_s": so.site_updates * evals,
+            "median_ms": statistics.median(times) * 1000.0}
     return evals, info
 
 
@@ -213,13 +213,14 @@ def run_reference(args, ws, rank):
         return
     from netrax_gb300 import synth
     w = synth.config(args.config, scale=args.scale)
-    steps = max(1, min(args.steps, 5))
-    evals, info = cpu_port_rate(w, args.cpu_sample, steps, min(args.warmup, 1), args.variant)
+    steps, warmup = args.steps, max(1, args.warmup)
+    evals, info = cpu_rate(w, steps, warmup, args.variant)
     line = {"impl": "reference", "metric": METRIC, "value": evals, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": steps, "warmup": min(args.warmup, 1), "ms_per_step": 1000.0 / evals,
+            "steps": steps, "warmup": warmup, "ms_per_step": 1000.0 / evals,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
-            "config": {"workload": w.name, "patterns": w.n_patterns, "variant": args.variant},
+            "config": {"workload": w.name, "patterns": w.n_patterns, "variant": args.variant,
+                       "l2": "no flush: every step streams tens of GB of CLVs, far above the CPU caches"},
             "cpu_baseline": info,
             "e2e": {"value": evals, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -356,7 +357,7 @@ def run_netlk(args, ws, rank, local):
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        _, cpu = cpu_port_rate(w, args.cpu_sample, 3, 1, args.variant)
+        _, cpu = cpu_rate(w, 3, 1, args.variant)
 
     if rank == 0:
         line = {

@@ -13,15 +13,18 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboracle.so")
 
 
+SOURCES = ["clv.c", "sweep.c"]
+
+
 def build(force: bool = False) -> str:
-    src = os.path.join(HERE, "clv.c")
+    srcs = [os.path.join(HERE, s) for s in SOURCES]
     if (not force and os.path.exists(LIB)
-            and os.path.getmtime(LIB) >= os.path.getmtime(src)):
+            and all(os.path.getmtime(LIB) >= os.path.getmtime(s) for s in srcs)):
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     tmp = LIB + ".tmp%d" % os.getpid()
-    subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-fopenmp",
-                           "-std=c99", src, "-o", tmp, "-lm"])
+    subprocess.check_call(["gcc", "-O3", "-fPIC", "-shared", "-fopenmp",
+                           "-std=c99"] + srcs + ["-o", tmp, "-lm"])
     os.replace(tmp, LIB)
     return LIB
 

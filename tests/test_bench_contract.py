@@ -1,5 +1,5 @@
 """The benchmark's reference arm prints one JSON line with the contract's
-fields (run on a tiny sample on the CPU)."""
+fields (run on the CPU at 1 % of the headline workload's sites)."""
 import json
 import os
 import subprocess
@@ -10,7 +10,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def test_reference_arm_json_line():
     out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--scale", "0.01",
-                          "--steps", "1", "--warmup", "1", "--cpu-sample", "256"],
+                          "--steps", "2", "--warmup", "1"],
                          capture_output=True, text=True, timeout=600, cwd=ROOT)
     assert out.returncode == 0, out.stderr[-2000:]
     line = json.loads(out.stdout.strip().splitlines()[-1])
@@ -23,3 +23,5 @@ def test_reference_arm_json_line():
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == line["value"] and cb["sample"]
     e2e = line["e2e"]
     assert e2e["value"] == line["value"] and e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+    assert line["steps"] == 2 and line["warmup"] == 1  # the arm runs the steps it is given
+    assert "full workload" in cb["sample"]
