@@ -10,14 +10,14 @@ and the reference's per-edge sumtable derivatives on the golden cases).
 * 100 taxa / 8 reticulations / 100k DNA sites (88,315 patterns): logL total,
   per partition and per displayed tree, AVERAGE and BEST, FP64 within 1e-9
   and FP32 within 1e-6 relative; FP64 scale counters of every variant equal
-  the oracle's pattern by pattern; gradients.
+  the oracle's pattern by pattern, also with branch lengths stretched until
+  sites need rescaling; gradients.
 * 50 taxa / 4 reticulations / 10 uneven DNA partitions (75.5k sites).
 * 40 taxa / 3 reticulations / 50k protein sites on the tensor-core path.
 * four candidates of the 64-network search-move batch, scored in one batch.
 
 Gradient tolerances are relative to the largest entry: FP64 1e-8, FP32 1e-5.
 """
-import math
 
 import numpy as np
 import pytest
@@ -97,15 +97,22 @@ def test_config2_full_size(config2, variant, precision):
         _check(lik, want, precision)
 
 
-def test_config2_fp64_scale_counters_bit_exact(config2):
+@pytest.mark.parametrize("stretch", [1.0, 100.0])
+def test_config2_fp64_scale_counters_bit_exact(config2, stretch):
     """Every variant's per-pattern scale counters (FP64, libpll's 2^-256 rule)
-    equal the oracle's; GPU variants map to the oracle's per node, in order."""
+    equal the oracle's; GPU variants map to the oracle's per node, in order.
+    With the generated branch lengths no site reaches 2^-256 (every counter
+    is 0); with every length stretched 100x (clamped at 100) a few tenths of
+    a percent of the (variant, pattern) counters are 1, and the logL still
+    matches in FP64 and FP32."""
     from netrax_gb300.likelihood import NetworkLikelihood
     so = _sweep_oracle(2, config2)
     so.orc.variant = "AVERAGE"
-    so.evaluate(gradient=False)
+    lengths = np.clip(np.array(so.orc.brlen) * stretch, 1e-6, 100.0)
+    want_total = so.evaluate(lengths, gradient=False)[0]
     with NetworkLikelihood(config2.network, config2.partitions, precision="fp64") as lik:
-        lik.loglikelihood()
+        lik.set_branch_lengths(lengths)
+        assert lik.loglikelihood() == pytest.approx(want_total, rel=FP64_REL)
         node, _, _, _ = lik.dag_export()
         rank = {}
         scaled = 0
@@ -115,8 +122,11 @@ def test_config2_fp64_scale_counters_bit_exact(config2):
             _, sc = lik.get_clv(v, 0)
             want = so.keep[0]["scaler"][so.variant_of[(int(node[v]), idx)]]
             assert np.array_equal(sc.astype(np.uint32), want), v
-            scaled += int(want.max() > 0)
-        assert scaled > 0
+            scaled += int(np.count_nonzero(want))
+        assert (scaled > 0) == (stretch > 1.0)
+    with NetworkLikelihood(config2.network, config2.partitions, precision="fp32") as lik:
+        lik.set_branch_lengths(lengths)
+        assert lik.loglikelihood() == pytest.approx(want_total, rel=FP32_REL)
 
 
 @pytest.mark.parametrize("variant", ["AVERAGE", "BEST"])
