@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--scale", type=float, default=1.0, help="site-count scale (1.0 = full workload)")
+    ap.add_argument("--checkpoint-segments", type=int, default=0,
+                    help="CLV checkpointing: 0 automatic (every CLV stored while they fit), 1 store every CLV, "
+                         "k >= 2: k level segments, the adjoint recomputes each segment's non-permanent CLVs")
     ap.add_argument("--op", default="eval", choices=["eval", "edge"],
                     help="eval: logL + gradient evaluations (the headline); edge: the branch-length "
                          "optimizer's per-edge calls (incremental edge logL, edge derivatives)")
@@ -234,7 +237,7 @@ def run_netlk(args, ws, rank, local):
     dev = torch.device("cuda", local)
     w = synth.config(args.config, scale=args.scale)
     lik = NetworkLikelihood(w.network, w.partitions, variant=args.variant, precision=args.precision,
-                            device=local)
+                            device=local, checkpoint_segments=args.checkpoint_segments)
     st = lik.stats
     E = lik.n_edges
     K, W = args.steps, max(3, args.warmup)
@@ -330,7 +333,9 @@ def run_netlk(args, ws, rank, local):
 
     # ------------------------------------------------------------- roofline
     peak, peak_kind = measured_peak()
-    fwd_b, bwd_b = st["forward_bytes"], st["backward_bytes"]
+    st = lik.stats  # after tuning: launch counts of the chosen shapes
+    # the adjoint's time includes the checkpoint recomputes, so its bytes do too
+    fwd_b, bwd_b = st["forward_bytes"], st["backward_bytes"] + st["recompute_bytes"]
     dom = "backward" if kavg["backward"] >= kavg["forward"] else "forward"
     dom_bytes = bwd_b if dom == "backward" else fwd_b
     achieved = dom_bytes / (kavg[dom] * 1e-3) / 1e9 if kavg[dom] > 0 else 0.0
@@ -338,7 +343,7 @@ def run_netlk(args, ws, rank, local):
     sched = "walk" if tuning.get(dom + "_walk") else "level"
     traffic = None
     tt = TRAFFIC_PER_UPDATE.get("%s_%s_%s_%d" % (dom, sched, args.precision, lik.states))
-    if tt:
+    if tt and st["checkpoint_segments"] == 1:  # captured without checkpointing
         traffic = tt * st["site_clv_updates"]
     if lik.states == 20:  # FP32 with 4 rates runs the tensor-core (tcgen05) sweeps
         kname = dom + ("20_tc_kernel" if args.precision == "fp32" and lik.rate_cats == 4 else "20_kernel")
@@ -370,6 +375,9 @@ def run_netlk(args, ws, rank, local):
                        "variant": args.variant, "precision": args.precision,
                        "displayed_trees": lik.n_roots, "dag_variants": st["n_variants"],
                        "site_clv_updates_per_eval": st["site_clv_updates"],
+                       "checkpoint_segments": st["checkpoint_segments"], "clv_buffers": st["clv_slots"],
+                       "recompute_site_updates_per_eval": st["recompute_site_updates"],
+                       "device_bytes": st["device_bytes"],
                        "l2": "no flush: every eval streams %.1f GB of CLVs, far above the 129 MB L2"
                              % ((fwd_b + bwd_b) / 1e9),
                        "parallelism": "replica per GPU" if ws > 1 else "1 GPU", "seed": w.seed},

@@ -160,6 +160,8 @@ typedef struct {
   int32_t checkpoint_segments; /* segments in use (1 = every CLV stored)     */
   int32_t clv_slots;           /* CLV buffers held (= n_variants when 1)     */
   int64_t recompute_site_updates; /* extra forward updates per gradient eval */
+  int64_t recompute_bytes;     /* algorithmic HBM bytes of those recomputes
+                                  (counted like forward_bytes)              */
 } netlk_dag_stats;
 
 /* --------------------------------------------------------------- lifecycle */
@@ -235,9 +237,11 @@ int netlk_adjoint_export(const netlk_ctx *ctx, int32_t *n_ops, int32_t *n_slot_r
 /* Walk schedule export, for checks of the host schedule. No counterpart in
  * the reference (introspection of this library's single-launch sweeps).
  * Counts: n_fwd forward ops, n_bwd adjoint ops, n_slot_reads message-slot
- * reads; all 0 when the context has no walk schedule (20 states, or more
- * than one checkpoint segment; FP64 contexts have one but run the level
- * sweeps). Arrays (NULL: counts only):
+ * reads; all 0 when the context has no walk schedule (20 states; FP64
+ * contexts have one but run the level sweeps). With checkpoint segments the
+ * forward walk lists the segments one after the other and the adjoint walk
+ * runs one launch per segment (netlk_walk_segments). Arrays (NULL: counts
+ * only):
  *   fwd_variant [n_fwd]   variant computed by each forward op, in walk order
  *   bwd_ops [6 * n_bwd]   per adjoint op in walk order: variant x, message
  *                         slot written for child a and for child b (-1 none,
@@ -247,6 +251,20 @@ int netlk_adjoint_export(const netlk_ctx *ctx, int32_t *n_ops, int32_t *n_slot_r
  *   slot_reads [n_slot_reads]  message slots the adjoint ops read */
 int netlk_walk_export(const netlk_ctx *ctx, int32_t *n_fwd, int32_t *n_bwd, int32_t *n_slot_reads,
                       int32_t *fwd_variant, int32_t *bwd_ops, int32_t *slot_reads);
+/* The walk schedule per checkpoint segment, no counterpart in the reference
+ * (introspection of the checkpointed single-launch sweeps). n_segments (0
+ * without a walk schedule), n_recompute: variants the recompute walks
+ * compute. Arrays (NULL: not written), segment s:
+ *   bwd_range [2 * n_segments]       adjoint walk ops [begin, end) of s in
+ *                                    netlk_walk_export's bwd_ops; segments
+ *                                    launch from the top (highest s) down
+ *   recompute_variant [n_recompute]  variants recomputed, in walk order
+ *   recompute_range [2 * n_segments] [begin, end) of s in recompute_variant:
+ *                                    its non-permanent variants, recomputed
+ *                                    right before its adjoint launch (empty
+ *                                    for the top segment) */
+int netlk_walk_segments(const netlk_ctx *ctx, int32_t *n_segments, int32_t *n_recompute, int32_t *bwd_range,
+                        int32_t *recompute_variant, int32_t *recompute_range);
 
 /* ----------------------------------------------------- parameter updates */
 /* Replace linked_branch_lengths (src/optimization/NetworkState.cpp:93-306). */
@@ -354,10 +372,10 @@ int netlk_kernel_times(netlk_ctx *ctx, double *ms, int64_t *launches, int32_t n)
 int netlk_tuning(const netlk_ctx *ctx, int32_t *fwd_shape, int32_t *bwd_shape, double *fwd_ms,
                  double *bwd_ms, int32_t n);
 /* Index of the first walk shape in the autotuner's table: shapes from it on
- * run a sweep as one op walk per warp (whole DAG per launch) instead of one
- * launch per DAG level. Equals the table size where the context has no walk
- * shapes (20 states, FP64, several checkpoint segments). No counterpart in the
- * reference (measurement). */
+ * run a sweep as one op walk per warp (the whole DAG, or with checkpointing
+ * one segment, per launch) instead of one launch per DAG level. Equals the
+ * table size where the context has no walk shapes (20 states, FP64). No
+ * counterpart in the reference (measurement). */
 int netlk_walk_shape_begin(const netlk_ctx *ctx, int32_t *first_walk_shape);
 
 /* ---------------------------------------------------- allocation-free mixing */

@@ -39,6 +39,7 @@ EXPORTED = [
     "netlk_mix_site_loglikelihoods_noalloc", "netlk_batch_create",
     "netlk_batch_loglikelihood_gradient", "netlk_batch_destroy", "netlk_edge_loglikelihood",
     "netlk_last_site_updates", "netlk_encode_states", "netlk_compress_patterns", "netlk_inject_failure",
+    "netlk_walk_segments",
 ]
 
 
@@ -78,7 +79,7 @@ class DagStats(ctypes.Structure):
                 ("device_bytes", ctypes.c_int64), ("forward_bytes", ctypes.c_int64),
                 ("backward_bytes", ctypes.c_int64), ("launches_per_gradient_eval", ctypes.c_int64),
                 ("checkpoint_segments", ctypes.c_int32), ("clv_slots", ctypes.c_int32),
-                ("recompute_site_updates", ctypes.c_int64)]
+                ("recompute_site_updates", ctypes.c_int64), ("recompute_bytes", ctypes.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -129,6 +130,7 @@ def lib():
     L.netlk_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
     L.netlk_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_int64)]
     L.netlk_inject_failure.argtypes = [vp, ctypes.c_int32]
+    L.netlk_walk_segments.argtypes = [vp, c_int32_p, c_int32_p, c_int32_p, c_int32_p, c_int32_p]
     L.netlk_set_branch_lengths_device.argtypes = [vp, ctypes.c_void_p, ctypes.c_int32]
     L.netlk_enqueue.argtypes = [vp, ctypes.c_int32]
     L.netlk_result_pointers.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(vp)]

@@ -123,13 +123,22 @@ struct netlk_ctx {
   std::vector<double> clv_brlen;
   std::vector<FwdOp> ifwd;                 // ops of the variants to recompute
   std::vector<int32_t> ifwd_level_begin;
-  // walk schedules (one segment only): the whole sweep as one op list per
-  // warp, in a depth-first order; wbwd carries its level-schedule index in pad0
-  std::vector<FwdOp> wfwd;
+  // walk schedules: each sweep as one op list per warp, in a depth-first
+  // order kept segment by segment (so checkpointing works with them); wbwd
+  // carries its level-schedule index in pad0. With k segments the forward is
+  // one walk over all segments, the adjoint one walk per segment from the
+  // top, each but the top one after a walk recomputing that segment's
+  // non-permanent CLVs (wrfwd).
+  std::vector<FwdOp> wfwd, wrfwd;
   std::vector<BwdOp> wbwd;
   std::vector<int32_t> wmsg_slots;
+  std::vector<int32_t> wfwd_var, wrfwd_var, wbwd_var;    // variant of each walk op
+  std::vector<std::pair<int32_t, int32_t>> wrfwd_range;  // per segment: [begin, end) in wrfwd
+  std::vector<std::pair<int32_t, int32_t>> wbwd_range;   // per segment: [begin, end) in wbwd
   int n_wadj = 0;
   bool walk_ok = false;
+  int fwd_wshape = 0;  // forward walk shape the checkpoint recompute walks use
+  int rfwd_level_launches = 0;
   // best level-schedule shapes (the walk shapes only run the full sweeps)
   int fwd_lshape = 0, bwd_lshape = 0;
   int64_t last_updates = 0;
@@ -144,7 +153,7 @@ struct netlk_ctx {
   cudaStream_t stream = nullptr;
   int64_t dev_bytes = 0;
   DevBuf d_clv, d_scaler, d_adj, d_msg_slots, d_tips, d_weights, d_unit_part, d_fwd, d_bwd, d_rfwd, d_ifwd;
-  DevBuf d_wfwd, d_wbwd, d_wmsg_slots;
+  DevBuf d_wfwd, d_wrfwd, d_wbwd, d_wmsg_slots;
   // one edge's derivative: the adjoint ops its terms depend on (the ops that
   // use the edge and every op above them), run through the level kernel
   std::vector<std::vector<int32_t>> bwd_parents;  // adjoint op -> ops that send it a message
@@ -163,7 +172,7 @@ struct netlk_ctx {
   bool probs_dirty = true, model_dirty = true;
   bool device_brlen = false;  // last branch lengths came from device memory
   int64_t launches = 0;
-  int64_t fwd_bytes = 0, bwd_bytes = 0;
+  int64_t fwd_bytes = 0, bwd_bytes = 0, rfwd_bytes = 0;
   // per-kernel event timing (profiling mode launches without graphs)
   bool profiling = false;
   std::vector<cudaEvent_t> prof_ev;
@@ -209,7 +218,7 @@ struct netlk_ctx {
                       &d_brlen, &d_site_partial, &d_tree_logl, &d_root_slot, &d_root_lp, &d_root_dlp,
                       &d_seeds, &d_wts, &d_dret, &d_slot_begin, &d_slot_roots, &d_parts, &d_out, &d_grad_partial, &d_grad,
                       &d_edge_begin, &d_edge_entries, &d_op_sum, &d_weights32, &d_model32, &d_seeds32,
-                      &d_wfwd, &d_wbwd, &d_wmsg_slots})
+                      &d_wfwd, &d_wrfwd, &d_wbwd, &d_wmsg_slots})
       b->free();
     if (stream) cudaStreamDestroy(stream);
   }
@@ -297,6 +306,8 @@ struct netlk_ctx {
   void upload_model();
   void upload_probs();
   void enqueue(bool pm, bool fwd_on, bool reduce, bool mixk, bool bwd_on);
+  void enqueue_adjoint(const SweepParams &sp, int bshape);
+  bool adjoint_walks(int bshape) const;
   void run(cudaGraphExec_t *cache, bool pm, bool fwd_on, bool reduce, bool mixk, bool bwd_on);
   // logL recomputing only the CLVs above changed branch lengths; false when a
   // full evaluation is needed instead
@@ -424,6 +435,7 @@ void netlk_ctx::build_schedules(int segments) {
     rfwd_level_begin.push_back((int32_t)rfwd.size());
     rfwd_launches += rfwd_level_begin[L] > rfwd_level_begin[L - 1];
   }
+  rfwd_level_launches = rfwd_launches;
   recompute_updates = (int64_t)rfwd.size() * N;
   site_updates = (int64_t)V * N;
   const int64_t clv_b = (int64_t)R * S * (opts.precision == NETLK_FP32 ? 4 : 8);
@@ -437,6 +449,8 @@ void netlk_ctx::build_schedules(int segments) {
     fwd_bytes += N * (clv_b + 4 + child_bytes(op.a) + child_bytes(op.b));
     if (op.slot >= 0) fwd_bytes += (int64_t)n_units_fwd * 8;
   }
+  rfwd_bytes = 0;
+  for (const FwdOp &op : rfwd) rfwd_bytes += N * (clv_b + 4 + child_bytes(op.a) + child_bytes(op.b));
   // adjoint: variants reachable backwards from the displayed-tree roots
   std::vector<char> inb(V, 0);
   for (auto &rv : dag.roots) inb[rv.dtroot_variant] = 1;
@@ -539,22 +553,38 @@ void netlk_ctx::build_schedules(int segments) {
   }
 }
 
-// Walk schedules: with one segment (CLV slot = variant id) every op can run
-// in any topological order, one warp carrying its patterns through all of
-// them. The forward order is a depth-first post-order from the top levels
+// Walk schedules: a lane only reads values it wrote itself, so every op can
+// run in any topological order, one warp carrying its patterns through all
+// of them. The forward order is a depth-first post-order from the top levels
 // down, the child with the larger subtree first, so a child CLV is read soon
-// after it was written (while it is still in L2); the adjoint runs the
-// reverse order. Message slots are reused as soon as their reader has run.
+// after it was written (while it is still in L2), kept segment by segment:
+// a segment's non-permanent CLV slots are reused by the next segment, and
+// nothing outside a segment reads them. The adjoint runs the reverse order
+// (top segment first), one launch per segment, each but the top one after a
+// walk that recomputes the segment's non-permanent CLVs in forward walk
+// order. Message slots are reused as soon as their reader has run; a message
+// is handed over in registers only to the next op of the same launch.
 // Called while the level schedule's adjoint ops still hold variant ids.
 void netlk_ctx::build_walk(const std::vector<char> &inb, const std::vector<int> &slot_of,
                            const std::vector<std::vector<int>> &by_level, const std::vector<int> &bwd_var) {
   wfwd.clear();
+  wrfwd.clear();
   wbwd.clear();
   wmsg_slots.clear();
+  wfwd_var.clear();
+  wrfwd_var.clear();
+  wbwd_var.clear();
+  wrfwd_range.assign(n_segments, {0, 0});
+  wbwd_range.assign(n_segments, {0, 0});
   n_wadj = 0;
   walk_ok = false;
-  if (n_segments != 1 || S != 4) return;
+  if (S != 4) return;
   const int V = (int)dag.vars.size();
+  auto map_ref = [&](int32_t r) { return r >= 0 ? var_slot[r] : r; };
+  std::vector<int> seg_of_var(V, 0);
+  for (int v = 0; v < V; ++v)
+    for (int sg = 0; sg < n_segments; ++sg)
+      if (dag.vars[v].level >= seg_lo[sg] && dag.vars[v].level <= seg_hi[sg]) seg_of_var[v] = sg;
   std::vector<double> size(V, 1.0);  // ordering heuristic: shared descendants counted per path
   for (int L = 1; L <= dag.n_levels; ++L)
     for (int v : by_level[L])
@@ -585,9 +615,24 @@ void netlk_ctx::build_walk(const std::vector<char> &inb, const std::vector<int> 
         }
       }
     }
+  // segment by segment (a stable partition keeps the order topological)
+  std::stable_sort(order.begin(), order.end(), [&](int u, int v) { return seg_of_var[u] < seg_of_var[v]; });
   for (int v : order) {
     const Variant &var = dag.vars[v];
-    wfwd.push_back(FwdOp{v, var.ref[0], var.ref[1], var.edge[0], var.edge[1], slot_of[v], 0, 0});
+    wfwd.push_back(FwdOp{var_slot[v], map_ref(var.ref[0]), map_ref(var.ref[1]), var.edge[0], var.edge[1],
+                         slot_of[v], 0, 0});
+    wfwd_var.push_back(v);
+  }
+  for (int sg = n_segments - 2; sg >= 0; --sg) {
+    wrfwd_range[sg].first = (int32_t)wrfwd.size();
+    for (int v : order)
+      if (seg_of_var[v] == sg && !var_ckpt[v]) {
+        const Variant &var = dag.vars[v];
+        wrfwd.push_back(FwdOp{var_slot[v], map_ref(var.ref[0]), map_ref(var.ref[1]), var.edge[0], var.edge[1], -1,
+                              0, 0});
+        wrfwd_var.push_back(v);
+      }
+    wrfwd_range[sg].second = (int32_t)wrfwd.size();
   }
   std::vector<int> level_index(V, -1);
   for (size_t j = 0; j < bwd.size(); ++j) level_index[bwd_var[j]] = (int)j;
@@ -601,11 +646,13 @@ void netlk_ctx::build_walk(const std::vector<char> &inb, const std::vector<int> 
   for (int x : radj)
     for (int i = 0; i < 2; ++i)
       if (dag.vars[x].ref[i] >= 0) n_senders[dag.vars[x].ref[i]]++;
+  for (auto &r : wbwd_range) r = {-1, -1};
   int carried_to = -1;  // variant whose only message the previous op kept in registers
   for (size_t j = 0; j < radj.size(); ++j) {
     const int x = radj[j];
-    const int y = j + 1 < radj.size() ? radj[j + 1] : -1;
-    BwdOp op = bwd[level_index[x]];  // a, b still variant ids (= CLV slots here)
+    // the next op of the same launch (segment), if any
+    const int y = j + 1 < radj.size() && seg_of_var[radj[j + 1]] == seg_of_var[x] ? radj[j + 1] : -1;
+    BwdOp op = bwd[level_index[x]];  // a, b still variant ids
     op.pad0 = level_index[x];
     op.pad4 = x == carried_to;  // the adjoint starts from the message in registers
     carried_to = -1;
@@ -642,8 +689,16 @@ void netlk_ctx::build_walk(const std::vector<char> &inb, const std::vector<int> 
     }
     for (const auto &m : pending[x]) free_slots.push_back(m.second);
     pending[x].clear();
+    op.a = map_ref(op.a);
+    op.b = map_ref(op.b);
+    auto &rg = wbwd_range[seg_of_var[x]];
+    if (rg.first < 0) rg.first = (int32_t)wbwd.size();
     wbwd.push_back(op);
+    wbwd_var.push_back(x);
+    rg.second = (int32_t)wbwd.size();
   }
+  for (auto &r : wbwd_range)
+    if (r.first < 0) r = {0, 0};
   // the walk shares the message buffers sized for the level schedule
   walk_ok = n_wadj <= std::max(1, n_adj) && (int)wbwd.size() == n_bwd_real;
 }
@@ -714,6 +769,7 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
   d_rfwd.alloc(std::max<size_t>(1, rfwd.size()) * sizeof(FwdOp), dev_bytes);
   if (walk_ok) {
     d_wfwd.alloc(wfwd.size() * sizeof(FwdOp), dev_bytes);
+    d_wrfwd.alloc(std::max<size_t>(1, wrfwd.size()) * sizeof(FwdOp), dev_bytes);
     d_wbwd.alloc(std::max<size_t>(1, wbwd.size()) * sizeof(BwdOp), dev_bytes);
     d_wmsg_slots.alloc(std::max<size_t>(1, wmsg_slots.size()) * 4, dev_bytes);
   }
@@ -787,6 +843,8 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
     CUDA_OK(cudaMemcpyAsync(d_rfwd.p, rfwd.data(), rfwd.size() * sizeof(FwdOp), cudaMemcpyHostToDevice, stream));
   if (walk_ok) {
     CUDA_OK(cudaMemcpyAsync(d_wfwd.p, wfwd.data(), wfwd.size() * sizeof(FwdOp), cudaMemcpyHostToDevice, stream));
+    if (!wrfwd.empty())
+      CUDA_OK(cudaMemcpyAsync(d_wrfwd.p, wrfwd.data(), wrfwd.size() * sizeof(FwdOp), cudaMemcpyHostToDevice, stream));
     if (!wbwd.empty())
       CUDA_OK(cudaMemcpyAsync(d_wbwd.p, wbwd.data(), wbwd.size() * sizeof(BwdOp), cudaMemcpyHostToDevice, stream));
     if (!wmsg_slots.empty())
@@ -916,13 +974,39 @@ void netlk_ctx::enqueue(bool pm, bool fwd_on, bool reduce, bool mixk, bool bwd_o
     prof_mark(3);
   }
   if (bwd_on && !bwd.empty()) {
-    // segments from the top: recompute the segment's non-permanent CLVs
-    // (every segment but the last), then its adjoint levels
-    SweepParams rp = sp;
-    rp.fwd_ops = d_rfwd.as<FwdOp>();
-    for (int sg = n_segments - 1; sg >= 0; --sg) {
-      const int lo = seg_lo[sg], nl = seg_hi[sg] - seg_lo[sg] + 1;
-      if (sg < n_segments - 1) {
+    enqueue_adjoint(sp, bwd_shape);
+    prof_mark(4);
+    launch_grad_reduce(stream, (int)bwd.size(), topo.n_edges, n_units, d_edge_begin.as<int32_t>(),
+                       d_edge_entries.as<int32_t>(), d_grad_partial.as<double>(), d_op_sum.as<double>(),
+                       d_grad.as<double>(), opts.precision == NETLK_FP32);
+    prof_mark(5);
+  }
+}
+
+// The adjoint sweep with launch shape `bshape`: segments from the top, each
+// but the top one after recomputing its non-permanent CLVs. Walk shapes run
+// one walk launch per segment (and one recompute walk before it), level
+// shapes one launch per level.
+bool netlk_ctx::adjoint_walks(int bshape) const {
+  return S == 4 && walk_ok && bshape >= num_level_shapes(opts.precision, R);
+}
+
+void netlk_ctx::enqueue_adjoint(const SweepParams &sp, int bshape) {
+  const bool walk = adjoint_walks(bshape);
+  SweepParams rp = sp;
+  rp.fwd_ops = d_rfwd.as<FwdOp>();
+  for (int sg = n_segments - 1; sg >= 0; --sg) {
+    const int lo = seg_lo[sg], nl = seg_hi[sg] - seg_lo[sg] + 1;
+    if (sg < n_segments - 1) {
+      if (walk) {
+        const auto rg = wrfwd_range[sg];
+        if (rg.second > rg.first) {
+          SweepParams wp = sp;
+          wp.walk_fwd_ops = d_wrfwd.as<FwdOp>() + rg.first;
+          wp.n_walk_fwd = rg.second - rg.first;
+          launch_forward(stream, opts.precision, R, fwd_wshape, wp, nullptr, 0);
+        }
+      } else {
         const int32_t *rb = rfwd_level_begin.data() + (lo - 1);
         if (use_tc)
           launch_forward20_tc(stream, rp, rb, nl, sms);
@@ -931,19 +1015,24 @@ void netlk_ctx::enqueue(bool pm, bool fwd_on, bool reduce, bool mixk, bool bwd_o
         else
           launch_forward(stream, opts.precision, R, fwd_lshape, rp, rb, nl);
       }
-      const int32_t *bb = bwd_level_begin.data() + (dag.n_levels - seg_hi[sg]);
-      if (use_tc)
-        launch_backward20_tc(stream, sp, bb, nl, sms);
-      else if (S == 20)
-        launch_sweep20(stream, opts.precision, R, true, sp, bb, nl);
-      else
-        launch_backward(stream, opts.precision, R, bwd_shape, sp, bb, nl);
     }
-    prof_mark(4);
-    launch_grad_reduce(stream, (int)bwd.size(), topo.n_edges, n_units, d_edge_begin.as<int32_t>(),
-                       d_edge_entries.as<int32_t>(), d_grad_partial.as<double>(), d_op_sum.as<double>(),
-                       d_grad.as<double>(), opts.precision == NETLK_FP32);
-    prof_mark(5);
+    if (walk) {
+      const auto rg = wbwd_range[sg];
+      if (rg.second > rg.first) {
+        SweepParams wp = sp;
+        wp.walk_bwd_ops = d_wbwd.as<BwdOp>() + rg.first;
+        wp.n_walk_bwd = rg.second - rg.first;
+        launch_backward(stream, opts.precision, R, bshape, wp, nullptr, 0);
+      }
+      continue;
+    }
+    const int32_t *bb = bwd_level_begin.data() + (dag.n_levels - seg_hi[sg]);
+    if (use_tc)
+      launch_backward20_tc(stream, sp, bb, nl, sms);
+    else if (S == 20)
+      launch_sweep20(stream, opts.precision, R, true, sp, bb, nl);
+    else
+      launch_backward(stream, opts.precision, R, bshape, sp, bb, nl);
   }
 }
 
@@ -1089,17 +1178,30 @@ void netlk_ctx::count_launches() {
   if (S != 4) return;
   const SweepParams sp = sweep();
   fwd_launches = sweep_launches(opts.precision, R, fwd_shape, sp, false, fwd_level_begin.data(), dag.n_levels);
-  if (!bwd.empty())
+  if (bwd.empty()) return;
+  if (!adjoint_walks(bwd_shape)) {
     bwd_launches = sweep_launches(opts.precision, R, bwd_shape, sp, true, bwd_level_begin.data(), dag.n_levels);
+    rfwd_launches = rfwd_level_launches;
+    return;
+  }
+  // one walk (in chunks of at most one wave) per segment, plus the recompute walks
+  const int bw = sweep_launches(opts.precision, R, bwd_shape, sp, true, nullptr, 0);
+  const int fw = sweep_launches(opts.precision, R, fwd_wshape, sp, false, nullptr, 0);
+  bwd_launches = rfwd_launches = 0;
+  for (int sg = 0; sg < n_segments; ++sg) {
+    bwd_launches += wbwd_range[sg].second > wbwd_range[sg].first ? bw : 0;
+    rfwd_launches += wrfwd_range[sg].second > wrfwd_range[sg].first ? fw : 0;
+  }
 }
 
 void netlk_ctx::autotune() {
   tuned = true;
-  // walk shapes only where the walk schedule exists (one segment, DNA)
+  // walk shapes only where the walk schedule exists (DNA)
   const int nls = S == 4 ? num_level_shapes(opts.precision, R) : 1;
   const int ns = S == 4 && walk_ok ? num_shapes(opts.precision, R) : nls;
   tune_fwd_ms.assign(ns, 0.0);
   tune_bwd_ms.assign(ns, 0.0);
+  fwd_wshape = nls < ns ? nls : 0;
   if (const char *forced = std::getenv("NETLK_SHAPES")) {  // "fwd,bwd": fixed shapes, no timing
     int f = 0, b = 0;
     if (std::sscanf(forced, "%d,%d", &f, &b) == 2 && f >= 0 && f < ns && b >= 0 && b < ns) {
@@ -1107,11 +1209,15 @@ void netlk_ctx::autotune() {
       bwd_shape = b;
       fwd_lshape = f < nls ? f : 0;
       bwd_lshape = b < nls ? b : 0;
+      if (f >= nls) fwd_wshape = f;
       count_launches();
       return;
     }
   }
-  if (ns <= 1 || !opts.autotune) return;
+  if (ns <= 1 || !opts.autotune) {
+    count_launches();
+    return;
+  }
   std::memcpy(h_brlen.p, brlen.data(), brlen.size() * 8);
   CUDA_OK(cudaMemcpyAsync(d_brlen.p, h_brlen.p, brlen.size() * 8, cudaMemcpyHostToDevice, stream));
   enqueue(true, true, true, true, true);
@@ -1122,9 +1228,11 @@ void netlk_ctx::autotune() {
   auto time_one = [&](bool backward, int sh) {
     float best = 1e30f;
     for (int rep = 0; rep < 2; ++rep) {
+      // the adjoint (with its checkpoint recomputes) starts from a fresh forward
+      if (backward) launch_forward(stream, opts.precision, R, fwd_shape, sp, fwd_level_begin.data(), dag.n_levels);
       CUDA_OK(cudaEventRecord(e0, stream));
       if (backward)
-        launch_backward(stream, opts.precision, R, sh, sp, bwd_level_begin.data(), dag.n_levels);
+        enqueue_adjoint(sp, sh);
       else
         launch_forward(stream, opts.precision, R, sh, sp, fwd_level_begin.data(), dag.n_levels);
       CUDA_OK(cudaEventRecord(e1, stream));
@@ -1136,6 +1244,9 @@ void netlk_ctx::autotune() {
     return (double)best;
   };
   for (int sh = 0; sh < ns; ++sh) tune_fwd_ms[sh] = time_one(false, sh);
+  fwd_shape = (int)(std::min_element(tune_fwd_ms.begin(), tune_fwd_ms.end()) - tune_fwd_ms.begin());
+  if (nls < ns)
+    fwd_wshape = (int)(std::min_element(tune_fwd_ms.begin() + nls, tune_fwd_ms.end()) - tune_fwd_ms.begin());
   for (int sh = 0; sh < ns; ++sh) tune_bwd_ms[sh] = time_one(true, sh);
   CUDA_OK(cudaGetLastError());
   cudaEventDestroy(e0);
@@ -1406,6 +1517,7 @@ int netlk_get_dag_stats(const netlk_ctx *ctx, netlk_dag_stats *o) {
   o->checkpoint_segments = ctx->n_segments;
   o->clv_slots = ctx->n_clv_slots;
   o->recompute_site_updates = ctx->recompute_updates;
+  o->recompute_bytes = ctx->rfwd_bytes;
   return NETLK_OK;
 }
 
@@ -1439,15 +1551,37 @@ int netlk_walk_export(const netlk_ctx *ctx, int32_t *n_fwd, int32_t *n_bwd, int3
   if (n_slot_reads) *n_slot_reads = w ? (int32_t)ctx->wmsg_slots.size() : 0;
   if (!w) return NETLK_OK;
   if (fwd_variant)
-    for (size_t i = 0; i < ctx->wfwd.size(); ++i) fwd_variant[i] = ctx->wfwd[i].out;
+    for (size_t i = 0; i < ctx->wfwd.size(); ++i) fwd_variant[i] = ctx->wfwd_var[i];
   if (bwd_ops)
     for (size_t i = 0; i < ctx->wbwd.size(); ++i) {
       const BwdOp &o = ctx->wbwd[i];
-      const int32_t row[6] = {o.x, o.out_a, o.out_b, o.pad4, o.msg_begin, o.msg_count};
+      const int32_t row[6] = {ctx->wbwd_var[i], o.out_a, o.out_b, o.pad4, o.msg_begin, o.msg_count};
       for (int k = 0; k < 6; ++k) bwd_ops[6 * i + k] = row[k];
     }
   if (slot_reads)
     for (size_t i = 0; i < ctx->wmsg_slots.size(); ++i) slot_reads[i] = ctx->wmsg_slots[i];
+  return NETLK_OK;
+}
+
+int netlk_walk_segments(const netlk_ctx *ctx, int32_t *n_segments, int32_t *n_recompute, int32_t *bwd_range,
+                        int32_t *recompute_variant, int32_t *recompute_range) {
+  if (!ctx) return NETLK_ERR_INVALID_ARGUMENT;
+  const bool w = ctx->walk_ok;
+  if (n_segments) *n_segments = w ? ctx->n_segments : 0;
+  if (n_recompute) *n_recompute = w ? (int32_t)ctx->wrfwd_var.size() : 0;
+  if (!w) return NETLK_OK;
+  for (int sg = 0; sg < ctx->n_segments; ++sg) {
+    if (bwd_range) {
+      bwd_range[2 * sg] = ctx->wbwd_range[sg].first;
+      bwd_range[2 * sg + 1] = ctx->wbwd_range[sg].second;
+    }
+    if (recompute_range) {
+      recompute_range[2 * sg] = ctx->wrfwd_range[sg].first;
+      recompute_range[2 * sg + 1] = ctx->wrfwd_range[sg].second;
+    }
+  }
+  if (recompute_variant)
+    for (size_t i = 0; i < ctx->wrfwd_var.size(); ++i) recompute_variant[i] = ctx->wrfwd_var[i];
   return NETLK_OK;
 }
 

@@ -274,6 +274,20 @@ class NetworkLikelihood:
                                           _ptr(slots, ctypes.c_int32)), self._h)
         return fwd[:nf.value], bwd[:6 * nb.value].reshape(nb.value, 6), slots[:ns.value]
 
+    def walk_segments(self):
+        """Per checkpoint segment of the walk schedule: (adjoint op ranges
+        [n_segments][2] into walk_export's adjoint ops, recomputed variants,
+        their ranges [n_segments][2]); empty arrays without a walk schedule."""
+        ns, nr = ctypes.c_int32(), ctypes.c_int32()
+        N.check(N.lib().netlk_walk_segments(self._h, ctypes.byref(ns), ctypes.byref(nr), None, None, None),
+                self._h)
+        br = np.zeros(max(1, 2 * ns.value), np.int32)
+        rv = np.zeros(max(1, nr.value), np.int32)
+        rr = np.zeros(max(1, 2 * ns.value), np.int32)
+        N.check(N.lib().netlk_walk_segments(self._h, ctypes.byref(ns), ctypes.byref(nr), _ptr(br, ctypes.c_int32),
+                                            _ptr(rv, ctypes.c_int32), _ptr(rr, ctypes.c_int32)), self._h)
+        return (br[:2 * ns.value].reshape(-1, 2), rv[:nr.value], rr[:2 * ns.value].reshape(-1, 2))
+
     def get_clv(self, variant, part):
         n = self.n_patterns[part]
         clv = np.zeros(n * self.rate_cats * self.states)

@@ -285,7 +285,7 @@ def test_walk_schedule_invariants(case):
 @pytest.mark.parametrize("cfg", [1, 2])
 def test_walk_schedule_invariants_synthetic(cfg):
     """The 50-taxon / 4-reticulation and 100-taxon / 8-reticulation networks
-    (947 variants); with checkpoint segments there is no walk schedule."""
+    (947 variants), without and with checkpoint segments."""
     from netrax_gb300 import synth
     w = synth.config(cfg, scale=0.002)
     lik = NetworkLikelihood(w.network, w.partitions, host_only=True)
@@ -294,5 +294,5 @@ def test_walk_schedule_invariants_synthetic(cfg):
     assert (bwd[:, 1] == -2).sum() + (bwd[:, 2] == -2).sum() == bwd[:, 3].sum() > 0
     lik.close()
     seg = NetworkLikelihood(w.network, w.partitions, host_only=True, checkpoint_segments=2)
-    assert all(len(a) == 0 for a in seg.walk_export())
+    _check_walk(seg)
     seg.close()

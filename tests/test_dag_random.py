@@ -250,7 +250,71 @@ def test_random_network_checkpoint_plan_is_sound(seed):
         ns, n_slots, _, _, _ = lik.checkpoint_export()
         assert n_slots <= lik.n_variants
         _replay_checkpoint_plan(lik)
+        if len(lik.walk_export()[0]):
+            _replay_checkpointed_walk(lik)
         lik.close()
+
+
+def _replay_checkpointed_walk(lik):
+    """Replays the walk sweeps of a checkpointed context, as one warp runs
+    them, on symbolic buffers: the forward walk over every segment, then per
+    segment from the top a recompute walk of its non-permanent variants and
+    its adjoint walk. Every CLV read finds the expected variant in its buffer,
+    the recompute walk of a segment is exactly its non-permanent variants, a
+    message handed over in registers never crosses a launch, and every message
+    slot is read once, by its child, before it is written again."""
+    node, ch, _, _ = lik.dag_export()
+    ns, _, slot, perm, seg = lik.checkpoint_export()
+    fwd, bwd, reads = lik.walk_export()
+    brange, rvar, rrange = lik.walk_segments()
+    assert len(brange) == ns and len(rrange) == ns
+    V = len(node)
+    level = np.zeros(V, np.int64)
+    for v in range(V):
+        level[v] = 1 + max([level[int(c)] for c in ch[v] if c >= 0], default=0)
+    seg_of = np.searchsorted(seg[:, 1], level)  # segment of each variant's level
+    held = {}
+
+    def compute(v):
+        for c in ch[v]:
+            if c >= 0:
+                assert held.get(int(slot[c])) == int(c), ("child", int(v), int(c))
+        held[int(slot[v])] = int(v)
+
+    for v in fwd:
+        compute(v)
+    msgs = {}
+    covered = []
+    for s in range(ns - 1, -1, -1):
+        lo, hi = rrange[s]
+        if s == ns - 1:
+            assert lo == hi
+        want = sorted(v for v in range(V) if seg_of[v] == s and not perm[v]) if s < ns - 1 else []
+        assert sorted(rvar[lo:hi].tolist()) == want
+        for v in rvar[lo:hi]:
+            compute(v)
+        b0, b1 = brange[s]
+        covered += list(range(b0, b1))
+        carried = None
+        for x, oa, ob, from_regs, mb, mc in bwd[b0:b1].tolist():
+            assert seg_of[x] == s
+            assert held.get(int(slot[x])) == x, ("own CLV", x)
+            if from_regs:
+                assert carried == x
+            carried = None
+            for r in reads[mb:mb + mc].tolist():
+                assert msgs.pop(r) == x, "message read by the wrong op"
+            for c, out in zip(ch[x].tolist(), (oa, ob)):
+                if c >= 0:
+                    assert held.get(int(slot[c])) == c, ("adjoint child", x, c)
+                if out == -2:
+                    carried = c
+                elif out >= 0:
+                    assert out not in msgs, "message slot overwritten before it was read"
+                    msgs[out] = c
+        assert carried is None, "a message handed over in registers across a launch"
+    assert sorted(covered) == list(range(len(bwd)))
+    assert not msgs, "messages never read"
 
 
 def _replay_adjoint_messages(lik):
@@ -309,4 +373,19 @@ def test_checkpoint_export_without_segments():
     assert np.array_equal(slot, np.arange(lik.n_variants)) and perm.all()
     assert seg.tolist() == [[1, lik.stats["n_levels"]]]
     _replay_checkpoint_plan(lik)
+    _replay_checkpointed_walk(lik)
+    lik.close()
+
+
+@pytest.mark.parametrize("k", [2, 4, 6])
+def test_checkpointed_walk_on_the_100_taxon_network(k):
+    """The 100-taxon / 8-reticulation network (947 variants) with 2, 4 and 6
+    checkpoint segments: the walk sweeps replay soundly on symbolic buffers."""
+    from netrax_gb300 import synth
+    w = synth.config(2, scale=0.01)
+    lik = NetworkLikelihood(w.network, w.partitions, host_only=True, checkpoint_segments=k)
+    assert lik.checkpoint_export()[0] == k
+    assert len(lik.walk_export()[0]) == lik.n_variants
+    _replay_checkpoint_plan(lik)
+    _replay_checkpointed_walk(lik)
     lik.close()

@@ -388,6 +388,35 @@ def test_checkpointed_gradients_are_identical(kind):
                     assert tb2 == ta and np.array_equal(gb2, ga)
 
 
+@pytest.mark.parametrize("shapes", ["walk", "level"])
+def test_checkpointed_walk_sweeps_are_identical(shapes, monkeypatch):
+    """Checkpointing with the single-launch walk sweeps (one forward walk
+    over every segment; per segment from the top a recompute walk and an
+    adjoint walk), and with the level sweeps, on every walk shape: the logL
+    and gradient equal storing every CLV, bit for bit."""
+    from netrax_gb300 import synth
+    from netrax_gb300.likelihood import NetworkLikelihood
+    w = synth.config(2, scale=0.02)
+    import ctypes
+    from netrax_gb300 import _native as N
+    with NetworkLikelihood(w.network, w.partitions, checkpoint_segments=1) as a:
+        ta, ga, ra = a.loglikelihood_gradient()
+        ws = ctypes.c_int32()
+        N.check(N.lib().netlk_walk_shape_begin(a._h, ctypes.byref(ws)), a._h)
+        first_walk = ws.value
+    pairs = ([(first_walk + i, first_walk + j) for i, j in ((0, 0), (1, 2), (2, 3), (3, 4), (4, 1))]
+             if shapes == "walk" else [(0, 0), (3, 5), (11, 9)])
+    for k in (2, 4):
+        for f, b in pairs:
+            monkeypatch.setenv("NETLK_SHAPES", "%d,%d" % (f, b))
+            with NetworkLikelihood(w.network, w.partitions, checkpoint_segments=k) as lik:
+                tb, gb, rb = lik.loglikelihood_gradient()
+                t = lik.tuning()
+                assert t["backward_walk"] == (shapes == "walk") and t["backward_shape"] == b
+                assert lik.stats["checkpoint_segments"] == k
+                assert tb == ta and np.array_equal(gb, ga) and np.array_equal(rb, ra), (k, f, b)
+
+
 @pytest.mark.parametrize("kind", ["dna_fp32", "dna_fp64", "protein_tc"])
 def test_incremental_matches_full(kind):
     """Incremental evaluation (only the variants above changed branch
