@@ -323,10 +323,15 @@ int netlk_last_site_updates(const netlk_ctx *ctx, int64_t *site_updates);
  *   largest tree_logl * tree_prob. Trees are grouped by displayed tree at the
  *   network root (the reference groups by the virtually rerooted tree pairs
  *   at the edge).
- * d2 receives, when not NULL, the central difference of d1 over +-h (kept
- * inside [1e-6, 100]): h = min(1e-6, t/200) for FP64 contexts; for FP32 contexts
- * h = max(t/200, min(1e-4, (t - 1e-6)/3)), which keeps the FP32 rounding noise
- * of d1 from dominating (the reference computes d2 from its sumtables). */
+ * Both derivatives are analytic: one forward-mode (tangent) sweep over the
+ * variants above the edge gives every displayed tree's first and second
+ * derivative, which are then mixed like the reference's sumtable derivatives
+ * (LikelihoodDerivatives.cpp:13-188); the log-likelihood at the current
+ * lengths is recomputed on the way (incrementally). Contexts with several
+ * checkpoint segments or device-resident lengths take d1 from full adjoint
+ * sweeps and d2, when not NULL, as the central difference of d1 over +-h (kept
+ * inside [1e-6, 100]): h = min(1e-6, t/200) for FP64 contexts; for FP32
+ * contexts h = max(t/200, min(1e-4, (t - 1e-6)/3)). */
 int netlk_edge_derivatives(netlk_ctx *ctx, int32_t edge, int32_t mode,
                            double *d1, double *d2);
 

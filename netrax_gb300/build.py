@@ -13,7 +13,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libnetlk.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["dag.cpp", "model.cpp", "netlk.cpp", "kernels.cu", "kernels20.cu", "kernels20tc.cu", "noalloc.cu", "alignment.cpp"]
+SOURCES = ["dag.cpp", "model.cpp", "netlk.cpp", "kernels.cu", "kernels20.cu", "kernels20tc.cu", "tangent.cu",
+           "noalloc.cu", "alignment.cpp"]
 HEADERS = ["internal.hpp", "kernels.cuh", "kernels_common.cuh", "tc.cuh"]
 
 

@@ -145,6 +145,46 @@ void launch_sweep20(cudaStream_t s, int precision, int R, bool backward, const S
 bool sweep20_tc_supported(int precision, int R);
 void launch_forward20_tc(cudaStream_t s, const SweepParams &p, const int32_t *level_begin, int n_levels, int n_sms);
 void launch_backward20_tc(cudaStream_t s, const SweepParams &p, const int32_t *level_begin, int n_levels, int n_sms);
+// Forward-mode (tangent) sweep for the derivatives along one branch e
+// (tangent.cu). Op for a variant x whose subtree contains e: d = child on e's
+// side (mode 1: d hangs from e itself; mode 2: d contains e and its tangents
+// are in tangent slot td), o = the other child (ref as in FwdOp), ed / eo their
+// edges (eo = -1 for the fake child); tx: tangent slot x writes (-1: none
+// reads it); slot: displayed-tree root slot whose site sums x feeds, or -1.
+struct alignas(16) TanOp {
+  int32_t x, d, o, ed, eo, mode, td, tx, slot, pad0, pad1, pad2;
+};
+
+struct TanParams {
+  int64_t n_patterns;
+  int32_t n_edges;
+  int32_t n_blocks;             // blocks of tangent_patterns_per_block(R) patterns
+  const void *clv;              // [V][N][R][S] real
+  const int32_t *scaler;        // [V][N]
+  const uint8_t *tips;          // 4-state tip masks [n_tips][N]
+  const uint32_t *tips32;       // 20-state tip masks [n_tips][N]
+  const void *pmat;             // [n_parts][n_edges][R][S][S] real
+  const void *pderiv;           // [n_parts][2][R][S][S] real: d/dt and d2/dt2 of P_e
+  void *tan;                    // [n_tan][2][N][R][S] real: X', X''
+  const TanOp *ops;
+  const int32_t *block_part;    // [n_blocks] partition of each block
+  const double *weights;        // [N]
+  const double *freqs;          // [n_parts][S]
+  const double *rate_weights;   // [n_parts][R]
+  double *partial;              // [n_slots][2][n_blocks] sums of w L'/L and w (L''/L - (L'/L)^2)
+};
+
+int tangent_patterns_per_block(int R);
+void launch_pderiv(cudaStream_t s, int n_parts, int R, int S, const double *lambda, const double *U,
+                   const double *Uinv, const double *rates, double t, double *out64, float *out32);
+// One launch per level of ops [level_begin[L], level_begin[L+1]); false for
+// an unsupported (R, S).
+bool launch_tangent(cudaStream_t s, int precision, int R, int S, const TanParams &p, const int32_t *level_begin,
+                    int n_levels);
+// out [n_slots_total][n_parts][2] for the root slots listed in `slots`.
+void launch_tangent_reduce(cudaStream_t s, const TanParams &p, const int32_t *slots, int n_slots,
+                           const int32_t *part_block_begin, int n_parts, double *out);
+
 // Number of kernel launches issued by the launchers above (host counter).
 int64_t launches_issued();
 void add_launches(int64_t n);

@@ -154,19 +154,19 @@ struct netlk_ctx {
   int64_t dev_bytes = 0;
   DevBuf d_clv, d_scaler, d_adj, d_msg_slots, d_tips, d_weights, d_unit_part, d_fwd, d_bwd, d_rfwd, d_ifwd;
   DevBuf d_wfwd, d_wrfwd, d_wbwd, d_wmsg_slots;
-  // one edge's derivative: the adjoint ops its terms depend on (the ops that
-  // use the edge and every op above them), run through the level kernel
-  std::vector<std::vector<int32_t>> bwd_parents;  // adjoint op -> ops that send it a message
-  std::vector<BwdOp> ibwd;
-  std::vector<int32_t> ibwd_level_begin;
-  DevBuf d_ibwd;
+  // analytic edge derivatives: tangent buffers and per-call schedule
+  DevBuf d_tan, d_tan_ops, d_tan_partial, d_tan_out, d_pderiv64, d_pderiv32, d_block_part, d_part_block_begin,
+      d_tan_slots;
+  PinnedBuf h_tan_ops, h_tan_out, h_tan_slots;
+  int n_tan_cap = -1;  // tangent slot pairs allocated (-1: not set up yet)
+  int tan_blocks = 0;
   DevBuf d_pmat64, d_pmat32, d_lambda, d_U, d_Uinv, d_rates, d_rw, d_freqs, d_Q, d_brlen;
   // FP32 contexts: float copies the sweeps read (weights as hi/lo pairs)
   DevBuf d_weights32, d_model32, d_seeds32;
   size_t m32_freqs = 0, m32_rw = 0, m32_rates = 0;  // offsets (floats) in d_model32; Q at 0
   DevBuf d_site_partial, d_tree_logl, d_root_slot, d_root_lp, d_root_dlp, d_seeds, d_wts, d_dret;
   DevBuf d_slot_begin, d_slot_roots, d_parts, d_out, d_grad_partial, d_grad, d_edge_begin, d_edge_entries, d_op_sum;
-  PinnedBuf h_brlen, h_root_lp, h_root_dlp, h_out, h_grad, h_tree, h_ifwd, h_ibwd;
+  PinnedBuf h_brlen, h_root_lp, h_root_dlp, h_out, h_grad, h_tree, h_ifwd;
   cudaGraphExec_t graph_logl = nullptr, graph_grad = nullptr, graph_partials = nullptr,
                   graph_mixbwd = nullptr;
   bool probs_dirty = true, model_dirty = true;
@@ -218,7 +218,8 @@ struct netlk_ctx {
                       &d_brlen, &d_site_partial, &d_tree_logl, &d_root_slot, &d_root_lp, &d_root_dlp,
                       &d_seeds, &d_wts, &d_dret, &d_slot_begin, &d_slot_roots, &d_parts, &d_out, &d_grad_partial, &d_grad,
                       &d_edge_begin, &d_edge_entries, &d_op_sum, &d_weights32, &d_model32, &d_seeds32,
-                      &d_wfwd, &d_wrfwd, &d_wbwd, &d_wmsg_slots})
+                      &d_wfwd, &d_wrfwd, &d_wbwd, &d_wmsg_slots, &d_tan, &d_tan_ops, &d_tan_partial, &d_tan_out,
+                      &d_pderiv64, &d_pderiv32, &d_block_part, &d_part_block_begin, &d_tan_slots})
       b->free();
     if (stream) cudaStreamDestroy(stream);
   }
@@ -315,7 +316,15 @@ struct netlk_ctx {
   // d logL / d t_e from an incremental forward and the adjoint ops edge e's
   // terms depend on, bit-identical to the full gradient's entry; false where
   // the full evaluation is needed instead
-  bool edge_d1_partial(int e, double *d1);
+  // analytic d1 and d2 along edge e from a tangent sweep over the variants
+  // above it; false where that path does not apply (several checkpoint
+  // segments, device-resident lengths)
+  bool edge_derivs_analytic(int e, int mode, double *d1, double *d2);
+  int tangent_schedule(int e, std::vector<TanOp> &ops, std::vector<int32_t> &level_begin,
+                       std::vector<int32_t> &slots) const;
+  // roots (displayed trees) on which edge e counts as active for the
+  // reference's derivative formula
+  std::vector<char> active_roots_of(int e) const;
   void prepare_state();  // model / probabilities uploads and launch-shape tuning
   void prepare();        // prepare_state + branch-length upload
   void finish(double *total, double *part_logl, double *d_brlen, double *d_ret);
@@ -533,7 +542,6 @@ void netlk_ctx::build_schedules(int segments) {
     op.b = map_ref(op.b);
     op.pad0 = (int32_t)j;  // the op's grad_partial row, wherever it is launched from
   }
-  bwd_parents.clear();
   bwd_launches = 0;
   for (int L = 0; L < dag.n_levels; ++L) bwd_launches += bwd_level_begin[L + 1] > bwd_level_begin[L];
   // edge -> (adjoint op, side) entries for the gradient reduction
@@ -774,7 +782,6 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
     d_wmsg_slots.alloc(std::max<size_t>(1, wmsg_slots.size()) * 4, dev_bytes);
   }
   d_ifwd.alloc(fwd.size() * sizeof(FwdOp), dev_bytes);
-  d_ibwd.alloc(std::max<size_t>(1, bwd.size()) * sizeof(BwdOp), dev_bytes);
   const size_t nm = (size_t)P * topo.n_edges * R * S * S;
   d_pmat64.alloc(nm * 8, dev_bytes);
   if (opts.precision == NETLK_FP32) d_pmat32.alloc(nm * 4, dev_bytes);
@@ -869,7 +876,6 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
   h_grad.alloc(topo.n_edges * 8);
   h_tree.alloc((size_t)n_slots * P * 8);
   h_ifwd.alloc(fwd.size() * sizeof(FwdOp));
-  h_ibwd.alloc(std::max<size_t>(1, bwd.size()) * sizeof(BwdOp));
 }
 
 void netlk_ctx::upload_model() {
@@ -1111,62 +1117,240 @@ bool netlk_ctx::run_incremental() {
   return true;
 }
 
-bool netlk_ctx::edge_d1_partial(int e, double *d1) {
-  if (bwd.empty() || n_segments != 1 || !opts.incremental || device_brlen || profiling) return false;
-  prepare();
-  if (!run_incremental()) return false;
-  const int nb = (int)bwd.size();
-  if (bwd_parents.empty()) {  // with one segment CLV slots are variant ids
-    std::vector<int32_t> op_of(dag.vars.size(), -1);
-    for (int j = 0; j < nb; ++j) op_of[bwd[j].x] = j;
-    bwd_parents.assign(nb, {});
-    for (int j = 0; j < nb; ++j)
-      for (int32_t c : {bwd[j].a, bwd[j].b})
-        if (c >= 0 && op_of[c] >= 0) bwd_parents[op_of[c]].push_back(j);
+// isActiveBranch (src/helper/EdgeHelper.cpp:84-95): a displayed tree's
+// configuration set is compatible with taking this edge's parent; always true
+// for an edge that does not enter a reticulation.
+std::vector<char> netlk_ctx::active_roots_of(int edge) const {
+  const Topology &T = topo;
+  const int child = T.edge_child[edge], k = T.node_ret[child];
+  std::vector<char> act(dag.roots.size(), 1);
+  if (k < 0) return act;
+  const int want = edge == T.ret_second_edge[k] ? 1 : 0;
+  const size_t n_cfg = (size_t)1 << T.n_ret;
+  for (size_t i = 0; i < dag.roots.size(); ++i) {
+    const Bits &set = dag.vars[dag.roots[i].variant].set;
+    bool any = false;
+    for (size_t t = 0; t < n_cfg && !any; ++t)
+      if (set.test(t) && (int)((t >> k) & 1) == want) any = true;
+    act[i] = any;
   }
-  // the ops using edge e, closed upward: every message such an op reads comes
-  // from an op that runs in this call (parents precede children in bwd)
-  std::vector<char> need(nb, 0);
-  for (int j = 0; j < nb; ++j) need[j] = bwd[j].ea == e || (bwd[j].b != kFake && bwd[j].eb == e);
-  for (int j = nb - 1; j >= 0; --j)
-    if (need[j])
-      for (int32_t q : bwd_parents[j]) need[q] = 1;
-  ibwd.clear();
-  ibwd_level_begin.assign(1, 0);
-  int n_launch = 0;
+  return act;
+}
+
+// Tangent schedule for edge e, level by level over the forward schedule (one
+// checkpoint segment: CLV slots are variant ids): every variant whose
+// subtree contains e, with its e-side child (mode 1: the child hangs from e;
+// mode 2: the child contains e), tangent slots reused once their last reader's
+// level has run, and the displayed-tree root slots it feeds. Returns the
+// tangent slots needed, or -1 where a variant would contain e on both sides
+// (impossible in a displayed tree; the caller then takes another path).
+int netlk_ctx::tangent_schedule(int e, std::vector<TanOp> &ops, std::vector<int32_t> &level_begin,
+                                std::vector<int32_t> &slots) const {
+  const int V = (int)dag.vars.size();
+  std::vector<int32_t> dirty_op(V, -1);  // variant -> its tangent op
+  std::vector<int> last_read(V, -1);     // variant -> level of its last tangent reader
+  ops.clear();
+  slots.clear();
+  level_begin.assign(1, 0);
+  std::vector<int> lvl;
   for (int L = 0; L < dag.n_levels; ++L) {
-    for (int j = bwd_level_begin[L]; j < bwd_level_begin[L + 1]; ++j)
-      if (need[j]) ibwd.push_back(bwd[j]);  // pad0 keeps its grad_partial row
-    ibwd_level_begin.push_back((int32_t)ibwd.size());
-    n_launch += ibwd_level_begin[L + 1] > ibwd_level_begin[L];
+    for (int i = fwd_level_begin[L]; i < fwd_level_begin[L + 1]; ++i) {
+      const FwdOp &f = fwd[i];
+      const bool fake = f.b == kFake;
+      const bool da = f.a >= 0 && dirty_op[f.a] >= 0, db = f.b >= 0 && dirty_op[f.b] >= 0;
+      const bool ua = f.ea == e, ub = !fake && f.eb == e;
+      const int n_dirty = (int)da + (int)db + (int)ua + (int)ub;
+      if (n_dirty == 0) continue;
+      if (n_dirty > 1) return -1;
+      TanOp t{};
+      const bool side_a = da || ua;
+      t.x = f.out;
+      t.d = side_a ? f.a : f.b;
+      t.o = side_a ? f.b : f.a;
+      t.ed = side_a ? f.ea : f.eb;
+      t.eo = side_a ? (fake ? -1 : f.eb) : f.ea;
+      t.mode = (ua || ub) ? 1 : 2;
+      t.td = -1;
+      t.tx = -1;
+      t.slot = f.slot;
+      if (t.mode == 2) last_read[t.d] = L;
+      dirty_op[f.out] = (int32_t)ops.size();
+      ops.push_back(t);
+      lvl.push_back(L);
+      if (f.slot >= 0) slots.push_back(f.slot);
+    }
+    level_begin.push_back((int32_t)ops.size());
   }
-  std::memcpy(h_ibwd.p, ibwd.data(), ibwd.size() * sizeof(BwdOp));
-  CUDA_OK(cudaMemcpyAsync(d_ibwd.p, h_ibwd.p, ibwd.size() * sizeof(BwdOp), cudaMemcpyHostToDevice, stream));
-  SweepParams bp = sweep();
-  bp.bwd_ops = d_ibwd.as<BwdOp>();
-  if (use_tc)
-    launch_backward20_tc(stream, bp, ibwd_level_begin.data(), dag.n_levels, sms);
-  else if (S == 20)
-    launch_sweep20(stream, opts.precision, R, true, bp, ibwd_level_begin.data(), dag.n_levels);
-  else
-    launch_backward(stream, opts.precision, R, bwd_lshape, bp, ibwd_level_begin.data(), dag.n_levels);
-  // rows of the ops not run hold older values: only edge e's sum is read
-  launch_grad_reduce(stream, nb, topo.n_edges, n_units, d_edge_begin.as<int32_t>(), d_edge_entries.as<int32_t>(),
-                     d_grad_partial.as<double>(), d_op_sum.as<double>(), d_grad.as<double>(),
-                     opts.precision == NETLK_FP32);
-  launches += n_launch + 2;
+  // tangent slots: an op's output is kept only if a later level reads it;
+  // a slot read at level L is free again from level L + 1 on
+  std::vector<int> free_slots;
+  std::vector<std::vector<int>> release(dag.n_levels + 1);
+  int n_slots_used = 0;
+  for (int L = 0; L < dag.n_levels; ++L) {
+    for (int j = level_begin[L]; j < level_begin[L + 1]; ++j) {
+      TanOp &t = ops[j];
+      if (t.mode == 2) t.td = ops[dirty_op[t.d]].tx;
+      if (last_read[t.x] >= 0) {
+        if (!free_slots.empty()) {
+          t.tx = free_slots.back();
+          free_slots.pop_back();
+        } else {
+          t.tx = n_slots_used++;
+        }
+        release[last_read[t.x]].push_back(t.tx);
+      }
+    }
+    for (int sl : release[L]) free_slots.push_back(sl);
+  }
+  return n_slots_used;
+}
+
+bool netlk_ctx::edge_derivs_analytic(int e, int mode, double *d1, double *d2) {
+  if (n_segments != 1 || device_brlen) return false;
+  prepare();
+  const size_t real_b = opts.precision == NETLK_FP32 ? 4 : 8;
+  const size_t plane = (size_t)N * R * S * real_b;  // one tangent plane (X' or X'')
+  if (n_tan_cap < 0) {
+    // set up once: the most tangent slots any edge needs, and the block maps
+    int need = 0;
+    std::vector<TanOp> ops;
+    std::vector<int32_t> lb, sl;
+    for (int k = 0; k < topo.n_edges; ++k) need = std::max(need, tangent_schedule(k, ops, lb, sl));
+    const int ppb = tangent_patterns_per_block(R);
+    tan_blocks = (int)(N / ppb);
+    std::vector<int32_t> block_part(tan_blocks), pbb(P + 1);
+    for (int p = 0; p < P; ++p) {
+      pbb[p] = (int32_t)(parts[p].offset / ppb);
+      for (int64_t b = parts[p].offset / ppb; b < (parts[p].offset + parts[p].n_pad) / ppb; ++b) block_part[b] = p;
+    }
+    pbb[P] = tan_blocks;
+    if (N % ppb) throw Error(NETLK_ERR_INVALID_ARGUMENT, "tangent sweep: patterns not a whole number of blocks");
+    size_t free_b = 0, total_b = 0;
+    CUDA_OK(cudaMemGetInfo(&free_b, &total_b));
+    if ((double)need * 2 * plane > 0.5 * (double)free_b) {  // too big: keep the full-gradient path
+      n_tan_cap = 0;
+      return false;
+    }
+    int64_t scratch = 0;
+    d_tan.alloc(std::max<size_t>(1, (size_t)need) * 2 * plane, scratch);
+    d_tan_ops.alloc(dag.vars.size() * sizeof(TanOp), scratch);
+    d_tan_partial.alloc((size_t)std::max(1, n_slots) * 2 * tan_blocks * 8, scratch);
+    d_tan_out.alloc((size_t)std::max(1, n_slots) * P * 2 * 8, scratch);
+    d_tan_slots.alloc((size_t)std::max(1, n_slots) * 4, scratch);
+    d_pderiv64.alloc((size_t)P * 2 * R * S * S * 8, scratch);
+    d_pderiv32.alloc((size_t)P * 2 * R * S * S * 4, scratch);
+    d_block_part.alloc(block_part.size() * 4, scratch);
+    d_part_block_begin.alloc(pbb.size() * 4, scratch);
+    dev_bytes += scratch;
+    h_tan_ops.alloc(dag.vars.size() * sizeof(TanOp));
+    h_tan_out.alloc((size_t)std::max(1, n_slots) * P * 2 * 8);
+    h_tan_slots.alloc((size_t)std::max(1, n_slots) * 4);
+    CUDA_OK(cudaMemcpy(d_block_part.p, block_part.data(), block_part.size() * 4, cudaMemcpyHostToDevice));
+    CUDA_OK(cudaMemcpy(d_part_block_begin.p, pbb.data(), pbb.size() * 4, cudaMemcpyHostToDevice));
+    n_tan_cap = need;
+  }
+  std::vector<TanOp> ops;
+  std::vector<int32_t> lb, dslots;
+  const int need = tangent_schedule(e, ops, lb, dslots);
+  if (need < 0 || need > n_tan_cap || n_tan_cap == 0) return false;
+  // CLVs and per-tree logL at the current lengths
+  if (!run_incremental()) run(&graph_logl, true, true, true, true, false);
+  CUDA_OK(cudaMemcpyAsync(h_tree.p, d_tree_logl.p, (size_t)n_slots * P * 8, cudaMemcpyDeviceToHost, stream));
+  if (!ops.empty()) {
+    std::memcpy(h_tan_ops.p, ops.data(), ops.size() * sizeof(TanOp));
+    CUDA_OK(cudaMemcpyAsync(d_tan_ops.p, h_tan_ops.p, ops.size() * sizeof(TanOp), cudaMemcpyHostToDevice, stream));
+    std::memcpy(h_tan_slots.p, dslots.data(), dslots.size() * 4);
+    if (!dslots.empty())
+      CUDA_OK(cudaMemcpyAsync(d_tan_slots.p, h_tan_slots.p, dslots.size() * 4, cudaMemcpyHostToDevice, stream));
+    launch_pderiv(stream, P, R, S, d_lambda.as<double>(), d_U.as<double>(), d_Uinv.as<double>(), d_rates.as<double>(),
+                  brlen[e], d_pderiv64.as<double>(), opts.precision == NETLK_FP32 ? d_pderiv32.as<float>() : nullptr);
+    TanParams tp{};
+    tp.n_patterns = N;
+    tp.n_edges = topo.n_edges;
+    tp.n_blocks = tan_blocks;
+    tp.clv = d_clv.p;
+    tp.scaler = d_scaler.as<int32_t>();
+    tp.tips = S == 4 ? d_tips.as<uint8_t>() : nullptr;
+    tp.tips32 = S == 20 ? d_tips.as<uint32_t>() : nullptr;
+    tp.pmat = opts.precision == NETLK_FP32 ? d_pmat32.p : d_pmat64.p;
+    tp.pderiv = opts.precision == NETLK_FP32 ? d_pderiv32.p : d_pderiv64.p;
+    tp.tan = d_tan.p;
+    tp.ops = d_tan_ops.as<TanOp>();
+    tp.block_part = d_block_part.as<int32_t>();
+    tp.weights = d_weights.as<double>();
+    tp.freqs = d_freqs.as<double>();
+    tp.rate_weights = d_rw.as<double>();
+    tp.partial = d_tan_partial.as<double>();
+    if (!launch_tangent(stream, opts.precision, R, S, tp, lb.data(), dag.n_levels)) return false;
+    launch_tangent_reduce(stream, tp, d_tan_slots.as<int32_t>(), (int)dslots.size(),
+                          d_part_block_begin.as<int32_t>(), P, d_tan_out.as<double>());
+    if (!dslots.empty())
+      CUDA_OK(cudaMemcpyAsync(h_tan_out.p, d_tan_out.p, (size_t)n_slots * P * 2 * 8, cudaMemcpyDeviceToHost, stream));
+  }
   const int nout = 3 + P + topo.n_ret;
   CUDA_OK(cudaMemcpyAsync(h_out.p, d_out.p, nout * 8, cudaMemcpyDeviceToHost, stream));
-  CUDA_OK(cudaMemcpyAsync(h_grad.p, d_grad.as<double>() + e, 8, cudaMemcpyDeviceToHost, stream));
   CUDA_OK(cudaStreamSynchronize(stream));
   CUDA_OK(cudaGetLastError());
-  const double *o = h_out.as<double>();
   check_injected();
+  const double *o = h_out.as<double>();
   if (use_tc && *reinterpret_cast<const int32_t *>(o + nout - 1) != 0)
     throw Error(NETLK_ERR_TIMEOUT, "tensor-core sweep: an MMA completion wait timed out");
   if (o[1] != 0.0 || !std::isfinite(o[0]))
     throw Error(NETLK_ERR_NUMERIC, "Invalid network likelihood: negative infinity or NaN");
-  *d1 = h_grad.as<double>()[0];
+  // per-tree l' and l'' (0 for trees without e), mixed per partition
+  std::vector<char> has(n_slots, 0);
+  for (int32_t sl : dslots) has[sl] = 1;
+  const double *tl = h_tree.as<double>(), *tan = h_tan_out.as<double>();
+  const std::vector<char> act = mode == 1 ? active_roots_of(e) : std::vector<char>(dag.roots.size(), 1);
+  const double min_lp = opts.min_interesting_tree_logprob;
+  double D1 = 0.0, D2 = 0.0;
+  for (int p = 0; p < P; ++p) {
+    auto a1 = [&](size_t i) { return has[root_slot[i]] ? tan[((size_t)root_slot[i] * P + p) * 2] : 0.0; };
+    auto a2 = [&](size_t i) { return has[root_slot[i]] ? tan[((size_t)root_slot[i] * P + p) * 2 + 1] : 0.0; };
+    auto ll = [&](size_t i) { return tl[(size_t)root_slot[i] * P + p]; };
+    if (opts.variant == NETLK_AVERAGE) {
+      double m = -INFINITY;
+      for (size_t i = 0; i < dag.roots.size(); ++i)
+        if (act[i] && dag.roots[i].logprob >= min_lp) m = std::max(m, dag.roots[i].logprob + ll(i));
+      if (!(m > -INFINITY)) {
+        if (mode == 1) throw Error(NETLK_ERR_NUMERIC, "no displayed tree contains the edge");
+        continue;
+      }
+      double z = 0.0, s1 = 0.0, s2 = 0.0;
+      for (size_t i = 0; i < dag.roots.size(); ++i) {
+        if (!act[i] || dag.roots[i].logprob < min_lp) continue;
+        const double w = std::exp(dag.roots[i].logprob + ll(i) - m);
+        z += w;
+        s1 += w * a1(i);
+        s2 += w * (a2(i) + a1(i) * a1(i));
+      }
+      const double g = s1 / z;
+      D1 += g;
+      D2 += s2 / z - g * g;
+    } else {
+      int best = -1;
+      double score = -INFINITY;
+      for (size_t i = 0; i < dag.roots.size(); ++i) {
+        const double lpi = dag.roots[i].logprob;
+        if (!act[i] || lpi < min_lp) continue;
+        // mode 0: the tree the BEST mixture takes (ties to the lower index);
+        // mode 1: the reference's choice by tree_logl * tree_prob
+        const double v = mode == 1 ? ll(i) * std::exp(lpi) : lpi + ll(i);
+        if (best < 0 || v > score) {
+          score = v;
+          best = (int)i;
+        }
+      }
+      if (best < 0) {
+        if (mode == 1) throw Error(NETLK_ERR_NUMERIC, "no displayed tree contains the edge");
+        continue;
+      }
+      D1 += a1(best);
+      D2 += a2(best);
+    }
+  }
+  if (d1) *d1 = D1;
+  if (d2) *d2 = D2;
   return true;
 }
 
@@ -1706,26 +1890,8 @@ int netlk_loglikelihood_gradient(netlk_ctx *ctx, double *total, double *part_log
 
 namespace {
 
-// Roots (displayed trees) on which an edge counts as active for the
-// reference's derivative: isActiveBranch (src/helper/EdgeHelper.cpp:84-95)
-// - the tree's configuration set is compatible with taking this edge's
-// parent; always true for an edge that does not enter a reticulation.
-std::vector<char> active_roots(const netlk_ctx *c, int edge) {
-  const Topology &T = c->topo;
-  const int child = T.edge_child[edge], k = T.node_ret[child];
-  std::vector<char> act(c->dag.roots.size(), 1);
-  if (k < 0) return act;
-  const int want = edge == T.ret_second_edge[k] ? 1 : 0;
-  const size_t n_cfg = (size_t)1 << T.n_ret;
-  for (size_t i = 0; i < c->dag.roots.size(); ++i) {
-    const Bits &set = c->dag.vars[c->dag.roots[i].variant].set;
-    bool any = false;
-    for (size_t t = 0; t < n_cfg && !any; ++t)
-      if (set.test(t) && (int)((t >> k) & 1) == want) any = true;
-    act[i] = any;
-  }
-  return act;
-}
+// Roots on which an edge is active for the reference's derivative formula.
+std::vector<char> active_roots(const netlk_ctx *c, int edge) { return c->active_roots_of(edge); }
 
 // d logL / d t_edge as the reference's computeLoglikelihoodDerivatives
 // computes it (src/likelihood/LikelihoodDerivatives.cpp:30-183), per
@@ -1784,11 +1950,12 @@ int netlk_edge_derivatives(netlk_ctx *ctx, int32_t edge, int32_t mode, double *d
   return guarded(ctx, [&] {
     if (edge < 0 || edge >= ctx->topo.n_edges) throw Error(NETLK_ERR_INVALID_ARGUMENT, "edge");
     if (mode != 0 && mode != 1) throw Error(NETLK_ERR_INVALID_ARGUMENT, "mode must be 0 or 1");
-    // first derivative at the context's current lengths
+    // analytic d1 and d2 from one tangent sweep over the variants above the edge
+    if (ctx->edge_derivs_analytic(edge, mode, d1, d2)) return;
+    // checkpointed contexts and device-resident lengths: d1 from full adjoint
+    // sweeps, d2 as a central difference of d1 (below)
     auto first = [&]() -> double {
       if (mode == 1) return reference_edge_d1(ctx, edge);
-      double d;
-      if (ctx->edge_d1_partial(edge, &d)) return d;
       std::vector<double> g(ctx->topo.n_edges);
       double tot;
       ctx->prepare();

@@ -1,0 +1,308 @@
+// Analytic first and second derivatives of the network log-likelihood along
+// one branch, by forward-mode differentiation of the pruning above it.
+//
+// For the branch e and every variant x whose subtree contains e, with
+// X = f (M_d d) * (M_o o) (d the child on e's side, o the other child, f the
+// op's power-of-two rescaling), the tangents are
+//   X'  = f (M'_e d) * (M_o o),  X'' = f (M''_e d) * (M_o o)   where d hangs from e,
+//   X'  = f (M_d d') * (M_o o),  X'' = f (M_d d'') * (M_o o)   where d contains e,
+// (a branch occurs at most once in a displayed tree, so never on both sides).
+// At a displayed tree's root, L'/L and L''/L per site follow from the same
+// root sums as L; per tree, l' = sum_s w_s L'/L and l'' = sum_s w_s (L''/L -
+// (L'/L)^2). The host mixes the trees (AVERAGE: posterior-weighted; BEST: the
+// chosen tree). The reference evaluates the same per-tree derivatives through
+// sumtables at the virtually rerooted branch
+// (src/likelihood/LikelihoodDerivatives.cpp:249-344, pll_compute_loglikelihood_derivatives
+// at :95-104) and combines them at :13-188.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "kernels.cuh"
+
+namespace netlk {
+
+namespace {
+
+// dP/dt and d2P/dt2 of P(rho_r t) = U diag(exp(lambda rho_r t)) U^-1 for one
+// branch length t, every partition and rate: out [part][2][R][S][S].
+__global__ void pderiv_kernel(int n_parts, int R, int S, const double *__restrict__ lambda,
+                              const double *__restrict__ U, const double *__restrict__ Uinv,
+                              const double *__restrict__ rates, double t, double *__restrict__ out64,
+                              float *__restrict__ out32) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int SS = S * S;
+  const int64_t total = (int64_t)n_parts * 2 * R * SS;
+  if (idx >= total) return;
+  const int ij = (int)(idx % SS);
+  const int i = ij / S, j = ij - i * S;
+  const int64_t q = idx / SS;  // (part, order, rate)
+  const int rr = (int)(q % R);
+  const int order = (int)(q / R % 2);
+  const int part = (int)(q / R / 2);
+  const double rho = rates[part * R + rr];
+  double v = 0.0;
+  for (int k = 0; k < S; ++k) {
+    const double lr = lambda[part * S + k] * rho;
+    const double f = order ? lr * lr : lr;
+    v += U[(size_t)part * SS + i * S + k] * f * exp(lr * t) * Uinv[(size_t)part * SS + k * S + j];
+  }
+  out64[idx] = v;
+  if (out32) out32[idx] = (float)v;
+}
+
+// x times the op's rescaling factor for a counter increase of k: FP32
+// counters count single powers of two, FP64 counters factors of 2^256.
+template <typename real>
+struct ScaleShift;
+template <>
+struct ScaleShift<float> {
+  static __device__ __forceinline__ float apply(float x, int k) { return ldexpf(x, k); }
+};
+template <>
+struct ScaleShift<double> {
+  static __device__ __forceinline__ double apply(double x, int k) { return ldexp(x, 256 * k); }
+};
+
+// One child's row for the thread's (pattern, rate): a CLV row, a tip's 0/1
+// state mask, or the fake child's ones; returns its scale counter.
+template <typename real, int R, int S>
+__device__ __forceinline__ int load_row(const TanParams &p, int32_t ref, int64_t s, int r, real (&c)[S]) {
+  if (ref >= 0) {
+    const real *src = static_cast<const real *>(p.clv) + (((size_t)ref * p.n_patterns + s) * R + r) * S;
+#pragma unroll
+    for (int i = 0; i < S; ++i) c[i] = src[i];
+    return p.scaler[(size_t)ref * p.n_patterns + s];
+  }
+  if (ref == INT32_MIN) {
+#pragma unroll
+    for (int i = 0; i < S; ++i) c[i] = (real)1;
+    return 0;
+  }
+  uint32_t code;
+  if constexpr (S == 4)
+    code = p.tips[(size_t)(-1 - ref) * p.n_patterns + s];
+  else
+    code = p.tips32[(size_t)(-1 - ref) * p.n_patterns + s];
+#pragma unroll
+  for (int i = 0; i < S; ++i) c[i] = (real)((code >> i) & 1u);
+  return 0;
+}
+
+template <typename real, int S>
+__device__ __forceinline__ void matvec(const real *M, const real (&x)[S], real (&y)[S]) {
+#pragma unroll
+  for (int i = 0; i < S; ++i) {
+    real acc = M[i * S] * x[0];
+#pragma unroll
+    for (int j = 1; j < S; ++j) acc = fma(M[i * S + j], x[j], acc);
+    y[i] = acc;
+  }
+}
+
+// One launch per DAG level (blockIdx.y = op of the level); a thread owns one
+// (pattern, rate), a block 256 / R patterns of one partition. Shared memory:
+// the other side's P, then the two matrices applied to the e side (P'_e and
+// P''_e, or P_d twice).
+template <typename real, int R, int S>
+__global__ void __launch_bounds__(256) tangent_kernel(const TanParams p, int op_begin) {
+  constexpr int RSS = R * S * S;
+  constexpr int SPB = 256 / R;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  real *sM = reinterpret_cast<real *>(smem_raw);
+  const TanOp op = p.ops[op_begin + blockIdx.y];
+  const int part = p.block_part[blockIdx.x];
+  const real *pm = static_cast<const real *>(p.pmat) + (size_t)part * p.n_edges * RSS;
+  const real *pd = static_cast<const real *>(p.pderiv) + (size_t)part * 2 * RSS;
+  for (int i = threadIdx.x; i < RSS; i += blockDim.x) {
+    sM[i] = op.eo >= 0 ? pm[(size_t)op.eo * RSS + i] : (real)0;
+    if (op.mode == 1) {
+      sM[RSS + i] = pd[i];
+      sM[2 * RSS + i] = pd[RSS + i];
+    } else {
+      const real v = pm[(size_t)op.ed * RSS + i];
+      sM[RSS + i] = v;
+      sM[2 * RSS + i] = v;
+    }
+  }
+  __syncthreads();
+  const int r = threadIdx.x % R;
+  const int64_t s = (int64_t)blockIdx.x * SPB + threadIdx.x / R;
+  real c[S], vo[S], t1[S], t2[S];
+  const int so = load_row<real, R, S>(p, op.o, s, r, c);
+  if (op.o == INT32_MIN) {
+#pragma unroll
+    for (int i = 0; i < S; ++i) vo[i] = (real)1;
+  } else {
+    matvec<real, S>(sM + r * S * S, c, vo);
+  }
+  int sd;
+  if (op.mode == 1) {
+    sd = load_row<real, R, S>(p, op.d, s, r, c);
+    matvec<real, S>(sM + RSS + r * S * S, c, t1);
+    matvec<real, S>(sM + 2 * RSS + r * S * S, c, t2);
+  } else {
+    sd = p.scaler[(size_t)op.d * p.n_patterns + s];
+    const size_t plane = (size_t)p.n_patterns * R * S;
+    const real *src = static_cast<const real *>(p.tan) + (size_t)op.td * 2 * plane + ((size_t)s * R + r) * S;
+#pragma unroll
+    for (int i = 0; i < S; ++i) c[i] = src[i];
+    matvec<real, S>(sM + RSS + r * S * S, c, t1);
+#pragma unroll
+    for (int i = 0; i < S; ++i) c[i] = src[plane + i];
+    matvec<real, S>(sM + 2 * RSS + r * S * S, c, t2);
+  }
+  const int k = p.scaler[(size_t)op.x * p.n_patterns + s] - sd - so;
+#pragma unroll
+  for (int i = 0; i < S; ++i) {
+    t1[i] = ScaleShift<real>::apply(t1[i] * vo[i], k);
+    t2[i] = ScaleShift<real>::apply(t2[i] * vo[i], k);
+  }
+  if (op.tx >= 0) {
+    const size_t plane = (size_t)p.n_patterns * R * S;
+    real *dst = static_cast<real *>(p.tan) + (size_t)op.tx * 2 * plane + ((size_t)s * R + r) * S;
+#pragma unroll
+    for (int i = 0; i < S; ++i) {
+      dst[i] = t1[i];
+      dst[plane + i] = t2[i];
+    }
+  }
+  if (op.slot < 0) return;  // uniform over the block
+  // displayed-tree root: L, L', L'' of the site (sums over the R rate lanes)
+  const real *xr = static_cast<const real *>(p.clv) + (((size_t)op.x * p.n_patterns + s) * R + r) * S;
+  const double rw = p.rate_weights[part * R + r];
+  double L = 0.0, L1 = 0.0, L2 = 0.0;
+#pragma unroll
+  for (int i = 0; i < S; ++i) {
+    const double pi = p.freqs[part * S + i];
+    L += pi * (double)xr[i];
+    L1 += pi * (double)t1[i];
+    L2 += pi * (double)t2[i];
+  }
+  L *= rw;
+  L1 *= rw;
+  L2 *= rw;
+#pragma unroll
+  for (int o = 1; o < R; o <<= 1) {
+    L += __shfl_xor_sync(0xffffffffu, L, o);
+    L1 += __shfl_xor_sync(0xffffffffu, L1, o);
+    L2 += __shfl_xor_sync(0xffffffffu, L2, o);
+  }
+  double a1 = 0.0, a2 = 0.0;
+  if (r == 0) {
+    const double w = p.weights[s];
+    if (w != 0.0) {
+      const double r1 = L1 / L, r2 = L2 / L;
+      a1 = w * r1;
+      a2 = w * (r2 - r1 * r1);
+    }
+  }
+  // fixed-order block sum: warp shuffles, then warp 0 over the warp sums
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a1 += __shfl_down_sync(0xffffffffu, a1, o);
+    a2 += __shfl_down_sync(0xffffffffu, a2, o);
+  }
+  __shared__ double red[2][8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    red[0][warp] = a1;
+    red[1][warp] = a2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double b1 = 0.0, b2 = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+      b1 += red[0][k];
+      b2 += red[1][k];
+    }
+    p.partial[((size_t)op.slot * 2 + 0) * p.n_blocks + blockIdx.x] = b1;
+    p.partial[((size_t)op.slot * 2 + 1) * p.n_blocks + blockIdx.x] = b2;
+  }
+}
+
+// out[(slot * n_parts + part) * 2 + q] = compensated sum of the slot's block
+// partials over the partition's blocks, for the slots listed in `slots`.
+__global__ void tangent_reduce_kernel(const TanParams p, const int32_t *__restrict__ slots,
+                                      const int32_t *__restrict__ part_block_begin, int n_parts,
+                                      double *__restrict__ out) {
+  const int slot = slots[blockIdx.x], part = blockIdx.y, q = blockIdx.z;
+  const int b0 = part_block_begin[part], b1 = part_block_begin[part + 1];
+  const double *src = p.partial + ((size_t)slot * 2 + q) * p.n_blocks;
+  double s = 0.0, c = 0.0;
+  for (int b = b0 + threadIdx.x; b < b1; b += blockDim.x) {
+    const double y = src[b] - c;
+    const double t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __shared__ double red[128];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[((size_t)slot * n_parts + part) * 2 + q] = red[0];
+}
+
+template <typename real, int R, int S>
+void run_levels(cudaStream_t st, const TanParams &p, const int32_t *level_begin, int n_levels) {
+  const size_t smem = 3 * (size_t)R * S * S * sizeof(real);
+  for (int L = 0; L < n_levels; ++L) {
+    const int n = level_begin[L + 1] - level_begin[L];
+    if (n > 0) tangent_kernel<real, R, S><<<dim3(p.n_blocks, n), 256, smem, st>>>(p, level_begin[L]);
+  }
+}
+
+template <typename real>
+bool dispatch_levels(cudaStream_t st, int R, int S, const TanParams &p, const int32_t *level_begin, int n_levels) {
+  if (S == 4) {
+    switch (R) {
+      case 1: run_levels<real, 1, 4>(st, p, level_begin, n_levels); return true;
+      case 2: run_levels<real, 2, 4>(st, p, level_begin, n_levels); return true;
+      case 4: run_levels<real, 4, 4>(st, p, level_begin, n_levels); return true;
+      case 8: run_levels<real, 8, 4>(st, p, level_begin, n_levels); return true;
+      default: return false;
+    }
+  }
+  if (S == 20) {
+    switch (R) {
+      case 1: run_levels<real, 1, 20>(st, p, level_begin, n_levels); return true;
+      case 2: run_levels<real, 2, 20>(st, p, level_begin, n_levels); return true;
+      case 4: run_levels<real, 4, 20>(st, p, level_begin, n_levels); return true;
+      default: return false;
+    }
+  }
+  return false;
+}
+
+}  // namespace
+
+int tangent_patterns_per_block(int R) { return 256 / R; }
+
+void launch_pderiv(cudaStream_t s, int n_parts, int R, int S, const double *lambda, const double *U,
+                   const double *Uinv, const double *rates, double t, double *out64, float *out32) {
+  const int64_t total = (int64_t)n_parts * 2 * R * S * S;
+  pderiv_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(n_parts, R, S, lambda, U, Uinv, rates, t, out64,
+                                                                out32);
+  add_launches(1);
+}
+
+bool launch_tangent(cudaStream_t s, int precision, int R, int S, const TanParams &p, const int32_t *level_begin,
+                    int n_levels) {
+  const bool ok = precision == 1 ? dispatch_levels<float>(s, R, S, p, level_begin, n_levels)
+                                 : dispatch_levels<double>(s, R, S, p, level_begin, n_levels);
+  if (ok)
+    for (int L = 0; L < n_levels; ++L) add_launches(level_begin[L + 1] > level_begin[L]);
+  return ok;
+}
+
+void launch_tangent_reduce(cudaStream_t s, const TanParams &p, const int32_t *slots, int n_slots,
+                           const int32_t *part_block_begin, int n_parts, double *out) {
+  if (n_slots <= 0) return;
+  tangent_reduce_kernel<<<dim3(n_slots, n_parts, 2), 128, 0, s>>>(p, slots, part_block_begin, n_parts, out);
+  add_launches(1);
+}
+
+}  // namespace netlk

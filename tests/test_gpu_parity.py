@@ -534,39 +534,62 @@ def test_walk_sweeps_in_several_chunks(monkeypatch):
 
 
 @pytest.mark.parametrize("config", [1, 3], ids=["dna", "protein"])
-@pytest.mark.parametrize("precision", ["fp32", "fp64"])
-def test_edge_derivatives_from_partial_adjoint(precision, config):
-    """netlk_edge_derivatives mode 0 runs an incremental forward and only the
-    adjoint ops the edge's terms depend on; its d1 is the full gradient's
-    entry bit for bit, and d2 the central difference of two full gradients
-    (step min(1e-6, t/200) in FP64, max(t/200, min(1e-4, (t - 1e-6)/3)) in FP32). DNA
-    (50 taxa, 10 partitions) and protein (40 taxa; FP32 on the tensor cores)."""
+def test_edge_derivatives_match_full_gradients(config):
+    """netlk_edge_derivatives takes d1 and d2 analytically from one tangent
+    sweep over the variants above the edge. DNA (50 taxa, 10 partitions) and
+    protein (40 taxa): FP64 d1 equals the adjoint gradient's entry (1e-10
+    relative) and d2 the central difference of two FP64 full gradients
+    (1e-5); FP32 d1 and d2 equal the FP64 ones (1e-5 of max(1, |value|));
+    the context keeps evaluating the network at its own lengths."""
     from netrax_gb300 import synth
     from netrax_gb300.likelihood import NetworkLikelihood
     w = synth.config(config, scale=0.02)
     net = w.network
-    with NetworkLikelihood(net, w.partitions, precision=precision) as lik:
+    ret_edges = [int(x) for x in net.ret_first_edge] + [int(x) for x in net.ret_second_edge]
+    tip_edges = [e for e in range(net.n_edges) if int(net.edge_child[e]) < net.n_tips][:2]
+    inner = [e for e in range(net.n_edges) if e not in ret_edges and e not in tip_edges][:3]
+    edges = ret_edges[:2] + tip_edges + inner
+    base = np.array(net.branch_lengths, np.float64)
+    want = {}
+    with NetworkLikelihood(net, w.partitions, precision="fp64") as lik:
         logl0, g0, _ = lik.loglikelihood_gradient()
-        base = np.array(net.branch_lengths, np.float64)
-        ret_edges = [int(x) for x in net.ret_first_edge] + [int(x) for x in net.ret_second_edge]
-        tip_edges = [e for e in range(lik.n_edges) if int(net.edge_child[e]) < net.n_tips][:2]
-        inner = [e for e in range(lik.n_edges) if e not in ret_edges and e not in tip_edges][:3]
-        for e in ret_edges[:2] + tip_edges + inner:
-            d1 = lik.edge_derivatives(e, second=False)
-            assert d1 == g0[e]
-            d1b, d2 = lik.edge_derivatives(e, second=True)
-            assert d1b == g0[e]
+        for e in edges:
+            d1, d2 = lik.edge_derivatives(e, second=True)
+            assert d1 == pytest.approx(g0[e], rel=1e-10, abs=1e-8)
             t = base[e]
-            h = max(t / 200.0, min(1e-4, (t - 1e-6) / 3.0)) if precision == "fp32" else min(1e-6, t / 200.0)
+            h = min(1e-6, t / 200.0)
             b = base.copy()
-            b[e] = min(t + h, 100.0)
-            hp = b[e] - t
+            b[e] = t + h
             lik.set_branch_lengths(b)
             gp = lik.loglikelihood_gradient()[1][e]
             b[e] = max(t - h, 1e-6)
-            hm = t - b[e]
             lik.set_branch_lengths(b)
             gm = lik.loglikelihood_gradient()[1][e]
             lik.set_branch_lengths(base)
-            assert d2 == (gp - gm) / (hp + hm)
+            assert d2 == pytest.approx((gp - gm) / (t + h - b[e]), rel=1e-5, abs=1e-3)
             assert lik.loglikelihood() == logl0
+            want[e] = (d1, d2)
+    with NetworkLikelihood(net, w.partitions, precision="fp32") as lik:
+        for e in edges:
+            d1, d2 = lik.edge_derivatives(e, second=True)
+            assert abs(d1 - want[e][0]) <= 1e-5 * max(1.0, abs(want[e][0]))
+            assert abs(d2 - want[e][1]) <= 1e-5 * max(1.0, abs(want[e][1]))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_checkpointed_edge_derivatives_take_the_full_path(precision):
+    """With several checkpoint segments netlk_edge_derivatives takes d1 from
+    full adjoint sweeps and d2 as a central difference: they agree with the
+    analytic values of a context that stores every CLV."""
+    from netrax_gb300 import synth
+    from netrax_gb300.likelihood import NetworkLikelihood
+    w = synth.config(2, scale=0.01)
+    edges = [0, 5, 17, int(w.network.ret_first_edge[0])]
+    with NetworkLikelihood(w.network, w.partitions, precision=precision) as a, \
+            NetworkLikelihood(w.network, w.partitions, precision=precision, checkpoint_segments=3) as b:
+        for e in edges:
+            x1, x2 = a.edge_derivatives(e)
+            y1, y2 = b.edge_derivatives(e)
+            tol = 1e-9 if precision == "fp64" else 1e-4
+            assert abs(x1 - y1) <= tol * max(1.0, abs(x1))
+            assert abs(x2 - y2) <= (1e-4 if precision == "fp64" else 5e-3) * max(1.0, abs(x2))
