@@ -100,14 +100,18 @@ __device__ __forceinline__ void matvec(const real *M, const real (&x)[S], real (
   }
 }
 
+// Patterns per thread: a block covers kTanPPT * 256 / R patterns, which is
+// the padding unit of every partition, so a block never spans two.
+constexpr int kTanPPT = 4;
+
 // One launch per DAG level (blockIdx.y = op of the level); a thread owns one
-// (pattern, rate), a block 256 / R patterns of one partition. Shared memory:
-// the other side's P, then the two matrices applied to the e side (P'_e and
-// P''_e, or P_d twice).
+// rate of kTanPPT patterns (strided by 256 / R), a block 1024 / R patterns of
+// one partition. Shared memory: the other side's P, then the two matrices
+// applied to the e side (P'_e and P''_e, or P_d twice).
 template <typename real, int R, int S>
 __global__ void __launch_bounds__(256) tangent_kernel(const TanParams p, int op_begin) {
   constexpr int RSS = R * S * S;
-  constexpr int SPB = 256 / R;
+  constexpr int ROWS = 256 / R;  // patterns per pass of the block
   extern __shared__ __align__(16) unsigned char smem_raw[];
   real *sM = reinterpret_cast<real *>(smem_raw);
   const TanOp op = p.ops[op_begin + blockIdx.y];
@@ -127,77 +131,80 @@ __global__ void __launch_bounds__(256) tangent_kernel(const TanParams p, int op_
   }
   __syncthreads();
   const int r = threadIdx.x % R;
-  const int64_t s = (int64_t)blockIdx.x * SPB + threadIdx.x / R;
-  real c[S], vo[S], t1[S], t2[S];
-  const int so = load_row<real, R, S>(p, op.o, s, r, c);
-  if (op.o == INT32_MIN) {
+  const size_t plane = (size_t)p.n_patterns * R * S;
+  const real *Mo = sM + r * S * S, *M1 = sM + RSS + r * S * S, *M2 = sM + 2 * RSS + r * S * S;
+  double a1 = 0.0, a2 = 0.0;  // root slots: this thread's site sums
+  for (int q = 0; q < kTanPPT; ++q) {
+    const int64_t s = ((int64_t)blockIdx.x * kTanPPT + q) * ROWS + threadIdx.x / R;
+    real c[S], vo[S], t1[S], t2[S];
+    const int so = load_row<real, R, S>(p, op.o, s, r, c);
+    if (op.o == INT32_MIN) {
 #pragma unroll
-    for (int i = 0; i < S; ++i) vo[i] = (real)1;
-  } else {
-    matvec<real, S>(sM + r * S * S, c, vo);
-  }
-  int sd;
-  if (op.mode == 1) {
-    sd = load_row<real, R, S>(p, op.d, s, r, c);
-    matvec<real, S>(sM + RSS + r * S * S, c, t1);
-    matvec<real, S>(sM + 2 * RSS + r * S * S, c, t2);
-  } else {
-    sd = p.scaler[(size_t)op.d * p.n_patterns + s];
-    const size_t plane = (size_t)p.n_patterns * R * S;
-    const real *src = static_cast<const real *>(p.tan) + (size_t)op.td * 2 * plane + ((size_t)s * R + r) * S;
+      for (int i = 0; i < S; ++i) vo[i] = (real)1;
+    } else {
+      matvec<real, S>(Mo, c, vo);
+    }
+    int sd;
+    if (op.mode == 1) {
+      sd = load_row<real, R, S>(p, op.d, s, r, c);
+      matvec<real, S>(M1, c, t1);
+      matvec<real, S>(M2, c, t2);
+    } else {
+      sd = p.scaler[(size_t)op.d * p.n_patterns + s];
+      const real *src = static_cast<const real *>(p.tan) + (size_t)op.td * 2 * plane + ((size_t)s * R + r) * S;
 #pragma unroll
-    for (int i = 0; i < S; ++i) c[i] = src[i];
-    matvec<real, S>(sM + RSS + r * S * S, c, t1);
+      for (int i = 0; i < S; ++i) c[i] = src[i];
+      matvec<real, S>(M1, c, t1);
 #pragma unroll
-    for (int i = 0; i < S; ++i) c[i] = src[plane + i];
-    matvec<real, S>(sM + 2 * RSS + r * S * S, c, t2);
-  }
-  const int k = p.scaler[(size_t)op.x * p.n_patterns + s] - sd - so;
-#pragma unroll
-  for (int i = 0; i < S; ++i) {
-    t1[i] = ScaleShift<real>::apply(t1[i] * vo[i], k);
-    t2[i] = ScaleShift<real>::apply(t2[i] * vo[i], k);
-  }
-  if (op.tx >= 0) {
-    const size_t plane = (size_t)p.n_patterns * R * S;
-    real *dst = static_cast<real *>(p.tan) + (size_t)op.tx * 2 * plane + ((size_t)s * R + r) * S;
+      for (int i = 0; i < S; ++i) c[i] = src[plane + i];
+      matvec<real, S>(M2, c, t2);
+    }
+    const int k = p.scaler[(size_t)op.x * p.n_patterns + s] - sd - so;
 #pragma unroll
     for (int i = 0; i < S; ++i) {
-      dst[i] = t1[i];
-      dst[plane + i] = t2[i];
+      t1[i] = ScaleShift<real>::apply(t1[i] * vo[i], k);
+      t2[i] = ScaleShift<real>::apply(t2[i] * vo[i], k);
+    }
+    if (op.tx >= 0) {
+      real *dst = static_cast<real *>(p.tan) + (size_t)op.tx * 2 * plane + ((size_t)s * R + r) * S;
+#pragma unroll
+      for (int i = 0; i < S; ++i) {
+        dst[i] = t1[i];
+        dst[plane + i] = t2[i];
+      }
+    }
+    if (op.slot < 0) continue;  // uniform over the block
+    // displayed-tree root: L, L', L'' of the site (sums over the R rate lanes)
+    const real *xr = static_cast<const real *>(p.clv) + (((size_t)op.x * p.n_patterns + s) * R + r) * S;
+    const double rw = p.rate_weights[part * R + r];
+    double L = 0.0, L1 = 0.0, L2 = 0.0;
+#pragma unroll
+    for (int i = 0; i < S; ++i) {
+      const double pi = p.freqs[part * S + i];
+      L += pi * (double)xr[i];
+      L1 += pi * (double)t1[i];
+      L2 += pi * (double)t2[i];
+    }
+    L *= rw;
+    L1 *= rw;
+    L2 *= rw;
+#pragma unroll
+    for (int o = 1; o < R; o <<= 1) {
+      L += __shfl_xor_sync(0xffffffffu, L, o);
+      L1 += __shfl_xor_sync(0xffffffffu, L1, o);
+      L2 += __shfl_xor_sync(0xffffffffu, L2, o);
+    }
+    if (r == 0) {
+      const double w = p.weights[s];
+      if (w != 0.0) {
+        const double r1 = L1 / L, r2 = L2 / L;
+        a1 += w * r1;
+        a2 += w * (r2 - r1 * r1);
+      }
     }
   }
   if (op.slot < 0) return;  // uniform over the block
-  // displayed-tree root: L, L', L'' of the site (sums over the R rate lanes)
-  const real *xr = static_cast<const real *>(p.clv) + (((size_t)op.x * p.n_patterns + s) * R + r) * S;
-  const double rw = p.rate_weights[part * R + r];
-  double L = 0.0, L1 = 0.0, L2 = 0.0;
-#pragma unroll
-  for (int i = 0; i < S; ++i) {
-    const double pi = p.freqs[part * S + i];
-    L += pi * (double)xr[i];
-    L1 += pi * (double)t1[i];
-    L2 += pi * (double)t2[i];
-  }
-  L *= rw;
-  L1 *= rw;
-  L2 *= rw;
-#pragma unroll
-  for (int o = 1; o < R; o <<= 1) {
-    L += __shfl_xor_sync(0xffffffffu, L, o);
-    L1 += __shfl_xor_sync(0xffffffffu, L1, o);
-    L2 += __shfl_xor_sync(0xffffffffu, L2, o);
-  }
-  double a1 = 0.0, a2 = 0.0;
-  if (r == 0) {
-    const double w = p.weights[s];
-    if (w != 0.0) {
-      const double r1 = L1 / L, r2 = L2 / L;
-      a1 = w * r1;
-      a2 = w * (r2 - r1 * r1);
-    }
-  }
-  // fixed-order block sum: warp shuffles, then warp 0 over the warp sums
+  // fixed-order block sum: warp shuffles, then thread 0 over the warp sums
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     a1 += __shfl_down_sync(0xffffffffu, a1, o);
@@ -279,7 +286,7 @@ bool dispatch_levels(cudaStream_t st, int R, int S, const TanParams &p, const in
 
 }  // namespace
 
-int tangent_patterns_per_block(int R) { return 256 / R; }
+int tangent_patterns_per_block(int R) { return kTanPPT * 256 / R; }
 
 void launch_pderiv(cudaStream_t s, int n_parts, int R, int S, const double *lambda, const double *U,
                    const double *Uinv, const double *rates, double t, double *out64, float *out32) {
