@@ -64,15 +64,47 @@ struct ScaleShift<double> {
   static __device__ __forceinline__ double apply(double x, int k) { return ldexp(x, 256 * k); }
 };
 
+// S consecutive reals through the read-only path, 16 bytes at a time (S is a
+// multiple of 4; rows start on 16-byte boundaries).
+template <typename real, int S>
+__device__ __forceinline__ void ldg_row(const real *src, real (&c)[S]) {
+  if constexpr (sizeof(real) == 4) {
+#pragma unroll
+    for (int i = 0; i < S; i += 4) {
+      const float4 v = __ldg(reinterpret_cast<const float4 *>(src + i));
+      c[i] = v.x;
+      c[i + 1] = v.y;
+      c[i + 2] = v.z;
+      c[i + 3] = v.w;
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < S; i += 2) {
+      const double2 v = __ldg(reinterpret_cast<const double2 *>(src + i));
+      c[i] = v.x;
+      c[i + 1] = v.y;
+    }
+  }
+}
+
+template <typename real, int S>
+__device__ __forceinline__ void st_row(real *dst, const real (&c)[S]) {
+  if constexpr (sizeof(real) == 4) {
+#pragma unroll
+    for (int i = 0; i < S; i += 4) *reinterpret_cast<float4 *>(dst + i) = make_float4(c[i], c[i + 1], c[i + 2], c[i + 3]);
+  } else {
+#pragma unroll
+    for (int i = 0; i < S; i += 2) *reinterpret_cast<double2 *>(dst + i) = make_double2(c[i], c[i + 1]);
+  }
+}
+
 // One child's row for the thread's (pattern, rate): a CLV row, a tip's 0/1
 // state mask, or the fake child's ones; returns its scale counter.
 template <typename real, int R, int S>
 __device__ __forceinline__ int load_row(const TanParams &p, int32_t ref, int64_t s, int r, real (&c)[S]) {
   if (ref >= 0) {
-    const real *src = static_cast<const real *>(p.clv) + (((size_t)ref * p.n_patterns + s) * R + r) * S;
-#pragma unroll
-    for (int i = 0; i < S; ++i) c[i] = src[i];
-    return p.scaler[(size_t)ref * p.n_patterns + s];
+    ldg_row<real, S>(static_cast<const real *>(p.clv) + (((size_t)ref * p.n_patterns + s) * R + r) * S, c);
+    return __ldg(p.scaler + (size_t)ref * p.n_patterns + s);
   }
   if (ref == INT32_MIN) {
 #pragma unroll
@@ -81,9 +113,9 @@ __device__ __forceinline__ int load_row(const TanParams &p, int32_t ref, int64_t
   }
   uint32_t code;
   if constexpr (S == 4)
-    code = p.tips[(size_t)(-1 - ref) * p.n_patterns + s];
+    code = __ldg(p.tips + (size_t)(-1 - ref) * p.n_patterns + s);
   else
-    code = p.tips32[(size_t)(-1 - ref) * p.n_patterns + s];
+    code = __ldg(p.tips32 + (size_t)(-1 - ref) * p.n_patterns + s);
 #pragma unroll
   for (int i = 0; i < S; ++i) c[i] = (real)((code >> i) & 1u);
   return 0;
@@ -107,35 +139,46 @@ constexpr int kTanPPT = 4;
 // One launch per DAG level (blockIdx.y = op of the level); a thread owns one
 // rate of kTanPPT patterns (strided by 256 / R), a block 1024 / R patterns of
 // one partition. Shared memory: the other side's P, then the two matrices
-// applied to the e side (P'_e and P''_e, or P_d twice).
+// applied to the e side (P'_e and P''_e, or P_d twice), then the partition's
+// frequencies and rate weights. Every read goes through the read-only path:
+// nothing a launch reads is written in it (a tangent slot is reused only
+// after the level that read it). At displayed-tree roots the site sums run
+// in the context's precision; only the per-site accumulation is FP64.
 template <typename real, int R, int S>
 __global__ void __launch_bounds__(256) tangent_kernel(const TanParams p, int op_begin) {
   constexpr int RSS = R * S * S;
   constexpr int ROWS = 256 / R;  // patterns per pass of the block
   extern __shared__ __align__(16) unsigned char smem_raw[];
   real *sM = reinterpret_cast<real *>(smem_raw);
+  real *sPi = sM + 3 * RSS, *sRw = sPi + S;
   const TanOp op = p.ops[op_begin + blockIdx.y];
   const int part = p.block_part[blockIdx.x];
   const real *pm = static_cast<const real *>(p.pmat) + (size_t)part * p.n_edges * RSS;
   const real *pd = static_cast<const real *>(p.pderiv) + (size_t)part * 2 * RSS;
   for (int i = threadIdx.x; i < RSS; i += blockDim.x) {
-    sM[i] = op.eo >= 0 ? pm[(size_t)op.eo * RSS + i] : (real)0;
+    sM[i] = op.eo >= 0 ? __ldg(pm + (size_t)op.eo * RSS + i) : (real)0;
     if (op.mode == 1) {
-      sM[RSS + i] = pd[i];
-      sM[2 * RSS + i] = pd[RSS + i];
+      sM[RSS + i] = __ldg(pd + i);
+      sM[2 * RSS + i] = __ldg(pd + RSS + i);
     } else {
-      const real v = pm[(size_t)op.ed * RSS + i];
+      const real v = __ldg(pm + (size_t)op.ed * RSS + i);
       sM[RSS + i] = v;
       sM[2 * RSS + i] = v;
     }
   }
+  if (threadIdx.x < S) sPi[threadIdx.x] = (real)p.freqs[part * S + threadIdx.x];
+  if (threadIdx.x < R) sRw[threadIdx.x] = (real)p.rate_weights[part * R + threadIdx.x];
   __syncthreads();
   const int r = threadIdx.x % R;
   const size_t plane = (size_t)p.n_patterns * R * S;
   const real *Mo = sM + r * S * S, *M1 = sM + RSS + r * S * S, *M2 = sM + 2 * RSS + r * S * S;
+  const real *tsrc = static_cast<const real *>(p.tan) + (size_t)op.td * 2 * plane;
+  real *tdst = static_cast<real *>(p.tan) + (size_t)op.tx * 2 * plane;
   double a1 = 0.0, a2 = 0.0;  // root slots: this thread's site sums
+#pragma unroll
   for (int q = 0; q < kTanPPT; ++q) {
     const int64_t s = ((int64_t)blockIdx.x * kTanPPT + q) * ROWS + threadIdx.x / R;
+    const size_t row = ((size_t)s * R + r) * S;
     real c[S], vo[S], t1[S], t2[S];
     const int so = load_row<real, R, S>(p, op.o, s, r, c);
     if (op.o == INT32_MIN) {
@@ -150,44 +193,36 @@ __global__ void __launch_bounds__(256) tangent_kernel(const TanParams p, int op_
       matvec<real, S>(M1, c, t1);
       matvec<real, S>(M2, c, t2);
     } else {
-      sd = p.scaler[(size_t)op.d * p.n_patterns + s];
-      const real *src = static_cast<const real *>(p.tan) + (size_t)op.td * 2 * plane + ((size_t)s * R + r) * S;
-#pragma unroll
-      for (int i = 0; i < S; ++i) c[i] = src[i];
+      sd = __ldg(p.scaler + (size_t)op.d * p.n_patterns + s);
+      ldg_row<real, S>(tsrc + row, c);
       matvec<real, S>(M1, c, t1);
-#pragma unroll
-      for (int i = 0; i < S; ++i) c[i] = src[plane + i];
+      ldg_row<real, S>(tsrc + plane + row, c);
       matvec<real, S>(M2, c, t2);
     }
-    const int k = p.scaler[(size_t)op.x * p.n_patterns + s] - sd - so;
+    const int k = __ldg(p.scaler + (size_t)op.x * p.n_patterns + s) - sd - so;
 #pragma unroll
     for (int i = 0; i < S; ++i) {
       t1[i] = ScaleShift<real>::apply(t1[i] * vo[i], k);
       t2[i] = ScaleShift<real>::apply(t2[i] * vo[i], k);
     }
     if (op.tx >= 0) {
-      real *dst = static_cast<real *>(p.tan) + (size_t)op.tx * 2 * plane + ((size_t)s * R + r) * S;
-#pragma unroll
-      for (int i = 0; i < S; ++i) {
-        dst[i] = t1[i];
-        dst[plane + i] = t2[i];
-      }
+      st_row<real, S>(tdst + row, t1);
+      st_row<real, S>(tdst + plane + row, t2);
     }
     if (op.slot < 0) continue;  // uniform over the block
     // displayed-tree root: L, L', L'' of the site (sums over the R rate lanes)
-    const real *xr = static_cast<const real *>(p.clv) + (((size_t)op.x * p.n_patterns + s) * R + r) * S;
-    const double rw = p.rate_weights[part * R + r];
-    double L = 0.0, L1 = 0.0, L2 = 0.0;
+    real xr[S];
+    ldg_row<real, S>(static_cast<const real *>(p.clv) + (size_t)op.x * plane + row, xr);
+    real L = 0, L1 = 0, L2 = 0;
 #pragma unroll
     for (int i = 0; i < S; ++i) {
-      const double pi = p.freqs[part * S + i];
-      L += pi * (double)xr[i];
-      L1 += pi * (double)t1[i];
-      L2 += pi * (double)t2[i];
+      L = fma(sPi[i], xr[i], L);
+      L1 = fma(sPi[i], t1[i], L1);
+      L2 = fma(sPi[i], t2[i], L2);
     }
-    L *= rw;
-    L1 *= rw;
-    L2 *= rw;
+    L *= sRw[r];
+    L1 *= sRw[r];
+    L2 *= sRw[r];
 #pragma unroll
     for (int o = 1; o < R; o <<= 1) {
       L += __shfl_xor_sync(0xffffffffu, L, o);
@@ -195,11 +230,11 @@ __global__ void __launch_bounds__(256) tangent_kernel(const TanParams p, int op_
       L2 += __shfl_xor_sync(0xffffffffu, L2, o);
     }
     if (r == 0) {
-      const double w = p.weights[s];
+      const double w = __ldg(p.weights + s);
       if (w != 0.0) {
-        const double r1 = L1 / L, r2 = L2 / L;
-        a1 += w * r1;
-        a2 += w * (r2 - r1 * r1);
+        const real q1 = L1 / L, q2 = L2 / L;
+        a1 += w * (double)q1;
+        a2 += w * ((double)q2 - (double)q1 * (double)q1);
       }
     }
   }
@@ -255,7 +290,7 @@ __global__ void tangent_reduce_kernel(const TanParams p, const int32_t *__restri
 
 template <typename real, int R, int S>
 void run_levels(cudaStream_t st, const TanParams &p, const int32_t *level_begin, int n_levels) {
-  const size_t smem = 3 * (size_t)R * S * S * sizeof(real);
+  const size_t smem = (3 * (size_t)R * S * S + S + R) * sizeof(real);
   for (int L = 0; L < n_levels; ++L) {
     const int n = level_begin[L + 1] - level_begin[L];
     if (n > 0) tangent_kernel<real, R, S><<<dim3(p.n_blocks, n), 256, smem, st>>>(p, level_begin[L]);
