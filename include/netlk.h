@@ -423,16 +423,36 @@ int netlk_mix_site_loglikelihoods_noalloc(const double *d_site_logl, int32_t n_t
  * sequential perform / computeLoglikelihood / undo loop over candidates in
  * filterCandidates (src/search/Filtering.cpp:239-249). A batch holds n
  * contexts (any topologies and partitions, one device) and captures one
- * logL + gradient evaluation of each - branch-length upload, the whole
- * launch sequence, result download - into ONE CUDA graph in which the
- * contexts' branches run concurrently; every call is one graph launch and
- * one synchronisation. The contexts stay owned by the caller, must outlive
+ * logL + gradient evaluation of each - branch-length upload, the launches,
+ * result download - into ONE CUDA graph (below: persistent launches over all
+ * candidates, or each context's launch sequence on its own stream); every
+ * call is one graph launch and one synchronisation. The contexts stay owned
+ * by the caller, must outlive
  * the batch, and must not be evaluated concurrently with it. Each context
  * uses the branch lengths of its last netlk_set_branch_lengths
  * (netlk_set_branch_lengths_device lengths are rejected). Errors return a
  * status; netlk_last_error(NULL) names the failing candidate. */
 typedef struct netlk_batch netlk_batch;
+/* Same as netlk_batch_create_ex(..., NETLK_BATCH_AUTO, ...). */
 int netlk_batch_create(netlk_ctx *const *ctxs, int32_t n, netlk_batch **out);
+/* mode NETLK_BATCH_AUTO: when every context is DNA, FP32, 4 rate categories,
+ * with one checkpoint segment, a call runs all candidates in persistent
+ * launches - P-matrices of every candidate in one launch, one forward walk
+ * whose warps take (candidate, pattern unit) items from a device counter,
+ * longest candidate first, site sums and mixtures in one launch each, one
+ * adjoint walk the same way, batched gradient reductions and one result
+ * gather (nine kernels, one upload of every length, one download of every
+ * result, captured once as a CUDA graph); the walk shape of the two
+ * persistent launches is timed on the batch at its first call. Otherwise,
+ * and with mode NETLK_BATCH_PER_CONTEXT, the graph holds each context's own
+ * launch sequence on its own stream. */
+#define NETLK_BATCH_AUTO 0
+#define NETLK_BATCH_PER_CONTEXT 1
+int netlk_batch_create_ex(netlk_ctx *const *ctxs, int32_t n, int32_t mode, netlk_batch **out);
+/* Introspection, no counterpart in the reference: whether the batch runs
+ * the persistent launches, kernels per call, and the walk shapes chosen. */
+int netlk_batch_info(const netlk_batch *b, int32_t *persistent, int64_t *launches_per_call, int32_t *fwd_shape,
+                     int32_t *bwd_shape);
 /* totals [n]; d_brlen[i] [n_edges of context i] and d_retprob[i]
  * [n_reticulations of context i] may be NULL (either array or entry). */
 int netlk_batch_loglikelihood_gradient(netlk_batch *batch, double *totals, double *const *d_brlen,

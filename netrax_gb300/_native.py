@@ -39,7 +39,7 @@ EXPORTED = [
     "netlk_mix_site_loglikelihoods_noalloc", "netlk_batch_create",
     "netlk_batch_loglikelihood_gradient", "netlk_batch_destroy", "netlk_edge_loglikelihood",
     "netlk_last_site_updates", "netlk_encode_states", "netlk_compress_patterns", "netlk_inject_failure",
-    "netlk_walk_segments",
+    "netlk_walk_segments", "netlk_batch_create_ex", "netlk_batch_info",
 ]
 
 
@@ -141,6 +141,8 @@ def lib():
     L.netlk_walk_shape_begin.argtypes = [vp, c_int32_p]
     L.netlk_kernel_times.argtypes = [vp, c_double_p, ctypes.POINTER(ctypes.c_int64), ctypes.c_int32]
     L.netlk_batch_create.argtypes = [ctypes.POINTER(vp), ctypes.c_int32, ctypes.POINTER(vp)]
+    L.netlk_batch_create_ex.argtypes = [ctypes.POINTER(vp), ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(vp)]
+    L.netlk_batch_info.argtypes = [vp, c_int32_p, ctypes.POINTER(ctypes.c_int64), c_int32_p, c_int32_p]
     L.netlk_batch_loglikelihood_gradient.argtypes = [vp, c_double_p, ctypes.POINTER(c_double_p),
                                                      ctypes.POINTER(c_double_p)]
     L.netlk_batch_destroy.argtypes = [vp]

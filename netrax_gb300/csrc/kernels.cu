@@ -345,14 +345,8 @@ __global__ void __launch_bounds__(THREADS, MINB) forward_kernel(const SweepParam
 // (a topological order chosen for cache locality) for its own unit. A lane
 // only reads values it wrote itself, so no warp waits for another; a child
 // CLV is read back soon after it was written, mostly from L2.
-template <typename real, int R, int THREADS, int MINB, int PPL>
-__global__ void __launch_bounds__(THREADS, MINB) forward_walk_kernel(const SweepParams p, int unit_begin, int unit_end) {
-  constexpr int WPB = THREADS / 32;
-  __shared__ __align__(16) real sPw[WPB][2 * R * PLayout<real>::kRow];
-  const int unit = unit_begin + blockIdx.x * WPB + (threadIdx.x >> 5);
-  if (unit >= unit_end) return;  // whole warp
-  real *sP = sPw[threadIdx.x >> 5];
-  const int lane = threadIdx.x & 31;
+template <typename real, int R, int PPL>
+__device__ __forceinline__ void forward_walk_unit(const SweepParams &p, int unit, real *sP, int lane) {
   constexpr int PPW = 32 / R;
   const size_t g0 = (size_t)unit * PPW * PPL + lane / R;
   const int n = p.n_walk_fwd;
@@ -367,6 +361,15 @@ __global__ void __launch_bounds__(THREADS, MINB) forward_walk_kernel(const Sweep
     prefetch_child<real, R, PPL>(p, h.y, g0, lane % R, PPW);
     prefetch_child<real, R, PPL>(p, h.z, g0, lane % R, PPW);
   }
+}
+
+template <typename real, int R, int THREADS, int MINB, int PPL>
+__global__ void __launch_bounds__(THREADS, MINB) forward_walk_kernel(const SweepParams p, int unit_begin, int unit_end) {
+  constexpr int WPB = THREADS / 32;
+  __shared__ __align__(16) real sPw[WPB][2 * R * PLayout<real>::kRow];
+  const int unit = unit_begin + blockIdx.x * WPB + (threadIdx.x >> 5);
+  if (unit >= unit_end) return;  // whole warp
+  forward_walk_unit<real, R, PPL>(p, unit, sPw[threadIdx.x >> 5], threadIdx.x & 31);
 }
 
 // ------------------------------------------------------------------ adjoint
@@ -659,16 +662,8 @@ __global__ void __launch_bounds__(THREADS, MINB) backward_kernel(const SweepPara
 // The whole adjoint sweep in one launch: each warp walks walk_bwd_ops (the
 // reverse of the forward walk, with its own message slots) for its unit. An
 // op's level-schedule index (its grad_partial row) travels in pad0.
-template <typename real, int R, int THREADS, int MINB, int PPL>
-__global__ void __launch_bounds__(THREADS, MINB) backward_walk_kernel(const SweepParams p, int unit_begin,
-                                                                       int unit_end) {
-  constexpr int WPB = THREADS / 32;
-  __shared__ __align__(16) real sPw[WPB][2 * R * PLayout<real>::kRow];
-  __shared__ __align__(16) real sQw[WPB][ModelSlice<R>::kSize];
-  const int unit = unit_begin + blockIdx.x * WPB + (threadIdx.x >> 5);
-  if (unit >= unit_end) return;  // whole warp
-  const int lane = threadIdx.x & 31;
-  real *sQ = sQw[threadIdx.x >> 5];
+template <typename real, int R, int PPL, int G>
+__device__ __forceinline__ void backward_walk_unit(const SweepParams &p, int unit, real *sP, real *sQ, int lane) {
   // a warp's patterns belong to one partition for the whole walk
   stage_model<real, R>(p, p.unit_part[unit * (PPL / kPPLBase)], sQ, lane);
   constexpr int PPW = 32 / R;
@@ -687,21 +682,32 @@ __global__ void __launch_bounds__(THREADS, MINB) backward_walk_kernel(const Swee
     if (i + 1 < n) h = __ldg(reinterpret_cast<const int4 *>(p.walk_bwd_ops + i + 1));
     __syncwarp();  // every lane is done with the previous op's staged values
     const BwdOp op = load_bwd_op<true>(p.walk_bwd_ops, i);
-    backward_op<real, R, PPL, AdjGroup<THREADS, MINB, PPL>::G, true>(p, op, op.pad0, p.walk_msg_slots, unit,
-                                                                     sPw[threadIdx.x >> 5], sQ, lane, carry);
+    backward_op<real, R, PPL, G, true>(p, op, op.pad0, p.walk_msg_slots, unit, sP, sQ, lane, carry);
     prefetch_child<real, R, PPL>(p, h.y, g0, lane % R, PPW);
     prefetch_child<real, R, PPL>(p, h.z, g0, lane % R, PPW);
   }
 }
 
+template <typename real, int R, int THREADS, int MINB, int PPL>
+__global__ void __launch_bounds__(THREADS, MINB) backward_walk_kernel(const SweepParams p, int unit_begin,
+                                                                       int unit_end) {
+  constexpr int WPB = THREADS / 32;
+  __shared__ __align__(16) real sPw[WPB][2 * R * PLayout<real>::kRow];
+  __shared__ __align__(16) real sQw[WPB][ModelSlice<R>::kSize];
+  const int unit = unit_begin + blockIdx.x * WPB + (threadIdx.x >> 5);
+  if (unit >= unit_end) return;  // whole warp
+  backward_walk_unit<real, R, PPL, AdjGroup<THREADS, MINB, PPL>::G>(p, unit, sPw[threadIdx.x >> 5],
+                                                                    sQw[threadIdx.x >> 5], threadIdx.x & 31);
+}
+
 // ------------------------------------------------------------- P-matrices
 // P(t r) = U diag(exp(lambda r t)) U^-1 in FP64; a zero length gives the
 // identity. One thread per entry of pmat[part][edge][rate][S][S].
-__global__ void pmatrix_kernel(int n_parts, int n_edges, int R, int S, const double *__restrict__ lambda,
-                               const double *__restrict__ U, const double *__restrict__ Uinv,
-                               const double *__restrict__ rates, const double *__restrict__ brlen,
-                               double *__restrict__ pmat64, float *__restrict__ pmat32) {
-  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void pmatrix_entry(int64_t idx, int n_parts, int n_edges, int R, int S,
+                                              const double *__restrict__ lambda, const double *__restrict__ U,
+                                              const double *__restrict__ Uinv, const double *__restrict__ rates,
+                                              const double *__restrict__ brlen, double *__restrict__ pmat64,
+                                              float *__restrict__ pmat32) {
   const int SS = S * S;
   const int64_t total = (int64_t)n_parts * n_edges * R * SS;
   if (idx >= total) return;
@@ -724,10 +730,17 @@ __global__ void pmatrix_kernel(int n_parts, int n_edges, int R, int S, const dou
   if (pmat32) pmat32[idx] = (float)v;
 }
 
+__global__ void pmatrix_kernel(int n_parts, int n_edges, int R, int S, const double *__restrict__ lambda,
+                               const double *__restrict__ U, const double *__restrict__ Uinv,
+                               const double *__restrict__ rates, const double *__restrict__ brlen,
+                               double *__restrict__ pmat64, float *__restrict__ pmat32) {
+  pmatrix_entry((int64_t)blockIdx.x * blockDim.x + threadIdx.x, n_parts, n_edges, R, S, lambda, U, Uinv, rates,
+                brlen, pmat64, pmat32);
+}
+
 // ------------------------------------------ per-(tree, partition) site sums
 // Deterministic compensated (Kahan) FP64 sum of the per-unit partials.
-__global__ void tree_reduce_kernel(const MixParams m) {
-  const int slot = blockIdx.x, part = blockIdx.y;
+__device__ __forceinline__ void tree_reduce_block(const MixParams &m, int slot, int part) {
   const int ub = m.parts[part].unit_begin, ue = m.parts[part].unit_end;
   const double *src = m.site_partial + (size_t)slot * m.n_units;
   const float2 *src32 = reinterpret_cast<const float2 *>(src);
@@ -748,6 +761,8 @@ __global__ void tree_reduce_kernel(const MixParams m) {
   if (threadIdx.x == 0) m.tree_logl[(size_t)slot * m.n_parts + part] = red[0];
 }
 
+__global__ void tree_reduce_kernel(const MixParams m) { tree_reduce_block(m, blockIdx.x, blockIdx.y); }
+
 // --------------------------------------------------------------- mixture
 // AVERAGE: logL_p = log sum_T P(T) L_{T,p} (max-shifted); BEST: max_T.
 // Posterior tree weights become the adjoint seeds; the reticulation gradient
@@ -758,7 +773,7 @@ __global__ void tree_reduce_kernel(const MixParams m) {
 // posterior weights w[p][root], the adjoint seeds per slot, and the partition's
 // d logL / d p_k partials; then thread 0 adds the partitions in index order.
 // All sums use fixed shuffle trees, so results do not depend on scheduling.
-__global__ void mix_kernel(const MixParams m) {
+__device__ __forceinline__ void mix_block(const MixParams &m) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, n_warps = blockDim.x >> 5;
   for (int part = warp; part < m.n_parts; part += n_warps) {
     double *wts = m.weights + (size_t)part * m.n_roots;
@@ -838,14 +853,15 @@ __global__ void mix_kernel(const MixParams m) {
   }
 }
 
+__global__ void mix_kernel(const MixParams m) { mix_block(m); }
+
 // Gradient reduction in two fixed-order stages: per adjoint op, the block
 // partials of its launch (grid_partial[op][b][side]) -> op_sum[op][side];
 // then per edge e, the op sides that use it (CSR edge_entries[edge_begin[e] ..
 // edge_begin[e+1]) = op * 2 + side) -> d logL / d t_e.
 // ff: each partial is a pair of float pairs (FP32 sweeps), else two doubles.
-__global__ void op_reduce_kernel(int n_bx, const double *__restrict__ partial, double *__restrict__ op_sum,
-                                 int ff) {
-  const int op = blockIdx.x;
+__device__ __forceinline__ void op_reduce_block(int op, int n_bx, const double *__restrict__ partial,
+                                                double *__restrict__ op_sum, int ff) {
   __shared__ double ra[128], rb[128];
   const double2 *src = reinterpret_cast<const double2 *>(partial) + (size_t)op * n_bx;
   const float4 *src32 = reinterpret_cast<const float4 *>(src);
@@ -882,6 +898,11 @@ __global__ void op_reduce_kernel(int n_bx, const double *__restrict__ partial, d
     op_sum[2 * op] = ra[0];
     op_sum[2 * op + 1] = rb[0];
   }
+}
+
+__global__ void op_reduce_kernel(int n_bx, const double *__restrict__ partial, double *__restrict__ op_sum,
+                                 int ff) {
+  op_reduce_block(blockIdx.x, n_bx, partial, op_sum, ff);
 }
 
 __global__ void edge_reduce_kernel(int n_edges, const int32_t *__restrict__ edge_begin,
@@ -1028,7 +1049,144 @@ int dispatch_walk(int w, A &&...a) {
   }
 }
 
+// ---------------------------------------------------- persistent batches
+// The candidates of a search move in a handful of launches: every warp of a
+// persistent grid takes (candidate, unit) items from a counter, LPT order
+// (the candidates with the longest walks first), and walks that candidate's
+// whole DAG for its unit - the single-context walk, with the candidate's
+// parameters copied into shared memory. No warp waits for another.
+__device__ __forceinline__ void load_params(const SweepParams *src, SweepParams *dst, int lane) {
+  static_assert(sizeof(SweepParams) % 16 == 0 && alignof(SweepParams) <= 16, "copied as int4 words");
+  const int4 *a = reinterpret_cast<const int4 *>(src);
+  int4 *d = reinterpret_cast<int4 *>(dst);
+  for (int i = lane; i < (int)(sizeof(SweepParams) / 16); i += 32) d[i] = a[i];
+  __syncwarp();
+}
+
+__device__ __forceinline__ int next_item(const BatchParams &b, int lane) {
+  int it = 0;
+  if (lane == 0) it = atomicAdd(b.counter, 1);
+  return __shfl_sync(kFull, it, 0);
+}
+
+template <typename real, int R, int THREADS, int MINB, int PPL>
+__global__ void __launch_bounds__(THREADS, MINB) forward_walk_batch_kernel(const BatchParams b) {
+  constexpr int WPB = THREADS / 32;
+  __shared__ __align__(16) real sPw[WPB][2 * R * PLayout<real>::kRow];
+  __shared__ __align__(16) SweepParams sp[WPB];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int item = next_item(b, lane); item < b.n_items; item = next_item(b, lane)) {
+    const int2 it = b.items[item];
+    __syncwarp();  // the previous item is done with sp and sP
+    load_params(&b.cands[it.x].sweep, &sp[w], lane);
+    forward_walk_unit<real, R, PPL>(sp[w], it.y, sPw[w], lane);
+  }
+}
+
+template <typename real, int R, int THREADS, int MINB, int PPL>
+__global__ void __launch_bounds__(THREADS, MINB) backward_walk_batch_kernel(const BatchParams b) {
+  constexpr int WPB = THREADS / 32;
+  __shared__ __align__(16) real sPw[WPB][2 * R * PLayout<real>::kRow];
+  __shared__ __align__(16) real sQw[WPB][ModelSlice<R>::kSize];
+  __shared__ __align__(16) SweepParams sp[WPB];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int item = next_item(b, lane); item < b.n_items; item = next_item(b, lane)) {
+    const int2 it = b.items[item];
+    __syncwarp();
+    load_params(&b.cands[it.x].sweep, &sp[w], lane);
+    backward_walk_unit<real, R, PPL, AdjGroup<THREADS, MINB, PPL>::G>(sp[w], it.y, sPw[w], sQw[w], lane);
+  }
+}
+
+__global__ void pmatrix_batch_kernel(const BatchParams b) {
+  const BatchCand &c = b.cands[blockIdx.y];
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= c.n_pmat) return;
+  pmatrix_entry(idx, c.n_parts, c.n_edges, 4, 4, c.lambda, c.U, c.Uinv, c.rates, c.brlen, c.pmat64, c.pmat32);
+}
+
+__global__ void tree_reduce_batch_kernel(const BatchParams b) {
+  const MixParams &m = b.cands[blockIdx.z].mix;
+  if ((int)blockIdx.x >= m.n_slots || (int)blockIdx.y >= m.n_parts) return;  // whole block
+  tree_reduce_block(m, blockIdx.x, blockIdx.y);
+}
+
+__global__ void mix_batch_kernel(const BatchParams b) { mix_block(b.cands[blockIdx.x].mix); }
+
+__global__ void op_reduce_batch_kernel(const BatchParams b) {
+  const BatchCand &c = b.cands[blockIdx.y];
+  if ((int)blockIdx.x >= c.n_ops) return;  // whole block
+  op_reduce_block(blockIdx.x, c.n_bx, c.grad_partial, c.op_sum, 1);
+}
+
+__global__ void edge_reduce_batch_kernel(const BatchParams b) {
+  const BatchCand &c = b.cands[blockIdx.y];
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= c.n_edges) return;
+  double s = 0.0;
+  for (int q = c.edge_begin[e]; q < c.edge_begin[e + 1]; ++q) s += c.op_sum[c.edge_entries[q]];
+  c.grad[e] = s;
+  b.results[c.result_offset + c.n_out + e] = s;
+}
+
+__global__ void gather_out_batch_kernel(const BatchParams b) {
+  const BatchCand &c = b.cands[blockIdx.x];
+  for (int i = threadIdx.x; i < c.n_out; i += blockDim.x) b.results[c.result_offset + i] = c.out[i];
+}
+
+template <typename real, int R, int T, int M, int FPPL, int BPPL>
+struct FwdBatchRun {
+  static int run(cudaStream_t s, const BatchParams &b) {
+    auto k = forward_walk_batch_kernel<real, R, T, M, FPPL>;
+    int dev = 0, sms = 1, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, T, 0);
+    const int grid = std::max(1, std::min(per_sm * sms, (b.n_items + T / 32 - 1) / (T / 32)));
+    k<<<grid, T, 0, s>>>(b);
+    return 1;
+  }
+};
+template <typename real, int R, int T, int M, int FPPL, int BPPL>
+struct BwdBatchRun {
+  static int run(cudaStream_t s, const BatchParams &b) {
+    auto k = backward_walk_batch_kernel<real, R, T, M, BPPL>;
+    int dev = 0, sms = 1, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, T, 0);
+    const int grid = std::max(1, std::min(per_sm * sms, (b.n_items + T / 32 - 1) / (T / 32)));
+    k<<<grid, T, 0, s>>>(b);
+    return 1;
+  }
+};
+template <typename real, int R, int T, int M, int FPPL, int BPPL>
+struct BwdPplRun {
+  static int run() { return BPPL; }
+};
+
 }  // namespace
+
+int num_batch_shapes() { return kNumWalkShapes; }
+int batch_shape_bwd_ppl(int shape) { return dispatch_walk<BwdPplRun>(shape); }
+
+void launch_batch_forward(cudaStream_t s, const BatchParams &b, int shape) {
+  pmatrix_batch_kernel<<<dim3((unsigned)((b.max_pmat + 255) / 256), b.n_cands), 256, 0, s>>>(b);
+  cudaMemsetAsync(b.counter, 0, 4, s);
+  g_launches += 1 + dispatch_walk<FwdBatchRun>(shape, s, b);
+  tree_reduce_batch_kernel<<<dim3(b.max_slots, b.max_parts, b.n_cands), 256, 0, s>>>(b);
+  mix_batch_kernel<<<b.n_cands, 256, 0, s>>>(b);
+  g_launches += 2;
+}
+
+void launch_batch_backward(cudaStream_t s, const BatchParams &b, int shape) {
+  cudaMemsetAsync(b.counter, 0, 4, s);
+  g_launches += dispatch_walk<BwdBatchRun>(shape, s, b);
+  op_reduce_batch_kernel<<<dim3(std::max(1, b.max_ops), b.n_cands), 128, 0, s>>>(b);
+  edge_reduce_batch_kernel<<<dim3((b.max_edges + 127) / 128, b.n_cands), 128, 0, s>>>(b);
+  gather_out_batch_kernel<<<b.n_cands, 64, 0, s>>>(b);
+  g_launches += 3;
+}
 
 int num_level_shapes(int precision, int R) { return (precision == 1 && R == 4) ? kNumShapes : 1; }
 int num_shapes(int precision, int R) { return (precision == 1 && R == 4) ? kNumShapes + kNumWalkShapes : 1; }

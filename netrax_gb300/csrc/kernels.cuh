@@ -145,6 +145,53 @@ void launch_sweep20(cudaStream_t s, int precision, int R, bool backward, const S
 bool sweep20_tc_supported(int precision, int R);
 void launch_forward20_tc(cudaStream_t s, const SweepParams &p, const int32_t *level_begin, int n_levels, int n_sms);
 void launch_backward20_tc(cudaStream_t s, const SweepParams &p, const int32_t *level_begin, int n_levels, int n_sms);
+// Candidate batch in persistent launches (DNA, FP32, 4 rates, walk
+// schedules): everything one logL + gradient evaluation of candidate c reads
+// and writes, in a device table the batch kernels index by candidate.
+struct BatchCand {
+  SweepParams sweep;            // walk ops, CLVs, messages, site / gradient partials
+  MixParams mix;                // site sums and mixture
+  // P-matrices: n_pmat = n_parts * n_edges * R * 16 entries from brlen
+  const double *lambda, *U, *Uinv, *rates, *brlen;
+  double *pmat64;
+  float *pmat32;
+  int64_t n_pmat;
+  int32_t n_parts, n_edges;
+  // gradient reduction (as launch_grad_reduce)
+  int32_t n_ops, n_bx;
+  const int32_t *edge_begin, *edge_entries;
+  const double *grad_partial;
+  double *op_sum, *grad;
+  // results: out [n_out] then grad [n_edges] go to results + result_offset
+  const double *out;
+  int32_t n_out;
+  int64_t result_offset;
+};
+
+struct BatchParams {
+  const BatchCand *cands;
+  int32_t n_cands;
+  const int2 *items;            // (candidate, unit) in the order warps take them
+  int32_t n_items;
+  int32_t *counter;             // next item (reset before every walk launch)
+  double *results;
+  // grid extents: the largest candidate's
+  int64_t max_pmat;
+  int32_t max_slots, max_parts, max_ops, max_edges;
+};
+
+// Walk shapes the persistent batch kernels run (0 .. num_batch_shapes() - 1),
+// and the adjoint patterns per lane of each (the items differ: a unit is
+// 32 * ppl / 4 patterns).
+int num_batch_shapes();
+int batch_shape_bwd_ppl(int shape);
+// Forward half: P-matrices, counter reset, persistent forward walk over every
+// (candidate, unit) item, site sums, mixture. b.items: forward items.
+void launch_batch_forward(cudaStream_t s, const BatchParams &b, int shape);
+// Adjoint half: counter reset, persistent adjoint walk, gradient reduction,
+// results gathered into b.results. b.items: adjoint items for the shape.
+void launch_batch_backward(cudaStream_t s, const BatchParams &b, int shape);
+
 // Forward-mode (tangent) sweep for the derivatives along one branch e
 // (tangent.cu). Op for a variant x whose subtree contains e: d = child on e's
 // side (mode 1: d hangs from e itself; mode 2: d contains e and its tangents

@@ -2193,9 +2193,186 @@ struct netlk_batch {
   cudaEvent_t fork = nullptr;
   std::vector<cudaEvent_t> join;
   cudaGraphExec_t exec = nullptr;
+  // persistent path: every context DNA, FP32, 4 rate categories, one
+  // checkpoint segment, with walk schedules. A call is one graph of nine
+  // launches: batched P-matrices, one persistent forward walk over every
+  // (candidate, unit) item, batched site sums and mixtures, one persistent
+  // adjoint walk, batched gradient reductions and a result gather, plus one
+  // upload of all lengths and one download of all results.
+  bool persistent = false, ready = false;
+  int fshape = 0, bshape = 0;
+  int64_t launches_per_call = 0;
+  DevBuf d_cands, d_items_f, d_items_b2, d_items_b4, d_counter, d_results, d_lengths;
+  PinnedBuf h_results, h_lengths;
+  int n_items_f = 0, n_items_b2 = 0, n_items_b4 = 0;
+  std::vector<int64_t> res_off, len_off;
+  int64_t n_results = 0, n_lengths = 0, dev_bytes = 0;
+  BatchParams base{};
+  std::vector<double> tune_fwd_ms, tune_bwd_ms;
+
+  BatchParams fwd_params() const {
+    BatchParams p = base;
+    p.items = d_items_f.as<int2>();
+    p.n_items = n_items_f;
+    return p;
+  }
+  BatchParams bwd_params(int shape) const {
+    BatchParams p = base;
+    const bool two = batch_shape_bwd_ppl(shape) == 2;
+    p.items = two ? d_items_b2.as<int2>() : d_items_b4.as<int2>();
+    p.n_items = two ? n_items_b2 : n_items_b4;
+    return p;
+  }
+
+  static bool eligible(const netlk_ctx *c) {
+    return c->S == 4 && c->R == 4 && c->opts.precision == NETLK_FP32 && c->n_segments == 1 && c->walk_ok;
+  }
+
+  // Device tables of every candidate, the work items (longest walks first),
+  // and the walk shapes, timed on this batch.
+  void setup_persistent() {
+    const int n = (int)ctxs.size();
+    std::vector<BatchCand> cands(n);
+    res_off.assign(n, 0);
+    len_off.assign(n, 0);
+    n_results = n_lengths = 0;
+    for (int i = 0; i < n; ++i) {
+      const netlk_ctx *c = ctxs[i];
+      res_off[i] = n_results;
+      len_off[i] = n_lengths;
+      n_results += 3 + c->P + c->topo.n_ret + c->topo.n_edges;
+      n_lengths += c->topo.n_edges;
+    }
+    d_lengths.alloc(n_lengths * 8, dev_bytes);
+    d_results.alloc(n_results * 8, dev_bytes);
+    d_counter.alloc(16, dev_bytes);
+    h_lengths.alloc(n_lengths * 8);
+    h_results.alloc(n_results * 8);
+    stage_lengths();
+    BatchParams b{};
+    for (int i = 0; i < n; ++i) {
+      const netlk_ctx *c = ctxs[i];
+      BatchCand &k = cands[i];
+      k.sweep = c->sweep();
+      k.mix = c->mix();
+      k.lambda = c->d_lambda.as<double>();
+      k.U = c->d_U.as<double>();
+      k.Uinv = c->d_Uinv.as<double>();
+      k.rates = c->d_rates.as<double>();
+      k.brlen = d_lengths.as<double>() + len_off[i];
+      k.pmat64 = c->d_pmat64.as<double>();
+      k.pmat32 = c->d_pmat32.as<float>();
+      k.n_pmat = (int64_t)c->P * c->topo.n_edges * 16 * 4;
+      k.n_parts = c->P;
+      k.n_edges = c->topo.n_edges;
+      k.n_ops = (int32_t)c->bwd.size();
+      k.n_bx = c->n_units;
+      k.edge_begin = c->d_edge_begin.as<int32_t>();
+      k.edge_entries = c->d_edge_entries.as<int32_t>();
+      k.grad_partial = c->d_grad_partial.as<double>();
+      k.op_sum = c->d_op_sum.as<double>();
+      k.grad = c->d_grad.as<double>();
+      k.out = c->d_out.as<double>();
+      k.n_out = 3 + c->P + c->topo.n_ret;
+      k.result_offset = res_off[i];
+      b.max_pmat = std::max(b.max_pmat, k.n_pmat);
+      b.max_slots = std::max(b.max_slots, c->n_slots);
+      b.max_parts = std::max(b.max_parts, c->P);
+      b.max_ops = std::max(b.max_ops, k.n_ops);
+      b.max_edges = std::max(b.max_edges, k.n_edges);
+    }
+    d_cands.alloc(cands.size() * sizeof(BatchCand), dev_bytes);
+    CUDA_OK(cudaMemcpy(d_cands.p, cands.data(), cands.size() * sizeof(BatchCand), cudaMemcpyHostToDevice));
+    // items: candidates with the longest walks first, units in order
+    auto items = [&](bool backward, int per_warp_units) {
+      std::vector<int> order(n);
+      for (int i = 0; i < n; ++i) order[i] = i;
+      std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
+        const size_t la = backward ? ctxs[a]->wbwd.size() : ctxs[a]->wfwd.size();
+        const size_t lc = backward ? ctxs[c]->wbwd.size() : ctxs[c]->wfwd.size();
+        return la > lc;
+      });
+      std::vector<int2> out;
+      for (int i : order) {
+        const int units = (backward ? ctxs[i]->n_units : ctxs[i]->n_units_fwd) / per_warp_units;
+        if (backward && ctxs[i]->bwd.empty()) continue;
+        for (int u = 0; u < units; ++u) out.push_back(make_int2(i, u));
+      }
+      return out;
+    };
+    const std::vector<int2> f = items(false, 1), b2 = items(true, 1), b4 = items(true, 2);
+    n_items_f = (int)f.size();
+    n_items_b2 = (int)b2.size();
+    n_items_b4 = (int)b4.size();
+    d_items_f.alloc(std::max<size_t>(1, f.size()) * sizeof(int2), dev_bytes);
+    d_items_b2.alloc(std::max<size_t>(1, b2.size()) * sizeof(int2), dev_bytes);
+    d_items_b4.alloc(std::max<size_t>(1, b4.size()) * sizeof(int2), dev_bytes);
+    if (!f.empty()) CUDA_OK(cudaMemcpy(d_items_f.p, f.data(), f.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    if (!b2.empty()) CUDA_OK(cudaMemcpy(d_items_b2.p, b2.data(), b2.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    if (!b4.empty()) CUDA_OK(cudaMemcpy(d_items_b4.p, b4.data(), b4.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    b.cands = d_cands.as<BatchCand>();
+    b.n_cands = n;
+    b.counter = d_counter.as<int32_t>();
+    b.results = d_results.as<double>();
+    base = b;
+    // time every walk shape on this batch, forward and adjoint
+    CUDA_OK(cudaMemcpyAsync(d_lengths.p, h_lengths.p, n_lengths * 8, cudaMemcpyHostToDevice, stream));
+    const int ns = num_batch_shapes();
+    tune_fwd_ms.assign(ns, 0.0);
+    tune_bwd_ms.assign(ns, 0.0);
+    cudaEvent_t e0, e1;
+    CUDA_OK(cudaEventCreate(&e0));
+    CUDA_OK(cudaEventCreate(&e1));
+    auto time = [&](bool backward, int sh) {
+      float best = 1e30f;
+      for (int rep = 0; rep < 2; ++rep) {
+        if (backward) launch_batch_forward(stream, fwd_params(), fshape);
+        CUDA_OK(cudaEventRecord(e0, stream));
+        if (backward)
+          launch_batch_backward(stream, bwd_params(sh), sh);
+        else
+          launch_batch_forward(stream, fwd_params(), sh);
+        CUDA_OK(cudaEventRecord(e1, stream));
+        CUDA_OK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CUDA_OK(cudaEventElapsedTime(&ms, e0, e1));
+        if (rep) best = std::min(best, ms);
+      }
+      return (double)best;
+    };
+    for (int sh = 0; sh < ns; ++sh) tune_fwd_ms[sh] = time(false, sh);
+    fshape = (int)(std::min_element(tune_fwd_ms.begin(), tune_fwd_ms.end()) - tune_fwd_ms.begin());
+    for (int sh = 0; sh < ns; ++sh) tune_bwd_ms[sh] = time(true, sh);
+    bshape = (int)(std::min_element(tune_bwd_ms.begin(), tune_bwd_ms.end()) - tune_bwd_ms.begin());
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    CUDA_OK(cudaGetLastError());
+    launches_per_call = 9;
+    ready = true;
+  }
+
+  // every context's host lengths into the pinned upload buffer
+  void stage_lengths() {
+    for (size_t i = 0; i < ctxs.size(); ++i)
+      std::memcpy(h_lengths.as<double>() + len_off[i], ctxs[i]->brlen.data(), ctxs[i]->brlen.size() * 8);
+  }
+
+  void capture_persistent() {
+    CUDA_OK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    CUDA_OK(cudaMemcpyAsync(d_lengths.p, h_lengths.p, n_lengths * 8, cudaMemcpyHostToDevice, stream));
+    launch_batch_forward(stream, fwd_params(), fshape);
+    launch_batch_backward(stream, bwd_params(bshape), bshape);
+    CUDA_OK(cudaMemcpyAsync(h_results.p, d_results.p, n_results * 8, cudaMemcpyDeviceToHost, stream));
+    cudaGraph_t graph;
+    CUDA_OK(cudaStreamEndCapture(stream, &graph));
+    cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    CUDA_OK(e);
+  }
 
   ~netlk_batch() {
     cudaSetDevice(device);
+    for (DevBuf *b : {&d_cands, &d_items_f, &d_items_b2, &d_items_b4, &d_counter, &d_results, &d_lengths}) b->free();
     if (exec) cudaGraphExecDestroy(exec);
     for (cudaEvent_t e : join) cudaEventDestroy(e);
     if (fork) cudaEventDestroy(fork);
@@ -2233,6 +2410,14 @@ struct netlk_batch {
 
 
 int netlk_batch_create(netlk_ctx *const *ctxs, int32_t n, netlk_batch **out) {
+  return netlk_batch_create_ex(ctxs, n, NETLK_BATCH_AUTO, out);
+}
+
+int netlk_batch_create_ex(netlk_ctx *const *ctxs, int32_t n, int32_t mode, netlk_batch **out) {
+  if (mode != NETLK_BATCH_AUTO && mode != NETLK_BATCH_PER_CONTEXT) {
+    netlk::set_global_error("batch: mode must be NETLK_BATCH_AUTO or NETLK_BATCH_PER_CONTEXT");
+    return NETLK_ERR_INVALID_ARGUMENT;
+  }
   if (!ctxs || n <= 0 || !out) {
     netlk::set_global_error("batch: contexts and output pointer required, n > 0");
     return NETLK_ERR_INVALID_ARGUMENT;
@@ -2251,6 +2436,8 @@ int netlk_batch_create(netlk_ctx *const *ctxs, int32_t n, netlk_batch **out) {
     }
     b->ctxs.assign(ctxs, ctxs + n);
     b->device = ctxs[0]->device;
+    b->persistent = mode == NETLK_BATCH_AUTO;
+    for (int i = 0; i < n; ++i) b->persistent = b->persistent && netlk_batch::eligible(ctxs[i]);
     CUDA_OK(cudaSetDevice(b->device));
     CUDA_OK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
     CUDA_OK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
@@ -2278,6 +2465,35 @@ int netlk_batch_loglikelihood_gradient(netlk_batch *b, double *totals, double *c
       std::memcpy(c->h_brlen.p, c->brlen.data(), c->brlen.size() * 8);
     }
     CUDA_OK(cudaSetDevice(b->device));
+    if (b->persistent) {
+      if (!b->ready) b->setup_persistent();
+      b->stage_lengths();
+      if (!b->exec) b->capture_persistent();
+      CUDA_OK(cudaGraphLaunch(b->exec, b->stream));
+      CUDA_OK(cudaStreamSynchronize(b->stream));
+      CUDA_OK(cudaGetLastError());
+      const double *res = b->h_results.as<double>();
+      for (size_t i = 0; i < b->ctxs.size(); ++i) {
+        netlk_ctx *c = b->ctxs[i];
+        const double *o = res + b->res_off[i];
+        const int nout = 3 + c->P + c->topo.n_ret;
+        if (o[1] != 0.0 || !std::isfinite(o[0]))
+          throw Error(NETLK_ERR_NUMERIC, "batch: candidate " + std::to_string(i) +
+                                             ": Invalid network likelihood: negative infinity or NaN");
+        if (totals) totals[i] = o[0];
+        if (d_retprob && d_retprob[i] && c->topo.n_ret) std::memcpy(d_retprob[i], o + 2 + c->P, c->topo.n_ret * 8);
+        if (d_brlen && d_brlen[i]) {
+          if (c->bwd.empty())
+            std::fill(d_brlen[i], d_brlen[i] + c->topo.n_edges, 0.0);
+          else
+            std::memcpy(d_brlen[i], o + nout, c->topo.n_edges * 8);
+        }
+        c->clv_valid = true;  // every CLV now matches the context's host lengths
+        c->clv_brlen = c->brlen;
+        c->last_updates = c->site_updates;
+      }
+      return;
+    }
     if (!b->exec) b->capture();
     CUDA_OK(cudaGraphLaunch(b->exec, b->stream));
     CUDA_OK(cudaStreamSynchronize(b->stream));
@@ -2300,6 +2516,22 @@ int netlk_batch_loglikelihood_gradient(netlk_batch *b, double *totals, double *c
       if (d_brlen && d_brlen[i]) std::memcpy(d_brlen[i], g.data(), g.size() * 8);
     }
   });
+}
+
+int netlk_batch_info(const netlk_batch *b, int32_t *persistent, int64_t *launches_per_call, int32_t *fwd_shape,
+                     int32_t *bwd_shape) {
+  if (!b) return NETLK_ERR_INVALID_ARGUMENT;
+  if (persistent) *persistent = b->persistent ? 1 : 0;
+  if (launches_per_call) {
+    int64_t n = b->launches_per_call;
+    if (!b->persistent)
+      for (const netlk_ctx *c : b->ctxs)
+        n += 1 + c->fwd_launches + 2 + (c->bwd.empty() ? 0 : c->bwd_launches + c->rfwd_launches + 2);
+    *launches_per_call = n;
+  }
+  if (fwd_shape) *fwd_shape = b->fshape;
+  if (bwd_shape) *bwd_shape = b->bshape;
+  return NETLK_OK;
 }
 
 int netlk_batch_destroy(netlk_batch *b) {

@@ -388,13 +388,24 @@ class NetworkBatch:
     call (``netlk_batch_*``). The contexts stay owned by the caller and must
     outlive the batch."""
 
-    def __init__(self, liks):
+    def __init__(self, liks, per_context=False):
+        """per_context: each context's own launch sequence in the graph
+        instead of the persistent launches over all candidates."""
         self.liks = list(liks)
         L = N.lib()
         arr = (ctypes.c_void_p * len(self.liks))(*[lk._h for lk in self.liks])
         h = ctypes.c_void_p()
-        N.check(L.netlk_batch_create(arr, len(self.liks), ctypes.byref(h)))
+        N.check(L.netlk_batch_create_ex(arr, len(self.liks), 1 if per_context else 0, ctypes.byref(h)))
         self._h = h
+
+    def info(self):
+        """(persistent launches in use, kernels per call, forward / adjoint walk shape)."""
+        pers, fs, bs = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        n = ctypes.c_int64()
+        N.check(N.lib().netlk_batch_info(self._h, ctypes.byref(pers), ctypes.byref(n), ctypes.byref(fs),
+                                         ctypes.byref(bs)))
+        return {"persistent": bool(pers.value), "launches_per_call": n.value, "forward_shape": fs.value,
+                "backward_shape": bs.value}
 
     def loglikelihood_gradient(self):
         """Returns (totals [n], list of d logL / d branch length, list of

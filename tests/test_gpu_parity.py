@@ -285,8 +285,9 @@ def test_launch_count_reported():
 
 def test_batch_matches_individual_contexts():
     """One CUDA graph over several candidate networks (DNA of different sizes,
-    plus a protein context on the tensor-core path) == each context alone;
-    a second call picks up new branch lengths."""
+    plus a protein context on the tensor-core path, so each context runs its
+    own launch sequence) == each context alone; a second call picks up new
+    branch lengths."""
     from netrax_gb300 import synth
     from netrax_gb300.likelihood import NetworkBatch, NetworkLikelihood
     ws = synth.candidate_batch(5, scale=0.03)
@@ -305,6 +306,41 @@ def test_batch_matches_individual_contexts():
                     assert tot[i] == t1
                     assert np.array_equal(gb[i], g1)
                     assert np.array_equal(gr[i], r1)
+    finally:
+        for lk in liks:
+            lk.close()
+
+
+@pytest.mark.parametrize("variant", ["AVERAGE", "BEST"])
+@pytest.mark.parametrize("mode", ["persistent", "per_context"])
+def test_persistent_batch_matches_individual_contexts(variant, mode):
+    """Candidate networks of different sizes (DNA, FP32: the persistent
+    launches, where warps take (candidate, pattern unit) items; or the graph of
+    per-context launches) == each context evaluated alone, bit for bit, on
+    three calls with new branch lengths; every walk shape gives the same
+    bits, so the shape the batch picks does not matter."""
+    from netrax_gb300 import synth
+    from netrax_gb300.likelihood import NetworkBatch, NetworkLikelihood
+    ws = synth.candidate_batch(9, scale=0.02)
+    liks = [NetworkLikelihood(w.network, w.partitions, precision="fp32", variant=variant) for w in ws]
+    try:
+        with NetworkBatch(liks, per_context=mode == "per_context") as batch:
+            info = batch.info()
+            assert info["persistent"] == (mode == "persistent")
+            if info["persistent"]:
+                assert info["launches_per_call"] == 9
+            rng = np.random.default_rng(4)
+            for rep in range(3):
+                if rep:
+                    for lk, w in zip(liks, ws):
+                        lk.set_branch_lengths(w.network.branch_lengths * np.exp(0.1 * rng.standard_normal(lk.n_edges)))
+                tot, gb, gr = batch.loglikelihood_gradient()
+                for i, lk in enumerate(liks):
+                    t1, g1, r1 = lk.loglikelihood_gradient()
+                    assert tot[i] == t1, (rep, i)
+                    assert np.array_equal(gb[i], g1)
+                    assert np.array_equal(gr[i], r1)
+                    assert lk.loglikelihood() == t1  # the batch left valid CLVs behind
     finally:
         for lk in liks:
             lk.close()
