@@ -2347,7 +2347,6 @@ struct netlk_batch {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     CUDA_OK(cudaGetLastError());
-    launches_per_call = 9;
     ready = true;
   }
 
@@ -2438,6 +2437,7 @@ int netlk_batch_create_ex(netlk_ctx *const *ctxs, int32_t n, int32_t mode, netlk
     b->device = ctxs[0]->device;
     b->persistent = mode == NETLK_BATCH_AUTO;
     for (int i = 0; i < n; ++i) b->persistent = b->persistent && netlk_batch::eligible(ctxs[i]);
+    if (b->persistent) b->launches_per_call = 9;
     CUDA_OK(cudaSetDevice(b->device));
     CUDA_OK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
     CUDA_OK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
