@@ -23,7 +23,6 @@
 
 #include "kernels.cuh"
 #include "kernels_common.cuh"
-#include "tc.cuh"
 
 namespace netlk {
 
@@ -79,103 +78,6 @@ __device__ __forceinline__ void prefetch_child(const SweepParams &p, int32_t ref
   if (r == 0) {
     const int32_t *sc = p.scaler + (size_t)ref * p.n_patterns + g0;
     asm volatile("prefetch.global.L2 [%0];" ::"l"(sc));
-  }
-}
-
-// Bulk-copy staging for the adjoint walk. While a warp computes one op, the
-// tensor memory accelerator copies the next op's child CLV rows and scale
-// counters for the warp's unit (UNIT patterns, contiguous in memory) into the
-// warp's shared memory (cp.async.bulk; completion counted in bytes on a
-// per-warp mbarrier), so the op starts from shared memory instead of a round
-// trip to L2 or DRAM. Only children are staged: they were written by the
-// forward sweep, never by the adjoint, so a copy issued one op early reads
-// final values. Every wait is bounded; a wait that gives up sets the fault
-// word, which the host reports as NETLK_ERR_TIMEOUT.
-template <typename real, int R, int PPL>
-struct StageBuf {
-  static constexpr int kUnit = (32 / R) * PPL;  // patterns per adjoint unit
-  static constexpr int kClv = kUnit * R * 4;    // reals of one child's rows
-  alignas(128) real clv[2][kClv];
-  alignas(16) int32_t sc[2][kUnit];
-  alignas(8) unsigned long long bar;
-};
-
-// `phase`: bit 0 the parity of the barrier's next completion, kStageBroken
-// once a wait has given up: the warp then issues no more copies and waits no
-// more (its results are void; the fault word says so), and before it leaves
-// it waits once more, bounded, for the copy that did not complete.
-constexpr uint32_t kStageBroken = 2u;
-
-__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-               "l"(src), "r"(bytes), "r"(bar)
-               : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-
-// Lane 0 starts the copies of variant children a and b (tips and the fake
-// child are not staged); every lane returns whether anything was copied.
-// The caller has synchronised the warp after its last read of the stage.
-template <typename real, int R, int PPL>
-__device__ __forceinline__ int stage_issue(const SweepParams &p, StageBuf<real, R, PPL> *sb, int32_t a, int32_t b,
-                                           int unit, int lane, uint32_t phase) {
-  using SB = StageBuf<real, R, PPL>;
-  const int na = a >= 0, nb = b >= 0;
-  if ((!na && !nb) || (phase & kStageBroken)) return 0;
-  if (lane == 0) {
-    constexpr uint32_t kC = SB::kClv * sizeof(real), kS = SB::kUnit * 4;
-    const uint32_t bar = tc::smem_u32(&sb->bar);
-    tc::fence_proxy_async();  // the warp's reads of the stage come before the copies overwrite it
-    mbar_expect_tx(bar, (uint32_t)(na + nb) * (kC + kS));
-    const size_t N = (size_t)p.n_patterns, first = (size_t)unit * SB::kUnit;
-    const real *clv = static_cast<const real *>(p.clv);
-    if (na) {
-      bulk_g2s(tc::smem_u32(sb->clv[0]), clv + ((size_t)a * N + first) * (R * 4), kC, bar);
-      bulk_g2s(tc::smem_u32(sb->sc[0]), p.scaler + (size_t)a * N + first, kS, bar);
-    }
-    if (nb) {
-      bulk_g2s(tc::smem_u32(sb->clv[1]), clv + ((size_t)b * N + first) * (R * 4), kC, bar);
-      bulk_g2s(tc::smem_u32(sb->sc[1]), p.scaler + (size_t)b * N + first, kS, bar);
-    }
-  }
-  return 1;
-}
-
-// Waits (bounded) for the stage's copies; a wait that gives up marks the fault.
-template <typename real, int R, int PPL>
-__device__ __forceinline__ void stage_wait(const SweepParams &p, StageBuf<real, R, PPL> *sb, uint32_t &phase,
-                                           int lane) {
-  if (phase & kStageBroken) return;
-  const bool ok = tc::mbar_wait(tc::smem_u32(&sb->bar), phase & 1u);
-  if (ok) {
-    phase ^= 1u;
-    return;
-  }
-  phase |= kStageBroken;
-  if (lane == 0 && p.fault) atomicExch(p.fault, 1);
-}
-
-// On leaving: a warp whose wait gave up waits once more for that copy.
-template <typename real, int R, int PPL>
-__device__ __forceinline__ void stage_drain(StageBuf<real, R, PPL> *sb, uint32_t phase) {
-  if (phase & kStageBroken) (void)tc::mbar_wait(tc::smem_u32(&sb->bar), phase & 1u);
-}
-
-// Group `grp` (G patterns per lane) of staged child `side`: the same values
-// load_child reads from global memory.
-template <typename real, int R, int PPL, int G>
-__device__ __forceinline__ void load_staged(const StageBuf<real, R, PPL> *sb, int side, int grp, int pl, int r,
-                                            real (&c)[G][4], int (&sc)[G]) {
-  constexpr int PPW = 32 / R;
-#pragma unroll
-  for (int k = 0; k < G; ++k) {
-    const int lp = (grp * G + k) * PPW + pl;  // pattern within the unit
-    const real *src = sb->clv[side] + (size_t)lp * (R * 4) + r * 4;
-    Vec<real>::load(src, c[k]);
-    sc[k] = sb->sc[side][lp];
   }
 }
 
@@ -529,12 +431,10 @@ struct AdjGroup {
 // WALK: the walk schedule's op: model values already staged in sQ, and a
 // message marked for the next op (out = -2) passed in `carry` (pad4 = 1:
 // the op's adjoint starts from it).
-template <typename real, int R, int PPL, int G, bool WALK = false, bool STAGE = false>
+template <typename real, int R, int PPL, int G, bool WALK = false>
 __device__ __forceinline__ void backward_op(const SweepParams &p, const BwdOp &op, int opi,
                                             const int32_t *__restrict__ msg_slots, int unit, real *sP, real *sQ,
-                                            int lane, real (&carry)[PPL][4],
-                                            StageBuf<real, R, PPL> *sb = nullptr, uint32_t *phase = nullptr,
-                                            const BwdOp *next = nullptr) {
+                                            int lane, real (&carry)[PPL][4]) {
   constexpr int PPW = 32 / R;
   constexpr int UNIT = PPW * PPL;      // patterns per adjoint unit
   // the lane's patterns are processed in groups of G (whole base units): the
@@ -554,7 +454,7 @@ __device__ __forceinline__ void backward_op(const SweepParams &p, const BwdOp &o
   real *msg = static_cast<real *>(p.msg);
 
   real ca[G][4], cb[G][4], ax[G][4], cx[G][4];
-  int sa[G], sb_[G], sx[G];
+  int sa[G], sb[G], sx[G];
   // the group's children, counters, incoming messages (+ the message kept in
   // registers by the previous op) and, at a displayed-tree root, its own CLV
   auto load_group = [&](int grp) {
@@ -572,19 +472,8 @@ __device__ __forceinline__ void backward_op(const SweepParams &p, const BwdOp &o
           for (int i = 0; i < 4; ++i) ax[k][i] += carry[grp * G + k][i];
       }
     }
-    if constexpr (STAGE) {  // variant children are in the stage, tips and the fake child are not
-      if (op.a >= 0)
-        load_staged<real, R, PPL, G>(sb, 0, grp, pl, r, ca, sa);
-      else
-        load_child<real, R, G>(p, op.a, gg, r, PPW, ca, sa);
-      if (op.b >= 0)
-        load_staged<real, R, PPL, G>(sb, 1, grp, pl, r, cb, sb_);
-      else
-        load_child<real, R, G>(p, op.b, gg, r, PPW, cb, sb_);
-    } else {
-      load_child<real, R, G>(p, op.a, gg, r, PPW, ca, sa);
-      load_child<real, R, G>(p, op.b, gg, r, PPW, cb, sb_);
-    }
+    load_child<real, R, G>(p, op.a, gg, r, PPW, ca, sa);
+    load_child<real, R, G>(p, op.b, gg, r, PPW, cb, sb);
     const int32_t *sxp = p.scaler + (size_t)op.x * N + gg;
 #pragma unroll
     for (int k = 0; k < G; ++k) sx[k] = sxp[(size_t)k * PPW];
@@ -607,21 +496,7 @@ __device__ __forceinline__ void backward_op(const SweepParams &p, const BwdOp &o
       for (int k = 0; k < G; ++k) Vec<real>::load(cxp + (size_t)k * PPW * (R * 4), cx[k]);
     }
   };
-  // the next op's children, copied into the stage once this op has read it
-  auto issue_next = [&]() {
-    __syncwarp();
-    if (next) {
-      const int4 h = __ldg(reinterpret_cast<const int4 *>(next));  // x, a, b, ea
-      stage_issue<real, R, PPL>(p, sb, h.y, h.z, unit, lane, *phase);
-    }
-  };
-  if constexpr (STAGE) {
-    if (op.a >= 0 || op.b >= 0) stage_wait<real, R, PPL>(p, sb, *phase, lane);
-  }
   load_group(0);
-  if constexpr (STAGE) {
-    if (PPL / G == 1) issue_next();  // the op's last read of the stage
-  }
   if (!WALK) stage_model<real, R>(p, part, sQ, lane);
   stage_pmats_warp<real, R>(sP, static_cast<const real *>(p.pmat) + (size_t)part * p.n_edges * (R * 16), op.ea,
                             fake ? -1 : op.eb, lane);  // its __syncwarp also publishes sQ
@@ -638,12 +513,7 @@ __device__ __forceinline__ void backward_op(const SweepParams &p, const BwdOp &o
   for (int u = 0; u < UPU; ++u) ga[u] = gb[u] = 0;
 #pragma unroll
   for (int grp = 0; grp < PPL / G; ++grp) {
-    if (grp > 0) {
-      load_group(grp);
-      if constexpr (STAGE) {
-        if (grp == PPL / G - 1) issue_next();
-      }
-    }
+    if (grp > 0) load_group(grp);
     const size_t gg = g0 + (size_t)grp * G * PPW;
     const size_t off = lane_off + (size_t)grp * G * PPW * (R * 4);
     if (op.seed >= 0) {
@@ -673,7 +543,7 @@ __device__ __forceinline__ void backward_op(const SweepParams &p, const BwdOp &o
     real ua[G][4], ub[G][4];
 #pragma unroll
     for (int k = 0; k < G; ++k) {
-      const int sh = sx[k] - sa[k] - sb_[k];
+      const int sh = sx[k] - sa[k] - sb[k];
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
         ua[k][i] = ax[k][i] * pb[k][i];
@@ -793,26 +663,29 @@ __global__ void __launch_bounds__(THREADS, MINB) backward_kernel(const SweepPara
 // reverse of the forward walk, with its own message slots) for its unit. An
 // op's level-schedule index (its grad_partial row) travels in pad0.
 template <typename real, int R, int PPL, int G>
-__device__ __forceinline__ void backward_walk_unit(const SweepParams &p, int unit, real *sP, real *sQ, int lane,
-                                                   StageBuf<real, R, PPL> *sb, uint32_t &phase) {
+__device__ __forceinline__ void backward_walk_unit(const SweepParams &p, int unit, real *sP, real *sQ, int lane) {
   // a warp's patterns belong to one partition for the whole walk
   stage_model<real, R>(p, p.unit_part[unit * (PPL / kPPLBase)], sQ, lane);
+  constexpr int PPW = 32 / R;
+  const size_t g0 = (size_t)unit * PPW * PPL + lane / R;
   const int n = p.n_walk_bwd;
   real carry[PPL][4];  // a message passed to the next op in registers
-  // the first op's children are copied before the loop, every later op's
-  // while the op before it computes
+  // the next op's children are asked for in L2 as each op ends (the first
+  // op's before the loop)
   if (n > 0) {
     const int4 h = __ldg(reinterpret_cast<const int4 *>(p.walk_bwd_ops));  // x, a, b, ea
-    __syncwarp();  // the previous item is done with the stage
-    stage_issue<real, R, PPL>(p, sb, h.y, h.z, unit, lane, phase);
+    prefetch_child<real, R, PPL>(p, h.y, g0, lane % R, PPW);
+    prefetch_child<real, R, PPL>(p, h.z, g0, lane % R, PPW);
   }
   for (int i = 0; i < n; ++i) {
+    int4 h = make_int4(-1, -1, -1, -1);
+    if (i + 1 < n) h = __ldg(reinterpret_cast<const int4 *>(p.walk_bwd_ops + i + 1));
     __syncwarp();  // every lane is done with the previous op's staged values
     const BwdOp op = load_bwd_op<true>(p.walk_bwd_ops, i);
-    backward_op<real, R, PPL, G, true, true>(p, op, op.pad0, p.walk_msg_slots, unit, sP, sQ, lane, carry, sb,
-                                             &phase, i + 1 < n ? p.walk_bwd_ops + i + 1 : nullptr);
+    backward_op<real, R, PPL, G, true>(p, op, op.pad0, p.walk_msg_slots, unit, sP, sQ, lane, carry);
+    prefetch_child<real, R, PPL>(p, h.y, g0, lane % R, PPW);
+    prefetch_child<real, R, PPL>(p, h.z, g0, lane % R, PPW);
   }
-  stage_drain<real, R, PPL>(sb, phase);
 }
 
 template <typename real, int R, int THREADS, int MINB, int PPL>
@@ -821,14 +694,10 @@ __global__ void __launch_bounds__(THREADS, MINB) backward_walk_kernel(const Swee
   constexpr int WPB = THREADS / 32;
   __shared__ __align__(16) real sPw[WPB][2 * R * PLayout<real>::kRow];
   __shared__ __align__(16) real sQw[WPB][ModelSlice<R>::kSize];
-  __shared__ StageBuf<real, R, PPL> sbw[WPB];
   const int unit = unit_begin + blockIdx.x * WPB + (threadIdx.x >> 5);
   if (unit >= unit_end) return;  // whole warp
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (lane == 0) tc::mbar_init(tc::smem_u32(&sbw[w].bar), 1);
-  __syncwarp();
-  uint32_t phase = 0;
-  backward_walk_unit<real, R, PPL, AdjGroup<THREADS, MINB, PPL>::G>(p, unit, sPw[w], sQw[w], lane, &sbw[w], phase);
+  backward_walk_unit<real, R, PPL, AdjGroup<THREADS, MINB, PPL>::G>(p, unit, sPw[threadIdx.x >> 5],
+                                                                    sQw[threadIdx.x >> 5], threadIdx.x & 31);
 }
 
 // ------------------------------------------------------------- P-matrices
@@ -1220,24 +1089,18 @@ __global__ void __launch_bounds__(THREADS, MINB) backward_walk_batch_kernel(cons
   __shared__ __align__(16) real sPw[WPB][2 * R * PLayout<real>::kRow];
   __shared__ __align__(16) real sQw[WPB][ModelSlice<R>::kSize];
   __shared__ __align__(16) SweepParams sp[WPB];
-  __shared__ StageBuf<real, R, PPL> sbw[WPB];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (lane == 0) tc::mbar_init(tc::smem_u32(&sbw[w].bar), 1);
-  __syncwarp();
-  uint32_t phase = 0;
   for (int item = next_item(b, lane); item < b.n_items; item = next_item(b, lane)) {
     const int2 it = b.items[item];
     __syncwarp();
     load_params(&b.cands[it.x].sweep, &sp[w], lane);
-    backward_walk_unit<real, R, PPL, AdjGroup<THREADS, MINB, PPL>::G>(sp[w], it.y, sPw[w], sQw[w], lane, &sbw[w],
-                                                                      phase);
+    backward_walk_unit<real, R, PPL, AdjGroup<THREADS, MINB, PPL>::G>(sp[w], it.y, sPw[w], sQw[w], lane);
   }
 }
 
 __global__ void pmatrix_batch_kernel(const BatchParams b) {
   const BatchCand &c = b.cands[blockIdx.y];
   const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx == 0 && c.sweep.fault) *c.sweep.fault = 0;  // the adjoint walk's bounded waits report here
   if (idx >= c.n_pmat) return;
   pmatrix_entry(idx, c.n_parts, c.n_edges, 4, 4, c.lambda, c.U, c.Uinv, c.rates, c.brlen, c.pmat64, c.pmat32);
 }

@@ -961,9 +961,7 @@ void netlk_ctx::enqueue(bool pm, bool fwd_on, bool reduce, bool mixk, bool bwd_o
   }
   const SweepParams sp = sweep();
   const MixParams mp = mix();
-  // the fault word of the bounded device waits (tensor-core MMAs, the adjoint
-  // walk's staged copies)
-  if ((use_tc || walk_ok) && (fwd_on || bwd_on)) CUDA_OK(cudaMemsetAsync(sp.fault, 0, 8, stream));
+  if (use_tc && (fwd_on || bwd_on)) CUDA_OK(cudaMemsetAsync(sp.fault, 0, 8, stream));
   if (fwd_on) {
     if (use_tc)
       launch_forward20_tc(stream, sp, fwd_level_begin.data(), dag.n_levels, sms);
@@ -1475,8 +1473,8 @@ void netlk_ctx::read_results(double *total, double *part_logl, double *d_brlen, 
   const int nout = 3 + P + topo.n_ret;
   const double *o = h_out.as<double>();
   check_injected();
-  if ((use_tc || walk_ok) && *reinterpret_cast<const int32_t *>(o + nout - 1) != 0)
-    throw Error(NETLK_ERR_TIMEOUT, "a bounded device wait timed out (tensor-core MMA or staged adjoint copy)");
+  if (use_tc && *reinterpret_cast<const int32_t *>(o + nout - 1) != 0)
+    throw Error(NETLK_ERR_TIMEOUT, "tensor-core sweep: an MMA completion wait timed out");
   if (o[1] != 0.0 || !std::isfinite(o[0]))
     throw Error(NETLK_ERR_NUMERIC, "Invalid network likelihood: negative infinity or NaN");
   if (total) *total = o[0];
@@ -2479,9 +2477,6 @@ int netlk_batch_loglikelihood_gradient(netlk_batch *b, double *totals, double *c
         netlk_ctx *c = b->ctxs[i];
         const double *o = res + b->res_off[i];
         const int nout = 3 + c->P + c->topo.n_ret;
-        if (*reinterpret_cast<const int32_t *>(o + nout - 1) != 0)
-          throw Error(NETLK_ERR_TIMEOUT, "batch: candidate " + std::to_string(i) +
-                                             ": a staged adjoint copy's bounded wait timed out");
         if (o[1] != 0.0 || !std::isfinite(o[0]))
           throw Error(NETLK_ERR_NUMERIC, "batch: candidate " + std::to_string(i) +
                                              ": Invalid network likelihood: negative infinity or NaN");
