@@ -16,12 +16,23 @@ oracle (test harness; not a test module itself).
   (``optimize_reticulation``, :75-102; pll-modules' ``pllmod_opt_minimize_brent``,
   not vendored), repeated until a pass leaves the log-likelihood unchanged.
 
+* Model parameters, the one-dimensional part of ``optimize_params``
+  (src/optimization/ModelOptimization.cpp:25-97): per partition a Brent
+  search of the Gamma shape (pll-modules' ``pllmod_algo_opt_onedim_treeinfo``
+  with PLLMOD_OPT_PARAM_ALPHA, bounds 0.02 and 1000), then each
+  exchangeability (the last one, GT, fixed at its value) by Brent on its
+  logarithm within [1e-3, 1e3] - a coordinate search standing in for
+  pll-modules' BFGS over the rates - each evaluation through the
+  log-likelihood callback (``likelihood_target_function``).
+
 The Newton and Brent searches follow the published methods: Newton's step
 -f'/f'' toward a maximum, clamped to the bounds, with a halving / doubling step
 where the curvature is not negative; Brent (1973) golden-section search with
 parabolic interpolation.
 """
 import math
+
+import numpy as np
 
 BRLEN_MIN, BRLEN_MAX = 1e-6, 100.0           # RAXML_BRLEN_MIN / MAX
 BRPROB_MIN, BRPROB_MAX = 1e-6, 1.0 - 1e-6    # NetraxOptions.hpp:102-103
@@ -144,3 +155,35 @@ def optimize_reticulations(logl_at, probs, tol, max_passes=10):
             break
         act = loop
     return probs, logl_at(probs)
+
+
+ALPHA_MIN, ALPHA_MAX = 0.02, 1000.0     # PLLMOD_OPT_MIN_ALPHA / MAX_ALPHA
+SUBST_MIN, SUBST_MAX = 1e-3, 1e3        # PLLMOD_OPT_MIN_SUBST_RATE / MAX
+
+
+def optimize_model(logl_at, models, tol=1e-6, exchangeabilities=True):
+    """models: per partition (freqs, exch, alpha). logl_at(models) -> logL.
+    Brent on each alpha, then each exchangeability but the last on a log
+    scale; returns the final models and logL."""
+    models = [(np.asarray(f, float).copy(), np.asarray(x, float).copy(), float(a)) for f, x, a in models]
+
+    def with_param(p, alpha=None, k=None, value=None):
+        out = [(f, x.copy(), a) for f, x, a in models]
+        f, x, a = out[p]
+        if alpha is not None:
+            a = alpha
+        if k is not None:
+            x[k] = value
+        out[p] = (f, x, a)
+        return out
+
+    for p in range(len(models)):
+        la, _ = brent_minimize(lambda u: -logl_at(with_param(p, alpha=math.exp(u))),
+                               math.log(ALPHA_MIN), math.log(ALPHA_MAX), math.log(models[p][2]), tol)
+        models = with_param(p, alpha=math.exp(la))
+        if exchangeabilities:
+            for k in range(len(models[p][1]) - 1):
+                lx, _ = brent_minimize(lambda u: -logl_at(with_param(p, k=k, value=math.exp(u))),
+                                       math.log(SUBST_MIN), math.log(SUBST_MAX), math.log(models[p][1][k]), tol)
+                models = with_param(p, k=k, value=math.exp(lx))
+    return models, logl_at(models)

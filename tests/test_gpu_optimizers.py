@@ -13,6 +13,11 @@ loops on the oracle (``tests/optimizer_loops.py`` restates them).
 * Reticulation probabilities: the Brent loop on ``netlk_set_reticulation_probs``
   + ``netlk_loglikelihood`` against the same loop on the oracle; the
   probabilities agree within 1e-5 and the logL within 1e-9 / 1e-6.
+* Model parameters: Brent on each partition's Gamma shape and on the
+  exchangeabilities through ``netlk_set_model`` + ``netlk_loglikelihood``
+  (the model optimizer's callback) against the same searches on the oracle:
+  parameters within 1e-4 (FP64) / 1e-2 (FP32) relative, logL within 1e-9 /
+  1e-6.
 """
 import numpy as np
 import pytest
@@ -124,3 +129,34 @@ def test_brent_reticulation_loop_matches_the_oracle(name, variant):
             p, logl = opt.optimize_reticulations(logl_at, list(lik.ret_probs), tol=1e-8)
             assert logl == pytest.approx(want_logl, rel=rel_logl)
             assert np.abs(np.array(p) - np.array(want_p)).max() <= tol_p, (precision, p, want_p)
+
+
+@pytest.mark.parametrize("name,exch", [("twoReticulations", True), ("synthetic_12taxa_3ret_2parts", False)])
+def test_model_optimizer_callbacks_match_the_oracle(name, exch):
+    from oracle import improved, pllmath
+    orc = _oracle(name, "AVERAGE")
+    start = [(p.freqs, p.exch, GoldenPartition(d).alpha) for p, d in zip(orc.parts, CASES[name]["partitions"])]
+
+    def orc_logl(models):
+        for part, (f, x, a) in zip(orc.parts, models):
+            part.exch = np.asarray(x, float)
+            part.rates = pllmath.gamma_rates_mean(a, part.R)
+            part.lam, part.U, part.Uinv, part.Q = pllmath.eigensystem(part.exch, part.freqs)
+        return orc.loglikelihood()
+
+    want_models, want_logl = opt.optimize_model(orc_logl, start, exchangeabilities=exch)
+    for precision, rel_logl, rel_par in (("fp64", 1e-9, 1e-4), ("fp32", 1e-6, 1e-2)):
+        with _lik(name, "AVERAGE", precision) as lik:
+            start_logl = lik.loglikelihood()
+
+            def logl_at(models):
+                for p, (f, x, a) in enumerate(models):
+                    lik.set_model(p, f, x, a)
+                return lik.loglikelihood()
+
+            models, logl = opt.optimize_model(logl_at, start, exchangeabilities=exch)
+            assert logl >= start_logl
+            assert logl == pytest.approx(want_logl, rel=rel_logl)
+            for (f, x, a), (wf, wx, wa) in zip(models, want_models):
+                assert a == pytest.approx(wa, rel=rel_par)
+                assert np.allclose(x, wx, rtol=rel_par)
