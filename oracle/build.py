@@ -43,7 +43,7 @@ def lib():
             dp, up, dp]
         _lib.oracle_update_partial.restype = None
         _lib.oracle_root_logl.argtypes = [
-            ctypes.c_int64, ctypes.c_int, ctypes.c_int, dp, up, dp, dp, dp, dp]
+            ctypes.c_int64, ctypes.c_int, ctypes.c_int, dp, up, dp, dp, dp, dp, ctypes.c_double, dp]
         _lib.oracle_root_logl.restype = ctypes.c_double
         _lib.oracle_num_threads.restype = ctypes.c_int
     return _lib
@@ -71,8 +71,8 @@ def update_partial(parent, parent_scaler, left, left_scaler, pl,
                                 _dp(right), _up(right_scaler), _dp(pr))
 
 
-def root_logl(clv, scaler, freqs, rate_weights, weights, persite=None):
+def root_logl(clv, scaler, freqs, rate_weights, weights, persite=None, gamma_frac=1.0, inv_term=None):
     n, R, S = clv.shape
     return lib().oracle_root_logl(n, R, S, _dp(clv), _up(scaler), _dp(freqs),
                                   _dp(rate_weights), _dp(weights),
-                                  _dp(persite))
+                                  _dp(persite), float(gamma_frac), _dp(inv_term))

@@ -17,6 +17,8 @@
  *  - pll_compute_root_loglikelihood, called at ImprovedLoglikelihood.cpp:450:
  *      logl = sum_n w_n [ log(sum_r rw_r sum_i pi_i clv[n][r][i])
  *                         + scaler_n * log(2^-256) ]
+ *    (with invariant sites the site likelihood is (1 - pinv) times that
+ *    mixture plus pinv times the invariant state's frequency)
  *
  * The same code is the timed CPU baseline (OpenMP over sites).
  */
@@ -68,11 +70,13 @@ void oracle_update_partial(int64_t n, int R, int S, double *parent,
 }
 
 /* Returns the weighted root log-likelihood; persite (optional) receives the
- * unweighted per-site values. */
+ * unweighted per-site values. With invariant sites (+I) the site likelihood
+ * is gamma_frac * (the Gamma mixture above) + inv_term[s]; inv_term NULL
+ * (and gamma_frac 1) without. */
 double oracle_root_logl(int64_t n, int R, int S, const double *clv,
                         const uint32_t *scaler, const double *freqs,
                         const double *rate_weights, const double *weights,
-                        double *persite) {
+                        double *persite, double gamma_frac, const double *inv_term) {
   const int64_t span = (int64_t)R * S;
   const double log_thr = log(ORACLE_SCALE_THRESHOLD);
   double total = 0.0;
@@ -85,8 +89,12 @@ double oracle_root_logl(int64_t n, int R, int S, const double *clv,
       for (int i = 0; i < S; ++i) t += freqs[i] * c[r * S + i];
       site += rate_weights[r] * t;
     }
-    double l = log(site);
+    double l = log(gamma_frac * site);
     if (scaler) l += (double)scaler[s] * log_thr;
+    if (inv_term && inv_term[s] > 0.0) { /* log(exp(l) + inv), without overflow */
+      const double b = log(inv_term[s]);
+      l = l > b ? l + log1p(exp(b - l)) : b + log1p(exp(l - b));
+    }
     if (persite) persite[s] = l;
     total += weights[s] * l;
   }

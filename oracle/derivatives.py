@@ -144,12 +144,21 @@ def _tree_derivatives(orc, part, n_edges):
             st = np.einsum("nri,im->nrm", A, part.U) * np.einsum("mj,nrj->nrm", part.Uinv, B)
             e0 = np.exp(x * length)[None, :, :]
             w = part.rate_weights[None, :, None]
-            L0 = (w * st * e0).sum(axis=(1, 2))
-            L1 = (w * st * x[None] * e0).sum(axis=(1, 2))
-            L2 = (w * st * (x * x)[None] * e0).sum(axis=(1, 2))
-            logl_seen.append(float(np.dot(part.weights, np.log(L0) + asc + bsc)))
-            g1 = float(np.dot(part.weights, L1 / L0))
-            g2 = float(np.dot(part.weights, L2 / L0 - (L1 / L0) ** 2))
+            L0 = part.gamma_frac * (w * st * e0).sum(axis=(1, 2))
+            L1 = part.gamma_frac * (w * st * x[None] * e0).sum(axis=(1, 2))
+            L2 = part.gamma_frac * (w * st * (x * x)[None] * e0).sum(axis=(1, 2))
+            sc = asc + bsc
+            if part.inv_term is None:
+                logl_seen.append(float(np.dot(part.weights, np.log(L0) + sc)))
+                den = L0
+            else:
+                # + pinv * pi(invariant state) per site, in the scaled units of L0
+                with np.errstate(divide="ignore"):
+                    logl_seen.append(float(np.dot(part.weights,
+                                                  np.logaddexp(np.log(L0) + sc, np.log(part.inv_term)))))
+                den = L0 + part.inv_term * np.exp(np.minimum(-sc, 700.0))
+            g1 = float(np.dot(part.weights, L1 / den))
+            g2 = float(np.dot(part.weights, L2 / den - (L1 / den) ** 2))
             for e in edges:
                 d1[e], d2[e] = g1, g2
             # top of v: sum_i A_i P_ij(length) (A already holds u's outside and the sibling)

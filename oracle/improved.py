@@ -32,14 +32,25 @@ MIN_INTERESTING_LOGPROB = math.log(1e-6)   # src/NetraxOptions.hpp:108
 
 
 class Partition:
-    """One alignment partition: tips, weights and a GTR+Gamma model."""
+    """One alignment partition: tips, weights and a GTR+Gamma(+I) model.
 
-    def __init__(self, tip_codes, weights, freqs, exch, rates, rate_weights=None):
+    ``pinv`` > 0 adds invariant sites (``pllmath`` docstring): ``rates`` are
+    then the effective category rates rates / (1 - pinv), ``gamma_frac`` is
+    1 - pinv and ``inv_term[s]`` = pinv * pi(invariant state of s) or 0."""
+
+    def __init__(self, tip_codes, weights, freqs, exch, rates, rate_weights=None, pinv=0.0):
         self.tip_codes = np.ascontiguousarray(tip_codes, dtype=np.uint32)
         self.weights = np.ascontiguousarray(weights, dtype=np.float64)
         self.freqs = np.ascontiguousarray(freqs, dtype=np.float64)
         self.exch = np.asarray(exch, dtype=np.float64)
-        self.rates = np.asarray(rates, dtype=np.float64)
+        self.pinv = float(pinv)
+        self.rates = np.asarray(rates, dtype=np.float64) / (1.0 - self.pinv)
+        self.gamma_frac = 1.0 - self.pinv
+        self.inv_term = None
+        if self.pinv > 0.0:
+            st = pllmath.invariant_states(self.tip_codes)
+            self.inv_term = np.ascontiguousarray(
+                np.where(st >= 0, self.pinv * self.freqs[np.maximum(st, 0)], 0.0), dtype=np.float64)
         R = self.rates.size
         self.rate_weights = (np.full(R, 1.0 / R) if rate_weights is None
                              else np.ascontiguousarray(rate_weights, dtype=np.float64))
@@ -382,7 +393,8 @@ class ImprovedOracle:
         tree.partition_logl = []
         for p, part in enumerate(self.parts):
             ll = cbuild.root_logl(m.clv[p], m.scaler[p], part.freqs,
-                                  part.rate_weights, part.weights)
+                                  part.rate_weights, part.weights, gamma_frac=part.gamma_frac,
+                                  inv_term=part.inv_term)
             tree.partition_logl.append(ll)
         tree.logl_valid = True
 
@@ -443,7 +455,8 @@ class ImprovedOracle:
             dn, di = t.dtroot
             m = self.pernode[dn][di]
             t.partition_logl = [cbuild.root_logl(m.clv[p], m.scaler[p], part.freqs, part.rate_weights,
-                                                 part.weights) for p, part in enumerate(self.parts)]
+                                                 part.weights, gamma_frac=part.gamma_frac,
+                                                 inv_term=part.inv_term) for p, part in enumerate(self.parts)]
         return self.evaluate()[0]
 
     def root_trees(self):

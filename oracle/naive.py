@@ -53,7 +53,8 @@ def _tree_logl(orc, part, p):
         return parent, ps
 
     clv, sc = clv_of(dt)
-    return cbuild.root_logl(clv, sc, part.freqs, part.rate_weights, part.weights)
+    return cbuild.root_logl(clv, sc, part.freqs, part.rate_weights, part.weights,
+                            gamma_frac=part.gamma_frac, inv_term=part.inv_term)
 
 
 def naive_loglikelihood(orc):

@@ -12,6 +12,12 @@ Test infrastructure only. libpll is not vendored in the reference (empty
   (``PLL_GAMMA_RATES_MEAN``, ``src/RaxmlWrapper.cpp:621``).
 * Nucleotide IUPAC tip encoding (A=1, C=2, G=4, T=8; gaps, N, ? = 15) and
   pattern compression with weights (``src/RaxmlWrapper.cpp:330``).
+* Invariant sites for +I: a pattern is invariant in state j when the state
+  masks of all its tips have exactly state j in common (their AND has one
+  bit); the model's site likelihood is (1 - pinv) times the Gamma mixture
+  (rates divided by 1 - pinv, so the mean rate stays 1) plus pinv times the
+  frequency of that state (libpll's ``prop_invar``, set by NetRAX through
+  raxml-ng's model, ``src/RaxmlWrapper.cpp:621-640``).
 """
 import numpy as np
 from scipy import special
@@ -112,3 +118,16 @@ def read_fasta(text):
         else:
             cur.append(line)
     return names, ["".join(s) for s in seqs]
+
+
+def invariant_states(tip_codes):
+    """Per pattern: the one state every tip admits, or -1 (libpll's
+    invariant-site rule as described in the module docstring)."""
+    codes = np.asarray(tip_codes, dtype=np.uint64)
+    common = np.bitwise_and.reduce(codes, axis=0)
+    single = (common != 0) & ((common & (common - np.uint64(1))) == 0)
+    state = np.full(codes.shape[1], -1, dtype=np.int64)
+    idx = np.nonzero(single)[0]
+    if idx.size:
+        state[idx] = np.log2(common[idx].astype(np.float64)).round().astype(np.int64)
+    return state

@@ -19,6 +19,9 @@
  * partial sums are added in thread order, so results depend only on the
  * thread count.
  *
+ * With invariant sites (+I) the site likelihood is gamma_frac times the
+ * root mixture plus inv_term[s] (in unscaled units).
+ *
  * Adjoint (no counterpart in the reference, which differentiates one edge at
  * a time through sumtables, LikelihoodDerivatives.cpp:190-344): reverse-mode
  * differentiation of the same pruning. For op x with
@@ -63,6 +66,8 @@ typedef struct {
   double *clv;                /* [n_var][n][R][S] */
   uint32_t *scaler;           /* [n_var][n] */
   double *adj;                /* [n_var][n][R][S] (adjoint only) */
+  double gamma_frac;          /* 1 - pinv */
+  const double *inv_term;     /* [n] pinv * pi(invariant state), or NULL without +I */
 } oracle_part;
 
 static int n_threads(void) {
@@ -233,7 +238,11 @@ int oracle_sweep_forward(int32_t n_ops, const oracle_op *ops, int32_t n_parts, c
         double acc = 0.0;
         for (int64_t s = lo; s < hi; ++s) {
           const double site = root_site(pp, pp->clv + ((int64_t)v * pp->n + s) * RS, R, S);
-          const double l = log(site) + (double)pp->scaler[(int64_t)v * pp->n + s] * LOG_SCALE_THRESHOLD;
+          double l = log(pp->gamma_frac * site) + (double)pp->scaler[(int64_t)v * pp->n + s] * LOG_SCALE_THRESHOLD;
+          if (pp->inv_term && pp->inv_term[s] > 0.0) {  /* + pinv * pi(state), in log space */
+            const double b = log(pp->inv_term[s]);
+            l = l > b ? l + log1p(exp(b - l)) : b + log1p(exp(l - b));
+          }
           acc += pp->weights[s] * l;
         }
         partial[((size_t)t * n_slots + d) * n_parts + p] = acc;
@@ -277,7 +286,11 @@ int oracle_sweep_adjoint(int32_t n_ops, const oracle_op *bwd_ops, int32_t n_var,
         for (int64_t s = lo; s < hi; ++s) {
           const double *x = pp->clv + ((int64_t)v * pp->n + s) * RS;
           double *ad = pp->adj + ((int64_t)v * pp->n + s) * RS;
-          const double c = w * pp->weights[s] / root_site(pp, x, R, S);
+          /* d log L_s / d X[r][i] = gamma_frac rw_r pi_i / L_s, L_s in X's scaled units */
+          double den = pp->gamma_frac * root_site(pp, x, R, S);
+          if (pp->inv_term && pp->inv_term[s] > 0.0)
+            den += ldexp(pp->inv_term[s], 256 * (int)pp->scaler[(int64_t)v * pp->n + s]);
+          const double c = w * pp->weights[s] * pp->gamma_frac / den;
           for (int r = 0; r < R; ++r)
             for (int i = 0; i < S; ++i) ad[r * S + i] = c * pp->rate_weights[r] * pp->freqs[i];
         }

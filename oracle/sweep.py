@@ -39,7 +39,8 @@ class _Part(ctypes.Structure):
     _fields_ = [("R", ctypes.c_int32), ("S", ctypes.c_int32), ("n", ctypes.c_int64),
                 ("tips", ctypes.c_void_p), ("weights", ctypes.c_void_p), ("freqs", ctypes.c_void_p),
                 ("rate_weights", ctypes.c_void_p), ("pmat", ctypes.c_void_p), ("dpmat", ctypes.c_void_p),
-                ("clv", ctypes.c_void_p), ("scaler", ctypes.c_void_p), ("adj", ctypes.c_void_p)]
+                ("clv", ctypes.c_void_p), ("scaler", ctypes.c_void_p), ("adj", ctypes.c_void_p),
+                ("gamma_frac", ctypes.c_double), ("inv_term", ctypes.c_void_p)]
 
 
 def _lib():
@@ -129,13 +130,15 @@ class SweepOracle:
         for p, part in enumerate(orc.parts):
             rec = self.parts[p]
             rec.R, rec.S, rec.n = part.R, part.S, part.n
+            rec.gamma_frac = part.gamma_frac
             clv = np.empty((self.n_var, part.n, part.R, part.S))
             sc = np.empty((self.n_var, part.n), np.uint32)
             adj = np.empty_like(clv) if with_gradient else None
             pm = np.empty((net.n_edges, part.R, part.S, part.S))
             dpm = np.empty_like(pm)
             arrs = dict(tips=part.tip_codes, weights=part.weights, freqs=part.freqs,
-                        rate_weights=part.rate_weights, pmat=pm, dpmat=dpm, clv=clv, scaler=sc, adj=adj)
+                        rate_weights=part.rate_weights, pmat=pm, dpmat=dpm, clv=clv, scaler=sc, adj=adj,
+                        inv_term=part.inv_term)
             for k, a in arrs.items():
                 if a is not None:
                     assert a.flags["C_CONTIGUOUS"]
