@@ -87,6 +87,12 @@ typedef struct {
   double alpha;                   /* Gamma shape; used when rates == NULL     */
   const double *rates;            /* optional [rate_cats] category rates      */
   const double *rate_weights;     /* optional [rate_cats]; default 1/rate_cats */
+  double prop_invar;              /* proportion of invariant sites (+I), in
+                                     [0, 0.99]; 0 = none. With p > 0 a site's
+                                     likelihood is (1 - p) x the rate mixture
+                                     (category rates divided by 1 - p) + p x
+                                     the frequency of the one state every tip
+                                     admits, if any (libpll's prop_invar)     */
 } netlk_partition;
 
 typedef struct {
@@ -279,6 +285,13 @@ int netlk_set_reticulation_probs(netlk_ctx *ctx, const double *first_probs,
 int netlk_set_model(netlk_ctx *ctx, int32_t partition, const double *freqs,
                     const double *exchangeabilities, double alpha,
                     const double *rates);
+
+/* Replace the proportion of invariant sites of one partition (libpll's
+ * pll_update_invariant_sites_proportion, which raxml-ng's model code calls
+ * for NetRAX's partitions, src/RaxmlWrapper.cpp:621-640; the model
+ * optimizer's PINV step, src/optimization/ModelOptimization.cpp:68-76).
+ * prop_invar in [0, 0.99]. */
+int netlk_set_prop_invar(netlk_ctx *ctx, int32_t partition, double prop_invar);
 
 /* -------------------------------------------------------------- evaluation */
 /* Network log-likelihood. Replaces computeLoglikelihood(ann_network, 0, 1)

@@ -40,6 +40,7 @@ EXPORTED = [
     "netlk_batch_loglikelihood_gradient", "netlk_batch_destroy", "netlk_edge_loglikelihood",
     "netlk_last_site_updates", "netlk_encode_states", "netlk_compress_patterns", "netlk_inject_failure",
     "netlk_walk_segments", "netlk_batch_create_ex", "netlk_batch_info",
+    "netlk_set_prop_invar",
 ]
 
 
@@ -57,7 +58,7 @@ class Partition(ctypes.Structure):
                 ("n_patterns", ctypes.c_int32), ("tip_states", c_uint32_p),
                 ("pattern_weights", c_double_p), ("freqs", c_double_p),
                 ("exchangeabilities", c_double_p), ("alpha", ctypes.c_double),
-                ("rates", c_double_p), ("rate_weights", c_double_p)]
+                ("rates", c_double_p), ("rate_weights", c_double_p), ("prop_invar", ctypes.c_double)]
 
 
 class Options(ctypes.Structure):
@@ -121,6 +122,7 @@ def lib():
     L.netlk_set_branch_lengths.argtypes = [vp, c_double_p, ctypes.c_int32]
     L.netlk_set_reticulation_probs.argtypes = [vp, c_double_p, ctypes.c_int32]
     L.netlk_set_model.argtypes = [vp, ctypes.c_int32, c_double_p, c_double_p, ctypes.c_double, c_double_p]
+    L.netlk_set_prop_invar.argtypes = [vp, ctypes.c_int32, ctypes.c_double]
     L.netlk_loglikelihood.argtypes = [vp, c_double_p, c_double_p, c_double_p]
     L.netlk_loglikelihood_gradient.argtypes = [vp, c_double_p, c_double_p, c_double_p, c_double_p]
     L.netlk_edge_derivatives.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, c_double_p, c_double_p]

@@ -317,7 +317,12 @@ __device__ __forceinline__ void forward_op(const SweepParams &p, const FwdOp &op
     for (int k = 0; k < PPL; ++k) {
       real t = rw * (freq[0] * v[k][0] + freq[1] * v[k][1] + freq[2] * v[k][2] + freq[3] * v[k][3]);
       t = rate_sum<R>(t);
-      if (r == 0) ll.add(p, g0 + (size_t)k * PPW, t, s[k]);
+      if (r == 0) {
+        if (p.inv_term)
+          ll.add_inv(p, part, g0 + (size_t)k * PPW, t, s[k]);
+        else
+          ll.add(p, g0 + (size_t)k * PPW, t, s[k]);
+      }
     }
     // the warp's first forward unit carries its sum, the others zero
     double *sp = p.site_partial + (size_t)op.slot * p.n_units_fwd + (size_t)unit * UFW;
@@ -524,7 +529,8 @@ __device__ __forceinline__ void backward_op(const SweepParams &p, const BwdOp &o
         t = rate_sum<R>(t);
         const real sw = sd * pattern_weight<real>(p, gg + (size_t)k * PPW);
         if (t > (real)0 && sw != (real)0) {
-          const real f = sw * rw / t;
+          const real f = p.inv_term ? sw * rw * root_seed_factor<real>(p, part, gg + (size_t)k * PPW, t, sx[k])
+                                    : sw * rw / t;
 #pragma unroll
           for (int i = 0; i < 4; ++i) ax[k][i] += f * sF[i];
         }

@@ -74,6 +74,13 @@ struct SweepParams {
   const float *rates32;         // [n_parts][R]
   const float *Q32;             // [n_parts][S*S]
   const float *seeds32;         // [n_slots][n_parts]
+  // invariant sites (+I): null when no partition has any; else the site
+  // likelihood at a displayed-tree root is gamma_frac[part] * (rate mixture)
+  // + inv_term[pattern] (pinv * pi of the invariant state, 0 if none)
+  const double *gamma_frac;     // [n_parts] 1 - pinv
+  const float *gamma_frac32;
+  const double *inv_term;       // [N]
+  const float *inv_term32;
   void *clv;                    // [V][N][R][S] real
   int32_t *scaler;              // [V][N]
   void *msg;                    // [M][N][R][4] real adjoint messages
@@ -218,6 +225,8 @@ struct TanParams {
   const double *weights;        // [N]
   const double *freqs;          // [n_parts][S]
   const double *rate_weights;   // [n_parts][R]
+  const double *gamma_frac;     // invariant sites (+I), as in SweepParams; null without
+  const double *inv_term;
   double *partial;              // [n_slots][2][n_blocks] sums of w L'/L and w (L''/L - (L'/L)^2)
 };
 

@@ -207,7 +207,12 @@ __global__ void __launch_bounds__(kWarps20 * 32) forward20_kernel(const SweepPar
 #pragma unroll
       for (int i = 0; i < S20; ++i) t += model_val<real>(p.freqs, p.freqs32, part * S20 + i) * v[i];
       t = rate_sum<R>(rw * t);
-      if (r == 0) ll.add(p, g, t, s);
+      if (r == 0) {
+        if (p.inv_term)
+          ll.add_inv(p, part, g, t, s);
+        else
+          ll.add(p, g, t, s);
+      }
     }
   }
   if (op.slot >= 0) ll.store(p.site_partial + (size_t)op.slot * p.n_units_fwd + unit, lane);
@@ -287,7 +292,9 @@ __global__ void __launch_bounds__(kWarps20 * 32) backward20_kernel(const SweepPa
       const real sw = model_val<real>(p.seeds, p.seeds32, (size_t)op.seed * p.n_parts + part) *
                       pattern_weight<real>(p, g);
       if (t > (real)0 && sw != (real)0) {
-        const real f = sw * rw / t;
+        const real f = p.inv_term
+                           ? sw * rw * root_seed_factor<real>(p, part, g, t, p.scaler[(size_t)op.x * N + g])
+                           : sw * rw / t;
 #pragma unroll
         for (int i = 0; i < S20; ++i) ax[i] += f * sF[i];
       }

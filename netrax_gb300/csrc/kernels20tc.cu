@@ -312,7 +312,10 @@ __global__ void __launch_bounds__(kTThreads, 1)
       __syncthreads();
       if (h == 0) {
         SiteSum<float> ll;
-        ll.add_w(wg, s_t[m] + s_t[kTM + m], sc);
+        if (p.inv_term32)
+          ll.add_inv_w(wg, s_t[m] + s_t[kTM + m], sc, p.gamma_frac32[part], p.inv_term32[g]);
+        else
+          ll.add_w(wg, s_t[m] + s_t[kTM + m], sc);
         ll.store(p.site_partial + (size_t)cur.slot * p.n_units_fwd + g0 / 32 + q, lane);
       }
     }
@@ -641,7 +644,11 @@ __global__ void __launch_bounds__(kTThreads, 1)
         }
       }
       if (op.seed >= 0 && tseed > 0.f && sw != 0.f) {
-        const float f = sw * p.rate_weights32[part * 4 + r] / tseed;
+        const float f =
+            p.inv_term32
+                ? sw * p.rate_weights32[part * 4 + r] *
+                      root_seed_factor<float>(p, part, g, tseed, p.scaler[(size_t)op.x * N + g])
+                : sw * p.rate_weights32[part * 4 + r] / tseed;
 #pragma unroll
         for (int i = 0; i < 20; ++i) ax[i] += f * p.freqs32[part * 20 + i];
       }

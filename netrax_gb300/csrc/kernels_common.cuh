@@ -192,6 +192,18 @@ struct SiteSum<double> {
     const double w = p.weights[g];
     if (w != 0.0) ll += w * (log(t) + (double)k * Scale<double>::kLogUnit);
   }
+  // with invariant sites: w log(gf t 2^(-256 k) + it)
+  __device__ __forceinline__ void add_inv(const SweepParams &p, int part, size_t g, double t, int k) {
+    const double w = p.weights[g];
+    if (w == 0.0) return;
+    double a = log(p.gamma_frac[part] * t) + (double)k * Scale<double>::kLogUnit;
+    const double it = p.inv_term[g];
+    if (it > 0.0) {
+      const double b = log(it);
+      a = a > b ? a + log1p(exp(b - a)) : b + log1p(exp(a - b));
+    }
+    ll += w * a;
+  }
   __device__ __forceinline__ void store(double *dst, int lane) {
     ll = warp_sum(ll);
     if (lane == 0) *dst = ll;
@@ -218,6 +230,30 @@ struct SiteSum<float> {
     const FF y = ff_add(ku, FF{lt, 0.f});
     ll = ff_add(ll, ff_mul(FF{w.x, w.y}, y));
   }
+  // with invariant sites: w log(gf t 2^(-k) + it), gf and it given
+  __device__ __forceinline__ void add_inv_w(float2 w, float t, int k, float gf, float it) {
+    if (w.x == 0.f) return;
+    if (!(it > 0.f)) {
+      add_w(w, gf * t, k);
+      return;
+    }
+    const float lt = logf(gf * t);
+    const float b = logf(it);
+    FF y;
+    if (!isfinite(lt)) {
+      y = FF{b, 0.f};
+    } else {
+      const float kf = (float)k;
+      const float ph = kf * kUnitHi;
+      const FF a = ff_add(quick_two_sum(ph, __fmaf_rn(kf, kUnitHi, -ph) + kf * kUnitLo), FF{lt, 0.f});
+      const float d = b - a.hi;
+      y = d > 0.f ? ff_add(FF{b, 0.f}, FF{log1pf(expf(-d)), 0.f}) : ff_add(a, FF{log1pf(expf(d)), 0.f});
+    }
+    ll = ff_add(ll, ff_mul(FF{w.x, w.y}, y));
+  }
+  __device__ __forceinline__ void add_inv(const SweepParams &p, int part, size_t g, float t, int k) {
+    add_inv_w(p.weights32[g], t, k, p.gamma_frac32[part], p.inv_term32[g]);
+  }
   __device__ __forceinline__ void store(double *dst, int lane) {
     ll = warp_sum_ff(ll);
     bad = warp_sum(bad);
@@ -231,6 +267,25 @@ template <typename real>
 __device__ __forceinline__ real model_val(const double *d, const float *f, size_t i) {
   if constexpr (sizeof(real) == 4) return f[i];
   else return d[i];
+}
+
+// Adjoint seed factor of a displayed-tree root for site g: d log L_s / d
+// (rate-mixture term t in the root's scaled units) = 1 / t, or with invariant
+// sites gf / (gf t + it 2^(unit k)) (k: the root's scale counter).
+template <typename real>
+__device__ __forceinline__ real root_seed_factor(const SweepParams &p, int part, size_t g, real t, int k) {
+  if (!p.inv_term) return (real)1 / t;
+  real gf, it;
+  if constexpr (sizeof(real) == 4) {
+    gf = p.gamma_frac32[part];
+    it = p.inv_term32[g];
+  } else {
+    gf = p.gamma_frac[part];
+    it = p.inv_term[g];
+  }
+  real den = gf * t;
+  if (it > (real)0) den += Scale<real>::shift(it, k);
+  return gf / den;
 }
 
 // A pattern's weight as the sweep's arithmetic type.

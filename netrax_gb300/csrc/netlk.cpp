@@ -84,6 +84,7 @@ struct PartInfo {
   int unit_begin = 0, unit_end = 0;
   std::vector<double> freqs, exch, rates, rate_weights;
   double alpha = 1.0;
+  double pinv = 0.0;  // proportion of invariant sites (+I)
   bool explicit_rates = false;
   Eigen eig;
 };
@@ -163,6 +164,11 @@ struct netlk_ctx {
   DevBuf d_pmat64, d_pmat32, d_lambda, d_U, d_Uinv, d_rates, d_rw, d_freqs, d_Q, d_brlen;
   // FP32 contexts: float copies the sweeps read (weights as hi/lo pairs)
   DevBuf d_weights32, d_model32, d_seeds32;
+  // invariant sites (+I): per partition 1 - pinv, per pattern pinv * pi of its
+  // invariant state (0 if it has none); used only while has_pinv
+  DevBuf d_gfrac, d_gfrac32, d_invt, d_invt32;
+  std::vector<int8_t> inv_state;  // [N] the one state every tip admits, or -1
+  bool has_pinv = false;
   size_t m32_freqs = 0, m32_rw = 0, m32_rates = 0;  // offsets (floats) in d_model32; Q at 0
   DevBuf d_site_partial, d_tree_logl, d_root_slot, d_root_lp, d_root_dlp, d_seeds, d_wts, d_dret;
   DevBuf d_slot_begin, d_slot_roots, d_parts, d_out, d_grad_partial, d_grad, d_edge_begin, d_edge_entries, d_op_sum;
@@ -219,7 +225,8 @@ struct netlk_ctx {
                       &d_seeds, &d_wts, &d_dret, &d_slot_begin, &d_slot_roots, &d_parts, &d_out, &d_grad_partial, &d_grad,
                       &d_edge_begin, &d_edge_entries, &d_op_sum, &d_weights32, &d_model32, &d_seeds32,
                       &d_wfwd, &d_wrfwd, &d_wbwd, &d_wmsg_slots, &d_tan, &d_tan_ops, &d_tan_partial, &d_tan_out,
-                      &d_pderiv64, &d_pderiv32, &d_block_part, &d_part_block_begin, &d_tan_slots})
+                      &d_pderiv64, &d_pderiv32, &d_block_part, &d_part_block_begin, &d_tan_slots, &d_gfrac,
+                      &d_gfrac32, &d_invt, &d_invt32})
       b->free();
     if (stream) cudaStreamDestroy(stream);
   }
@@ -261,6 +268,12 @@ struct netlk_ctx {
     p.seeds = d_seeds.as<double>();
     p.grad_partial = d_grad_partial.as<double>();
     p.fault = reinterpret_cast<int32_t *>(d_out.as<double>() + 2 + P + topo.n_ret);
+    if (has_pinv) {
+      p.gamma_frac = d_gfrac.as<double>();
+      p.gamma_frac32 = d_gfrac32.as<float>();
+      p.inv_term = d_invt.as<double>();
+      p.inv_term32 = d_invt32.as<float>();
+    }
     if (walk_ok) {
       p.walk_fwd_ops = d_wfwd.as<FwdOp>();
       p.n_walk_fwd = (int32_t)wfwd.size();
@@ -762,6 +775,20 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
     }
     for (int u = (int)(pi.offset / ppw); u < (int)((pi.offset + pi.n_pad) / ppw); ++u) unit_part[u] = p;
   }
+  // invariant states: the AND of every tip's mask at a pattern, when it is one state
+  inv_state.assign(N, -1);
+  for (int p = 0; p < P; ++p) {
+    const PartInfo &pi = parts[p];
+    for (int s = 0; s < pi.n; ++s) {
+      uint32_t common = all_states;
+      for (int t = 0; t < topo.n_tips; ++t) common &= in[p].tip_states[(size_t)t * pi.n + s];
+      if (common && !(common & (common - 1))) {
+        int k = 0;
+        while (!((common >> k) & 1u)) ++k;
+        inv_state[pi.offset + s] = (int8_t)k;
+      }
+    }
+  }
   const size_t real_sz = opts.precision == NETLK_FP32 ? 4 : 8;
   const size_t clv_per_var = (size_t)N * R * S * real_sz;
   (void)V;
@@ -789,6 +816,10 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
   d_U.alloc(P * S * S * 8, dev_bytes);
   d_Uinv.alloc(P * S * S * 8, dev_bytes);
   d_rates.alloc(P * R * 8, dev_bytes);
+  d_gfrac.alloc(P * 8, dev_bytes);
+  d_gfrac32.alloc(P * 4, dev_bytes);
+  d_invt.alloc(N * 8, dev_bytes);
+  d_invt32.alloc(N * 4, dev_bytes);
   d_rw.alloc(P * R * 8, dev_bytes);
   d_freqs.alloc(P * S * 8, dev_bytes);
   d_Q.alloc(P * S * S * 8, dev_bytes);
@@ -888,7 +919,9 @@ void netlk_ctx::upload_model() {
     std::copy(pi.eig.U.begin(), pi.eig.U.end(), U.begin() + p * S * S);
     std::copy(pi.eig.Uinv.begin(), pi.eig.Uinv.end(), Ui.begin() + p * S * S);
     std::copy(pi.eig.Q.begin(), pi.eig.Q.end(), Q.begin() + p * S * S);
-    std::copy(pi.rates.begin(), pi.rates.end(), rates.begin() + p * R);
+    // with invariant sites the rate categories carry 1 - pinv of the sites:
+    // rates / (1 - pinv) keep the mean substitution rate at 1
+    for (int k = 0; k < R; ++k) rates[p * R + k] = pi.rates[k] / (1.0 - pi.pinv);
     std::copy(pi.rate_weights.begin(), pi.rate_weights.end(), rw.begin() + p * R);
     std::copy(pi.freqs.begin(), pi.freqs.end(), fr.begin() + p * S);
   }
@@ -899,6 +932,29 @@ void netlk_ctx::upload_model() {
   CUDA_OK(cudaMemcpyAsync(d_rw.p, rw.data(), rw.size() * 8, cudaMemcpyHostToDevice, stream));
   CUDA_OK(cudaMemcpyAsync(d_freqs.p, fr.data(), fr.size() * 8, cudaMemcpyHostToDevice, stream));
   CUDA_OK(cudaMemcpyAsync(d_Q.p, Q.data(), Q.size() * 8, cudaMemcpyHostToDevice, stream));
+  has_pinv = false;
+  for (const PartInfo &pi : parts) has_pinv = has_pinv || pi.pinv > 0.0;
+  if (has_pinv) {
+    std::vector<double> gf(P), it(N, 0.0);
+    std::vector<float> gf32(P), it32(N, 0.f);
+    for (int p = 0; p < P; ++p) {
+      const PartInfo &pi = parts[p];
+      gf[p] = 1.0 - pi.pinv;
+      gf32[p] = (float)gf[p];
+      for (int s = 0; s < pi.n; ++s) {
+        const int k = inv_state[pi.offset + s];
+        if (k >= 0 && pi.pinv > 0.0) {
+          it[pi.offset + s] = pi.pinv * pi.freqs[k];
+          it32[pi.offset + s] = (float)it[pi.offset + s];
+        }
+      }
+    }
+    CUDA_OK(cudaMemcpyAsync(d_gfrac.p, gf.data(), P * 8, cudaMemcpyHostToDevice, stream));
+    CUDA_OK(cudaMemcpyAsync(d_gfrac32.p, gf32.data(), P * 4, cudaMemcpyHostToDevice, stream));
+    CUDA_OK(cudaMemcpyAsync(d_invt.p, it.data(), N * 8, cudaMemcpyHostToDevice, stream));
+    CUDA_OK(cudaMemcpyAsync(d_invt32.p, it32.data(), N * 4, cudaMemcpyHostToDevice, stream));
+    CUDA_OK(cudaStreamSynchronize(stream));  // the host vectors go out of scope
+  }
   std::vector<float> m32;
   if (opts.precision == NETLK_FP32) {
     m32.assign(d_model32.bytes / 4, 0.f);
@@ -1280,6 +1336,8 @@ bool netlk_ctx::edge_derivs_analytic(int e, int mode, double *d1, double *d2) {
     tp.weights = d_weights.as<double>();
     tp.freqs = d_freqs.as<double>();
     tp.rate_weights = d_rw.as<double>();
+    tp.gamma_frac = has_pinv ? d_gfrac.as<double>() : nullptr;
+    tp.inv_term = has_pinv ? d_invt.as<double>() : nullptr;
     tp.partial = d_tan_partial.as<double>();
     if (!launch_tangent(stream, opts.precision, R, S, tp, lb.data(), dag.n_levels)) return false;
     launch_tangent_reduce(stream, tp, d_tan_slots.as<int32_t>(), (int)dslots.size(),
@@ -1620,6 +1678,9 @@ int netlk_create(const netlk_topology *topo, const netlk_partition *in_parts, in
       pi.freqs.assign(ip.freqs, ip.freqs + c->S);
       pi.exch.assign(ip.exchangeabilities, ip.exchangeabilities + c->S * (c->S - 1) / 2);
       pi.alpha = ip.alpha;
+      if (!(ip.prop_invar >= 0.0 && ip.prop_invar <= 0.99))
+        throw Error(NETLK_ERR_INVALID_ARGUMENT, "prop_invar must lie in [0, 0.99]");
+      pi.pinv = ip.prop_invar;
       pi.explicit_rates = ip.rates != nullptr;
       if (ip.rates) {
         pi.rates.assign(ip.rates, ip.rates + c->R);
@@ -1848,6 +1909,17 @@ int netlk_set_model(netlk_ctx *ctx, int32_t part, const double *freqs, const dou
     pi.alpha = alpha;
     pi.explicit_rates = rates != nullptr;
     if (rates) pi.rates.assign(rates, rates + ctx->R);
+    ctx->model_dirty = true;
+  });
+}
+
+int netlk_set_prop_invar(netlk_ctx *ctx, int32_t part, double prop_invar) {
+  if (!ctx) return NETLK_ERR_INVALID_ARGUMENT;
+  return guarded(ctx, [&] {
+    if (part < 0 || part >= ctx->P) throw Error(NETLK_ERR_INVALID_ARGUMENT, "partition");
+    if (!(prop_invar >= 0.0 && prop_invar <= 0.99))
+      throw Error(NETLK_ERR_INVALID_ARGUMENT, "prop_invar must lie in [0, 0.99]");
+    ctx->parts[part].pinv = prop_invar;
     ctx->model_dirty = true;
   });
 }

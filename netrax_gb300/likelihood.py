@@ -82,6 +82,7 @@ class NetworkLikelihood:
             r = None if rates is None else rates[i]
             p.rates = _ptr(arr(r, np.float64), ctypes.c_double) if r is not None else None
             p.rate_weights = None
+            p.prop_invar = float(getattr(pd, "prop_invar", 0.0))
         opts = N.Options()
         L.netlk_options_default(ctypes.byref(opts))
         opts.variant = VARIANTS[variant]
@@ -151,6 +152,10 @@ class NetworkLikelihood:
         r = None if rates is None else np.ascontiguousarray(rates, np.float64)
         N.check(N.lib().netlk_set_model(self._h, part, _ptr(f, ctypes.c_double), _ptr(x, ctypes.c_double),
                                         float(alpha), _ptr(r, ctypes.c_double)), self._h)
+
+    def set_prop_invar(self, part, prop_invar):
+        """Proportion of invariant sites (+I) of one partition."""
+        N.check(N.lib().netlk_set_prop_invar(self._h, int(part), float(prop_invar)), self._h)
 
     # ---------------------------------------------------------- evaluation
     def loglikelihood(self, details=False):

@@ -39,6 +39,7 @@ class PartitionData:
     n_sites: int
     rate_cats: int = 4
     states: int = 4
+    prop_invar: float = 0.0      # proportion of invariant sites (+I)
 
     @property
     def n_patterns(self):
