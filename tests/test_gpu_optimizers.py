@@ -133,30 +133,40 @@ def test_brent_reticulation_loop_matches_the_oracle(name, variant):
 
 @pytest.mark.parametrize("name,exch", [("twoReticulations", True), ("synthetic_12taxa_3ret_2parts", False)])
 def test_model_optimizer_callbacks_match_the_oracle(name, exch):
-    from oracle import improved, pllmath
+    """The model optimizer's searches (Gamma shape, exchangeabilities) on the
+    oracle, every model they evaluate recorded: the library's logL at each of
+    those models equals the oracle's (FP64 1e-9, FP32 1e-6), and the same
+    searches on the library end at the oracle's optimum within the searches'
+    own tolerance (Brent can take a different path when values differ in the
+    last bits: logL 1e-6 relative, parameters 5 %)."""
+    from oracle import pllmath
     orc = _oracle(name, "AVERAGE")
     start = [(p.freqs, p.exch, GoldenPartition(d).alpha) for p, d in zip(orc.parts, CASES[name]["partitions"])]
+    seen = []
 
     def orc_logl(models):
         for part, (f, x, a) in zip(orc.parts, models):
             part.exch = np.asarray(x, float)
             part.rates = pllmath.gamma_rates_mean(a, part.R)
             part.lam, part.U, part.Uinv, part.Q = pllmath.eigensystem(part.exch, part.freqs)
-        return orc.loglikelihood()
+        v = orc.loglikelihood()
+        seen.append(([(f, x.copy(), a) for f, x, a in models], v))
+        return v
 
     want_models, want_logl = opt.optimize_model(orc_logl, start, exchangeabilities=exch)
-    for precision, rel_logl, rel_par in (("fp64", 1e-9, 1e-4), ("fp32", 1e-6, 1e-2)):
+    for precision, rel_logl in (("fp64", 1e-9), ("fp32", 1e-6)):
         with _lik(name, "AVERAGE", precision) as lik:
-            start_logl = lik.loglikelihood()
-
             def logl_at(models):
                 for p, (f, x, a) in enumerate(models):
                     lik.set_model(p, f, x, a)
                 return lik.loglikelihood()
 
+            for models, v in seen[::max(1, len(seen) // 40)]:
+                assert logl_at(models) == pytest.approx(v, rel=rel_logl)
+            start_logl = logl_at(start)
             models, logl = opt.optimize_model(logl_at, start, exchangeabilities=exch)
             assert logl >= start_logl
-            assert logl == pytest.approx(want_logl, rel=rel_logl)
+            assert logl == pytest.approx(want_logl, rel=1e-6)
             for (f, x, a), (wf, wx, wa) in zip(models, want_models):
-                assert a == pytest.approx(wa, rel=rel_par)
-                assert np.allclose(x, wx, rtol=rel_par)
+                assert a == pytest.approx(wa, rel=5e-2)
+                assert np.allclose(x, wx, rtol=5e-2)
