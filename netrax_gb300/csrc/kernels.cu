@@ -529,8 +529,8 @@ __device__ __forceinline__ void backward_op(const SweepParams &p, const BwdOp &o
         t = rate_sum<R>(t);
         const real sw = sd * pattern_weight<real>(p, gg + (size_t)k * PPW);
         if (t > (real)0 && sw != (real)0) {
-          const real f = p.inv_term ? sw * rw * root_seed_factor<real>(p, part, gg + (size_t)k * PPW, t, sx[k])
-                                    : sw * rw / t;
+          const real e = p.inv_term ? root_inv_term<real>(p, gg + (size_t)k * PPW, sx[k]) : (real)0;
+          const real f = sw * rw / (t + e);
 #pragma unroll
           for (int i = 0; i < 4; ++i) ax[k][i] += f * sF[i];
         }

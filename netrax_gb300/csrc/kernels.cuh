@@ -75,8 +75,9 @@ struct SweepParams {
   const float *Q32;             // [n_parts][S*S]
   const float *seeds32;         // [n_slots][n_parts]
   // invariant sites (+I): null when no partition has any; else the site
-  // likelihood at a displayed-tree root is gamma_frac[part] * (rate mixture)
-  // + inv_term[pattern] (pinv * pi of the invariant state, 0 if none)
+  // likelihood at a displayed-tree root is
+  // gamma_frac[part] * (rate mixture + inv_term[pattern]), inv_term =
+  // pinv * pi(invariant state) / (1 - pinv), 0 for a pattern without one
   const double *gamma_frac;     // [n_parts] 1 - pinv
   const float *gamma_frac32;
   const double *inv_term;       // [N]
@@ -225,8 +226,7 @@ struct TanParams {
   const double *weights;        // [N]
   const double *freqs;          // [n_parts][S]
   const double *rate_weights;   // [n_parts][R]
-  const double *gamma_frac;     // invariant sites (+I), as in SweepParams; null without
-  const double *inv_term;
+  const double *inv_term;       // invariant sites (+I), as in SweepParams; null without
   double *partial;              // [n_slots][2][n_blocks] sums of w L'/L and w (L''/L - (L'/L)^2)
 };
 

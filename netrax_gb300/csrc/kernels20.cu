@@ -292,9 +292,8 @@ __global__ void __launch_bounds__(kWarps20 * 32) backward20_kernel(const SweepPa
       const real sw = model_val<real>(p.seeds, p.seeds32, (size_t)op.seed * p.n_parts + part) *
                       pattern_weight<real>(p, g);
       if (t > (real)0 && sw != (real)0) {
-        const real f = p.inv_term
-                           ? sw * rw * root_seed_factor<real>(p, part, g, t, p.scaler[(size_t)op.x * N + g])
-                           : sw * rw / t;
+        const real e = p.inv_term ? root_inv_term<real>(p, g, p.scaler[(size_t)op.x * N + g]) : (real)0;
+        const real f = sw * rw / (t + e);
 #pragma unroll
         for (int i = 0; i < S20; ++i) ax[i] += f * sF[i];
       }

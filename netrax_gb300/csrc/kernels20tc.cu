@@ -644,11 +644,8 @@ __global__ void __launch_bounds__(kTThreads, 1)
         }
       }
       if (op.seed >= 0 && tseed > 0.f && sw != 0.f) {
-        const float f =
-            p.inv_term32
-                ? sw * p.rate_weights32[part * 4 + r] *
-                      root_seed_factor<float>(p, part, g, tseed, p.scaler[(size_t)op.x * N + g])
-                : sw * p.rate_weights32[part * 4 + r] / tseed;
+        const float e = p.inv_term32 ? root_inv_term<float>(p, g, p.scaler[(size_t)op.x * N + g]) : 0.f;
+        const float f = sw * p.rate_weights32[part * 4 + r] / (tseed + e);
 #pragma unroll
         for (int i = 0; i < 20; ++i) ax[i] += f * p.freqs32[part * 20 + i];
       }

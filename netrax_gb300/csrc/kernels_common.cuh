@@ -192,17 +192,17 @@ struct SiteSum<double> {
     const double w = p.weights[g];
     if (w != 0.0) ll += w * (log(t) + (double)k * Scale<double>::kLogUnit);
   }
-  // with invariant sites: w log(gf t 2^(-256 k) + it)
+  // with invariant sites: w log(gf (t 2^(-256 k) + iq))
   __device__ __forceinline__ void add_inv(const SweepParams &p, int part, size_t g, double t, int k) {
     const double w = p.weights[g];
     if (w == 0.0) return;
-    double a = log(p.gamma_frac[part] * t) + (double)k * Scale<double>::kLogUnit;
-    const double it = p.inv_term[g];
-    if (it > 0.0) {
-      const double b = log(it);
+    double a = log(t) + (double)k * Scale<double>::kLogUnit;
+    const double iq = p.inv_term[g];
+    if (iq > 0.0) {
+      const double b = log(iq);
       a = a > b ? a + log1p(exp(b - a)) : b + log1p(exp(a - b));
     }
-    ll += w * a;
+    ll += w * (a + log(p.gamma_frac[part]));
   }
   __device__ __forceinline__ void store(double *dst, int lane) {
     ll = warp_sum(ll);
@@ -230,16 +230,18 @@ struct SiteSum<float> {
     const FF y = ff_add(ku, FF{lt, 0.f});
     ll = ff_add(ll, ff_mul(FF{w.x, w.y}, y));
   }
-  // with invariant sites: w log(gf t 2^(-k) + it), gf and it given
-  __device__ __forceinline__ void add_inv_w(float2 w, float t, int k, float gf, float it) {
+  // with invariant sites: w log(gf (t 2^(-k) + iq)), gf and iq given
+  __device__ __forceinline__ void add_inv_w(float2 w, float t, int k, float gf, float iq) {
     if (w.x == 0.f) return;
-    if (!(it > 0.f)) {
-      add_w(w, gf * t, k);
+    const float lt = logf(t);
+    const float lg = logf(gf);
+    FF y;
+    if (!(iq > 0.f)) {
+      add_w(w, t, k);
+      if (isfinite(lt)) ll = ff_add(ll, ff_mul(FF{w.x, w.y}, FF{lg, 0.f}));
       return;
     }
-    const float lt = logf(gf * t);
-    const float b = logf(it);
-    FF y;
+    const float b = logf(iq);
     if (!isfinite(lt)) {
       y = FF{b, 0.f};
     } else {
@@ -249,7 +251,7 @@ struct SiteSum<float> {
       const float d = b - a.hi;
       y = d > 0.f ? ff_add(FF{b, 0.f}, FF{log1pf(expf(-d)), 0.f}) : ff_add(a, FF{log1pf(expf(d)), 0.f});
     }
-    ll = ff_add(ll, ff_mul(FF{w.x, w.y}, y));
+    ll = ff_add(ll, ff_mul(FF{w.x, w.y}, ff_add(y, FF{lg, 0.f})));
   }
   __device__ __forceinline__ void add_inv(const SweepParams &p, int part, size_t g, float t, int k) {
     add_inv_w(p.weights32[g], t, k, p.gamma_frac32[part], p.inv_term32[g]);
@@ -269,23 +271,15 @@ __device__ __forceinline__ real model_val(const double *d, const float *f, size_
   else return d[i];
 }
 
-// Adjoint seed factor of a displayed-tree root for site g: d log L_s / d
-// (rate-mixture term t in the root's scaled units) = 1 / t, or with invariant
-// sites gf / (gf t + it 2^(unit k)) (k: the root's scale counter).
+// With invariant sites, the invariant term of site g in the scaled units of
+// a root CLV with scale counter k (0 without +I): the adjoint seed of a
+// displayed-tree root is w rw pi / (t + root_inv_term), t its rate mixture.
 template <typename real>
-__device__ __forceinline__ real root_seed_factor(const SweepParams &p, int part, size_t g, real t, int k) {
-  if (!p.inv_term) return (real)1 / t;
-  real gf, it;
-  if constexpr (sizeof(real) == 4) {
-    gf = p.gamma_frac32[part];
-    it = p.inv_term32[g];
-  } else {
-    gf = p.gamma_frac[part];
-    it = p.inv_term[g];
-  }
-  real den = gf * t;
-  if (it > (real)0) den += Scale<real>::shift(it, k);
-  return gf / den;
+__device__ __forceinline__ real root_inv_term(const SweepParams &p, size_t g, int k) {
+  real iq;
+  if constexpr (sizeof(real) == 4) iq = p.inv_term32[g];
+  else iq = p.inv_term[g];
+  return iq > (real)0 ? Scale<real>::shift(iq, k) : (real)0;
 }
 
 // A pattern's weight as the sweep's arithmetic type.

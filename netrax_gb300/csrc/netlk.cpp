@@ -165,7 +165,7 @@ struct netlk_ctx {
   // FP32 contexts: float copies the sweeps read (weights as hi/lo pairs)
   DevBuf d_weights32, d_model32, d_seeds32;
   // invariant sites (+I): per partition 1 - pinv, per pattern pinv * pi of its
-  // invariant state (0 if it has none); used only while has_pinv
+  // invariant state / (1 - pinv) (0 if it has none); used only while has_pinv
   DevBuf d_gfrac, d_gfrac32, d_invt, d_invt32;
   std::vector<int8_t> inv_state;  // [N] the one state every tip admits, or -1
   bool has_pinv = false;
@@ -943,8 +943,8 @@ void netlk_ctx::upload_model() {
       gf32[p] = (float)gf[p];
       for (int s = 0; s < pi.n; ++s) {
         const int k = inv_state[pi.offset + s];
-        if (k >= 0 && pi.pinv > 0.0) {
-          it[pi.offset + s] = pi.pinv * pi.freqs[k];
+        if (k >= 0 && pi.pinv > 0.0) {  // relative to the rate mixture's weight 1 - pinv
+          it[pi.offset + s] = pi.pinv * pi.freqs[k] / (1.0 - pi.pinv);
           it32[pi.offset + s] = (float)it[pi.offset + s];
         }
       }
@@ -1336,7 +1336,6 @@ bool netlk_ctx::edge_derivs_analytic(int e, int mode, double *d1, double *d2) {
     tp.weights = d_weights.as<double>();
     tp.freqs = d_freqs.as<double>();
     tp.rate_weights = d_rw.as<double>();
-    tp.gamma_frac = has_pinv ? d_gfrac.as<double>() : nullptr;
     tp.inv_term = has_pinv ? d_invt.as<double>() : nullptr;
     tp.partial = d_tan_partial.as<double>();
     if (!launch_tangent(stream, opts.precision, R, S, tp, lb.data(), dag.n_levels)) return false;

@@ -232,13 +232,9 @@ __global__ void __launch_bounds__(256) tangent_kernel(const TanParams p, int op_
     if (r == 0) {
       const double w = __ldg(p.weights + s);
       if (w != 0.0) {
-        if (p.inv_term) {  // invariant sites: L = gf L_mix + it (in the root's scaled units)
-          const real gf = (real)p.gamma_frac[part];
-          const real it = (real)p.inv_term[s];
-          L *= gf;
-          L1 *= gf;
-          L2 *= gf;
-          if (it > (real)0) L += ScaleShift<real>::apply(it, __ldg(p.scaler + (size_t)op.x * p.n_patterns + s));
+        if (p.inv_term) {  // invariant sites: L = gf (L_mix + iq), gf cancels in the ratios
+          const real iq = (real)p.inv_term[s];
+          if (iq > (real)0) L += ScaleShift<real>::apply(iq, __ldg(p.scaler + (size_t)op.x * p.n_patterns + s));
         }
         const real q1 = L1 / L, q2 = L2 / L;
         a1 += w * (double)q1;
