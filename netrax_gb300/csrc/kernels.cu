@@ -709,11 +709,13 @@ __global__ void __launch_bounds__(THREADS, MINB) backward_walk_kernel(const Swee
 // ------------------------------------------------------------- P-matrices
 // P(t r) = U diag(exp(lambda r t)) U^-1 in FP64; a zero length gives the
 // identity. One thread per entry of pmat[part][edge][rate][S][S].
+// len_stride: 0 when every partition shares the lengths brlen[e] (linked),
+// n_edges when partition p has its own, brlen[p * n_edges + e].
 __device__ __forceinline__ void pmatrix_entry(int64_t idx, int n_parts, int n_edges, int R, int S,
                                               const double *__restrict__ lambda, const double *__restrict__ U,
                                               const double *__restrict__ Uinv, const double *__restrict__ rates,
                                               const double *__restrict__ brlen, double *__restrict__ pmat64,
-                                              float *__restrict__ pmat32) {
+                                              float *__restrict__ pmat32, int len_stride = 0) {
   const int SS = S * S;
   const int64_t total = (int64_t)n_parts * n_edges * R * SS;
   if (idx >= total) return;
@@ -723,9 +725,10 @@ __device__ __forceinline__ void pmatrix_entry(int64_t idx, int n_parts, int n_ed
   const int rr = (int)(q % R);
   const int e = (int)(q / R % n_edges);
   const int part = (int)(q / R / n_edges);
-  const double t = brlen[e] * rates[part * R + rr];
+  const double len = brlen[(size_t)part * len_stride + e];
+  const double t = len * rates[part * R + rr];
   double v;
-  if (brlen[e] == 0.0) {
+  if (len == 0.0) {
     v = (i == j) ? 1.0 : 0.0;
   } else {
     v = 0.0;
@@ -739,9 +742,9 @@ __device__ __forceinline__ void pmatrix_entry(int64_t idx, int n_parts, int n_ed
 __global__ void pmatrix_kernel(int n_parts, int n_edges, int R, int S, const double *__restrict__ lambda,
                                const double *__restrict__ U, const double *__restrict__ Uinv,
                                const double *__restrict__ rates, const double *__restrict__ brlen,
-                               double *__restrict__ pmat64, float *__restrict__ pmat32) {
+                               double *__restrict__ pmat64, float *__restrict__ pmat32, int len_stride) {
   pmatrix_entry((int64_t)blockIdx.x * blockDim.x + threadIdx.x, n_parts, n_edges, R, S, lambda, U, Uinv, rates,
-                brlen, pmat64, pmat32);
+                brlen, pmat64, pmat32, len_stride);
 }
 
 // ------------------------------------------ per-(tree, partition) site sums
@@ -1237,11 +1240,80 @@ void launch_backward(cudaStream_t s, int precision, int R, int shape, const Swee
 
 void launch_pmatrix(cudaStream_t s, int n_parts, int n_edges, int R, int S, const double *lambda, const double *U,
                     const double *Uinv, const double *rates, const double *brlen, double *pmat64,
-                    float *pmat32) {
+                    float *pmat32, int len_stride) {
   const int64_t total = (int64_t)n_parts * n_edges * R * S * S;
   pmatrix_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(n_parts, n_edges, R, S, lambda, U, Uinv, rates,
-                                                                 brlen, pmat64, pmat32);
+                                                                 brlen, pmat64, pmat32, len_stride);
   g_launches++;
+}
+
+// Per-partition gradient (for branch lengths that differ between partitions):
+// per adjoint op and partition, the edge terms of the partition's units
+// (base units [unit_begin, unit_end)) in a fixed order -> op_sum[op][part][2];
+// per edge and partition, the op sides that use the edge -> grad[part][edge].
+__global__ void op_reduce_part_kernel(int n_units, const double *__restrict__ partial,
+                                      const int32_t *__restrict__ part_unit_begin, int n_parts,
+                                      double *__restrict__ op_sum, int ff) {
+  const int op = blockIdx.x, part = blockIdx.y;
+  const int ub = part_unit_begin[part], ue = part_unit_begin[part + 1];
+  __shared__ double ra[128], rb[128];
+  const double2 *src = reinterpret_cast<const double2 *>(partial) + (size_t)op * n_units;
+  const float4 *src32 = reinterpret_cast<const float4 *>(src);
+  double a = 0.0, b = 0.0;
+  if (ff) {
+    FF fa{0.f, 0.f}, fb{0.f, 0.f};
+    for (int i = ub + threadIdx.x; i < ue; i += blockDim.x) {
+      const float4 v = src32[i];
+      fa = ff_add(fa, FF{v.x, v.y});
+      fb = ff_add(fb, FF{v.z, v.w});
+    }
+    a = ff_to_double(make_float2(fa.hi, fa.lo));
+    b = ff_to_double(make_float2(fb.hi, fb.lo));
+  } else {
+    for (int i = ub + threadIdx.x; i < ue; i += blockDim.x) {
+      const double2 v = src[i];
+      a += v.x;
+      b += v.y;
+    }
+  }
+  ra[threadIdx.x] = a;
+  rb[threadIdx.x] = b;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      ra[threadIdx.x] += ra[threadIdx.x + o];
+      rb[threadIdx.x] += rb[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    op_sum[((size_t)op * n_parts + part) * 2] = ra[0];
+    op_sum[((size_t)op * n_parts + part) * 2 + 1] = rb[0];
+  }
+}
+
+__global__ void edge_reduce_part_kernel(int n_edges, int n_parts, const int32_t *__restrict__ edge_begin,
+                                        const int32_t *__restrict__ edge_entries, const double *__restrict__ op_sum,
+                                        double *__restrict__ grad) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x, part = blockIdx.y;
+  if (e >= n_edges) return;
+  double s = 0.0;
+  for (int q = edge_begin[e]; q < edge_begin[e + 1]; ++q) {
+    const int entry = edge_entries[q];  // op * 2 + side
+    s += op_sum[((size_t)(entry >> 1) * n_parts + part) * 2 + (entry & 1)];
+  }
+  grad[(size_t)part * n_edges + e] = s;
+}
+
+void launch_grad_reduce_partitions(cudaStream_t s, int n_ops, int n_edges, int n_units, int n_parts,
+                                   const int32_t *part_unit_begin, const int32_t *edge_begin,
+                                   const int32_t *edge_entries, const double *partial, double *op_sum,
+                                   double *grad, bool ff) {
+  if (n_ops > 0) op_reduce_part_kernel<<<dim3(n_ops, n_parts), 128, 0, s>>>(n_units, partial, part_unit_begin,
+                                                                              n_parts, op_sum, ff ? 1 : 0);
+  edge_reduce_part_kernel<<<dim3((n_edges + 127) / 128, n_parts), 128, 0, s>>>(n_edges, n_parts, edge_begin,
+                                                                              edge_entries, op_sum, grad);
+  g_launches += 2;
 }
 
 void launch_tree_reduce(cudaStream_t s, const MixParams &m) {

@@ -121,9 +121,17 @@ struct MixParams {
   double *out;                    // [2 + n_parts + n_ret]: total, status, part logl, dret
 };
 
+// len_stride 0: brlen[e] for every partition; n_edges: brlen[part * n_edges + e].
 void launch_pmatrix(cudaStream_t s, int n_parts, int n_edges, int R, int S, const double *lambda,
                     const double *U, const double *Uinv, const double *rates, const double *brlen,
-                    double *pmat64, float *pmat32);
+                    double *pmat64, float *pmat32, int len_stride = 0);
+// The gradient per partition, grad [n_parts][n_edges], from the adjoint's
+// per-unit edge terms (part_unit_begin: [n_parts + 1] base units); op_sum
+// scratch [n_ops][n_parts][2].
+void launch_grad_reduce_partitions(cudaStream_t s, int n_ops, int n_edges, int n_units, int n_parts,
+                                   const int32_t *part_unit_begin, const int32_t *edge_begin,
+                                   const int32_t *edge_entries, const double *partial, double *op_sum,
+                                   double *grad, bool ff);
 // Sweep launch shapes (threads per block, minimum blocks per SM): shape 0 is
 // the default; num_shapes() > 1 where the autotuner has alternatives. Shapes
 // from num_level_shapes() on are walk shapes: the whole sweep in one launch
@@ -231,8 +239,10 @@ struct TanParams {
 };
 
 int tangent_patterns_per_block(int R);
+// at length brlen[part * len_stride + edge] for each partition
 void launch_pderiv(cudaStream_t s, int n_parts, int R, int S, const double *lambda, const double *U,
-                   const double *Uinv, const double *rates, double t, double *out64, float *out32);
+                   const double *Uinv, const double *rates, const double *brlen, int len_stride, int edge,
+                   double *out64, float *out32);
 // One launch per level of ops [level_begin[L], level_begin[L+1]); false for
 // an unsupported (R, S).
 bool launch_tangent(cudaStream_t s, int precision, int R, int S, const TanParams &p, const int32_t *level_begin,

@@ -25,11 +25,12 @@ namespace netlk {
 namespace {
 
 // dP/dt and d2P/dt2 of P(rho_r t) = U diag(exp(lambda rho_r t)) U^-1 for one
-// branch length t, every partition and rate: out [part][2][R][S][S].
+// edge, every partition (its length brlen[part * len_stride + edge]) and
+// rate: out [part][2][R][S][S].
 __global__ void pderiv_kernel(int n_parts, int R, int S, const double *__restrict__ lambda,
                               const double *__restrict__ U, const double *__restrict__ Uinv,
-                              const double *__restrict__ rates, double t, double *__restrict__ out64,
-                              float *__restrict__ out32) {
+                              const double *__restrict__ rates, const double *__restrict__ brlen, int len_stride,
+                              int edge, double *__restrict__ out64, float *__restrict__ out32) {
   const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int SS = S * S;
   const int64_t total = (int64_t)n_parts * 2 * R * SS;
@@ -41,6 +42,7 @@ __global__ void pderiv_kernel(int n_parts, int R, int S, const double *__restric
   const int order = (int)(q / R % 2);
   const int part = (int)(q / R / 2);
   const double rho = rates[part * R + rr];
+  const double t = brlen[(size_t)part * len_stride + edge];
   double v = 0.0;
   for (int k = 0; k < S; ++k) {
     const double lr = lambda[part * S + k] * rho;
@@ -328,10 +330,11 @@ bool dispatch_levels(cudaStream_t st, int R, int S, const TanParams &p, const in
 int tangent_patterns_per_block(int R) { return kTanPPT * 256 / R; }
 
 void launch_pderiv(cudaStream_t s, int n_parts, int R, int S, const double *lambda, const double *U,
-                   const double *Uinv, const double *rates, double t, double *out64, float *out32) {
+                   const double *Uinv, const double *rates, const double *brlen, int len_stride, int edge,
+                   double *out64, float *out32) {
   const int64_t total = (int64_t)n_parts * 2 * R * S * S;
-  pderiv_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(n_parts, R, S, lambda, U, Uinv, rates, t, out64,
-                                                                out32);
+  pderiv_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(n_parts, R, S, lambda, U, Uinv, rates, brlen,
+                                                                len_stride, edge, out64, out32);
   add_launches(1);
 }
 

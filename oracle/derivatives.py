@@ -60,9 +60,10 @@ from . import configsets as cs
 from .improved import AVERAGE
 
 
-def _displayed_tree(orc):
-    """The current configuration's displayed tree: (root, children) where
-    children[u] = [(child end node, merged length, [network edge ids])]."""
+def _displayed_tree(orc, brlen):
+    """The current configuration's displayed tree with lengths ``brlen``:
+    (root, children) where children[u] = [(child end node, merged length,
+    [network edge ids])]."""
     dead, dt = orc.collect_dead_nodes()
     children = {}
 
@@ -74,14 +75,14 @@ def _displayed_tree(orc):
         out = []
         for c in ch:
             e = orc.edge_to(u, c)
-            edges, length, v = [e], orc.brlen[e], c
+            edges, length, v = [e], brlen[e], c
             while v >= orc.net.n_tips:
                 nxt = orc._active_alive_children(v, dead)
                 if len(nxt) != 1:
                     break
                 e2 = orc.edge_to(v, nxt[0])
                 edges.append(e2)
-                length += orc.brlen[e2]
+                length += brlen[e2]
                 v = nxt[0]
             out.append((v, length, edges))
             build(v)
@@ -102,10 +103,11 @@ def _pmats(part, t):
     return np.stack([part.pmat(t)[r] for r in range(part.R)])
 
 
-def _tree_derivatives(orc, part, n_edges):
+def _tree_derivatives(orc, part, n_edges, brlen):
     """(logL_T, d1[e], d2[e]) of the current configuration's displayed tree
-    for one partition; d1, d2 are 0 for edges the tree does not contain."""
-    dt, children = _displayed_tree(orc)
+    for one partition with lengths ``brlen``; d1, d2 are 0 for edges the tree
+    does not contain."""
+    dt, children = _displayed_tree(orc, brlen)
     n = part.n
     down, dscale = {}, {}
 
@@ -184,7 +186,7 @@ class EdgeDerivativeOracle:
             rep = covered[0]
             for k in range(orc.r):
                 orc.toggle[k] = (rep >> k) & 1
-            per_part = [_tree_derivatives(orc, part, E) for part in orc.parts]
+            per_part = [_tree_derivatives(orc, part, E, orc.lengths(p)) for p, part in enumerate(orc.parts)]
             self.trees.append({
                 "logprob": t.logprob, "configs": covered,
                 "logl": np.array([x[0] for x in per_part]),
@@ -235,6 +237,22 @@ class EdgeDerivativeOracle:
                 D1 += float(best["d1"][p][e])
                 D2 += float(best["d2"][p][e])
         return D1, D2
+
+    def gradient_per_partition(self):
+        """d logL / d (partition p's length of edge e) [n_parts][n_edges]."""
+        trees = [t for t in self.trees if self._use(t)]
+        out = np.zeros((len(self.orc.parts), self.orc.net.n_edges))
+        for p in range(len(self.orc.parts)):
+            a = np.array([t["logprob"] + t["logl"][p] for t in trees])
+            if self.orc.variant == AVERAGE:
+                w = np.exp(a - a.max())
+                w /= w.sum()
+            else:
+                w = np.zeros(len(trees))
+                w[int(np.argmax(a))] = 1.0
+            for i, t in enumerate(trees):
+                out[p] += w[i] * t["d1"][p]
+        return out
 
     def gradient(self):
         """(d logL / d branch length [n_edges], d logL / d p_k [r]), exact."""

@@ -93,6 +93,9 @@ class ImprovedOracle:
         self.r = net.n_ret
         self.width = width if width is not None else max(1, net.n_ret)
         self.brlen = list(net.edge_length)
+        # per-partition lengths (the reference's unlinked / scaled linkage,
+        # fake_treeinfo->branch_lengths[p]); None: every partition uses brlen
+        self.part_brlen = None
         self.set_ret_probs(list(net.ret_first_prob))
         self.toggle = [0] * net.n_ret   # ReticulationData active_parent_toggle
         self.ret_index = {node: k for k, node in enumerate(net.ret_node)}
@@ -104,6 +107,10 @@ class ImprovedOracle:
         self.ret_probs = list(probs)
         self.first_lp = [math.log(p) for p in probs] + [0.0] * (self.width - len(probs))
         self.second_lp = [math.log(1.0 - p) for p in probs] + [0.0] * (self.width - len(probs))
+
+    def lengths(self, p):
+        """Branch lengths partition p uses."""
+        return self.brlen if self.part_brlen is None else self.part_brlen[p]
 
     # ------------------------------------------------------ network helpers
     def is_ret(self, v):
@@ -249,7 +256,7 @@ class ImprovedOracle:
             ps = np.zeros(part.n, dtype=np.uint32)
             lclv = part.tip_clv(lnode) if ltree.is_tip else ltree.clv[p]
             lsc = None if ltree.is_tip else ltree.scaler[p]
-            pl = part.pmat(self.brlen[le])
+            pl = part.pmat(self.lengths(p)[le])
             if rinfo is None:
                 cbuild.update_partial(parent, ps, lclv, lsc, pl, None, None, None)
             else:
@@ -258,7 +265,7 @@ class ImprovedOracle:
                 rclv = part.tip_clv(rnode) if rtree.is_tip else rtree.clv[p]
                 rsc = None if rtree.is_tip else rtree.scaler[p]
                 cbuild.update_partial(parent, ps, lclv, lsc, pl, rclv, rsc,
-                                      part.pmat(self.brlen[re]))
+                                      part.pmat(self.lengths(p)[re]))
             tree.clv.append(parent)
             tree.scaler.append(ps)
             self.update_count += part.n
@@ -428,7 +435,7 @@ class ImprovedOracle:
         pm = {}
         for p, part in enumerate(self.parts):
             for e in range(self.net.n_edges):
-                pm[(p, e)] = part.pmat(self.brlen[e])
+                pm[(p, e)] = part.pmat(self.lengths(p)[e])
         for v in self.travbuffer:
             for tree in self.pernode[v]:
                 if tree.is_tip or tree.children is None:

@@ -33,7 +33,7 @@ def _tree_logl(orc, part, p):
             if len(ch) != 1 or u < orc.net.n_tips:
                 return u, length
             c = ch[0]
-            length += orc.brlen[orc.edge_to(u, c)]
+            length += orc.lengths(p)[orc.edge_to(u, c)]
             u = c
 
     def clv_of(u):
@@ -43,7 +43,7 @@ def _tree_logl(orc, part, p):
         assert len(ch) == 2, "inner node of a displayed tree must be binary"
         ops = []
         for c in ch:
-            end, length = down(c, orc.brlen[orc.edge_to(u, c)])
+            end, length = down(c, orc.lengths(p)[orc.edge_to(u, c)])
             clv, sc = clv_of(end)
             ops.append((clv, sc, part.pmat(length)))
         parent = np.empty((part.n, part.R, part.S))

@@ -263,20 +263,20 @@ int oracle_sweep_forward(int32_t n_ops, const oracle_op *ops, int32_t n_parts, c
  * is reachable from a used displayed-tree root, parents before children,
  * with their `first` flags set. Every root slot's variant is seeded (stored,
  * not added) before the ops run; slot_weight [n_slots][n_parts] is each
- * slot's posterior weight in its partition's mixture. grad [n_edges]
- * receives d logL / d t_e. */
+ * slot's posterior weight in its partition's mixture. grad [n_parts][n_edges]
+ * receives d logL / d t_e per partition (the partition's own lengths). */
 int oracle_sweep_adjoint(int32_t n_ops, const oracle_op *bwd_ops, int32_t n_var, int32_t n_parts,
                          const oracle_part *parts, int32_t n_slots, const int32_t *slot_variant,
                          const double *slot_weight, int32_t n_edges, double *grad) {
   (void)n_var;
   const int T = n_threads();
-  double *partial = (double *)calloc((size_t)T * n_edges, sizeof(double));
+  double *partial = (double *)calloc((size_t)T * n_parts * n_edges, sizeof(double));
   if (!partial) return 1;
 #pragma omp parallel
   {
     const int t = thread_id();
-    double *g = partial + (size_t)t * n_edges;
     for (int p = 0; p < n_parts; ++p) {
+      double *g = partial + ((size_t)t * n_parts + p) * n_edges;
       const oracle_part *pp = &parts[p];
       const int R = pp->R, S = pp->S, RS = R * S;
       const int64_t lo = pp->n * t / T, hi = pp->n * (t + 1) / T;
@@ -309,11 +309,12 @@ int oracle_sweep_adjoint(int32_t n_ops, const oracle_op *bwd_ops, int32_t n_var,
       }
     }
   }
-  for (int e = 0; e < n_edges; ++e) {
-    double acc = 0.0;
-    for (int t = 0; t < T; ++t) acc += partial[(size_t)t * n_edges + e];
-    grad[e] = acc;
-  }
+  for (int p = 0; p < n_parts; ++p)
+    for (int e = 0; e < n_edges; ++e) {
+      double acc = 0.0;
+      for (int t = 0; t < T; ++t) acc += partial[((size_t)t * n_parts + p) * n_edges + e];
+      grad[(size_t)p * n_edges + e] = acc;
+    }
   free(partial);
   return 0;
 }

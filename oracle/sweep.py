@@ -149,14 +149,18 @@ class SweepOracle:
     def _pmats(self, brlen, grad):
         for p, part in enumerate(self.orc.parts):
             pm, dpm = self.keep[p]["pmat"], self.keep[p]["dpmat"]
-            for e, t in enumerate(brlen):
+            lengths = brlen if self.orc.part_brlen is None or brlen is not self.orc.brlen else self.orc.lengths(p)
+            for e, t in enumerate(lengths):
                 pm[e] = pllmath.pmatrices(part.lam, part.U, part.Uinv, t, part.rates)
                 if grad:
                     dpm[e] = pllmath.dpmatrices(part.lam, part.U, part.Uinv, t, part.rates)
 
     def evaluate(self, brlen=None, gradient=True):
         """(total, partition logL [P], per-tree logL [n_trees][P], d logL / d
-        branch length [n_edges] or None, d logL / d p_k [r] or None)."""
+        branch length [n_edges] or None, d logL / d p_k [r] or None). With
+        ``brlen`` None the oracle's own lengths (per partition where it has
+        them); the per-partition gradient of the last call is kept in
+        ``grad_per_partition`` [P][n_edges]."""
         orc = self.orc
         brlen = orc.brlen if brlen is None else brlen
         L = _lib()
@@ -184,11 +188,13 @@ class SweepOracle:
         slot_w = np.zeros((len(self.slots), P))
         for i, s in enumerate(self.tree_slot):
             slot_w[s] += w[i]
-        grad = np.empty(orc.net.n_edges)
+        gpp = np.empty((P, orc.net.n_edges))
         if L.oracle_sweep_adjoint(self.n_bwd, self.bwd, self.n_var, P, self.parts, len(self.slots),
                                   self.slots.ctypes.data, slot_w.ctypes.data, orc.net.n_edges,
-                                  grad.ctypes.data):
+                                  gpp.ctypes.data):
             raise MemoryError("oracle_sweep_adjoint")
+        self.grad_per_partition = gpp
+        grad = gpp.sum(axis=0)
         r = orc.r
         probs = orc.ret_probs
         gret = np.zeros(r)
