@@ -137,7 +137,21 @@ typedef struct {
                                         clv_valid flags, InvalidationHelper.cpp
                                         :52-237); 0: every call recomputes
                                         every CLV. Results are identical.     */
+  int32_t brlen_linkage;             /* NETLK_BRLEN_LINKED (default): one
+                                        length per edge for every partition;
+                                        NETLK_BRLEN_UNLINKED: each partition
+                                        has its own lengths
+                                        (netlk_set_partition_branch_lengths);
+                                        NETLK_BRLEN_SCALED: partition p uses
+                                        scaler[p] x the linked length
+                                        (netlk_set_branch_length_scalers). The
+                                        reference's --brlen linked / unlinked /
+                                        scaled (src/main.cpp:101,226-230).    */
 } netlk_options;
+
+#define NETLK_BRLEN_LINKED 0
+#define NETLK_BRLEN_UNLINKED 1
+#define NETLK_BRLEN_SCALED 2
 
 typedef struct {
   int32_t n_variants;        /* inner displayed-tree variants (DAG nodes)    */
@@ -286,6 +300,24 @@ int netlk_set_model(netlk_ctx *ctx, int32_t partition, const double *freqs,
                     const double *exchangeabilities, double alpha,
                     const double *rates);
 
+/* Per-partition branch lengths (NETLK_BRLEN_UNLINKED contexts): partition
+ * `partition`'s lengths [n_edges], clamped like every length. Replaces
+ * fake_treeinfo->branch_lengths[partition] (the reference's unlinked
+ * linkage, src/optimization/BranchLengthOptimization.cpp:174-185). On an
+ * unlinked context netlk_set_branch_lengths gives every partition the same
+ * lengths. */
+int netlk_set_partition_branch_lengths(netlk_ctx *ctx, int32_t partition, const double *branch_lengths,
+                                       int32_t n_edges);
+/* Per-partition length scalers (NETLK_BRLEN_SCALED contexts) [n_parts], each
+ * > 0: partition p's length of edge e is scalers[p] x the linked length
+ * (pllmod_treeinfo's brlen_scalers). */
+int netlk_set_branch_length_scalers(netlk_ctx *ctx, const double *scalers, int32_t n_parts);
+/* d logL / d (partition p's length of edge e) [n_parts * n_edges] of the last
+ * logL + gradient evaluation (any linkage; on a linked context the rows add
+ * up to the gradient). On a scaled context d logL / d scaler[p] =
+ * sum_e linked_length[e] * row p [e]. */
+int netlk_partition_gradient(netlk_ctx *ctx, double *d_brlen_partition);
+
 /* Replace the proportion of invariant sites of one partition (libpll's
  * pll_update_invariant_sites_proportion, which raxml-ng's model code calls
  * for NetRAX's partitions, src/RaxmlWrapper.cpp:621-640; the model
@@ -320,6 +352,11 @@ int netlk_loglikelihood_gradient(netlk_ctx *ctx, double *total,
  * probes: with incremental evaluation on, only the variants above the edge
  * are recomputed. */
 int netlk_edge_loglikelihood(netlk_ctx *ctx, int32_t edge, double length, double *total);
+/* The same for one partition's length of the edge (NETLK_BRLEN_UNLINKED
+ * contexts): the reference's computeLoglikelihoodBrlenOpt with
+ * fake_treeinfo->branch_lengths[partition] changed. */
+int netlk_edge_loglikelihood_partition(netlk_ctx *ctx, int32_t edge, int32_t partition, double length,
+                                       double *total);
 /* Site-CLV updates the last evaluation computed in its forward sweep
  * (fewer than n_variants * patterns after an incremental evaluation). */
 int netlk_last_site_updates(const netlk_ctx *ctx, int64_t *site_updates);
@@ -336,6 +373,9 @@ int netlk_last_site_updates(const netlk_ctx *ctx, int64_t *site_updates);
  *   largest tree_logl * tree_prob. Trees are grouped by displayed tree at the
  *   network root (the reference groups by the virtually rerooted tree pairs
  *   at the edge).
+ * With unlinked lengths d1 / d2 are w.r.t. moving every partition's length
+ * of the edge together (the sum of the partition shares); with scaled
+ * lengths w.r.t. the linked length (sum of s_p x and s_p^2 x the shares).
  * Both derivatives are analytic: one forward-mode (tangent) sweep over the
  * variants above the edge gives every displayed tree's first and second
  * derivative, which are then mixed like the reference's sumtable derivatives
@@ -347,6 +387,14 @@ int netlk_last_site_updates(const netlk_ctx *ctx, int64_t *site_updates);
  * contexts h = max(t/200, min(1e-4, (t - 1e-6)/3)). */
 int netlk_edge_derivatives(netlk_ctx *ctx, int32_t edge, int32_t mode,
                            double *d1, double *d2);
+/* Partition `partition`'s share: the derivatives of that partition's logL
+ * w.r.t. its own length of the edge - the df[p] / ddf[p] the reference's
+ * Newton-Raphson callback returns for unlinked lengths
+ * (BranchLengthOptimization.cpp:189-195). On linked and scaled contexts the
+ * same per-partition terms (w.r.t. the partition's effective length). Needs
+ * one checkpoint segment and host lengths. */
+int netlk_edge_derivatives_partition(netlk_ctx *ctx, int32_t edge, int32_t partition, int32_t mode, double *d1,
+                                     double *d2);
 
 /* ------------------------------------------------- sharded (multi-rank) use */
 /* Per-(root variant, partition) log-likelihood partial sums over the patterns

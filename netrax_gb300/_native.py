@@ -40,8 +40,10 @@ EXPORTED = [
     "netlk_batch_loglikelihood_gradient", "netlk_batch_destroy", "netlk_edge_loglikelihood",
     "netlk_last_site_updates", "netlk_encode_states", "netlk_compress_patterns", "netlk_inject_failure",
     "netlk_walk_segments", "netlk_batch_create_ex", "netlk_batch_info",
-    "netlk_set_prop_invar",
+    "netlk_set_prop_invar", "netlk_set_partition_branch_lengths", "netlk_set_branch_length_scalers",
+    "netlk_partition_gradient", "netlk_edge_loglikelihood_partition", "netlk_edge_derivatives_partition",
 ]
+NETLK_BRLEN_LINKED, NETLK_BRLEN_UNLINKED, NETLK_BRLEN_SCALED = 0, 1, 2
 
 
 class Topology(ctypes.Structure):
@@ -67,7 +69,7 @@ class Options(ctypes.Structure):
                 ("device", ctypes.c_int32), ("use_cuda_graph", ctypes.c_int32),
                 ("host_only", ctypes.c_int32), ("autotune", ctypes.c_int32),
                 ("tensor_cores", ctypes.c_int32), ("checkpoint_segments", ctypes.c_int32),
-                ("incremental", ctypes.c_int32)]
+                ("incremental", ctypes.c_int32), ("brlen_linkage", ctypes.c_int32)]
 
 
 class DagStats(ctypes.Structure):
@@ -123,6 +125,13 @@ def lib():
     L.netlk_set_reticulation_probs.argtypes = [vp, c_double_p, ctypes.c_int32]
     L.netlk_set_model.argtypes = [vp, ctypes.c_int32, c_double_p, c_double_p, ctypes.c_double, c_double_p]
     L.netlk_set_prop_invar.argtypes = [vp, ctypes.c_int32, ctypes.c_double]
+    L.netlk_set_partition_branch_lengths.argtypes = [vp, ctypes.c_int32, c_double_p, ctypes.c_int32]
+    L.netlk_set_branch_length_scalers.argtypes = [vp, c_double_p, ctypes.c_int32]
+    L.netlk_partition_gradient.argtypes = [vp, c_double_p]
+    L.netlk_edge_loglikelihood_partition.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                                                     c_double_p]
+    L.netlk_edge_derivatives_partition.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                                   c_double_p, c_double_p]
     L.netlk_loglikelihood.argtypes = [vp, c_double_p, c_double_p, c_double_p]
     L.netlk_loglikelihood_gradient.argtypes = [vp, c_double_p, c_double_p, c_double_p, c_double_p]
     L.netlk_edge_derivatives.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, c_double_p, c_double_p]

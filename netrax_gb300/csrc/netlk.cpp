@@ -97,6 +97,18 @@ struct netlk_ctx {
   Topology topo;
   Dag dag;
   std::vector<double> brlen, ret_probs;
+  // branch-length linkage: unlinked and scaled contexts keep per-partition
+  // lengths plen [P][E] (what the device uses); linked ones use brlen for
+  // every partition
+  int linkage = NETLK_BRLEN_LINKED;
+  std::vector<double> plen, scalers;
+  int len_stride() const { return linkage == NETLK_BRLEN_LINKED ? 0 : topo.n_edges; }
+  const std::vector<double> &dev_len() const { return linkage == NETLK_BRLEN_LINKED ? brlen : plen; }
+  void refresh_scaled() {
+    const int E = topo.n_edges;
+    for (int p = 0; p < P; ++p)
+      for (int e = 0; e < E; ++e) plen[(size_t)p * E + e] = scalers[p] * brlen[e];
+  }
   std::vector<PartInfo> parts;
   int64_t N = 0;
   int n_units = 0, n_units_fwd = 0, ppw = 8;
@@ -162,6 +174,7 @@ struct netlk_ctx {
   int n_tan_cap = -1;  // tangent slot pairs allocated (-1: not set up yet)
   int tan_blocks = 0;
   DevBuf d_pmat64, d_pmat32, d_lambda, d_U, d_Uinv, d_rates, d_rw, d_freqs, d_Q, d_brlen;
+  DevBuf d_grad_part, d_op_sum_part, d_part_unit_begin;  // per-partition gradient (on request)
   // FP32 contexts: float copies the sweeps read (weights as hi/lo pairs)
   DevBuf d_weights32, d_model32, d_seeds32;
   // invariant sites (+I): per partition 1 - pinv, per pattern pinv * pi of its
@@ -226,7 +239,7 @@ struct netlk_ctx {
                       &d_edge_begin, &d_edge_entries, &d_op_sum, &d_weights32, &d_model32, &d_seeds32,
                       &d_wfwd, &d_wrfwd, &d_wbwd, &d_wmsg_slots, &d_tan, &d_tan_ops, &d_tan_partial, &d_tan_out,
                       &d_pderiv64, &d_pderiv32, &d_block_part, &d_part_block_begin, &d_tan_slots, &d_gfrac,
-                      &d_gfrac32, &d_invt, &d_invt32})
+                      &d_gfrac32, &d_invt, &d_invt32, &d_grad_part, &d_op_sum_part, &d_part_unit_begin})
       b->free();
     if (stream) cudaStreamDestroy(stream);
   }
@@ -332,9 +345,13 @@ struct netlk_ctx {
   // analytic d1 and d2 along edge e from a tangent sweep over the variants
   // above it; false where that path does not apply (several checkpoint
   // segments, device-resident lengths)
-  bool edge_derivs_analytic(int e, int mode, double *d1, double *d2);
+  // part >= 0: that partition's share only
+  bool edge_derivs_analytic(int e, int mode, double *d1, double *d2, int part = -1);
   int tangent_schedule(int e, std::vector<TanOp> &ops, std::vector<int32_t> &level_begin,
                        std::vector<int32_t> &slots) const;
+  // d logL / d (partition p's length of edge e) [P][E] from the last adjoint
+  // sweep's per-unit edge terms (two extra reductions)
+  void partition_gradient(double *out);
   // roots (displayed trees) on which edge e counts as active for the
   // reference's derivative formula
   std::vector<char> active_roots_of(int e) const;
@@ -823,7 +840,7 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
   d_rw.alloc(P * R * 8, dev_bytes);
   d_freqs.alloc(P * S * 8, dev_bytes);
   d_Q.alloc(P * S * S * 8, dev_bytes);
-  d_brlen.alloc(topo.n_edges * 8, dev_bytes);
+  d_brlen.alloc((size_t)topo.n_edges * (linkage == NETLK_BRLEN_LINKED ? 1 : P) * 8, dev_bytes);
   d_site_partial.alloc((size_t)n_slots * n_units_fwd * 8, dev_bytes);
   d_tree_logl.alloc((size_t)n_slots * P * 8, dev_bytes);
   d_root_slot.alloc(root_slot.size() * 4, dev_bytes);
@@ -900,7 +917,7 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
   CUDA_OK(cudaMemcpyAsync(d_parts.p, dparts.data(), P * sizeof(DevPartition), cudaMemcpyHostToDevice, stream));
   CUDA_OK(cudaStreamSynchronize(stream));  // host staging vectors go out of scope
 
-  h_brlen.alloc(topo.n_edges * 8);
+  h_brlen.alloc((size_t)topo.n_edges * (linkage == NETLK_BRLEN_LINKED ? 1 : P) * 8);
   h_root_lp.alloc(dag.roots.size() * 8);
   h_root_dlp.alloc(dag.roots.size() * std::max(1, topo.n_ret) * 8);
   h_out.alloc((3 + P + topo.n_ret) * 8);
@@ -1012,7 +1029,7 @@ void netlk_ctx::enqueue(bool pm, bool fwd_on, bool reduce, bool mixk, bool bwd_o
   if (pm) {
     launch_pmatrix(stream, P, topo.n_edges, R, S, d_lambda.as<double>(), d_U.as<double>(), d_Uinv.as<double>(),
                    d_rates.as<double>(), d_brlen.as<double>(), d_pmat64.as<double>(),
-                   opts.precision == NETLK_FP32 ? d_pmat32.as<float>() : nullptr);
+                   opts.precision == NETLK_FP32 ? d_pmat32.as<float>() : nullptr, len_stride());
     prof_mark(0);
   }
   const SweepParams sp = sweep();
@@ -1103,7 +1120,7 @@ void netlk_ctx::run(cudaGraphExec_t *cache, bool pm, bool fwd_on, bool reduce, b
                 (bwd_on && !bwd.empty() ? bwd_launches + rfwd_launches + 2 : 0);
   if (fwd_on && pm) {  // every CLV recomputed from the current lengths
     clv_valid = !device_brlen;
-    clv_brlen = brlen;
+    clv_brlen = dev_len();
     last_updates = site_updates;
   }
   if (!opts.use_cuda_graph || profiling) {
@@ -1128,7 +1145,12 @@ bool netlk_ctx::run_incremental() {
   if (!opts.incremental || !clv_valid || n_segments != 1 || device_brlen || profiling) return false;
   const int E = topo.n_edges;
   std::vector<char> dirty_edge(E, 0);
-  for (int e = 0; e < E; ++e) dirty_edge[e] = brlen[e] != clv_brlen[e];
+  {  // an edge is dirty when any partition's length of it changed
+    const std::vector<double> &L = dev_len();
+    const int np = linkage == NETLK_BRLEN_LINKED ? 1 : P;
+    for (int p = 0; p < np; ++p)
+      for (int e = 0; e < E; ++e) dirty_edge[e] |= L[(size_t)p * E + e] != clv_brlen[(size_t)p * E + e];
+  }
   // with one segment the CLV slots are the variant ids; fwd is in level order
   std::vector<char> dirty(dag.vars.size(), 0);
   ifwd.clear();
@@ -1152,7 +1174,7 @@ bool netlk_ctx::run_incremental() {
   if (use_tc) CUDA_OK(cudaMemsetAsync(sp.fault, 0, 8, stream));
   launch_pmatrix(stream, P, topo.n_edges, R, S, d_lambda.as<double>(), d_U.as<double>(), d_Uinv.as<double>(),
                  d_rates.as<double>(), d_brlen.as<double>(), d_pmat64.as<double>(),
-                 opts.precision == NETLK_FP32 ? d_pmat32.as<float>() : nullptr);
+                 opts.precision == NETLK_FP32 ? d_pmat32.as<float>() : nullptr, len_stride());
   if (!ifwd.empty()) {
     std::memcpy(h_ifwd.p, ifwd.data(), ifwd.size() * sizeof(FwdOp));
     CUDA_OK(cudaMemcpyAsync(d_ifwd.p, h_ifwd.p, ifwd.size() * sizeof(FwdOp), cudaMemcpyHostToDevice, stream));
@@ -1168,7 +1190,7 @@ bool netlk_ctx::run_incremental() {
   launch_tree_reduce(stream, mp);
   launch_mix(stream, mp);
   launches += 3 + n_launch;
-  clv_brlen = brlen;
+  clv_brlen = dev_len();
   last_updates = (int64_t)ifwd.size() * N;
   return true;
 }
@@ -1191,6 +1213,34 @@ std::vector<char> netlk_ctx::active_roots_of(int edge) const {
     act[i] = any;
   }
   return act;
+}
+
+void netlk_ctx::partition_gradient(double *out) {
+  prepare_state();
+  const int E = topo.n_edges;
+  if (bwd.empty()) {
+    std::fill(out, out + (size_t)P * E, 0.0);
+    return;
+  }
+  if (!d_part_unit_begin.p) {
+    std::vector<int32_t> pub(P + 1);
+    for (int p = 0; p < P; ++p) pub[p] = (int32_t)(parts[p].offset / ppw);
+    pub[P] = n_units;
+    int64_t scratch = 0;
+    d_part_unit_begin.alloc(pub.size() * 4, scratch);
+    d_op_sum_part.alloc(bwd.size() * P * 2 * 8, scratch);
+    d_grad_part.alloc((size_t)P * E * 8, scratch);
+    dev_bytes += scratch;
+    CUDA_OK(cudaMemcpy(d_part_unit_begin.p, pub.data(), pub.size() * 4, cudaMemcpyHostToDevice));
+  }
+  launch_grad_reduce_partitions(stream, (int)bwd.size(), E, n_units, P, d_part_unit_begin.as<int32_t>(),
+                                d_edge_begin.as<int32_t>(), d_edge_entries.as<int32_t>(),
+                                d_grad_partial.as<double>(), d_op_sum_part.as<double>(), d_grad_part.as<double>(),
+                                opts.precision == NETLK_FP32);
+  launches += 2;
+  CUDA_OK(cudaMemcpyAsync(out, d_grad_part.p, (size_t)P * E * 8, cudaMemcpyDeviceToHost, stream));
+  CUDA_OK(cudaStreamSynchronize(stream));
+  CUDA_OK(cudaGetLastError());
 }
 
 // Tangent schedule for edge e, level by level over the forward schedule (one
@@ -1261,7 +1311,7 @@ int netlk_ctx::tangent_schedule(int e, std::vector<TanOp> &ops, std::vector<int3
   return n_slots_used;
 }
 
-bool netlk_ctx::edge_derivs_analytic(int e, int mode, double *d1, double *d2) {
+bool netlk_ctx::edge_derivs_analytic(int e, int mode, double *d1, double *d2, int part) {
   if (n_segments != 1 || device_brlen) return false;
   prepare();
   const size_t real_b = opts.precision == NETLK_FP32 ? 4 : 8;
@@ -1319,7 +1369,8 @@ bool netlk_ctx::edge_derivs_analytic(int e, int mode, double *d1, double *d2) {
     if (!dslots.empty())
       CUDA_OK(cudaMemcpyAsync(d_tan_slots.p, h_tan_slots.p, dslots.size() * 4, cudaMemcpyHostToDevice, stream));
     launch_pderiv(stream, P, R, S, d_lambda.as<double>(), d_U.as<double>(), d_Uinv.as<double>(), d_rates.as<double>(),
-                  brlen[e], d_pderiv64.as<double>(), opts.precision == NETLK_FP32 ? d_pderiv32.as<float>() : nullptr);
+                  d_brlen.as<double>(), len_stride(), e, d_pderiv64.as<double>(),
+                  opts.precision == NETLK_FP32 ? d_pderiv32.as<float>() : nullptr);
     TanParams tp{};
     tp.n_patterns = N;
     tp.n_edges = topo.n_edges;
@@ -1360,7 +1411,7 @@ bool netlk_ctx::edge_derivs_analytic(int e, int mode, double *d1, double *d2) {
   const double *tl = h_tree.as<double>(), *tan = h_tan_out.as<double>();
   const std::vector<char> act = mode == 1 ? active_roots_of(e) : std::vector<char>(dag.roots.size(), 1);
   const double min_lp = opts.min_interesting_tree_logprob;
-  double D1 = 0.0, D2 = 0.0;
+  std::vector<double> D1(P, 0.0), D2(P, 0.0);  // per partition, w.r.t. its own length
   for (int p = 0; p < P; ++p) {
     auto a1 = [&](size_t i) { return has[root_slot[i]] ? tan[((size_t)root_slot[i] * P + p) * 2] : 0.0; };
     auto a2 = [&](size_t i) { return has[root_slot[i]] ? tan[((size_t)root_slot[i] * P + p) * 2 + 1] : 0.0; };
@@ -1382,8 +1433,8 @@ bool netlk_ctx::edge_derivs_analytic(int e, int mode, double *d1, double *d2) {
         s2 += w * (a2(i) + a1(i) * a1(i));
       }
       const double g = s1 / z;
-      D1 += g;
-      D2 += s2 / z - g * g;
+      D1[p] = g;
+      D2[p] = s2 / z - g * g;
     } else {
       int best = -1;
       double score = -INFINITY;
@@ -1402,12 +1453,22 @@ bool netlk_ctx::edge_derivs_analytic(int e, int mode, double *d1, double *d2) {
         if (mode == 1) throw Error(NETLK_ERR_NUMERIC, "no displayed tree contains the edge");
         continue;
       }
-      D1 += a1(best);
-      D2 += a2(best);
+      D1[p] = a1(best);
+      D2[p] = a2(best);
     }
   }
-  if (d1) *d1 = D1;
-  if (d2) *d2 = D2;
+  // the derivative of the total w.r.t. the length the caller moves: one
+  // partition's own, all partitions' together, or the linked length of a
+  // scaled context (partition p's length is s_p t)
+  double T1 = 0.0, T2 = 0.0;
+  for (int p = 0; p < P; ++p) {
+    if (part >= 0 && p != part) continue;
+    const double f = part < 0 && linkage == NETLK_BRLEN_SCALED ? scalers[p] : 1.0;
+    T1 += f * D1[p];
+    T2 += f * f * D2[p];
+  }
+  if (d1) *d1 = T1;
+  if (d2) *d2 = T2;
   return true;
 }
 
@@ -1459,8 +1520,8 @@ void netlk_ctx::autotune() {
     count_launches();
     return;
   }
-  std::memcpy(h_brlen.p, brlen.data(), brlen.size() * 8);
-  CUDA_OK(cudaMemcpyAsync(d_brlen.p, h_brlen.p, brlen.size() * 8, cudaMemcpyHostToDevice, stream));
+  std::memcpy(h_brlen.p, dev_len().data(), dev_len().size() * 8);
+  CUDA_OK(cudaMemcpyAsync(d_brlen.p, h_brlen.p, dev_len().size() * 8, cudaMemcpyHostToDevice, stream));
   enqueue(true, true, true, true, true);
   cudaEvent_t e0, e1;
   CUDA_OK(cudaEventCreate(&e0));
@@ -1510,8 +1571,8 @@ void netlk_ctx::prepare_state() {
 void netlk_ctx::prepare() {
   prepare_state();
   if (!device_brlen) {  // lengths set from device memory stay where they are
-    std::memcpy(h_brlen.p, brlen.data(), brlen.size() * 8);
-    CUDA_OK(cudaMemcpyAsync(d_brlen.p, h_brlen.p, brlen.size() * 8, cudaMemcpyHostToDevice, stream));
+    std::memcpy(h_brlen.p, dev_len().data(), dev_len().size() * 8);
+    CUDA_OK(cudaMemcpyAsync(d_brlen.p, h_brlen.p, dev_len().size() * 8, cudaMemcpyHostToDevice, stream));
   }
 }
 
@@ -1596,6 +1657,10 @@ void set_brlen(netlk_ctx *c, const double *b) {
   c->brlen.assign(b, b + c->topo.n_edges);
   for (double &x : c->brlen) x = std::min(std::max(x, 1e-6), 100.0);  // brlen_min / brlen_max
   c->device_brlen = false;
+  if (c->linkage == NETLK_BRLEN_UNLINKED)  // every partition the same lengths
+    for (int p = 0; p < c->P; ++p) std::copy(c->brlen.begin(), c->brlen.end(), c->plen.begin() + (size_t)p * c->topo.n_edges);
+  else if (c->linkage == NETLK_BRLEN_SCALED)
+    c->refresh_scaled();
 }
 
 void set_probs(netlk_ctx *c, const double *p) {
@@ -1621,6 +1686,7 @@ int netlk_options_default(netlk_options *o) {
   o->tensor_cores = 1;
   o->checkpoint_segments = 0;
   o->incremental = 1;
+  o->brlen_linkage = NETLK_BRLEN_LINKED;
   return NETLK_OK;
 }
 
@@ -1690,6 +1756,11 @@ int netlk_create(const netlk_topology *topo, const netlk_partition *in_parts, in
       (void)gtr_eigen(c->S, pi.freqs.data(), pi.exch.data());  // validate now
       if (!pi.explicit_rates) (void)gamma_mean_rates(pi.alpha, c->R);
     }
+    if (c->opts.brlen_linkage < NETLK_BRLEN_LINKED || c->opts.brlen_linkage > NETLK_BRLEN_SCALED)
+      throw Error(NETLK_ERR_INVALID_ARGUMENT, "brlen_linkage");
+    c->linkage = c->opts.brlen_linkage;
+    c->scalers.assign(c->P, 1.0);
+    if (c->linkage != NETLK_BRLEN_LINKED) c->plen.assign((size_t)c->P * t.n_edges, 0.0);
     set_brlen(c.get(), branch_lengths);
     if (t.n_ret) {
       if (!ret_first_probs) throw Error(NETLK_ERR_INVALID_ARGUMENT, "reticulation probabilities");
@@ -1952,6 +2023,15 @@ int netlk_loglikelihood_gradient(netlk_ctx *ctx, double *total, double *part_log
     std::vector<double> g(ctx->topo.n_edges);
     ctx->finish(total, part_logl, g.data(), d_retprob);
     if (ctx->bwd.empty()) std::fill(g.begin(), g.end(), 0.0);
+    if (d_brlen && ctx->linkage == NETLK_BRLEN_SCALED && !ctx->bwd.empty()) {
+      // w.r.t. the linked length t_e: sum_p s_p d logL / d (s_p t_e)
+      const int E = ctx->topo.n_edges;
+      std::vector<double> gp((size_t)ctx->P * E);
+      ctx->partition_gradient(gp.data());
+      std::fill(g.begin(), g.end(), 0.0);
+      for (int p = 0; p < ctx->P; ++p)
+        for (int e = 0; e < E; ++e) g[e] += ctx->scalers[p] * gp[(size_t)p * E + e];
+    }
     if (d_brlen) {
       // the gradient is taken w.r.t. the clamped length; zero where the clamp binds
       for (int e = 0; e < ctx->topo.n_edges; ++e) d_brlen[e] = g[e];
@@ -2023,6 +2103,9 @@ int netlk_edge_derivatives(netlk_ctx *ctx, int32_t edge, int32_t mode, double *d
     if (mode != 0 && mode != 1) throw Error(NETLK_ERR_INVALID_ARGUMENT, "mode must be 0 or 1");
     // analytic d1 and d2 from one tangent sweep over the variants above the edge
     if (ctx->edge_derivs_analytic(edge, mode, d1, d2)) return;
+    if (ctx->linkage != NETLK_BRLEN_LINKED)
+      throw Error(NETLK_ERR_UNSUPPORTED,
+                  "edge derivatives of per-partition lengths need one checkpoint segment and host lengths");
     // checkpointed contexts and device-resident lengths: d1 from full adjoint
     // sweeps, d2 as a central difference of d1 (below)
     auto first = [&]() -> double {
@@ -2077,10 +2160,74 @@ int netlk_edge_loglikelihood(netlk_ctx *ctx, int32_t edge, double length, double
     if (ctx->device_brlen)
       throw Error(NETLK_ERR_INVALID_ARGUMENT, "branch lengths are device-resident: set them on the host first");
     ctx->brlen[edge] = std::min(std::max(length, 1e-6), 100.0);
+    const int E = ctx->topo.n_edges;
+    if (ctx->linkage == NETLK_BRLEN_UNLINKED)  // every partition's length of the edge
+      for (int p = 0; p < ctx->P; ++p) ctx->plen[(size_t)p * E + edge] = ctx->brlen[edge];
+    else if (ctx->linkage == NETLK_BRLEN_SCALED)
+      ctx->refresh_scaled();
     ctx->prepare();
     if (!ctx->run_incremental()) ctx->run(&ctx->graph_logl, true, true, true, true, false);
     ctx->finish(total, nullptr, nullptr, nullptr);
   });
+}
+
+int netlk_edge_loglikelihood_partition(netlk_ctx *ctx, int32_t edge, int32_t part, double length,
+                                       double *total) {
+  if (!ctx) return NETLK_ERR_INVALID_ARGUMENT;
+  return guarded(ctx, [&] {
+    if (ctx->linkage != NETLK_BRLEN_UNLINKED)
+      throw Error(NETLK_ERR_UNSUPPORTED, "per-partition lengths need a NETLK_BRLEN_UNLINKED context");
+    if (edge < 0 || edge >= ctx->topo.n_edges) throw Error(NETLK_ERR_INVALID_ARGUMENT, "edge");
+    if (part < 0 || part >= ctx->P) throw Error(NETLK_ERR_INVALID_ARGUMENT, "partition");
+    if (!std::isfinite(length) || length < 0.0) throw Error(NETLK_ERR_INVALID_ARGUMENT, "branch length");
+    ctx->plen[(size_t)part * ctx->topo.n_edges + edge] = std::min(std::max(length, 1e-6), 100.0);
+    ctx->prepare();
+    if (!ctx->run_incremental()) ctx->run(&ctx->graph_logl, true, true, true, true, false);
+    ctx->finish(total, nullptr, nullptr, nullptr);
+  });
+}
+
+int netlk_edge_derivatives_partition(netlk_ctx *ctx, int32_t edge, int32_t part, int32_t mode, double *d1,
+                                     double *d2) {
+  if (!ctx) return NETLK_ERR_INVALID_ARGUMENT;
+  return guarded(ctx, [&] {
+    if (edge < 0 || edge >= ctx->topo.n_edges) throw Error(NETLK_ERR_INVALID_ARGUMENT, "edge");
+    if (part < 0 || part >= ctx->P) throw Error(NETLK_ERR_INVALID_ARGUMENT, "partition");
+    if (mode != 0 && mode != 1) throw Error(NETLK_ERR_INVALID_ARGUMENT, "mode must be 0 or 1");
+    if (!ctx->edge_derivs_analytic(edge, mode, d1, d2, part))
+      throw Error(NETLK_ERR_UNSUPPORTED, "per-partition edge derivatives need one checkpoint segment and host lengths");
+  });
+}
+
+int netlk_set_partition_branch_lengths(netlk_ctx *ctx, int32_t part, const double *b, int32_t n) {
+  if (!ctx) return NETLK_ERR_INVALID_ARGUMENT;
+  return guarded(ctx, [&] {
+    if (ctx->linkage != NETLK_BRLEN_UNLINKED)
+      throw Error(NETLK_ERR_UNSUPPORTED, "per-partition lengths need a NETLK_BRLEN_UNLINKED context");
+    if (part < 0 || part >= ctx->P) throw Error(NETLK_ERR_INVALID_ARGUMENT, "partition");
+    if (!b || n != ctx->topo.n_edges) throw Error(NETLK_ERR_INVALID_ARGUMENT, "branch length count");
+    check_finite(b, n, "branch length", 0.0, 1e300);
+    for (int e = 0; e < n; ++e)
+      ctx->plen[(size_t)part * n + e] = std::min(std::max(b[e], 1e-6), 100.0);
+    ctx->device_brlen = false;
+  });
+}
+
+int netlk_set_branch_length_scalers(netlk_ctx *ctx, const double *sc, int32_t n) {
+  if (!ctx) return NETLK_ERR_INVALID_ARGUMENT;
+  return guarded(ctx, [&] {
+    if (ctx->linkage != NETLK_BRLEN_SCALED)
+      throw Error(NETLK_ERR_UNSUPPORTED, "length scalers need a NETLK_BRLEN_SCALED context");
+    if (!sc || n != ctx->P) throw Error(NETLK_ERR_INVALID_ARGUMENT, "scaler count");
+    check_finite(sc, n, "branch length scaler", 1e-300, 1e300);
+    ctx->scalers.assign(sc, sc + n);
+    ctx->refresh_scaled();
+  });
+}
+
+int netlk_partition_gradient(netlk_ctx *ctx, double *out) {
+  if (!ctx || !out) return NETLK_ERR_INVALID_ARGUMENT;
+  return guarded(ctx, [&] { ctx->partition_gradient(out); });
 }
 
 int netlk_last_site_updates(const netlk_ctx *ctx, int64_t *site_updates) {
@@ -2125,6 +2272,8 @@ int netlk_mix_and_backward(netlk_ctx *ctx, const double *global, double *total, 
 int netlk_set_branch_lengths_device(netlk_ctx *ctx, const double *d_b, int32_t n) {
   if (!ctx) return NETLK_ERR_INVALID_ARGUMENT;
   return guarded(ctx, [&] {
+    if (ctx->linkage != NETLK_BRLEN_LINKED)
+      throw Error(NETLK_ERR_UNSUPPORTED, "device-resident lengths need linked branch lengths");
     if (ctx->opts.host_only) throw Error(NETLK_ERR_NO_DEVICE, "context was created host_only");
     if (!d_b || n != ctx->topo.n_edges) throw Error(NETLK_ERR_INVALID_ARGUMENT, "branch length count");
     CUDA_OK(cudaSetDevice(ctx->device));
@@ -2499,6 +2648,8 @@ int netlk_batch_create_ex(netlk_ctx *const *ctxs, int32_t n, int32_t mode, netlk
       if (!ctxs[i]) throw Error(NETLK_ERR_INVALID_ARGUMENT, "batch: context " + std::to_string(i) + " is NULL");
       if (ctxs[i]->opts.host_only)
         throw Error(NETLK_ERR_NO_DEVICE, "batch: context " + std::to_string(i) + " was created host_only");
+      if (ctxs[i]->linkage != NETLK_BRLEN_LINKED)
+        throw Error(NETLK_ERR_UNSUPPORTED, "batch: context " + std::to_string(i) + " has per-partition lengths");
       if (i && ctxs[i]->device != ctxs[0]->device)
         throw Error(NETLK_ERR_INVALID_ARGUMENT, "batch: all contexts must be on one device");
       for (int j = 0; j < i; ++j)
@@ -2560,7 +2711,7 @@ int netlk_batch_loglikelihood_gradient(netlk_batch *b, double *totals, double *c
             std::memcpy(d_brlen[i], o + nout, c->topo.n_edges * 8);
         }
         c->clv_valid = true;  // every CLV now matches the context's host lengths
-        c->clv_brlen = c->brlen;
+        c->clv_brlen = c->dev_len();
         c->last_updates = c->site_updates;
       }
       return;
@@ -2581,7 +2732,7 @@ int netlk_batch_loglikelihood_gradient(netlk_batch *b, double *totals, double *c
       }
       if (c->bwd.empty()) std::fill(g.begin(), g.end(), 0.0);
       c->clv_valid = true;  // every CLV now matches the context's host lengths
-      c->clv_brlen = c->brlen;
+      c->clv_brlen = c->dev_len();
       c->last_updates = c->site_updates;
       if (totals) totals[i] = tot;
       if (d_brlen && d_brlen[i]) std::memcpy(d_brlen[i], g.data(), g.size() * 8);

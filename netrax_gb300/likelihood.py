@@ -38,7 +38,7 @@ class NetworkLikelihood:
     def __init__(self, network: NetworkDesc, partitions, variant="AVERAGE", precision="fp32",
                  min_interesting_tree_logprob=math.log(1e-6), device=0, use_cuda_graph=True,
                  host_only=False, rates=None, autotune=True, tensor_cores=True, checkpoint_segments=0,
-                 incremental=True):
+                 incremental=True, brlen_linkage="linked"):
         L = N.lib()
         self.network = network
         self.n_parts = len(partitions)
@@ -95,6 +95,8 @@ class NetworkLikelihood:
         opts.tensor_cores = int(bool(tensor_cores))
         opts.checkpoint_segments = int(checkpoint_segments)
         opts.incremental = int(bool(incremental))
+        opts.brlen_linkage = {"linked": N.NETLK_BRLEN_LINKED, "unlinked": N.NETLK_BRLEN_UNLINKED,
+                              "scaled": N.NETLK_BRLEN_SCALED}[brlen_linkage]
         bl = arr(network.branch_lengths, np.float64)
         rp = arr(network.ret_first_probs, np.float64) if self.n_ret else None
         h = ctypes.c_void_p()
@@ -152,6 +154,36 @@ class NetworkLikelihood:
         r = None if rates is None else np.ascontiguousarray(rates, np.float64)
         N.check(N.lib().netlk_set_model(self._h, part, _ptr(f, ctypes.c_double), _ptr(x, ctypes.c_double),
                                         float(alpha), _ptr(r, ctypes.c_double)), self._h)
+
+    def set_partition_branch_lengths(self, part, b):
+        """One partition's own branch lengths (unlinked contexts)."""
+        b = np.ascontiguousarray(b, np.float64)
+        N.check(N.lib().netlk_set_partition_branch_lengths(self._h, int(part), _ptr(b, ctypes.c_double), b.size),
+                self._h)
+
+    def set_branch_length_scalers(self, scalers):
+        """Per-partition length scalers (scaled contexts)."""
+        sc = np.ascontiguousarray(scalers, np.float64)
+        N.check(N.lib().netlk_set_branch_length_scalers(self._h, _ptr(sc, ctypes.c_double), sc.size), self._h)
+
+    def partition_gradient(self):
+        """d logL / d (partition p's length of edge e) [n_parts][n_edges] of
+        the last logL + gradient evaluation."""
+        out = np.zeros(self.n_parts * self.n_edges)
+        N.check(N.lib().netlk_partition_gradient(self._h, _ptr(out, ctypes.c_double)), self._h)
+        return out.reshape(self.n_parts, self.n_edges)
+
+    def edge_loglikelihood_partition(self, edge, part, length):
+        tot = ctypes.c_double()
+        N.check(N.lib().netlk_edge_loglikelihood_partition(self._h, int(edge), int(part), float(length),
+                                                           ctypes.byref(tot)), self._h)
+        return tot.value
+
+    def edge_derivatives_partition(self, edge, part, mode=0):
+        d1, d2 = ctypes.c_double(), ctypes.c_double()
+        N.check(N.lib().netlk_edge_derivatives_partition(self._h, int(edge), int(part), int(mode), ctypes.byref(d1),
+                                                         ctypes.byref(d2)), self._h)
+        return d1.value, d2.value
 
     def set_prop_invar(self, part, prop_invar):
         """Proportion of invariant sites (+I) of one partition."""

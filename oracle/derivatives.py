@@ -209,13 +209,15 @@ class EdgeDerivativeOracle:
     def _use(self, tree):
         return tree["logprob"] >= self.orc.min_lp
 
-    def edge(self, e, mode="true"):
-        """(d logL / d t_e, d2 logL / d t_e^2) summed over partitions."""
+    def edge(self, e, mode="true", partitions=None):
+        """(d logL / d t_e, d2 logL / d t_e^2) summed over partitions (or
+        over ``partitions``: each term is the derivative of the partition's
+        logL w.r.t. its own length of the edge)."""
         ref = mode == "reference"
         trees = [t for t in self.trees if self._use(t) and (not ref or self._active(t, e))]
         D1 = D2 = 0.0
         for p in range(len(self.orc.parts)):
-            if not trees:
+            if not trees or (partitions is not None and p not in partitions):
                 continue
             if self.orc.variant == AVERAGE:
                 with mpmath.workprec(53):
