@@ -508,8 +508,13 @@ def run_edge(args, ws, rank, local):
     synchronous like its Newton-Raphson loop (BranchLengthOptimization.cpp:
     171-200, VirtualRerooting.cpp:348-585): a full logL after every length
     changed, netlk_edge_loglikelihood (only the variants above the edge are
-    recomputed) and netlk_edge_derivatives (d1 from the adjoint sweep, d2 by a
-    central difference of d1)."""
+    recomputed), netlk_edge_derivatives (analytic d1 and d2 from one tangent
+    sweep over the variants above the edge), and the sumtable route of the
+    Newton-Raphson loop: netlk_edge_sumtable (the per-tree outside vectors at
+    the edge, once per edge) and netlk_edge_sumtable_derivatives (logL, d1, d2
+    at a proposed length: one pass over the tables) - against one iteration
+    of the tangent route (netlk_edge_loglikelihood at the proposal, then
+    netlk_edge_derivatives)."""
     import torch
     from netrax_gb300 import synth
     from netrax_gb300.likelihood import NetworkLikelihood
@@ -553,6 +558,30 @@ def run_edge(args, ws, rank, local):
     for k in range(nd):
         lik.edge_derivatives(edges[k])
     der_s = (time.perf_counter() - t) / nd
+
+    # sumtables: build once per edge, then evaluations at proposed lengths
+    sedges = [edges[k] for k in range(nd)]
+    lik.edge_sumtable(sedges[0])
+    t = time.perf_counter()
+    built = [lik.edge_sumtable(e) for e in sedges]
+    build_s = (time.perf_counter() - t) / nd
+    n_tab = built[-1][1]
+    table_bytes = (n_tab * lik.stats["n_patterns_total"] * lik.rate_cats * lik.states
+                   * (4 if args.precision == "fp32" else 8))
+    n_eval = 0
+    t = time.perf_counter()
+    for e in sedges[-1:]:
+        for j in range(max(10, K)):
+            lik.edge_sumtable_derivatives(e, base[e] * (0.5 + 0.05 * (j % 20)))
+            n_eval += 1
+    eval_s = (time.perf_counter() - t) / n_eval
+    t = time.perf_counter()
+    for k in range(nd):
+        e = sedges[k]
+        lik.edge_loglikelihood(e, base[e] * 1.1)
+        lik.edge_derivatives(e)
+        lik.edge_loglikelihood(e, base[e])
+    tangent_iter_s = (time.perf_counter() - t) / nd - edge_s
     lik.close()
     if rank == 0:
         line = {
@@ -567,6 +596,13 @@ def run_edge(args, ws, rank, local):
             "mean_site_updates_per_edge_eval": upd / K,
             "full_logl_ms": full_s * 1000.0, "full_site_updates": full_updates,
             "edge_derivatives_ms": der_s * 1000.0, "edge_derivatives_per_s": 1.0 / der_s,
+            "sumtable": {"applies": all(b for b, _ in built), "build_ms": build_s * 1000.0,
+                         "eval_ms": eval_s * 1000.0, "tables_of_evaluated_edge": n_tab,
+                         "table_bytes_of_evaluated_edge": table_bytes,
+                         "eval_table_GBps_wall": table_bytes / eval_s / 1e9,
+                         "tangent_nr_iteration_ms": tangent_iter_s * 1000.0,
+                         "note": "eval: logL, d1, d2 at a proposed length from the tables; tangent iteration: "
+                                 "edge logL at the proposal + tangent derivatives"},
         }
         print(json.dumps(line), flush=True)
 

@@ -396,6 +396,46 @@ int netlk_edge_derivatives(netlk_ctx *ctx, int32_t edge, int32_t mode,
 int netlk_edge_derivatives_partition(netlk_ctx *ctx, int32_t edge, int32_t partition, int32_t mode, double *d1,
                                      double *d2);
 
+/* Edge sumtables for the Newton-Raphson iterations along one edge: the
+ * reference computes the sumtables of an edge once per optimize_branch
+ * (computePartitionSumtables, src/likelihood/LikelihoodDerivatives.cpp:249-344,
+ * at the virtual reroot of computeLoglikelihoodBrlenOpt) and every NR
+ * callback (network_derivative_func_multi,
+ * src/optimization/BranchLengthOptimization.cpp:171-200) evaluates them at
+ * the proposed length (pll_compute_loglikelihood_derivatives,
+ * LikelihoodDerivatives.cpp:95-104). Here the tables are, per displayed tree
+ * containing the edge, its outside vector at the edge per (pattern, rate):
+ * one forward-mode sweep of the message's S unit directions over the
+ * variants above the edge. An evaluation at length t is one pass over them:
+ * L = sum_r O_r . (P_r(t) I_r) with I the edge's child CLV (every term
+ * non-negative), and L', L'' with P', P''.
+ *
+ * netlk_edge_sumtable builds the tables at the current parameters (the
+ * evaluation builds them itself when they are missing or stale; this entry
+ * lets a caller pay for the build where it chooses). *built = 1 when the
+ * sumtable path applies, 0 when it does not (20-state partitions, several
+ * checkpoint segments, device-resident lengths, or tables that would take
+ * more than half the free device memory); evaluations then take the tangent
+ * path. *n_tables (may be NULL): the tables built, one per displayed tree
+ * that contains the edge. */
+int netlk_edge_sumtable(netlk_ctx *ctx, int32_t edge, int32_t *built, int32_t *n_tables);
+/* logL and its first / second derivative with the edge at the given
+ * length(s), without changing the context's parameters. n_lengths = 1: one
+ * length t for the edge (scaled contexts: partition p at s_p t); logl[0],
+ * d1[0], d2[0] are the totals w.r.t. t, mode as in netlk_edge_derivatives.
+ * n_lengths = n_parts (unlinked contexts): partition p's length is
+ * lengths[p], and logl[p], d1[p], d2[p] are partition p's logL and its
+ * derivatives w.r.t. its own length - the reference's df[p], ddf[p].
+ * Lengths are clamped to [1e-6, 100]. The tables stay current while only
+ * this edge's lengths (or nothing) change; any other length, model,
+ * +I or reticulation probability change rebuilds them on the next call.
+ * Where the sumtable path does not apply, the edge is set to the length,
+ * evaluated incrementally with the tangent sweep, and set back (its CLVs
+ * are recomputed by the next evaluation); contexts with several checkpoint
+ * segments or device-resident lengths get NETLK_ERR_UNSUPPORTED there. */
+int netlk_edge_sumtable_derivatives(netlk_ctx *ctx, int32_t edge, const double *lengths, int32_t n_lengths,
+                                    int32_t mode, double *logl, double *d1, double *d2);
+
 /* ------------------------------------------------- sharded (multi-rank) use */
 /* Per-(root variant, partition) log-likelihood partial sums over the patterns
  * this context holds [n_root_variants*n_parts]; ranks that hold disjoint

@@ -251,6 +251,41 @@ bool launch_tangent(cudaStream_t s, int precision, int R, int S, const TanParams
 void launch_tangent_reduce(cudaStream_t s, const TanParams &p, const int32_t *slots, int n_slots,
                            const int32_t *part_block_begin, int n_parts, double *out);
 
+// Edge sumtables (tangent.cu): for branch e, each displayed tree's outside
+// vector at e, O[i] = d L_site / d m_i with m = P_e I the message e carries
+// up from its child CLV I (the tree's root site likelihood in the scaled
+// units of the forward sweep), per (tree, pattern, rate). Built by a
+// forward-mode sweep of the S unit directions of m over the variants above
+// e (the tangent schedule); then L(t) = sum_r O_r . (P_r(t) I_r) for any
+// length t, and L', L'' with P', P'': one pass over the tables per
+// Newton-Raphson iterate. Every term is non-negative, so L keeps full
+// relative precision at short lengths (a sum over eigencomponents would
+// cancel there).
+struct StabParams {
+  TanParams t;                  // t.tan: [n_work][S][N][R][S] unit-direction planes; t.ops' slot = table index
+  void *table;                  // [n_tab][N][R][S] real: O per (table, pattern, rate)
+  int32_t *table_scaler;        // [n_tab][N]: the root's scale counter when the table was built
+  const double *U;              // [n_parts][S][S] eigenvectors (unused by the evaluation)
+  const void *pm3;              // [n_parts][3][R][S][S] real: P, P', P'' at the evaluated lengths
+  const int32_t *group_ref;     // [n_groups] child ref (as FwdOp) whose CLV is I for the group's tables
+  const int32_t *group_begin;   // [n_groups + 1] tables of each group (tables sorted by child)
+  int32_t n_groups;
+  int32_t n_tables, tables_per_block;  // evaluation: tables, and tables per block (blockIdx.y)
+  double *partial;              // [n_tab][3][N / 32] per-warp sums of w log L, w L'/L, w (L''/L - (L'/L)^2); FP32: float pairs
+};
+
+// Builds the tables (one launch per level of the tangent schedule); false
+// for an unsupported (R, S): DNA only.
+bool launch_sumtable_build(cudaStream_t s, int precision, int R, int S, const StabParams &p,
+                           const int32_t *level_begin, int n_levels);
+// P, P', P'' of edge-independent length len[part] for each partition, rate: out [part][3][R][S][S].
+void launch_pmat3(cudaStream_t s, int n_parts, int R, int S, const double *lambda, const double *U,
+                  const double *Uinv, const double *rates, const double *len, double *out64, float *out32);
+// Evaluates every table at p.pm3 and reduces per (table, partition):
+// out [n_tab][n_parts][3] (w log L with the scale counters applied, l', l'').
+bool launch_sumtable_eval(cudaStream_t s, int precision, int R, int S, const StabParams &p, int n_tab,
+                          const int32_t *part_warp_begin, int n_parts, double *out);
+
 // Number of kernel launches issued by the launchers above (host counter).
 int64_t launches_issued();
 void add_launches(int64_t n);

@@ -85,6 +85,7 @@ struct PartInfo {
   std::vector<double> freqs, exch, rates, rate_weights;
   double alpha = 1.0;
   double pinv = 0.0;  // proportion of invariant sites (+I)
+  double wsum = 0.0;  // sum of the pattern weights
   bool explicit_rates = false;
   Eigen eig;
 };
@@ -173,6 +174,17 @@ struct netlk_ctx {
   PinnedBuf h_tan_ops, h_tan_out, h_tan_slots;
   int n_tan_cap = -1;  // tangent slot pairs allocated (-1: not set up yet)
   int tan_blocks = 0;
+  // edge sumtables: unit-direction work planes, per-tree outside vectors at
+  // the edge (tables), their scale counters, and the evaluation buffers
+  DevBuf d_stab_work, d_stab, d_stab_scaler, d_stab_partial, d_stab_out, d_stab_pm3_64, d_stab_pm3_32, d_stab_len,
+      d_stab_groups, d_stab_ops, d_part_warp_begin;
+  PinnedBuf h_stab_len, h_stab_out, h_stab_ops;
+  int stab_cap_work = -1, stab_cap_tab = 0;  // work slots / tables allocated (-1: not set up yet)
+  int stab_edge = -1;                        // edge whose tables are current (-1: none)
+  int stab_n_tab = 0, stab_n_groups = 0;
+  std::vector<int32_t> stab_root_tab;                  // per root: its table, or -1 (edge not in the tree)
+  std::vector<double> stab_lens, stab_probs, stab_tree;  // parameters at the build; per-(slot, part) tree logL
+  uint64_t model_gen = 0, stab_gen = 0;
   DevBuf d_pmat64, d_pmat32, d_lambda, d_U, d_Uinv, d_rates, d_rw, d_freqs, d_Q, d_brlen;
   DevBuf d_grad_part, d_op_sum_part, d_part_unit_begin;  // per-partition gradient (on request)
   // FP32 contexts: float copies the sweeps read (weights as hi/lo pairs)
@@ -239,7 +251,9 @@ struct netlk_ctx {
                       &d_edge_begin, &d_edge_entries, &d_op_sum, &d_weights32, &d_model32, &d_seeds32,
                       &d_wfwd, &d_wrfwd, &d_wbwd, &d_wmsg_slots, &d_tan, &d_tan_ops, &d_tan_partial, &d_tan_out,
                       &d_pderiv64, &d_pderiv32, &d_block_part, &d_part_block_begin, &d_tan_slots, &d_gfrac,
-                      &d_gfrac32, &d_invt, &d_invt32, &d_grad_part, &d_op_sum_part, &d_part_unit_begin})
+                      &d_gfrac32, &d_invt, &d_invt32, &d_grad_part, &d_op_sum_part, &d_part_unit_begin, &d_stab_work,
+                      &d_stab, &d_stab_scaler, &d_stab_partial, &d_stab_out, &d_stab_pm3_64, &d_stab_pm3_32,
+                      &d_stab_len, &d_stab_groups, &d_stab_ops, &d_part_warp_begin})
       b->free();
     if (stream) cudaStreamDestroy(stream);
   }
@@ -347,6 +361,57 @@ struct netlk_ctx {
   // segments, device-resident lengths)
   // part >= 0: that partition's share only
   bool edge_derivs_analytic(int e, int mode, double *d1, double *d2, int part = -1);
+  void setup_tangent_blocks();
+  TanParams tan_params() const {  // the fields shared by the tangent and sumtable sweeps
+    TanParams tp{};
+    tp.n_patterns = N;
+    tp.n_edges = topo.n_edges;
+    tp.n_blocks = tan_blocks;
+    tp.clv = d_clv.p;
+    tp.scaler = d_scaler.as<int32_t>();
+    tp.tips = S == 4 ? d_tips.as<uint8_t>() : nullptr;
+    tp.tips32 = S == 20 ? d_tips.as<uint32_t>() : nullptr;
+    tp.pmat = opts.precision == NETLK_FP32 ? d_pmat32.p : d_pmat64.p;
+    tp.block_part = d_block_part.as<int32_t>();
+    tp.weights = d_weights.as<double>();
+    tp.freqs = d_freqs.as<double>();
+    tp.rate_weights = d_rw.as<double>();
+    tp.inv_term = has_pinv ? d_invt.as<double>() : nullptr;
+    return tp;
+  }
+  StabParams stab_params() const {
+    StabParams sp{};
+    sp.t = tan_params();
+    sp.t.tan = d_stab_work.p;
+    sp.t.ops = d_stab_ops.as<TanOp>();
+    sp.table = d_stab.p;
+    sp.table_scaler = d_stab_scaler.as<int32_t>();
+    sp.U = d_U.as<double>();
+    sp.pm3 = opts.precision == NETLK_FP32 ? d_stab_pm3_32.p : d_stab_pm3_64.p;
+    sp.group_ref = d_stab_groups.as<int32_t>();
+    sp.group_begin = d_stab_groups.as<int32_t>() + stab_n_groups;
+    sp.n_groups = stab_n_groups;
+    sp.n_tables = stab_n_tab;
+    // about four blocks of each pattern range per SM at the largest counts,
+    // at least 4 tables per block (the child's P I is formed once per block)
+    sp.tables_per_block = std::max(4, (int)((int64_t)stab_n_tab * (N / 128) / (152 * 16) + 1));
+    sp.partial = d_stab_partial.as<double>();
+    return sp;
+  }
+  // Per-partition mixture of per-tree (l, l', l'') along edge e: logL of the
+  // partition (over every tree) and its first / second derivative (mode 0:
+  // of the mixture; mode 1: the reference's formula over the trees active at
+  // e). false when mode 1 finds no tree.
+  template <class LL, class A1, class A2>
+  bool mix_edge(int e_mode, const std::vector<char> &act, LL ll, A1 a1, A2 a2, double *logl, double *D1,
+                double *D2) const;
+  // edge sumtables (Newton-Raphson along one edge): build at the current
+  // parameters (false where the path does not apply: 20 states, several
+  // checkpoint segments, device-resident lengths, too little memory);
+  // current while only edge e's lengths and nothing else changed since
+  bool sumtable_build(int e);
+  bool sumtable_current(int e) const;
+  void sumtable_eval(int e, const double *len, int n_len, int mode, double *logl, double *d1, double *d2);
   int tangent_schedule(int e, std::vector<TanOp> &ops, std::vector<int32_t> &level_begin,
                        std::vector<int32_t> &slots) const;
   // d logL / d (partition p's length of edge e) [P][E] from the last adjoint
@@ -789,6 +854,7 @@ void netlk_ctx::allocate_and_upload(const netlk_partition *in) {
       double w = in[p].pattern_weights ? in[p].pattern_weights[s] : 1.0;
       if (!(w >= 0.0) || !std::isfinite(w)) throw Error(NETLK_ERR_INVALID_ARGUMENT, "pattern weight");
       weights[pi.offset + s] = w;
+      parts[p].wsum += w;
     }
     for (int u = (int)(pi.offset / ppw); u < (int)((pi.offset + pi.n_pad) / ppw); ++u) unit_part[u] = p;
   }
@@ -1322,15 +1388,7 @@ bool netlk_ctx::edge_derivs_analytic(int e, int mode, double *d1, double *d2, in
     std::vector<TanOp> ops;
     std::vector<int32_t> lb, sl;
     for (int k = 0; k < topo.n_edges; ++k) need = std::max(need, tangent_schedule(k, ops, lb, sl));
-    const int ppb = tangent_patterns_per_block(R);
-    tan_blocks = (int)(N / ppb);
-    std::vector<int32_t> block_part(tan_blocks), pbb(P + 1);
-    for (int p = 0; p < P; ++p) {
-      pbb[p] = (int32_t)(parts[p].offset / ppb);
-      for (int64_t b = parts[p].offset / ppb; b < (parts[p].offset + parts[p].n_pad) / ppb; ++b) block_part[b] = p;
-    }
-    pbb[P] = tan_blocks;
-    if (N % ppb) throw Error(NETLK_ERR_INVALID_ARGUMENT, "tangent sweep: patterns not a whole number of blocks");
+    setup_tangent_blocks();
     size_t free_b = 0, total_b = 0;
     CUDA_OK(cudaMemGetInfo(&free_b, &total_b));
     if ((double)need * 2 * plane > 0.5 * (double)free_b) {  // too big: keep the full-gradient path
@@ -1345,14 +1403,10 @@ bool netlk_ctx::edge_derivs_analytic(int e, int mode, double *d1, double *d2, in
     d_tan_slots.alloc((size_t)std::max(1, n_slots) * 4, scratch);
     d_pderiv64.alloc((size_t)P * 2 * R * S * S * 8, scratch);
     d_pderiv32.alloc((size_t)P * 2 * R * S * S * 4, scratch);
-    d_block_part.alloc(block_part.size() * 4, scratch);
-    d_part_block_begin.alloc(pbb.size() * 4, scratch);
     dev_bytes += scratch;
     h_tan_ops.alloc(dag.vars.size() * sizeof(TanOp));
     h_tan_out.alloc((size_t)std::max(1, n_slots) * P * 2 * 8);
     h_tan_slots.alloc((size_t)std::max(1, n_slots) * 4);
-    CUDA_OK(cudaMemcpy(d_block_part.p, block_part.data(), block_part.size() * 4, cudaMemcpyHostToDevice));
-    CUDA_OK(cudaMemcpy(d_part_block_begin.p, pbb.data(), pbb.size() * 4, cudaMemcpyHostToDevice));
     n_tan_cap = need;
   }
   std::vector<TanOp> ops;
@@ -1371,23 +1425,10 @@ bool netlk_ctx::edge_derivs_analytic(int e, int mode, double *d1, double *d2, in
     launch_pderiv(stream, P, R, S, d_lambda.as<double>(), d_U.as<double>(), d_Uinv.as<double>(), d_rates.as<double>(),
                   d_brlen.as<double>(), len_stride(), e, d_pderiv64.as<double>(),
                   opts.precision == NETLK_FP32 ? d_pderiv32.as<float>() : nullptr);
-    TanParams tp{};
-    tp.n_patterns = N;
-    tp.n_edges = topo.n_edges;
-    tp.n_blocks = tan_blocks;
-    tp.clv = d_clv.p;
-    tp.scaler = d_scaler.as<int32_t>();
-    tp.tips = S == 4 ? d_tips.as<uint8_t>() : nullptr;
-    tp.tips32 = S == 20 ? d_tips.as<uint32_t>() : nullptr;
-    tp.pmat = opts.precision == NETLK_FP32 ? d_pmat32.p : d_pmat64.p;
+    TanParams tp = tan_params();
     tp.pderiv = opts.precision == NETLK_FP32 ? d_pderiv32.p : d_pderiv64.p;
     tp.tan = d_tan.p;
     tp.ops = d_tan_ops.as<TanOp>();
-    tp.block_part = d_block_part.as<int32_t>();
-    tp.weights = d_weights.as<double>();
-    tp.freqs = d_freqs.as<double>();
-    tp.rate_weights = d_rw.as<double>();
-    tp.inv_term = has_pinv ? d_invt.as<double>() : nullptr;
     tp.partial = d_tan_partial.as<double>();
     if (!launch_tangent(stream, opts.precision, R, S, tp, lb.data(), dag.n_levels)) return false;
     launch_tangent_reduce(stream, tp, d_tan_slots.as<int32_t>(), (int)dslots.size(),
@@ -1410,52 +1451,13 @@ bool netlk_ctx::edge_derivs_analytic(int e, int mode, double *d1, double *d2, in
   for (int32_t sl : dslots) has[sl] = 1;
   const double *tl = h_tree.as<double>(), *tan = h_tan_out.as<double>();
   const std::vector<char> act = mode == 1 ? active_roots_of(e) : std::vector<char>(dag.roots.size(), 1);
-  const double min_lp = opts.min_interesting_tree_logprob;
   std::vector<double> D1(P, 0.0), D2(P, 0.0);  // per partition, w.r.t. its own length
   for (int p = 0; p < P; ++p) {
     auto a1 = [&](size_t i) { return has[root_slot[i]] ? tan[((size_t)root_slot[i] * P + p) * 2] : 0.0; };
     auto a2 = [&](size_t i) { return has[root_slot[i]] ? tan[((size_t)root_slot[i] * P + p) * 2 + 1] : 0.0; };
     auto ll = [&](size_t i) { return tl[(size_t)root_slot[i] * P + p]; };
-    if (opts.variant == NETLK_AVERAGE) {
-      double m = -INFINITY;
-      for (size_t i = 0; i < dag.roots.size(); ++i)
-        if (act[i] && dag.roots[i].logprob >= min_lp) m = std::max(m, dag.roots[i].logprob + ll(i));
-      if (!(m > -INFINITY)) {
-        if (mode == 1) throw Error(NETLK_ERR_NUMERIC, "no displayed tree contains the edge");
-        continue;
-      }
-      double z = 0.0, s1 = 0.0, s2 = 0.0;
-      for (size_t i = 0; i < dag.roots.size(); ++i) {
-        if (!act[i] || dag.roots[i].logprob < min_lp) continue;
-        const double w = std::exp(dag.roots[i].logprob + ll(i) - m);
-        z += w;
-        s1 += w * a1(i);
-        s2 += w * (a2(i) + a1(i) * a1(i));
-      }
-      const double g = s1 / z;
-      D1[p] = g;
-      D2[p] = s2 / z - g * g;
-    } else {
-      int best = -1;
-      double score = -INFINITY;
-      for (size_t i = 0; i < dag.roots.size(); ++i) {
-        const double lpi = dag.roots[i].logprob;
-        if (!act[i] || lpi < min_lp) continue;
-        // mode 0: the tree the BEST mixture takes (ties to the lower index);
-        // mode 1: the reference's choice by tree_logl * tree_prob
-        const double v = mode == 1 ? ll(i) * std::exp(lpi) : lpi + ll(i);
-        if (best < 0 || v > score) {
-          score = v;
-          best = (int)i;
-        }
-      }
-      if (best < 0) {
-        if (mode == 1) throw Error(NETLK_ERR_NUMERIC, "no displayed tree contains the edge");
-        continue;
-      }
-      D1[p] = a1(best);
-      D2[p] = a2(best);
-    }
+    if (!mix_edge(mode, act, ll, a1, a2, nullptr, &D1[p], &D2[p]))
+      throw Error(NETLK_ERR_NUMERIC, "no displayed tree contains the edge");
   }
   // the derivative of the total w.r.t. the length the caller moves: one
   // partition's own, all partitions' together, or the linked length of a
@@ -1470,6 +1472,256 @@ bool netlk_ctx::edge_derivs_analytic(int e, int mode, double *d1, double *d2, in
   if (d1) *d1 = T1;
   if (d2) *d2 = T2;
   return true;
+}
+
+void netlk_ctx::setup_tangent_blocks() {
+  if (tan_blocks > 0) return;
+  const int ppb = tangent_patterns_per_block(R);
+  if (N % ppb) throw Error(NETLK_ERR_INVALID_ARGUMENT, "tangent sweep: patterns not a whole number of blocks");
+  const int nb = (int)(N / ppb);
+  std::vector<int32_t> block_part(nb), pbb(P + 1);
+  for (int p = 0; p < P; ++p) {
+    pbb[p] = (int32_t)(parts[p].offset / ppb);
+    for (int64_t b = parts[p].offset / ppb; b < (parts[p].offset + parts[p].n_pad) / ppb; ++b) block_part[b] = p;
+  }
+  pbb[P] = nb;
+  int64_t scratch = 0;
+  d_block_part.alloc(block_part.size() * 4, scratch);
+  d_part_block_begin.alloc(pbb.size() * 4, scratch);
+  dev_bytes += scratch;
+  CUDA_OK(cudaMemcpy(d_block_part.p, block_part.data(), block_part.size() * 4, cudaMemcpyHostToDevice));
+  CUDA_OK(cudaMemcpy(d_part_block_begin.p, pbb.data(), pbb.size() * 4, cudaMemcpyHostToDevice));
+  tan_blocks = nb;
+}
+
+template <class LL, class A1, class A2>
+bool netlk_ctx::mix_edge(int mode, const std::vector<char> &act, LL ll, A1 a1, A2 a2, double *logl, double *D1,
+                         double *D2) const {
+  const double min_lp = opts.min_interesting_tree_logprob;
+  const size_t nr = dag.roots.size();
+  if (logl) {  // the partition's logL over every tree, as the mixture kernel forms it
+    double best = -INFINITY;
+    for (size_t i = 0; i < nr; ++i)
+      if (dag.roots[i].logprob >= min_lp) best = std::max(best, dag.roots[i].logprob + ll(i));
+    if (opts.variant == NETLK_AVERAGE && best > -INFINITY) {
+      double acc = 0.0;
+      for (size_t i = 0; i < nr; ++i)
+        if (dag.roots[i].logprob >= min_lp) acc += std::exp(dag.roots[i].logprob + ll(i) - best);
+      best += std::log(acc);
+    }
+    *logl = best;
+  }
+  *D1 = *D2 = 0.0;
+  if (opts.variant == NETLK_AVERAGE) {
+    double m = -INFINITY;
+    for (size_t i = 0; i < nr; ++i)
+      if (act[i] && dag.roots[i].logprob >= min_lp) m = std::max(m, dag.roots[i].logprob + ll(i));
+    if (!(m > -INFINITY)) return mode != 1;
+    double z = 0.0, s1 = 0.0, s2 = 0.0;
+    for (size_t i = 0; i < nr; ++i) {
+      if (!act[i] || dag.roots[i].logprob < min_lp) continue;
+      const double w = std::exp(dag.roots[i].logprob + ll(i) - m);
+      const double g1 = a1(i);
+      z += w;
+      s1 += w * g1;
+      s2 += w * (a2(i) + g1 * g1);
+    }
+    const double g = s1 / z;
+    *D1 = g;
+    *D2 = s2 / z - g * g;
+    return true;
+  }
+  int best = -1;
+  double score = -INFINITY;
+  for (size_t i = 0; i < nr; ++i) {
+    const double lpi = dag.roots[i].logprob;
+    if (!act[i] || lpi < min_lp) continue;
+    // mode 0: the tree the BEST mixture takes (ties to the lower index);
+    // mode 1: the reference's choice by tree_logl * tree_prob
+    const double v = mode == 1 ? ll(i) * std::exp(lpi) : lpi + ll(i);
+    if (best < 0 || v > score) {
+      score = v;
+      best = (int)i;
+    }
+  }
+  if (best < 0) return mode != 1;
+  *D1 = a1(best);
+  *D2 = a2(best);
+  return true;
+}
+
+bool netlk_ctx::sumtable_current(int e) const {
+  if (stab_edge != e || stab_gen != model_gen || device_brlen || stab_probs != ret_probs) return false;
+  const std::vector<double> &L = dev_len();
+  const int E = topo.n_edges;
+  for (size_t i = 0; i < L.size(); ++i)
+    if ((int)(i % E) != e && L[i] != stab_lens[i]) return false;
+  return true;
+}
+
+bool netlk_ctx::sumtable_build(int e) {
+  stab_edge = -1;
+  if (n_segments != 1 || device_brlen || S != 4 || opts.host_only) return false;
+  prepare();
+  const size_t real_b = opts.precision == NETLK_FP32 ? 4 : 8;
+  const size_t plane = (size_t)N * R * S * real_b;  // one (pattern, rate, state) plane
+  if (stab_cap_work < 0) {
+    // set up once: the most work slots and tables any edge needs
+    int need = 0, tabs = 0;
+    std::vector<TanOp> ops;
+    std::vector<int32_t> lb, sl;
+    for (int k = 0; k < topo.n_edges; ++k) {
+      need = std::max(need, tangent_schedule(k, ops, lb, sl));
+      tabs = std::max(tabs, (int)sl.size());
+    }
+    setup_tangent_blocks();
+    size_t free_b = 0, total_b = 0;
+    CUDA_OK(cudaMemGetInfo(&free_b, &total_b));
+    const double bytes = ((double)need * S + tabs) * plane + (double)tabs * N * (4 + 3 * 8 / 32.0);
+    if (bytes > 0.5 * (double)free_b) {  // too big: keep the tangent path
+      stab_cap_work = 0;
+      return false;
+    }
+    int64_t scratch = 0;
+    d_stab_work.alloc(std::max<size_t>(1, (size_t)need * S) * plane, scratch);
+    d_stab.alloc(std::max<size_t>(1, (size_t)tabs) * plane, scratch);
+    d_stab_scaler.alloc(std::max<size_t>(1, (size_t)tabs) * N * 4, scratch);
+    d_stab_partial.alloc(std::max<size_t>(1, (size_t)tabs) * 3 * (N / 32) * 8, scratch);
+    d_stab_out.alloc(std::max<size_t>(1, (size_t)tabs) * P * 3 * 8, scratch);
+    d_stab_pm3_64.alloc((size_t)P * 3 * R * S * S * 8, scratch);
+    d_stab_pm3_32.alloc((size_t)P * 3 * R * S * S * 4, scratch);
+    d_stab_len.alloc((size_t)P * 8, scratch);
+    d_stab_groups.alloc((size_t)(2 * tabs + 2) * 4, scratch);
+    d_stab_ops.alloc(dag.vars.size() * sizeof(TanOp), scratch);
+    d_part_warp_begin.alloc((size_t)(P + 1) * 4, scratch);
+    dev_bytes += scratch;
+    h_stab_len.alloc((size_t)P * 8);
+    h_stab_out.alloc(std::max<size_t>(1, (size_t)tabs) * P * 3 * 8);
+    h_stab_ops.alloc(dag.vars.size() * sizeof(TanOp) + (size_t)(2 * tabs + 2) * 4);
+    std::vector<int32_t> pwb(P + 1);
+    for (int p = 0; p < P; ++p) pwb[p] = (int32_t)(parts[p].offset / 32);
+    pwb[P] = (int32_t)(N / 32);
+    CUDA_OK(cudaMemcpy(d_part_warp_begin.p, pwb.data(), pwb.size() * 4, cudaMemcpyHostToDevice));
+    stab_cap_work = need;
+    stab_cap_tab = tabs;
+  }
+  std::vector<TanOp> ops;
+  std::vector<int32_t> lb, dslots;
+  const int need = tangent_schedule(e, ops, lb, dslots);
+  if (need < 0 || need > stab_cap_work || stab_cap_work == 0 || (int)dslots.size() > stab_cap_tab) return false;
+  // the child whose CLV each root's path starts from (the message e carries);
+  // tables sorted by it so the evaluation forms P I once per child
+  std::vector<int32_t> origin(ops.size()), op_of(dag.vars.size(), -1);
+  std::vector<std::pair<int32_t, int32_t>> roots_by_child;  // (child ref, op)
+  for (size_t j = 0; j < ops.size(); ++j) {
+    op_of[ops[j].x] = (int32_t)j;
+    origin[j] = ops[j].mode == 1 ? ops[j].d : origin[op_of[ops[j].d]];
+    if (ops[j].slot >= 0) roots_by_child.push_back({origin[j], (int32_t)j});
+  }
+  std::stable_sort(roots_by_child.begin(), roots_by_child.end(),
+                   [](const std::pair<int32_t, int32_t> &a, const std::pair<int32_t, int32_t> &b) {
+                     return a.first < b.first;
+                   });
+  std::vector<int32_t> slot_tab(n_slots, -1), gref, gbegin;
+  for (size_t t = 0; t < roots_by_child.size(); ++t) {
+    TanOp &op = ops[roots_by_child[t].second];
+    slot_tab[op.slot] = (int32_t)t;
+    op.slot = (int32_t)t;
+    if (gref.empty() || gref.back() != roots_by_child[t].first) {
+      gref.push_back(roots_by_child[t].first);
+      gbegin.push_back((int32_t)t);
+    }
+  }
+  gbegin.push_back((int32_t)roots_by_child.size());
+  stab_n_tab = (int)roots_by_child.size();
+  stab_n_groups = (int)gref.size();
+  stab_root_tab.assign(dag.roots.size(), -1);
+  for (size_t i = 0; i < dag.roots.size(); ++i) stab_root_tab[i] = slot_tab[root_slot[i]];
+  // CLVs and per-tree logL at the current parameters
+  if (!run_incremental()) run(&graph_logl, true, true, true, true, false);
+  CUDA_OK(cudaMemcpyAsync(h_tree.p, d_tree_logl.p, (size_t)n_slots * P * 8, cudaMemcpyDeviceToHost, stream));
+  if (!ops.empty()) {
+    unsigned char *hp = static_cast<unsigned char *>(h_stab_ops.p);
+    std::memcpy(hp, ops.data(), ops.size() * sizeof(TanOp));
+    CUDA_OK(cudaMemcpyAsync(d_stab_ops.p, hp, ops.size() * sizeof(TanOp), cudaMemcpyHostToDevice, stream));
+    int32_t *hg = reinterpret_cast<int32_t *>(hp + dag.vars.size() * sizeof(TanOp));
+    std::memcpy(hg, gref.data(), gref.size() * 4);
+    std::memcpy(hg + gref.size(), gbegin.data(), gbegin.size() * 4);
+    CUDA_OK(cudaMemcpyAsync(d_stab_groups.p, hg, (gref.size() + gbegin.size()) * 4, cudaMemcpyHostToDevice, stream));
+    StabParams sp = stab_params();
+    if (!launch_sumtable_build(stream, opts.precision, R, S, sp, lb.data(), dag.n_levels)) return false;
+  }
+  const int nout = 3 + P + topo.n_ret;
+  CUDA_OK(cudaMemcpyAsync(h_out.p, d_out.p, nout * 8, cudaMemcpyDeviceToHost, stream));
+  CUDA_OK(cudaStreamSynchronize(stream));
+  CUDA_OK(cudaGetLastError());
+  check_injected();
+  const double *o = h_out.as<double>();
+  if (o[1] != 0.0 || !std::isfinite(o[0]))
+    throw Error(NETLK_ERR_NUMERIC, "Invalid network likelihood: negative infinity or NaN");
+  stab_tree.assign(h_tree.as<double>(), h_tree.as<double>() + (size_t)n_slots * P);
+  stab_lens = dev_len();
+  stab_probs = ret_probs;
+  stab_gen = model_gen;
+  stab_edge = e;
+  return true;
+}
+
+void netlk_ctx::sumtable_eval(int e, const double *len, int n_len, int mode, double *logl, double *d1, double *d2) {
+  const bool per_part = n_len > 1;  // one length per partition (else one for all, scaled by s_p)
+  std::vector<double> lp(P);        // each partition's length of e
+  for (int p = 0; p < P; ++p) {
+    const double t = std::min(std::max(per_part ? len[p] : len[0], 1e-6), 100.0);
+    lp[p] = !per_part && linkage == NETLK_BRLEN_SCALED ? scalers[p] * t : t;
+  }
+  if (stab_n_tab > 0) {
+    std::memcpy(h_stab_len.p, lp.data(), P * 8);
+    CUDA_OK(cudaMemcpyAsync(d_stab_len.p, h_stab_len.p, P * 8, cudaMemcpyHostToDevice, stream));
+    launch_pmat3(stream, P, R, S, d_lambda.as<double>(), d_U.as<double>(), d_Uinv.as<double>(), d_rates.as<double>(),
+                 d_stab_len.as<double>(), d_stab_pm3_64.as<double>(),
+                 opts.precision == NETLK_FP32 ? d_stab_pm3_32.as<float>() : nullptr);
+    StabParams sp = stab_params();
+    if (!launch_sumtable_eval(stream, opts.precision, R, S, sp, stab_n_tab, d_part_warp_begin.as<int32_t>(), P,
+                              d_stab_out.as<double>()))
+      throw Error(NETLK_ERR_UNSUPPORTED, "edge sumtables: unsupported state or rate count");
+    CUDA_OK(cudaMemcpyAsync(h_stab_out.p, d_stab_out.p, (size_t)stab_n_tab * P * 3 * 8, cudaMemcpyDeviceToHost,
+                            stream));
+    CUDA_OK(cudaStreamSynchronize(stream));
+    CUDA_OK(cudaGetLastError());
+  }
+  check_injected();
+  const double *out = h_stab_out.as<double>();
+  const std::vector<char> act = mode == 1 ? active_roots_of(e) : std::vector<char>(dag.roots.size(), 1);
+  double T0 = 0.0, T1 = 0.0, T2 = 0.0;
+  for (int p = 0; p < P; ++p) {
+    const double lg = parts[p].pinv > 0.0 ? parts[p].wsum * std::log(1.0 - parts[p].pinv) : 0.0;
+    auto q = [&](size_t i, int k) { return out[((size_t)stab_root_tab[i] * P + p) * 3 + k]; };
+    auto ll = [&](size_t i) {
+      return stab_root_tab[i] >= 0 ? q(i, 0) + lg : stab_tree[(size_t)root_slot[i] * P + p];
+    };
+    auto a1 = [&](size_t i) { return stab_root_tab[i] >= 0 ? q(i, 1) : 0.0; };
+    auto a2 = [&](size_t i) { return stab_root_tab[i] >= 0 ? q(i, 2) : 0.0; };
+    double L0, D1, D2;
+    if (!mix_edge(mode, act, ll, a1, a2, &L0, &D1, &D2))
+      throw Error(NETLK_ERR_NUMERIC, "no displayed tree contains the edge");
+    if (!std::isfinite(L0) || !std::isfinite(D1) || !std::isfinite(D2))
+      throw Error(NETLK_ERR_NUMERIC, "Invalid network likelihood: negative infinity or NaN");
+    if (per_part) {
+      if (logl) logl[p] = L0;
+      if (d1) d1[p] = D1;
+      if (d2) d2[p] = D2;
+    } else {
+      const double f = linkage == NETLK_BRLEN_SCALED ? scalers[p] : 1.0;
+      T0 += L0;
+      T1 += f * D1;
+      T2 += f * f * D2;
+    }
+  }
+  if (!per_part) {
+    if (logl) *logl = T0;
+    if (d1) *d1 = T1;
+    if (d2) *d2 = T2;
+  }
 }
 
 // Times every launch shape of the two sweeps once on this context's own
@@ -1980,6 +2232,7 @@ int netlk_set_model(netlk_ctx *ctx, int32_t part, const double *freqs, const dou
     pi.explicit_rates = rates != nullptr;
     if (rates) pi.rates.assign(rates, rates + ctx->R);
     ctx->model_dirty = true;
+    ++ctx->model_gen;
   });
 }
 
@@ -1991,6 +2244,7 @@ int netlk_set_prop_invar(netlk_ctx *ctx, int32_t part, double prop_invar) {
       throw Error(NETLK_ERR_INVALID_ARGUMENT, "prop_invar must lie in [0, 0.99]");
     ctx->parts[part].pinv = prop_invar;
     ctx->model_dirty = true;
+    ++ctx->model_gen;
   });
 }
 
@@ -2196,6 +2450,73 @@ int netlk_edge_derivatives_partition(netlk_ctx *ctx, int32_t edge, int32_t part,
     if (mode != 0 && mode != 1) throw Error(NETLK_ERR_INVALID_ARGUMENT, "mode must be 0 or 1");
     if (!ctx->edge_derivs_analytic(edge, mode, d1, d2, part))
       throw Error(NETLK_ERR_UNSUPPORTED, "per-partition edge derivatives need one checkpoint segment and host lengths");
+  });
+}
+
+int netlk_edge_sumtable(netlk_ctx *ctx, int32_t edge, int32_t *built, int32_t *n_tables) {
+  if (!ctx) return NETLK_ERR_INVALID_ARGUMENT;
+  return guarded(ctx, [&] {
+    if (edge < 0 || edge >= ctx->topo.n_edges) throw Error(NETLK_ERR_INVALID_ARGUMENT, "edge");
+    const bool ok = ctx->sumtable_build(edge);
+    if (built) *built = ok ? 1 : 0;
+    if (n_tables) *n_tables = ok ? ctx->stab_n_tab : 0;
+  });
+}
+
+int netlk_edge_sumtable_derivatives(netlk_ctx *ctx, int32_t edge, const double *lengths, int32_t n_lengths,
+                                    int32_t mode, double *logl, double *d1, double *d2) {
+  if (!ctx) return NETLK_ERR_INVALID_ARGUMENT;
+  return guarded(ctx, [&] {
+    const int E = ctx->topo.n_edges, P = ctx->P;
+    if (edge < 0 || edge >= E) throw Error(NETLK_ERR_INVALID_ARGUMENT, "edge");
+    if (mode != 0 && mode != 1) throw Error(NETLK_ERR_INVALID_ARGUMENT, "mode must be 0 or 1");
+    if (!lengths || !(n_lengths == 1 || (n_lengths == P && ctx->linkage == NETLK_BRLEN_UNLINKED)))
+      throw Error(NETLK_ERR_INVALID_ARGUMENT, "one length, or one per partition on an unlinked context");
+    check_finite(lengths, n_lengths, "branch length", 0.0, 1e300);
+    if (ctx->device_brlen)
+      throw Error(NETLK_ERR_UNSUPPORTED, "branch lengths are device-resident: set them on the host first");
+    if (ctx->sumtable_current(edge) || ctx->sumtable_build(edge)) {
+      ctx->sumtable_eval(edge, lengths, n_lengths, mode, logl, d1, d2);
+      return;
+    }
+    // the tangent path at the proposed length; the lengths are put back
+    // however this block is left
+    struct Restore {
+      netlk_ctx *c;
+      std::vector<double> b, pl;
+      ~Restore() {
+        c->brlen = b;
+        c->plen = pl;
+      }
+    } restore{ctx, ctx->brlen, ctx->plen};
+    auto clamp = [](double t) { return std::min(std::max(t, 1e-6), 100.0); };
+    if (n_lengths == 1) {
+      ctx->brlen[edge] = clamp(lengths[0]);
+      if (ctx->linkage == NETLK_BRLEN_UNLINKED)
+        for (int p = 0; p < P; ++p) ctx->plen[(size_t)p * E + edge] = ctx->brlen[edge];
+      else if (ctx->linkage == NETLK_BRLEN_SCALED)
+        ctx->refresh_scaled();
+    } else {
+      for (int p = 0; p < P; ++p) ctx->plen[(size_t)p * E + edge] = clamp(lengths[p]);
+    }
+    ctx->prepare();
+    if (!ctx->run_incremental()) ctx->run(&ctx->graph_logl, true, true, true, true, false);
+    double total;
+    std::vector<double> pl(P);
+    ctx->finish(&total, pl.data(), nullptr, nullptr);
+    const char *why = "edge derivatives need one checkpoint segment and host lengths";
+    if (n_lengths == 1) {
+      if (!ctx->edge_derivs_analytic(edge, mode, d1, d2)) throw Error(NETLK_ERR_UNSUPPORTED, why);
+      if (logl) *logl = total;
+    } else {
+      for (int p = 0; p < P; ++p) {
+        double a = 0.0, b = 0.0;
+        if (!ctx->edge_derivs_analytic(edge, mode, &a, &b, p)) throw Error(NETLK_ERR_UNSUPPORTED, why);
+        if (logl) logl[p] = pl[p];
+        if (d1) d1[p] = a;
+        if (d2) d2[p] = b;
+      }
+    }
   });
 }
 

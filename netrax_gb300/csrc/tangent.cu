@@ -19,6 +19,7 @@
 #include <cstdint>
 
 #include "kernels.cuh"
+#include "kernels_common.cuh"
 
 namespace netlk {
 
@@ -59,11 +60,15 @@ template <typename real>
 struct ScaleShift;
 template <>
 struct ScaleShift<float> {
+  static constexpr double kLogUnit = -0.69314718055994530942;  // log(2^-1)
   static __device__ __forceinline__ float apply(float x, int k) { return ldexpf(x, k); }
+  static __device__ __forceinline__ float log(float x) { return logf(x); }
 };
 template <>
 struct ScaleShift<double> {
+  static constexpr double kLogUnit = -177.44567822334599921;  // log(2^-256)
   static __device__ __forceinline__ double apply(double x, int k) { return ldexp(x, 256 * k); }
+  static __device__ __forceinline__ double log(double x) { return ::log(x); }
 };
 
 // S consecutive reals through the read-only path, 16 bytes at a time (S is a
@@ -294,6 +299,295 @@ __global__ void tangent_reduce_kernel(const TanParams p, const int32_t *__restri
   if (threadIdx.x == 0) out[((size_t)slot * n_parts + part) * 2 + q] = red[0];
 }
 
+// ------------------------------------------------------------ sumtables
+// P, P', P'' of P(rho_r t) = U diag(exp(lambda rho_r t)) U^-1 at t = len[part]:
+// out [part][3][R][S][S]. P follows pmatrix_kernel's arithmetic (so the
+// tables evaluated at the forward's length reproduce its P exactly), the
+// derivatives pderiv_kernel's.
+__global__ void pmat3_kernel(int n_parts, int R, int S, const double *__restrict__ lambda,
+                             const double *__restrict__ U, const double *__restrict__ Uinv,
+                             const double *__restrict__ rates, const double *__restrict__ len,
+                             double *__restrict__ out64, float *__restrict__ out32) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int SS = S * S;
+  const int64_t total = (int64_t)n_parts * 3 * R * SS;
+  if (idx >= total) return;
+  const int ij = (int)(idx % SS);
+  const int i = ij / S, j = ij - i * S;
+  const int64_t q = idx / SS;  // (part, order, rate)
+  const int rr = (int)(q % R);
+  const int order = (int)(q / R % 3);
+  const int part = (int)(q / R / 3);
+  const double rho = rates[part * R + rr];
+  const double t = len[part];
+  double v = 0.0;
+  if (order == 0) {
+    if (t == 0.0) {
+      v = i == j ? 1.0 : 0.0;
+    } else {
+      const double tr = t * rho;
+      for (int k = 0; k < S; ++k)
+        v += U[(size_t)part * SS + i * S + k] * exp(lambda[part * S + k] * tr) * Uinv[(size_t)part * SS + k * S + j];
+    }
+  } else {
+    for (int k = 0; k < S; ++k) {
+      const double lr = lambda[part * S + k] * rho;
+      const double f = order == 2 ? lr * lr : lr;
+      v += U[(size_t)part * SS + i * S + k] * f * exp(lr * t) * Uinv[(size_t)part * SS + k * S + j];
+    }
+  }
+  out64[idx] = v;
+  if (out32) out32[idx] = (float)v;
+}
+
+// Table build, one launch per level of the tangent schedule (blockIdx.y = op
+// of the level); threads as in tangent_kernel. The S unit directions of e's
+// message take the place of (X', X''): where x takes the message itself
+// (mode 1) direction i is vo_i at state i and 0 elsewhere; where x's child d
+// contains e (mode 2) it is (P_d times d's direction i) * vo; both times the
+// op's rescaling. At a displayed-tree root the thread writes its (pattern,
+// rate) row of the outside vector, O_i = w_r sum_j pi_j X_i[j], and the
+// root's scale counter.
+template <typename real, int R, int S>
+__global__ void __launch_bounds__(256, 4) sumtable_build_kernel(const StabParams sp, int op_begin) {
+  const TanParams &p = sp.t;
+  constexpr int RSS = R * S * S;
+  constexpr int ROWS = 256 / R;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  real *sMo = reinterpret_cast<real *>(smem_raw);
+  real *sMd = sMo + RSS, *sPi = sMd + RSS, *sRw = sPi + S;
+  const TanOp op = p.ops[op_begin + blockIdx.y];
+  const int part = p.block_part[blockIdx.x];
+  const real *pm = static_cast<const real *>(p.pmat) + (size_t)part * p.n_edges * RSS;
+  for (int i = threadIdx.x; i < RSS; i += blockDim.x) {
+    sMo[i] = op.eo >= 0 ? __ldg(pm + (size_t)op.eo * RSS + i) : (real)0;
+    sMd[i] = op.mode == 2 ? __ldg(pm + (size_t)op.ed * RSS + i) : (real)0;
+  }
+  if (threadIdx.x < S) sPi[threadIdx.x] = (real)p.freqs[part * S + threadIdx.x];
+  if (threadIdx.x < R) sRw[threadIdx.x] = (real)p.rate_weights[part * R + threadIdx.x];
+  __syncthreads();
+  const int r = threadIdx.x % R;
+  const size_t plane = (size_t)p.n_patterns * R * S;
+  const real *Mo = sMo + r * S * S, *Md = sMd + r * S * S;
+  const real *dsrc = static_cast<const real *>(p.tan) + (size_t)(op.td < 0 ? 0 : op.td) * S * plane;
+  real *ddst = static_cast<real *>(p.tan) + (size_t)(op.tx < 0 ? 0 : op.tx) * S * plane;
+#pragma unroll
+  for (int q = 0; q < kTanPPT; ++q) {
+    const int64_t s = ((int64_t)blockIdx.x * kTanPPT + q) * ROWS + threadIdx.x / R;
+    const size_t row = ((size_t)s * R + r) * S;
+    real c[S], vo[S], o[S];
+    const int so = load_row<real, R, S>(p, op.o, s, r, c);
+    if (op.o == INT32_MIN) {
+#pragma unroll
+      for (int i = 0; i < S; ++i) vo[i] = (real)1;
+    } else {
+      matvec<real, S>(Mo, c, vo);
+    }
+    const int sd = op.d >= 0 ? __ldg(p.scaler + (size_t)op.d * p.n_patterns + s) : 0;
+    const int sx = __ldg(p.scaler + (size_t)op.x * p.n_patterns + s);
+    const int k = sx - sd - so;
+#pragma unroll
+    for (int i = 0; i < S; ++i) {
+      real t[S];
+      if (op.mode == 1) {
+#pragma unroll
+        for (int j = 0; j < S; ++j) t[j] = j == i ? ScaleShift<real>::apply(vo[j], k) : (real)0;
+      } else {
+        ldg_row<real, S>(dsrc + i * plane + row, c);
+        matvec<real, S>(Md, c, t);
+#pragma unroll
+        for (int j = 0; j < S; ++j) t[j] = ScaleShift<real>::apply(t[j] * vo[j], k);
+      }
+      if (op.tx >= 0) st_row<real, S>(ddst + i * plane + row, t);
+      real a = (real)0;
+#pragma unroll
+      for (int j = 0; j < S; ++j) a = fma(sPi[j], t[j], a);
+      o[i] = a * sRw[r];
+    }
+    if (op.slot < 0) continue;  // uniform over the block
+    st_row<real, S>(static_cast<real *>(sp.table) + ((size_t)op.slot * p.n_patterns + s) * R * S + r * S, o);
+    if (r == 0) sp.table_scaler[(size_t)op.slot * p.n_patterns + s] = sx;
+  }
+}
+
+// One table's site terms for the thread's pattern s (site likelihood L and
+// its derivatives L1, L2 in the table's scaled units), summed over the warp
+// into partial[table][q][warp].
+template <typename real>
+__device__ __forceinline__ void sumtable_site_terms(const StabParams &sp, int tb, int64_t s, double w, real iq,
+                                                    real L, real L1, real L2) {
+  const int64_t n_warps = sp.t.n_patterns / 32, gw = s / 32;
+  const bool lead = (threadIdx.x & 31) == 0;
+  if constexpr (sizeof(real) == 4) {
+    // FP32 sweeps: per-site terms and the warp sums in FP32 (the log term as
+    // a float-float pair), stored as float pairs in the partial's 8 bytes:
+    // no FP64 instruction per table
+    float v0 = 0.f, v1 = 0.f, v2 = 0.f;
+    const float wf = (float)w;
+    if (wf != 0.f) {
+      const int k = __ldg(sp.table_scaler + (size_t)tb * sp.t.n_patterns + s);
+      if (iq > 0.f) L += ldexpf(iq, k);
+      const float inv = 1.0f / L, q1 = L1 * inv, q2 = L2 * inv;
+      v0 = wf * (logf(L) + (float)k * (float)ScaleShift<float>::kLogUnit);
+      v1 = wf * q1;
+      v2 = wf * (q2 - q1 * q1);
+    }
+    const FF f0 = warp_sum_ff(FF{v0, 0.f});
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      v1 += __shfl_xor_sync(0xffffffffu, v1, o);
+      v2 += __shfl_xor_sync(0xffffffffu, v2, o);
+    }
+    if (lead) {
+      float2 *dst = reinterpret_cast<float2 *>(sp.partial);
+      dst[((size_t)tb * 3 + 0) * n_warps + gw] = make_float2(f0.hi, f0.lo);
+      dst[((size_t)tb * 3 + 1) * n_warps + gw] = make_float2(v1, 0.f);
+      dst[((size_t)tb * 3 + 2) * n_warps + gw] = make_float2(v2, 0.f);
+    }
+  } else {
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+    if (w != 0.0) {
+      const int k = __ldg(sp.table_scaler + (size_t)tb * sp.t.n_patterns + s);
+      if (iq > (real)0) L += ScaleShift<real>::apply(iq, k);
+      const real q1 = L1 / L, q2 = L2 / L;
+      a0 = w * ((double)ScaleShift<real>::log(L) + (double)k * ScaleShift<real>::kLogUnit);
+      a1 = w * (double)q1;
+      a2 = w * ((double)q2 - (double)q1 * (double)q1);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a0 += __shfl_down_sync(0xffffffffu, a0, o);
+      a1 += __shfl_down_sync(0xffffffffu, a1, o);
+      a2 += __shfl_down_sync(0xffffffffu, a2, o);
+    }
+    if (lead) {
+      sp.partial[((size_t)tb * 3 + 0) * n_warps + gw] = a0;
+      sp.partial[((size_t)tb * 3 + 1) * n_warps + gw] = a1;
+      sp.partial[((size_t)tb * 3 + 2) * n_warps + gw] = a2;
+    }
+  }
+}
+
+// Table evaluation: one thread per pattern, 128 per block (a partition's
+// padding unit, 1024 / R patterns, is a multiple of 128, so a block never
+// spans two), blockIdx.y = a run of tables_per_block tables (enough blocks
+// to fill the GPU whatever the pattern count). Per child group the thread
+// forms m = P I, m' = P' I and
+// m'' = P'' I for its R rates once, then per table of the group L, L', L''
+// (dot products with the table's rows), the site's w log L (with the
+// table's scale counter and the +I term) and w L'/L, w (L''/L - (L'/L)^2);
+// the warp's sums go to partial[table][q][warp] (fixed order; FP32 tables:
+// float pairs whose sum is the value).
+template <typename real, int R, int S>
+__global__ void __launch_bounds__(128) sumtable_eval_kernel(const StabParams sp) {
+  const TanParams &p = sp.t;
+  constexpr int RSS = R * S * S;
+  __shared__ __align__(16) real sM[3 * RSS];
+  const int64_t s = (int64_t)blockIdx.x * 128 + threadIdx.x;
+  const int part = p.block_part[(blockIdx.x * 128) / (kTanPPT * 256 / R)];
+  const real *src = static_cast<const real *>(sp.pm3) + (size_t)part * 3 * RSS;
+  for (int i = threadIdx.x; i < 3 * RSS; i += blockDim.x) sM[i] = src[i];
+  __syncthreads();
+  const double w = __ldg(p.weights + s);
+  const real iq = p.inv_term ? (real)p.inv_term[s] : (real)0;
+  const int tb_lo = blockIdx.y * sp.tables_per_block, tb_hi = tb_lo + sp.tables_per_block;
+  for (int g = 0; g < sp.n_groups; ++g) {
+    const int g_lo = max(sp.group_begin[g], tb_lo), g_hi = min(sp.group_begin[g + 1], tb_hi);
+    if (g_lo >= g_hi) continue;  // uniform over the block
+    real m0[R][S], m1[R][S], m2[R][S];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      real c[S];
+      load_row<real, R, S>(p, sp.group_ref[g], s, r, c);
+      matvec<real, S>(sM + r * S * S, c, m0[r]);
+      matvec<real, S>(sM + RSS + r * S * S, c, m1[r]);
+      matvec<real, S>(sM + 2 * RSS + r * S * S, c, m2[r]);
+    }
+    // two tables per step: both tables' rows are in flight before either
+    // is reduced (tb2 == tb on a run's odd last table)
+    for (int tb = g_lo; tb < g_hi; tb += 2) {
+      const int tb2 = min(tb + 1, g_hi - 1);
+      real oa[R][S], ob[R][S];
+      const real *rowa = static_cast<const real *>(sp.table) + ((size_t)tb * p.n_patterns + s) * R * S;
+      const real *rowb = static_cast<const real *>(sp.table) + ((size_t)tb2 * p.n_patterns + s) * R * S;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        ldg_row<real, S>(rowa + r * S, oa[r]);
+        ldg_row<real, S>(rowb + r * S, ob[r]);
+      }
+      real La = 0, La1 = 0, La2 = 0, Lb = 0, Lb1 = 0, Lb2 = 0;
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+#pragma unroll
+        for (int i = 0; i < S; ++i) {
+          La = fma(oa[r][i], m0[r][i], La);
+          La1 = fma(oa[r][i], m1[r][i], La1);
+          La2 = fma(oa[r][i], m2[r][i], La2);
+          Lb = fma(ob[r][i], m0[r][i], Lb);
+          Lb1 = fma(ob[r][i], m1[r][i], Lb1);
+          Lb2 = fma(ob[r][i], m2[r][i], Lb2);
+        }
+      sumtable_site_terms<real>(sp, tb, s, w, iq, La, La1, La2);
+      if (tb2 != tb) sumtable_site_terms<real>(sp, tb2, s, w, iq, Lb, Lb1, Lb2);  // uniform over the block
+    }
+  }
+}
+
+// out[(table * n_parts + part) * 3 + q] = compensated sum of the table's warp
+// partials over the partition's warps.
+__global__ void sumtable_reduce_kernel(const double *__restrict__ partial, int64_t n_warps,
+                                       const int32_t *__restrict__ part_warp_begin, int n_parts,
+                                       double *__restrict__ out, int ff) {
+  const int tb = blockIdx.x, part = blockIdx.y, q = blockIdx.z;
+  const int b0 = part_warp_begin[part], b1 = part_warp_begin[part + 1];
+  const double *src = partial + ((size_t)tb * 3 + q) * n_warps;
+  const float2 *src32 = reinterpret_cast<const float2 *>(src);
+  double s = 0.0, c = 0.0;
+  for (int b = b0 + threadIdx.x; b < b1; b += blockDim.x) {
+    const double v = ff ? (double)src32[b].x + (double)src32[b].y : src[b];
+    const double y = v - c;
+    const double t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __shared__ double red[128];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[((size_t)tb * n_parts + part) * 3 + q] = red[0];
+}
+
+template <typename real, int R, int S>
+void run_sumtable(cudaStream_t st, const StabParams &p, const int32_t *level_begin, int n_levels) {
+  const size_t smem = (2 * (size_t)R * S * S + S + R) * sizeof(real);
+  for (int L = 0; L < n_levels; ++L) {
+    const int n = level_begin[L + 1] - level_begin[L];
+    if (n > 0) sumtable_build_kernel<real, R, S><<<dim3(p.t.n_blocks, n), 256, smem, st>>>(p, level_begin[L]);
+  }
+}
+
+template <typename real, int R, int S>
+void run_sumtable_eval(cudaStream_t st, const StabParams &p) {
+  const unsigned ny = (unsigned)((p.n_tables + p.tables_per_block - 1) / p.tables_per_block);
+  sumtable_eval_kernel<real, R, S><<<dim3((unsigned)(p.t.n_patterns / 128), ny), 128, 0, st>>>(p);
+}
+
+template <typename real>
+bool dispatch_sumtable(cudaStream_t st, int R, int S, const StabParams &p, const int32_t *level_begin, int n_levels,
+                       bool eval) {
+  if (S != 4) return false;
+  switch (R) {
+    case 1: eval ? run_sumtable_eval<real, 1, 4>(st, p) : run_sumtable<real, 1, 4>(st, p, level_begin, n_levels); return true;
+    case 2: eval ? run_sumtable_eval<real, 2, 4>(st, p) : run_sumtable<real, 2, 4>(st, p, level_begin, n_levels); return true;
+    case 4: eval ? run_sumtable_eval<real, 4, 4>(st, p) : run_sumtable<real, 4, 4>(st, p, level_begin, n_levels); return true;
+    case 8: eval ? run_sumtable_eval<real, 8, 4>(st, p) : run_sumtable<real, 8, 4>(st, p, level_begin, n_levels); return true;
+    default: return false;
+  }
+}
+
 template <typename real, int R, int S>
 void run_levels(cudaStream_t st, const TanParams &p, const int32_t *level_begin, int n_levels) {
   const size_t smem = (3 * (size_t)R * S * S + S + R) * sizeof(real);
@@ -352,6 +646,35 @@ void launch_tangent_reduce(cudaStream_t s, const TanParams &p, const int32_t *sl
   if (n_slots <= 0) return;
   tangent_reduce_kernel<<<dim3(n_slots, n_parts, 2), 128, 0, s>>>(p, slots, part_block_begin, n_parts, out);
   add_launches(1);
+}
+
+bool launch_sumtable_build(cudaStream_t s, int precision, int R, int S, const StabParams &p,
+                           const int32_t *level_begin, int n_levels) {
+  const bool ok = precision == 1 ? dispatch_sumtable<float>(s, R, S, p, level_begin, n_levels, false)
+                                 : dispatch_sumtable<double>(s, R, S, p, level_begin, n_levels, false);
+  if (ok)
+    for (int L = 0; L < n_levels; ++L) add_launches(level_begin[L + 1] > level_begin[L]);
+  return ok;
+}
+
+void launch_pmat3(cudaStream_t s, int n_parts, int R, int S, const double *lambda, const double *U,
+                  const double *Uinv, const double *rates, const double *len, double *out64, float *out32) {
+  const int64_t total = (int64_t)n_parts * 3 * R * S * S;
+  pmat3_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(n_parts, R, S, lambda, U, Uinv, rates, len, out64,
+                                                               out32);
+  add_launches(1);
+}
+
+bool launch_sumtable_eval(cudaStream_t s, int precision, int R, int S, const StabParams &p, int n_tab,
+                          const int32_t *part_warp_begin, int n_parts, double *out) {
+  if (n_tab <= 0) return true;
+  const bool ok = precision == 1 ? dispatch_sumtable<float>(s, R, S, p, nullptr, 0, true)
+                                 : dispatch_sumtable<double>(s, R, S, p, nullptr, 0, true);
+  if (!ok) return false;
+  sumtable_reduce_kernel<<<dim3(n_tab, n_parts, 3), 128, 0, s>>>(p.partial, p.t.n_patterns / 32, part_warp_begin,
+                                                                  n_parts, out, precision == 1);
+  add_launches(2);
+  return true;
 }
 
 }  // namespace netlk

@@ -185,6 +185,27 @@ class NetworkLikelihood:
                                                          ctypes.byref(d2)), self._h)
         return d1.value, d2.value
 
+    def edge_sumtable(self, edge):
+        """Builds the edge's sumtables now: (built, number of tables); built
+        is False where that path does not apply (evaluations then take the
+        tangent path)."""
+        built, n_tab = ctypes.c_int32(), ctypes.c_int32()
+        N.check(N.lib().netlk_edge_sumtable(self._h, int(edge), ctypes.byref(built), ctypes.byref(n_tab)), self._h)
+        return bool(built.value), n_tab.value
+
+    def edge_sumtable_derivatives(self, edge, length, mode=0):
+        """(logL, d1, d2) with ``edge`` at ``length``, the context unchanged:
+        one length -> totals; one length per partition (unlinked) -> arrays."""
+        lens = np.atleast_1d(np.asarray(length, dtype=np.float64))
+        n = lens.size
+        out = [np.zeros(n) for _ in range(3)]
+        N.check(N.lib().netlk_edge_sumtable_derivatives(self._h, int(edge), _ptr(lens, ctypes.c_double), n,
+                                                        int(mode), *[_ptr(o, ctypes.c_double) for o in out]),
+                self._h)
+        if np.ndim(length) == 0:
+            return tuple(float(o[0]) for o in out)
+        return tuple(out)
+
     def set_prop_invar(self, part, prop_invar):
         """Proportion of invariant sites (+I) of one partition."""
         N.check(N.lib().netlk_set_prop_invar(self._h, int(part), float(prop_invar)), self._h)

@@ -108,10 +108,13 @@ def brent_minimize(f, a, b, x0, tol, max_iters=200):
     return x, fx
 
 
-def optimize_branches(edge_logl, edge_derivs, lengths, max_iters=30):
+def optimize_branches(edge_logl, edge_derivs, lengths, max_iters=30, derivs_at=None):
     """One pass over every edge. edge_logl(e, t): logL with edge e at length
-    t (kept); edge_derivs(e): (d1, d2) at the current lengths. Returns the
-    final lengths and logL, and whether any step lowered the logL."""
+    t (kept); edge_derivs(e): (d1, d2) at the current lengths; or
+    derivs_at(e, t): (d1, d2) with edge e at t, nothing kept (the
+    reference's callback on sumtables, which only invalidates the edge's
+    P-matrix). Returns the final lengths and logL, and whether any step
+    lowered the logL."""
     lengths = list(lengths)
     logl = None
     worse = False
@@ -120,6 +123,8 @@ def optimize_branches(edge_logl, edge_derivs, lengths, max_iters=30):
         start = edge_logl(e, t0)
 
         def derivs(t, e=e):
+            if derivs_at is not None:
+                return derivs_at(e, t)
             edge_logl(e, t)
             return edge_derivs(e)
 
