@@ -263,7 +263,7 @@ void launch_tangent_reduce(cudaStream_t s, const TanParams &p, const int32_t *sl
 // cancel there).
 struct StabParams {
   TanParams t;                  // t.tan: [n_work][S][N][R][S] unit-direction planes; t.ops' slot = table index
-  void *table;                  // [n_tab][N][R][S] real: O per (table, pattern, rate)
+  void *table;                  // [n_tab][N / 128][R][128][S] real: O per (table, pattern, rate)
   int32_t *table_scaler;        // [n_tab][N]: the root's scale counter when the table was built
   const double *U;              // [n_parts][S][S] eigenvectors (unused by the evaluation)
   const void *pm3;              // [n_parts][3][R][S][S] real: P, P', P'' at the evaluated lengths
@@ -271,6 +271,7 @@ struct StabParams {
   const int32_t *group_begin;   // [n_groups + 1] tables of each group (tables sorted by child)
   int32_t n_groups;
   int32_t n_tables, tables_per_block;  // evaluation: tables, and tables per block (blockIdx.y)
+  int32_t *fault;                      // set to 1 by an evaluation whose bounded wait gave up
   double *partial;              // [n_tab][3][N / 32] per-warp sums of w log L, w L'/L, w (L''/L - (L'/L)^2); FP32: float pairs
 };
 

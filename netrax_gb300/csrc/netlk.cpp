@@ -396,6 +396,7 @@ struct netlk_ctx {
     // at least 4 tables per block (the child's P I is formed once per block)
     sp.tables_per_block = std::max(4, (int)((int64_t)stab_n_tab * (N / 128) / (152 * 16) + 1));
     sp.partial = d_stab_partial.as<double>();
+    sp.fault = reinterpret_cast<int32_t *>(d_stab_out.as<double>() + (size_t)std::max(1, stab_cap_tab) * P * 3);
     return sp;
   }
   // Per-partition mixture of per-tree (l, l', l'') along edge e: logL of the
@@ -1587,7 +1588,7 @@ bool netlk_ctx::sumtable_build(int e) {
     d_stab.alloc(std::max<size_t>(1, (size_t)tabs) * plane, scratch);
     d_stab_scaler.alloc(std::max<size_t>(1, (size_t)tabs) * N * 4, scratch);
     d_stab_partial.alloc(std::max<size_t>(1, (size_t)tabs) * 3 * (N / 32) * 8, scratch);
-    d_stab_out.alloc(std::max<size_t>(1, (size_t)tabs) * P * 3 * 8, scratch);
+    d_stab_out.alloc((std::max<size_t>(1, (size_t)tabs) * P * 3 + 1) * 8, scratch);  // + the fault word
     d_stab_pm3_64.alloc((size_t)P * 3 * R * S * S * 8, scratch);
     d_stab_pm3_32.alloc((size_t)P * 3 * R * S * S * 4, scratch);
     d_stab_len.alloc((size_t)P * 8, scratch);
@@ -1596,7 +1597,7 @@ bool netlk_ctx::sumtable_build(int e) {
     d_part_warp_begin.alloc((size_t)(P + 1) * 4, scratch);
     dev_bytes += scratch;
     h_stab_len.alloc((size_t)P * 8);
-    h_stab_out.alloc(std::max<size_t>(1, (size_t)tabs) * P * 3 * 8);
+    h_stab_out.alloc((std::max<size_t>(1, (size_t)tabs) * P * 3 + 1) * 8);
     h_stab_ops.alloc(dag.vars.size() * sizeof(TanOp) + (size_t)(2 * tabs + 2) * 4);
     std::vector<int32_t> pwb(P + 1);
     for (int p = 0; p < P; ++p) pwb[p] = (int32_t)(parts[p].offset / 32);
@@ -1681,13 +1682,17 @@ void netlk_ctx::sumtable_eval(int e, const double *len, int n_len, int mode, dou
                  d_stab_len.as<double>(), d_stab_pm3_64.as<double>(),
                  opts.precision == NETLK_FP32 ? d_stab_pm3_32.as<float>() : nullptr);
     StabParams sp = stab_params();
+    CUDA_OK(cudaMemsetAsync(sp.fault, 0, 8, stream));
     if (!launch_sumtable_eval(stream, opts.precision, R, S, sp, stab_n_tab, d_part_warp_begin.as<int32_t>(), P,
                               d_stab_out.as<double>()))
       throw Error(NETLK_ERR_UNSUPPORTED, "edge sumtables: unsupported state or rate count");
-    CUDA_OK(cudaMemcpyAsync(h_stab_out.p, d_stab_out.p, (size_t)stab_n_tab * P * 3 * 8, cudaMemcpyDeviceToHost,
-                            stream));
+    const size_t nb = (size_t)stab_n_tab * P * 3 * 8;
+    CUDA_OK(cudaMemcpyAsync(h_stab_out.p, d_stab_out.p, nb, cudaMemcpyDeviceToHost, stream));
+    int32_t fault = 0;
+    CUDA_OK(cudaMemcpyAsync(&fault, sp.fault, 4, cudaMemcpyDeviceToHost, stream));
     CUDA_OK(cudaStreamSynchronize(stream));
     CUDA_OK(cudaGetLastError());
+    if (fault) throw Error(NETLK_ERR_TIMEOUT, "edge sumtable evaluation: a bulk-copy wait timed out");
   }
   check_injected();
   const double *out = h_stab_out.as<double>();

@@ -20,6 +20,7 @@
 
 #include "kernels.cuh"
 #include "kernels_common.cuh"
+#include "tc.cuh"
 
 namespace netlk {
 
@@ -405,7 +406,11 @@ __global__ void __launch_bounds__(256, 4) sumtable_build_kernel(const StabParams
       o[i] = a * sRw[r];
     }
     if (op.slot < 0) continue;  // uniform over the block
-    st_row<real, S>(static_cast<real *>(sp.table) + ((size_t)op.slot * p.n_patterns + s) * R * S + r * S, o);
+    // table layout [table][pattern / 128][rate][pattern % 128][S]: one
+    // contiguous chunk per (table, 128 patterns), rate-major inside
+    st_row<real, S>(static_cast<real *>(sp.table) + ((size_t)op.slot * p.n_patterns + (s & ~(int64_t)127)) * R * S +
+                        ((size_t)r * 128 + (s & 127)) * S,
+                    o);
     if (r == 0) sp.table_scaler[(size_t)op.slot * p.n_patterns + s] = sx;
   }
 }
@@ -415,7 +420,7 @@ __global__ void __launch_bounds__(256, 4) sumtable_build_kernel(const StabParams
 // into partial[table][q][warp].
 template <typename real>
 __device__ __forceinline__ void sumtable_site_terms(const StabParams &sp, int tb, int64_t s, double w, real iq,
-                                                    real L, real L1, real L2) {
+                                                    int k, real L, real L1, real L2) {
   const int64_t n_warps = sp.t.n_patterns / 32, gw = s / 32;
   const bool lead = (threadIdx.x & 31) == 0;
   if constexpr (sizeof(real) == 4) {
@@ -425,7 +430,6 @@ __device__ __forceinline__ void sumtable_site_terms(const StabParams &sp, int tb
     float v0 = 0.f, v1 = 0.f, v2 = 0.f;
     const float wf = (float)w;
     if (wf != 0.f) {
-      const int k = __ldg(sp.table_scaler + (size_t)tb * sp.t.n_patterns + s);
       if (iq > 0.f) L += ldexpf(iq, k);
       const float inv = 1.0f / L, q1 = L1 * inv, q2 = L2 * inv;
       v0 = wf * (logf(L) + (float)k * (float)ScaleShift<float>::kLogUnit);
@@ -447,7 +451,6 @@ __device__ __forceinline__ void sumtable_site_terms(const StabParams &sp, int tb
   } else {
     double a0 = 0.0, a1 = 0.0, a2 = 0.0;
     if (w != 0.0) {
-      const int k = __ldg(sp.table_scaler + (size_t)tb * sp.t.n_patterns + s);
       if (iq > (real)0) L += ScaleShift<real>::apply(iq, k);
       const real q1 = L1 / L, q2 = L2 / L;
       a0 = w * ((double)ScaleShift<real>::log(L) + (double)k * ScaleShift<real>::kLogUnit);
@@ -471,65 +474,120 @@ __device__ __forceinline__ void sumtable_site_terms(const StabParams &sp, int tb
 // Table evaluation: one thread per pattern, 128 per block (a partition's
 // padding unit, 1024 / R patterns, is a multiple of 128, so a block never
 // spans two), blockIdx.y = a run of tables_per_block tables (enough blocks
-// to fill the GPU whatever the pattern count). Per child group the thread
-// forms m = P I, m' = P' I and
-// m'' = P'' I for its R rates once, then per table of the group L, L', L''
-// (dot products with the table's rows), the site's w log L (with the
-// table's scale counter and the +I term) and w L'/L, w (L''/L - (L'/L)^2);
-// the warp's sums go to partial[table][q][warp] (fixed order; FP32 tables:
-// float pairs whose sum is the value).
+// to fill the GPU whatever the pattern count). A table's rows for the
+// block's 128 patterns are one contiguous 128 R S-real chunk, its scale
+// counters one 512-byte chunk: thread 0 streams both into a ring of
+// kEvalStages shared-memory stages with cp.async.bulk (completion on the
+// stage's mbarrier), so several tables per block are in flight while the
+// threads reduce an earlier one. Per child group the threads form
+// m = P I, m' = P' I and m'' = P'' I for their R rates once, then per table
+// L, L', L'' (dot products with the table's rows), the site's w log L (with
+// the table's scale counter and the +I term) and w L'/L, w (L''/L -
+// (L'/L)^2); the warp's sums go to partial[table][q][warp] (fixed order;
+// FP32 tables: float pairs whose sum is the value). Every mbarrier wait is
+// bounded: past about a second the block sets *fault, waits (bounded) for
+// its copies in flight and returns.
+template <typename real, int R>
+__host__ __device__ constexpr int eval_stages() {
+  return 128 * R * 4 * (int)sizeof(real) <= 8192 ? 4 : 2;
+}
+
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void *src, uint32_t bytes, uint32_t mbar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(mbar)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect(uint32_t mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+
 template <typename real, int R, int S>
 __global__ void __launch_bounds__(128) sumtable_eval_kernel(const StabParams sp) {
   const TanParams &p = sp.t;
   constexpr int RSS = R * S * S;
-  __shared__ __align__(16) real sM[3 * RSS];
-  const int64_t s = (int64_t)blockIdx.x * 128 + threadIdx.x;
-  const int part = p.block_part[(blockIdx.x * 128) / (kTanPPT * 256 / R)];
+  constexpr int K = eval_stages<real, R>();
+  constexpr uint32_t kRows = 128 * R * S * sizeof(real), kSc = 128 * 4;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  real *stage_rows = reinterpret_cast<real *>(smem_raw);                          // [K][128][R][S]
+  int32_t *stage_sc = reinterpret_cast<int32_t *>(smem_raw + K * kRows);          // [K][128]
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw + K * (kRows + kSc));    // [K]
+  real *sM = reinterpret_cast<real *>(smem_raw + K * (kRows + kSc) + 8 * K);      // [3][R][S][S]
+  const int64_t x0 = (int64_t)blockIdx.x * 128, s = x0 + threadIdx.x;
+  const int part = p.block_part[x0 / (kTanPPT * 256 / R)];
   const real *src = static_cast<const real *>(sp.pm3) + (size_t)part * 3 * RSS;
   for (int i = threadIdx.x; i < 3 * RSS; i += blockDim.x) sM[i] = src[i];
+  const int tb_lo = blockIdx.y * sp.tables_per_block;
+  const int tb_end = min(tb_lo + sp.tables_per_block, sp.n_tables);
+  const int n = tb_end - tb_lo;  // tables of this block, streamed in order
+  const uint32_t bar0 = (uint32_t)__cvta_generic_to_shared(bars);
+  const uint32_t rows0 = (uint32_t)__cvta_generic_to_shared(stage_rows);
+  const uint32_t sc0 = (uint32_t)__cvta_generic_to_shared(stage_sc);
+  auto issue = [&](int j) {  // thread 0: table tb_lo + j into stage j % K
+    const int st = j % K;
+    const size_t tb = (size_t)(tb_lo + j);
+    mbar_expect(bar0 + 8 * st, kRows + kSc);
+    bulk_load(rows0 + st * kRows, static_cast<const real *>(sp.table) + (tb * p.n_patterns + x0) * R * S, kRows,
+              bar0 + 8 * st);
+    bulk_load(sc0 + st * kSc, sp.table_scaler + tb * p.n_patterns + x0, kSc, bar0 + 8 * st);
+  };
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < K; ++st) tc::mbar_init(bar0 + 8 * st, 1);
+    for (int j = 0; j < min(K, n); ++j) issue(j);
+  }
   __syncthreads();
   const double w = __ldg(p.weights + s);
   const real iq = p.inv_term ? (real)p.inv_term[s] : (real)0;
-  const int tb_lo = blockIdx.y * sp.tables_per_block, tb_hi = tb_lo + sp.tables_per_block;
-  for (int g = 0; g < sp.n_groups; ++g) {
-    const int g_lo = max(sp.group_begin[g], tb_lo), g_hi = min(sp.group_begin[g + 1], tb_hi);
-    if (g_lo >= g_hi) continue;  // uniform over the block
-    real m0[R][S], m1[R][S], m2[R][S];
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      real c[S];
-      load_row<real, R, S>(p, sp.group_ref[g], s, r, c);
-      matvec<real, S>(sM + r * S * S, c, m0[r]);
-      matvec<real, S>(sM + RSS + r * S * S, c, m1[r]);
-      matvec<real, S>(sM + 2 * RSS + r * S * S, c, m2[r]);
-    }
-    // two tables per step: both tables' rows are in flight before either
-    // is reduced (tb2 == tb on a run's odd last table)
-    for (int tb = g_lo; tb < g_hi; tb += 2) {
-      const int tb2 = min(tb + 1, g_hi - 1);
-      real oa[R][S], ob[R][S];
-      const real *rowa = static_cast<const real *>(sp.table) + ((size_t)tb * p.n_patterns + s) * R * S;
-      const real *rowb = static_cast<const real *>(sp.table) + ((size_t)tb2 * p.n_patterns + s) * R * S;
+  int g = 0;
+  while (g < sp.n_groups && sp.group_begin[g + 1] <= tb_lo) ++g;
+  real m0[R][S], m1[R][S], m2[R][S];
+  int g_end = -1;  // first table past the group m0..m2 belong to
+  for (int j = 0; j < n; ++j) {
+    const int tb = tb_lo + j;
+    if (tb >= g_end) {  // uniform over the block
+      while (sp.group_begin[g + 1] <= tb) ++g;
+      g_end = sp.group_begin[g + 1];
 #pragma unroll
       for (int r = 0; r < R; ++r) {
-        ldg_row<real, S>(rowa + r * S, oa[r]);
-        ldg_row<real, S>(rowb + r * S, ob[r]);
+        real c[S];
+        load_row<real, R, S>(p, sp.group_ref[g], s, r, c);
+        matvec<real, S>(sM + r * S * S, c, m0[r]);
+        matvec<real, S>(sM + RSS + r * S * S, c, m1[r]);
+        matvec<real, S>(sM + 2 * RSS + r * S * S, c, m2[r]);
       }
-      real La = 0, La1 = 0, La2 = 0, Lb = 0, Lb1 = 0, Lb2 = 0;
-#pragma unroll
-      for (int r = 0; r < R; ++r)
-#pragma unroll
-        for (int i = 0; i < S; ++i) {
-          La = fma(oa[r][i], m0[r][i], La);
-          La1 = fma(oa[r][i], m1[r][i], La1);
-          La2 = fma(oa[r][i], m2[r][i], La2);
-          Lb = fma(ob[r][i], m0[r][i], Lb);
-          Lb1 = fma(ob[r][i], m1[r][i], Lb1);
-          Lb2 = fma(ob[r][i], m2[r][i], Lb2);
-        }
-      sumtable_site_terms<real>(sp, tb, s, w, iq, La, La1, La2);
-      if (tb2 != tb) sumtable_site_terms<real>(sp, tb2, s, w, iq, Lb, Lb1, Lb2);  // uniform over the block
     }
+    const int st = j % K;
+    const bool ok = tc::mbar_wait(bar0 + 8 * st, (uint32_t)((j / K) & 1));
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) {
+        *sp.fault = 1;
+        for (int q = j; q < min(j + K, n); ++q) (void)tc::mbar_wait(bar0 + 8 * (q % K), (uint32_t)((q / K) & 1));
+      }
+      return;  // uniform over the block
+    }
+    // the thread's rows: rate r of the chunk's 128 patterns are contiguous,
+    // so a warp's reads of one rate cover consecutive 16-byte pieces
+    const real *chunk = stage_rows + (size_t)st * 128 * R * S;
+    real L = 0, L1 = 0, L2 = 0;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      real o[S];
+#pragma unroll
+      for (int i = 0; i < S; ++i) o[i] = chunk[((size_t)r * 128 + threadIdx.x) * S + i];
+#pragma unroll
+      for (int i = 0; i < S; ++i) {
+        L = fma(o[i], m0[r][i], L);
+        L1 = fma(o[i], m1[r][i], L1);
+        L2 = fma(o[i], m2[r][i], L2);
+      }
+    }
+    const int k = stage_sc[st * 128 + threadIdx.x];
+    __syncthreads();  // every thread is done with stage st
+    if (threadIdx.x == 0 && j + K < n) {
+      tc::fence_proxy_async();
+      issue(j + K);
+    }
+    sumtable_site_terms<real>(sp, tb, s, w, iq, k, L, L1, L2);
   }
 }
 
@@ -571,8 +629,15 @@ void run_sumtable(cudaStream_t st, const StabParams &p, const int32_t *level_beg
 
 template <typename real, int R, int S>
 void run_sumtable_eval(cudaStream_t st, const StabParams &p) {
+  constexpr int K = eval_stages<real, R>();
+  const size_t smem = K * (128 * R * S * sizeof(real) + 128 * 4) + 8 * K + 3 * R * S * S * sizeof(real);
+  static bool attr = false;  // once per instantiation: more than 48 KB for the larger (R, precision)
+  if (!attr) {
+    cudaFuncSetAttribute(sumtable_eval_kernel<real, R, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr = true;
+  }
   const unsigned ny = (unsigned)((p.n_tables + p.tables_per_block - 1) / p.tables_per_block);
-  sumtable_eval_kernel<real, R, S><<<dim3((unsigned)(p.t.n_patterns / 128), ny), 128, 0, st>>>(p);
+  sumtable_eval_kernel<real, R, S><<<dim3((unsigned)(p.t.n_patterns / 128), ny), 128, smem, st>>>(p);
 }
 
 template <typename real>
