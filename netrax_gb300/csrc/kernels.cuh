@@ -265,8 +265,7 @@ struct StabParams {
   TanParams t;                  // t.tan: [n_work][S][N][R][S] unit-direction planes; t.ops' slot = table index
   void *table;                  // [n_tab][N / 128][R][128][S] real: O per (table, pattern, rate)
   int32_t *table_scaler;        // [n_tab][N]: the root's scale counter when the table was built
-  const double *U;              // [n_parts][S][S] eigenvectors (unused by the evaluation)
-  const void *pm3;              // [n_parts][3][R][S][S] real: P, P', P'' at the evaluated lengths
+  const void *pm3;              // [n_parts][3][R][S][S] real: P, P', P'' at the evaluated lengths (host-made)
   const int32_t *group_ref;     // [n_groups] child ref (as FwdOp) whose CLV is I for the group's tables
   const int32_t *group_begin;   // [n_groups + 1] tables of each group (tables sorted by child)
   int32_t n_groups;
@@ -279,9 +278,9 @@ struct StabParams {
 // for an unsupported (R, S): DNA only.
 bool launch_sumtable_build(cudaStream_t s, int precision, int R, int S, const StabParams &p,
                            const int32_t *level_begin, int n_levels);
-// P, P', P'' of edge-independent length len[part] for each partition, rate: out [part][3][R][S][S].
-void launch_pmat3(cudaStream_t s, int n_parts, int R, int S, const double *lambda, const double *U,
-                  const double *Uinv, const double *rates, const double *len, double *out64, float *out32);
+// Once per context before the first evaluation (outside any graph capture):
+// the evaluation's shared-memory size; false for an unsupported (R, S).
+bool sumtable_eval_setup(int precision, int R, int S);
 // Evaluates every table at p.pm3 and reduces per (table, partition):
 // out [n_tab][n_parts][3] (w log L with the scale counters applied, l', l'').
 bool launch_sumtable_eval(cudaStream_t s, int precision, int R, int S, const StabParams &p, int n_tab,

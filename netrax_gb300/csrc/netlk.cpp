@@ -176,9 +176,10 @@ struct netlk_ctx {
   int tan_blocks = 0;
   // edge sumtables: unit-direction work planes, per-tree outside vectors at
   // the edge (tables), their scale counters, and the evaluation buffers
-  DevBuf d_stab_work, d_stab, d_stab_scaler, d_stab_partial, d_stab_out, d_stab_pm3_64, d_stab_pm3_32, d_stab_len,
+  DevBuf d_stab_work, d_stab, d_stab_scaler, d_stab_partial, d_stab_out, d_stab_pm3_64, d_stab_pm3_32,
       d_stab_groups, d_stab_ops, d_part_warp_begin;
-  PinnedBuf h_stab_len, h_stab_out, h_stab_ops;
+  PinnedBuf h_stab_pm3, h_stab_out, h_stab_ops;
+  cudaGraphExec_t graph_stab = nullptr;  // one evaluation of the current tables
   int stab_cap_work = -1, stab_cap_tab = 0;  // work slots / tables allocated (-1: not set up yet)
   int stab_edge = -1;                        // edge whose tables are current (-1: none)
   int stab_n_tab = 0, stab_n_groups = 0;
@@ -242,7 +243,7 @@ struct netlk_ctx {
   ~netlk_ctx() {
     if (device >= 0) cudaSetDevice(device);
     for (auto e : prof_ev) cudaEventDestroy(e);
-    for (auto g : {graph_logl, graph_grad, graph_partials, graph_mixbwd})
+    for (auto g : {graph_logl, graph_grad, graph_partials, graph_mixbwd, graph_stab})
       if (g) cudaGraphExecDestroy(g);
     for (DevBuf *b : {&d_clv, &d_scaler, &d_adj, &d_msg_slots, &d_tips, &d_weights, &d_unit_part, &d_fwd, &d_bwd, &d_rfwd, &d_ifwd,
                       &d_pmat64, &d_pmat32, &d_lambda, &d_U, &d_Uinv, &d_rates, &d_rw, &d_freqs, &d_Q,
@@ -253,7 +254,7 @@ struct netlk_ctx {
                       &d_pderiv64, &d_pderiv32, &d_block_part, &d_part_block_begin, &d_tan_slots, &d_gfrac,
                       &d_gfrac32, &d_invt, &d_invt32, &d_grad_part, &d_op_sum_part, &d_part_unit_begin, &d_stab_work,
                       &d_stab, &d_stab_scaler, &d_stab_partial, &d_stab_out, &d_stab_pm3_64, &d_stab_pm3_32,
-                      &d_stab_len, &d_stab_groups, &d_stab_ops, &d_part_warp_begin})
+                      &d_stab_groups, &d_stab_ops, &d_part_warp_begin})
       b->free();
     if (stream) cudaStreamDestroy(stream);
   }
@@ -386,7 +387,6 @@ struct netlk_ctx {
     sp.t.ops = d_stab_ops.as<TanOp>();
     sp.table = d_stab.p;
     sp.table_scaler = d_stab_scaler.as<int32_t>();
-    sp.U = d_U.as<double>();
     sp.pm3 = opts.precision == NETLK_FP32 ? d_stab_pm3_32.p : d_stab_pm3_64.p;
     sp.group_ref = d_stab_groups.as<int32_t>();
     sp.group_begin = d_stab_groups.as<int32_t>() + stab_n_groups;
@@ -1562,6 +1562,10 @@ bool netlk_ctx::sumtable_current(int e) const {
 
 bool netlk_ctx::sumtable_build(int e) {
   stab_edge = -1;
+  if (graph_stab) {  // captured for the previous tables
+    cudaGraphExecDestroy(graph_stab);
+    graph_stab = nullptr;
+  }
   if (n_segments != 1 || device_brlen || S != 4 || opts.host_only) return false;
   prepare();
   const size_t real_b = opts.precision == NETLK_FP32 ? 4 : 8;
@@ -1591,12 +1595,15 @@ bool netlk_ctx::sumtable_build(int e) {
     d_stab_out.alloc((std::max<size_t>(1, (size_t)tabs) * P * 3 + 1) * 8, scratch);  // + the fault word
     d_stab_pm3_64.alloc((size_t)P * 3 * R * S * S * 8, scratch);
     d_stab_pm3_32.alloc((size_t)P * 3 * R * S * S * 4, scratch);
-    d_stab_len.alloc((size_t)P * 8, scratch);
     d_stab_groups.alloc((size_t)(2 * tabs + 2) * 4, scratch);
     d_stab_ops.alloc(dag.vars.size() * sizeof(TanOp), scratch);
     d_part_warp_begin.alloc((size_t)(P + 1) * 4, scratch);
     dev_bytes += scratch;
-    h_stab_len.alloc((size_t)P * 8);
+    h_stab_pm3.alloc((size_t)P * 3 * R * S * S * 8);
+    if (!sumtable_eval_setup(opts.precision, R, S)) {
+      stab_cap_work = 0;
+      return false;
+    }
     h_stab_out.alloc((std::max<size_t>(1, (size_t)tabs) * P * 3 + 1) * 8);
     h_stab_ops.alloc(dag.vars.size() * sizeof(TanOp) + (size_t)(2 * tabs + 2) * 4);
     std::vector<int32_t> pwb(P + 1);
@@ -1676,23 +1683,75 @@ void netlk_ctx::sumtable_eval(int e, const double *len, int n_len, int mode, dou
     lp[p] = !per_part && linkage == NETLK_BRLEN_SCALED ? scalers[p] * t : t;
   }
   if (stab_n_tab > 0) {
-    std::memcpy(h_stab_len.p, lp.data(), P * 8);
-    CUDA_OK(cudaMemcpyAsync(d_stab_len.p, h_stab_len.p, P * 8, cudaMemcpyHostToDevice, stream));
-    launch_pmat3(stream, P, R, S, d_lambda.as<double>(), d_U.as<double>(), d_Uinv.as<double>(), d_rates.as<double>(),
-                 d_stab_len.as<double>(), d_stab_pm3_64.as<double>(),
-                 opts.precision == NETLK_FP32 ? d_stab_pm3_32.as<float>() : nullptr);
-    StabParams sp = stab_params();
-    CUDA_OK(cudaMemsetAsync(sp.fault, 0, 8, stream));
-    if (!launch_sumtable_eval(stream, opts.precision, R, S, sp, stab_n_tab, d_part_warp_begin.as<int32_t>(), P,
-                              d_stab_out.as<double>()))
-      throw Error(NETLK_ERR_UNSUPPORTED, "edge sumtables: unsupported state or rate count");
-    const size_t nb = (size_t)stab_n_tab * P * 3 * 8;
-    CUDA_OK(cudaMemcpyAsync(h_stab_out.p, d_stab_out.p, nb, cudaMemcpyDeviceToHost, stream));
-    int32_t fault = 0;
-    CUDA_OK(cudaMemcpyAsync(&fault, sp.fault, 4, cudaMemcpyDeviceToHost, stream));
+    // P, P', P'' of each partition's length, as pmatrix_kernel and
+    // pderiv_kernel form them (rates scaled for +I as the device's)
+    const int SS = S * S;
+    const bool f32 = opts.precision == NETLK_FP32;
+    double *h64 = h_stab_pm3.as<double>();
+    float *h32 = h_stab_pm3.as<float>();
+    std::vector<double> f(3 * S);  // per eigenvalue: the factor of order 0, 1, 2
+    for (int p = 0; p < P; ++p) {
+      const Eigen &eg = parts[p].eig;
+      for (int r = 0; r < R; ++r) {
+        const double rho = parts[p].rates[r] / (1.0 - parts[p].pinv), t = lp[p];
+        for (int k = 0; k < S; ++k) {
+          const double lr = eg.lambda[k] * rho, ed = std::exp(lr * t);
+          f[k] = std::exp(eg.lambda[k] * (t * rho));
+          f[S + k] = lr * ed;
+          f[2 * S + k] = lr * lr * ed;
+        }
+        for (int o = 0; o < 3; ++o)
+          for (int i = 0; i < S; ++i)
+            for (int j = 0; j < S; ++j) {
+              double v = 0.0;
+              if (o == 0 && t == 0.0)
+                v = i == j ? 1.0 : 0.0;
+              else
+                for (int k = 0; k < S; ++k) v += eg.U[i * S + k] * f[o * S + k] * eg.Uinv[k * S + j];
+              const size_t idx = (((size_t)p * 3 + o) * R + r) * SS + i * S + j;
+              if (f32) h32[idx] = (float)v;
+              else h64[idx] = v;
+            }
+      }
+    }
+    const size_t tail = (size_t)std::max(1, stab_cap_tab) * P * 3;  // fault word, after the largest output
+    auto enqueue_eval = [&]() {
+      StabParams sp = stab_params();
+      const size_t pm_b = (size_t)P * 3 * R * SS * (f32 ? 4 : 8);
+      CUDA_OK(cudaMemcpyAsync(f32 ? d_stab_pm3_32.p : d_stab_pm3_64.p, h_stab_pm3.p, pm_b, cudaMemcpyHostToDevice,
+                              stream));
+      CUDA_OK(cudaMemsetAsync(sp.fault, 0, 8, stream));
+      if (!launch_sumtable_eval(stream, opts.precision, R, S, sp, stab_n_tab, d_part_warp_begin.as<int32_t>(), P,
+                                d_stab_out.as<double>()))
+        throw Error(NETLK_ERR_UNSUPPORTED, "edge sumtables: unsupported state or rate count");
+      CUDA_OK(cudaMemcpyAsync(h_stab_out.p, d_stab_out.p, (size_t)stab_n_tab * P * 3 * 8, cudaMemcpyDeviceToHost,
+                              stream));
+      CUDA_OK(cudaMemcpyAsync(h_stab_out.as<double>() + tail, sp.fault, 8, cudaMemcpyDeviceToHost, stream));
+    };
+    if (!opts.use_cuda_graph || profiling) {
+      enqueue_eval();
+    } else {
+      if (!graph_stab) {
+        cudaGraph_t graph;
+        CUDA_OK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        try {
+          enqueue_eval();
+        } catch (...) {
+          cudaStreamEndCapture(stream, &graph);
+          if (graph) cudaGraphDestroy(graph);
+          throw;
+        }
+        CUDA_OK(cudaStreamEndCapture(stream, &graph));
+        cudaError_t err = cudaGraphInstantiate(&graph_stab, graph, 0);
+        cudaGraphDestroy(graph);
+        CUDA_OK(err);
+      }
+      CUDA_OK(cudaGraphLaunch(graph_stab, stream));
+    }
     CUDA_OK(cudaStreamSynchronize(stream));
     CUDA_OK(cudaGetLastError());
-    if (fault) throw Error(NETLK_ERR_TIMEOUT, "edge sumtable evaluation: a bulk-copy wait timed out");
+    if (*reinterpret_cast<const int32_t *>(h_stab_out.as<double>() + tail))
+      throw Error(NETLK_ERR_TIMEOUT, "edge sumtable evaluation: a bulk-copy wait timed out");
   }
   check_injected();
   const double *out = h_stab_out.as<double>();

@@ -301,46 +301,6 @@ __global__ void tangent_reduce_kernel(const TanParams p, const int32_t *__restri
 }
 
 // ------------------------------------------------------------ sumtables
-// P, P', P'' of P(rho_r t) = U diag(exp(lambda rho_r t)) U^-1 at t = len[part]:
-// out [part][3][R][S][S]. P follows pmatrix_kernel's arithmetic (so the
-// tables evaluated at the forward's length reproduce its P exactly), the
-// derivatives pderiv_kernel's.
-__global__ void pmat3_kernel(int n_parts, int R, int S, const double *__restrict__ lambda,
-                             const double *__restrict__ U, const double *__restrict__ Uinv,
-                             const double *__restrict__ rates, const double *__restrict__ len,
-                             double *__restrict__ out64, float *__restrict__ out32) {
-  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int SS = S * S;
-  const int64_t total = (int64_t)n_parts * 3 * R * SS;
-  if (idx >= total) return;
-  const int ij = (int)(idx % SS);
-  const int i = ij / S, j = ij - i * S;
-  const int64_t q = idx / SS;  // (part, order, rate)
-  const int rr = (int)(q % R);
-  const int order = (int)(q / R % 3);
-  const int part = (int)(q / R / 3);
-  const double rho = rates[part * R + rr];
-  const double t = len[part];
-  double v = 0.0;
-  if (order == 0) {
-    if (t == 0.0) {
-      v = i == j ? 1.0 : 0.0;
-    } else {
-      const double tr = t * rho;
-      for (int k = 0; k < S; ++k)
-        v += U[(size_t)part * SS + i * S + k] * exp(lambda[part * S + k] * tr) * Uinv[(size_t)part * SS + k * S + j];
-    }
-  } else {
-    for (int k = 0; k < S; ++k) {
-      const double lr = lambda[part * S + k] * rho;
-      const double f = order == 2 ? lr * lr : lr;
-      v += U[(size_t)part * SS + i * S + k] * f * exp(lr * t) * Uinv[(size_t)part * SS + k * S + j];
-    }
-  }
-  out64[idx] = v;
-  if (out32) out32[idx] = (float)v;
-}
-
 // Table build, one launch per level of the tangent schedule (blockIdx.y = op
 // of the level); threads as in tangent_kernel. The S unit directions of e's
 // message take the place of (X', X''): where x takes the message itself
@@ -592,30 +552,25 @@ __global__ void __launch_bounds__(128) sumtable_eval_kernel(const StabParams sp)
 }
 
 // out[(table * n_parts + part) * 3 + q] = compensated sum of the table's warp
-// partials over the partition's warps.
-__global__ void sumtable_reduce_kernel(const double *__restrict__ partial, int64_t n_warps,
-                                       const int32_t *__restrict__ part_warp_begin, int n_parts,
-                                       double *__restrict__ out, int ff) {
-  const int tb = blockIdx.x, part = blockIdx.y, q = blockIdx.z;
+// partials over the partition's warps: block (table, partition), warp q.
+__global__ void __launch_bounds__(96) sumtable_reduce_kernel(const double *__restrict__ partial, int64_t n_warps,
+                                                             const int32_t *__restrict__ part_warp_begin,
+                                                             int n_parts, double *__restrict__ out, int ff) {
+  const int tb = blockIdx.x, part = blockIdx.y, q = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int b0 = part_warp_begin[part], b1 = part_warp_begin[part + 1];
   const double *src = partial + ((size_t)tb * 3 + q) * n_warps;
   const float2 *src32 = reinterpret_cast<const float2 *>(src);
   double s = 0.0, c = 0.0;
-  for (int b = b0 + threadIdx.x; b < b1; b += blockDim.x) {
+  for (int b = b0 + lane; b < b1; b += 32) {
     const double v = ff ? (double)src32[b].x + (double)src32[b].y : src[b];
     const double y = v - c;
     const double t = s + y;
     c = (t - s) - y;
     s = t;
   }
-  __shared__ double red[128];
-  red[threadIdx.x] = s;
-  __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) out[((size_t)tb * n_parts + part) * 3 + q] = red[0];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (lane == 0) out[((size_t)tb * n_parts + part) * 3 + q] = s;
 }
 
 template <typename real, int R, int S>
@@ -628,14 +583,14 @@ void run_sumtable(cudaStream_t st, const StabParams &p, const int32_t *level_beg
 }
 
 template <typename real, int R, int S>
+constexpr size_t eval_smem() {
+  return eval_stages<real, R>() * (128 * R * S * sizeof(real) + 128 * 4) + 8 * eval_stages<real, R>() +
+         3 * R * S * S * sizeof(real);
+}
+
+template <typename real, int R, int S>
 void run_sumtable_eval(cudaStream_t st, const StabParams &p) {
-  constexpr int K = eval_stages<real, R>();
-  const size_t smem = K * (128 * R * S * sizeof(real) + 128 * 4) + 8 * K + 3 * R * S * S * sizeof(real);
-  static bool attr = false;  // once per instantiation: more than 48 KB for the larger (R, precision)
-  if (!attr) {
-    cudaFuncSetAttribute(sumtable_eval_kernel<real, R, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr = true;
-  }
+  const size_t smem = eval_smem<real, R, S>();
   const unsigned ny = (unsigned)((p.n_tables + p.tables_per_block - 1) / p.tables_per_block);
   sumtable_eval_kernel<real, R, S><<<dim3((unsigned)(p.t.n_patterns / 128), ny), 128, smem, st>>>(p);
 }
@@ -722,12 +677,22 @@ bool launch_sumtable_build(cudaStream_t s, int precision, int R, int S, const St
   return ok;
 }
 
-void launch_pmat3(cudaStream_t s, int n_parts, int R, int S, const double *lambda, const double *U,
-                  const double *Uinv, const double *rates, const double *len, double *out64, float *out32) {
-  const int64_t total = (int64_t)n_parts * 3 * R * S * S;
-  pmat3_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(n_parts, R, S, lambda, U, Uinv, rates, len, out64,
-                                                               out32);
-  add_launches(1);
+bool sumtable_eval_setup(int precision, int R, int S) {
+  if (S != 4) return false;
+  auto set = [](auto kernel, size_t smem) {
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess;
+  };
+  switch (R * 2 + (precision == 1)) {
+    case 2: return set(sumtable_eval_kernel<double, 1, 4>, eval_smem<double, 1, 4>());
+    case 3: return set(sumtable_eval_kernel<float, 1, 4>, eval_smem<float, 1, 4>());
+    case 4: return set(sumtable_eval_kernel<double, 2, 4>, eval_smem<double, 2, 4>());
+    case 5: return set(sumtable_eval_kernel<float, 2, 4>, eval_smem<float, 2, 4>());
+    case 8: return set(sumtable_eval_kernel<double, 4, 4>, eval_smem<double, 4, 4>());
+    case 9: return set(sumtable_eval_kernel<float, 4, 4>, eval_smem<float, 4, 4>());
+    case 16: return set(sumtable_eval_kernel<double, 8, 4>, eval_smem<double, 8, 4>());
+    case 17: return set(sumtable_eval_kernel<float, 8, 4>, eval_smem<float, 8, 4>());
+    default: return false;
+  }
 }
 
 bool launch_sumtable_eval(cudaStream_t s, int precision, int R, int S, const StabParams &p, int n_tab,
@@ -736,8 +701,8 @@ bool launch_sumtable_eval(cudaStream_t s, int precision, int R, int S, const Sta
   const bool ok = precision == 1 ? dispatch_sumtable<float>(s, R, S, p, nullptr, 0, true)
                                  : dispatch_sumtable<double>(s, R, S, p, nullptr, 0, true);
   if (!ok) return false;
-  sumtable_reduce_kernel<<<dim3(n_tab, n_parts, 3), 128, 0, s>>>(p.partial, p.t.n_patterns / 32, part_warp_begin,
-                                                                  n_parts, out, precision == 1);
+  sumtable_reduce_kernel<<<dim3(n_tab, n_parts), 96, 0, s>>>(p.partial, p.t.n_patterns / 32, part_warp_begin,
+                                                              n_parts, out, precision == 1);
   add_launches(2);
   return true;
 }
