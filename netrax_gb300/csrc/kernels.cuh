@@ -274,8 +274,8 @@ struct StabParams {
   double *partial;              // [n_tab][3][N / 32] per-warp sums of w log L, w L'/L, w (L''/L - (L'/L)^2); FP32: float pairs
 };
 
-// Builds the tables (one launch per level of the tangent schedule); false
-// for an unsupported (R, S): DNA only.
+// Builds the tables (one walk launch over the tangent schedule's ops in
+// level order); false for an unsupported (R, S): DNA only.
 bool launch_sumtable_build(cudaStream_t s, int precision, int R, int S, const StabParams &p,
                            const int32_t *level_begin, int n_levels);
 // Once per context before the first evaluation (outside any graph capture):

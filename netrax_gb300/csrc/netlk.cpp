@@ -16,6 +16,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/netlk.h"
@@ -411,6 +412,10 @@ struct netlk_ctx {
   // checkpoint segments, device-resident lengths, too little memory);
   // current while only edge e's lengths and nothing else changed since
   bool sumtable_build(int e);
+  // Reorders a tangent schedule depth-first for one walk (each op right
+  // before the ops that read its directions) and reassigns the work slots
+  // by live range in that order; returns the slots used, or -1.
+  static int walk_order(std::vector<TanOp> &ops);
   bool sumtable_current(int e) const;
   void sumtable_eval(int e, const double *len, int n_len, int mode, double *logl, double *d1, double *d2);
   int tangent_schedule(int e, std::vector<TanOp> &ops, std::vector<int32_t> &level_begin,
@@ -1551,6 +1556,61 @@ bool netlk_ctx::mix_edge(int mode, const std::vector<char> &act, LL ll, A1 a1, A
   return true;
 }
 
+int netlk_ctx::walk_order(std::vector<TanOp> &ops) {
+  const int n = (int)ops.size();
+  std::unordered_map<int32_t, int> op_of;  // variant -> its op
+  for (int j = 0; j < n; ++j) op_of[ops[j].x] = j;
+  std::vector<std::vector<int>> readers(n);
+  std::vector<int> roots;  // ops that take e's message itself
+  for (int j = 0; j < n; ++j) {
+    if (ops[j].mode == 1) {
+      roots.push_back(j);
+    } else {
+      auto it = op_of.find(ops[j].d);
+      if (it == op_of.end() || it->second >= j) return -1;
+      readers[it->second].push_back(j);
+    }
+  }
+  std::vector<int> order;
+  order.reserve(n);
+  std::vector<int> stack(roots.rbegin(), roots.rend());
+  while (!stack.empty()) {
+    const int j = stack.back();
+    stack.pop_back();
+    order.push_back(j);
+    for (auto it = readers[j].rbegin(); it != readers[j].rend(); ++it) stack.push_back(*it);
+  }
+  if ((int)order.size() != n) return -1;
+  std::vector<int> pos(n), last(n, -1);
+  for (int q = 0; q < n; ++q) pos[order[q]] = q;
+  for (int j = 0; j < n; ++j)
+    for (int rd : readers[j]) last[j] = std::max(last[j], pos[rd]);
+  std::vector<TanOp> out(n);
+  std::vector<int32_t> slot_of(n, -1), free_slots;
+  std::vector<std::vector<int32_t>> release(n);
+  int used = 0;
+  for (int q = 0; q < n; ++q) {
+    const int j = order[q];
+    TanOp t = ops[j];
+    t.td = t.mode == 2 ? slot_of[op_of[t.d]] : -1;
+    t.tx = -1;
+    if (last[j] >= 0) {
+      if (!free_slots.empty()) {
+        t.tx = free_slots.back();
+        free_slots.pop_back();
+      } else {
+        t.tx = used++;
+      }
+      slot_of[j] = t.tx;
+      release[last[j]].push_back(t.tx);
+    }
+    for (int32_t sl : release[q]) free_slots.push_back(sl);  // read for the last time here
+    out[q] = t;
+  }
+  ops.swap(out);
+  return used;
+}
+
 bool netlk_ctx::sumtable_current(int e) const {
   if (stab_edge != e || stab_gen != model_gen || device_brlen || stab_probs != ret_probs) return false;
   const std::vector<double> &L = dev_len();
@@ -1576,7 +1636,8 @@ bool netlk_ctx::sumtable_build(int e) {
     std::vector<TanOp> ops;
     std::vector<int32_t> lb, sl;
     for (int k = 0; k < topo.n_edges; ++k) {
-      need = std::max(need, tangent_schedule(k, ops, lb, sl));
+      if (tangent_schedule(k, ops, lb, sl) < 0) continue;
+      need = std::max(need, walk_order(ops));
       tabs = std::max(tabs, (int)sl.size());
     }
     setup_tangent_blocks();
@@ -1615,7 +1676,9 @@ bool netlk_ctx::sumtable_build(int e) {
   }
   std::vector<TanOp> ops;
   std::vector<int32_t> lb, dslots;
-  const int need = tangent_schedule(e, ops, lb, dslots);
+  if (tangent_schedule(e, ops, lb, dslots) < 0) return false;
+  const int need = walk_order(ops);
+  lb.assign({0, (int32_t)ops.size()});  // one walk over every op
   if (need < 0 || need > stab_cap_work || stab_cap_work == 0 || (int)dslots.size() > stab_cap_tab) return false;
   // the child whose CLV each root's path starts from (the message e carries);
   // tables sorted by it so the evaluation forms P I once per child
@@ -1657,7 +1720,7 @@ bool netlk_ctx::sumtable_build(int e) {
     std::memcpy(hg + gref.size(), gbegin.data(), gbegin.size() * 4);
     CUDA_OK(cudaMemcpyAsync(d_stab_groups.p, hg, (gref.size() + gbegin.size()) * 4, cudaMemcpyHostToDevice, stream));
     StabParams sp = stab_params();
-    if (!launch_sumtable_build(stream, opts.precision, R, S, sp, lb.data(), dag.n_levels)) return false;
+    if (!launch_sumtable_build(stream, opts.precision, R, S, sp, lb.data(), 1)) return false;
   }
   const int nout = 3 + P + topo.n_ret;
   CUDA_OK(cudaMemcpyAsync(h_out.p, d_out.p, nout * 8, cudaMemcpyDeviceToHost, stream));

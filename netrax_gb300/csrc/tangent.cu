@@ -301,80 +301,6 @@ __global__ void tangent_reduce_kernel(const TanParams p, const int32_t *__restri
 }
 
 // ------------------------------------------------------------ sumtables
-// Table build, one launch per level of the tangent schedule (blockIdx.y = op
-// of the level); threads as in tangent_kernel. The S unit directions of e's
-// message take the place of (X', X''): where x takes the message itself
-// (mode 1) direction i is vo_i at state i and 0 elsewhere; where x's child d
-// contains e (mode 2) it is (P_d times d's direction i) * vo; both times the
-// op's rescaling. At a displayed-tree root the thread writes its (pattern,
-// rate) row of the outside vector, O_i = w_r sum_j pi_j X_i[j], and the
-// root's scale counter.
-template <typename real, int R, int S>
-__global__ void __launch_bounds__(256, 4) sumtable_build_kernel(const StabParams sp, int op_begin) {
-  const TanParams &p = sp.t;
-  constexpr int RSS = R * S * S;
-  constexpr int ROWS = 256 / R;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  real *sMo = reinterpret_cast<real *>(smem_raw);
-  real *sMd = sMo + RSS, *sPi = sMd + RSS, *sRw = sPi + S;
-  const TanOp op = p.ops[op_begin + blockIdx.y];
-  const int part = p.block_part[blockIdx.x];
-  const real *pm = static_cast<const real *>(p.pmat) + (size_t)part * p.n_edges * RSS;
-  for (int i = threadIdx.x; i < RSS; i += blockDim.x) {
-    sMo[i] = op.eo >= 0 ? __ldg(pm + (size_t)op.eo * RSS + i) : (real)0;
-    sMd[i] = op.mode == 2 ? __ldg(pm + (size_t)op.ed * RSS + i) : (real)0;
-  }
-  if (threadIdx.x < S) sPi[threadIdx.x] = (real)p.freqs[part * S + threadIdx.x];
-  if (threadIdx.x < R) sRw[threadIdx.x] = (real)p.rate_weights[part * R + threadIdx.x];
-  __syncthreads();
-  const int r = threadIdx.x % R;
-  const size_t plane = (size_t)p.n_patterns * R * S;
-  const real *Mo = sMo + r * S * S, *Md = sMd + r * S * S;
-  const real *dsrc = static_cast<const real *>(p.tan) + (size_t)(op.td < 0 ? 0 : op.td) * S * plane;
-  real *ddst = static_cast<real *>(p.tan) + (size_t)(op.tx < 0 ? 0 : op.tx) * S * plane;
-#pragma unroll
-  for (int q = 0; q < kTanPPT; ++q) {
-    const int64_t s = ((int64_t)blockIdx.x * kTanPPT + q) * ROWS + threadIdx.x / R;
-    const size_t row = ((size_t)s * R + r) * S;
-    real c[S], vo[S], o[S];
-    const int so = load_row<real, R, S>(p, op.o, s, r, c);
-    if (op.o == INT32_MIN) {
-#pragma unroll
-      for (int i = 0; i < S; ++i) vo[i] = (real)1;
-    } else {
-      matvec<real, S>(Mo, c, vo);
-    }
-    const int sd = op.d >= 0 ? __ldg(p.scaler + (size_t)op.d * p.n_patterns + s) : 0;
-    const int sx = __ldg(p.scaler + (size_t)op.x * p.n_patterns + s);
-    const int k = sx - sd - so;
-#pragma unroll
-    for (int i = 0; i < S; ++i) {
-      real t[S];
-      if (op.mode == 1) {
-#pragma unroll
-        for (int j = 0; j < S; ++j) t[j] = j == i ? ScaleShift<real>::apply(vo[j], k) : (real)0;
-      } else {
-        ldg_row<real, S>(dsrc + i * plane + row, c);
-        matvec<real, S>(Md, c, t);
-#pragma unroll
-        for (int j = 0; j < S; ++j) t[j] = ScaleShift<real>::apply(t[j] * vo[j], k);
-      }
-      if (op.tx >= 0) st_row<real, S>(ddst + i * plane + row, t);
-      real a = (real)0;
-#pragma unroll
-      for (int j = 0; j < S; ++j) a = fma(sPi[j], t[j], a);
-      o[i] = a * sRw[r];
-    }
-    if (op.slot < 0) continue;  // uniform over the block
-    // table layout [table][pattern / 128][rate][pattern % 128][S]: one
-    // contiguous chunk per (table, 128 patterns), rate-major inside
-    st_row<real, S>(static_cast<real *>(sp.table) + ((size_t)op.slot * p.n_patterns + (s & ~(int64_t)127)) * R * S +
-                        ((size_t)r * 128 + (s & 127)) * S,
-                    o);
-    if (r == 0) sp.table_scaler[(size_t)op.slot * p.n_patterns + s] = sx;
-  }
-}
-
 // One table's site terms for the thread's pattern s (site likelihood L and
 // its derivatives L1, L2 in the table's scaled units), summed over the warp
 // into partial[table][q][warp].
@@ -428,6 +354,80 @@ __device__ __forceinline__ void sumtable_site_terms(const StabParams &sp, int tb
       sp.partial[((size_t)tb * 3 + 1) * n_warps + gw] = a1;
       sp.partial[((size_t)tb * 3 + 2) * n_warps + gw] = a2;
     }
+  }
+}
+
+// Table build as a walk: one warp per unit of 32 / R patterns (lane =
+// (pattern, rate)) runs every op of the tangent schedule in level order, so
+// the direction rows an op writes are read back by the same lanes soon
+// after, mostly from L2 (the level form, one launch per DAG level, wrote and
+// re-read them through DRAM). Per op: where x takes e's message (mode 1)
+// direction i is vo_i at state i and 0 elsewhere; where x's child d contains
+// e (mode 2) it is (P_d times d's direction i) * vo, vo = P_o o the other
+// child's message; both times the op's rescaling (its scale counter minus
+// the children's). At a displayed-tree root the lane writes its (pattern,
+// rate) row of the outside vector, O_i = w_r sum_j pi_j X_i[j], and lane
+// r = 0 the root's scale counter. Direction rows are read with plain
+// (coherent) loads: this kernel writes them.
+template <typename real, int R>
+__global__ void __launch_bounds__(256) sumtable_walk_kernel(const StabParams sp, int n_ops) {
+  constexpr int S = 4, PPW = 32 / R;
+  const TanParams &p = sp.t;
+  const int lane = threadIdx.x & 31, r = lane % R;
+  const int64_t s = ((int64_t)blockIdx.x * 8 + (threadIdx.x >> 5)) * PPW + lane / R;
+  if (s >= p.n_patterns) return;  // whole warps: n_patterns is a multiple of 32 / R
+  const int part = p.block_part[s / (kTanPPT * 256 / R)];
+  const real *pm = static_cast<const real *>(p.pmat) + ((size_t)part * p.n_edges * R + r) * S * S;
+  real pi[S];
+#pragma unroll
+  for (int i = 0; i < S; ++i) pi[i] = (real)p.freqs[part * S + i];
+  const real rw = (real)p.rate_weights[part * R + r];
+  const size_t plane = (size_t)p.n_patterns * R * S, row = ((size_t)s * R + r) * S;
+  real *dir = static_cast<real *>(p.tan);
+  for (int j = 0; j < n_ops; ++j) {
+    const TanOp op = p.ops[j];
+    real M[S * S], c[S], vo[S];
+    const int so = load_row<real, R, S>(p, op.o, s, r, c);
+    if (op.o == INT32_MIN) {
+#pragma unroll
+      for (int i = 0; i < S; ++i) vo[i] = (real)1;
+    } else {
+#pragma unroll
+      for (int i = 0; i < S; ++i) ldg_row<real, S>(pm + (size_t)op.eo * R * S * S + i * S, *reinterpret_cast<real(*)[S]>(M + i * S));
+      matvec<real, S>(M, c, vo);
+    }
+    const int sd = op.d >= 0 ? __ldg(p.scaler + (size_t)op.d * p.n_patterns + s) : 0;
+    const int sx = __ldg(p.scaler + (size_t)op.x * p.n_patterns + s);
+    const int k = sx - sd - so;
+    if (op.mode == 2)
+#pragma unroll
+      for (int i = 0; i < S; ++i) ldg_row<real, S>(pm + (size_t)op.ed * R * S * S + i * S, *reinterpret_cast<real(*)[S]>(M + i * S));
+    real o[S];
+#pragma unroll
+    for (int i = 0; i < S; ++i) {
+      real t[S];
+      if (op.mode == 1) {
+#pragma unroll
+        for (int jj = 0; jj < S; ++jj) t[jj] = jj == i ? ScaleShift<real>::apply(vo[jj], k) : (real)0;
+      } else {
+        const real *src = dir + ((size_t)op.td * S + i) * plane + row;
+#pragma unroll
+        for (int jj = 0; jj < S; ++jj) c[jj] = src[jj];
+        matvec<real, S>(M, c, t);
+#pragma unroll
+        for (int jj = 0; jj < S; ++jj) t[jj] = ScaleShift<real>::apply(t[jj] * vo[jj], k);
+      }
+      if (op.tx >= 0) st_row<real, S>(dir + ((size_t)op.tx * S + i) * plane + row, t);
+      real a = (real)0;
+#pragma unroll
+      for (int jj = 0; jj < S; ++jj) a = fma(pi[jj], t[jj], a);
+      o[i] = a * rw;
+    }
+    if (op.slot < 0) continue;  // uniform over the warp
+    st_row<real, S>(static_cast<real *>(sp.table) + ((size_t)op.slot * p.n_patterns + (s & ~(int64_t)127)) * R * S +
+                        ((size_t)r * 128 + (s & 127)) * S,
+                    o);
+    if (r == 0) sp.table_scaler[(size_t)op.slot * p.n_patterns + s] = sx;
   }
 }
 
@@ -575,11 +575,8 @@ __global__ void __launch_bounds__(96) sumtable_reduce_kernel(const double *__res
 
 template <typename real, int R, int S>
 void run_sumtable(cudaStream_t st, const StabParams &p, const int32_t *level_begin, int n_levels) {
-  const size_t smem = (2 * (size_t)R * S * S + S + R) * sizeof(real);
-  for (int L = 0; L < n_levels; ++L) {
-    const int n = level_begin[L + 1] - level_begin[L];
-    if (n > 0) sumtable_build_kernel<real, R, S><<<dim3(p.t.n_blocks, n), 256, smem, st>>>(p, level_begin[L]);
-  }
+  const int64_t warps = p.t.n_patterns * R / 32;
+  sumtable_walk_kernel<real, R><<<(unsigned)((warps + 7) / 8), 256, 0, st>>>(p, level_begin[n_levels]);
 }
 
 template <typename real, int R, int S>
@@ -672,8 +669,7 @@ bool launch_sumtable_build(cudaStream_t s, int precision, int R, int S, const St
                            const int32_t *level_begin, int n_levels) {
   const bool ok = precision == 1 ? dispatch_sumtable<float>(s, R, S, p, level_begin, n_levels, false)
                                  : dispatch_sumtable<double>(s, R, S, p, level_begin, n_levels, false);
-  if (ok)
-    for (int L = 0; L < n_levels; ++L) add_launches(level_begin[L + 1] > level_begin[L]);
+  if (ok) add_launches(1);
   return ok;
 }
 
