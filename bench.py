@@ -508,8 +508,9 @@ def run_edge(args, ws, rank, local):
     synchronous like its Newton-Raphson loop (BranchLengthOptimization.cpp:
     171-200, VirtualRerooting.cpp:348-585): a full logL after every length
     changed, netlk_edge_loglikelihood (only the variants above the edge are
-    recomputed), netlk_edge_derivatives (analytic d1 and d2 from one tangent
-    sweep over the variants above the edge), and the sumtable route of the
+    recomputed), netlk_edge_derivatives (analytic d1 and d2; timed on a new
+    edge each call, so each call builds that edge's sumtables), and the
+    sumtable route of the
     Newton-Raphson loop: netlk_edge_sumtable (the per-tree outside vectors at
     the edge, once per edge) and netlk_edge_sumtable_derivatives (logL, d1, d2
     at a proposed length: one pass over the tables) - against one iteration

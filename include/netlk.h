@@ -376,11 +376,16 @@ int netlk_last_site_updates(const netlk_ctx *ctx, int64_t *site_updates);
  * With unlinked lengths d1 / d2 are w.r.t. moving every partition's length
  * of the edge together (the sum of the partition shares); with scaled
  * lengths w.r.t. the linked length (sum of s_p x and s_p^2 x the shares).
- * Both derivatives are analytic: one forward-mode (tangent) sweep over the
- * variants above the edge gives every displayed tree's first and second
- * derivative, which are then mixed like the reference's sumtable derivatives
- * (LikelihoodDerivatives.cpp:13-188); the log-likelihood at the current
- * lengths is recomputed on the way (incrementally). Contexts with several
+ * Both derivatives are analytic. DNA contexts evaluate the edge's sumtables
+ * (netlk_edge_sumtable below) at the current lengths: built on the first
+ * call for the edge and kept while only that edge's lengths change, so a
+ * Newton-Raphson loop that sets each proposal (netlk_edge_loglikelihood)
+ * and asks for the derivatives pays for one build per edge. 20-state
+ * contexts take one forward-mode (tangent) sweep over the variants above
+ * the edge per call (the log-likelihood at the current lengths recomputed
+ * incrementally on the way). Either way every displayed tree's first and
+ * second derivative is mixed like the reference's sumtable derivatives
+ * (LikelihoodDerivatives.cpp:13-188). Contexts with several
  * checkpoint segments or device-resident lengths take d1 from full adjoint
  * sweeps and d2, when not NULL, as the central difference of d1 over +-h (kept
  * inside [1e-6, 100]): h = min(1e-6, t/200) for FP64 contexts; for FP32

@@ -15,6 +15,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <numeric>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -2482,7 +2483,25 @@ int netlk_edge_derivatives(netlk_ctx *ctx, int32_t edge, int32_t mode, double *d
   return guarded(ctx, [&] {
     if (edge < 0 || edge >= ctx->topo.n_edges) throw Error(NETLK_ERR_INVALID_ARGUMENT, "edge");
     if (mode != 0 && mode != 1) throw Error(NETLK_ERR_INVALID_ARGUMENT, "mode must be 0 or 1");
-    // analytic d1 and d2 from one tangent sweep over the variants above the edge
+    // DNA: the edge's sumtables evaluated at the current lengths (built on
+    // the first call for the edge and kept while only its lengths change,
+    // so a Newton-Raphson loop that sets each proposal and asks for the
+    // derivatives pays for one build per edge); else analytic d1 and d2
+    // from one tangent sweep over the variants above the edge
+    if (!ctx->device_brlen && (ctx->sumtable_current(edge) || ctx->sumtable_build(edge))) {
+      const int E = ctx->topo.n_edges, P = ctx->P;
+      if (ctx->linkage != NETLK_BRLEN_UNLINKED || P == 1) {
+        const double t = ctx->linkage == NETLK_BRLEN_UNLINKED ? ctx->plen[edge] : ctx->brlen[edge];
+        ctx->sumtable_eval(edge, &t, 1, mode, nullptr, d1, d2);
+      } else {  // each partition at its own length: the sum of the shares
+        std::vector<double> t(P), a(P), b(P);
+        for (int p = 0; p < P; ++p) t[p] = ctx->plen[(size_t)p * E + edge];
+        ctx->sumtable_eval(edge, t.data(), P, mode, nullptr, a.data(), b.data());
+        if (d1) *d1 = std::accumulate(a.begin(), a.end(), 0.0);
+        if (d2) *d2 = std::accumulate(b.begin(), b.end(), 0.0);
+      }
+      return;
+    }
     if (ctx->edge_derivs_analytic(edge, mode, d1, d2)) return;
     if (ctx->linkage != NETLK_BRLEN_LINKED)
       throw Error(NETLK_ERR_UNSUPPORTED,

@@ -6,7 +6,7 @@ loops on the oracle (``tests/optimizer_loops.py`` restates them).
   step after ``netlk_edge_loglikelihood`` sets the proposal) against the same
   pass with ``oracle/derivatives.py``'s sumtable derivatives and the oracle's
   log-likelihood. The final lengths agree within 1e-6 (FP64) / 1e-4 (FP32)
-  relative or 1e-9 absolute, the final logL within 1e-9 (FP64) / 1e-6 (FP32)
+  relative or 1e-9 (FP64) / 1e-7 (FP32, the NR stopping tolerance) absolute, the final logL within 1e-9 (FP64) / 1e-6 (FP32)
   relative, and no step lowers the log-likelihood. With the true
   derivatives (mode 0) repeated passes converge: the gradient vanishes on the
   edges away from the length bounds.
@@ -77,7 +77,9 @@ def _close(a, b, rel, atol):
 def test_newton_raphson_branch_pass_matches_the_oracle(name, variant):
     want_len, want_logl, want_worse = _oracle_branch_pass(name, variant)
     assert not want_worse
-    for precision, rel_len, rel_logl in (("fp64", 1e-6, 1e-9), ("fp32", 1e-4, 1e-6)):
+    # lengths: relative, or absolute within the NR stopping tolerance (1e-7)
+    # in FP32, whose derivatives near the 1e-6 clamp carry ~1e-4 relative noise
+    for precision, rel_len, abs_len, rel_logl in (("fp64", 1e-6, 1e-9, 1e-9), ("fp32", 1e-4, opt.NR_TOLERANCE, 1e-6)):
         with _lik(name, variant, precision) as lik:
             start = lik.loglikelihood()
             lengths, logl, worse = opt.optimize_branches(
@@ -85,7 +87,7 @@ def test_newton_raphson_branch_pass_matches_the_oracle(name, variant):
                 lik.branch_lengths)
             assert not worse and logl >= start - 1e-9 * abs(start)
             assert logl == pytest.approx(want_logl, rel=rel_logl)
-            assert _close(lengths, want_len, rel_len, 1e-9), (precision, np.abs(np.array(lengths) - want_len).max())
+            assert _close(lengths, want_len, rel_len, abs_len), (precision, np.abs(np.array(lengths) - want_len).max())
             assert lik.loglikelihood() == pytest.approx(logl, rel=1e-12)
 
 
