@@ -357,8 +357,8 @@ __device__ __forceinline__ void sumtable_site_terms(const StabParams &sp, int tb
   }
 }
 
-// Table build as a walk: one warp per unit of 32 / R patterns (lane =
-// (pattern, rate)) runs every op of the tangent schedule in level order, so
+// Table build as a walk: one warp per unit of PPL * 32 / R patterns (lane =
+// (rate, PPL patterns)) runs every op of the tangent schedule in level order, so
 // the direction rows an op writes are read back by the same lanes soon
 // after, mostly from L2 (the level form, one launch per DAG level, wrote and
 // re-read them through DRAM). Per op: where x takes e's message (mode 1)
@@ -369,65 +369,82 @@ __device__ __forceinline__ void sumtable_site_terms(const StabParams &sp, int tb
 // rate) row of the outside vector, O_i = w_r sum_j pi_j X_i[j], and lane
 // r = 0 the root's scale counter. Direction rows are read with plain
 // (coherent) loads: this kernel writes them.
-template <typename real, int R>
+template <typename real, int R, int PPL>
 __global__ void __launch_bounds__(256) sumtable_walk_kernel(const StabParams sp, int n_ops) {
   constexpr int S = 4, PPW = 32 / R;
   const TanParams &p = sp.t;
   const int lane = threadIdx.x & 31, r = lane % R;
-  const int64_t s = ((int64_t)blockIdx.x * 8 + (threadIdx.x >> 5)) * PPW + lane / R;
-  if (s >= p.n_patterns) return;  // whole warps: n_patterns is a multiple of 32 / R
-  const int part = p.block_part[s / (kTanPPT * 256 / R)];
+  // the warp's PPL * PPW patterns; lane: rate r of patterns s0 + q PPW
+  const int64_t s0 = ((int64_t)blockIdx.x * 8 + (threadIdx.x >> 5)) * PPL * PPW + lane / R;
+  if (s0 >= p.n_patterns) return;  // whole warps: n_patterns is a multiple of PPL * 32 / R
+  const int part = p.block_part[s0 / (kTanPPT * 256 / R)];
   const real *pm = static_cast<const real *>(p.pmat) + ((size_t)part * p.n_edges * R + r) * S * S;
   real pi[S];
 #pragma unroll
   for (int i = 0; i < S; ++i) pi[i] = (real)p.freqs[part * S + i];
   const real rw = (real)p.rate_weights[part * R + r];
-  const size_t plane = (size_t)p.n_patterns * R * S, row = ((size_t)s * R + r) * S;
+  const size_t plane = (size_t)p.n_patterns * R * S;
   real *dir = static_cast<real *>(p.tan);
   for (int j = 0; j < n_ops; ++j) {
     const TanOp op = p.ops[j];
-    real M[S * S], c[S], vo[S];
-    const int so = load_row<real, R, S>(p, op.o, s, r, c);
+    real M[S * S], c[PPL][S], vo[PPL][S];
+    int k[PPL], sx[PPL];
+#pragma unroll
+    for (int q = 0; q < PPL; ++q) {
+      const int64_t s = s0 + q * PPW;
+      const int so = load_row<real, R, S>(p, op.o, s, r, c[q]);
+      const int sd = op.d >= 0 ? __ldg(p.scaler + (size_t)op.d * p.n_patterns + s) : 0;
+      sx[q] = __ldg(p.scaler + (size_t)op.x * p.n_patterns + s);
+      k[q] = sx[q] - sd - so;
+    }
     if (op.o == INT32_MIN) {
 #pragma unroll
-      for (int i = 0; i < S; ++i) vo[i] = (real)1;
+      for (int q = 0; q < PPL; ++q)
+#pragma unroll
+        for (int i = 0; i < S; ++i) vo[q][i] = (real)1;
     } else {
 #pragma unroll
-      for (int i = 0; i < S; ++i) ldg_row<real, S>(pm + (size_t)op.eo * R * S * S + i * S, *reinterpret_cast<real(*)[S]>(M + i * S));
-      matvec<real, S>(M, c, vo);
+      for (int i = 0; i < S; ++i)
+        ldg_row<real, S>(pm + (size_t)op.eo * R * S * S + i * S, *reinterpret_cast<real(*)[S]>(M + i * S));
+#pragma unroll
+      for (int q = 0; q < PPL; ++q) matvec<real, S>(M, c[q], vo[q]);
     }
-    const int sd = op.d >= 0 ? __ldg(p.scaler + (size_t)op.d * p.n_patterns + s) : 0;
-    const int sx = __ldg(p.scaler + (size_t)op.x * p.n_patterns + s);
-    const int k = sx - sd - so;
     if (op.mode == 2)
 #pragma unroll
-      for (int i = 0; i < S; ++i) ldg_row<real, S>(pm + (size_t)op.ed * R * S * S + i * S, *reinterpret_cast<real(*)[S]>(M + i * S));
-    real o[S];
+      for (int i = 0; i < S; ++i)
+        ldg_row<real, S>(pm + (size_t)op.ed * R * S * S + i * S, *reinterpret_cast<real(*)[S]>(M + i * S));
 #pragma unroll
-    for (int i = 0; i < S; ++i) {
-      real t[S];
-      if (op.mode == 1) {
+    for (int q = 0; q < PPL; ++q) {
+      const int64_t s = s0 + q * PPW;
+      const size_t row = ((size_t)s * R + r) * S;
+      real o[S];
 #pragma unroll
-        for (int jj = 0; jj < S; ++jj) t[jj] = jj == i ? ScaleShift<real>::apply(vo[jj], k) : (real)0;
-      } else {
-        const real *src = dir + ((size_t)op.td * S + i) * plane + row;
+      for (int i = 0; i < S; ++i) {
+        real t[S];
+        if (op.mode == 1) {
 #pragma unroll
-        for (int jj = 0; jj < S; ++jj) c[jj] = src[jj];
-        matvec<real, S>(M, c, t);
+          for (int jj = 0; jj < S; ++jj) t[jj] = jj == i ? ScaleShift<real>::apply(vo[q][jj], k[q]) : (real)0;
+        } else {
+          const real *src = dir + ((size_t)op.td * S + i) * plane + row;
+          real d[S];
 #pragma unroll
-        for (int jj = 0; jj < S; ++jj) t[jj] = ScaleShift<real>::apply(t[jj] * vo[jj], k);
+          for (int jj = 0; jj < S; ++jj) d[jj] = src[jj];
+          matvec<real, S>(M, d, t);
+#pragma unroll
+          for (int jj = 0; jj < S; ++jj) t[jj] = ScaleShift<real>::apply(t[jj] * vo[q][jj], k[q]);
+        }
+        if (op.tx >= 0) st_row<real, S>(dir + ((size_t)op.tx * S + i) * plane + row, t);
+        real a = (real)0;
+#pragma unroll
+        for (int jj = 0; jj < S; ++jj) a = fma(pi[jj], t[jj], a);
+        o[i] = a * rw;
       }
-      if (op.tx >= 0) st_row<real, S>(dir + ((size_t)op.tx * S + i) * plane + row, t);
-      real a = (real)0;
-#pragma unroll
-      for (int jj = 0; jj < S; ++jj) a = fma(pi[jj], t[jj], a);
-      o[i] = a * rw;
+      if (op.slot < 0) continue;  // uniform over the warp
+      st_row<real, S>(static_cast<real *>(sp.table) + ((size_t)op.slot * p.n_patterns + (s & ~(int64_t)127)) * R * S +
+                          ((size_t)r * 128 + (s & 127)) * S,
+                      o);
+      if (r == 0) sp.table_scaler[(size_t)op.slot * p.n_patterns + s] = sx[q];
     }
-    if (op.slot < 0) continue;  // uniform over the warp
-    st_row<real, S>(static_cast<real *>(sp.table) + ((size_t)op.slot * p.n_patterns + (s & ~(int64_t)127)) * R * S +
-                        ((size_t)r * 128 + (s & 127)) * S,
-                    o);
-    if (r == 0) sp.table_scaler[(size_t)op.slot * p.n_patterns + s] = sx;
   }
 }
 
@@ -561,12 +578,21 @@ __global__ void __launch_bounds__(96) sumtable_reduce_kernel(const double *__res
   const double *src = partial + ((size_t)tb * 3 + q) * n_warps;
   const float2 *src32 = reinterpret_cast<const float2 *>(src);
   double s = 0.0, c = 0.0;
-  for (int b = b0 + lane; b < b1; b += 32) {
-    const double v = ff ? (double)src32[b].x + (double)src32[b].y : src[b];
-    const double y = v - c;
-    const double t = s + y;
-    c = (t - s) - y;
-    s = t;
+  // eight loads in flight per lane before they are added (in a fixed order)
+  for (int b = b0 + lane; b < b1; b += 32 * 8) {
+    double v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int i = b + 32 * u;
+      v[u] = i < b1 ? (ff ? (double)src32[i].x + (double)src32[i].y : src[i]) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const double y = v[u] - c;
+      const double t = s + y;
+      c = (t - s) - y;
+      s = t;
+    }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
@@ -575,8 +601,14 @@ __global__ void __launch_bounds__(96) sumtable_reduce_kernel(const double *__res
 
 template <typename real, int R, int S>
 void run_sumtable(cudaStream_t st, const StabParams &p, const int32_t *level_begin, int n_levels) {
-  const int64_t warps = p.t.n_patterns * R / 32;
-  sumtable_walk_kernel<real, R><<<(unsigned)((warps + 7) / 8), 256, 0, st>>>(p, level_begin[n_levels]);
+  // patterns per lane: two (two rows' loads in flight per op) once one per
+  // lane gives more than about two waves of warps, else one (more warps)
+  const int64_t warps1 = p.t.n_patterns * R / 32;
+  if (warps1 > 2 * 152 * 24) {
+    sumtable_walk_kernel<real, R, 2><<<(unsigned)((warps1 / 2 + 7) / 8), 256, 0, st>>>(p, level_begin[n_levels]);
+  } else {
+    sumtable_walk_kernel<real, R, 1><<<(unsigned)((warps1 + 7) / 8), 256, 0, st>>>(p, level_begin[n_levels]);
+  }
 }
 
 template <typename real, int R, int S>
