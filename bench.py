@@ -585,12 +585,17 @@ def run_edge(args, ws, rank, local):
         lik.edge_derivatives(e)
     nr_iter_s = (time.perf_counter() - t) / max(10, K)
     lik.edge_loglikelihood(e, base[e])
-    # the tangent sweep (per-partition derivatives take it on every call)
+    lik.close()
+    # the tangent sweep: a context without sumtables takes it on every call
+    likt = NetworkLikelihood(w.network, w.partitions, variant=args.variant, precision=args.precision,
+                             device=local, sumtables=False)
+    likt.loglikelihood_gradient()
+    likt.edge_derivatives(sedges[0])
     t = time.perf_counter()
     for k in range(nd):
-        lik.edge_derivatives_partition(sedges[k], 0)
+        likt.edge_derivatives(sedges[k])
     tangent_s = (time.perf_counter() - t) / nd
-    lik.close()
+    likt.close()
     if rank == 0:
         line = {
             "metric": "edge logL evals/s (incremental) & edge derivative evals/s",
@@ -613,7 +618,7 @@ def run_edge(args, ws, rank, local):
                          "tangent_sweep_ms": tangent_s * 1000.0,
                          "note": "eval: logL, d1, d2 at a proposed length from the tables; set-and-derive: "
                                  "netlk_edge_loglikelihood at the proposal + netlk_edge_derivatives (tables "
-                                 "current); tangent sweep: netlk_edge_derivatives_partition"},
+                                 "current); tangent sweep: netlk_edge_derivatives on a context created with sumtables = 0"},
         }
         print(json.dumps(line), flush=True)
 

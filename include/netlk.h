@@ -147,6 +147,10 @@ typedef struct {
                                         (netlk_set_branch_length_scalers). The
                                         reference's --brlen linked / unlinked /
                                         scaled (src/main.cpp:101,226-230).    */
+  int32_t sumtables;                 /* 1 (default): edge derivatives of DNA
+                                        contexts from the edge's sumtables
+                                        (netlk_edge_sumtable); 0: one tangent
+                                        sweep per call                        */
 } netlk_options;
 
 #define NETLK_BRLEN_LINKED 0
@@ -419,9 +423,9 @@ int netlk_edge_derivatives_partition(netlk_ctx *ctx, int32_t edge, int32_t parti
  * evaluation builds them itself when they are missing or stale; this entry
  * lets a caller pay for the build where it chooses). *built = 1 when the
  * sumtable path applies, 0 when it does not (20-state partitions, several
- * checkpoint segments, device-resident lengths, or tables that would take
- * more than half the free device memory); evaluations then take the tangent
- * path. *n_tables (may be NULL): the tables built, one per displayed tree
+ * checkpoint segments, device-resident lengths, the context's `sumtables`
+ * option 0, or tables that would take more than half the free device
+ * memory); evaluations then take the tangent path. *n_tables (may be NULL): the tables built, one per displayed tree
  * that contains the edge. */
 int netlk_edge_sumtable(netlk_ctx *ctx, int32_t edge, int32_t *built, int32_t *n_tables);
 /* logL and its first / second derivative with the edge at the given

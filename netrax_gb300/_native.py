@@ -70,7 +70,8 @@ class Options(ctypes.Structure):
                 ("device", ctypes.c_int32), ("use_cuda_graph", ctypes.c_int32),
                 ("host_only", ctypes.c_int32), ("autotune", ctypes.c_int32),
                 ("tensor_cores", ctypes.c_int32), ("checkpoint_segments", ctypes.c_int32),
-                ("incremental", ctypes.c_int32), ("brlen_linkage", ctypes.c_int32)]
+                ("incremental", ctypes.c_int32), ("brlen_linkage", ctypes.c_int32),
+                ("sumtables", ctypes.c_int32)]
 
 
 class DagStats(ctypes.Structure):

@@ -418,7 +418,10 @@ struct netlk_ctx {
   // by live range in that order; returns the slots used, or -1.
   static int walk_order(std::vector<TanOp> &ops);
   bool sumtable_current(int e) const;
-  void sumtable_eval(int e, const double *len, int n_len, int mode, double *logl, double *d1, double *d2);
+  // per_part: len, logl, d1, d2 hold one entry per partition (each at its
+  // own length); else len[0] is the edge's (linked or scaled) length and the
+  // outputs are totals w.r.t. it
+  void sumtable_eval(int e, const double *len, bool per_part, int mode, double *logl, double *d1, double *d2);
   int tangent_schedule(int e, std::vector<TanOp> &ops, std::vector<int32_t> &level_begin,
                        std::vector<int32_t> &slots) const;
   // d logL / d (partition p's length of edge e) [P][E] from the last adjoint
@@ -1627,7 +1630,7 @@ bool netlk_ctx::sumtable_build(int e) {
     cudaGraphExecDestroy(graph_stab);
     graph_stab = nullptr;
   }
-  if (n_segments != 1 || device_brlen || S != 4 || opts.host_only) return false;
+  if (n_segments != 1 || device_brlen || S != 4 || opts.host_only || !opts.sumtables) return false;
   prepare();
   const size_t real_b = opts.precision == NETLK_FP32 ? 4 : 8;
   const size_t plane = (size_t)N * R * S * real_b;  // one (pattern, rate, state) plane
@@ -1739,9 +1742,9 @@ bool netlk_ctx::sumtable_build(int e) {
   return true;
 }
 
-void netlk_ctx::sumtable_eval(int e, const double *len, int n_len, int mode, double *logl, double *d1, double *d2) {
-  const bool per_part = n_len > 1;  // one length per partition (else one for all, scaled by s_p)
-  std::vector<double> lp(P);        // each partition's length of e
+void netlk_ctx::sumtable_eval(int e, const double *len, bool per_part, int mode, double *logl, double *d1,
+                             double *d2) {
+  std::vector<double> lp(P);  // each partition's length of e
   for (int p = 0; p < P; ++p) {
     const double t = std::min(std::max(per_part ? len[p] : len[0], 1e-6), 100.0);
     lp[p] = !per_part && linkage == NETLK_BRLEN_SCALED ? scalers[p] * t : t;
@@ -2067,6 +2070,7 @@ int netlk_options_default(netlk_options *o) {
   o->checkpoint_segments = 0;
   o->incremental = 1;
   o->brlen_linkage = NETLK_BRLEN_LINKED;
+  o->sumtables = 1;
   return NETLK_OK;
 }
 
@@ -2492,11 +2496,11 @@ int netlk_edge_derivatives(netlk_ctx *ctx, int32_t edge, int32_t mode, double *d
       const int E = ctx->topo.n_edges, P = ctx->P;
       if (ctx->linkage != NETLK_BRLEN_UNLINKED || P == 1) {
         const double t = ctx->linkage == NETLK_BRLEN_UNLINKED ? ctx->plen[edge] : ctx->brlen[edge];
-        ctx->sumtable_eval(edge, &t, 1, mode, nullptr, d1, d2);
+        ctx->sumtable_eval(edge, &t, false, mode, nullptr, d1, d2);
       } else {  // each partition at its own length: the sum of the shares
         std::vector<double> t(P), a(P), b(P);
         for (int p = 0; p < P; ++p) t[p] = ctx->plen[(size_t)p * E + edge];
-        ctx->sumtable_eval(edge, t.data(), P, mode, nullptr, a.data(), b.data());
+        ctx->sumtable_eval(edge, t.data(), true, mode, nullptr, a.data(), b.data());
         if (d1) *d1 = std::accumulate(a.begin(), a.end(), 0.0);
         if (d2) *d2 = std::accumulate(b.begin(), b.end(), 0.0);
       }
@@ -2594,6 +2598,17 @@ int netlk_edge_derivatives_partition(netlk_ctx *ctx, int32_t edge, int32_t part,
     if (edge < 0 || edge >= ctx->topo.n_edges) throw Error(NETLK_ERR_INVALID_ARGUMENT, "edge");
     if (part < 0 || part >= ctx->P) throw Error(NETLK_ERR_INVALID_ARGUMENT, "partition");
     if (mode != 0 && mode != 1) throw Error(NETLK_ERR_INVALID_ARGUMENT, "mode must be 0 or 1");
+    // DNA: the edge's sumtables, every partition at its own current length
+    if (!ctx->device_brlen && (ctx->sumtable_current(edge) || ctx->sumtable_build(edge))) {
+      const int E = ctx->topo.n_edges, P = ctx->P;
+      const std::vector<double> &L = ctx->dev_len();
+      std::vector<double> t(P), a(P), b(P);
+      for (int p = 0; p < P; ++p) t[p] = L[(size_t)p * (ctx->linkage == NETLK_BRLEN_LINKED ? 0 : E) + edge];
+      ctx->sumtable_eval(edge, t.data(), true, mode, nullptr, a.data(), b.data());
+      if (d1) *d1 = a[part];
+      if (d2) *d2 = b[part];
+      return;
+    }
     if (!ctx->edge_derivs_analytic(edge, mode, d1, d2, part))
       throw Error(NETLK_ERR_UNSUPPORTED, "per-partition edge derivatives need one checkpoint segment and host lengths");
   });
@@ -2622,7 +2637,7 @@ int netlk_edge_sumtable_derivatives(netlk_ctx *ctx, int32_t edge, const double *
     if (ctx->device_brlen)
       throw Error(NETLK_ERR_UNSUPPORTED, "branch lengths are device-resident: set them on the host first");
     if (ctx->sumtable_current(edge) || ctx->sumtable_build(edge)) {
-      ctx->sumtable_eval(edge, lengths, n_lengths, mode, logl, d1, d2);
+      ctx->sumtable_eval(edge, lengths, n_lengths > 1, mode, logl, d1, d2);
       return;
     }
     // the tangent path at the proposed length; the lengths are put back

@@ -38,7 +38,7 @@ class NetworkLikelihood:
     def __init__(self, network: NetworkDesc, partitions, variant="AVERAGE", precision="fp32",
                  min_interesting_tree_logprob=math.log(1e-6), device=0, use_cuda_graph=True,
                  host_only=False, rates=None, autotune=True, tensor_cores=True, checkpoint_segments=0,
-                 incremental=True, brlen_linkage="linked"):
+                 incremental=True, brlen_linkage="linked", sumtables=True):
         L = N.lib()
         self.network = network
         self.n_parts = len(partitions)
@@ -97,6 +97,7 @@ class NetworkLikelihood:
         opts.incremental = int(bool(incremental))
         opts.brlen_linkage = {"linked": N.NETLK_BRLEN_LINKED, "unlinked": N.NETLK_BRLEN_UNLINKED,
                               "scaled": N.NETLK_BRLEN_SCALED}[brlen_linkage]
+        opts.sumtables = int(bool(sumtables))
         bl = arr(network.branch_lengths, np.float64)
         rp = arr(network.ret_first_probs, np.float64) if self.n_ret else None
         h = ctypes.c_void_p()

@@ -11,7 +11,8 @@ formulas; pinned on CPU against finite differences in
   1e-4 of the largest entry), for every branch length and reticulation
   probability;
 * ``netlk_edge_derivatives`` mode 0 (true derivative) and mode 1 (the
-  reference's formula), FP64: d1 within 1e-8 relative on every edge; d2 - a
+  reference's formula), on the edge sumtables (default) and on the tangent
+  sweep (``sumtables = 0``), FP64: d1 within 1e-8 relative on every edge; d2 - a
   central difference of d1 over +-1e-6 - within 1e-4 relative where the
   length is at least 1e-3 (nearer the 1e-6 clamp the difference is one-sided);
 * the same in FP32: d1 within 1e-4 relative (plus 1e-4 of the largest entry),
@@ -34,13 +35,13 @@ with open(os.path.join(GOLDEN, "derivative_cases.json")) as _f:
 NAMES = sorted(DERIVS)
 
 
-def _lik(name, variant, precision):
+def _lik(name, variant, precision, **kw):
     from netrax_gb300.likelihood import NetworkLikelihood
     from netrax_gb300.network import parse_extended_newick
     case = CASES[name]
     net = parse_extended_newick(case["newick"])
     parts = [GoldenPartition(d) for d in case["partitions"]]
-    return NetworkLikelihood(net, parts, variant=variant, precision=precision)
+    return NetworkLikelihood(net, parts, variant=variant, precision=precision, **kw)
 
 
 def _close(got, want, rel, abs_frac):
@@ -71,12 +72,13 @@ def test_gradient_matches_analytic_oracle(name, variant, precision):
 @pytest.mark.parametrize("name", NAMES)
 @pytest.mark.parametrize("variant", ["AVERAGE", "BEST"])
 @pytest.mark.parametrize("mode", [0, 1])
-def test_edge_derivatives_match_analytic_oracle(name, variant, mode):
+@pytest.mark.parametrize("sumtables", [True, False])
+def test_edge_derivatives_match_analytic_oracle(name, variant, mode, sumtables):
     want = DERIVS[name][variant]
     key = "true" if mode == 0 else "reference"
     w1 = np.array(want["d1_" + key])
     w2 = np.array(want["d2_" + key])
-    with _lik(name, variant, "fp64") as lik:
+    with _lik(name, variant, "fp64", sumtables=sumtables) as lik:
         lengths = lik.branch_lengths.copy()
         got1, got2 = [], []
         for e in range(lik.n_edges):
@@ -97,12 +99,13 @@ def test_edge_derivatives_match_analytic_oracle(name, variant, mode):
 @pytest.mark.parametrize("name", NAMES)
 @pytest.mark.parametrize("variant", ["AVERAGE", "BEST"])
 @pytest.mark.parametrize("mode", [0, 1])
-def test_fp32_edge_derivatives_match_analytic_oracle(name, variant, mode):
+@pytest.mark.parametrize("sumtables", [True, False])
+def test_fp32_edge_derivatives_match_analytic_oracle(name, variant, mode, sumtables):
     want = DERIVS[name][variant]
     key = "true" if mode == 0 else "reference"
     w1 = np.array(want["d1_" + key])
     w2 = np.array(want["d2_" + key])
-    with _lik(name, variant, "fp32") as lik:
+    with _lik(name, variant, "fp32", sumtables=sumtables) as lik:
         lengths = lik.branch_lengths.copy()
         got = np.array([lik.edge_derivatives(e, second=True, mode=mode) for e in range(lik.n_edges)])
     ok, worst = _close(got[:, 0], w1, 1e-4, 1e-4)
