@@ -2006,6 +2006,7 @@ int guarded(netlk_ctx *ctx, F &&f) {
     if (ctx) {
       ctx->err = e.what();
       ctx->clv_valid = false;
+      ctx->stab_edge = -1;  // the tables read the edge's child CLV at every evaluation
     } else {
       g_create_error = e.what();
     }
@@ -2014,6 +2015,7 @@ int guarded(netlk_ctx *ctx, F &&f) {
     if (ctx) {
       ctx->err = "host allocation failed";
       ctx->clv_valid = false;
+      ctx->stab_edge = -1;  // the tables read the edge's child CLV at every evaluation
     } else {
       g_create_error = "host allocation failed";
     }
@@ -2022,6 +2024,7 @@ int guarded(netlk_ctx *ctx, F &&f) {
     if (ctx) {
       ctx->err = e.what();
       ctx->clv_valid = false;
+      ctx->stab_edge = -1;  // the tables read the edge's child CLV at every evaluation
     } else {
       g_create_error = e.what();
     }

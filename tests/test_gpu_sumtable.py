@@ -224,3 +224,32 @@ def test_newton_raphson_pass_on_tables_matches_the_oracle(variant):
             assert logl == pytest.approx(want_logl, rel=rel_logl)
             a, b = np.array(lengths), np.array(want_len)
             assert np.all(np.abs(a - b) <= np.maximum(abs_len, rel_len * np.abs(b))), precision
+
+
+def test_unsupported_contexts_and_failures():
+    """Contexts the tables do not serve report NETLK_ERR_UNSUPPORTED and stay
+    usable; a failure injected into an evaluation surfaces with its status,
+    drops the tables (they read the edge's child CLV on every evaluation) and
+    the next call rebuilds them with the same results."""
+    from netrax_gb300 import _native as N
+    name = "threeReticulations"
+    with _lik(name) as ref:
+        want = ref.edge_sumtable_derivatives(3, 0.2)
+    from netrax_gb300.likelihood import NetworkLikelihood
+    from netrax_gb300.network import parse_extended_newick
+    net = parse_extended_newick(CASES[name]["newick"])
+    parts = [GoldenPartition(d) for d in CASES[name]["partitions"]]
+    with NetworkLikelihood(net, parts, precision="fp64", checkpoint_segments=2) as ck:
+        base = ck.loglikelihood()
+        assert ck.edge_sumtable(3) == (False, 0)
+        with pytest.raises(N.NetlkError) as ei:
+            ck.edge_sumtable_derivatives(3, 0.2)
+        assert ei.value.status == 7  # UNSUPPORTED
+        assert ck.loglikelihood() == base
+    with _lik(name) as lik:
+        assert lik.edge_sumtable(3)[0]
+        N.check(N.lib().netlk_inject_failure(lik._h, N.NETLK_ERR_TIMEOUT))
+        with pytest.raises(N.NetlkError) as ei:
+            lik.edge_sumtable_derivatives(3, 0.2)
+        assert ei.value.status == N.NETLK_ERR_TIMEOUT
+        assert lik.edge_sumtable_derivatives(3, 0.2) == want
