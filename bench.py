@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--variant", default="AVERAGE", choices=["AVERAGE", "BEST"])
     ap.add_argument("--fp64-steps", type=int, default=20)
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-checkpoint-arm", action="store_true",
+                    help="skip timing the same workload with 4 CLV checkpoint segments")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--scale", type=float, default=1.0, help="site-count scale (1.0 = full workload)")
     ap.add_argument("--checkpoint-segments", type=int, default=0,
@@ -331,6 +333,34 @@ def run_netlk(args, ws, rank, local):
                 "max_abs_retprob_grad_err": float(np.abs(r32 - r64).max()) if len(r64) else 0.0,
                 "kernel_ms": {k: (v[0] / v[1] if v[1] else 0.0) for k, v in kt64.items()}}
 
+    # ----------------------------------- the same workload with 4 CLV checkpoints
+    ckpt = None
+    if not args.no_checkpoint_arm and args.precision == "fp32" and args.checkpoint_segments == 0:
+        likc = NetworkLikelihood(w.network, w.partitions, variant=args.variant, precision="fp32",
+                                 device=local, checkpoint_segments=4)
+        lc, gc, rc = likc.loglikelihood_gradient()
+        sc = torch.cuda.ExternalStream(likc.stream(), device=dev)
+        for k in range(3):
+            likc.set_branch_lengths_device(dev_bl[k].data_ptr())
+            likc.enqueue(True)
+        torch.cuda.synchronize()
+        Kc = max(3, args.fp64_steps)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(sc)
+        for k in range(Kc):
+            likc.set_branch_lengths_device(dev_bl[W + k % K].data_ptr())
+            likc.enqueue(True)
+        b.record(sc)
+        b.synchronize()
+        msc = a.elapsed_time(b) / Kc
+        stc = likc.stats
+        likc.close()
+        ckpt = {"checkpoint_segments": stc["checkpoint_segments"], "evals_per_s": 1000.0 / msc,
+                "ms_per_step": msc, "clv_buffers": stc["clv_slots"], "dag_variants": stc["n_variants"],
+                "recompute_site_updates_per_eval": stc["recompute_site_updates"],
+                "logl_and_gradient_bit_identical_to_unsegmented": bool(lc == l32 and np.array_equal(gc, g32)
+                                                                       and np.array_equal(rc, r32))}
+
     # ------------------------------------------------------------- roofline
     peak, peak_kind = measured_peak()
     st = lik.stats  # after tuning: launch counts of the chosen shapes
@@ -389,6 +419,7 @@ def run_netlk(args, ws, rank, local):
                     "ms_per_step": e2e_s * 1000.0},
             "roofline": roofline,
             "fp64_plain": fp64,
+            "checkpointed": ckpt,
             "clocks": clocks,
             "cpu_baseline": cpu,
             "logl": l32,
