@@ -379,7 +379,9 @@ int netlk_last_site_updates(const netlk_ctx *ctx, int64_t *site_updates);
  *   at the edge).
  * With unlinked lengths d1 / d2 are w.r.t. moving every partition's length
  * of the edge together (the sum of the partition shares); with scaled
- * lengths w.r.t. the linked length (sum of s_p x and s_p^2 x the shares).
+ * lengths w.r.t. the linked length (sum of s_p x and s_p^2 x the shares),
+ * mode 0 only: mode 1 returns NETLK_ERR_UNSUPPORTED there, as the
+ * reference's formula throws for scaled lengths (LikelihoodDerivatives.cpp:42-46).
  * Both derivatives are analytic. DNA contexts evaluate the edge's sumtables
  * (netlk_edge_sumtable below) at the current lengths: built on the first
  * call for the edge and kept while only that edge's lengths change, so a

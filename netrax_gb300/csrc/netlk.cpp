@@ -365,6 +365,13 @@ struct netlk_ctx {
   // part >= 0: that partition's share only
   bool edge_derivs_analytic(int e, int mode, double *d1, double *d2, int part = -1);
   void setup_tangent_blocks();
+  // mode 1 reproduces the reference's derivative formula, which refuses
+  // scaled branch lengths (LikelihoodDerivatives.cpp:42-46)
+  void check_reference_mode(int mode) const {
+    if (mode == 1 && linkage == NETLK_BRLEN_SCALED)
+      throw Error(NETLK_ERR_UNSUPPORTED,
+                  "the reference's derivative formula (mode 1) does not take scaled branch lengths; mode 0 does");
+  }
   TanParams tan_params() const {  // the fields shared by the tangent and sumtable sweeps
     TanParams tp{};
     tp.n_patterns = N;
@@ -2490,6 +2497,7 @@ int netlk_edge_derivatives(netlk_ctx *ctx, int32_t edge, int32_t mode, double *d
   return guarded(ctx, [&] {
     if (edge < 0 || edge >= ctx->topo.n_edges) throw Error(NETLK_ERR_INVALID_ARGUMENT, "edge");
     if (mode != 0 && mode != 1) throw Error(NETLK_ERR_INVALID_ARGUMENT, "mode must be 0 or 1");
+    ctx->check_reference_mode(mode);
     // DNA: the edge's sumtables evaluated at the current lengths (built on
     // the first call for the edge and kept while only its lengths change,
     // so a Newton-Raphson loop that sets each proposal and asks for the
@@ -2601,6 +2609,7 @@ int netlk_edge_derivatives_partition(netlk_ctx *ctx, int32_t edge, int32_t part,
     if (edge < 0 || edge >= ctx->topo.n_edges) throw Error(NETLK_ERR_INVALID_ARGUMENT, "edge");
     if (part < 0 || part >= ctx->P) throw Error(NETLK_ERR_INVALID_ARGUMENT, "partition");
     if (mode != 0 && mode != 1) throw Error(NETLK_ERR_INVALID_ARGUMENT, "mode must be 0 or 1");
+    ctx->check_reference_mode(mode);
     // DNA: the edge's sumtables, every partition at its own current length
     if (!ctx->device_brlen && (ctx->sumtable_current(edge) || ctx->sumtable_build(edge))) {
       const int E = ctx->topo.n_edges, P = ctx->P;
@@ -2634,6 +2643,7 @@ int netlk_edge_sumtable_derivatives(netlk_ctx *ctx, int32_t edge, const double *
     const int E = ctx->topo.n_edges, P = ctx->P;
     if (edge < 0 || edge >= E) throw Error(NETLK_ERR_INVALID_ARGUMENT, "edge");
     if (mode != 0 && mode != 1) throw Error(NETLK_ERR_INVALID_ARGUMENT, "mode must be 0 or 1");
+    ctx->check_reference_mode(mode);
     if (!lengths || !(n_lengths == 1 || (n_lengths == P && ctx->linkage == NETLK_BRLEN_UNLINKED)))
       throw Error(NETLK_ERR_INVALID_ARGUMENT, "one length, or one per partition on an unlinked context");
     check_finite(lengths, n_lengths, "branch length", 0.0, 1e300);

@@ -76,3 +76,19 @@ def test_set_model_equals_a_fresh_context_and_the_oracle(precision):
               for p in new_parts]
     want = improved.ImprovedOracle(newick.parse_newick(CASE["newick"]), oparts).loglikelihood()
     assert t1 == pytest.approx(want, rel=1e-9 if precision == "fp64" else 1e-6)
+
+
+def test_reference_formula_refuses_scaled_lengths():
+    """Mode 1 (the reference's derivative formula) on a scaled-linkage
+    context returns NETLK_ERR_UNSUPPORTED before any device work, as the
+    reference throws for scaled lengths (LikelihoodDerivatives.cpp:42-46);
+    the sumtable entry refuses the same way."""
+    from netrax_gb300 import _native
+    from netrax_gb300.likelihood import NetworkLikelihood
+    net, parts = _net_parts()
+    with NetworkLikelihood(net, parts, host_only=True, brlen_linkage="scaled") as lik:
+        for call in (lambda: lik.edge_derivatives(0, mode=1), lambda: lik.edge_derivatives_partition(0, 0, mode=1),
+                     lambda: lik.edge_sumtable_derivatives(0, 0.1, mode=1)):
+            with pytest.raises(_native.NetlkError) as e:
+                call()
+            assert e.value.status == 7 and "scaled" in str(e.value)
