@@ -125,7 +125,9 @@ def test_random_networks_match_oracle(seed, precision):
     test_dag_random.py), 40 simulated-free random patterns: logL against the
     DAG oracle (FP64 1e-9, FP32 1e-6) and the adjoint gradient against the
     analytic derivative oracle (FP64 1e-8, FP32 1e-4 plus 1e-4 of the largest
-    entry), AVERAGE and BEST."""
+    entry), AVERAGE and BEST; edge sumtables at a proposed length on three
+    edges against the oracle at that length (logL as above, d1 and d2 FP64
+    1e-8, FP32 d1 1e-4 and d2 5e-4 of the gradient scale)."""
     from netrax_gb300.likelihood import NetworkLikelihood
     from netrax_gb300.network import parse_extended_newick
     from oracle import derivatives, improved, newick as onewick, pllmath
@@ -148,10 +150,30 @@ def test_random_networks_match_oracle(seed, precision):
         orc = improved.ImprovedOracle(onet, [opart], variant=variant)
         want_logl = orc.loglikelihood()
         g, gr = derivatives.EdgeDerivativeOracle(orc).gradient()
+        # edge sumtables at a proposed length (three edges) against the
+        # oracle with that length: logL, d1, d2
+        edges = rng.choice(net.n_edges, size=min(3, net.n_edges), replace=False)
+        stab = {}
         with NetworkLikelihood(net, [part], variant=variant, precision=precision) as lik:
             total, gb, gbr = lik.loglikelihood_gradient()
+            for e in edges:
+                stab[int(e)] = lik.edge_sumtable_derivatives(int(e), 0.37 * lik.branch_lengths[e] + 0.01)
         assert total == pytest.approx(want_logl, rel=1e-9 if precision == "fp64" else 1e-6), text
         ok, worst = _close(gb, g, rel, absf)
         assert ok, (variant, worst, text)
         ok, worst = _close(gbr, gr, rel, absf)
         assert ok, (variant, worst, text)
+        for e, (l, d1, d2) in stab.items():
+            t0 = orc.brlen[e]
+            orc.brlen[e] = 0.37 * t0 + 0.01
+            wl = orc.loglikelihood()
+            w1, w2 = derivatives.EdgeDerivativeOracle(orc).edge(e)
+            orc.brlen[e] = t0
+            orc.loglikelihood()
+            assert l == pytest.approx(wl, rel=1e-9 if precision == "fp64" else 1e-6), (variant, e, text)
+            scale = max(1.0, float(np.abs(g).max()))
+            # FP32 d2: per-site L''/L - (L'/L)^2 cancels in FP32 (measured worst
+            # on these networks 1.1e-4 of the scale)
+            tol1, tol2 = (1e-8, 1e-8) if precision == "fp64" else (1e-4, 5e-4)
+            assert abs(d1 - w1) <= tol1 * max(scale, abs(w1)), (variant, e, d1, w1, text)
+            assert abs(d2 - w2) <= tol2 * max(scale, abs(w2)), (variant, e, d2, w2, text)
