@@ -402,8 +402,10 @@ int netlk_edge_derivatives(netlk_ctx *ctx, int32_t edge, int32_t mode,
  * w.r.t. its own length of the edge - the df[p] / ddf[p] the reference's
  * Newton-Raphson callback returns for unlinked lengths
  * (BranchLengthOptimization.cpp:189-195). On linked and scaled contexts the
- * same per-partition terms (w.r.t. the partition's effective length). Needs
- * one checkpoint segment and host lengths. */
+ * same per-partition terms (w.r.t. the partition's effective length). DNA
+ * contexts evaluate the edge's sumtables, each partition at its current
+ * length; 20-state ones run the tangent sweep. Needs one checkpoint segment
+ * and host lengths. */
 int netlk_edge_derivatives_partition(netlk_ctx *ctx, int32_t edge, int32_t partition, int32_t mode, double *d1,
                                      double *d2);
 
