@@ -10,6 +10,9 @@ oracle (test harness; not a test module itself).
   pll-modules' ``pllmod_opt_minimize_newton_multi``, not vendored) with bounds
   [brlen_min, brlen_max] and tolerance brlen_min / 10 (:218-236), and the old
   length restored if the log-likelihood got worse (:317-330).
+* Branch lengths by Brent (the reference's BRENT_REROOT / BRENT_NORMAL
+  methods), ``optimize_branch_brent`` (BranchLengthOptimization.cpp:112-160)
+  per edge on the edge log-likelihood.
 * Reticulation probabilities, ``optimize_reticulations``
   (src/optimization/ReticulationOptimization.cpp:104-118): per reticulation a
   Brent minimisation of -logL over [brprob_min, brprob_max]
@@ -137,6 +140,22 @@ def optimize_branches(edge_logl, edge_derivs, lengths, max_iters=30, derivs_at=N
         worse = worse or (logl is not None and new < logl - 1e-6 * abs(logl))
         logl = new
     return lengths, logl, worse
+
+
+def optimize_branches_brent(logl_at, set_length, lengths, tol):
+    """One pass of optimize_branch_brent (BranchLengthOptimization.cpp:112-160)
+    over every edge: Brent on -logL within [brlen_min, brlen_max] from the
+    current length. logl_at(e, t): logL with edge e at t (nothing kept - the
+    reference's BRENT_REROOT evaluates computeLoglikelihoodBrlenOpt);
+    set_length(e, t): keep t and return the logL. Returns the final lengths
+    and logL."""
+    lengths = list(lengths)
+    logl = None
+    for e in range(len(lengths)):
+        x, fx = brent_minimize(lambda t, e=e: -logl_at(e, t), BRLEN_MIN, BRLEN_MAX, lengths[e], tol)
+        lengths[e] = x
+        logl = set_length(e, x)
+    return lengths, logl
 
 
 def optimize_reticulations(logl_at, probs, tol, max_passes=10):

@@ -253,3 +253,49 @@ def test_unsupported_contexts_and_failures():
             lik.edge_sumtable_derivatives(3, 0.2)
         assert ei.value.status == N.NETLK_ERR_TIMEOUT
         assert lik.edge_sumtable_derivatives(3, 0.2) == want
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_brent_branch_pass_on_tables_matches_the_oracle(precision):
+    """The reference's Brent branch-length pass (BRENT_REROOT: every probe an
+    edge log-likelihood) with each probe one table evaluation, against the
+    same pass on the oracle: FP64 final lengths within 1e-4 relative or 1e-6
+    absolute and final logL within 1e-9; FP32 (noisier probes) final logL
+    within 1e-4; the pass never lowers the logL."""
+    from oracle import improved, newick, pllmath
+    name = "twoReticulations"
+    parts = []
+    for d in CASES[name]["partitions"]:
+        gp = GoldenPartition(d)
+        parts.append(improved.Partition(gp.tip_states, gp.weights, gp.freqs, gp.exch,
+                                        pllmath.gamma_rates_mean(gp.alpha, 4)))
+    orc = improved.ImprovedOracle(newick.parse_newick(CASES[name]["newick"]), parts)
+    orc.loglikelihood()
+
+    def orc_at(e, t):
+        t0 = orc.brlen[e]
+        orc.brlen[e] = t
+        v = orc.loglikelihood()
+        orc.brlen[e] = t0
+        return v
+
+    def orc_set(e, t):
+        orc.brlen[e] = t
+        return orc.loglikelihood()
+
+    tol = 1e-7
+    want_len, want_logl = opt.optimize_branches_brent(orc_at, orc_set, list(orc.brlen), tol)
+    with _lik(name, precision) as lik:
+        start = lik.loglikelihood()
+        lengths, logl = opt.optimize_branches_brent(lambda e, t: lik.edge_sumtable_derivatives(e, t)[0],
+                                                    lik.edge_loglikelihood, lik.branch_lengths, tol)
+        assert logl >= start
+        if precision == "fp64":
+            assert logl == pytest.approx(want_logl, rel=1e-9)
+            a, b = np.array(lengths), np.array(want_len)
+            assert np.all(np.abs(a - b) <= np.maximum(1e-6, 1e-4 * np.abs(b))), np.abs(a - b).max()
+        else:
+            # FP32 probes carry ~1e-7 relative noise, so Brent settles at
+            # slightly different points on flat edges (here a few 1e-3 of logL
+            # on a -85.8 network, in either direction)
+            assert logl == pytest.approx(want_logl, rel=1e-4)
