@@ -448,6 +448,22 @@ int netlk_edge_sumtable(netlk_ctx *ctx, int32_t edge, int32_t *built, int32_t *n
  * segments or device-resident lengths get NETLK_ERR_UNSUPPORTED there. */
 int netlk_edge_sumtable_derivatives(netlk_ctx *ctx, int32_t edge, const double *lengths, int32_t n_lengths,
                                     int32_t mode, double *logl, double *d1, double *d2);
+/* The walk of an edge's table build, for checks of the host schedule (works
+ * on host-only contexts). No counterpart in the reference (introspection of
+ * netlk_edge_sumtable). Counts: n_ops ops (the variants whose subtree holds
+ * the edge), n_work work slots, n_tables tables (displayed-tree roots among
+ * them), n_groups child groups. Arrays (NULL: counts only):
+ *   ops [7 * n_ops]   per op in walk order: variant x, its child on the
+ *                     edge's side d and the other child o (refs as in
+ *                     netlk_dag_export), mode (1: d hangs from the edge,
+ *                     2: d's subtree holds it), work slot read (-1 for
+ *                     mode 1), work slot written (-1: no later op reads
+ *                     it), table written (-1: x is no displayed-tree root)
+ *   group_ref [n_groups]        child whose CLV the edge's message starts
+ *                               from, for the group's tables
+ *   group_begin [n_groups + 1]  each group's table range */
+int netlk_sumtable_export(const netlk_ctx *ctx, int32_t edge, int32_t *n_ops, int32_t *n_work, int32_t *n_tables,
+                          int32_t *n_groups, int32_t *ops, int32_t *group_ref, int32_t *group_begin);
 
 /* ------------------------------------------------- sharded (multi-rank) use */
 /* Per-(root variant, partition) log-likelihood partial sums over the patterns

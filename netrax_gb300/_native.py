@@ -42,7 +42,7 @@ EXPORTED = [
     "netlk_walk_segments", "netlk_batch_create_ex", "netlk_batch_info",
     "netlk_set_prop_invar", "netlk_set_partition_branch_lengths", "netlk_set_branch_length_scalers",
     "netlk_partition_gradient", "netlk_edge_loglikelihood_partition", "netlk_edge_derivatives_partition",
-    "netlk_edge_sumtable", "netlk_edge_sumtable_derivatives",
+    "netlk_edge_sumtable", "netlk_edge_sumtable_derivatives", "netlk_sumtable_export",
 ]
 NETLK_BRLEN_LINKED, NETLK_BRLEN_UNLINKED, NETLK_BRLEN_SCALED = 0, 1, 2
 
@@ -138,6 +138,8 @@ def lib():
                                       ctypes.POINTER(ctypes.c_int32)]
     L.netlk_edge_sumtable_derivatives.argtypes = [vp, ctypes.c_int32, c_double_p, ctypes.c_int32, ctypes.c_int32,
                                                   c_double_p, c_double_p, c_double_p]
+    i32p = ctypes.POINTER(ctypes.c_int32)
+    L.netlk_sumtable_export.argtypes = [vp, ctypes.c_int32, i32p, i32p, i32p, i32p, i32p, i32p, i32p]
     L.netlk_loglikelihood.argtypes = [vp, c_double_p, c_double_p, c_double_p]
     L.netlk_loglikelihood_gradient.argtypes = [vp, c_double_p, c_double_p, c_double_p, c_double_p]
     L.netlk_edge_derivatives.argtypes = [vp, ctypes.c_int32, ctypes.c_int32, c_double_p, c_double_p]

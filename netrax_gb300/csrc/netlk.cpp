@@ -420,6 +420,14 @@ struct netlk_ctx {
   // checkpoint segments, device-resident lengths, too little memory);
   // current while only edge e's lengths and nothing else changed since
   bool sumtable_build(int e);
+  // The walk of edge e's table build: ops in depth-first order with work
+  // slots (walk_order), their slot fields renumbered to table indices, the
+  // tables grouped by the child whose CLV the edge's message starts from
+  // (gref: that child per group, gbegin: [n_groups + 1] table ranges),
+  // slot_tab: table of each displayed-tree root slot (-1: edge not in it).
+  // Returns the work slots used, or -1.
+  int sumtable_schedule(int e, std::vector<TanOp> &ops, std::vector<int32_t> &gref, std::vector<int32_t> &gbegin,
+                        std::vector<int32_t> &slot_tab) const;
   // Reorders a tangent schedule depth-first for one walk (each op right
   // before the ops that read its directions) and reassigns the work slots
   // by live range in that order; returns the slots used, or -1.
@@ -1622,6 +1630,41 @@ int netlk_ctx::walk_order(std::vector<TanOp> &ops) {
   return used;
 }
 
+int netlk_ctx::sumtable_schedule(int e, std::vector<TanOp> &ops, std::vector<int32_t> &gref,
+                                 std::vector<int32_t> &gbegin, std::vector<int32_t> &slot_tab) const {
+  std::vector<int32_t> lb, dslots;
+  gref.clear();
+  gbegin.clear();
+  slot_tab.assign(n_slots, -1);
+  if (tangent_schedule(e, ops, lb, dslots) < 0) return -1;
+  const int need = walk_order(ops);
+  if (need < 0) return -1;
+  // the child whose CLV each root's path starts from (the message e carries);
+  // tables sorted by it so the evaluation forms P I once per child
+  std::vector<int32_t> origin(ops.size()), op_of(dag.vars.size(), -1);
+  std::vector<std::pair<int32_t, int32_t>> roots_by_child;  // (child ref, op)
+  for (size_t j = 0; j < ops.size(); ++j) {
+    op_of[ops[j].x] = (int32_t)j;
+    origin[j] = ops[j].mode == 1 ? ops[j].d : origin[op_of[ops[j].d]];
+    if (ops[j].slot >= 0) roots_by_child.push_back({origin[j], (int32_t)j});
+  }
+  std::stable_sort(roots_by_child.begin(), roots_by_child.end(),
+                   [](const std::pair<int32_t, int32_t> &a, const std::pair<int32_t, int32_t> &b) {
+                     return a.first < b.first;
+                   });
+  for (size_t t = 0; t < roots_by_child.size(); ++t) {
+    TanOp &op = ops[roots_by_child[t].second];
+    slot_tab[op.slot] = (int32_t)t;
+    op.slot = (int32_t)t;
+    if (gref.empty() || gref.back() != roots_by_child[t].first) {
+      gref.push_back(roots_by_child[t].first);
+      gbegin.push_back((int32_t)t);
+    }
+  }
+  gbegin.push_back((int32_t)roots_by_child.size());
+  return need;
+}
+
 bool netlk_ctx::sumtable_current(int e) const {
   if (stab_edge != e || stab_gen != model_gen || device_brlen || stab_probs != ret_probs) return false;
   const std::vector<double> &L = dev_len();
@@ -1686,36 +1729,12 @@ bool netlk_ctx::sumtable_build(int e) {
     stab_cap_tab = tabs;
   }
   std::vector<TanOp> ops;
-  std::vector<int32_t> lb, dslots;
-  if (tangent_schedule(e, ops, lb, dslots) < 0) return false;
-  const int need = walk_order(ops);
-  lb.assign({0, (int32_t)ops.size()});  // one walk over every op
-  if (need < 0 || need > stab_cap_work || stab_cap_work == 0 || (int)dslots.size() > stab_cap_tab) return false;
-  // the child whose CLV each root's path starts from (the message e carries);
-  // tables sorted by it so the evaluation forms P I once per child
-  std::vector<int32_t> origin(ops.size()), op_of(dag.vars.size(), -1);
-  std::vector<std::pair<int32_t, int32_t>> roots_by_child;  // (child ref, op)
-  for (size_t j = 0; j < ops.size(); ++j) {
-    op_of[ops[j].x] = (int32_t)j;
-    origin[j] = ops[j].mode == 1 ? ops[j].d : origin[op_of[ops[j].d]];
-    if (ops[j].slot >= 0) roots_by_child.push_back({origin[j], (int32_t)j});
-  }
-  std::stable_sort(roots_by_child.begin(), roots_by_child.end(),
-                   [](const std::pair<int32_t, int32_t> &a, const std::pair<int32_t, int32_t> &b) {
-                     return a.first < b.first;
-                   });
-  std::vector<int32_t> slot_tab(n_slots, -1), gref, gbegin;
-  for (size_t t = 0; t < roots_by_child.size(); ++t) {
-    TanOp &op = ops[roots_by_child[t].second];
-    slot_tab[op.slot] = (int32_t)t;
-    op.slot = (int32_t)t;
-    if (gref.empty() || gref.back() != roots_by_child[t].first) {
-      gref.push_back(roots_by_child[t].first);
-      gbegin.push_back((int32_t)t);
-    }
-  }
-  gbegin.push_back((int32_t)roots_by_child.size());
-  stab_n_tab = (int)roots_by_child.size();
+  std::vector<int32_t> gref, gbegin, slot_tab;
+  const int need = sumtable_schedule(e, ops, gref, gbegin, slot_tab);
+  const int n_tab = gbegin.empty() ? 0 : gbegin.back();
+  if (need < 0 || need > stab_cap_work || stab_cap_work == 0 || n_tab > stab_cap_tab) return false;
+  const int32_t lb[2] = {0, (int32_t)ops.size()};  // one walk over every op
+  stab_n_tab = n_tab;
   stab_n_groups = (int)gref.size();
   stab_root_tab.assign(dag.roots.size(), -1);
   for (size_t i = 0; i < dag.roots.size(); ++i) stab_root_tab[i] = slot_tab[root_slot[i]];
@@ -1731,7 +1750,7 @@ bool netlk_ctx::sumtable_build(int e) {
     std::memcpy(hg + gref.size(), gbegin.data(), gbegin.size() * 4);
     CUDA_OK(cudaMemcpyAsync(d_stab_groups.p, hg, (gref.size() + gbegin.size()) * 4, cudaMemcpyHostToDevice, stream));
     StabParams sp = stab_params();
-    if (!launch_sumtable_build(stream, opts.precision, R, S, sp, lb.data(), 1)) return false;
+    if (!launch_sumtable_build(stream, opts.precision, R, S, sp, lb, 1)) return false;
   }
   const int nout = 3 + P + topo.n_ret;
   CUDA_OK(cudaMemcpyAsync(h_out.p, d_out.p, nout * 8, cudaMemcpyDeviceToHost, stream));
@@ -2692,6 +2711,31 @@ int netlk_edge_sumtable_derivatives(netlk_ctx *ctx, int32_t edge, const double *
       }
     }
   });
+}
+
+int netlk_sumtable_export(const netlk_ctx *ctx, int32_t edge, int32_t *n_ops, int32_t *n_work, int32_t *n_tables,
+                          int32_t *n_groups, int32_t *ops, int32_t *group_ref, int32_t *group_begin) {
+  if (!ctx || edge < 0 || edge >= ctx->topo.n_edges) return NETLK_ERR_INVALID_ARGUMENT;
+  try {  // introspection: a failure leaves the context as it was
+    std::vector<TanOp> o;
+    std::vector<int32_t> gref, gbegin, slot_tab;
+    const int need = ctx->sumtable_schedule(edge, o, gref, gbegin, slot_tab);
+    if (need < 0) return NETLK_ERR_UNSUPPORTED;
+    if (n_ops) *n_ops = (int32_t)o.size();
+    if (n_work) *n_work = need;
+    if (n_tables) *n_tables = gbegin.back();
+    if (n_groups) *n_groups = (int32_t)gref.size();
+    if (ops)
+      for (size_t i = 0; i < o.size(); ++i) {
+        const int32_t row[7] = {o[i].x, o[i].d, o[i].o, o[i].mode, o[i].td, o[i].tx, o[i].slot};
+        for (int k = 0; k < 7; ++k) ops[7 * i + k] = row[k];
+      }
+    if (group_ref) std::copy(gref.begin(), gref.end(), group_ref);
+    if (group_begin) std::copy(gbegin.begin(), gbegin.end(), group_begin);
+  } catch (const std::bad_alloc &) {
+    return NETLK_ERR_OUT_OF_MEMORY;
+  }
+  return NETLK_OK;
 }
 
 int netlk_set_partition_branch_lengths(netlk_ctx *ctx, int32_t part, const double *b, int32_t n) {

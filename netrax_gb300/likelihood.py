@@ -207,6 +207,21 @@ class NetworkLikelihood:
             return tuple(float(o[0]) for o in out)
         return tuple(out)
 
+    def sumtable_export(self, edge):
+        """The walk of an edge's table build: (ops [n, 7] = (x, d, o, mode,
+        work slot read, work slot written, table), work slots, tables,
+        group_ref, group_begin)."""
+        n, w, t, g = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        N.check(N.lib().netlk_sumtable_export(self._h, int(edge), ctypes.byref(n), ctypes.byref(w), ctypes.byref(t),
+                                              ctypes.byref(g), None, None, None), self._h)
+        ops = np.zeros(7 * max(1, n.value), np.int32)
+        gref = np.zeros(max(1, g.value), np.int32)
+        gbeg = np.zeros(g.value + 1, np.int32)
+        N.check(N.lib().netlk_sumtable_export(self._h, int(edge), ctypes.byref(n), ctypes.byref(w), ctypes.byref(t),
+                                              ctypes.byref(g), _ptr(ops, ctypes.c_int32), _ptr(gref, ctypes.c_int32),
+                                              _ptr(gbeg, ctypes.c_int32)), self._h)
+        return ops[:7 * n.value].reshape(-1, 7), w.value, t.value, gref[:g.value], gbeg
+
     def set_prop_invar(self, part, prop_invar):
         """Proportion of invariant sites (+I) of one partition."""
         N.check(N.lib().netlk_set_prop_invar(self._h, int(part), float(prop_invar)), self._h)
