@@ -387,6 +387,17 @@ __global__ void __launch_bounds__(256) sumtable_walk_kernel(const StabParams sp,
   real *dir = static_cast<real *>(p.tan);
   for (int j = 0; j < n_ops; ++j) {
     const TanOp op = p.ops[j];
+    if (j + 1 < n_ops) {  // ask L2 for the next op's other child (a CLV written long before)
+      const int32_t on = __ldg(&p.ops[j + 1].o);
+      if (on >= 0) {
+#pragma unroll
+        for (int q = 0; q < PPL; ++q) {
+          const int64_t s = s0 + q * PPW;
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(static_cast<const real *>(p.clv) +
+                                                        (((size_t)on * p.n_patterns + s) * R + r) * S));
+        }
+      }
+    }
     real M[S * S], c[PPL][S], vo[PPL][S];
     int k[PPL], sx[PPL];
 #pragma unroll
