@@ -14,6 +14,13 @@
 // sumtables at the virtually rerooted branch
 // (src/likelihood/LikelihoodDerivatives.cpp:249-344, pll_compute_loglikelihood_derivatives
 // at :95-104) and combines them at :13-188.
+//
+// Edge sumtables (DNA): the same forward-mode sweep with the S unit
+// directions of e's message m = P_e I in place of the two tangents gives, at
+// every displayed-tree root, its outside vector O = dL/dm per (pattern,
+// rate); a Newton-Raphson iterate at length t is then one pass over those
+// tables, L = sum_r O_r . (P_r(t) I_r) and L', L'' with P', P''
+// (sumtable_walk_kernel builds them, sumtable_eval_kernel evaluates them).
 #include <cuda_runtime.h>
 
 #include <cstdint>
