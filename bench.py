@@ -162,9 +162,8 @@ class ClockSampler:
 
 
 # DRAM bytes per site-CLV update of each sweep (DNA: 4 states) from one ncu capture
-# (profiles/sweep_dram_traffic_config2_scale0.3.md: dram__bytes_read.sum +
-# dram__bytes_write.sum of the 100-taxon / 8-reticulation network at 0.3 of its
-# sites, scaled by updates; writes still dirty in L2 at a launch's end are not
+# (dram__bytes_read.sum + dram__bytes_write.sum of the 100-taxon /
+# 8-reticulation network at 0.3 of its sites, scaled by updates; writes still dirty in L2 at a launch's end are not
 # counted). Keyed by sweep, schedule (level: one launch per DAG level; walk:
 # one warp walks the whole DAG), precision and states. The level figures were
 # captured before the adjoint dropped read messages from L2, so they are an

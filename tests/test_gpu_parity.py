@@ -1,6 +1,6 @@
 """GPU parity: the CUDA path through the C ABI against the CPU oracle.
 
-Tolerances (the benchmark spec): plain FP64 GPU kernel within 1e-9 relative logL of the
+Tolerances: plain FP64 GPU kernel within 1e-9 relative logL of the
 oracle; FP32 CLVs with power-of-two scaling within 1e-6 relative; FP64 scale
 counters bit-exact; displayed-tree enumeration bit-exact (checked on CPU in
 test_dag_abi.py and here through the per-tree values). Gradients against
