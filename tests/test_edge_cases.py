@@ -115,9 +115,12 @@ def test_ten_reticulations():
 @pytest.mark.parametrize("states,rate_cats", [(4, 1), (4, 2), (4, 8), (20, 1), (20, 2)])
 def test_rate_category_counts(states, rate_cats):
     """Rate-category counts other than 4 (DNA 1/2/8, protein 1/2; the
-    CUDA-core sweeps) against the oracle, with a finite gradient."""
+    CUDA-core sweeps) against the oracle, with a finite gradient; DNA also
+    the edge sumtables (their build walk and bulk-copy evaluation for this
+    rate count) at a proposed length against the oracle's logL and sumtable
+    derivatives there."""
     from netrax_gb300.likelihood import NetworkLikelihood
-    from oracle import improved, newick, pllmath
+    from oracle import derivatives, improved, newick, pllmath
     rng = np.random.default_rng(10 + states + rate_cats)
     text = synth.random_network_newick(rng, 10, 2)
     n = 60
@@ -126,13 +129,29 @@ def test_rate_category_counts(states, rate_cats):
     exch = rng.gamma(1.0, 1.0, size=states * (states - 1) // 2) + 1e-3
     part = synth.PartitionData(codes, np.ones(n), freqs, exch, 0.6, n, rate_cats=rate_cats, states=states)
     opart = improved.Partition(codes, np.ones(n), freqs, exch, pllmath.gamma_rates_mean(0.6, rate_cats))
-    want = improved.ImprovedOracle(newick.parse_newick(text), [opart], variant="AVERAGE").loglikelihood()
+    orc = improved.ImprovedOracle(newick.parse_newick(text), [opart], variant="AVERAGE")
+    want = orc.loglikelihood()
     net = parse_extended_newick(text)
+    stab_want = {}
+    if states == 4:
+        g_scale = max(1.0, float(np.abs(derivatives.EdgeDerivativeOracle(orc).gradient()[0]).max()))
+        for e in (0, 3):
+            t0 = orc.brlen[e]
+            orc.brlen[e] = 0.5 * t0 + 0.02
+            stab_want[e] = (orc.loglikelihood(),) + tuple(derivatives.EdgeDerivativeOracle(orc).edge(e))
+            orc.brlen[e] = t0
+            orc.loglikelihood()
     for prec, tol in (("fp64", FP64_REL), ("fp32", FP32_REL)):
         with NetworkLikelihood(net, [part], precision=prec) as lik:
             got, gb, gr = lik.loglikelihood_gradient()
             assert got == pytest.approx(want, rel=tol)
             assert np.all(np.isfinite(gb)) and np.all(np.isfinite(gr))
+            dtol = 1e-8 if prec == "fp64" else 1e-4
+            for e, (wl, w1, w2) in stab_want.items():
+                l, d1, d2 = lik.edge_sumtable_derivatives(e, 0.5 * net.branch_lengths[e] + 0.02)
+                assert l == pytest.approx(wl, rel=tol)
+                assert abs(d1 - w1) <= dtol * max(g_scale, abs(w1)), (prec, e, d1, w1)
+                assert abs(d2 - w2) <= dtol * max(g_scale, abs(w2)), (prec, e, d2, w2)
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
