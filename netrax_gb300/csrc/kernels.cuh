@@ -235,6 +235,9 @@ struct TanParams {
   const double *freqs;          // [n_parts][S]
   const double *rate_weights;   // [n_parts][R]
   const double *inv_term;       // invariant sites (+I), as in SweepParams; null without
+  const float *inv_term32;      // FP32 contexts: its float copy (the tangent walk reads it)
+  const float2 *weights32;      // FP32 contexts: pattern weights as (hi, lo) float pairs
+  int32_t ff;                   // 1: partials are float pairs (hi, lo) in each double's 8 bytes
   double *partial;              // [n_slots][2][n_blocks] sums of w L'/L and w (L''/L - (L'/L)^2)
 };
 
@@ -247,6 +250,11 @@ void launch_pderiv(cudaStream_t s, int n_parts, int R, int S, const double *lamb
 // an unsupported (R, S).
 bool launch_tangent(cudaStream_t s, int precision, int R, int S, const TanParams &p, const int32_t *level_begin,
                     int n_levels);
+// DNA: the same sweep as one walk launch over ops in walk order
+// (netlk_ctx::walk_order), partials per unit of tangent_walk_patterns_per_unit(R)
+// patterns: p.partial [n_slots][2][n_patterns / that]; false for S != 4.
+int tangent_walk_patterns_per_unit(int R);
+bool launch_tangent_walk(cudaStream_t s, int precision, int R, int S, const TanParams &p, int n_ops);
 // out [n_slots_total][n_parts][2] for the root slots listed in `slots`.
 void launch_tangent_reduce(cudaStream_t s, const TanParams &p, const int32_t *slots, int n_slots,
                            const int32_t *part_block_begin, int n_parts, double *out);

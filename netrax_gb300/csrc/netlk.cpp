@@ -172,7 +172,7 @@ struct netlk_ctx {
   DevBuf d_wfwd, d_wrfwd, d_wbwd, d_wmsg_slots;
   // analytic edge derivatives: tangent buffers and per-call schedule
   DevBuf d_tan, d_tan_ops, d_tan_partial, d_tan_out, d_pderiv64, d_pderiv32, d_block_part, d_part_block_begin,
-      d_tan_slots;
+      d_tan_slots, d_part_tunit_begin;
   PinnedBuf h_tan_ops, h_tan_out, h_tan_slots;
   int n_tan_cap = -1;  // tangent slot pairs allocated (-1: not set up yet)
   int tan_blocks = 0;
@@ -256,7 +256,7 @@ struct netlk_ctx {
                       &d_pderiv64, &d_pderiv32, &d_block_part, &d_part_block_begin, &d_tan_slots, &d_gfrac,
                       &d_gfrac32, &d_invt, &d_invt32, &d_grad_part, &d_op_sum_part, &d_part_unit_begin, &d_stab_work,
                       &d_stab, &d_stab_scaler, &d_stab_partial, &d_stab_out, &d_stab_pm3_64, &d_stab_pm3_32,
-                      &d_stab_groups, &d_stab_ops, &d_part_warp_begin})
+                      &d_stab_groups, &d_stab_ops, &d_part_warp_begin, &d_part_tunit_begin})
       b->free();
     if (stream) cudaStreamDestroy(stream);
   }
@@ -387,6 +387,10 @@ struct netlk_ctx {
     tp.freqs = d_freqs.as<double>();
     tp.rate_weights = d_rw.as<double>();
     tp.inv_term = has_pinv ? d_invt.as<double>() : nullptr;
+    if (opts.precision == NETLK_FP32) {
+      tp.inv_term32 = has_pinv ? d_invt32.as<float>() : nullptr;
+      tp.weights32 = d_weights32.as<float2>();
+    }
     return tp;
   }
   StabParams stab_params() const {
@@ -1407,12 +1411,19 @@ bool netlk_ctx::edge_derivs_analytic(int e, int mode, double *d1, double *d2, in
   prepare();
   const size_t real_b = opts.precision == NETLK_FP32 ? 4 : 8;
   const size_t plane = (size_t)N * R * S * real_b;  // one tangent plane (X' or X'')
+  // DNA: one walk launch over the ops in walk order; 20 states: one launch
+  // per level
+  const bool walk = S == 4;
+  const int64_t n_units = walk ? N / tangent_walk_patterns_per_unit(R) : 0;
   if (n_tan_cap < 0) {
     // set up once: the most tangent slots any edge needs, and the block maps
     int need = 0;
     std::vector<TanOp> ops;
     std::vector<int32_t> lb, sl;
-    for (int k = 0; k < topo.n_edges; ++k) need = std::max(need, tangent_schedule(k, ops, lb, sl));
+    for (int k = 0; k < topo.n_edges; ++k) {
+      const int nk = tangent_schedule(k, ops, lb, sl);
+      need = std::max(need, walk && nk >= 0 ? walk_order(ops) : nk);
+    }
     setup_tangent_blocks();
     size_t free_b = 0, total_b = 0;
     CUDA_OK(cudaMemGetInfo(&free_b, &total_b));
@@ -1423,7 +1434,14 @@ bool netlk_ctx::edge_derivs_analytic(int e, int mode, double *d1, double *d2, in
     int64_t scratch = 0;
     d_tan.alloc(std::max<size_t>(1, (size_t)need) * 2 * plane, scratch);
     d_tan_ops.alloc(dag.vars.size() * sizeof(TanOp), scratch);
-    d_tan_partial.alloc((size_t)std::max(1, n_slots) * 2 * tan_blocks * 8, scratch);
+    d_tan_partial.alloc((size_t)std::max(1, n_slots) * 2 * (walk ? n_units : tan_blocks) * 8, scratch);
+    if (walk) {
+      std::vector<int32_t> pub(P + 1);
+      for (int p = 0; p < P; ++p) pub[p] = (int32_t)(parts[p].offset / tangent_walk_patterns_per_unit(R));
+      pub[P] = (int32_t)n_units;
+      d_part_tunit_begin.alloc(pub.size() * 4, scratch);
+      CUDA_OK(cudaMemcpy(d_part_tunit_begin.p, pub.data(), pub.size() * 4, cudaMemcpyHostToDevice));
+    }
     d_tan_out.alloc((size_t)std::max(1, n_slots) * P * 2 * 8, scratch);
     d_tan_slots.alloc((size_t)std::max(1, n_slots) * 4, scratch);
     d_pderiv64.alloc((size_t)P * 2 * R * S * S * 8, scratch);
@@ -1436,7 +1454,8 @@ bool netlk_ctx::edge_derivs_analytic(int e, int mode, double *d1, double *d2, in
   }
   std::vector<TanOp> ops;
   std::vector<int32_t> lb, dslots;
-  const int need = tangent_schedule(e, ops, lb, dslots);
+  int need = tangent_schedule(e, ops, lb, dslots);
+  if (walk && need >= 0) need = walk_order(ops);
   if (need < 0 || need > n_tan_cap || n_tan_cap == 0) return false;
   // CLVs and per-tree logL at the current lengths
   if (!run_incremental()) run(&graph_logl, true, true, true, true, false);
@@ -1455,9 +1474,17 @@ bool netlk_ctx::edge_derivs_analytic(int e, int mode, double *d1, double *d2, in
     tp.tan = d_tan.p;
     tp.ops = d_tan_ops.as<TanOp>();
     tp.partial = d_tan_partial.as<double>();
-    if (!launch_tangent(stream, opts.precision, R, S, tp, lb.data(), dag.n_levels)) return false;
-    launch_tangent_reduce(stream, tp, d_tan_slots.as<int32_t>(), (int)dslots.size(),
-                          d_part_block_begin.as<int32_t>(), P, d_tan_out.as<double>());
+    if (walk) {
+      if (!launch_tangent_walk(stream, opts.precision, R, S, tp, (int)ops.size())) return false;
+      tp.n_blocks = (int32_t)n_units;  // the reduction's partials are per walk unit
+      tp.ff = opts.precision == NETLK_FP32;  // and float pairs in FP32 contexts
+      launch_tangent_reduce(stream, tp, d_tan_slots.as<int32_t>(), (int)dslots.size(),
+                            d_part_tunit_begin.as<int32_t>(), P, d_tan_out.as<double>());
+    } else {
+      if (!launch_tangent(stream, opts.precision, R, S, tp, lb.data(), dag.n_levels)) return false;
+      launch_tangent_reduce(stream, tp, d_tan_slots.as<int32_t>(), (int)dslots.size(),
+                            d_part_block_begin.as<int32_t>(), P, d_tan_out.as<double>());
+    }
     if (!dslots.empty())
       CUDA_OK(cudaMemcpyAsync(h_tan_out.p, d_tan_out.p, (size_t)n_slots * P * 2 * 8, cudaMemcpyDeviceToHost, stream));
   }

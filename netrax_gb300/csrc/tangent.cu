@@ -290,9 +290,10 @@ __global__ void tangent_reduce_kernel(const TanParams p, const int32_t *__restri
   const int slot = slots[blockIdx.x], part = blockIdx.y, q = blockIdx.z;
   const int b0 = part_block_begin[part], b1 = part_block_begin[part + 1];
   const double *src = p.partial + ((size_t)slot * 2 + q) * p.n_blocks;
+  const float2 *src32 = reinterpret_cast<const float2 *>(src);
   double s = 0.0, c = 0.0;
   for (int b = b0 + threadIdx.x; b < b1; b += blockDim.x) {
-    const double y = src[b] - c;
+    const double y = (p.ff ? (double)src32[b].x + (double)src32[b].y : src[b]) - c;
     const double t = s + y;
     c = (t - s) - y;
     s = t;
@@ -305,6 +306,183 @@ __global__ void tangent_reduce_kernel(const TanParams p, const int32_t *__restri
     __syncthreads();
   }
   if (threadIdx.x == 0) out[((size_t)slot * n_parts + part) * 2 + q] = red[0];
+}
+
+// The tangent sweep as a walk (DNA): one warp per PPL * 32 / R patterns
+// (lane = (rate, PPL patterns)) runs every op of the schedule in depth-first
+// order (walk_order: each op right before the ops that read its tangents),
+// so tangent rows come back from L2. Per op the arithmetic of
+// tangent_kernel: where x takes e's message, X' and X'' are P'_e d and
+// P''_e d times vo; above, P_d times the child's X' and X''; both times the
+// op's rescaling. At a displayed-tree root the site sums L, L', L'' (over
+// the R rate lanes), then per pattern w L'/L and w (L''/L - (L'/L)^2),
+// summed over the warp into partial[slot][q][unit] (FP64 contexts: FP64;
+// FP32 contexts: FP32 terms, float-float warp sums). Tangent rows are
+// read with plain (coherent) loads: this kernel writes them.
+template <typename real, int R, int PPL>
+__global__ void __launch_bounds__(256) tangent_walk_kernel(const TanParams p, int n_ops, int64_t n_units) {
+  constexpr int S = 4, PPW = 32 / R, RSS = R * S * S;
+  const int lane = threadIdx.x & 31, r = lane % R;
+  const int64_t unit = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (unit >= n_units) return;  // whole warp
+  const int64_t s0 = unit * PPL * PPW + lane / R;
+  const int part = p.block_part[s0 / (kTanPPT * 256 / R)];
+  const real *pm = static_cast<const real *>(p.pmat) + ((size_t)part * p.n_edges * R + r) * S * S;
+  const real *pd = static_cast<const real *>(p.pderiv) + ((size_t)part * 2 * R + r) * S * S;
+  real pi[S];
+#pragma unroll
+  for (int i = 0; i < S; ++i) pi[i] = (real)p.freqs[part * S + i];
+  const real rw = (real)p.rate_weights[part * R + r];
+  const size_t plane = (size_t)p.n_patterns * R * S;
+  real *tan = static_cast<real *>(p.tan);
+  auto load_m = [&](const real *src, real (&M)[S * S]) {
+#pragma unroll
+    for (int i = 0; i < S; ++i) ldg_row<real, S>(src + i * S, *reinterpret_cast<real(*)[S]>(M + i * S));
+  };
+  for (int j = 0; j < n_ops; ++j) {
+    const TanOp op = p.ops[j];
+    if (j + 1 < n_ops) {  // ask L2 for the next op's other child (a CLV written long before)
+      const int32_t on = __ldg(&p.ops[j + 1].o);
+      if (on >= 0)
+#pragma unroll
+        for (int q = 0; q < PPL; ++q)
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(static_cast<const real *>(p.clv) +
+                                                        (((size_t)on * p.n_patterns + s0 + q * PPW) * R + r) * S));
+    }
+    real M[S * S], vo[PPL][S], t1[PPL][S], t2[PPL][S];
+    int k[PPL];
+#pragma unroll
+    for (int q = 0; q < PPL; ++q) {
+      const int64_t s = s0 + q * PPW;
+      real c[S];
+      const int so = load_row<real, R, S>(p, op.o, s, r, c);
+      const int sd = op.d >= 0 ? __ldg(p.scaler + (size_t)op.d * p.n_patterns + s) : 0;
+      k[q] = __ldg(p.scaler + (size_t)op.x * p.n_patterns + s) - sd - so;
+#pragma unroll
+      for (int i = 0; i < S; ++i) vo[q][i] = c[i];
+    }
+    if (op.o == INT32_MIN) {
+#pragma unroll
+      for (int q = 0; q < PPL; ++q)
+#pragma unroll
+        for (int i = 0; i < S; ++i) vo[q][i] = (real)1;
+    } else {
+      load_m(pm + (size_t)op.eo * RSS, M);
+#pragma unroll
+      for (int q = 0; q < PPL; ++q) {
+        real c[S];
+#pragma unroll
+        for (int i = 0; i < S; ++i) c[i] = vo[q][i];
+        matvec<real, S>(M, c, vo[q]);
+      }
+    }
+    if (op.mode == 1) {
+      real cd[PPL][S];
+#pragma unroll
+      for (int q = 0; q < PPL; ++q) load_row<real, R, S>(p, op.d, s0 + q * PPW, r, cd[q]);
+      load_m(pd, M);
+#pragma unroll
+      for (int q = 0; q < PPL; ++q) matvec<real, S>(M, cd[q], t1[q]);
+      load_m(pd + (size_t)R * S * S, M);
+#pragma unroll
+      for (int q = 0; q < PPL; ++q) matvec<real, S>(M, cd[q], t2[q]);
+    } else {
+      load_m(pm + (size_t)op.ed * RSS, M);
+#pragma unroll
+      for (int q = 0; q < PPL; ++q) {
+        const size_t row = ((size_t)(s0 + q * PPW) * R + r) * S;
+        real a[S], b[S];
+#pragma unroll
+        for (int i = 0; i < S; ++i) {
+          a[i] = tan[((size_t)op.td * 2) * plane + row + i];
+          b[i] = tan[((size_t)op.td * 2 + 1) * plane + row + i];
+        }
+        matvec<real, S>(M, a, t1[q]);
+        matvec<real, S>(M, b, t2[q]);
+      }
+    }
+    // root site terms: FP64 sums in FP64 contexts; in FP32 ones FP32 terms
+    // whose warp sums are float-float pairs (no FP64 instruction per root)
+    double a1 = 0.0, a2 = 0.0;
+    float f1 = 0.f, f2 = 0.f;
+#pragma unroll
+    for (int q = 0; q < PPL; ++q) {
+      const int64_t s = s0 + q * PPW;
+      const size_t row = ((size_t)s * R + r) * S;
+#pragma unroll
+      for (int i = 0; i < S; ++i) {
+        t1[q][i] = ScaleShift<real>::apply(t1[q][i] * vo[q][i], k[q]);
+        t2[q][i] = ScaleShift<real>::apply(t2[q][i] * vo[q][i], k[q]);
+      }
+      if (op.tx >= 0) {
+        st_row<real, S>(tan + ((size_t)op.tx * 2) * plane + row, t1[q]);
+        st_row<real, S>(tan + ((size_t)op.tx * 2 + 1) * plane + row, t2[q]);
+      }
+      if (op.slot < 0) continue;  // uniform over the warp
+      real xr[S];
+      ldg_row<real, S>(static_cast<const real *>(p.clv) + (size_t)op.x * plane + row, xr);
+      real L = 0, L1 = 0, L2 = 0;
+#pragma unroll
+      for (int i = 0; i < S; ++i) {
+        L = fma(pi[i], xr[i], L);
+        L1 = fma(pi[i], t1[q][i], L1);
+        L2 = fma(pi[i], t2[q][i], L2);
+      }
+      L *= rw;
+      L1 *= rw;
+      L2 *= rw;
+#pragma unroll
+      for (int o = 1; o < R; o <<= 1) {
+        L += __shfl_xor_sync(0xffffffffu, L, o);
+        L1 += __shfl_xor_sync(0xffffffffu, L1, o);
+        L2 += __shfl_xor_sync(0xffffffffu, L2, o);
+      }
+      if (r == 0) {
+        if constexpr (sizeof(real) == 4) {
+          const float w = __ldg(p.weights32 + s).x;
+          if (w != 0.f) {
+            if (p.inv_term32) {  // invariant sites: L = gf (L_mix + iq), gf cancels in the ratios
+              const float iq = p.inv_term32[s];
+              if (iq > 0.f) L += ldexpf(iq, __ldg(p.scaler + (size_t)op.x * p.n_patterns + s));
+            }
+            const float inv = 1.0f / L, q1 = L1 * inv, q2 = L2 * inv;
+            f1 += w * q1;
+            f2 += w * (q2 - q1 * q1);
+          }
+        } else {
+          const double w = __ldg(p.weights + s);
+          if (w != 0.0) {
+            if (p.inv_term) {  // invariant sites: L = gf (L_mix + iq), gf cancels in the ratios
+              const real iq = (real)p.inv_term[s];
+              if (iq > (real)0) L += ScaleShift<real>::apply(iq, __ldg(p.scaler + (size_t)op.x * p.n_patterns + s));
+            }
+            const real q1 = L1 / L, q2 = L2 / L;
+            a1 += w * (double)q1;
+            a2 += w * ((double)q2 - (double)q1 * (double)q1);
+          }
+        }
+      }
+    }
+    if (op.slot < 0) continue;  // uniform over the warp
+    if constexpr (sizeof(real) == 4) {
+      const FF g1 = warp_sum_ff(FF{f1, 0.f}), g2 = warp_sum_ff(FF{f2, 0.f});
+      if (lane == 0) {
+        float2 *dst = reinterpret_cast<float2 *>(p.partial);
+        dst[((size_t)op.slot * 2 + 0) * n_units + unit] = make_float2(g1.hi, g1.lo);
+        dst[((size_t)op.slot * 2 + 1) * n_units + unit] = make_float2(g2.hi, g2.lo);
+      }
+    } else {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        a1 += __shfl_down_sync(0xffffffffu, a1, o);
+        a2 += __shfl_down_sync(0xffffffffu, a2, o);
+      }
+      if (lane == 0) {
+        p.partial[((size_t)op.slot * 2 + 0) * n_units + unit] = a1;
+        p.partial[((size_t)op.slot * 2 + 1) * n_units + unit] = a2;
+      }
+    }
+  }
 }
 
 // ------------------------------------------------------------ sumtables
@@ -697,6 +875,25 @@ void launch_pderiv(cudaStream_t s, int n_parts, int R, int S, const double *lamb
   pderiv_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(n_parts, R, S, lambda, U, Uinv, rates, brlen,
                                                                 len_stride, edge, out64, out32);
   add_launches(1);
+}
+
+int tangent_walk_patterns_per_unit(int R) { return 32 / R; }
+
+bool launch_tangent_walk(cudaStream_t s, int precision, int R, int S, const TanParams &p, int n_ops) {
+  if (S != 4) return false;
+  const int64_t n_units = p.n_patterns * R / 32;
+  const unsigned grid = (unsigned)((n_units + 7) / 8);
+  auto go = [&](auto kernel) { kernel<<<grid, 256, 0, s>>>(p, n_ops, n_units); };
+  const bool f32 = precision == 1;
+  switch (R) {
+    case 1: f32 ? go(tangent_walk_kernel<float, 1, 1>) : go(tangent_walk_kernel<double, 1, 1>); break;
+    case 2: f32 ? go(tangent_walk_kernel<float, 2, 1>) : go(tangent_walk_kernel<double, 2, 1>); break;
+    case 4: f32 ? go(tangent_walk_kernel<float, 4, 1>) : go(tangent_walk_kernel<double, 4, 1>); break;
+    case 8: f32 ? go(tangent_walk_kernel<float, 8, 1>) : go(tangent_walk_kernel<double, 8, 1>); break;
+    default: return false;
+  }
+  add_launches(1);
+  return true;
 }
 
 bool launch_tangent(cudaStream_t s, int precision, int R, int S, const TanParams &p, const int32_t *level_begin,

@@ -33,12 +33,12 @@ def _parts(name):
     return [_P(d, PINV[k % 2]) for k, d in enumerate(CASES[name]["partitions"])]
 
 
-def _lik(name, variant, precision, parts=None):
+def _lik(name, variant, precision, parts=None, **kw):
     from netrax_gb300.likelihood import NetworkLikelihood
     from netrax_gb300.network import parse_extended_newick
     net = parse_extended_newick(CASES[name]["newick"])
     return NetworkLikelihood(net, parts if parts is not None else _parts(name), variant=variant,
-                             precision=precision)
+                             precision=precision, **kw)
 
 
 def _oracle(name, variant):
@@ -70,12 +70,14 @@ def test_pinv_logl_and_gradient_match_the_oracle(name, variant):
 
 @pytest.mark.parametrize("name", NAMES[:3] + NAMES[3:4])
 @pytest.mark.parametrize("mode", [0, 1])
-def test_pinv_edge_derivatives_match_the_sumtable_oracle(name, mode):
+@pytest.mark.parametrize("sumtables", [True, False])
+def test_pinv_edge_derivatives_match_the_sumtable_oracle(name, mode, sumtables):
+    """Both derivative paths (edge sumtables; the tangent sweep) with +I."""
     from oracle import derivatives
     orc = _oracle(name, "AVERAGE")
     d = derivatives.EdgeDerivativeOracle(orc)
     key = "true" if mode == 0 else "reference"
-    with _lik(name, "AVERAGE", "fp64") as lik:
+    with _lik(name, "AVERAGE", "fp64", sumtables=sumtables) as lik:
         for e in range(0, lik.n_edges, max(1, lik.n_edges // 12)):
             w1, w2 = d.edge(e, mode=key)
             d1, d2 = lik.edge_derivatives(e, second=True, mode=mode)
