@@ -246,8 +246,8 @@ int tangent_patterns_per_block(int R);
 void launch_pderiv(cudaStream_t s, int n_parts, int R, int S, const double *lambda, const double *U,
                    const double *Uinv, const double *rates, const double *brlen, int len_stride, int edge,
                    double *out64, float *out32);
-// One launch per level of ops [level_begin[L], level_begin[L+1]); false for
-// an unsupported (R, S).
+// One launch per level of ops [level_begin[L], level_begin[L+1]) (20
+// states; DNA takes launch_tangent_walk); false for an unsupported (R, S).
 bool launch_tangent(cudaStream_t s, int precision, int R, int S, const TanParams &p, const int32_t *level_begin,
                     int n_levels);
 // DNA: the same sweep as one walk launch over ops in walk order

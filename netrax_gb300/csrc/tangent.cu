@@ -844,15 +844,7 @@ void run_levels(cudaStream_t st, const TanParams &p, const int32_t *level_begin,
 
 template <typename real>
 bool dispatch_levels(cudaStream_t st, int R, int S, const TanParams &p, const int32_t *level_begin, int n_levels) {
-  if (S == 4) {
-    switch (R) {
-      case 1: run_levels<real, 1, 4>(st, p, level_begin, n_levels); return true;
-      case 2: run_levels<real, 2, 4>(st, p, level_begin, n_levels); return true;
-      case 4: run_levels<real, 4, 4>(st, p, level_begin, n_levels); return true;
-      case 8: run_levels<real, 8, 4>(st, p, level_begin, n_levels); return true;
-      default: return false;
-    }
-  }
+  // DNA runs the walk (tangent_walk_kernel); the level launches serve 20 states
   if (S == 20) {
     switch (R) {
       case 1: run_levels<real, 1, 20>(st, p, level_begin, n_levels); return true;
