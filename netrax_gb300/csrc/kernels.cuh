@@ -280,10 +280,18 @@ struct StabParams {
   int32_t n_tables, tables_per_block;  // evaluation: tables, and tables per block (blockIdx.y)
   int32_t *fault;                      // set to 1 by an evaluation whose bounded wait gave up
   double *partial;              // [n_tab][3][N / 32] per-warp sums of w log L, w L'/L, w (L''/L - (L'/L)^2); FP32: float pairs
+                                // (20 states: [n_tab][3][N R / 32], warps of 32 / R patterns)
+  // 20 states: tables [n_tab][N][R][S], built by reverse walks along each
+  // tree's path: path_ops [6 per op] = (x, d, o, ed, eo, mode) from the
+  // root down, path_begin [n_tab + 1]
+  const int32_t *path_ops;
+  const int32_t *path_begin;
 };
 
 // Builds the tables (one walk launch over the tangent schedule's ops in
-// level order); false for an unsupported (R, S): DNA only.
+// depth-first order); false for an unsupported (R, S): DNA only.
+// 20 states: the reverse path walks (grid.y = table); false for R > 4.
+bool launch_sumtable_path20(cudaStream_t s, int precision, int R, const StabParams &p, int n_tab);
 bool launch_sumtable_build(cudaStream_t s, int precision, int R, int S, const StabParams &p,
                            const int32_t *level_begin, int n_levels);
 // Once per context before the first evaluation (outside any graph capture):

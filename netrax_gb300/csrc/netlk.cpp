@@ -179,8 +179,9 @@ struct netlk_ctx {
   // edge sumtables: unit-direction work planes, per-tree outside vectors at
   // the edge (tables), their scale counters, and the evaluation buffers
   DevBuf d_stab_work, d_stab, d_stab_scaler, d_stab_partial, d_stab_out, d_stab_pm3_64, d_stab_pm3_32,
-      d_stab_groups, d_stab_ops, d_part_warp_begin;
-  PinnedBuf h_stab_pm3, h_stab_out, h_stab_ops;
+      d_stab_groups, d_stab_ops, d_part_warp_begin, d_stab_paths;
+  PinnedBuf h_stab_pm3, h_stab_out, h_stab_ops, h_stab_paths;
+  int64_t stab_cap_path = 0;  // 20 states: path ops allocated
   cudaGraphExec_t graph_stab = nullptr;  // one evaluation of the current tables
   int stab_cap_work = -1, stab_cap_tab = 0;  // work slots / tables allocated (-1: not set up yet)
   int stab_edge = -1;                        // edge whose tables are current (-1: none)
@@ -256,7 +257,7 @@ struct netlk_ctx {
                       &d_pderiv64, &d_pderiv32, &d_block_part, &d_part_block_begin, &d_tan_slots, &d_gfrac,
                       &d_gfrac32, &d_invt, &d_invt32, &d_grad_part, &d_op_sum_part, &d_part_unit_begin, &d_stab_work,
                       &d_stab, &d_stab_scaler, &d_stab_partial, &d_stab_out, &d_stab_pm3_64, &d_stab_pm3_32,
-                      &d_stab_groups, &d_stab_ops, &d_part_warp_begin, &d_part_tunit_begin})
+                      &d_stab_groups, &d_stab_ops, &d_part_warp_begin, &d_part_tunit_begin, &d_stab_paths})
       b->free();
     if (stream) cudaStreamDestroy(stream);
   }
@@ -436,6 +437,11 @@ struct netlk_ctx {
   // before the ops that read its directions) and reassigns the work slots
   // by live range in that order; returns the slots used, or -1.
   static int walk_order(std::vector<TanOp> &ops);
+  // 20 states: per table (ops' slot fields numbered as tables), the ops from
+  // its root down to the op that takes the edge's message, 6 ints each
+  // (x, d, o, ed, eo, mode); path_begin [n_tab + 1]
+  void sumtable_paths(const std::vector<TanOp> &ops, int n_tab, std::vector<int32_t> &path_ops,
+                      std::vector<int32_t> &path_begin) const;
   bool sumtable_current(int e) const;
   // per_part: len, logl, d1, d2 hold one entry per partition (each at its
   // own length); else len[0] is the edge's (linked or scaled) length and the
@@ -1692,6 +1698,29 @@ int netlk_ctx::sumtable_schedule(int e, std::vector<TanOp> &ops, std::vector<int
   return need;
 }
 
+void netlk_ctx::sumtable_paths(const std::vector<TanOp> &ops, int n_tab, std::vector<int32_t> &path_ops,
+                               std::vector<int32_t> &path_begin) const {
+  std::unordered_map<int32_t, int> op_of;  // variant -> its op
+  std::vector<int> op_of_tab(n_tab, -1);
+  for (size_t j = 0; j < ops.size(); ++j) {
+    op_of[ops[j].x] = (int)j;
+    if (ops[j].slot >= 0) op_of_tab[ops[j].slot] = (int)j;
+  }
+  path_ops.clear();
+  path_begin.assign(1, 0);
+  for (int t = 0; t < n_tab; ++t) {
+    for (int j = op_of_tab[t]; j >= 0;) {
+      const TanOp &o = ops[j];
+      const int32_t row[6] = {o.x, o.d, o.o, o.ed, o.eo, o.mode};
+      path_ops.insert(path_ops.end(), row, row + 6);
+      if (o.mode == 1) break;
+      auto it = op_of.find(o.d);
+      j = it == op_of.end() ? -1 : it->second;
+    }
+    path_begin.push_back((int32_t)(path_ops.size() / 6));
+  }
+}
+
 bool netlk_ctx::sumtable_current(int e) const {
   if (stab_edge != e || stab_gen != model_gen || device_brlen || stab_probs != ret_probs) return false;
   const std::vector<double> &L = dev_len();
@@ -1707,33 +1736,47 @@ bool netlk_ctx::sumtable_build(int e) {
     cudaGraphExecDestroy(graph_stab);
     graph_stab = nullptr;
   }
-  if (n_segments != 1 || device_brlen || S != 4 || opts.host_only || !opts.sumtables) return false;
+  const bool prot = S == 20;  // 20 states: tables by reverse path walks
+  if (n_segments != 1 || device_brlen || !(S == 4 || (prot && R <= 4)) || opts.host_only || !opts.sumtables)
+    return false;
   prepare();
   const size_t real_b = opts.precision == NETLK_FP32 ? 4 : 8;
   const size_t plane = (size_t)N * R * S * real_b;  // one (pattern, rate, state) plane
+  const int64_t n_warps = prot ? N * R / 32 : N / 32;  // evaluation partials per table
   if (stab_cap_work < 0) {
-    // set up once: the most work slots and tables any edge needs
+    // set up once: the most work slots, tables and path ops any edge needs
     int need = 0, tabs = 0;
+    int64_t paths = 0;
     std::vector<TanOp> ops;
-    std::vector<int32_t> lb, sl;
+    std::vector<int32_t> gref, gbegin, slot_tab, pops, pbeg;
     for (int k = 0; k < topo.n_edges; ++k) {
-      if (tangent_schedule(k, ops, lb, sl) < 0) continue;
-      need = std::max(need, walk_order(ops));
-      tabs = std::max(tabs, (int)sl.size());
+      const int nk = sumtable_schedule(k, ops, gref, gbegin, slot_tab);
+      if (nk < 0) continue;
+      need = std::max(need, prot ? 0 : nk);
+      tabs = std::max(tabs, gbegin.back());
+      if (prot) {
+        sumtable_paths(ops, gbegin.back(), pops, pbeg);
+        paths = std::max<int64_t>(paths, (int64_t)pops.size() / 6);
+      }
     }
     setup_tangent_blocks();
     size_t free_b = 0, total_b = 0;
     CUDA_OK(cudaMemGetInfo(&free_b, &total_b));
-    const double bytes = ((double)need * S + tabs) * plane + (double)tabs * N * (4 + 3 * 8 / 32.0);
+    const double bytes = ((double)need * S + tabs) * plane + (double)tabs * (N * 4 + n_warps * 3 * 8);
     if (bytes > 0.5 * (double)free_b) {  // too big: keep the tangent path
       stab_cap_work = 0;
       return false;
     }
     int64_t scratch = 0;
-    d_stab_work.alloc(std::max<size_t>(1, (size_t)need * S) * plane, scratch);
+    d_stab_work.alloc(prot ? 16 : std::max<size_t>(1, (size_t)need * S) * plane, scratch);
     d_stab.alloc(std::max<size_t>(1, (size_t)tabs) * plane, scratch);
     d_stab_scaler.alloc(std::max<size_t>(1, (size_t)tabs) * N * 4, scratch);
-    d_stab_partial.alloc(std::max<size_t>(1, (size_t)tabs) * 3 * (N / 32) * 8, scratch);
+    d_stab_partial.alloc(std::max<size_t>(1, (size_t)tabs) * 3 * n_warps * 8, scratch);
+    if (prot) {
+      d_stab_paths.alloc(((size_t)std::max<int64_t>(1, paths) * 6 + tabs + 1) * 4, scratch);
+      h_stab_paths.alloc(((size_t)std::max<int64_t>(1, paths) * 6 + tabs + 1) * 4);
+      stab_cap_path = paths;
+    }
     d_stab_out.alloc((std::max<size_t>(1, (size_t)tabs) * P * 3 + 1) * 8, scratch);  // + the fault word
     d_stab_pm3_64.alloc((size_t)P * 3 * R * S * S * 8, scratch);
     d_stab_pm3_32.alloc((size_t)P * 3 * R * S * S * 4, scratch);
@@ -1748,18 +1791,18 @@ bool netlk_ctx::sumtable_build(int e) {
     }
     h_stab_out.alloc((std::max<size_t>(1, (size_t)tabs) * P * 3 + 1) * 8);
     h_stab_ops.alloc(dag.vars.size() * sizeof(TanOp) + (size_t)(2 * tabs + 2) * 4);
-    std::vector<int32_t> pwb(P + 1);
-    for (int p = 0; p < P; ++p) pwb[p] = (int32_t)(parts[p].offset / 32);
-    pwb[P] = (int32_t)(N / 32);
+    std::vector<int32_t> pwb(P + 1);  // each partition's evaluation warps
+    for (int p = 0; p < P; ++p) pwb[p] = (int32_t)(prot ? parts[p].offset * R / 32 : parts[p].offset / 32);
+    pwb[P] = (int32_t)n_warps;
     CUDA_OK(cudaMemcpy(d_part_warp_begin.p, pwb.data(), pwb.size() * 4, cudaMemcpyHostToDevice));
-    stab_cap_work = need;
+    stab_cap_work = std::max(1, need);  // 0 is kept for "not available"
     stab_cap_tab = tabs;
   }
   std::vector<TanOp> ops;
   std::vector<int32_t> gref, gbegin, slot_tab;
   const int need = sumtable_schedule(e, ops, gref, gbegin, slot_tab);
   const int n_tab = gbegin.empty() ? 0 : gbegin.back();
-  if (need < 0 || need > stab_cap_work || stab_cap_work == 0 || n_tab > stab_cap_tab) return false;
+  if (need < 0 || (!prot && need > stab_cap_work) || stab_cap_work == 0 || n_tab > stab_cap_tab) return false;
   const int32_t lb[2] = {0, (int32_t)ops.size()};  // one walk over every op
   stab_n_tab = n_tab;
   stab_n_groups = (int)gref.size();
@@ -1777,7 +1820,21 @@ bool netlk_ctx::sumtable_build(int e) {
     std::memcpy(hg + gref.size(), gbegin.data(), gbegin.size() * 4);
     CUDA_OK(cudaMemcpyAsync(d_stab_groups.p, hg, (gref.size() + gbegin.size()) * 4, cudaMemcpyHostToDevice, stream));
     StabParams sp = stab_params();
-    if (!launch_sumtable_build(stream, opts.precision, R, S, sp, lb, 1)) return false;
+    if (prot) {
+      std::vector<int32_t> pops, pbeg;
+      sumtable_paths(ops, n_tab, pops, pbeg);
+      if ((int64_t)pops.size() / 6 > stab_cap_path) return false;
+      int32_t *hpth = h_stab_paths.as<int32_t>();
+      std::memcpy(hpth, pops.data(), pops.size() * 4);
+      std::memcpy(hpth + pops.size(), pbeg.data(), pbeg.size() * 4);
+      CUDA_OK(cudaMemcpyAsync(d_stab_paths.p, hpth, (pops.size() + pbeg.size()) * 4, cudaMemcpyHostToDevice,
+                              stream));
+      sp.path_ops = d_stab_paths.as<int32_t>();
+      sp.path_begin = d_stab_paths.as<int32_t>() + pops.size();
+      if (!launch_sumtable_path20(stream, opts.precision, R, sp, n_tab)) return false;
+    } else if (!launch_sumtable_build(stream, opts.precision, R, S, sp, lb, 1)) {
+      return false;
+    }
   }
   const int nout = 3 + P + topo.n_ret;
   CUDA_OK(cudaMemcpyAsync(h_out.p, d_out.p, nout * 8, cudaMemcpyDeviceToHost, stream));

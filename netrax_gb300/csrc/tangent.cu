@@ -490,9 +490,8 @@ __global__ void __launch_bounds__(256) tangent_walk_kernel(const TanParams p, in
 // its derivatives L1, L2 in the table's scaled units), summed over the warp
 // into partial[table][q][warp].
 template <typename real>
-__device__ __forceinline__ void sumtable_site_terms(const StabParams &sp, int tb, int64_t s, double w, real iq,
-                                                    int k, real L, real L1, real L2) {
-  const int64_t n_warps = sp.t.n_patterns / 32, gw = s / 32;
+__device__ __forceinline__ void sumtable_site_terms(const StabParams &sp, int tb, int64_t gw, int64_t n_warps,
+                                                    double w, real iq, int k, real L, real L1, real L2) {
   const bool lead = (threadIdx.x & 31) == 0;
   if constexpr (sizeof(real) == 4) {
     // FP32 sweeps: per-site terms and the warp sums in FP32 (the log term as
@@ -760,7 +759,130 @@ __global__ void __launch_bounds__(128) sumtable_eval_kernel(const StabParams sp)
       tc::fence_proxy_async();
       issue(j + K);
     }
-    sumtable_site_terms<real>(sp, tb, s, w, iq, k, L, L1, L2);
+    sumtable_site_terms<real>(sp, tb, s / 32, p.n_patterns / 32, w, iq, k, L, L1, L2);
+  }
+}
+
+// Tables for 20-state partitions, by reverse walks (the forward-mode build
+// would carry 20 directions): per displayed tree containing e, from its
+// root down the path to e (the tangent schedule's chain of children that
+// hold e), O starts as w_r pi at the root; at a variant v with the path
+// child d and the other child o, u = O * (P_o o) * 2^k (k: v's scale counter
+// minus its children's), then O <- P_d^T u; at the variant that takes e's
+// message, u is the table row (the same O = dL/dm as the DNA build).
+// Block: 256 threads = 256 / R patterns x R rates of one partition,
+// blockIdx.y = table; each op's two P matrices staged in shared memory.
+template <typename real, int R>
+__global__ void __launch_bounds__(256) sumtable_path20_kernel(const StabParams sp) {
+  constexpr int S = 20, SS = S * S, ROWS = 256 / R;
+  const TanParams &p = sp.t;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  real *sPo = reinterpret_cast<real *>(smem_raw);  // [R][S][S]
+  real *sPd = sPo + R * SS;                         // [R][S][S]
+  const int tb = blockIdx.y, r = threadIdx.x % R;
+  const int64_t s = (int64_t)blockIdx.x * ROWS + threadIdx.x / R;
+  const int part = p.block_part[(blockIdx.x * ROWS) / (kTanPPT * 256 / R)];
+  const real *pm = static_cast<const real *>(p.pmat) + (size_t)part * p.n_edges * R * SS;
+  const real rw = (real)p.rate_weights[part * R + r];
+  real O[S], u[S];
+#pragma unroll
+  for (int i = 0; i < S; ++i) O[i] = rw * (real)p.freqs[part * S + i];
+  int sx_root = 0;
+  const int kb = sp.path_begin[tb], ke = sp.path_begin[tb + 1];
+  for (int q = kb; q < ke; ++q) {
+    const int32_t *po = sp.path_ops + 6 * (size_t)q;  // x, d, o, ed, eo, mode
+    const int32_t x = po[0], d = po[1], o = po[2], ed = po[3], eo = po[4], mode = po[5];
+    __syncthreads();  // every thread is done with the previous op's matrices
+    for (int i = threadIdx.x; i < R * SS; i += blockDim.x) {
+      sPo[i] = eo >= 0 ? __ldg(pm + (size_t)eo * R * SS + i) : (real)0;
+      sPd[i] = mode == 2 ? __ldg(pm + (size_t)ed * R * SS + i) : (real)0;
+    }
+    __syncthreads();
+    real c[S], vo[S];
+    const int so = load_row<real, R, S>(p, o, s, r, c);
+    if (o == INT32_MIN) {
+#pragma unroll
+      for (int i = 0; i < S; ++i) vo[i] = (real)1;
+    } else {
+      matvec<real, S>(sPo + r * SS, c, vo);
+    }
+    const int sd = d >= 0 ? __ldg(p.scaler + (size_t)d * p.n_patterns + s) : 0;
+    const int sx = __ldg(p.scaler + (size_t)x * p.n_patterns + s);
+    if (q == kb) sx_root = sx;
+#pragma unroll
+    for (int i = 0; i < S; ++i) u[i] = ScaleShift<real>::apply(O[i] * vo[i], sx - sd - so);
+    if (mode == 2) {  // O = P_d^T u
+      const real *Md = sPd + r * SS;
+#pragma unroll
+      for (int j = 0; j < S; ++j) {
+        real a = (real)0;
+#pragma unroll
+        for (int i = 0; i < S; ++i) a = fma(Md[i * S + j], u[i], a);
+        O[j] = a;
+      }
+    }
+  }
+  // the path ends at the op that takes e's message: u is the table row
+  real *dst = static_cast<real *>(sp.table) + (((size_t)tb * p.n_patterns + s) * R + r) * S;
+#pragma unroll
+  for (int i = 0; i < S; i += 4) {
+    if constexpr (sizeof(real) == 4)
+      *reinterpret_cast<float4 *>(dst + i) = make_float4(u[i], u[i + 1], u[i + 2], u[i + 3]);
+    else
+      for (int j = 0; j < 4; ++j) dst[i + j] = u[i + j];
+  }
+  if (r == 0) sp.table_scaler[(size_t)tb * p.n_patterns + s] = sx_root;
+}
+
+// Evaluation of 20-state tables: thread = (pattern, rate), 256 per block;
+// per child group P I, P' I, P'' I for the thread's rate, then per table the
+// dot products with its row, summed over the R rate lanes, and the site
+// terms (as the DNA evaluation) summed over the warp into
+// partial[table][q][warp], warps of 32 / R patterns.
+template <typename real, int R>
+__global__ void __launch_bounds__(256) sumtable_eval20_kernel(const StabParams sp) {
+  constexpr int S = 20, SS = S * S, ROWS = 256 / R;
+  const TanParams &p = sp.t;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  real *sM = reinterpret_cast<real *>(smem_raw);  // [3][R][S][S]
+  const int r = threadIdx.x % R;
+  const int64_t s = (int64_t)blockIdx.x * ROWS + threadIdx.x / R;
+  const int part = p.block_part[(blockIdx.x * ROWS) / (kTanPPT * 256 / R)];
+  const real *src = static_cast<const real *>(sp.pm3) + (size_t)part * 3 * R * SS;
+  for (int i = threadIdx.x; i < 3 * R * SS; i += blockDim.x) sM[i] = src[i];
+  __syncthreads();
+  const double w = r == 0 ? __ldg(p.weights + s) : 0.0;
+  const real iq = p.inv_term ? (real)p.inv_term[s] : (real)0;
+  const int64_t n_warps = p.n_patterns * R / 32, gw = ((int64_t)blockIdx.x * 256 + threadIdx.x) / 32;
+  const int tb_lo = blockIdx.y * sp.tables_per_block;
+  const int tb_end = min(tb_lo + sp.tables_per_block, sp.n_tables);
+  for (int g = 0; g < sp.n_groups; ++g) {
+    const int g_lo = max(sp.group_begin[g], tb_lo), g_hi = min(sp.group_begin[g + 1], tb_end);
+    if (g_lo >= g_hi) continue;  // uniform over the block
+    real c[S], m0[S], m1[S], m2[S];
+    load_row<real, R, S>(p, sp.group_ref[g], s, r, c);
+    matvec<real, S>(sM + r * SS, c, m0);
+    matvec<real, S>(sM + (R + r) * SS, c, m1);
+    matvec<real, S>(sM + (2 * R + r) * SS, c, m2);
+    for (int tb = g_lo; tb < g_hi; ++tb) {
+      real o[S];
+      ldg_row<real, S>(static_cast<const real *>(sp.table) + (((size_t)tb * p.n_patterns + s) * R + r) * S, o);
+      real L = 0, L1 = 0, L2 = 0;
+#pragma unroll
+      for (int i = 0; i < S; ++i) {
+        L = fma(o[i], m0[i], L);
+        L1 = fma(o[i], m1[i], L1);
+        L2 = fma(o[i], m2[i], L2);
+      }
+#pragma unroll
+      for (int x = 1; x < R; x <<= 1) {
+        L += __shfl_xor_sync(0xffffffffu, L, x);
+        L1 += __shfl_xor_sync(0xffffffffu, L1, x);
+        L2 += __shfl_xor_sync(0xffffffffu, L2, x);
+      }
+      const int k = __ldg(sp.table_scaler + (size_t)tb * p.n_patterns + s);
+      sumtable_site_terms<real>(sp, tb, gw, n_warps, w, iq, k, L, L1, L2);
+    }
   }
 }
 
@@ -904,6 +1026,21 @@ void launch_tangent_reduce(cudaStream_t s, const TanParams &p, const int32_t *sl
   add_launches(1);
 }
 
+bool launch_sumtable_path20(cudaStream_t s, int precision, int R, const StabParams &p, int n_tab) {
+  if (n_tab <= 0) return true;
+  const dim3 grid((unsigned)(p.t.n_patterns * R / 256), (unsigned)n_tab);
+  const size_t smem = (size_t)2 * R * 400 * (precision == 1 ? 4 : 8);
+  if (precision == 1 && R == 4) sumtable_path20_kernel<float, 4><<<grid, 256, smem, s>>>(p);
+  else if (precision == 1 && R == 2) sumtable_path20_kernel<float, 2><<<grid, 256, smem, s>>>(p);
+  else if (precision == 1 && R == 1) sumtable_path20_kernel<float, 1><<<grid, 256, smem, s>>>(p);
+  else if (precision != 1 && R == 4) sumtable_path20_kernel<double, 4><<<grid, 256, smem, s>>>(p);
+  else if (precision != 1 && R == 2) sumtable_path20_kernel<double, 2><<<grid, 256, smem, s>>>(p);
+  else if (precision != 1 && R == 1) sumtable_path20_kernel<double, 1><<<grid, 256, smem, s>>>(p);
+  else return false;
+  add_launches(1);
+  return true;
+}
+
 bool launch_sumtable_build(cudaStream_t s, int precision, int R, int S, const StabParams &p,
                            const int32_t *level_begin, int n_levels) {
   const bool ok = precision == 1 ? dispatch_sumtable<float>(s, R, S, p, level_begin, n_levels, false)
@@ -913,6 +1050,7 @@ bool launch_sumtable_build(cudaStream_t s, int precision, int R, int S, const St
 }
 
 bool sumtable_eval_setup(int precision, int R, int S) {
+  if (S == 20) return R == 1 || R == 2 || R == 4;  // shared memory below 48 KB
   if (S != 4) return false;
   auto set = [](auto kernel, size_t smem) {
     return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess;
@@ -933,11 +1071,27 @@ bool sumtable_eval_setup(int precision, int R, int S) {
 bool launch_sumtable_eval(cudaStream_t s, int precision, int R, int S, const StabParams &p, int n_tab,
                           const int32_t *part_warp_begin, int n_parts, double *out) {
   if (n_tab <= 0) return true;
-  const bool ok = precision == 1 ? dispatch_sumtable<float>(s, R, S, p, nullptr, 0, true)
-                                 : dispatch_sumtable<double>(s, R, S, p, nullptr, 0, true);
+  bool ok;
+  if (S == 20) {
+    const unsigned ny = (unsigned)((p.n_tables + p.tables_per_block - 1) / p.tables_per_block);
+    const dim3 grid((unsigned)(p.t.n_patterns * R / 256), ny);
+    const size_t smem = (size_t)3 * R * 400 * (precision == 1 ? 4 : 8);
+    ok = true;
+    if (precision == 1 && R == 4) sumtable_eval20_kernel<float, 4><<<grid, 256, smem, s>>>(p);
+    else if (precision == 1 && R == 2) sumtable_eval20_kernel<float, 2><<<grid, 256, smem, s>>>(p);
+    else if (precision == 1 && R == 1) sumtable_eval20_kernel<float, 1><<<grid, 256, smem, s>>>(p);
+    else if (precision != 1 && R == 4) sumtable_eval20_kernel<double, 4><<<grid, 256, smem, s>>>(p);
+    else if (precision != 1 && R == 2) sumtable_eval20_kernel<double, 2><<<grid, 256, smem, s>>>(p);
+    else if (precision != 1 && R == 1) sumtable_eval20_kernel<double, 1><<<grid, 256, smem, s>>>(p);
+    else ok = false;
+  } else {
+    ok = precision == 1 ? dispatch_sumtable<float>(s, R, S, p, nullptr, 0, true)
+                        : dispatch_sumtable<double>(s, R, S, p, nullptr, 0, true);
+  }
   if (!ok) return false;
-  sumtable_reduce_kernel<<<dim3(n_tab, n_parts), 96, 0, s>>>(p.partial, p.t.n_patterns / 32, part_warp_begin,
-                                                              n_parts, out, precision == 1);
+  const int64_t n_warps = S == 20 ? p.t.n_patterns * R / 32 : p.t.n_patterns / 32;
+  sumtable_reduce_kernel<<<dim3(n_tab, n_parts), 96, 0, s>>>(p.partial, n_warps, part_warp_begin, n_parts, out,
+                                                              precision == 1);
   add_launches(2);
   return true;
 }

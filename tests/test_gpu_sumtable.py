@@ -15,8 +15,8 @@ src/likelihood/LikelihoodDerivatives.cpp:95-104,249-344).
   ddf[p] against the oracle with those lengths; scaled lengths: the totals
   equal the unlinked evaluation at s_p t.
 * +I; both mixtures and both derivative modes; tables rebuilt after another
-  edge's length, the model or the probabilities change; 20-state contexts
-  take the tangent path with the same results.
+  edge's length, the model or the probabilities change; 20-state tables
+  (reverse walks down each tree's path) against the tangent sweep.
 * The reference's Newton-Raphson pass driven by table evaluations ends where
   the same pass on the oracle ends.
 """
@@ -31,7 +31,7 @@ pytestmark = pytest.mark.gpu
 CASES = {c["name"]: c for c in golden_cases()}
 
 
-def _lik(name, precision="fp64", variant="AVERAGE", linkage="linked", pinv=None):
+def _lik(name, precision="fp64", variant="AVERAGE", linkage="linked", pinv=None, **kw):
     from netrax_gb300.likelihood import NetworkLikelihood
     from netrax_gb300.network import parse_extended_newick
     net = parse_extended_newick(CASES[name]["newick"])
@@ -39,7 +39,7 @@ def _lik(name, precision="fp64", variant="AVERAGE", linkage="linked", pinv=None)
     if pinv is not None:
         for p in parts:
             p.prop_invar = pinv
-    return NetworkLikelihood(net, parts, precision=precision, variant=variant, brlen_linkage=linkage)
+    return NetworkLikelihood(net, parts, precision=precision, variant=variant, brlen_linkage=linkage, **kw)
 
 
 def _scale(lik):
@@ -176,20 +176,27 @@ def test_tables_rebuilt_when_parameters_change():
                                                                       rel=1e-12)
 
 
-def test_protein_takes_the_tangent_path():
-    name = "protein_10taxa_3ret_2parts"
-    for precision, tol in (("fp64", 1e-11), ("fp32", 1e-6)):
-        with _lik(name, precision) as a, _lik(name, precision) as ref:
+@pytest.mark.parametrize("name", ["protein_8taxa_2ret", "protein_10taxa_3ret_2parts"])
+def test_protein_tables_match_the_tangent_path(name):
+    """20-state tables (reverse walks down each tree's path to the edge)
+    against an FP64 context set to the proposal with the tangent sweep:
+    logL FP64 1e-10 / FP32 1e-6, d1 and d2 FP64 1e-8 / FP32 1e-4 of the
+    gradient scale; the tables' context keeps its own parameters."""
+    for precision, tl, td in (("fp64", 1e-10, 1e-8), ("fp32", 1e-6, 1e-4)):
+        with _lik(name, precision) as a, _lik(name, "fp64", sumtables=False) as ref:
             base = a.loglikelihood()
-            assert a.edge_sumtable(2) == (False, 0)
-            for e in (2, 7):
-                want_l = ref.edge_loglikelihood(e, 0.35)
-                w1, w2 = ref.edge_derivatives(e, second=True)
-                l, d1, d2 = a.edge_sumtable_derivatives(e, 0.35)
-                assert l == pytest.approx(want_l, rel=tol)
-                assert d1 == pytest.approx(w1, rel=tol, abs=tol)
-                assert d2 == pytest.approx(w2, rel=tol, abs=tol)
-                ref.edge_loglikelihood(e, a.branch_lengths[e])
+            assert a.edge_sumtable(2)[0]
+            scale = _scale(ref)
+            for e in (2, 5, 7):
+                t0 = ref.branch_lengths[e]
+                for t in (1e-6, 0.35 * t0 + 0.01, 2.0):
+                    want_l = ref.edge_loglikelihood(e, t)
+                    w1, w2 = ref.edge_derivatives(e, second=True)
+                    l, d1, d2 = a.edge_sumtable_derivatives(e, t)
+                    assert l == pytest.approx(want_l, rel=tl), (precision, e, t)
+                    assert abs(d1 - w1) <= td * max(scale, abs(w1)), (precision, e, t, d1, w1)
+                    assert abs(d2 - w2) <= td * max(scale, abs(w2)), (precision, e, t, d2, w2)
+                ref.edge_loglikelihood(e, t0)
             assert a.loglikelihood() == base
 
 
