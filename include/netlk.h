@@ -147,8 +147,8 @@ typedef struct {
                                         (netlk_set_branch_length_scalers). The
                                         reference's --brlen linked / unlinked /
                                         scaled (src/main.cpp:101,226-230).    */
-  int32_t sumtables;                 /* 1 (default): edge derivatives of DNA
-                                        contexts from the edge's sumtables
+  int32_t sumtables;                 /* 1 (default): edge derivatives from
+                                        the edge's sumtables
                                         (netlk_edge_sumtable); 0: one tangent
                                         sweep per call                        */
 } netlk_options;
@@ -382,14 +382,16 @@ int netlk_last_site_updates(const netlk_ctx *ctx, int64_t *site_updates);
  * lengths w.r.t. the linked length (sum of s_p x and s_p^2 x the shares),
  * mode 0 only: mode 1 returns NETLK_ERR_UNSUPPORTED there, as the
  * reference's formula throws for scaled lengths (LikelihoodDerivatives.cpp:42-46).
- * Both derivatives are analytic. DNA contexts evaluate the edge's sumtables
+ * Both derivatives are analytic. Contexts evaluate the edge's sumtables
  * (netlk_edge_sumtable below) at the current lengths: built on the first
  * call for the edge and kept while only that edge's lengths change, so a
  * Newton-Raphson loop that sets each proposal (netlk_edge_loglikelihood)
- * and asks for the derivatives pays for one build per edge. 20-state
- * contexts take one forward-mode (tangent) sweep over the variants above
- * the edge per call (the log-likelihood at the current lengths recomputed
- * incrementally on the way). Either way every displayed tree's first and
+ * and asks for the derivatives pays for one build per edge. Where the
+ * tables do not apply (the `sumtables` option 0, more than 4 rate
+ * categories with 20 states, tables too large) one forward-mode (tangent)
+ * sweep over the variants above the edge runs per call (the log-likelihood
+ * at the current lengths recomputed incrementally on the way). Either way
+ * every displayed tree's first and
  * second derivative is mixed like the reference's sumtable derivatives
  * (LikelihoodDerivatives.cpp:13-188). Contexts with several
  * checkpoint segments or device-resident lengths take d1 from full adjoint
@@ -402,10 +404,10 @@ int netlk_edge_derivatives(netlk_ctx *ctx, int32_t edge, int32_t mode,
  * w.r.t. its own length of the edge - the df[p] / ddf[p] the reference's
  * Newton-Raphson callback returns for unlinked lengths
  * (BranchLengthOptimization.cpp:189-195). On linked and scaled contexts the
- * same per-partition terms (w.r.t. the partition's effective length). DNA
- * contexts evaluate the edge's sumtables, each partition at its current
- * length; 20-state ones run the tangent sweep. Needs one checkpoint segment
- * and host lengths. */
+ * same per-partition terms (w.r.t. the partition's effective length), from
+ * the edge's sumtables with each partition at its current length where they
+ * apply, else the tangent sweep. Needs one checkpoint segment and host
+ * lengths. */
 int netlk_edge_derivatives_partition(netlk_ctx *ctx, int32_t edge, int32_t partition, int32_t mode, double *d1,
                                      double *d2);
 
@@ -426,10 +428,13 @@ int netlk_edge_derivatives_partition(netlk_ctx *ctx, int32_t edge, int32_t parti
  * netlk_edge_sumtable builds the tables at the current parameters (the
  * evaluation builds them itself when they are missing or stale; this entry
  * lets a caller pay for the build where it chooses). *built = 1 when the
- * sumtable path applies, 0 when it does not (20-state partitions, several
- * checkpoint segments, device-resident lengths, the context's `sumtables`
- * option 0, or tables that would take more than half the free device
- * memory); evaluations then take the tangent path. *n_tables (may be NULL): the tables built, one per displayed tree
+ * sumtable path applies, 0 when it does not (20 states with more than 4
+ * rate categories, several checkpoint segments, device-resident lengths,
+ * the context's `sumtables` option 0, or tables that would take more than
+ * half the free device memory); evaluations then take the tangent path.
+ * DNA tables come from one forward-mode sweep of the message's 4 unit
+ * directions; 20-state tables from one reverse walk per displayed tree
+ * down its path to the edge. *n_tables (may be NULL): the tables built, one per displayed tree
  * that contains the edge. */
 int netlk_edge_sumtable(netlk_ctx *ctx, int32_t edge, int32_t *built, int32_t *n_tables);
 /* logL and its first / second derivative with the edge at the given

@@ -289,7 +289,7 @@ struct StabParams {
 };
 
 // Builds the tables (one walk launch over the tangent schedule's ops in
-// depth-first order); false for an unsupported (R, S): DNA only.
+// depth-first order); false for an unsupported (R, S): DNA.
 // 20 states: the reverse path walks (grid.y = table); false for R > 4.
 bool launch_sumtable_path20(cudaStream_t s, int precision, int R, const StabParams &p, int n_tab);
 bool launch_sumtable_build(cudaStream_t s, int precision, int R, int S, const StabParams &p,
