@@ -115,10 +115,11 @@ def test_ten_reticulations():
 @pytest.mark.parametrize("states,rate_cats", [(4, 1), (4, 2), (4, 8), (20, 1), (20, 2)])
 def test_rate_category_counts(states, rate_cats):
     """Rate-category counts other than 4 (DNA 1/2/8, protein 1/2; the
-    CUDA-core sweeps) against the oracle, with a finite gradient; DNA also
-    the edge sumtables (their build walk and bulk-copy evaluation for this
-    rate count) at a proposed length against the oracle's logL and sumtable
-    derivatives there."""
+    CUDA-core sweeps) against the oracle, with a finite gradient, and the
+    edge sumtables (DNA: build walk and bulk-copy evaluation; 20 states:
+    reverse path walks and their evaluation, for this rate count) at a
+    proposed length against the oracle's logL and sumtable derivatives
+    there."""
     from netrax_gb300.likelihood import NetworkLikelihood
     from oracle import derivatives, improved, newick, pllmath
     rng = np.random.default_rng(10 + states + rate_cats)
@@ -133,14 +134,13 @@ def test_rate_category_counts(states, rate_cats):
     want = orc.loglikelihood()
     net = parse_extended_newick(text)
     stab_want = {}
-    if states == 4:
-        g_scale = max(1.0, float(np.abs(derivatives.EdgeDerivativeOracle(orc).gradient()[0]).max()))
-        for e in (0, 3):
-            t0 = orc.brlen[e]
-            orc.brlen[e] = 0.5 * t0 + 0.02
-            stab_want[e] = (orc.loglikelihood(),) + tuple(derivatives.EdgeDerivativeOracle(orc).edge(e))
-            orc.brlen[e] = t0
-            orc.loglikelihood()
+    g_scale = max(1.0, float(np.abs(derivatives.EdgeDerivativeOracle(orc).gradient()[0]).max()))
+    for e in (0, 3):
+        t0 = orc.brlen[e]
+        orc.brlen[e] = 0.5 * t0 + 0.02
+        stab_want[e] = (orc.loglikelihood(),) + tuple(derivatives.EdgeDerivativeOracle(orc).edge(e))
+        orc.brlen[e] = t0
+        orc.loglikelihood()
     for prec, tol in (("fp64", FP64_REL), ("fp32", FP32_REL)):
         with NetworkLikelihood(net, [part], precision=prec) as lik:
             got, gb, gr = lik.loglikelihood_gradient()
