@@ -1824,6 +1824,11 @@ bool netlk_ctx::sumtable_build(int e) {
       std::vector<int32_t> pops, pbeg;
       sumtable_paths(ops, n_tab, pops, pbeg);
       if ((int64_t)pops.size() / 6 > stab_cap_path) return false;
+      // one reverse walk per tree costs about a quarter of a tangent-sweep op
+      // per path op (measured on 40 taxa / 3 reticulations): past 16 path ops
+      // per tangent op the build would cost over four tangent sweeps, more
+      // than a Newton-Raphson search saves, so keep the tangent path
+      if (pops.size() / 6 > 16 * ops.size()) return false;
       int32_t *hpth = h_stab_paths.as<int32_t>();
       std::memcpy(hpth, pops.data(), pops.size() * 4);
       std::memcpy(hpth + pops.size(), pbeg.data(), pbeg.size() * 4);
