@@ -94,3 +94,19 @@ def test_golden_network_sumtable_schedules(case):
         root_vars = {int(v) for v in dt}
         work = [_check_edge(lik, e, node, ch, ed, root_vars)[1] for e in range(net.n_edges)]
     assert max(work) >= 1 or net.n_edges <= 2
+
+
+def test_host_only_contexts_report_no_device():
+    """On a host-only context the table build reports that it does not apply
+    and every derivative entry returns NETLK_ERR_NO_DEVICE (no device work)."""
+    from conftest import GoldenPartition
+    from netrax_gb300 import _native as N
+    case = {c["name"]: c for c in golden_cases()}["twoReticulations"]
+    net = parse_extended_newick(case["newick"])
+    with NetworkLikelihood(net, [GoldenPartition(d) for d in case["partitions"]], host_only=True) as lik:
+        assert lik.edge_sumtable(0) == (False, 0)
+        for call in (lambda: lik.edge_sumtable_derivatives(0, 0.1), lambda: lik.edge_derivatives(0),
+                     lambda: lik.edge_derivatives_partition(0, 0)):
+            with pytest.raises(N.NetlkError) as e:
+                call()
+            assert e.value.status == N.NETLK_ERR_NO_DEVICE
