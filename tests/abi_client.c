@@ -71,6 +71,15 @@ int main(void) {
   printf("n_variants=%d\nn_root_variants=%d\nn_levels=%d\nn_backward_ops=%d\nsite_clv_updates=%lld\n",
          st.n_variants, st.n_root_variants, st.n_levels, st.n_backward_ops, (long long)st.site_clv_updates);
 
+  /* the edge-sumtable schedule of edge 2 (host work only) and the table
+     build, which a host-only context declines */
+  int32_t n_ops = 0, n_work = 0, n_tables = 0, n_groups = 0, built = -1, n_built = -1;
+  CHECK(netlk_sumtable_export(ctx, 2, &n_ops, &n_work, &n_tables, &n_groups, NULL, NULL, NULL) == NETLK_OK,
+        "netlk_sumtable_export");
+  CHECK(netlk_edge_sumtable(ctx, 2, &built, &n_built) == NETLK_OK && built == 0 && n_built == 0,
+        "netlk_edge_sumtable declines on a host-only context");
+  printf("sumtable_ops=%d\nsumtable_tables=%d\nsumtable_groups=%d\n", n_ops, n_tables, n_groups);
+
   double total = 0.0;
   const int s = netlk_loglikelihood(ctx, &total, NULL, NULL);
   CHECK(s == NETLK_ERR_NO_DEVICE, "a host-only context refuses evaluation");

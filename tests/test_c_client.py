@@ -2,8 +2,8 @@
 
 ``tests/abi_client.c`` is what a reference-side binding looks like without
 Python: it fills the descriptors by hand in the reference's numbering, runs
-the alignment front end, builds a host-only context and exercises the error
-surface. It is compiled with ``-std=c99 -Wall -Wextra -Werror -pedantic``
+the alignment front end, builds a host-only context, reads an edge's
+sumtable schedule and exercises the error surface. It is compiled with ``-std=c99 -Wall -Wextra -Werror -pedantic``
 (the header is C, not only C++) and its DAG statistics must equal those of the
 same network and alignment built through the Python harness.
 """
@@ -46,8 +46,11 @@ def test_c_client_builds_and_matches_python(tmp_path):
                             "exch": [1.0, 2.5, 0.8, 1.2, 3.0, 1.0], "alpha": 0.8})
     with NetworkLikelihood(net, [part], host_only=True) as lik:
         st = lik.stats
+        ops, _, n_tab, gref, _ = lik.sumtable_export(2)
     assert int(got["n_site_patterns"]) == len(w)
     for k in ("n_variants", "n_root_variants", "n_levels", "n_backward_ops", "site_clv_updates"):
         assert int(got[k]) == st[k], k
+    assert (int(got["sumtable_ops"]), int(got["sumtable_tables"]), int(got["sumtable_groups"])) == \
+        (len(ops), n_tab, len(gref))
     assert got["evaluate_status"] == "no CUDA device"
     assert "branch length" in got["nan_length_error"]
